@@ -1,0 +1,181 @@
+/*
+ * kvsmc.h -- C ABI of the GB300 structured-grid marching-cubes library
+ * (libkvsmc.so, CUDA for sm_103a).
+ *
+ * This is the boundary under kvs::cuda::MarchingCubes, the drop-in for the
+ * reference mapper kvs::MarchingCubes
+ * (Source/Core/Visualization/Mapper/MarchingCubes.h:23-62).  Plain pointers
+ * and sizes only; every call returns a kvsmc_status and never aborts.
+ *
+ * Data model (the reference's, unchanged):
+ *   volume values: nx*ny*nz scalars, x fastest, then y, then z
+ *     (index = x + y*nx + z*nx*ny, MarchingCubes.cpp:162-164,187-194);
+ *   output, duplicated mode: coords float[9*T] (three vertices per triangle),
+ *     normals float[3*T] (one per triangle), no connections
+ *     (MarchingCubes.cpp:156-243);
+ *   output, shared-vertex modes: coords float[3*V], connections uint32[3*T],
+ *     normals float[3*T] (polygon) or float[3*V] (vertex)
+ *     (MarchingCubes.cpp:252-290).
+ * Triangles come out in the reference's cell order (z, y, x with x fastest)
+ * and in table order inside a cell, with the same vertex order and the same
+ * float bits.
+ */
+#ifndef KVSMC_H
+#define KVSMC_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define KVSMC_VERSION_MAJOR 1
+#define KVSMC_VERSION_MINOR 0
+
+typedef enum kvsmc_status {
+    KVSMC_OK = 0,
+    KVSMC_ERR_INVALID_ARGUMENT = 1,  /* null pointer, zero-sized volume, bad enum   */
+    KVSMC_ERR_UNSUPPORTED_DTYPE = 2, /* MarchingCubes.cpp:125-130                   */
+    KVSMC_ERR_OUT_OF_MEMORY = 3,     /* device or pinned allocation failed          */
+    KVSMC_ERR_CUDA = 4,              /* a CUDA runtime call failed (see last_error) */
+    KVSMC_ERR_NO_DEVICE = 5,         /* no usable CUDA device                       */
+    KVSMC_ERR_CAPACITY = 6,          /* caller buffer too small; sizes are returned */
+    KVSMC_ERR_TOO_LARGE = 7,         /* result does not fit the 32-bit vertex ids   */
+    KVSMC_ERR_TIMEOUT = 8,           /* a bounded device-side wait gave up          */
+    KVSMC_ERR_BUDGET = 9             /* serving: request larger than the budget     */
+} kvsmc_status;
+
+/* Scalar types, numbered as the reference's type switch (MarchingCubes.cpp:115-124). */
+typedef enum kvsmc_dtype {
+    KVSMC_I8 = 0, KVSMC_I16 = 1, KVSMC_I32 = 2, KVSMC_I64 = 3,
+    KVSMC_U8 = 4, KVSMC_U16 = 5, KVSMC_U32 = 6, KVSMC_U64 = 7,
+    KVSMC_F32 = 8, KVSMC_F64 = 9
+} kvsmc_dtype;
+
+/* Extraction modes: the reference's (duplication, normal type) combinations.
+ * VertexNormal forces shared vertices (MarchingCubes.cpp:69-73). */
+typedef enum kvsmc_mode {
+    KVSMC_DUP_POLYGON_NORMAL = 0,    /* duplication=true,  PolygonNormal */
+    KVSMC_SHARED_POLYGON_NORMAL = 1, /* duplication=false, PolygonNormal */
+    KVSMC_SHARED_VERTEX_NORMAL = 2   /* VertexNormal (either duplication) */
+} kvsmc_mode;
+
+typedef struct kvsmc_context kvsmc_context;
+typedef struct kvsmc_volume kvsmc_volume;
+
+/* Per-request parameters.  min/max and the coordinate transform are decided by
+ * the host layer exactly as MapperBase::setRange / setMinMaxCoords do
+ * (MapperBase.cpp:54-122); the library only applies them. */
+typedef struct kvsmc_params {
+    double isolevel;       /* MarchingCubes::m_isolevel                          */
+    int32_t mode;          /* kvsmc_mode                                         */
+    int32_t has_minmax;    /* 1: use min_value/max_value; 0: use the volume's
+                              device-computed min/max (GetMinMaxValues,
+                              StructuredVolumeObject.cpp:66-85)                 */
+    double min_value;      /* clamp range of interpolate_vertex (:347-348)       */
+    double max_value;
+    float min_coord[3];    /* volume->minObjectCoord()      (MarchingCubes.cpp:166) */
+    float scale[3];        /* (max_coord-min_coord)/ncells  (MarchingCubes.cpp:168) */
+} kvsmc_params;
+
+/* Sizes of one extraction (counts of elements, not bytes). */
+typedef struct kvsmc_sizes {
+    uint64_t ntriangles;
+    uint64_t nvertices;     /* 3*T in duplicated mode                             */
+    uint64_t ncoords;       /* floats                                             */
+    uint64_t nnormals;      /* floats                                             */
+    uint64_t nconnections;  /* uint32 (0 in duplicated mode)                      */
+    double min_value;       /* min/max actually used                              */
+    double max_value;
+    int32_t extracted;      /* 0: Math::Equal(min,max) early exit (MarchingCubes.cpp:108-110) */
+    int32_t reserved;
+} kvsmc_sizes;
+
+/* ------------------------------------------------------------------ context */
+
+/* One context per (host thread, device).  Owns a CUDA stream, the scratch
+ * arena and the device-resident volumes.  device < 0 picks the current one. */
+kvsmc_status kvsmc_create(int device, kvsmc_context** ctx);
+void kvsmc_destroy(kvsmc_context* ctx);
+const char* kvsmc_status_string(kvsmc_status st);
+/* Text of the last error on this context ("" if none). */
+const char* kvsmc_last_error(const kvsmc_context* ctx);
+/* The context's CUDA stream (a cudaStream_t), for event timing by callers. */
+void* kvsmc_stream(kvsmc_context* ctx);
+/* Run all later work of this context on a caller stream (NULL = own stream). */
+kvsmc_status kvsmc_set_stream(kvsmc_context* ctx, void* cuda_stream);
+kvsmc_status kvsmc_synchronize(kvsmc_context* ctx);
+/* Number of kernels this context has launched since creation. */
+uint64_t kvsmc_kernel_launches(const kvsmc_context* ctx);
+
+/* ------------------------------------------------------------------ volumes */
+
+/* Copy a host volume (x fastest) into a device-resident, row-padded buffer.
+ * Replaces the borrowed StructuredVolumeObject values of MapperBase::attachVolume
+ * (MapperBase.h:54) with a resident device copy. */
+kvsmc_status kvsmc_volume_upload(kvsmc_context* ctx, const void* host_values, kvsmc_dtype dtype,
+                                 uint32_t nx, uint32_t ny, uint32_t nz, kvsmc_volume** vol);
+/* Same, from a dense device buffer (x fastest, no padding). */
+kvsmc_status kvsmc_volume_from_device(kvsmc_context* ctx, const void* dev_values, kvsmc_dtype dtype,
+                                      uint32_t nx, uint32_t ny, uint32_t nz, kvsmc_volume** vol);
+/* Overwrite the values of an existing volume from host memory (same shape/type). */
+kvsmc_status kvsmc_volume_update(kvsmc_context* ctx, kvsmc_volume* vol, const void* host_values);
+void kvsmc_volume_free(kvsmc_context* ctx, kvsmc_volume* vol);
+/* Min/max of the values, computed on the device once and cached
+ * (StructuredVolumeObject::updateMinMaxValues, StructuredVolumeObject.cpp:431-450). */
+kvsmc_status kvsmc_volume_minmax(kvsmc_context* ctx, kvsmc_volume* vol, double* min_value, double* max_value);
+
+/* ------------------------------------------------------------- extraction */
+
+/* Count pass: exact output sizes for one request (no output written). */
+kvsmc_status kvsmc_count(kvsmc_context* ctx, kvsmc_volume* vol, const kvsmc_params* p, kvsmc_sizes* sizes);
+
+/* Count + emit into caller-provided DEVICE buffers.  Capacities are element
+ * counts; on KVSMC_ERR_CAPACITY nothing is written and *sizes holds the need.
+ * d_connections may be NULL in duplicated mode. */
+kvsmc_status kvsmc_extract_device(kvsmc_context* ctx, kvsmc_volume* vol, const kvsmc_params* p,
+                                  float* d_coords, uint64_t coords_capacity,
+                                  float* d_normals, uint64_t normals_capacity,
+                                  uint32_t* d_connections, uint64_t connections_capacity,
+                                  kvsmc_sizes* sizes);
+
+/* Host-side allocator for the output arrays: which = 0 coords (float),
+ * 1 normals (float), 2 connections (uint32); count = elements (> 0).
+ * Return NULL to fail the call with KVSMC_ERR_OUT_OF_MEMORY. */
+typedef void* (*kvsmc_host_alloc_fn)(void* user, int32_t which, uint64_t count);
+
+/* The whole mapper call on host buffers: upload the volume, min/max when not
+ * given, count, allocate the outputs through `alloc`, emit, copy back.  This is
+ * what kvs::cuda::MarchingCubes::exec calls
+ * (replaces MarchingCubes::mapping + extract_surfaces<T>, MarchingCubes.cpp:87-147). */
+kvsmc_status kvsmc_marching_cubes_host(kvsmc_context* ctx, const void* host_values, kvsmc_dtype dtype,
+                                       uint32_t nx, uint32_t ny, uint32_t nz, const kvsmc_params* p,
+                                       kvsmc_host_alloc_fn alloc, void* alloc_user, kvsmc_sizes* sizes);
+
+/* --------------------------------------------------------------- batching */
+
+/* One (volume, isolevel) request of a batch.  Outputs are device pointers with
+ * capacities as in kvsmc_extract_device. */
+typedef struct kvsmc_request {
+    kvsmc_volume* volume;
+    kvsmc_params params;
+    float* d_coords;       uint64_t coords_capacity;
+    float* d_normals;      uint64_t normals_capacity;
+    uint32_t* d_connections; uint64_t connections_capacity;
+    kvsmc_sizes sizes;     /* out */
+    kvsmc_status status;   /* out */
+} kvsmc_request;
+
+/* Count every request of a batch in one fused launch (all volumes and
+ * isolevels); fills reqs[i].sizes. */
+kvsmc_status kvsmc_count_batch(kvsmc_context* ctx, kvsmc_request* reqs, int32_t n);
+/* Count + emit a whole batch: fused launches over all requests, so each
+ * volume is read once per pass however many isolevels share it. */
+kvsmc_status kvsmc_extract_batch(kvsmc_context* ctx, kvsmc_request* reqs, int32_t n);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* KVSMC_H */

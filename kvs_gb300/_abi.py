@@ -1,0 +1,249 @@
+"""ctypes binding to libkvsmc.so (include/kvsmc.h).
+
+The library is built in-tree by kvs_gb300/build.py.  There is no fallback:
+if the shared library is missing, importing this module raises.
+"""
+import ctypes as C
+import os
+
+import numpy as np
+
+PKG = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(PKG, "lib", "libkvsmc.so")
+
+# status codes (kvsmc_status)
+OK = 0
+ERR_INVALID_ARGUMENT = 1
+ERR_UNSUPPORTED_DTYPE = 2
+ERR_OUT_OF_MEMORY = 3
+ERR_CUDA = 4
+ERR_NO_DEVICE = 5
+ERR_CAPACITY = 6
+ERR_TOO_LARGE = 7
+ERR_TIMEOUT = 8
+ERR_BUDGET = 9
+
+# dtype codes (kvsmc_dtype): the reference's type-switch order
+DTYPES = [np.int8, np.int16, np.int32, np.int64, np.uint8, np.uint16,
+          np.uint32, np.uint64, np.float32, np.float64]
+
+MODE_DUP_POLYGON_NORMAL = 0
+MODE_SHARED_POLYGON_NORMAL = 1
+MODE_SHARED_VERTEX_NORMAL = 2
+
+# Every exported symbol of include/kvsmc.h.
+EXPORTS = [
+    "kvsmc_create", "kvsmc_destroy", "kvsmc_status_string", "kvsmc_last_error",
+    "kvsmc_stream", "kvsmc_set_stream", "kvsmc_synchronize", "kvsmc_kernel_launches",
+    "kvsmc_volume_upload", "kvsmc_volume_from_device", "kvsmc_volume_update",
+    "kvsmc_volume_free", "kvsmc_volume_minmax",
+    "kvsmc_count", "kvsmc_extract_device", "kvsmc_marching_cubes_host",
+    "kvsmc_count_batch", "kvsmc_extract_batch",
+]
+
+
+def dtype_code(dt):
+    dt = np.dtype(dt)
+    for i, d in enumerate(DTYPES):
+        if np.dtype(d) == dt:
+            return i
+    raise TypeError(f"Unsupported data type '{dt}'.")
+
+
+class Params(C.Structure):
+    _fields_ = [("isolevel", C.c_double), ("mode", C.c_int32), ("has_minmax", C.c_int32),
+                ("min_value", C.c_double), ("max_value", C.c_double),
+                ("min_coord", C.c_float * 3), ("scale", C.c_float * 3)]
+
+
+class Sizes(C.Structure):
+    _fields_ = [("ntriangles", C.c_uint64), ("nvertices", C.c_uint64), ("ncoords", C.c_uint64),
+                ("nnormals", C.c_uint64), ("nconnections", C.c_uint64),
+                ("min_value", C.c_double), ("max_value", C.c_double),
+                ("extracted", C.c_int32), ("reserved", C.c_int32)]
+
+
+class Request(C.Structure):
+    _fields_ = [("volume", C.c_void_p), ("params", Params),
+                ("d_coords", C.c_void_p), ("coords_capacity", C.c_uint64),
+                ("d_normals", C.c_void_p), ("normals_capacity", C.c_uint64),
+                ("d_connections", C.c_void_p), ("connections_capacity", C.c_uint64),
+                ("sizes", Sizes), ("status", C.c_int)]
+
+
+HOST_ALLOC = C.CFUNCTYPE(C.c_void_p, C.c_void_p, C.c_int32, C.c_uint64)
+
+
+class KvsmcError(RuntimeError):
+    def __init__(self, status, message):
+        super().__init__(message)
+        self.status = status
+
+
+_lib = None
+
+
+def load(path=LIB_PATH):
+    """Load libkvsmc.so (raises if it has not been built)."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.exists(path):
+        raise ImportError(f"libkvsmc.so is not built ({path}); run kvs_gb300.build.build()")
+    lib = C.CDLL(path)
+    vp, u32, u64, i32 = C.c_void_p, C.c_uint32, C.c_uint64, C.c_int32
+    sig = {
+        "kvsmc_create": (C.c_int, [C.c_int, C.POINTER(vp)]),
+        "kvsmc_destroy": (None, [vp]),
+        "kvsmc_status_string": (C.c_char_p, [C.c_int]),
+        "kvsmc_last_error": (C.c_char_p, [vp]),
+        "kvsmc_stream": (vp, [vp]),
+        "kvsmc_set_stream": (C.c_int, [vp, vp]),
+        "kvsmc_synchronize": (C.c_int, [vp]),
+        "kvsmc_kernel_launches": (u64, [vp]),
+        "kvsmc_volume_upload": (C.c_int, [vp, vp, C.c_int, u32, u32, u32, C.POINTER(vp)]),
+        "kvsmc_volume_from_device": (C.c_int, [vp, vp, C.c_int, u32, u32, u32, C.POINTER(vp)]),
+        "kvsmc_volume_update": (C.c_int, [vp, vp, vp]),
+        "kvsmc_volume_free": (None, [vp, vp]),
+        "kvsmc_volume_minmax": (C.c_int, [vp, vp, C.POINTER(C.c_double), C.POINTER(C.c_double)]),
+        "kvsmc_count": (C.c_int, [vp, vp, C.POINTER(Params), C.POINTER(Sizes)]),
+        "kvsmc_extract_device": (C.c_int, [vp, vp, C.POINTER(Params), vp, u64, vp, u64, vp, u64,
+                                           C.POINTER(Sizes)]),
+        "kvsmc_marching_cubes_host": (C.c_int, [vp, vp, C.c_int, u32, u32, u32, C.POINTER(Params),
+                                                HOST_ALLOC, vp, C.POINTER(Sizes)]),
+        "kvsmc_count_batch": (C.c_int, [vp, C.POINTER(Request), i32]),
+        "kvsmc_extract_batch": (C.c_int, [vp, C.POINTER(Request), i32]),
+    }
+    for name, (res, args) in sig.items():
+        f = getattr(lib, name)
+        f.restype = res
+        f.argtypes = args
+    _lib = lib
+    return lib
+
+
+def status_string(st):
+    return load().kvsmc_status_string(st).decode()
+
+
+class Context:
+    """One libkvsmc context (CUDA stream + scratch arena) on one device."""
+
+    def __init__(self, device=-1):
+        self.lib = load()
+        h = C.c_void_p()
+        st = self.lib.kvsmc_create(device, C.byref(h))
+        if st != OK:
+            raise KvsmcError(st, f"kvsmc_create: {status_string(st)}")
+        self.handle = h
+
+    def check(self, st, what):
+        if st != OK:
+            msg = self.lib.kvsmc_last_error(self.handle).decode()
+            raise KvsmcError(st, f"{what}: {status_string(st)}: {msg}")
+
+    @property
+    def stream(self):
+        return self.lib.kvsmc_stream(self.handle)
+
+    def set_stream(self, cuda_stream_ptr):
+        self.check(self.lib.kvsmc_set_stream(self.handle, cuda_stream_ptr), "kvsmc_set_stream")
+
+    def synchronize(self):
+        self.check(self.lib.kvsmc_synchronize(self.handle), "kvsmc_synchronize")
+
+    @property
+    def kernel_launches(self):
+        return int(self.lib.kvsmc_kernel_launches(self.handle))
+
+    def close(self):
+        if getattr(self, "handle", None):
+            self.lib.kvsmc_destroy(self.handle)
+            self.handle = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+class DeviceVolume:
+    """A volume resident on the device (kvsmc_volume)."""
+
+    def __init__(self, ctx, handle, dtype, shape):
+        self.ctx, self.handle, self.dtype, self.shape = ctx, handle, np.dtype(dtype), shape
+
+    @classmethod
+    def upload(cls, ctx, values):
+        v = np.ascontiguousarray(values)
+        nz, ny, nx = v.shape
+        h = C.c_void_p()
+        ctx.check(ctx.lib.kvsmc_volume_upload(ctx.handle, v.ctypes.data, dtype_code(v.dtype), nx, ny, nz,
+                                              C.byref(h)), "kvsmc_volume_upload")
+        return cls(ctx, h, v.dtype, v.shape)
+
+    @classmethod
+    def from_device(cls, ctx, ptr, dtype, shape):
+        nz, ny, nx = shape
+        h = C.c_void_p()
+        ctx.check(ctx.lib.kvsmc_volume_from_device(ctx.handle, C.c_void_p(ptr), dtype_code(dtype), nx, ny, nz,
+                                                   C.byref(h)), "kvsmc_volume_from_device")
+        return cls(ctx, h, dtype, tuple(shape))
+
+    def minmax(self):
+        mn, mx = C.c_double(), C.c_double()
+        self.ctx.check(self.ctx.lib.kvsmc_volume_minmax(self.ctx.handle, self.handle, C.byref(mn), C.byref(mx)),
+                       "kvsmc_volume_minmax")
+        return mn.value, mx.value
+
+    def free(self):
+        if self.handle:
+            self.ctx.lib.kvsmc_volume_free(self.ctx.handle, self.handle)
+            self.handle = None
+
+    def __del__(self):
+        try:
+            if self.ctx.handle:
+                self.free()
+        except Exception:
+            pass
+
+
+def make_params(isolevel, mode, minmax=None, min_coord=(0.0, 0.0, 0.0), scale=(1.0, 1.0, 1.0)):
+    p = Params()
+    p.isolevel = float(isolevel)
+    p.mode = int(mode)
+    p.has_minmax = 1 if minmax is not None else 0
+    if minmax is not None:
+        p.min_value, p.max_value = float(minmax[0]), float(minmax[1])
+    for k in range(3):
+        p.min_coord[k] = float(min_coord[k])
+        p.scale[k] = float(scale[k])
+    return p
+
+
+def sizes_dict(s):
+    return dict(ntriangles=s.ntriangles, nvertices=s.nvertices, ncoords=s.ncoords, nnormals=s.nnormals,
+                nconnections=s.nconnections, min_value=s.min_value, max_value=s.max_value,
+                extracted=bool(s.extracted))
+
+
+def marching_cubes_host(ctx, values, params):
+    """kvsmc_marching_cubes_host on a numpy volume; returns (coords, normals, connections, sizes)."""
+    v = np.ascontiguousarray(values)
+    nz, ny, nx = v.shape
+    bufs = {}
+
+    def alloc(user, which, count):
+        a = np.empty(count, dtype=np.uint32 if which == 2 else np.float32)
+        bufs[which] = a
+        return a.ctypes.data
+
+    cb = HOST_ALLOC(alloc)
+    s = Sizes()
+    ctx.check(ctx.lib.kvsmc_marching_cubes_host(ctx.handle, v.ctypes.data, dtype_code(v.dtype), nx, ny, nz,
+                                                C.byref(params), cb, None, C.byref(s)),
+              "kvsmc_marching_cubes_host")
+    empty_f = np.zeros(0, np.float32)
+    return (bufs.get(0, empty_f), bufs.get(1, empty_f), bufs.get(2, np.zeros(0, np.uint32)), sizes_dict(s))

@@ -1,0 +1,154 @@
+"""ctypes binding to the reference kvs::MarchingCubes built by oracle/Makefile.ref.
+
+Test infrastructure only (parity anchor).  The library exists only where the
+reference sources were available to compile it; `available()` says whether it
+was built.  Runs Source/Core/Visualization/Mapper/MarchingCubes.cpp:25-37
+(constructor -> exec -> mapping) on a StructuredVolumeObject made from a
+numpy array and returns the PolygonObject's arrays.
+"""
+import ctypes as C
+import os
+import subprocess
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "_ref", "libkvsref_mc.so")
+REFERENCE_SOURCE = "/root/reference/Source"
+
+# dtype codes: order of the reference's type switch (MarchingCubes.cpp:115-124)
+DTYPES = [np.int8, np.int16, np.int32, np.int64, np.uint8, np.uint16,
+          np.uint32, np.uint64, np.float32, np.float64]
+
+
+def dtype_code(dt):
+    dt = np.dtype(dt)
+    for i, d in enumerate(DTYPES):
+        if np.dtype(d) == dt:
+            return i
+    raise ValueError(f"unsupported dtype {dt}")
+
+
+class _Result(C.Structure):
+    _fields_ = [
+        ("success", C.c_int),
+        ("ncoords", C.c_ulonglong), ("nnormals", C.c_ulonglong),
+        ("nconnections", C.c_ulonglong), ("ncolors", C.c_ulonglong),
+        ("nopacities", C.c_ulonglong),
+        ("coords", C.POINTER(C.c_float)), ("normals", C.POINTER(C.c_float)),
+        ("connections", C.POINTER(C.c_uint)), ("colors", C.POINTER(C.c_ubyte)),
+        ("opacities", C.POINTER(C.c_ubyte)),
+        ("polygon_type", C.c_int), ("normal_type", C.c_int), ("color_type", C.c_int),
+        ("vol_has_minmax", C.c_int), ("vol_min", C.c_double), ("vol_max", C.c_double),
+        ("min_obj", C.c_float * 3), ("max_obj", C.c_float * 3),
+        ("min_ext", C.c_float * 3), ("max_ext", C.c_float * 3),
+        ("seconds", C.c_double),
+    ]
+
+
+_lib = None
+
+
+def build(jobs=8, quiet=True):
+    """Compile the reference path from its sources (only where they exist)."""
+    if not os.path.isdir(REFERENCE_SOURCE):
+        return False
+    cmd = ["make", "-f", os.path.join(HERE, "Makefile.ref"), f"KVS_SRC={REFERENCE_SOURCE}",
+           f"-j{jobs}"]
+    out = subprocess.run(cmd, cwd=os.path.dirname(HERE), capture_output=quiet, text=True)
+    if out.returncode != 0:
+        raise RuntimeError("reference build failed:\n" + (out.stderr or "")[-4000:])
+    return True
+
+
+def available():
+    return os.path.exists(LIB_PATH)
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        _lib = C.CDLL(LIB_PATH)
+        _lib.kvsref_marching_cubes.restype = C.c_int
+        _lib.kvsref_marching_cubes.argtypes = [
+            C.c_int, C.c_void_p, C.c_uint, C.c_uint, C.c_uint,
+            C.c_double, C.c_int, C.c_int,
+            C.c_int, C.c_double, C.c_double,
+            C.c_int, C.c_void_p,
+            C.c_int, C.c_void_p, C.c_void_p,
+            C.c_int, C.c_int, C.c_float, C.c_float,
+            C.c_int, C.POINTER(_Result)]
+        _lib.kvsref_free.argtypes = [C.POINTER(_Result)]
+        _lib.kvsref_hydrogen.argtypes = [C.c_uint, C.c_void_p]
+        _lib.kvsref_default_colormap.argtypes = [C.c_int, C.c_void_p]
+        _lib.kvsref_color_at.argtypes = [C.c_int, C.c_float, C.c_float, C.c_float, C.c_void_p]
+    return _lib
+
+
+def _arr(ptr, n, dt):
+    if n == 0:
+        return np.zeros(0, dtype=dt)
+    return np.ctypeslib.as_array(ptr, shape=(n,)).copy()
+
+
+def marching_cubes(values, isolevel, normal_type="polygon", duplication=True,
+                   minmax=None, rect_coords=None, obj_coords=None,
+                   tf_resolution=256, tf_range=None, repeat=1):
+    """values: numpy array shaped (nz, ny, nx) (x fastest, like KVS)."""
+    v = np.ascontiguousarray(values)
+    nz, ny, nx = v.shape
+    r = _Result()
+    rc = np.ascontiguousarray(rect_coords, dtype=np.float32) if rect_coords is not None else None
+    mn = mx = None
+    if obj_coords is not None:
+        mn = np.ascontiguousarray(obj_coords[0], dtype=np.float32)
+        mx = np.ascontiguousarray(obj_coords[1], dtype=np.float32)
+    st = lib().kvsref_marching_cubes(
+        dtype_code(v.dtype), v.ctypes.data, nx, ny, nz, float(isolevel),
+        0 if normal_type == "polygon" else 1, 1 if duplication else 0,
+        1 if minmax is not None else 0,
+        float(minmax[0]) if minmax is not None else 0.0,
+        float(minmax[1]) if minmax is not None else 0.0,
+        1 if rc is not None else 0, rc.ctypes.data if rc is not None else None,
+        1 if obj_coords is not None else 0,
+        mn.ctypes.data if mn is not None else None,
+        mx.ctypes.data if mx is not None else None,
+        tf_resolution, 1 if tf_range is not None else 0,
+        float(tf_range[0]) if tf_range is not None else 0.0,
+        float(tf_range[1]) if tf_range is not None else 0.0,
+        repeat, C.byref(r))
+    if st != 0:
+        raise RuntimeError("kvsref_marching_cubes failed")
+    out = dict(
+        success=bool(r.success),
+        coords=_arr(r.coords, r.ncoords, np.float32),
+        normals=_arr(r.normals, r.nnormals, np.float32),
+        connections=_arr(r.connections, r.nconnections, np.uint32),
+        colors=_arr(r.colors, r.ncolors, np.uint8),
+        opacities=_arr(r.opacities, r.nopacities, np.uint8),
+        polygon_type=r.polygon_type, normal_type=r.normal_type, color_type=r.color_type,
+        vol_has_minmax=bool(r.vol_has_minmax), vol_min=r.vol_min, vol_max=r.vol_max,
+        min_obj=np.array(r.min_obj[:], np.float32), max_obj=np.array(r.max_obj[:], np.float32),
+        min_ext=np.array(r.min_ext[:], np.float32), max_ext=np.array(r.max_ext[:], np.float32),
+        seconds=r.seconds)
+    lib().kvsref_free(C.byref(r))
+    return out
+
+
+def hydrogen(res):
+    out = np.zeros((res, res, res), np.uint8)
+    if lib().kvsref_hydrogen(res, out.ctypes.data) != 0:
+        raise RuntimeError("hydrogen failed")
+    return out
+
+
+def default_colormap(resolution=256):
+    t = np.zeros(resolution * 3, np.uint8)
+    n = lib().kvsref_default_colormap(resolution, t.ctypes.data)
+    return t[:n].reshape(-1, 3)
+
+
+def color_at(resolution, tf_min, tf_max, value):
+    rgb = np.zeros(3, np.uint8)
+    lib().kvsref_color_at(resolution, tf_min, tf_max, value, rgb.ctypes.data)
+    return rgb

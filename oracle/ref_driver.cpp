@@ -1,0 +1,218 @@
+/*
+ * extern "C" driver around the reference kvs::MarchingCubes, linked with the
+ * reference's own sources by oracle/Makefile.ref into oracle/_ref/.
+ *
+ * Test infrastructure only.  It builds a kvs::StructuredVolumeObject from a
+ * raw buffer, runs the reference mapper through its public constructor
+ * (Source/Core/Visualization/Mapper/MarchingCubes.cpp:25-37), and copies the
+ * resulting kvs::PolygonObject arrays out so Python (ctypes) can compare them
+ * with the C restatement and write golden fixtures.
+ */
+#include <kvs/StructuredVolumeObject>
+#include <kvs/PolygonObject>
+#include <kvs/MarchingCubes>
+#include <kvs/TransferFunction>
+#include <kvs/HydrogenVolumeData>
+#include <kvs/ValueArray>
+#include <kvs/AnyValueArray>
+#include <chrono>
+#include <cstdlib>
+#include <cstring>
+
+extern "C" {
+
+struct kvsref_result
+{
+    int success;
+    unsigned long long ncoords;      // number of floats in coords
+    unsigned long long nnormals;     // number of floats in normals
+    unsigned long long nconnections; // number of uint32 in connections
+    unsigned long long ncolors;      // number of bytes in colors
+    unsigned long long nopacities;   // number of bytes in opacities
+    float* coords;
+    float* normals;
+    unsigned int* connections;
+    unsigned char* colors;
+    unsigned char* opacities;
+    int polygon_type;
+    int normal_type;
+    int color_type;
+    int vol_has_minmax;
+    double vol_min;
+    double vol_max;
+    float min_obj[3], max_obj[3], min_ext[3], max_ext[3];
+    double seconds;
+};
+
+} // extern "C"
+
+namespace
+{
+
+template <typename T>
+kvs::AnyValueArray MakeValues( const void* p, size_t n )
+{
+    return kvs::AnyValueArray( kvs::ValueArray<T>( static_cast<const T*>( p ), n ) );
+}
+
+// dtype codes follow the order of the reference's type switch
+// (MarchingCubes.cpp:115-124): i8 i16 i32 i64 u8 u16 u32 u64 f32 f64.
+kvs::AnyValueArray Values( int dtype, const void* p, size_t n )
+{
+    switch ( dtype )
+    {
+    case 0: return MakeValues<kvs::Int8>( p, n );
+    case 1: return MakeValues<kvs::Int16>( p, n );
+    case 2: return MakeValues<kvs::Int32>( p, n );
+    case 3: return MakeValues<kvs::Int64>( p, n );
+    case 4: return MakeValues<kvs::UInt8>( p, n );
+    case 5: return MakeValues<kvs::UInt16>( p, n );
+    case 6: return MakeValues<kvs::UInt32>( p, n );
+    case 7: return MakeValues<kvs::UInt64>( p, n );
+    case 8: return MakeValues<kvs::Real32>( p, n );
+    case 9: return MakeValues<kvs::Real64>( p, n );
+    default: return kvs::AnyValueArray();
+    }
+}
+
+template <typename T>
+T* CopyOut( const kvs::ValueArray<T>& a, unsigned long long* n )
+{
+    *n = a.size();
+    if ( a.size() == 0 ) return nullptr;
+    T* p = static_cast<T*>( std::malloc( a.size() * sizeof( T ) ) );
+    std::memcpy( p, a.data(), a.size() * sizeof( T ) );
+    return p;
+}
+
+void Copy3( float* dst, const kvs::Vec3& v ) { dst[0] = v.x(); dst[1] = v.y(); dst[2] = v.z(); }
+
+} // namespace
+
+extern "C" {
+
+/*
+ * grid_type: 0 uniform, 1 rectilinear (rect_coords = nx+ny+nz floats).
+ * has_obj_coords: preset the volume's min/max object coords.
+ * has_minmax: preset the volume's min/max values (skips the reference scan).
+ * tf_has_range: give the transfer function a range before the call.
+ * repeat: run the constructor this many times on fresh volume objects and
+ *         report the fastest (for the CPU baseline); outputs are the last run's.
+ */
+int kvsref_marching_cubes(
+    int dtype, const void* values, unsigned nx, unsigned ny, unsigned nz,
+    double isolevel, int normal_type, int duplication,
+    int has_minmax, double vmin, double vmax,
+    int grid_type, const float* rect_coords,
+    int has_obj_coords, const float* min_obj, const float* max_obj,
+    int tf_resolution, int tf_has_range, float tf_min, float tf_max,
+    int repeat, kvsref_result* out )
+{
+    std::memset( out, 0, sizeof( *out ) );
+    const size_t n = size_t( nx ) * ny * nz;
+    kvs::AnyValueArray vals = Values( dtype, values, n );
+    if ( vals.size() != n ) return -1;
+
+    kvs::TransferFunction tfunc( tf_resolution > 0 ? tf_resolution : 256 );
+    if ( tf_has_range ) tfunc.setRange( tf_min, tf_max );
+
+    const auto ntype = normal_type == 0 ? kvs::PolygonObject::PolygonNormal : kvs::PolygonObject::VertexNormal;
+    if ( repeat < 1 ) repeat = 1;
+    double best = 1e300;
+    kvs::MarchingCubes* mc = nullptr;
+    kvs::StructuredVolumeObject* vol = nullptr;
+    for ( int r = 0; r < repeat; ++r )
+    {
+        delete mc; mc = nullptr;
+        delete vol;
+        vol = new kvs::StructuredVolumeObject();
+        vol->setVeclen( 1 );
+        vol->setResolution( kvs::Vec3ui( nx, ny, nz ) );
+        vol->setValues( vals );
+        if ( grid_type == 1 )
+        {
+            vol->setGridTypeToRectilinear();
+            vol->setCoords( kvs::ValueArray<kvs::Real32>( rect_coords, size_t( nx ) + ny + nz ) );
+        }
+        else
+        {
+            vol->setGridTypeToUniform();
+        }
+        if ( has_obj_coords )
+        {
+            vol->setMinMaxObjectCoords( kvs::Vec3( min_obj[0], min_obj[1], min_obj[2] ),
+                                        kvs::Vec3( max_obj[0], max_obj[1], max_obj[2] ) );
+        }
+        if ( has_minmax ) vol->setMinMaxValues( vmin, vmax );
+
+        const auto t0 = std::chrono::steady_clock::now();
+        mc = new kvs::MarchingCubes( vol, isolevel, ntype, duplication != 0, tfunc );
+        const auto t1 = std::chrono::steady_clock::now();
+        const double s = std::chrono::duration<double>( t1 - t0 ).count();
+        if ( s < best ) best = s;
+    }
+
+    out->success = mc->isSuccess() ? 1 : 0;
+    out->coords = CopyOut( mc->coords(), &out->ncoords );
+    out->normals = CopyOut( mc->normals(), &out->nnormals );
+    out->connections = CopyOut( mc->connections(), &out->nconnections );
+    out->colors = CopyOut( mc->colors(), &out->ncolors );
+    out->opacities = CopyOut( mc->opacities(), &out->nopacities );
+    out->polygon_type = int( mc->polygonType() );
+    out->normal_type = int( mc->normalType() );
+    out->color_type = int( mc->colorType() );
+    out->vol_has_minmax = vol->hasMinMaxValues() ? 1 : 0;
+    out->vol_min = vol->minValue();
+    out->vol_max = vol->maxValue();
+    Copy3( out->min_obj, mc->minObjectCoord() );
+    Copy3( out->max_obj, mc->maxObjectCoord() );
+    Copy3( out->min_ext, mc->minExternalCoord() );
+    Copy3( out->max_ext, mc->maxExternalCoord() );
+    out->seconds = best;
+    delete mc;
+    delete vol;
+    return 0;
+}
+
+void kvsref_free( kvsref_result* r )
+{
+    std::free( r->coords );
+    std::free( r->normals );
+    std::free( r->connections );
+    std::free( r->colors );
+    std::free( r->opacities );
+    std::memset( r, 0, sizeof( *r ) );
+}
+
+/* HydrogenVolumeData (Source/Core/Visualization/Data/HydrogenVolumeData.cpp):
+ * the reference's own deterministic uint8 field, res^3 nodes. */
+int kvsref_hydrogen( unsigned res, unsigned char* out )
+{
+    kvs::HydrogenVolumeData h( kvs::Vec3ui( res, res, res ) );
+    h.exec();
+    const auto& v = h.values();
+    if ( v.size() != size_t( res ) * res * res ) return -1;
+    std::memcpy( out, v.data(), v.size() );
+    return 0;
+}
+
+/* The transfer function's colour table (resolution x RGB) and ColorMap::at
+ * for the default map, so the host-side colour can be pinned too. */
+int kvsref_default_colormap( int resolution, unsigned char* table )
+{
+    kvs::TransferFunction tf( resolution );
+    const auto& t = tf.colorMap().table();
+    std::memcpy( table, t.data(), t.size() );
+    return int( t.size() );
+}
+
+int kvsref_color_at( int resolution, float tf_min, float tf_max, float value, unsigned char* rgb )
+{
+    kvs::TransferFunction tf( resolution );
+    tf.setRange( tf_min, tf_max );
+    const kvs::RGBColor c = tf.colorMap().at( value );
+    rgb[0] = c.r(); rgb[1] = c.g(); rgb[2] = c.b();
+    return 0;
+}
+
+} // extern "C"
