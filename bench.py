@@ -1,0 +1,395 @@
+"""Benchmark: multi-isovalue marching-cubes sweep on one GB300.
+
+Default workload (the headline configuration): a 1024^3 float32 field of
+seeded 5-octave fBm gradient noise (base frequency 1/128, gain 0.5, rescaled
+to [0, 1]), 16 isovalues 0.2 + 0.04 k, duplicated vertices + polygon normals.
+A step is one kvsmc_extract_batch call over the 16 requests on the resident
+volume: the fused count launch, the scan, the fused emit launch, with output
+written to HBM.  `value` = cells x isovalues / s (Mcells/s).
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+                    [--workload sweep1024|blobs128]
+
+--impl reference times the reference's CPU algorithm on this host's cores: the
+C restatement under oracle/ (the reference sources are not present on the GPU
+host), on a bounded slab sample of the same workload, all cores.
+N > 1 (torchrun): independent replicas, one per GPU ("scaling": "weak").
+"""
+import argparse
+import concurrent.futures as cf
+import json
+import os
+import statistics
+import subprocess
+import sys
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+WORKLOADS = {
+    "sweep1024": dict(shape=(1024, 1024, 1024), kind="fbm", isos=[0.2 + 0.04 * k for k in range(16)],
+                      desc="1024^3 float32 fBm gradient noise (5 octaves, base freq 1/128, gain 0.5, in [0,1]), "
+                           "16 isovalues 0.2..0.8 in one batched call, duplication=true, PolygonNormal"),
+    "blobs128": dict(shape=(128, 128, 128), kind="blobs", isos=[0.5],
+                     desc="128^3 float32, 4 Gaussian blobs (sigma 8..24) + U[-0.01,0.01] noise, iso 0.5, "
+                          "duplication=true, PolygonNormal"),
+}
+
+
+def dist_env():
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return rank, world, local
+
+
+def barrier_max(value, world):
+    """Max over ranks of a float (identity for one rank)."""
+    if world == 1:
+        return value
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([value], dtype=torch.float64, device="cuda")
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def make_field(w, device, seed=42):
+    from kvs_gb300 import synthetic as S
+    if w["kind"] == "fbm":
+        return S.fbm(w["shape"], seed=seed, device=device)
+    return S.gaussian_blobs(w["shape"], seed=seed, device=device)
+
+
+class Clocks:
+    """nvidia-smi sampling during the timed region."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu):
+        self.gpu = gpu
+        self.proc = None
+        self.path = os.path.join(ROOT, "gpurun_out" if os.path.isdir(os.path.join(ROOT, "gpurun_out")) else ".",
+                                 f".clocks_{os.getpid()}.csv")
+
+    def start(self):
+        try:
+            self.f = open(self.path, "w")
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.gpu), f"--query-gpu={self.FIELDS}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=self.f, stderr=subprocess.DEVNULL)
+        except Exception:
+            self.proc = None
+
+    def stop(self):
+        if self.proc is None:
+            return None
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        self.f.close()
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        try:
+            for line in open(self.path):
+                p = [x.strip() for x in line.split(",")]
+                if len(p) < 9:
+                    continue
+                try:
+                    sm.append(float(p[1]))
+                    mx.append(float(p[2]))
+                except ValueError:
+                    continue
+                for n, val in zip(names, p[5:9]):
+                    if val.lower().startswith("active"):
+                        reasons.add(n)
+            os.remove(self.path)
+        except Exception:
+            pass
+        if not sm:
+            return None
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(mx), "samples": len(sm),
+                "reasons": sorted(reasons)}
+
+
+def peaks():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        d = json.load(open(p))
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+def traffic_per_launch(workload):
+    """DRAM bytes of one emit launch from the committed ncu summary, if any."""
+    p = os.path.join(ROOT, "profiles", f"stream_emit_{workload}.json")
+    if os.path.exists(p):
+        d = json.load(open(p))
+        return d.get("dram_bytes_per_launch")
+    return None
+
+
+# ----------------------------------------------------------------- our arm
+
+def run_ours(args, rank, world, local):
+    import ctypes as C
+
+    import torch
+
+    from kvs_gb300 import _abi
+
+    torch.cuda.set_device(local)
+    w = WORKLOADS[args.workload]
+    nz, ny, nx = w["shape"]
+    ctx = _abi.Context(local)
+    stream = torch.cuda.Stream()
+    ctx.set_stream(stream.cuda_stream)
+    field = make_field(w, "cuda")
+    torch.cuda.synchronize()
+    vol = _abi.DeviceVolume.from_device(ctx, field.data_ptr(), np.float32, field.shape)
+    host_field = None
+    if not args.no_e2e:
+        host_field = torch.empty(field.shape, dtype=torch.float32, pin_memory=True)
+        host_field.copy_(field)
+    # the CPU baseline's sample: the first z-slab of this same field
+    args.cpu_slab = field[:min(nz, 65)].cpu().numpy() if rank == 0 else None
+    del field
+    torch.cuda.empty_cache()
+    isos = w["isos"]
+    n = len(isos)
+    reqs = (_abi.Request * n)()
+    for i, iso in enumerate(isos):
+        reqs[i].volume = vol.handle
+        reqs[i].params = _abi.make_params(iso, _abi.MODE_DUP_POLYGON_NORMAL)
+    ctx.check(ctx.lib.kvsmc_count_batch(ctx.handle, reqs, n), "count")
+    outs = []
+    for i in range(n):
+        s = reqs[i].sizes
+        c = torch.empty(max(1, s.ncoords), dtype=torch.float32, device="cuda")
+        nn = torch.empty(max(1, s.nnormals), dtype=torch.float32, device="cuda")
+        outs.append((c, nn))
+        reqs[i].d_coords, reqs[i].coords_capacity = c.data_ptr(), s.ncoords
+        reqs[i].d_normals, reqs[i].normals_capacity = nn.data_ptr(), s.nnormals
+    ntri = sum(reqs[i].sizes.ntriangles for i in range(n))
+    cells = (nx - 1) * (ny - 1) * (nz - 1) * n
+
+    def step():
+        ctx.check(ctx.lib.kvsmc_extract_batch(ctx.handle, reqs, n), "extract_batch")
+
+    for _ in range(args.warmup):
+        step()
+    torch.cuda.synchronize()
+    clocks = Clocks(local)
+    clocks.start()
+    ctx.profile_enable(True)
+    launches0 = ctx.kernel_launches
+    if world > 1:
+        import torch.distributed as dist
+        dist.barrier()
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for _ in range(args.steps):
+        step()
+    e1.record(stream)
+    torch.cuda.synchronize()
+    ms = e0.elapsed_time(e1)
+    if world > 1:
+        dist.barrier()
+    prof = ctx.profile_read()
+    ctx.profile_enable(False)
+    launches = ctx.kernel_launches - launches0
+    clk = clocks.stop()
+    ms_max = barrier_max(ms, world)
+    step_ms = ms_max / args.steps
+    value = cells * world / (step_ms * 1e-3) / 1e6
+    # roofline of the dominant kernel (the fused emit launch)
+    hbm, peak_kind = peaks()
+    algo_bytes = nx * ny * nz * 4 + 48 * ntri
+    dom = max(prof.items(), key=lambda kv: kv[1][1])
+    emit_launches, emit_ms = prof.get("stream_emit", (0, 0.0))
+    roofline = None
+    if emit_launches:
+        per = emit_ms / emit_launches
+        achieved = algo_bytes / (per * 1e-3) / 1e9
+        tr = traffic_per_launch(args.workload)
+        roofline = {"kernel": "stream_emit", "bound": "hbm", "achieved": round(achieved, 1), "peak": hbm,
+                    "peak_kind": peak_kind, "unit": "GB/s", "frac": round(achieved / hbm, 4),
+                    "algorithmic_bytes_per_launch": algo_bytes, "launch_ms": round(per, 4),
+                    "traffic": tr}
+    # end to end through the C ABI with host buffers
+    e2e = None
+    if host_field is not None:
+        e2e = run_e2e(ctx, host_field, isos, reqs, args, stream)
+        if e2e is not None:
+            e2e["value"] = round(cells / (e2e.pop("step_ms") * 1e-3) / 1e6 * world, 1)
+            e2e["unit"] = "Mcells/s"
+    line = {
+        "metric": "Mcells/s", "value": round(value, 1), "unit": "Mcells/s", "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(step_ms, 4),
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+        "data": "synthetic (seeded fBm generated on the device)",
+        "config": {"workload": w["desc"], "volume": [nx, ny, nz], "isovalues": n,
+                   "mode": "duplication+PolygonNormal", "cache": "inputs larger than L2 (4 GiB volume, "
+                   "outputs ~48 B/triangle)" if args.workload == "sweep1024" else "input smaller than L2"},
+        "mtris_per_s": round(ntri * world / (step_ms * 1e-3) / 1e6, 1),
+        "triangles_per_step": int(ntri),
+        "roofline": roofline,
+        "kernels": {k: {"launches": v[0], "ms": round(v[1], 3)} for k, v in prof.items()},
+        "dominant_kernel": dom[0],
+        "e2e": e2e,
+        "gpu_launches": int(launches),
+        "clocks": clk,
+    }
+    return line
+
+
+def run_e2e(ctx, host_field, isos, reqs, args, stream):
+    """Same sweep through kvsmc_extract_batch_host: H2D of the volume from
+    pinned memory, both launches, D2H of every output into pinned buffers."""
+    import torch
+
+    from kvs_gb300 import _abi
+    n = len(isos)
+    pinned = {}
+    for i in range(n):
+        s = reqs[i].sizes
+        pinned[(i, 0)] = torch.empty(max(1, s.ncoords), dtype=torch.float32, pin_memory=True).numpy()
+        pinned[(i, 1)] = torch.empty(max(1, s.nnormals), dtype=torch.float32, pin_memory=True).numpy()
+    params = [_abi.make_params(iso, _abi.MODE_DUP_POLYGON_NORMAL) for iso in isos]
+    host = host_field.numpy()
+
+    def buf(req, kind, count):
+        a = pinned.get((req, kind))
+        return a if a is not None and a.size >= count else None
+
+    steps = max(1, min(args.steps, 3))
+    for _ in range(1):
+        _abi.extract_batch_host(ctx, host, params, buf)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for _ in range(steps):
+        out = _abi.extract_batch_host(ctx, host, params, buf)
+    torch.cuda.synchronize()
+    t = (time.perf_counter() - t0) / steps
+    h2d = host.nbytes
+    d2h = sum(o["coords"].nbytes + o["normals"].nbytes for o in out)
+    return {"step_ms": t * 1e3, "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h),
+            "api": "kvsmc_extract_batch_host", "steps": steps}
+
+
+# ----------------------------------------------------------------- CPU side
+
+def cpu_slab_sample(args, slab_planes):
+    """A z-slab of the workload's field (generated on the CPU, same generator)."""
+    import torch
+    from kvs_gb300 import synthetic as S
+    w = WORKLOADS[args.workload]
+    nz, ny, nx = w["shape"]
+    if w["kind"] == "fbm":
+        # same field: generate the full-depth statistics on a slab (rescaled
+        # per slab; the sample only sets the cost per cell)
+        f = S.fbm((slab_planes, ny, nx), seed=42, device="cpu")
+    else:
+        f = S.gaussian_blobs((min(slab_planes, nz), ny, nx), seed=42, device="cpu")
+    return f.numpy()
+
+
+def run_cpu(args, threads, planes, isos):
+    """The oracle (C restatement of kvs::MarchingCubes) over (isovalue) units on
+    `threads` host threads; returns (cells x isovalues)/s and the sample text."""
+    from oracle import oracle
+    oracle.build()
+    v = getattr(args, "cpu_slab", None)
+    if v is None:
+        v = cpu_slab_sample(args, planes)
+    vmin, vmax = float(v.min()), float(v.max())
+    nz, ny, nx = v.shape
+    cells = (nx - 1) * (ny - 1) * (nz - 1)
+
+    def one(iso):
+        oracle.extract(v, iso, 0, vmin, vmax)
+        return cells
+
+    t0 = time.perf_counter()
+    if threads == 1:
+        done = sum(one(i) for i in isos)
+    else:
+        with cf.ThreadPoolExecutor(max_workers=threads) as ex:
+            done = sum(ex.map(one, isos))
+    t = time.perf_counter() - t0
+    return done / t / 1e6, t, f"{len(isos)} isovalues x {nx}x{ny}x{nz} slab ({done / 1e6:.0f} M cell-isovalues)"
+
+
+def run_reference(args, rank, world):
+    if rank != 0:
+        return None
+    w = WORKLOADS[args.workload]
+    threads = os.cpu_count() or 1
+    planes = 65 if args.workload == "sweep1024" else w["shape"][0]
+    isos = w["isos"]
+    vals = []
+    sample = ""
+    for i in range(args.warmup + args.steps):
+        v, t, sample = run_cpu(args, threads, planes, isos)
+        if i >= args.warmup:
+            vals.append((v, t))
+    value = statistics.median(v for v, _ in vals)
+    ms = statistics.median(t for _, t in vals) * 1e3
+    return {
+        "impl": "reference", "metric": "Mcells/s", "value": round(value, 1), "unit": "Mcells/s",
+        "n_gpus": world, "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(ms, 1),
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+        "config": {"workload": w["desc"], "sample": sample},
+        "cpu_baseline": {"value": round(value, 1), "unit": "Mcells/s", "cores": threads, "kind": "port",
+                         "sample": sample + "; oracle/mc_oracle.c (C restatement of kvs::MarchingCubes, "
+                         "-O3 -ffp-contract=off), one isovalue per thread"},
+        "e2e": {"value": round(value, 1), "unit": "Mcells/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--workload", default="sweep1024", choices=sorted(WORKLOADS))
+    ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--no-cpu", action="store_true")
+    args = ap.parse_args()
+    args.warmup = max(3, args.warmup)
+    rank, world, local = dist_env()
+    if world > 1:
+        import torch
+        import torch.distributed as dist
+        torch.cuda.set_device(local)
+        dist.init_process_group("nccl")
+    if args.impl == "reference":
+        line = run_reference(args, rank, world)
+    else:
+        line = run_ours(args, rank, world, local)
+        if rank == 0 and world == 1 and not args.no_cpu:
+            planes = 65 if args.workload == "sweep1024" else WORKLOADS[args.workload]["shape"][0]
+            isos = WORKLOADS[args.workload]["isos"] if args.workload == "sweep1024" else \
+                WORKLOADS[args.workload]["isos"] * 50
+            v, t, sample = run_cpu(args, 1, planes, isos)
+            line["cpu_baseline"] = {"value": round(v, 1), "unit": "Mcells/s", "cores": 1, "kind": "port",
+                                    "sample": sample + f"; {t:.1f} s on 1 host core; oracle/mc_oracle.c"}
+    if rank == 0 and line is not None:
+        print(json.dumps(line), flush=True)
+    if world > 1:
+        import torch.distributed as dist
+        dist.barrier()
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

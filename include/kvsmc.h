@@ -108,6 +108,11 @@ kvsmc_status kvsmc_set_stream(kvsmc_context* ctx, void* cuda_stream);
 kvsmc_status kvsmc_synchronize(kvsmc_context* ctx);
 /* Number of kernels this context has launched since creation. */
 uint64_t kvsmc_kernel_launches(const kvsmc_context* ctx);
+/* Kernel family: 0 (default) = streaming kernels for duplicated-mode requests
+ * on 8/16-bit and float32 volumes, gather kernels for the rest; 1 = gather
+ * kernels for everything.  Both give identical results.  No counterpart in
+ * the reference (which has one CPU loop). */
+kvsmc_status kvsmc_set_kernel_path(kvsmc_context* ctx, int32_t path);
 
 /* ------------------------------------------------------------------ volumes */
 
@@ -167,12 +172,41 @@ typedef struct kvsmc_request {
     kvsmc_status status;   /* out */
 } kvsmc_request;
 
+/* Several isolevels (or modes) of one HOST volume in one call: the volume is
+ * uploaded once, all requests run batched, and each request's arrays are
+ * allocated through `alloc` (user pointer `alloc_user`, `which` as above plus
+ * 3 * request index) and copied back.  sizes: n entries.  The reference
+ * equivalent is n kvs::MarchingCubes constructions on the same volume
+ * (Tool/kvsview/Isosurface.cpp:238-249 re-extracts per isolevel). */
+kvsmc_status kvsmc_extract_batch_host(kvsmc_context* ctx, const void* host_values, kvsmc_dtype dtype,
+                                      uint32_t nx, uint32_t ny, uint32_t nz, const kvsmc_params* params,
+                                      int32_t n, kvsmc_host_alloc_fn alloc, void* alloc_user, kvsmc_sizes* sizes);
+
 /* Count every request of a batch in one fused launch (all volumes and
  * isolevels); fills reqs[i].sizes. */
 kvsmc_status kvsmc_count_batch(kvsmc_context* ctx, kvsmc_request* reqs, int32_t n);
 /* Count + emit a whole batch: fused launches over all requests, so each
  * volume is read once per pass however many isolevels share it. */
 kvsmc_status kvsmc_extract_batch(kvsmc_context* ctx, kvsmc_request* reqs, int32_t n);
+
+/* ------------------------------------------------------------ diagnostics */
+
+/* Per-kernel timing: with profiling on, every kernel family launched by this
+ * context is bracketed by CUDA events on its own stream.  enable() clears the
+ * totals.  read() waits for the recorded events and returns the number of
+ * kernel families; for the first `max` it fills the name, the launch count
+ * and the summed device milliseconds.  The reference times whole calls on
+ * the host (kvs::Timer, Utility/Timer.h); this is the device-side analogue. */
+kvsmc_status kvsmc_profile_enable(kvsmc_context* ctx, int32_t on);
+int32_t kvsmc_profile_read(kvsmc_context* ctx, int32_t max, const char** names, uint64_t* launches, double* ms);
+
+/* Device self-check of the FP32 interpolation path: n random straddling edges
+ * (several value distributions) interpolated both by the FP32 path and by the
+ * reference's FP64 sequence (interpolate_vertex, MarchingCubes.cpp:327-356).
+ * Reports how many were tested, how many float results differ (must be 0)
+ * and how many fell back to FP64.  No counterpart in the reference. */
+kvsmc_status kvsmc_selftest_interpolation(kvsmc_context* ctx, uint64_t n, uint64_t seed, uint64_t* tested,
+                                          uint64_t* mismatches, uint64_t* fallbacks);
 
 #ifdef __cplusplus
 }

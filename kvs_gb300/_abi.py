@@ -38,8 +38,13 @@ EXPORTS = [
     "kvsmc_volume_upload", "kvsmc_volume_from_device", "kvsmc_volume_update",
     "kvsmc_volume_free", "kvsmc_volume_minmax",
     "kvsmc_count", "kvsmc_extract_device", "kvsmc_marching_cubes_host",
-    "kvsmc_count_batch", "kvsmc_extract_batch",
+    "kvsmc_count_batch", "kvsmc_extract_batch", "kvsmc_set_kernel_path",
+    "kvsmc_selftest_interpolation", "kvsmc_profile_enable", "kvsmc_profile_read",
+    "kvsmc_extract_batch_host",
 ]
+
+PATH_AUTO = 0      # streaming kernels where eligible
+PATH_GATHER = 1    # gather kernels only
 
 
 def dtype_code(dt):
@@ -113,6 +118,13 @@ def load(path=LIB_PATH):
                                                 HOST_ALLOC, vp, C.POINTER(Sizes)]),
         "kvsmc_count_batch": (C.c_int, [vp, C.POINTER(Request), i32]),
         "kvsmc_extract_batch": (C.c_int, [vp, C.POINTER(Request), i32]),
+        "kvsmc_set_kernel_path": (C.c_int, [vp, i32]),
+        "kvsmc_selftest_interpolation": (C.c_int, [vp, u64, u64, C.POINTER(u64), C.POINTER(u64),
+                                                   C.POINTER(u64)]),
+        "kvsmc_extract_batch_host": (C.c_int, [vp, vp, C.c_int, u32, u32, u32, C.POINTER(Params), i32,
+                                               HOST_ALLOC, vp, C.POINTER(Sizes)]),
+        "kvsmc_profile_enable": (C.c_int, [vp, i32]),
+        "kvsmc_profile_read": (i32, [vp, i32, C.POINTER(C.c_char_p), C.POINTER(u64), C.POINTER(C.c_double)]),
     }
     for name, (res, args) in sig.items():
         f = getattr(lib, name)
@@ -155,6 +167,27 @@ class Context:
     @property
     def kernel_launches(self):
         return int(self.lib.kvsmc_kernel_launches(self.handle))
+
+    def set_kernel_path(self, path):
+        self.check(self.lib.kvsmc_set_kernel_path(self.handle, int(path)), "kvsmc_set_kernel_path")
+
+    def profile_enable(self, on=True):
+        self.check(self.lib.kvsmc_profile_enable(self.handle, 1 if on else 0), "kvsmc_profile_enable")
+
+    def profile_read(self):
+        """{kernel family: (launches, device ms)} since profile_enable()."""
+        n = self.lib.kvsmc_profile_read(self.handle, 0, None, None, None)
+        names = (C.c_char_p * max(1, n))()
+        launches = (C.c_uint64 * max(1, n))()
+        ms = (C.c_double * max(1, n))()
+        self.lib.kvsmc_profile_read(self.handle, n, names, launches, ms)
+        return {names[i].decode(): (int(launches[i]), float(ms[i])) for i in range(n)}
+
+    def selftest_interpolation(self, n, seed=1):
+        t, m, f = C.c_uint64(), C.c_uint64(), C.c_uint64()
+        self.check(self.lib.kvsmc_selftest_interpolation(self.handle, int(n), int(seed), C.byref(t), C.byref(m),
+                                                         C.byref(f)), "kvsmc_selftest_interpolation")
+        return t.value, m.value, f.value
 
     def close(self):
         if getattr(self, "handle", None):
@@ -247,3 +280,37 @@ def marching_cubes_host(ctx, values, params):
               "kvsmc_marching_cubes_host")
     empty_f = np.zeros(0, np.float32)
     return (bufs.get(0, empty_f), bufs.get(1, empty_f), bufs.get(2, np.zeros(0, np.uint32)), sizes_dict(s))
+
+
+def extract_batch_host(ctx, values, params_list, buffer_for=None):
+    """kvsmc_extract_batch_host: one host volume, several requests.
+
+    buffer_for(request, which, count) may return a preallocated numpy array of
+    at least `count` elements (e.g. pinned memory) to receive that output;
+    otherwise a fresh numpy array is allocated.  Returns one dict per request.
+    """
+    v = np.ascontiguousarray(values)
+    nz, ny, nx = v.shape
+    n = len(params_list)
+    ps = (Params * max(1, n))(*params_list)
+    sizes = (Sizes * max(1, n))()
+    bufs = {}
+
+    def alloc(user, which, count):
+        req, kind = divmod(which, 3)
+        a = buffer_for(req, kind, count) if buffer_for is not None else None
+        if a is None:
+            a = np.empty(count, dtype=np.uint32 if kind == 2 else np.float32)
+        bufs[(req, kind)] = a
+        return a.ctypes.data
+
+    cb = HOST_ALLOC(alloc)
+    ctx.check(ctx.lib.kvsmc_extract_batch_host(ctx.handle, v.ctypes.data, dtype_code(v.dtype), nx, ny, nz, ps, n, cb,
+                                               None, sizes), "kvsmc_extract_batch_host")
+    out = []
+    for i in range(n):
+        s = sizes_dict(sizes[i])
+        e = np.zeros(0, np.float32)
+        out.append(dict(coords=bufs.get((i, 0), e)[:s["ncoords"]], normals=bufs.get((i, 1), e)[:s["nnormals"]],
+                        connections=bufs.get((i, 2), np.zeros(0, np.uint32))[:s["nconnections"]], sizes=s))
+    return out

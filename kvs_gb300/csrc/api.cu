@@ -1,40 +1,19 @@
 // api.cu -- the C ABI of libkvsmc (include/kvsmc.h): contexts, resident
-// volumes, and the count -> size -> emit pipeline for one request.
+// volumes, and request pipelines.  Duplicated-mode requests on 8/16-bit and
+// float32 volumes run through the streaming kernels (batch.cu); the others
+// through the gather kernels (mc_gather.cu), one request at a time.
 #include <cmath>
 #include <cstdarg>
 #include <cstdio>
 #include <cstring>
 #include <string>
+#include <vector>
 
-#include "../../include/kvsmc.h"
-#include "mc_internal.h"
+#include "batch.h"
 
 using namespace kvsmc;
 
-struct kvsmc_volume {
-    VolumeView view;
-    void* dev = nullptr;        // owned device allocation
-    size_t bytes = 0;
-    bool has_minmax = false;
-    double vmin = 0.0, vmax = 0.0;
-};
-
-struct kvsmc_context {
-    int device = 0;
-    int num_sms = 0;
-    cudaStream_t own_stream = nullptr;
-    cudaStream_t stream = nullptr;
-    void* scratch = nullptr;     // grow-only arena for per-request intermediates
-    size_t scratch_bytes = 0;
-    void* out_arena = nullptr;   // grow-only device outputs of the host call
-    size_t out_bytes = 0;
-    kvsmc_volume* host_vol = nullptr;  // staging volume of the host call
-    uint64_t* h_small = nullptr; // pinned: totals read back from the device
-    uint64_t launches = 0;
-    std::string last_error;
-};
-
-namespace {
+namespace kvsmc_host {
 
 kvsmc_status fail(kvsmc_context* ctx, kvsmc_status st, const char* fmt, ...)
 {
@@ -48,19 +27,6 @@ kvsmc_status fail(kvsmc_context* ctx, kvsmc_status st, const char* fmt, ...)
     }
     return st;
 }
-
-#define KVSMC_CUDA(ctx, call)                                                          \
-    do {                                                                               \
-        cudaError_t e_ = (call);                                                       \
-        if (e_ != cudaSuccess)                                                         \
-            return fail(ctx, e_ == cudaErrorMemoryAllocation ? KVSMC_ERR_OUT_OF_MEMORY \
-                                                             : KVSMC_ERR_CUDA,         \
-                        "%s: %s (%s:%d)", #call, cudaGetErrorString(e_), __FILE__, __LINE__); \
-    } while (0)
-
-inline size_t align_up(size_t v, size_t a) { return (v + a - 1) / a * a; }
-
-Launch launch_of(kvsmc_context* ctx) { return Launch{ctx->stream, ctx->num_sms, &ctx->launches}; }
 
 kvsmc_status ensure_scratch(kvsmc_context* ctx, size_t bytes)
 {
@@ -77,25 +43,75 @@ kvsmc_status ensure_scratch(kvsmc_context* ctx, size_t bytes)
     return KVSMC_OK;
 }
 
-// Bump allocator over the scratch arena (256-byte aligned pieces).
-struct Carve {
-    char* base;
-    size_t off = 0;
-    template <typename P> P* take(size_t bytes) {
-        P* p = reinterpret_cast<P*>(base + off);
-        off = align_up(off + bytes, 256);
-        return p;
+kvsmc_status ensure_stage(kvsmc_context* ctx, size_t bytes)
+{
+    if (bytes <= ctx->h_stage_bytes) return KVSMC_OK;
+    if (ctx->h_stage) {
+        KVSMC_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+        cudaFreeHost(ctx->h_stage);
+        ctx->h_stage = nullptr;
+        ctx->h_stage_bytes = 0;
     }
-};
+    const size_t want = align_up(bytes + bytes / 4, 1 << 16);
+    KVSMC_CUDA(ctx, cudaMallocHost(&ctx->h_stage, want));
+    ctx->h_stage_bytes = want;
+    return KVSMC_OK;
+}
 
-uint64_t elems_per_16B(int dtype) { return 16 / dtype_size(dtype); }
+kvsmc_status volume_minmax(kvsmc_context* ctx, kvsmc_volume* v)
+{
+    if (v->has_minmax) return KVSMC_OK;
+    const size_t part = align_up(minmax_scratch_bytes(ctx->num_sms), 256);
+    kvsmc_status st = ensure_scratch(ctx, part + 256);
+    if (st) return st;
+    double* d_out = reinterpret_cast<double*>(static_cast<char*>(ctx->scratch) + part);
+    KVSMC_CUDA(ctx, launch_minmax(v->view, ctx->scratch, d_out, launch_of(ctx)));
+    KVSMC_CUDA(ctx, cudaMemcpyAsync(ctx->h_small, d_out, 2 * sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
+    KVSMC_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    double mm[2];
+    std::memcpy(mm, ctx->h_small, sizeof mm);
+    v->vmin = mm[0];
+    v->vmax = mm[1];
+    v->has_minmax = true;
+    return KVSMC_OK;
+}
+
+// kvs::Math::Equal for doubles (Utility/Math.h:135-138).
+bool equal_ref(double a, double b)
+{
+    const double d = a - b;
+    return ((d < 0) ? -d : d) < 1.e-6;
+}
+
+// Exact classification thresholds (see Classifier).
+Classifier make_classifier(double iso)
+{
+    Classifier c;
+    c.iso = iso;
+    c.pad = 0;
+    float f = (float)iso;
+    if (!std::isnan(iso) && (double)f > iso) f = std::nextafter(f, -INFINITY);
+    c.f_thr = f;
+    if (std::isnan(iso) || iso >= 4.0e18) c.i_thr = 0x7fffffffffffffffLL;
+    else if (iso < -4.0e18) c.i_thr = (long long)(-0x7fffffffffffffffLL - 1);
+    else c.i_thr = (long long)std::floor(iso);
+    return c;
+}
+
+}  // namespace kvsmc_host
+
+using namespace kvsmc_host;
+
+namespace {
+
+size_t elems_per_16B(int dtype) { return 16 / dtype_size(dtype); }
 
 kvsmc_status volume_alloc(kvsmc_context* ctx, kvsmc_dtype dtype, uint32_t nx, uint32_t ny, uint32_t nz,
                           kvsmc_volume* v)
 {
     const size_t es = dtype_size(dtype);
     const uint64_t pitch = align_up(nx, elems_per_16B(dtype));
-    const size_t bytes = (size_t)pitch * ny * nz * es + 256;  // tail slack for vector loads
+    const size_t bytes = (size_t)pitch * ny * nz * es + 256;
     v->view.nx = nx; v->view.ny = ny; v->view.nz = nz;
     v->view.dtype = dtype;
     v->view.pitch = pitch;
@@ -133,52 +149,12 @@ kvsmc_status check_shape(kvsmc_context* ctx, int dtype, uint32_t nx, uint32_t ny
     return KVSMC_OK;
 }
 
-kvsmc_status volume_minmax(kvsmc_context* ctx, kvsmc_volume* v)
-{
-    if (v->has_minmax) return KVSMC_OK;
-    kvsmc_status st = ensure_scratch(ctx, minmax_scratch_bytes(ctx->num_sms) + 256);
-    if (st) return st;
-    double* d_out = reinterpret_cast<double*>(static_cast<char*>(ctx->scratch) + align_up(minmax_scratch_bytes(ctx->num_sms), 256));
-    KVSMC_CUDA(ctx, launch_minmax(v->view, ctx->scratch, d_out, launch_of(ctx)));
-    KVSMC_CUDA(ctx, cudaMemcpyAsync(ctx->h_small, d_out, 2 * sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
-    KVSMC_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
-    double mm[2];
-    std::memcpy(mm, ctx->h_small, sizeof mm);
-    v->vmin = mm[0];
-    v->vmax = mm[1];
-    v->has_minmax = true;
-    return KVSMC_OK;
-}
-
-// kvs::Math::Equal for doubles (Utility/Math.h:135-138).
-bool equal_ref(double a, double b)
-{
-    const double d = a - b;
-    return ((d < 0) ? -d : d) < 1.e-6;
-}
-
-// Exact classification thresholds (see Classifier).
-Classifier make_classifier(int dtype, double iso)
-{
-    Classifier c;
-    c.iso = iso;
-    c.pad = 0;
-    float f = (float)iso;
-    if (!std::isnan(iso) && (double)f > iso) f = std::nextafter(f, -INFINITY);
-    c.f_thr = f;
-    if (std::isnan(iso) || iso >= 4.0e18) c.i_thr = 0x7fffffffffffffffLL;
-    else if (iso < -4.0e18) c.i_thr = (long long)(-0x7fffffffffffffffLL - 1);
-    else c.i_thr = (long long)std::floor(iso);
-    (void)dtype;
-    return c;
-}
+// ------------------------------------------------------------ gather pipeline
 
 struct Plan {
     Job job;
-    bool extracted = true;
     bool shared = false;
     uint64_t ntri = 0, nvert = 0;
-    double vmin = 0, vmax = 0;
 };
 
 uint32_t rows_for(uint32_t width, uint32_t limit)
@@ -190,30 +166,19 @@ uint32_t rows_for(uint32_t width, uint32_t limit)
     return r;
 }
 
-kvsmc_status plan_request(kvsmc_context* ctx, kvsmc_volume* vol, const kvsmc_params* p, Plan& pl)
+void gather_plan(const Item& it, Plan& pl)
 {
-    if (!vol || !p) return fail(ctx, KVSMC_ERR_INVALID_ARGUMENT, "null volume or params");
-    if (p->mode < 0 || p->mode > 2) return fail(ctx, KVSMC_ERR_INVALID_ARGUMENT, "bad mode %d", p->mode);
-    if (p->has_minmax) {
-        pl.vmin = p->min_value;
-        pl.vmax = p->max_value;
-    } else {
-        kvsmc_status st = volume_minmax(ctx, vol);
-        if (st) return st;
-        pl.vmin = vol->vmin;
-        pl.vmax = vol->vmax;
-    }
-    pl.extracted = !equal_ref(pl.vmin, pl.vmax);
-    pl.shared = p->mode != KVSMC_DUP_POLYGON_NORMAL;
+    pl.shared = it.params.mode != KVSMC_DUP_POLYGON_NORMAL;
     Job& j = pl.job;
     std::memset(&j, 0, sizeof j);
-    j.vol = vol->view;
-    j.cls = make_classifier(vol->view.dtype, p->isolevel);
-    j.vmin = pl.vmin;
-    j.vmax = pl.vmax;
-    for (int k = 0; k < 3; ++k) { j.min_coord[k] = p->min_coord[k]; j.scale[k] = p->scale[k]; }
-    j.mode = p->mode;
-    const uint32_t nx = vol->view.nx, ny = vol->view.ny, nz = vol->view.nz;
+    j.vol = it.vol->view;
+    j.cls = make_classifier(it.params.isolevel);
+    j.ip.iso = it.params.isolevel;
+    j.ip.vmin = it.vmin;
+    j.ip.vmax = it.vmax;
+    for (int k = 0; k < 3; ++k) { j.ip.min_coord[k] = it.params.min_coord[k]; j.ip.scale[k] = it.params.scale[k]; }
+    j.mode = it.params.mode;
+    const uint32_t nx = j.vol.nx, ny = j.vol.ny, nz = j.vol.nz;
     const bool has_cells = nx > 1 && ny > 1 && nz > 1;
     j.cell_rows = rows_for(nx - 1, ny - 1);
     j.cell_ytiles = has_cells ? (ny - 1 + j.cell_rows - 1) / j.cell_rows : 0;
@@ -222,14 +187,13 @@ kvsmc_status plan_request(kvsmc_context* ctx, kvsmc_volume* vol, const kvsmc_par
     j.node_ytiles = (ny + j.node_rows - 1) / j.node_rows;
     j.node_tiles = pl.shared ? (uint64_t)nz * j.node_ytiles : 0;
     j.words_per_row = (nx + 31) / 32;
-    return KVSMC_OK;
 }
 
-// Count pass: fills pl.ntri / pl.nvert; leaves per-tile offsets in scratch.
-kvsmc_status count_request(kvsmc_context* ctx, Plan& pl)
+// Count pass of one gather request: fills pl.ntri / pl.nvert and leaves the
+// per-tile offsets in the scratch arena for gather_emit.
+kvsmc_status gather_count(kvsmc_context* ctx, Plan& pl)
 {
     pl.ntri = pl.nvert = 0;
-    if (!pl.extracted) return KVSMC_OK;
     Job& j = pl.job;
     const size_t ct = j.cell_tiles, nt = j.node_tiles;
     const uint64_t rank_words = pl.shared ? (uint64_t)j.vol.nz * j.vol.ny * j.words_per_row : 0;
@@ -247,7 +211,7 @@ kvsmc_status count_request(kvsmc_context* ctx, Plan& pl)
     j.rank = cv.take<uint4>(rank_words * 16);
     void* scan_a = cv.take<char>(scan_scratch_bytes(ct));
     void* scan_b = cv.take<char>(scan_scratch_bytes(nt));
-    const Launch L = launch_of(ctx);
+    const kvsmc::Launch L = launch_of(ctx);
     KVSMC_CUDA(ctx, cudaMemsetAsync(d_totals, 0, 2 * sizeof(uint64_t), ctx->stream));
     if (ct) {
         KVSMC_CUDA(ctx, launch_cell_count(j, L));
@@ -267,37 +231,34 @@ kvsmc_status count_request(kvsmc_context* ctx, Plan& pl)
     return KVSMC_OK;
 }
 
-void fill_sizes(const Plan& pl, const kvsmc_params* p, kvsmc_sizes* s)
+void gather_sizes(const Plan& pl, const Item& it, kvsmc_sizes* s)
 {
     std::memset(s, 0, sizeof *s);
     s->ntriangles = pl.ntri;
     s->nvertices = pl.nvert;
-    s->min_value = pl.vmin;
-    s->max_value = pl.vmax;
-    s->extracted = pl.extracted ? 1 : 0;
-    if (!pl.extracted) return;
+    s->min_value = it.vmin;
+    s->max_value = it.vmax;
+    s->extracted = 1;
     if (!pl.shared) {
         s->ncoords = 9 * pl.ntri;
         s->nnormals = 3 * pl.ntri;
-        s->nconnections = 0;
     } else {
         s->ncoords = 3 * pl.nvert;
         s->nconnections = 3 * pl.ntri;
-        // calculate_normals_on_polygon sizes by connections, on_vertex by coords;
-        // both produce nothing when there are no coords (MarchingCubes.cpp:536,574).
+        // calculate_normals_on_polygon sizes by connections, on_vertex by
+        // coords; both leave nothing when there are no coords (MarchingCubes.cpp:536,574).
         if (pl.nvert == 0) s->nnormals = 0;
-        else s->nnormals = (p->mode == KVSMC_SHARED_VERTEX_NORMAL) ? 3 * pl.nvert : 3 * pl.ntri;
+        else s->nnormals = (it.params.mode == KVSMC_SHARED_VERTEX_NORMAL) ? 3 * pl.nvert : 3 * pl.ntri;
     }
 }
 
-kvsmc_status emit_request(kvsmc_context* ctx, Plan& pl, float* coords, float* normals, uint32_t* conn)
+kvsmc_status gather_emit(kvsmc_context* ctx, Plan& pl, float* coords, float* normals, uint32_t* conn)
 {
-    if (!pl.extracted) return KVSMC_OK;
     Job& j = pl.job;
     j.coords = coords;
     j.normals = normals;
     j.connections = conn;
-    const Launch L = launch_of(ctx);
+    const kvsmc::Launch L = launch_of(ctx);
     if (!pl.shared) {
         if (pl.ntri) KVSMC_CUDA(ctx, launch_emit_dup(j, L));
         return KVSMC_OK;
@@ -306,6 +267,97 @@ kvsmc_status emit_request(kvsmc_context* ctx, Plan& pl, float* coords, float* no
     if (pl.ntri) KVSMC_CUDA(ctx, launch_connect(j, L));
     if (pl.nvert && j.mode == KVSMC_SHARED_VERTEX_NORMAL) KVSMC_CUDA(ctx, launch_vertex_normals(j, L));
     return KVSMC_OK;
+}
+
+// ------------------------------------------------------------ request setup
+
+// Decide min/max (MapperBase::setRange) and the Equal early exit.
+kvsmc_status prepare(kvsmc_context* ctx, Item& it)
+{
+    if (!it.vol) return fail(ctx, KVSMC_ERR_INVALID_ARGUMENT, "null volume");
+    if (it.params.mode < 0 || it.params.mode > 2) return fail(ctx, KVSMC_ERR_INVALID_ARGUMENT, "bad mode %d", it.params.mode);
+    if (it.params.has_minmax) {
+        it.vmin = it.params.min_value;
+        it.vmax = it.params.max_value;
+    } else {
+        kvsmc_status st = volume_minmax(ctx, it.vol);
+        if (st) return st;
+        it.vmin = it.vol->vmin;
+        it.vmax = it.vol->vmax;
+    }
+    it.extracted = !equal_ref(it.vmin, it.vmax);
+    std::memset(&it.sizes, 0, sizeof it.sizes);
+    it.sizes.min_value = it.vmin;
+    it.sizes.max_value = it.vmax;
+    return KVSMC_OK;
+}
+
+bool capacity_ok(const Item& it)
+{
+    return it.sizes.ncoords <= it.coords_cap && it.sizes.nnormals <= it.normals_cap &&
+           it.sizes.nconnections <= it.conn_cap && (!it.sizes.ncoords || it.d_coords) &&
+           (!it.sizes.nnormals || it.d_normals) && (!it.sizes.nconnections || it.d_conn);
+}
+
+// Run a list of prepared items: streaming ones together, the rest one by
+// one.  emit=false only counts.  Per-item status in it.status; returns the
+// first error.
+kvsmc_status run_items(kvsmc_context* ctx, std::vector<Item*>& items, bool emit)
+{
+    std::vector<Item*> stream_items, gather_items;
+    for (Item* it : items) {
+        if (it->status) continue;
+        if (!it->extracted) continue;
+        (stream_eligible(ctx, *it) ? stream_items : gather_items).push_back(it);
+    }
+    kvsmc_status first = KVSMC_OK;
+    if (!stream_items.empty()) {
+        StreamBatch b;
+        b.ctx = ctx;
+        b.items = stream_items;
+        kvsmc_status st = b.plan();
+        if (!st) st = b.count();
+        if (!st && emit) {
+            for (Item* it : stream_items) {
+                it->emit = true;
+                if (!capacity_ok(*it)) {
+                    it->status = fail(ctx, KVSMC_ERR_CAPACITY, "output needs %llu coords, %llu normals",
+                                      (unsigned long long)it->sizes.ncoords, (unsigned long long)it->sizes.nnormals);
+                }
+            }
+            st = b.emit();
+            if (!st) st = b.finish();
+        }
+        if (st) {
+            for (Item* it : stream_items) if (!it->status) it->status = st;
+            first = st;
+        }
+    }
+    for (Item* it : gather_items) {
+        Plan pl;
+        gather_plan(*it, pl);
+        kvsmc_status st = gather_count(ctx, pl);
+        if (!st) {
+            gather_sizes(pl, *it, &it->sizes);
+            if (emit) {
+                if (!capacity_ok(*it)) {
+                    st = fail(ctx, KVSMC_ERR_CAPACITY, "output needs %llu coords, %llu normals, %llu connections",
+                              (unsigned long long)it->sizes.ncoords, (unsigned long long)it->sizes.nnormals,
+                              (unsigned long long)it->sizes.nconnections);
+                } else {
+                    st = gather_emit(ctx, pl, it->d_coords, it->d_normals, it->d_conn);
+                    if (!st) KVSMC_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+                }
+            }
+        }
+        if (st) {
+            it->status = st;
+            if (!first) first = st;
+        }
+    }
+    for (Item* it : items)
+        if (it->status && !first) first = it->status;
+    return first;
 }
 
 kvsmc_status use_device(kvsmc_context* ctx)
@@ -361,6 +413,7 @@ kvsmc_status kvsmc_create(int device, kvsmc_context** out)
         return KVSMC_ERR_CUDA;
     }
     ctx->stream = ctx->own_stream;
+    ctx->prof = profiler_create();
     *out = ctx;
     return KVSMC_OK;
 }
@@ -374,6 +427,8 @@ void kvsmc_destroy(kvsmc_context* ctx)
     if (ctx->scratch) cudaFree(ctx->scratch);
     if (ctx->out_arena) cudaFree(ctx->out_arena);
     if (ctx->h_small) cudaFreeHost(ctx->h_small);
+    if (ctx->h_stage) cudaFreeHost(ctx->h_stage);
+    profiler_destroy(ctx->prof);
     if (ctx->own_stream) cudaStreamDestroy(ctx->own_stream);
     delete ctx;
 }
@@ -386,6 +441,13 @@ kvsmc_status kvsmc_set_stream(kvsmc_context* ctx, void* s)
 {
     if (!ctx) return KVSMC_ERR_INVALID_ARGUMENT;
     ctx->stream = s ? static_cast<cudaStream_t>(s) : ctx->own_stream;
+    return KVSMC_OK;
+}
+
+kvsmc_status kvsmc_set_kernel_path(kvsmc_context* ctx, int32_t path)
+{
+    if (!ctx || path < 0 || path > 1) return KVSMC_ERR_INVALID_ARGUMENT;
+    ctx->path = path;
     return KVSMC_OK;
 }
 
@@ -467,12 +529,15 @@ kvsmc_status kvsmc_count(kvsmc_context* ctx, kvsmc_volume* vol, const kvsmc_para
 {
     kvsmc_status st = use_device(ctx);
     if (st) return st;
-    if (!sizes) return fail(ctx, KVSMC_ERR_INVALID_ARGUMENT, "null sizes");
-    Plan pl;
-    if ((st = plan_request(ctx, vol, p, pl))) return st;
-    if ((st = count_request(ctx, pl))) return st;
-    fill_sizes(pl, p, sizes);
-    return KVSMC_OK;
+    if (!sizes || !p) return fail(ctx, KVSMC_ERR_INVALID_ARGUMENT, "null pointer");
+    Item it;
+    it.vol = vol;
+    it.params = *p;
+    if ((st = prepare(ctx, it))) return st;
+    std::vector<Item*> v{&it};
+    st = run_items(ctx, v, false);
+    *sizes = it.sizes;
+    return st;
 }
 
 kvsmc_status kvsmc_extract_device(kvsmc_context* ctx, kvsmc_volume* vol, const kvsmc_params* p,
@@ -481,20 +546,18 @@ kvsmc_status kvsmc_extract_device(kvsmc_context* ctx, kvsmc_volume* vol, const k
 {
     kvsmc_status st = use_device(ctx);
     if (st) return st;
-    if (!sizes) return fail(ctx, KVSMC_ERR_INVALID_ARGUMENT, "null sizes");
-    Plan pl;
-    if ((st = plan_request(ctx, vol, p, pl))) return st;
-    if ((st = count_request(ctx, pl))) return st;
-    fill_sizes(pl, p, sizes);
-    if (sizes->ncoords > coords_cap || sizes->nnormals > normals_cap || sizes->nconnections > conn_cap)
-        return fail(ctx, KVSMC_ERR_CAPACITY, "output needs %llu coords, %llu normals, %llu connections",
-                    (unsigned long long)sizes->ncoords, (unsigned long long)sizes->nnormals,
-                    (unsigned long long)sizes->nconnections);
-    if ((sizes->ncoords && !d_coords) || (sizes->nnormals && !d_normals) || (sizes->nconnections && !d_conn))
-        return fail(ctx, KVSMC_ERR_INVALID_ARGUMENT, "null output buffer");
-    if ((st = emit_request(ctx, pl, d_coords, d_normals, d_conn))) return st;
-    KVSMC_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
-    return KVSMC_OK;
+    if (!sizes || !p) return fail(ctx, KVSMC_ERR_INVALID_ARGUMENT, "null pointer");
+    Item it;
+    it.vol = vol;
+    it.params = *p;
+    it.d_coords = d_coords; it.coords_cap = coords_cap;
+    it.d_normals = d_normals; it.normals_cap = normals_cap;
+    it.d_conn = d_conn; it.conn_cap = conn_cap;
+    if ((st = prepare(ctx, it))) return st;
+    std::vector<Item*> v{&it};
+    st = run_items(ctx, v, true);
+    *sizes = it.sizes;
+    return st;
 }
 
 kvsmc_status kvsmc_marching_cubes_host(kvsmc_context* ctx, const void* host, kvsmc_dtype dtype,
@@ -509,13 +572,31 @@ kvsmc_status kvsmc_marching_cubes_host(kvsmc_context* ctx, const void* host, kvs
     kvsmc_volume* v = ctx->host_vol;
     if ((st = volume_alloc(ctx, dtype, nx, ny, nz, v))) return st;
     if ((st = volume_copy_in(ctx, v, host, cudaMemcpyHostToDevice))) return st;
+    Item it;
+    it.vol = v;
+    it.params = *p;
+    if ((st = prepare(ctx, it))) return st;
+    *sizes = it.sizes;
+    if (!it.extracted) return KVSMC_OK;
+    // count, size the device outputs, emit
+    std::vector<Item*> items{&it};
+    const bool streaming = stream_eligible(ctx, it);
+    StreamBatch b;
     Plan pl;
-    if ((st = plan_request(ctx, v, p, pl))) return st;
-    if ((st = count_request(ctx, pl))) return st;
-    fill_sizes(pl, p, sizes);
+    if (streaming) {
+        b.ctx = ctx;
+        b.items = items;
+        if ((st = b.plan()) || (st = b.count())) return st;
+    } else {
+        gather_plan(it, pl);
+        if ((st = gather_count(ctx, pl))) return st;
+        gather_sizes(pl, it, &it.sizes);
+    }
+    *sizes = it.sizes;
     const size_t bc = align_up(sizes->ncoords * 4, 256), bn = align_up(sizes->nnormals * 4, 256);
     const size_t bk = align_up(sizes->nconnections * 4, 256);
     if (bc + bn + bk > ctx->out_bytes) {
+        KVSMC_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
         if (ctx->out_arena) cudaFree(ctx->out_arena);
         ctx->out_arena = nullptr;
         ctx->out_bytes = 0;
@@ -524,49 +605,185 @@ kvsmc_status kvsmc_marching_cubes_host(kvsmc_context* ctx, const void* host, kvs
         ctx->out_bytes = want;
     }
     char* base = static_cast<char*>(ctx->out_arena);
-    float* dc = reinterpret_cast<float*>(base);
-    float* dn = reinterpret_cast<float*>(base + bc);
-    uint32_t* dk = reinterpret_cast<uint32_t*>(base + bc + bn);
-    if ((st = emit_request(ctx, pl, dc, dn, dk))) return st;
+    it.d_coords = reinterpret_cast<float*>(base);
+    it.d_normals = reinterpret_cast<float*>(base + bc);
+    it.d_conn = reinterpret_cast<uint32_t*>(base + bc + bn);
+    it.coords_cap = sizes->ncoords;
+    it.normals_cap = sizes->nnormals;
+    it.conn_cap = sizes->nconnections;
+    it.emit = true;
+    if (streaming) {
+        if ((st = b.emit()) || (st = b.finish())) return st;
+    } else {
+        if ((st = gather_emit(ctx, pl, it.d_coords, it.d_normals, it.d_conn))) return st;
+    }
     void* hc = nullptr;
     void* hn = nullptr;
     void* hk = nullptr;
     if (sizes->ncoords && !(hc = alloc(user, 0, sizes->ncoords))) return fail(ctx, KVSMC_ERR_OUT_OF_MEMORY, "host alloc (coords)");
     if (sizes->nnormals && !(hn = alloc(user, 1, sizes->nnormals))) return fail(ctx, KVSMC_ERR_OUT_OF_MEMORY, "host alloc (normals)");
     if (sizes->nconnections && !(hk = alloc(user, 2, sizes->nconnections))) return fail(ctx, KVSMC_ERR_OUT_OF_MEMORY, "host alloc (connections)");
-    if (hc) KVSMC_CUDA(ctx, cudaMemcpyAsync(hc, dc, sizes->ncoords * 4, cudaMemcpyDeviceToHost, ctx->stream));
-    if (hn) KVSMC_CUDA(ctx, cudaMemcpyAsync(hn, dn, sizes->nnormals * 4, cudaMemcpyDeviceToHost, ctx->stream));
-    if (hk) KVSMC_CUDA(ctx, cudaMemcpyAsync(hk, dk, sizes->nconnections * 4, cudaMemcpyDeviceToHost, ctx->stream));
+    if (hc) KVSMC_CUDA(ctx, cudaMemcpyAsync(hc, it.d_coords, sizes->ncoords * 4, cudaMemcpyDeviceToHost, ctx->stream));
+    if (hn) KVSMC_CUDA(ctx, cudaMemcpyAsync(hn, it.d_normals, sizes->nnormals * 4, cudaMemcpyDeviceToHost, ctx->stream));
+    if (hk) KVSMC_CUDA(ctx, cudaMemcpyAsync(hk, it.d_conn, sizes->nconnections * 4, cudaMemcpyDeviceToHost, ctx->stream));
     KVSMC_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
     return KVSMC_OK;
+}
+
+// Point the items' device outputs into the (grow-only) output arena.
+static kvsmc_status arena_outputs(kvsmc_context* ctx, std::vector<Item*>& its)
+{
+    size_t total = 0;
+    for (Item* it : its)
+        total += align_up(it->sizes.ncoords * 4, 256) + align_up(it->sizes.nnormals * 4, 256) +
+                 align_up(it->sizes.nconnections * 4, 256);
+    if (total > ctx->out_bytes) {
+        KVSMC_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+        if (ctx->out_arena) cudaFree(ctx->out_arena);
+        ctx->out_arena = nullptr;
+        ctx->out_bytes = 0;
+        const size_t want = align_up(total, 1 << 20);
+        KVSMC_CUDA(ctx, cudaMalloc(&ctx->out_arena, want));
+        ctx->out_bytes = want;
+    }
+    Carve cv{static_cast<char*>(ctx->out_arena)};
+    for (Item* it : its) {
+        it->d_coords = cv.take<float>(it->sizes.ncoords * 4);
+        it->d_normals = cv.take<float>(it->sizes.nnormals * 4);
+        it->d_conn = cv.take<uint32_t>(it->sizes.nconnections * 4);
+        it->coords_cap = it->sizes.ncoords;
+        it->normals_cap = it->sizes.nnormals;
+        it->conn_cap = it->sizes.nconnections;
+        it->emit = true;
+    }
+    return KVSMC_OK;
+}
+
+// Allocate each item's host arrays through the callback and copy them back.
+static kvsmc_status copy_back(kvsmc_context* ctx, std::vector<Item*>& its, const Item* first_item,
+                              kvsmc_host_alloc_fn alloc, void* user)
+{
+    for (Item* it : its) {
+        const int32_t base = 3 * (int32_t)(it - first_item);
+        const kvsmc_sizes& s = it->sizes;
+        void* hc = nullptr;
+        void* hn = nullptr;
+        void* hk = nullptr;
+        if (s.ncoords && !(hc = alloc(user, base + 0, s.ncoords))) return fail(ctx, KVSMC_ERR_OUT_OF_MEMORY, "host alloc (coords)");
+        if (s.nnormals && !(hn = alloc(user, base + 1, s.nnormals))) return fail(ctx, KVSMC_ERR_OUT_OF_MEMORY, "host alloc (normals)");
+        if (s.nconnections && !(hk = alloc(user, base + 2, s.nconnections)))
+            return fail(ctx, KVSMC_ERR_OUT_OF_MEMORY, "host alloc (connections)");
+        if (hc) KVSMC_CUDA(ctx, cudaMemcpyAsync(hc, it->d_coords, s.ncoords * 4, cudaMemcpyDeviceToHost, ctx->stream));
+        if (hn) KVSMC_CUDA(ctx, cudaMemcpyAsync(hn, it->d_normals, s.nnormals * 4, cudaMemcpyDeviceToHost, ctx->stream));
+        if (hk) KVSMC_CUDA(ctx, cudaMemcpyAsync(hk, it->d_conn, s.nconnections * 4, cudaMemcpyDeviceToHost, ctx->stream));
+    }
+    KVSMC_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    return KVSMC_OK;
+}
+
+kvsmc_status kvsmc_extract_batch_host(kvsmc_context* ctx, const void* host, kvsmc_dtype dtype, uint32_t nx,
+                                      uint32_t ny, uint32_t nz, const kvsmc_params* params, int32_t n,
+                                      kvsmc_host_alloc_fn alloc, void* user, kvsmc_sizes* sizes)
+{
+    kvsmc_status st = use_device(ctx);
+    if (st) return st;
+    if (!host || (!params && n) || !alloc || (!sizes && n) || n < 0) return fail(ctx, KVSMC_ERR_INVALID_ARGUMENT, "null pointer");
+    if ((st = check_shape(ctx, dtype, nx, ny, nz))) return st;
+    if (!ctx->host_vol) ctx->host_vol = new kvsmc_volume();
+    kvsmc_volume* v = ctx->host_vol;
+    if ((st = volume_alloc(ctx, dtype, nx, ny, nz, v))) return st;
+    if ((st = volume_copy_in(ctx, v, host, cudaMemcpyHostToDevice))) return st;
+    std::vector<Item> items((size_t)n);
+    std::vector<Item*> s_items, g_items;
+    kvsmc_status first = KVSMC_OK;
+    for (int32_t i = 0; i < n; ++i) {
+        items[i].vol = v;
+        items[i].params = params[i];
+        items[i].status = prepare(ctx, items[i]);
+        if (items[i].status) { if (!first) first = items[i].status; continue; }
+        if (!items[i].extracted) continue;
+        (stream_eligible(ctx, items[i]) ? s_items : g_items).push_back(&items[i]);
+    }
+    if (!s_items.empty()) {
+        StreamBatch b;
+        b.ctx = ctx;
+        b.items = s_items;
+        if ((st = b.plan()) || (st = b.count()) || (st = arena_outputs(ctx, s_items)) || (st = b.emit()) ||
+            (st = b.finish()) || (st = copy_back(ctx, s_items, items.data(), alloc, user))) {
+            for (Item* it : s_items) it->status = st;
+            if (!first) first = st;
+        }
+    }
+    for (Item* it : g_items) {
+        Plan pl;
+        gather_plan(*it, pl);
+        st = gather_count(ctx, pl);
+        if (!st) {
+            gather_sizes(pl, *it, &it->sizes);
+            std::vector<Item*> one{it};
+            if (!(st = arena_outputs(ctx, one)) && !(st = gather_emit(ctx, pl, it->d_coords, it->d_normals, it->d_conn)))
+                st = copy_back(ctx, one, items.data(), alloc, user);
+        }
+        if (st) { it->status = st; if (!first) first = st; }
+    }
+    for (int32_t i = 0; i < n; ++i) sizes[i] = items[i].sizes;
+    return first;
+}
+
+static kvsmc_status batch_items(kvsmc_context* ctx, kvsmc_request* reqs, int32_t n, bool emit)
+{
+    std::vector<Item> items((size_t)n);
+    std::vector<Item*> ptrs;
+    for (int32_t i = 0; i < n; ++i) {
+        Item& it = items[i];
+        it.vol = reqs[i].volume;
+        it.params = reqs[i].params;
+        it.d_coords = reqs[i].d_coords; it.coords_cap = reqs[i].coords_capacity;
+        it.d_normals = reqs[i].d_normals; it.normals_cap = reqs[i].normals_capacity;
+        it.d_conn = reqs[i].d_connections; it.conn_cap = reqs[i].connections_capacity;
+        it.status = prepare(ctx, it);
+        ptrs.push_back(&it);
+    }
+    kvsmc_status first = run_items(ctx, ptrs, emit);
+    for (int32_t i = 0; i < n; ++i) {
+        reqs[i].sizes = items[i].sizes;
+        reqs[i].status = items[i].status;
+        if (items[i].status && !first) first = items[i].status;
+    }
+    return first;
 }
 
 kvsmc_status kvsmc_count_batch(kvsmc_context* ctx, kvsmc_request* reqs, int32_t n)
 {
     kvsmc_status st = use_device(ctx);
     if (st) return st;
-    if (!reqs || n < 0) return fail(ctx, KVSMC_ERR_INVALID_ARGUMENT, "bad batch");
-    kvsmc_status first = KVSMC_OK;
-    for (int32_t i = 0; i < n; ++i) {
-        reqs[i].status = kvsmc_count(ctx, reqs[i].volume, &reqs[i].params, &reqs[i].sizes);
-        if (reqs[i].status && !first) first = reqs[i].status;
-    }
-    return first;
+    if ((!reqs && n) || n < 0) return fail(ctx, KVSMC_ERR_INVALID_ARGUMENT, "bad batch");
+    return batch_items(ctx, reqs, n, false);
 }
 
 kvsmc_status kvsmc_extract_batch(kvsmc_context* ctx, kvsmc_request* reqs, int32_t n)
 {
     kvsmc_status st = use_device(ctx);
     if (st) return st;
-    if (!reqs || n < 0) return fail(ctx, KVSMC_ERR_INVALID_ARGUMENT, "bad batch");
-    kvsmc_status first = KVSMC_OK;
-    for (int32_t i = 0; i < n; ++i) {
-        kvsmc_request& r = reqs[i];
-        r.status = kvsmc_extract_device(ctx, r.volume, &r.params, r.d_coords, r.coords_capacity, r.d_normals,
-                                        r.normals_capacity, r.d_connections, r.connections_capacity, &r.sizes);
-        if (r.status && !first) first = r.status;
-    }
-    return first;
+    if ((!reqs && n) || n < 0) return fail(ctx, KVSMC_ERR_INVALID_ARGUMENT, "bad batch");
+    return batch_items(ctx, reqs, n, true);
+}
+
+kvsmc_status kvsmc_selftest_interpolation(kvsmc_context* ctx, uint64_t n, uint64_t seed, uint64_t* tested,
+                                          uint64_t* mismatches, uint64_t* fallbacks)
+{
+    kvsmc_status st = use_device(ctx);
+    if (st) return st;
+    if ((st = ensure_scratch(ctx, 256))) return st;
+    unsigned long long* d = static_cast<unsigned long long*>(ctx->scratch);
+    KVSMC_CUDA(ctx, cudaMemsetAsync(d, 0, 3 * sizeof(unsigned long long), ctx->stream));
+    KVSMC_CUDA(ctx, launch_selftest(n, seed, d, launch_of(ctx)));
+    KVSMC_CUDA(ctx, cudaMemcpyAsync(ctx->h_small, d, 3 * sizeof(unsigned long long), cudaMemcpyDeviceToHost, ctx->stream));
+    KVSMC_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    if (tested) *tested = ctx->h_small[0];
+    if (mismatches) *mismatches = ctx->h_small[1];
+    if (fallbacks) *fallbacks = ctx->h_small[2];
+    return KVSMC_OK;
 }
 
 }  // extern "C"

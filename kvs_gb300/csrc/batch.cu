@@ -1,0 +1,266 @@
+// batch.cu -- planning and launching of the streaming kernels for a batch of
+// (volume, isolevel) requests: one count launch and one emit launch per
+// value type present, whatever the number of volumes and isolevels.
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <map>
+
+#include "batch.h"
+
+namespace kvsmc_host {
+
+using kvsmc::StreamGroup;
+using kvsmc::StreamIso;
+
+namespace {
+
+bool stream_dtype(int dt) { return dt == KVSMC_I8 || dt == KVSMC_I16 || dt == KVSMC_U8 || dt == KVSMC_U16 || dt == KVSMC_F32; }
+
+void tiling(const kvsmc::VolumeView& v, uint32_t& wpr, uint32_t& rows, uint64_t& plane_elems)
+{
+    const uint32_t cx = v.nx - 1;
+    wpr = (cx + kvsmc::kStreamSegCells - 1) / kvsmc::kStreamSegCells;
+    rows = (kvsmc::kStreamThreads / 32) / (wpr ? wpr : 1);
+    if (rows < 1) rows = 1;
+    if (rows > v.ny - 1) rows = v.ny - 1;
+    const uint64_t need = std::max<uint64_t>((uint64_t)(rows + 1) * v.pitch,
+                                             (uint64_t)rows * v.pitch + (uint64_t)wpr * kvsmc::kStreamSegCells + 16);
+    const uint64_t quantum = 128 / kvsmc::dtype_size(v.dtype);
+    plane_elems = (need + quantum - 1) / quantum * quantum;
+}
+
+}  // namespace
+
+// FP32 fast-path constants of one request (see mc_interp.cuh).
+kvsmc::FastIso make_fast(double iso, double vmin, double vmax, int dtype)
+{
+    kvsmc::FastIso f;
+    std::memset(&f, 0, sizeof f);
+    const kvsmc::Classifier c = make_classifier(iso);
+    if (dtype == KVSMC_F32) {
+        f.f_thr = c.f_thr;
+    } else {
+        // integer data: v > floor(iso) <=> float(v) > float(floor(iso)), |v| < 2^16
+        long long t = c.i_thr;
+        if (t > (1LL << 24)) t = 1LL << 24;
+        if (t < -(1LL << 24)) t = -(1LL << 24);
+        f.f_thr = (float)t;
+    }
+    f.ih = (float)iso;
+    f.il = (float)(iso - (double)f.ih);
+    const double rep = std::fabs(iso - ((double)f.ih + (double)f.il));
+    float err = (float)rep;
+    if ((double)err < rep) err = std::nextafter(err, INFINITY);
+    f.iso_err = err;
+    f.vmin_f = (float)vmin;
+    f.vmax_f = (float)vmax;
+    const double lim = 1.152921504606846976e18;  // 2^60
+    f.fast_ok = std::isfinite(iso) && std::fabs(iso) <= lim && std::isfinite(vmin) && std::isfinite(vmax) &&
+                std::fabs(vmin) <= lim && std::fabs(vmax) <= lim && (double)f.vmin_f == vmin &&
+                (double)f.vmax_f == vmax && std::isfinite(f.ih) && std::isfinite(f.il);
+    return f;
+}
+
+bool stream_eligible(const kvsmc_context* ctx, const Item& it)
+{
+    if (ctx->path != 0 || !it.vol) return false;
+    if (it.params.mode != KVSMC_DUP_POLYGON_NORMAL) return false;
+    const kvsmc::VolumeView& v = it.vol->view;
+    if (!stream_dtype(v.dtype)) return false;
+    if (v.nx < 2 || v.ny < 2 || v.nz < 2) return false;
+    if (v.nx - 1 > (uint32_t)(kvsmc::kStreamMaxWarpsPerRow * kvsmc::kStreamSegCells)) return false;
+    const double iso = it.params.isolevel;
+    if (!std::isfinite(iso) || std::fabs(iso) > 1.0e30) return false;
+    uint32_t wpr, rows;
+    uint64_t pe;
+    tiling(v, wpr, rows, pe);
+    const size_t smem = kvsmc::stream_shared_bytes(pe * kvsmc::dtype_size(v.dtype), true);
+    return smem <= (size_t)227 * 1024;
+}
+
+kvsmc_status StreamBatch::plan()
+{
+    // group by volume in request order, at most kStreamMaxIso per group
+    std::vector<std::vector<Item*>> lists;
+    std::map<kvsmc_volume*, size_t> open;
+    for (Item* it : items) {
+        auto f = open.find(it->vol);
+        if (f == open.end() || lists[f->second].size() == (size_t)kvsmc::kStreamMaxIso) {
+            open[it->vol] = lists.size();
+            lists.push_back({});
+            f = open.find(it->vol);
+        }
+        lists[f->second].push_back(it);
+    }
+    // launches by value type
+    std::vector<int> dtypes;
+    for (auto& l : lists)
+        if (std::find(dtypes.begin(), dtypes.end(), l[0]->vol->view.dtype) == dtypes.end())
+            dtypes.push_back(l[0]->vol->view.dtype);
+    groups.clear();
+    isos.clear();
+    iso_item.clear();
+    launches.clear();
+    uint64_t tiles = 0;
+    for (int dt : dtypes) {
+        Launch1 L;
+        L.dtype = dt;
+        L.g0 = (int)groups.size();
+        L.nctas = 0;
+        size_t max_plane = 0;
+        for (auto& l : lists) {
+            if (l[0]->vol->view.dtype != dt) continue;
+            kvsmc::VolumeView v = l[0]->vol->view;
+            StreamGroup g;
+            std::memset(&g, 0, sizeof g);
+            g.vol = v;
+            tiling(v, g.wpr, g.rows, g.plane_elems);
+            const uint32_t cy = v.ny - 1, cz = v.nz - 1;
+            g.ytiles = (cy + g.rows - 1) / g.rows;
+            const uint32_t want = std::max<uint32_t>(1, (uint32_t)(2 * ctx->num_sms + g.ytiles - 1) / g.ytiles);
+            uint32_t zc = (cz + want - 1) / want;
+            zc = std::min<uint32_t>(std::max<uint32_t>(zc, 4), 32);
+            g.zchunk = zc;
+            const uint32_t zchunks = (cz + zc - 1) / zc;
+            g.cta_begin = L.nctas;
+            L.nctas += g.ytiles * zchunks;
+            max_plane = std::max(max_plane, (size_t)g.plane_elems * kvsmc::dtype_size(dt));
+            // isolevels sorted by threshold
+            std::vector<std::pair<float, Item*>> sorted;
+            for (Item* it : l) {
+                const kvsmc::FastIso f = make_fast(it->params.isolevel, it->vmin, it->vmax, dt);
+                sorted.push_back({f.f_thr, it});
+            }
+            std::stable_sort(sorted.begin(), sorted.end(),
+                             [](const std::pair<float, Item*>& a, const std::pair<float, Item*>& b) { return a.first < b.first; });
+            g.iso_begin = (int32_t)isos.size();
+            g.niso = (int32_t)sorted.size();
+            const float t0 = sorted.front().first, t1 = sorted.back().first;
+            const float span = t1 - t0;
+            g.bt0 = t0;
+            g.bscale = (span > 0.0f && std::isfinite(span)) ? (float)kvsmc::kStreamBuckets / span
+                                                           : 1.0f / (1.0f + std::fabs(t0));
+            if (!(g.bscale > 0.0f) || !std::isfinite(g.bscale)) g.bscale = 1.0f;
+            const uint64_t tiles_per_iso = (uint64_t)cz * g.ytiles;
+            for (auto& pr : sorted) {
+                Item* it = pr.second;
+                StreamIso s;
+                std::memset(&s, 0, sizeof s);
+                s.f = make_fast(it->params.isolevel, it->vmin, it->vmax, dt);
+                s.ip.iso = it->params.isolevel;
+                s.ip.vmin = it->vmin;
+                s.ip.vmax = it->vmax;
+                for (int k = 0; k < 3; ++k) { s.ip.min_coord[k] = it->params.min_coord[k]; s.ip.scale[k] = it->params.scale[k]; }
+                s.count_base = tiles;
+                tiles += tiles_per_iso;
+                isos.push_back(s);
+                iso_item.push_back(it);
+            }
+            groups.push_back(g);
+        }
+        L.ng = (int)groups.size() - L.g0;
+        L.smem_count = kvsmc::stream_shared_bytes(max_plane, false);
+        L.smem_emit = kvsmc::stream_shared_bytes(max_plane, true);
+        launches.push_back(L);
+    }
+    total_tiles = tiles;
+
+    // device scratch
+    const size_t niso = isos.size();
+    const size_t need = 16 * 256 + align_up(groups.size() * sizeof(StreamGroup), 256) +
+                        align_up(niso * sizeof(StreamIso), 256) + align_up(tiles * 4, 256) +
+                        align_up(tiles * 8, 256) + align_up(kvsmc::scan_scratch_bytes(tiles), 256) +
+                        align_up(niso * 8, 256) + 4 * 256;
+    kvsmc_status st = ensure_scratch(ctx, need);
+    if (st) return st;
+    Carve cv{static_cast<char*>(ctx->scratch)};
+    d_groups = cv.take<StreamGroup>(groups.size() * sizeof(StreamGroup));
+    d_isos = cv.take<StreamIso>(niso * sizeof(StreamIso));
+    d_counts = cv.take<uint32_t>(tiles * 4);
+    d_offsets = cv.take<uint64_t>(tiles * 8);
+    d_scan = cv.take<char>(kvsmc::scan_scratch_bytes(tiles));
+    d_totals = cv.take<uint64_t>(niso * 8);
+    d_total = cv.take<uint64_t>(256);
+    d_status = cv.take<int>(256);
+    return upload_tables();
+}
+
+kvsmc_status StreamBatch::upload_tables()
+{
+    const size_t bg = groups.size() * sizeof(StreamGroup), bi = isos.size() * sizeof(StreamIso);
+    kvsmc_status st = ensure_stage(ctx, bg + bi + 64);
+    if (st) return st;
+    char* h = static_cast<char*>(ctx->h_stage);
+    std::memcpy(h, groups.data(), bg);
+    std::memcpy(h + bg, isos.data(), bi);
+    KVSMC_CUDA(ctx, cudaMemcpyAsync(d_groups, h, bg, cudaMemcpyHostToDevice, ctx->stream));
+    KVSMC_CUDA(ctx, cudaMemcpyAsync(d_isos, h + bg, bi, cudaMemcpyHostToDevice, ctx->stream));
+    return KVSMC_OK;
+}
+
+kvsmc_status StreamBatch::count()
+{
+    const kvsmc::Launch L = launch_of(ctx);
+    KVSMC_CUDA(ctx, cudaMemsetAsync(d_status, 0, sizeof(int), ctx->stream));
+    for (const Launch1& l : launches)
+        KVSMC_CUDA(ctx, kvsmc::launch_stream(false, l.dtype, d_groups + l.g0, l.ng, l.nctas, l.smem_count, d_isos,
+                                             d_counts, d_offsets, d_status, L));
+    KVSMC_CUDA(ctx, kvsmc::launch_scan(d_counts, d_offsets, total_tiles, d_scan, d_total, L));
+    KVSMC_CUDA(ctx, kvsmc::launch_iso_totals(d_isos, (int)isos.size(), d_offsets, d_total, d_totals, L));
+    // read back: status word, then one total per isolevel
+    const size_t n = isos.size();
+    kvsmc_status st = ensure_stage(ctx, (n + 2) * 8);
+    if (st) return st;
+    uint64_t* h = static_cast<uint64_t*>(ctx->h_stage);
+    KVSMC_CUDA(ctx, cudaMemcpyAsync(h, d_status, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
+    KVSMC_CUDA(ctx, cudaMemcpyAsync(h + 1, d_totals, n * 8, cudaMemcpyDeviceToHost, ctx->stream));
+    KVSMC_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    int status;
+    std::memcpy(&status, h, sizeof(int));
+    if (status) return fail(ctx, KVSMC_ERR_TIMEOUT, "streaming count: a shared-memory load did not complete");
+    for (size_t i = 0; i < n; ++i) {
+        Item* it = iso_item[i];
+        const uint64_t t = h[1 + i];
+        std::memset(&it->sizes, 0, sizeof it->sizes);
+        it->sizes.ntriangles = t;
+        it->sizes.nvertices = 3 * t;
+        it->sizes.ncoords = 9 * t;
+        it->sizes.nnormals = 3 * t;
+        it->sizes.min_value = it->vmin;
+        it->sizes.max_value = it->vmax;
+        it->sizes.extracted = 1;
+    }
+    return KVSMC_OK;
+}
+
+kvsmc_status StreamBatch::emit()
+{
+    bool any = false;
+    for (size_t i = 0; i < isos.size(); ++i) {
+        Item* it = iso_item[i];
+        const bool ok = it->emit && it->status == KVSMC_OK && it->sizes.ntriangles > 0;
+        isos[i].coords = ok ? it->d_coords : nullptr;
+        isos[i].normals = ok ? it->d_normals : nullptr;
+        any = any || ok;
+    }
+    if (!any) return KVSMC_OK;
+    kvsmc_status st = upload_tables();
+    if (st) return st;
+    const kvsmc::Launch L = launch_of(ctx);
+    for (const Launch1& l : launches)
+        KVSMC_CUDA(ctx, kvsmc::launch_stream(true, l.dtype, d_groups + l.g0, l.ng, l.nctas, l.smem_emit, d_isos,
+                                             nullptr, d_offsets, d_status, L));
+    return KVSMC_OK;
+}
+
+kvsmc_status StreamBatch::finish()
+{
+    int* h = static_cast<int*>(ctx->h_stage);
+    KVSMC_CUDA(ctx, cudaMemcpyAsync(h, d_status, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
+    KVSMC_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    if (*h) return fail(ctx, KVSMC_ERR_TIMEOUT, "streaming emit: a shared-memory load did not complete");
+    return KVSMC_OK;
+}
+
+}  // namespace kvsmc_host

@@ -1,0 +1,100 @@
+// context.h -- host-side state of libkvsmc shared by api.cu and batch.cu.
+#pragma once
+#include <cstdint>
+#include <string>
+#include <vector>
+
+#include "../../include/kvsmc.h"
+#include "mc_internal.h"
+
+struct kvsmc_volume {
+    kvsmc::VolumeView view;
+    void* dev = nullptr;        // owned device allocation
+    size_t bytes = 0;
+    bool has_minmax = false;
+    double vmin = 0.0, vmax = 0.0;
+};
+
+struct kvsmc_context {
+    int device = 0;
+    int num_sms = 0;
+    cudaStream_t own_stream = nullptr;
+    cudaStream_t stream = nullptr;
+    void* scratch = nullptr;     // grow-only device arena for per-call intermediates
+    size_t scratch_bytes = 0;
+    void* out_arena = nullptr;   // grow-only device outputs of the host call
+    size_t out_bytes = 0;
+    kvsmc_volume* host_vol = nullptr;  // staging volume of the host call
+    uint64_t* h_small = nullptr; // pinned: small read-backs (totals, min/max, status)
+    void* h_stage = nullptr;     // pinned: staging of work tables sent to the device
+    size_t h_stage_bytes = 0;
+    uint64_t launches = 0;
+    int path = 0;                // 0: streaming kernels where eligible, 1: gather kernels only
+    kvsmc::Profiler* prof = nullptr;
+    std::string last_error;
+};
+
+namespace kvsmc {
+Profiler* profiler_create();
+void profiler_destroy(Profiler* p);
+}  // namespace kvsmc
+
+namespace kvsmc_host {
+
+kvsmc_status fail(kvsmc_context* ctx, kvsmc_status st, const char* fmt, ...);
+inline size_t align_up(size_t v, size_t a) { return (v + a - 1) / a * a; }
+inline kvsmc::Launch launch_of(kvsmc_context* ctx)
+{
+    return kvsmc::Launch{ctx->stream, ctx->num_sms, &ctx->launches, ctx->prof};
+}
+kvsmc_status ensure_scratch(kvsmc_context* ctx, size_t bytes);
+kvsmc_status ensure_stage(kvsmc_context* ctx, size_t bytes);
+kvsmc_status volume_minmax(kvsmc_context* ctx, kvsmc_volume* v);
+bool equal_ref(double a, double b);
+kvsmc::Classifier make_classifier(double iso);
+
+// Bump allocator over an arena (256-byte aligned pieces).
+struct Carve {
+    char* base;
+    size_t off = 0;
+    template <typename P> P* take(size_t bytes)
+    {
+        P* p = reinterpret_cast<P*>(base + off);
+        off = align_up(off + bytes, 256);
+        return p;
+    }
+};
+
+// One request of a batch after host-side planning.
+struct Item {
+    kvsmc_volume* vol = nullptr;
+    kvsmc_params params{};
+    double vmin = 0, vmax = 0;
+    bool extracted = true;
+    float* d_coords = nullptr;
+    uint64_t coords_cap = 0;
+    float* d_normals = nullptr;
+    uint64_t normals_cap = 0;
+    uint32_t* d_conn = nullptr;
+    uint64_t conn_cap = 0;
+    bool emit = false;           // write outputs (false: count only)
+    kvsmc_sizes sizes{};
+    kvsmc_status status = KVSMC_OK;
+};
+
+// Requests the streaming kernels can take (duplicated mode, 8/16-bit and
+// float32 data, finite isolevel, width <= 4096 cells).
+bool stream_eligible(const kvsmc_context* ctx, const Item& it);
+// Count (and, for items with emit set, emit) all eligible items together.
+kvsmc_status stream_run(kvsmc_context* ctx, std::vector<Item*>& items);
+
+}  // namespace kvsmc_host
+
+#define KVSMC_CUDA(ctx, call)                                                                              \
+    do {                                                                                                   \
+        cudaError_t e_ = (call);                                                                           \
+        if (e_ != cudaSuccess)                                                                             \
+            return kvsmc_host::fail(ctx, e_ == cudaErrorMemoryAllocation ? KVSMC_ERR_OUT_OF_MEMORY         \
+                                                                         : KVSMC_ERR_CUDA,                 \
+                                    "%s: %s (%s:%d)", #call, cudaGetErrorString(e_), __FILE__, __LINE__); \
+    } while (0)

@@ -93,6 +93,20 @@ def render(tri_rows, vert_rows):
     out.append("}")
     out.append("static const uint64_t MC_TRI_PACKED[256] = MC_TRI_PACKED_INIT;")
     out.append("")
+    out.append("/* case -> bit mask of the edges its triangles use */")
+    masks = []
+    for r in tri_rows:
+        m = 0
+        for t in range(ntri(r)):
+            for e in r[3 * t:3 * t + 3]:
+                m |= 1 << e
+        masks.append(m)
+    out.append("#define MC_EDGE_MASK_INIT { \\")
+    for i in range(0, 256, 16):
+        out.append("    " + ", ".join("0x%03x" % v for v in masks[i:i + 16]) + ", \\")
+    out.append("}")
+    out.append("static const unsigned short MC_EDGE_MASK[256] = MC_EDGE_MASK_INIT;")
+    out.append("")
     # edge -> packed endpoints: bits 0-2 start corner (x,y,z), bits 3-5 end corner
     out.append("/* edge -> start offset bits (x | y<<1 | z<<2) in bits 0..2, end offset in bits 3..5 */")
     ep = []

@@ -39,13 +39,19 @@ struct Classifier {
     long long i_thr;
 };
 
+// Constants of the FP64 interpolation sequence of one request.
+struct Interp {
+    double iso;
+    double vmin, vmax;      // clamp range (volume min/max or preset)
+    float min_coord[3];     // volume->minObjectCoord()
+    float scale[3];         // (max_coord - min_coord) / ncells
+};
+
 // One extraction request as the kernels see it.
 struct Job {
     VolumeView vol;
     Classifier cls;
-    double vmin, vmax;      // clamp range (volume min/max or preset)
-    float min_coord[3];
-    float scale[3];
+    Interp ip;
     int32_t mode;
     uint32_t cell_rows;     // cell rows (y) per cell tile
     uint32_t cell_ytiles;   // ceil((ny-1)/cell_rows)
@@ -150,13 +156,13 @@ __device__ __forceinline__ double clamp_ref(double a, double lo, double hi)
 // interpolate_vertex<T> (MarchingCubes.cpp:327-356) then the (p + min) * scale
 // lambda (:168-173).  a/b are the edge endpoints in the table's direction,
 // va/vb their values.  Exact FP64 sequence, no contraction.
-__device__ __forceinline__ float3 interpolate_exact(const Job& j, double va, double vb,
+__device__ __forceinline__ float3 interpolate_exact(const Interp& j, double va, double vb,
                                                     float ax, float ay, float az,
                                                     float bx, float by, float bz)
 {
     const double v0 = clamp_ref(va, j.vmin, j.vmax);
     const double v1 = clamp_ref(vb, j.vmin, j.vmax);
-    const double q = __ddiv_rn(__dsub_rn(j.cls.iso, v0), __dsub_rn(v1, v0));
+    const double q = __ddiv_rn(__dsub_rn(j.iso, v0), __dsub_rn(v1, v0));
     const double r = (q < 0.0) ? -q : q;            // kvs::Math::Abs
     const double s = __dsub_rn(1.0, r);
     const double px = __dadd_rn(__dmul_rn(s, (double)ax), __dmul_rn(r, (double)bx));
@@ -181,7 +187,7 @@ __device__ __forceinline__ float3 cell_edge_vertex(const Job& j, const T* vol, c
     const uint32_t bx = x + (b & 1u), by = y + ((b >> 1) & 1u), bz = z + (b >> 2);
     const double va = to_double(load(vol, node_index<T>(j.vol, ax, ay, az)));
     const double vb = to_double(load(vol, node_index<T>(j.vol, bx, by, bz)));
-    return interpolate_exact(j, va, vb, __uint2float_rn(ax), __uint2float_rn(ay), __uint2float_rn(az),
+    return interpolate_exact(j.ip, va, vb, __uint2float_rn(ax), __uint2float_rn(ay), __uint2float_rn(az),
                              __uint2float_rn(bx), __uint2float_rn(by), __uint2float_rn(bz));
 }
 

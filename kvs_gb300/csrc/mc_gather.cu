@@ -260,7 +260,7 @@ __device__ __forceinline__ float3 node_edge_vertex(const Job& j, const T* vol, u
     const double va = to_double(load(vol, i0));
     const double vb = to_double(load(vol, i0 + step));
     const float fx = __uint2float_rn(x), fy = __uint2float_rn(y), fz = __uint2float_rn(z);
-    return interpolate_exact(j, va, vb, fx, fy, fz,
+    return interpolate_exact(j.ip, va, vb, fx, fy, fz,
                              axis == 0 ? __uint2float_rn(x + 1) : fx,
                              axis == 1 ? __uint2float_rn(y + 1) : fy,
                              axis == 2 ? __uint2float_rn(z + 1) : fz);
@@ -566,11 +566,13 @@ size_t minmax_scratch_bytes(int num_sms)
 cudaError_t launch_minmax(const VolumeView& v, void* scratch, double* d_out, const Launch& L)
 {
     const int nb = minmax_blocks(L.num_sms);
+    prof_begin(L, "minmax");
     KVSMC_DTYPE_SWITCH(v.dtype, {
         MinMax<T>* part = static_cast<MinMax<T>*>(scratch);
         k_minmax_partial<T><<<nb, 256, 0, L.stream>>>(v, part);
         k_minmax_final<T><<<1, 256, 0, L.stream>>>(v, part, nb, d_out);
     });
+    prof_end(L);
     *L.counter += 2;
     return cudaGetLastError();
 }
@@ -587,51 +589,65 @@ cudaError_t launch_scan(const uint32_t* counts, uint64_t* offsets, uint64_t n, v
     uint64_t nb = (n + kScanTile - 1) / kScanTile;
     if (nb == 0) nb = 1;
     uint64_t* bs = static_cast<uint64_t*>(scratch);
+    prof_begin(L, "scan");
     k_scan_reduce<<<(unsigned)nb, kScanThreads, 0, L.stream>>>(counts, n, bs);
     k_scan_top<<<1, kScanThreads, 0, L.stream>>>(bs, nb, d_total);
     k_scan_down<<<(unsigned)nb, kScanThreads, 0, L.stream>>>(counts, n, bs, offsets);
+    prof_end(L);
     *L.counter += 3;
     return cudaGetLastError();
 }
 
 cudaError_t launch_cell_count(const Job& j, const Launch& L)
 {
+    prof_begin(L, "gather_cell_count");
     KVSMC_DTYPE_SWITCH(j.vol.dtype, { k_cell_count<T><<<grid_for(j.cell_tiles, L), kThreads, 0, L.stream>>>(j); });
+    prof_end(L);
     *L.counter += 1;
     return cudaGetLastError();
 }
 
 cudaError_t launch_emit_dup(const Job& j, const Launch& L)
 {
+    prof_begin(L, "gather_emit_dup");
     KVSMC_DTYPE_SWITCH(j.vol.dtype, { k_emit_dup<T><<<grid_for(j.cell_tiles, L), kThreads, 0, L.stream>>>(j); });
+    prof_end(L);
     *L.counter += 1;
     return cudaGetLastError();
 }
 
 cudaError_t launch_node_count(const Job& j, const Launch& L)
 {
+    prof_begin(L, "gather_node_count");
     KVSMC_DTYPE_SWITCH(j.vol.dtype, { k_node_count<T><<<grid_for(j.node_tiles, L), kThreads, 0, L.stream>>>(j); });
+    prof_end(L);
     *L.counter += 1;
     return cudaGetLastError();
 }
 
 cudaError_t launch_node_emit(const Job& j, const Launch& L)
 {
+    prof_begin(L, "gather_node_emit");
     KVSMC_DTYPE_SWITCH(j.vol.dtype, { k_node_emit<T><<<grid_for(j.node_tiles, L), kThreads, 0, L.stream>>>(j); });
+    prof_end(L);
     *L.counter += 1;
     return cudaGetLastError();
 }
 
 cudaError_t launch_connect(const Job& j, const Launch& L)
 {
+    prof_begin(L, "gather_connect");
     KVSMC_DTYPE_SWITCH(j.vol.dtype, { k_connect<T><<<grid_for(j.cell_tiles, L), kThreads, 0, L.stream>>>(j); });
+    prof_end(L);
     *L.counter += 1;
     return cudaGetLastError();
 }
 
 cudaError_t launch_vertex_normals(const Job& j, const Launch& L)
 {
+    prof_begin(L, "gather_vertex_normals");
     KVSMC_DTYPE_SWITCH(j.vol.dtype, { k_vertex_normals<T><<<grid_for(j.node_tiles, L), kThreads, 0, L.stream>>>(j); });
+    prof_end(L);
     *L.counter += 1;
     return cudaGetLastError();
 }

@@ -4,15 +4,23 @@
 #include <cuda_runtime.h>
 
 #include "mc_device.cuh"
+#include "mc_interp.cuh"
 
 namespace kvsmc {
+
+struct Profiler;
 
 // Launch bookkeeping passed to every launcher.
 struct Launch {
     cudaStream_t stream;
     int num_sms;
     uint64_t* counter;   // incremented once per kernel launch
+    Profiler* prof;      // per-kernel CUDA-event timing when enabled (may be null)
 };
+
+// CUDA events on the launching stream around one kernel family's launch.
+void prof_begin(const Launch& L, const char* name);
+void prof_end(const Launch& L);
 
 // Size in bytes of one value of a dtype code (0 if unknown).
 size_t dtype_size(int dtype);
@@ -27,12 +35,51 @@ size_t scan_scratch_bytes(uint64_t n);
 cudaError_t launch_scan(const uint32_t* counts, uint64_t* offsets, uint64_t n, void* scratch,
                         uint64_t* d_total, const Launch& L);
 
-// ---- gather-form kernels (mc_gather.cu)
+// ---- gather-form kernels (mc_gather.cu): every mode and dtype
 cudaError_t launch_cell_count(const Job& j, const Launch& L);
 cudaError_t launch_emit_dup(const Job& j, const Launch& L);
 cudaError_t launch_node_count(const Job& j, const Launch& L);
 cudaError_t launch_node_emit(const Job& j, const Launch& L);
 cudaError_t launch_connect(const Job& j, const Launch& L);
 cudaError_t launch_vertex_normals(const Job& j, const Launch& L);
+
+// ---- streaming kernels (mc_stream.cu): duplicated mode, batched
+constexpr int kStreamThreads = 512;   // 16 warps
+constexpr int kStreamMaxIso = 16;     // isolevels of one volume per group
+constexpr int kStreamBuckets = 256;   // threshold lookup buckets
+constexpr int kStreamSegCells = 256;  // cells per warp segment
+constexpr int kStreamMaxWarpsPerRow = 16;
+
+// One isolevel request inside a streaming launch.
+struct StreamIso {
+    FastIso f;
+    Interp ip;
+    uint64_t count_base;   // first slot of its tiles in the concatenated count/offset arrays
+    float* coords;         // outputs (null: not written)
+    float* normals;
+};
+
+// One volume with up to kStreamMaxIso isolevels, sorted by threshold.
+struct StreamGroup {
+    VolumeView vol;
+    int32_t iso_begin, niso;
+    uint32_t wpr;          // warps (256-cell segments) per cell row
+    uint32_t rows;         // cell rows per y-tile
+    uint32_t ytiles;
+    uint32_t zchunk;       // cell planes per CTA
+    uint32_t cta_begin;    // first CTA of this group in its launch
+    float bt0, bscale;     // bucket(v) = clamp(floor((v - bt0) * bscale), -1, kStreamBuckets + 1)
+    uint64_t plane_elems;  // elements per staged node plane (rows+1 rows + slack)
+};
+
+size_t stream_shared_bytes(size_t plane_bytes, bool emit);
+cudaError_t launch_stream(bool emit, int dtype, const StreamGroup* d_groups, int ngroups, uint32_t nctas,
+                          size_t smem_bytes, const StreamIso* d_isos, uint32_t* d_counts, const uint64_t* d_offsets,
+                          int* d_status, const Launch& L);
+cudaError_t launch_iso_totals(const StreamIso* d_isos, int n, const uint64_t* d_offsets, const uint64_t* d_total,
+                              uint64_t* d_totals, const Launch& L);
+
+// ---- diagnostics (selftest.cu)
+cudaError_t launch_selftest(uint64_t n, uint64_t seed, unsigned long long* d_counters, const Launch& L);
 
 }  // namespace kvsmc

@@ -1,0 +1,159 @@
+// mc_interp.cuh -- exact edge interpolation without FP64 on the common path.
+//
+// The reference interpolates in FP64 and rounds to float
+// (interpolate_vertex<T>, MarchingCubes.cpp:327-356):
+//     r = |RN64(RN64(iso - v0) / RN64(v1 - v0))|,  X = RN64(RN64(RN64(1-r)*a) + RN64(r*b))
+//     F = RN32(X)
+// GB300 runs FP64 at 1/58 of the FP32 rate (measured: 0.63 T DFMA/s, 61 G DDIV/s),
+// so the kernels compute F with FP32 "double-float" arithmetic (Knuth's
+// TwoSum, Dekker's product via FMA, one Newton correction for the quotient:
+// the classic error-free transformations) and a rigorous error bound E, and
+// accept the FP32 answer only when no float rounding boundary lies within E
+// of it.  Otherwise (about one vertex in 10^6) they run the exact FP64
+// sequence.  Either way the float bits equal the reference's.
+//
+// Why it is exact (a, b = edge endpoint coordinates, integers < 2^24;
+// v0, v1 = clamped endpoint values, exactly representable as float):
+//  * The endpoints straddle the isolevel in the reference's double test, so
+//    RN64(iso - v0) and RN64(v1 - v0) have equal signs and |num| <= |den|:
+//    r lies in [0, 1].
+//  * Constant axes (a == b == c): (1-r)*c + r*c evaluated in FP64 is within
+//    3*2^-53 |c| of c, so RN32 gives c exactly.  No work is needed.
+//  * Varying axis (b = a +- 1): with R = (iso - v0)/(v1 - v0) in exact
+//    arithmetic, |X - (a + (b-a) R)| <= 2^-51 (max(|a|,|b|) + 1)   (E_D).
+//    The double-float Y approximates a + (b-a) R within
+//        E_Y = 2^-40 |q| + err(num)/|den| + 2^-23 |y_lo|
+//    (the quotient error is below 26 u^2 |R| < 2^-43 |R|, u = 2^-24; the
+//    bound keeps a factor 8 of slack).  If every real in [Y - E, Y + E],
+//    E = E_Y + E_D, rounds to the same float, that float is RN32(X) = F.
+#pragma once
+#include <cstdint>
+#include <cuda_runtime.h>
+
+#include "mc_device.cuh"
+
+namespace kvsmc {
+
+// Per-request constants of the fast path (computed on the host).
+struct FastIso {
+    float ih, il;        // iso ~ ih + il
+    float iso_err;       // upper bound of |iso - (ih + il)|
+    float f_thr;         // largest float <= iso: v > f_thr <=> double(v) > iso
+    float vmin_f, vmax_f;// the clamp range as floats (exact when fast_ok)
+    int32_t fast_ok;     // 0: always take the FP64 sequence
+    int32_t pad;
+};
+
+__device__ __forceinline__ void two_sum(float a, float b, float& s, float& e)
+{
+    s = __fadd_rn(a, b);
+    const float bb = __fsub_rn(s, a);
+    e = __fadd_rn(__fsub_rn(a, __fsub_rn(s, bb)), __fsub_rn(b, bb));
+}
+
+__device__ __forceinline__ float clampf_ref(float a, float lo, float hi)
+{
+    return a <= lo ? lo : (a <= hi ? a : hi);
+}
+
+// Half the distance from y (>= 0, finite) to the next float above / below.
+__device__ __forceinline__ float half_gap_up(float y)
+{
+    return __fmul_rn(__fsub_rn(__int_as_float(__float_as_int(y) + 1), y), 0.5f);
+}
+__device__ __forceinline__ float half_gap_down(float y)
+{
+    return __fmul_rn(__fsub_rn(y, __int_as_float(__float_as_int(y) - 1)), 0.5f);
+}
+
+// The varying-axis coordinate RN32(X) for an edge from coordinate a (value
+// v0) to b = a + d (value v1), d = +-1.  Returns false when the FP32 path
+// cannot decide; `out` is then unspecified.
+__device__ __forceinline__ bool fast_axis(float v0, float v1, float a, float b, const FastIso& f, float& out)
+{
+    // num = iso - v0 as a double-float (nh, nl); err_num bounds its error.
+    float s, e;
+    two_sum(f.ih, -v0, s, e);
+    const float e2 = __fadd_rn(e, f.il);
+    float nh, nl;
+    two_sum(s, e2, nh, nl);
+    if (nh == 0.0f && nl == 0.0f && f.iso_err == 0.0f) {
+        // iso == v0 exactly: r = 0 and the reference returns a exactly
+        out = a;
+        return true;
+    }
+    const float err_num = __fadd_rn(f.iso_err, __fmul_rn(fabsf(e2), 1.1920929e-07f));  // + 2^-23 |e2|
+    // den = v1 - v0 exactly as (dh, dl).
+    float dh, dl;
+    two_sum(v1, -v0, dh, dl);
+    const float adh = fabsf(dh);
+    if (!(adh >= 8.67361738e-19f) || !(adh <= 1.15292150e+18f)) return false;  // 2^-60 .. 2^60
+    // q = num / den: q1 from the reciprocal, then one residual correction.
+    const float inv = __frcp_rn(dh);
+    const float q1 = __fmul_rn(nh, inv);
+    const float p = __fmul_rn(q1, dh);
+    const float pe = __fmaf_rn(q1, dh, -p);
+    const float p2 = __fmul_rn(q1, dl);
+    const float pe2 = __fmaf_rn(q1, dl, -p2);
+    const float rho = __fsub_rn(__fadd_rn(__fsub_rn(__fsub_rn(nh, p), pe), __fsub_rn(nl, p2)), pe2);
+    const float q2 = __fmul_rn(rho, inv);
+    const float aq = fabsf(q1);
+    if (!(aq <= 1.5f)) return false;
+    // Y = a + d*(q1 + q2) as (yh, yl).
+    const bool up = b > a;
+    const float dq1 = up ? q1 : -q1, dq2 = up ? q2 : -q2;
+    float ya, yb;
+    two_sum(a, dq1, ya, yb);
+    const float yb2 = __fadd_rn(yb, dq2);
+    float yh, yl;
+    two_sum(ya, yb2, yh, yl);
+    // E = E_R + rounding of yb2 + E_D, each with slack.
+    const float m = fmaxf(a, b);
+    float E = __fmul_rn(aq, 9.09494702e-13f);                                   // 2^-40 |q|
+    E = __fadd_rn(E, __fmul_rn(__fmul_rn(err_num, __frcp_ru(adh)), 1.0001f));  // err(num)/|den|
+    E = __fadd_rn(E, __fmul_rn(fabsf(yb2), 1.1920929e-07f));                    // 2^-23 |yb2|
+    E = __fadd_rn(E, __fmul_rn(__fadd_rn(m, 1.0f), 8.8817842e-16f));            // 2^-50 (M + 1)
+    E = __fmul_rn(E, 1.001f);
+    if (!(yh > 0.0f) || !(yh < 3.0e7f)) {
+        // Y at (or below) zero: exact only if the double-float is exactly 0
+        if (yh == 0.0f && yl == 0.0f && E < 1.0e-30f) { out = 0.0f; return true; }
+        return false;
+    }
+    const float dist = (yl >= 0.0f) ? __fsub_rn(half_gap_up(yh), yl) : __fadd_rn(half_gap_down(yh), yl);
+    if (!(dist > E)) return false;
+    out = yh;
+    return true;
+}
+
+// Vertex of an edge whose endpoints differ along `axis` (0, 1, 2): A = (ax,
+// ay, az) with value va, B with value vb (both raw values as float).  `j`
+// carries the FP64 constants for the fallback.  Output after the
+// (p + min_coord) * scale transform.
+__device__ __forceinline__ float3 edge_vertex_fast(const Interp& j, const FastIso& f, float va, float vb,
+                                                   float ax, float ay, float az, float bx, float by, float bz,
+                                                   int axis)
+{
+    float px = ax, py = ay, pz = az;
+    bool ok = f.fast_ok != 0;
+    if (ok) {
+        const float v0 = clampf_ref(va, f.vmin_f, f.vmax_f);
+        const float v1 = clampf_ref(vb, f.vmin_f, f.vmax_f);
+        ok = (v0 > f.f_thr) != (v1 > f.f_thr);
+        if (ok) {
+            float r;
+            if (axis == 0) ok = fast_axis(v0, v1, ax, bx, f, r), px = r;
+            else if (axis == 1) ok = fast_axis(v0, v1, ay, by, f, r), py = r;
+            else ok = fast_axis(v0, v1, az, bz, f, r), pz = r;
+        }
+    }
+    if (ok) {
+        float3 o;
+        o.x = __fmul_rn(__fadd_rn(px, j.min_coord[0]), j.scale[0]);
+        o.y = __fmul_rn(__fadd_rn(py, j.min_coord[1]), j.scale[1]);
+        o.z = __fmul_rn(__fadd_rn(pz, j.min_coord[2]), j.scale[2]);
+        return o;
+    }
+    return interpolate_exact(j, (double)va, (double)vb, ax, ay, az, bx, by, bz);
+}
+
+}  // namespace kvsmc

@@ -1,0 +1,103 @@
+// selftest.cu -- on-device check of the FP32 interpolation path against the
+// FP64 sequence of the reference, on random edges (diagnostic entry point).
+#include <cuda_runtime.h>
+
+#include "mc_internal.h"
+#include "mc_interp.cuh"
+
+namespace kvsmc {
+
+namespace {
+
+__device__ __forceinline__ uint64_t mix64(uint64_t x)
+{
+    x ^= x >> 33; x *= 0xff51afd7ed558ccdull;
+    x ^= x >> 33; x *= 0xc4ceb9fe1a85ec53ull;
+    x ^= x >> 33;
+    return x;
+}
+
+__device__ __forceinline__ double unit(uint64_t h) { return (double)(h >> 11) * (1.0 / 9007199254740992.0); }
+
+// One random straddling edge per index; several value distributions.
+__global__ void k_selftest(uint64_t n, uint64_t seed, unsigned long long* counters)
+{
+    unsigned long long mism = 0, fall = 0, tested = 0;
+    for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < n; i += (uint64_t)gridDim.x * blockDim.x) {
+        const uint64_t h0 = mix64(seed * 0x9e3779b97f4a7c15ull + i);
+        const uint64_t h1 = mix64(h0 + 1), h2 = mix64(h0 + 2), h3 = mix64(h0 + 3);
+        const int kind = (int)(h0 & 7);
+        double iso;
+        float va, vb;
+        if (kind == 0) {          // float data in [0,1], double isolevel
+            va = (float)unit(h1); vb = (float)unit(h2); iso = unit(h3);
+        } else if (kind == 1) {   // float data, float isolevel
+            va = (float)unit(h1); vb = (float)unit(h2); iso = (double)(float)unit(h3);
+        } else if (kind == 2) {   // uint8-like data, isolevel k + 0.5 or k
+            va = (float)(h1 & 255); vb = (float)(h2 & 255); iso = (double)(h3 & 255) + ((h3 >> 8) & 1 ? 0.5 : 0.0);
+        } else if (kind == 3) {   // uint16-like data, random double isolevel
+            va = (float)(h1 & 65535); vb = (float)(h2 & 65535); iso = unit(h3) * 65535.0;
+        } else if (kind == 4) {   // close values (small denominators)
+            va = (float)unit(h1); vb = __int_as_float(__float_as_int(va) + (int)(h2 & 15) - 7);
+            iso = (double)va + ((double)vb - (double)va) * unit(h3);
+        } else if (kind == 5) {   // isolevel just above v0 (small numerators)
+            va = (float)unit(h1); vb = (float)unit(h2);
+            iso = (double)fminf(va, vb) + unit(h3) * 1e-9;
+        } else if (kind == 6) {   // wide dynamic range
+            va = (float)((unit(h1) - 0.5) * 2e6); vb = (float)((unit(h2) - 0.5) * 2e6); iso = (unit(h3) - 0.5) * 2e6;
+        } else {                  // ratio near 1/2 (midpoint-prone)
+            va = (float)(h1 & 1023); vb = va + 1.0f; iso = (double)va + 0.5 + (unit(h3) - 0.5) * 1e-12;
+        }
+        const float f_iso = (float)iso;
+        float thr = f_iso;
+        if ((double)thr > iso) thr = nextafterf(thr, -INFINITY);
+        const bool b0 = va > thr, b1 = vb > thr;
+        if (b0 == b1) continue;
+        FastIso f;
+        f.ih = f_iso;
+        f.il = (float)(iso - (double)f.ih);
+        const double rep = iso - ((double)f.ih + (double)f.il);
+        f.iso_err = (float)fabs(rep) * 1.0001f;
+        f.f_thr = thr;
+        f.vmin_f = -3.0e38f; f.vmax_f = 3.0e38f;
+        f.fast_ok = 1; f.pad = 0;
+        Interp j;
+        j.iso = iso;
+        j.vmin = -3.0e38; j.vmax = 3.0e38;
+        for (int k = 0; k < 3; ++k) { j.min_coord[k] = 0.0f; j.scale[k] = 1.0f; }
+        const int axis = (int)((h3 >> 20) % 3);
+        const float a = (float)((h3 >> 24) & 2047);
+        const bool rev = (h3 >> 40) & 1;
+        float ax = (float)((h2 >> 30) & 2047), ay = (float)((h2 >> 41) & 2047), az = (float)((h1 >> 30) & 2047);
+        float bx = ax, by = ay, bz = az;
+        float* pa = axis == 0 ? &ax : (axis == 1 ? &ay : &az);
+        float* pb = axis == 0 ? &bx : (axis == 1 ? &by : &bz);
+        *pa = rev ? a + 1.0f : a;
+        *pb = rev ? a : a + 1.0f;
+        const float3 ex = interpolate_exact(j, (double)va, (double)vb, ax, ay, az, bx, by, bz);
+        // the fast path alone (no fallback) to count fallbacks
+        float r;
+        const float v0 = va, v1 = vb;
+        const bool ok = fast_axis(v0, v1, *pa, *pb, f, r);
+        const float3 fv = edge_vertex_fast(j, f, va, vb, ax, ay, az, bx, by, bz, axis);
+        ++tested;
+        if (!ok) ++fall;
+        if (__float_as_int(ex.x) != __float_as_int(fv.x) || __float_as_int(ex.y) != __float_as_int(fv.y) ||
+            __float_as_int(ex.z) != __float_as_int(fv.z))
+            ++mism;
+    }
+    atomicAdd(&counters[0], tested);
+    atomicAdd(&counters[1], mism);
+    atomicAdd(&counters[2], fall);
+}
+
+}  // namespace
+
+cudaError_t launch_selftest(uint64_t n, uint64_t seed, unsigned long long* d_counters, const Launch& L)
+{
+    k_selftest<<<L.num_sms * 8, 256, 0, L.stream>>>(n, seed, d_counters);
+    *L.counter += 1;
+    return cudaGetLastError();
+}
+
+}  // namespace kvsmc
