@@ -47,14 +47,21 @@ def dist_env():
 
 
 def barrier_max(value, world):
-    """Max over ranks of a float (identity for one rank)."""
+    """Max over ranks of a float (identity for one rank); NCCL or gloo."""
     if world == 1:
         return value
     import torch
     import torch.distributed as dist
-    t = torch.tensor([value], dtype=torch.float64, device="cuda")
+    dev = "cuda" if dist.get_backend() == "nccl" else "cpu"
+    t = torch.tensor([value], dtype=torch.float64, device=dev)
     dist.all_reduce(t, op=dist.ReduceOp.MAX)
     return float(t.item())
+
+
+def replica_value(units_per_rank, ms_per_rank, world):
+    """Whole-job throughput of independent replicas: all ranks' units over the
+    slowest rank's time (units/s)."""
+    return units_per_rank * world / (barrier_max(ms_per_rank, world) * 1e-3)
 
 
 def make_field(w, device, seed=42):

@@ -17,6 +17,8 @@ namespace {
 
 bool stream_dtype(int dt) { return dt == KVSMC_I8 || dt == KVSMC_I16 || dt == KVSMC_U8 || dt == KVSMC_U16 || dt == KVSMC_F32; }
 
+}  // namespace
+
 void tiling(const kvsmc::VolumeView& v, uint32_t& wpr, uint32_t& rows, uint64_t& plane_elems)
 {
     const uint32_t cx = v.nx - 1;
@@ -29,8 +31,6 @@ void tiling(const kvsmc::VolumeView& v, uint32_t& wpr, uint32_t& rows, uint64_t&
     const uint64_t quantum = 128 / kvsmc::dtype_size(v.dtype);
     plane_elems = (need + quantum - 1) / quantum * quantum;
 }
-
-}  // namespace
 
 // FP32 fast-path constants of one request (see mc_interp.cuh).
 kvsmc::FastIso make_fast(double iso, double vmin, double vmax, int dtype)

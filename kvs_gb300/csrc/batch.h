@@ -7,6 +7,8 @@
 namespace kvsmc_host {
 
 kvsmc::FastIso make_fast(double iso, double vmin, double vmax, int dtype);
+// Warps per row, cell rows per y-tile and staged plane size of a volume.
+void tiling(const kvsmc::VolumeView& v, uint32_t& wpr, uint32_t& rows, uint64_t& plane_elems);
 
 // A batch of streaming-eligible requests.  plan() builds the work tables,
 // count() fills every item's sizes, emit() writes the outputs of the items

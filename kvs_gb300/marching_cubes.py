@@ -341,7 +341,12 @@ class MarchingCubes(PolygonObject):
             return None
         if self.normalType() == PolygonObject.VertexNormal:
             self._duplication = False
-        self._mapping(obj)
+        try:
+            self._mapping(obj)
+        except _abi.KvsmcError as e:
+            # no CPU fallback: the GPU call failed, so the mapper failed
+            message_error(f"libkvsmc: {e}")
+            return None
         self._success = True
         return self
 

@@ -1,0 +1,117 @@
+"""Generate the golden fixtures from the reference kvs::MarchingCubes.
+
+Runs the reference mapper compiled from its own sources (oracle/_ref, built by
+oracle/Makefile.ref) on small seeded inputs and stores inputs + outputs in
+tests/golden/golden.npz, with the case list in tests/golden/cases.json.  The
+reference ships no tests or golden vectors of its own, so these fixtures pin the
+oracle restatement and the CUDA path on hosts where the reference is absent.
+
+    python tests/golden/make_golden.py
+"""
+import json
+import os
+import sys
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.dirname(os.path.dirname(HERE))
+sys.path.insert(0, ROOT)
+
+from oracle import ref  # noqa: E402
+
+MODES = [("polygon", True), ("polygon", False), ("vertex", True)]
+
+
+def cases():
+    rng = np.random.default_rng(2024)
+    out = []
+    h = ref.hydrogen(32)
+    out.append(("hydrogen32", h, [(float(h.min()) + float(h.max())) / 2], {}))
+    for dt in ref.DTYPES:
+        dt = np.dtype(dt)
+        if dt.kind == "f":
+            v = rng.random((9, 10, 11)).astype(dt)
+            isos = [0.5, float(np.float32(0.37))]
+        else:
+            info = np.iinfo(dt)
+            lo, hi = max(int(info.min), -100), min(int(info.max), 100)
+            v = rng.integers(lo, hi, size=(9, 10, 11), endpoint=True).astype(dt)
+            isos = [0.5, 7.0]
+        out.append((f"random_{dt.name}", v, isos, {}))
+    x, y, z = np.meshgrid(np.arange(26), np.arange(24), np.arange(22), indexing="xy")
+    blob = np.exp(-((x - 12.3) ** 2 + (y - 11.1) ** 2 + (z - 10.7) ** 2) / (2 * 6.0 ** 2)).transpose(2, 0, 1)
+    blob = np.ascontiguousarray(blob).astype(np.float32)
+    out.append(("blob_f32", blob, [0.5, 0.123456789], {}))
+    f = rng.random((8, 9, 10)).astype(np.float32)
+    out.append(("clamp_f32", f, [0.5], {"minmax": (0.3, 0.7)}))
+    out.append(("objcoords_f32", f, [0.5], {"obj": ([1.5, -2.0, 3.25], [7.0, 9.0, 4.0])}))
+    rect = np.concatenate([np.linspace(0, 3, 10), np.linspace(-1, 1, 9), np.linspace(2, 5, 8)]).astype(np.float32)
+    out.append(("rectilinear_f32", f, [0.5], {"rect": rect}))
+    out.append(("tfrange_f32", f, [0.5], {"tf_range": (-1.0, 3.0)}))
+    out.append(("thin_x1_f32", rng.random((5, 6, 1)).astype(np.float32), [0.5], {}))
+    out.append(("constant_f32", np.full((4, 5, 6), 2.0, np.float32), [2.0], {}))
+    w = f.copy()
+    w[3, 4, 5] = np.nan
+    w[0, 0, 1] = -0.0
+    out.append(("nan_f32", w, [0.5], {}))
+    odd = rng.integers(0, 255, size=(6, 7, 33)).astype(np.uint8)
+    out.append(("odd_u8", odd, [127.5, 100.0], {}))
+    return out
+
+
+def main():
+    if not ref.available():
+        ref.build()
+    arrays = {}
+    manifest = []
+    for name, v, isos, opts in cases():
+        arrays[f"{name}__input"] = v
+        if "rect" in opts:
+            arrays[f"{name}__rect"] = opts["rect"]
+        for iso in isos:
+            for nt, dup in MODES:
+                key = f"{name}__{iso!r}__{nt}__{int(dup)}"
+                r = ref.marching_cubes(v, iso, nt, dup, minmax=opts.get("minmax"), rect_coords=opts.get("rect"),
+                                       obj_coords=opts.get("obj"), tf_range=opts.get("tf_range"))
+                for f in ("coords", "normals", "connections", "colors"):
+                    arrays[f"{key}__{f}"] = r[f]
+                manifest.append(dict(key=key, case=name, iso=iso, normal_type=nt, duplication=dup,
+                                     minmax=opts.get("minmax"), obj=opts.get("obj"), rect="rect" in opts,
+                                     tf_range=opts.get("tf_range"), success=r["success"],
+                                     vol_min=r["vol_min"], vol_max=r["vol_max"],
+                                     polygon_type=r["polygon_type"], normal_type_out=r["normal_type"],
+                                     color_type=r["color_type"], min_obj=r["min_obj"].tolist(),
+                                     max_obj=r["max_obj"].tolist(), ntriangles=int(
+                                         r["coords"].size // 9 if dup and nt == "polygon"
+                                         else r["connections"].size // 3)))
+    # every corner configuration, each in its own 2x2x2 volume
+    corner = [(0, 0, 0), (1, 0, 0), (1, 1, 0), (0, 1, 0), (0, 0, 1), (1, 0, 1), (1, 1, 1), (0, 1, 1)]
+    for case in range(256):
+        v = np.zeros((2, 2, 2), np.float32)
+        for k, (x, y, z) in enumerate(corner):
+            v[z, y, x] = 1.0 if case & (1 << k) else 0.0
+        arrays[f"case{case}__input"] = v
+        for nt, dup in MODES:
+            key = f"case{case}__0.5__{nt}__{int(dup)}"
+            r = ref.marching_cubes(v, 0.5, nt, dup)
+            for f in ("coords", "normals", "connections", "colors"):
+                arrays[f"{key}__{f}"] = r[f]
+            manifest.append(dict(key=key, case=f"case{case}", iso=0.5, normal_type=nt, duplication=dup,
+                                 minmax=None, obj=None, rect=False, tf_range=None, success=r["success"],
+                                 vol_min=r["vol_min"], vol_max=r["vol_max"], polygon_type=r["polygon_type"],
+                                 normal_type_out=r["normal_type"], color_type=r["color_type"],
+                                 min_obj=r["min_obj"].tolist(), max_obj=r["max_obj"].tolist(), ntriangles=-1))
+    # the default colour table and ColorMap::at on a sweep of values
+    arrays["colormap256"] = ref.default_colormap(256)
+    vals = np.linspace(-1.5, 2.5, 97).astype(np.float32)
+    arrays["color_at_values"] = vals
+    arrays["color_at_rgb"] = np.stack([ref.color_at(256, np.float32(-1.0), np.float32(2.0), v) for v in vals])
+    np.savez_compressed(os.path.join(HERE, "golden.npz"), **arrays)
+    with open(os.path.join(HERE, "cases.json"), "w") as f:
+        json.dump(manifest, f, indent=0)
+    print(f"{len(manifest)} golden cases")
+
+
+if __name__ == "__main__":
+    main()

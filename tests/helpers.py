@@ -31,3 +31,33 @@ def first_diff(a, b):
         return None if a.size == b.size else ("size", a.size, b.size)
     i = int(d[0])
     return (i, a[i], b[i], int(d.size))
+
+
+# ------------------------------------------------------------------ golden fixtures
+
+import json as _json
+import os as _os
+
+GOLDEN_DIR = _os.path.join(_os.path.dirname(_os.path.abspath(__file__)), "golden")
+_golden = None
+
+
+def golden():
+    """(manifest list, npz arrays) of tests/golden (made by make_golden.py)."""
+    global _golden
+    if _golden is None:
+        man = _json.load(open(_os.path.join(GOLDEN_DIR, "cases.json")))
+        arr = np.load(_os.path.join(GOLDEN_DIR, "golden.npz"))
+        _golden = (man, arr)
+    return _golden
+
+
+def golden_inputs(entry, arr):
+    v = arr[f"{entry['case']}__input"]
+    rect = arr[f"{entry['case']}__rect"] if entry["rect"] else None
+    return v, rect
+
+
+def golden_outputs(entry, arr):
+    k = entry["key"]
+    return {f: arr[f"{k}__{f}"] for f in ("coords", "normals", "connections", "colors")}

@@ -1,0 +1,32 @@
+// Drives kvs::cuda::MarchingCubes the way user code drives kvs::MarchingCubes
+// (Example/Visualization/Isosurface/main.cpp:36-44): a Hydrogen volume, iso =
+// (min+max)/2, the constructor form and the pipeline-module form.  Prints one
+// line per call: success flag, vertex count, connection count, colour.
+#include <cstdio>
+#include <kvs/HydrogenVolumeData>
+#include <kvs/TransferFunction>
+#include "kvs/cuda/MarchingCubes.h"
+
+int main()
+{
+    kvs::HydrogenVolumeData data( kvs::Vec3u( 32, 32, 32 ) );
+    kvs::StructuredVolumeObject* volume = data.exec();
+    volume->updateMinMaxValues();
+    const double iso = ( volume->minValue() + volume->maxValue() ) * 0.5;
+    const kvs::TransferFunction tf( 256 );
+
+    kvs::cuda::MarchingCubes* a = new kvs::cuda::MarchingCubes( volume, iso, kvs::PolygonObject::PolygonNormal, true, tf );
+    std::printf( "ctor success=%d vertices=%zu connections=%zu\n", a->isSuccess() ? 1 : 0,
+                 a->numberOfVertices(), a->numberOfConnections() );
+
+    kvs::cuda::MarchingCubes m;               // PipelineModule form
+    m.setIsolevel( iso );
+    m.setNormalType( kvs::PolygonObject::VertexNormal );
+    kvs::ObjectBase* r = m.exec( volume );
+    std::printf( "exec success=%d returned=%d module=%s\n", m.isSuccess() ? 1 : 0, r ? 1 : 0, m.moduleName() );
+
+    kvs::ObjectBase* none = m.exec( nullptr );
+    std::printf( "null success=%d returned=%d\n", m.isSuccess() ? 1 : 0, none ? 1 : 0 );
+    delete a;
+    return 0;
+}
