@@ -189,6 +189,36 @@ kvsmc_status kvsmc_count_batch(kvsmc_context* ctx, kvsmc_request* reqs, int32_t 
  * volume is read once per pass however many isolevels share it. */
 kvsmc_status kvsmc_extract_batch(kvsmc_context* ctx, kvsmc_request* reqs, int32_t n);
 
+/* ------------------------------------------------- no-allocation variant */
+
+/* For callers that may not allocate device memory: a plugin whose host
+ * application owns the whole device-memory budget, or an interactive frame
+ * loop in which cudaMalloc/cudaFree (which can synchronize the device) would
+ * stall.  No counterpart in the reference; this is the duplicated-vertex,
+ * polygon-normal extraction (p->mode must be KVSMC_DUP_POLYGON_NORMAL) run
+ * by the streaming kernels, with no context and no allocation of any kind:
+ *   - the caller passes the volume (dense device array, x fastest; its rows,
+ *     nx * sizeof(value), must be 16-byte multiples and d_values 16-byte
+ *     aligned), the output arrays with their capacities (floats), and a
+ *     CUDA stream (NULL = the legacy default stream);
+ *   - dtype is int8, uint8, int16, uint16 or float32; 2 <= nx <= 4097;
+ *     ny, nz >= 2; the isolevel is finite;
+ *   - the intermediates live in a 4 MiB static device array that every GPU
+ *     loading this library holds until exit; a volume whose intermediates do
+ *     not fit (beyond about 1024^3 float32) is refused with
+ *     KVSMC_ERR_TOO_LARGE;
+ *   - the first call on each device looks up that array's device address
+ *     (cudaGetSymbolAddress) with the device current: make that first call
+ *     before starting any stream capture;
+ *   - all calls share the array: calls that overlap on the GPU race on it
+ *     and must be serialized by the caller.
+ * Returns KVSMC_ERR_CAPACITY (with *sizes filled) when the outputs are too
+ * small.  Results are identical to kvsmc_extract_device's. */
+kvsmc_status kvsmc_extract_noalloc(const void* d_values, kvsmc_dtype dtype, uint32_t nx, uint32_t ny,
+                                   uint32_t nz, const kvsmc_params* p, float* d_coords,
+                                   uint64_t coords_capacity, float* d_normals, uint64_t normals_capacity,
+                                   void* cuda_stream, kvsmc_sizes* sizes);
+
 /* ------------------------------------------------------------ diagnostics */
 
 /* Per-kernel timing: with profiling on, every kernel family launched by this

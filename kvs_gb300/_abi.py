@@ -40,7 +40,7 @@ EXPORTS = [
     "kvsmc_count", "kvsmc_extract_device", "kvsmc_marching_cubes_host",
     "kvsmc_count_batch", "kvsmc_extract_batch", "kvsmc_set_kernel_path",
     "kvsmc_selftest_interpolation", "kvsmc_profile_enable", "kvsmc_profile_read",
-    "kvsmc_extract_batch_host",
+    "kvsmc_extract_batch_host", "kvsmc_extract_noalloc",
 ]
 
 PATH_AUTO = 0      # streaming kernels where eligible
@@ -123,6 +123,8 @@ def load(path=LIB_PATH):
                                                    C.POINTER(u64)]),
         "kvsmc_extract_batch_host": (C.c_int, [vp, vp, C.c_int, u32, u32, u32, C.POINTER(Params), i32,
                                                HOST_ALLOC, vp, C.POINTER(Sizes)]),
+        "kvsmc_extract_noalloc": (C.c_int, [vp, C.c_int, u32, u32, u32, C.POINTER(Params), vp, u64, vp, u64,
+                                            vp, C.POINTER(Sizes)]),
         "kvsmc_profile_enable": (C.c_int, [vp, i32]),
         "kvsmc_profile_read": (i32, [vp, i32, C.POINTER(C.c_char_p), C.POINTER(u64), C.POINTER(C.c_double)]),
     }

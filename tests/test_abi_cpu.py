@@ -43,6 +43,12 @@ def test_no_gpu_no_fallback():
     assert lib.kvsmc_create(0, C.byref(h)) == _abi.ERR_NO_DEVICE
     with pytest.raises(_abi.KvsmcError):
         _abi.Context()
+    s = _abi.Sizes()
+    p = _abi.make_params(0.5, 0)
+    x = np.zeros(64, np.float32)
+    # the no-allocation entry point refuses before touching memory
+    assert lib.kvsmc_extract_noalloc(x.ctypes.data, 8, 4, 4, 4, C.byref(p), None, 0, None, 0, None,
+                                     C.byref(s)) in (_abi.ERR_NO_DEVICE, _abi.ERR_CUDA)
 
 
 @pytest.mark.skipif(gpu_available(), reason="checks the no-GPU behaviour")
