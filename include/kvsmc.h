@@ -205,8 +205,7 @@ kvsmc_status kvsmc_extract_batch(kvsmc_context* ctx, kvsmc_request* reqs, int32_
  *     ny, nz >= 2; the isolevel is finite;
  *   - the intermediates live in a 4 MiB static device array that every GPU
  *     loading this library holds until exit; a volume whose intermediates do
- *     not fit (beyond about 1024^3 float32) is refused with
- *     KVSMC_ERR_TOO_LARGE;
+ *     not fit (beyond about 512^3) is refused with KVSMC_ERR_TOO_LARGE;
  *   - the first call on each device looks up that array's device address
  *     (cudaGetSymbolAddress) with the device current: make that first call
  *     before starting any stream capture;

@@ -1,6 +1,7 @@
 // batch.cu -- planning and launching of the streaming kernels for a batch of
-// (volume, isolevel) requests: one count launch and one emit launch per
-// value type present, whatever the number of volumes and isolevels.
+// (volume, isolevel) requests: per value type present one count launch and one
+// emit launch, plus the unit scan and the plane scan, whatever the number of
+// volumes and isolevels.
 #include <algorithm>
 #include <cmath>
 #include <cstring>
@@ -17,20 +18,12 @@ namespace {
 
 bool stream_dtype(int dt) { return dt == KVSMC_I8 || dt == KVSMC_I16 || dt == KVSMC_U8 || dt == KVSMC_U16 || dt == KVSMC_F32; }
 
-}  // namespace
-
-void tiling(const kvsmc::VolumeView& v, uint32_t& wpr, uint32_t& rows, uint64_t& plane_elems)
+uint32_t segments_per_row(const kvsmc::VolumeView& v)
 {
-    const uint32_t cx = v.nx - 1;
-    wpr = (cx + kvsmc::kStreamSegCells - 1) / kvsmc::kStreamSegCells;
-    rows = (kvsmc::kStreamThreads / 32) / (wpr ? wpr : 1);
-    if (rows < 1) rows = 1;
-    if (rows > v.ny - 1) rows = v.ny - 1;
-    const uint64_t need = std::max<uint64_t>((uint64_t)(rows + 1) * v.pitch,
-                                             (uint64_t)rows * v.pitch + (uint64_t)wpr * kvsmc::kStreamSegCells + 16);
-    const uint64_t quantum = 128 / kvsmc::dtype_size(v.dtype);
-    plane_elems = (need + quantum - 1) / quantum * quantum;
+    return (v.nx - 1 + kvsmc::kStreamSegCells - 1) / kvsmc::kStreamSegCells;
 }
+
+}  // namespace
 
 // FP32 fast-path constants of one request (see mc_interp.cuh).
 kvsmc::FastIso make_fast(double iso, double vmin, double vmax, int dtype)
@@ -62,6 +55,24 @@ kvsmc::FastIso make_fast(double iso, double vmin, double vmax, int dtype)
     return f;
 }
 
+void bucket_params(float t0, float t1, float& bt0, float& bscale)
+{
+    const float span = t1 - t0;
+    bt0 = t0;
+    bscale = (span > 0.0f && std::isfinite(span)) ? (float)kvsmc::kStreamBuckets / span : 1.0f / (1.0f + std::fabs(t0));
+    if (!(bscale > 0.0f) || !std::isfinite(bscale)) bscale = 1.0f;
+}
+
+uint32_t stream_zchunk(const kvsmc::VolumeView& v, uint32_t wpr, int num_sms)
+{
+    const uint64_t warp_steps = (uint64_t)(v.nz - 1) * (v.ny - 1) * wpr;
+    const uint64_t want_tasks = (uint64_t)num_sms * 24 * 4;
+    uint64_t zc = (warp_steps + want_tasks - 1) / want_tasks;
+    if (zc < 4) zc = 4;
+    if (zc > 64) zc = 64;
+    return (uint32_t)zc;
+}
+
 bool stream_eligible(const kvsmc_context* ctx, const Item& it)
 {
     if (ctx->path != 0 || !it.vol) return false;
@@ -69,14 +80,12 @@ bool stream_eligible(const kvsmc_context* ctx, const Item& it)
     const kvsmc::VolumeView& v = it.vol->view;
     if (!stream_dtype(v.dtype)) return false;
     if (v.nx < 2 || v.ny < 2 || v.nz < 2) return false;
-    if (v.nx - 1 > (uint32_t)(kvsmc::kStreamMaxWarpsPerRow * kvsmc::kStreamSegCells)) return false;
+    if (segments_per_row(v) > (uint32_t)kvsmc::kStreamMaxSegments) return false;
+    // triangles of one (isolevel, z) plane must fit the u32 plane offsets
+    if ((double)(v.nx - 1) * (double)(v.ny - 1) * 5.0 >= 4294967295.0) return false;
     const double iso = it.params.isolevel;
     if (!std::isfinite(iso) || std::fabs(iso) > 1.0e30) return false;
-    uint32_t wpr, rows;
-    uint64_t pe;
-    tiling(v, wpr, rows, pe);
-    const size_t smem = kvsmc::stream_shared_bytes(pe * kvsmc::dtype_size(v.dtype), true);
-    return smem <= (size_t)227 * 1024;
+    return kvsmc::stream_shared_bytes(v.dtype, true) <= (size_t)227 * 1024;
 }
 
 kvsmc_status StreamBatch::plan()
@@ -93,7 +102,6 @@ kvsmc_status StreamBatch::plan()
         }
         lists[f->second].push_back(it);
     }
-    // launches by value type
     std::vector<int> dtypes;
     for (auto& l : lists)
         if (std::find(dtypes.begin(), dtypes.end(), l[0]->vol->view.dtype) == dtypes.end())
@@ -102,47 +110,42 @@ kvsmc_status StreamBatch::plan()
     isos.clear();
     iso_item.clear();
     launches.clear();
-    uint64_t tiles = 0;
+    unit_elems = 0;
+    scan_blocks = 0;
+    iso_planes = 0;
     for (int dt : dtypes) {
         Launch1 L;
         L.dtype = dt;
         L.g0 = (int)groups.size();
-        L.nctas = 0;
-        size_t max_plane = 0;
+        L.ntasks = 0;
         for (auto& l : lists) {
             if (l[0]->vol->view.dtype != dt) continue;
-            kvsmc::VolumeView v = l[0]->vol->view;
+            const kvsmc::VolumeView v = l[0]->vol->view;
             StreamGroup g;
             std::memset(&g, 0, sizeof g);
             g.vol = v;
-            tiling(v, g.wpr, g.rows, g.plane_elems);
+            g.wpr = segments_per_row(v);
+            g.zchunk = stream_zchunk(v, g.wpr, ctx->num_sms);
             const uint32_t cy = v.ny - 1, cz = v.nz - 1;
-            g.ytiles = (cy + g.rows - 1) / g.rows;
-            const uint32_t want = std::max<uint32_t>(1, (uint32_t)(2 * ctx->num_sms + g.ytiles - 1) / g.ytiles);
-            uint32_t zc = (cz + want - 1) / want;
-            zc = std::min<uint32_t>(std::max<uint32_t>(zc, 4), 32);
-            g.zchunk = zc;
-            const uint32_t zchunks = (cz + zc - 1) / zc;
-            g.cta_begin = L.nctas;
-            L.nctas += g.ytiles * zchunks;
-            max_plane = std::max(max_plane, (size_t)g.plane_elems * kvsmc::dtype_size(dt));
+            const uint32_t zchunks = (cz + g.zchunk - 1) / g.zchunk;
+            g.task_begin = L.ntasks;
+            L.ntasks += (uint64_t)cy * g.wpr * zchunks;
+            g.seg_elems = (uint32_t)kvsmc::stream_row_elems(dt);
+            g.seg_copy_bytes = g.seg_elems * (uint32_t)kvsmc::dtype_size(dt);
+            g.warp_smem_bytes = (uint32_t)kvsmc::stream_warp_smem_bytes(dt, true);
+            g.warp_smem_offset = (uint32_t)kvsmc::stream_warp_smem_offset();
             // isolevels sorted by threshold
             std::vector<std::pair<float, Item*>> sorted;
-            for (Item* it : l) {
-                const kvsmc::FastIso f = make_fast(it->params.isolevel, it->vmin, it->vmax, dt);
-                sorted.push_back({f.f_thr, it});
-            }
+            for (Item* it : l) sorted.push_back({make_fast(it->params.isolevel, it->vmin, it->vmax, dt).f_thr, it});
             std::stable_sort(sorted.begin(), sorted.end(),
                              [](const std::pair<float, Item*>& a, const std::pair<float, Item*>& b) { return a.first < b.first; });
             g.iso_begin = (int32_t)isos.size();
             g.niso = (int32_t)sorted.size();
-            const float t0 = sorted.front().first, t1 = sorted.back().first;
-            const float span = t1 - t0;
-            g.bt0 = t0;
-            g.bscale = (span > 0.0f && std::isfinite(span)) ? (float)kvsmc::kStreamBuckets / span
-                                                           : 1.0f / (1.0f + std::fabs(t0));
-            if (!(g.bscale > 0.0f) || !std::isfinite(g.bscale)) g.bscale = 1.0f;
-            const uint64_t tiles_per_iso = (uint64_t)cz * g.ytiles;
+            bucket_params(sorted.front().first, sorted.back().first, g.bt0, g.bscale);
+            g.unit_base = unit_elems;
+            unit_elems += (uint64_t)cz * cy * g.wpr * g.niso;
+            g.plane_begin = scan_blocks;
+            scan_blocks += cz;
             for (auto& pr : sorted) {
                 Item* it = pr.second;
                 StreamIso s;
@@ -152,34 +155,33 @@ kvsmc_status StreamBatch::plan()
                 s.ip.vmin = it->vmin;
                 s.ip.vmax = it->vmax;
                 for (int k = 0; k < 3; ++k) { s.ip.min_coord[k] = it->params.min_coord[k]; s.ip.scale[k] = it->params.scale[k]; }
-                s.count_base = tiles;
-                tiles += tiles_per_iso;
+                s.plane_index = iso_planes;
+                iso_planes += cz;
                 isos.push_back(s);
                 iso_item.push_back(it);
             }
             groups.push_back(g);
         }
         L.ng = (int)groups.size() - L.g0;
-        L.smem_count = kvsmc::stream_shared_bytes(max_plane, false);
-        L.smem_emit = kvsmc::stream_shared_bytes(max_plane, true);
         launches.push_back(L);
     }
-    total_tiles = tiles;
 
     // device scratch
     const size_t niso = isos.size();
     const size_t need = 16 * 256 + align_up(groups.size() * sizeof(StreamGroup), 256) +
-                        align_up(niso * sizeof(StreamIso), 256) + align_up(tiles * 4, 256) +
-                        align_up(tiles * 8, 256) + align_up(kvsmc::scan_scratch_bytes(tiles), 256) +
-                        align_up(niso * 8, 256) + 4 * 256;
+                        align_up(niso * sizeof(StreamIso), 256) + align_up(unit_elems * 2, 256) +
+                        align_up(unit_elems * 4, 256) + align_up(iso_planes * 4, 256) + align_up(iso_planes * 8, 256) +
+                        align_up(kvsmc::scan_scratch_bytes(iso_planes), 256) + align_up(niso * 8, 256) + 4 * 256;
     kvsmc_status st = ensure_scratch(ctx, need);
     if (st) return st;
     Carve cv{static_cast<char*>(ctx->scratch)};
     d_groups = cv.take<StreamGroup>(groups.size() * sizeof(StreamGroup));
     d_isos = cv.take<StreamIso>(niso * sizeof(StreamIso));
-    d_counts = cv.take<uint32_t>(tiles * 4);
-    d_offsets = cv.take<uint64_t>(tiles * 8);
-    d_scan = cv.take<char>(kvsmc::scan_scratch_bytes(tiles));
+    d_unit_counts = cv.take<uint16_t>(unit_elems * 2);
+    d_unit_offsets = cv.take<uint32_t>(unit_elems * 4);
+    d_plane_totals = cv.take<uint32_t>(iso_planes * 4);
+    d_plane_base = cv.take<uint64_t>(iso_planes * 8);
+    d_scan = cv.take<char>(kvsmc::scan_scratch_bytes(iso_planes));
     d_totals = cv.take<uint64_t>(niso * 8);
     d_total = cv.take<uint64_t>(256);
     d_status = cv.take<int>(256);
@@ -204,10 +206,12 @@ kvsmc_status StreamBatch::count()
     const kvsmc::Launch L = launch_of(ctx);
     KVSMC_CUDA(ctx, cudaMemsetAsync(d_status, 0, sizeof(int), ctx->stream));
     for (const Launch1& l : launches)
-        KVSMC_CUDA(ctx, kvsmc::launch_stream(false, l.dtype, d_groups + l.g0, l.ng, l.nctas, l.smem_count, d_isos,
-                                             d_counts, d_offsets, d_status, L));
-    KVSMC_CUDA(ctx, kvsmc::launch_scan(d_counts, d_offsets, total_tiles, d_scan, d_total, L));
-    KVSMC_CUDA(ctx, kvsmc::launch_iso_totals(d_isos, (int)isos.size(), d_offsets, d_total, d_totals, L));
+        KVSMC_CUDA(ctx, kvsmc::launch_stream(false, l.dtype, d_groups + l.g0, l.ng, l.ntasks, d_isos, d_unit_counts,
+                                             nullptr, nullptr, d_status, L));
+    KVSMC_CUDA(ctx, kvsmc::launch_unit_scan(d_groups, (int)groups.size(), scan_blocks, d_isos, d_unit_counts,
+                                            d_unit_offsets, d_plane_totals, L));
+    KVSMC_CUDA(ctx, kvsmc::launch_scan(d_plane_totals, d_plane_base, iso_planes, d_scan, d_total, L));
+    KVSMC_CUDA(ctx, kvsmc::launch_iso_totals(d_isos, (int)isos.size(), d_plane_base, d_total, d_totals, L));
     // read back: status word, then one total per isolevel
     const size_t n = isos.size();
     kvsmc_status st = ensure_stage(ctx, (n + 2) * 8);
@@ -249,8 +253,8 @@ kvsmc_status StreamBatch::emit()
     if (st) return st;
     const kvsmc::Launch L = launch_of(ctx);
     for (const Launch1& l : launches)
-        KVSMC_CUDA(ctx, kvsmc::launch_stream(true, l.dtype, d_groups + l.g0, l.ng, l.nctas, l.smem_emit, d_isos,
-                                             nullptr, d_offsets, d_status, L));
+        KVSMC_CUDA(ctx, kvsmc::launch_stream(true, l.dtype, d_groups + l.g0, l.ng, l.ntasks, d_isos, nullptr,
+                                             d_unit_offsets, d_plane_base, d_status, L));
     return KVSMC_OK;
 }
 

@@ -44,39 +44,50 @@ cudaError_t launch_connect(const Job& j, const Launch& L);
 cudaError_t launch_vertex_normals(const Job& j, const Launch& L);
 
 // ---- streaming kernels (mc_stream.cu): duplicated mode, batched
-constexpr int kStreamThreads = 512;   // 16 warps
+constexpr int kStreamThreads = 256;   // 8 independent warps per CTA
 constexpr int kStreamMaxIso = 16;     // isolevels of one volume per group
 constexpr int kStreamBuckets = 256;   // threshold lookup buckets
 constexpr int kStreamSegCells = 256;  // cells per warp segment
-constexpr int kStreamMaxWarpsPerRow = 16;
+constexpr int kStreamMaxSegments = 16;  // segments per row (width <= 4096 cells)
 
 // One isolevel request inside a streaming launch.
 struct StreamIso {
     FastIso f;
     Interp ip;
-    uint64_t count_base;   // first slot of its tiles in the concatenated count/offset arrays
+    uint64_t plane_index;  // its first (isolevel, z) plane in the plane arrays
     float* coords;         // outputs (null: not written)
     float* normals;
 };
 
 // One volume with up to kStreamMaxIso isolevels, sorted by threshold.
+// Warp tasks (z-chunk, row y, segment) are numbered segment fastest, then y,
+// then z-chunk; units (z, y, segment) likewise, each with niso counters.
 struct StreamGroup {
     VolumeView vol;
     int32_t iso_begin, niso;
-    uint32_t wpr;          // warps (256-cell segments) per cell row
-    uint32_t rows;         // cell rows per y-tile
-    uint32_t ytiles;
-    uint32_t zchunk;       // cell planes per CTA
-    uint32_t cta_begin;    // first CTA of this group in its launch
-    float bt0, bscale;     // bucket(v) = clamp(floor((v - bt0) * bscale), -1, kStreamBuckets + 1)
-    uint64_t plane_elems;  // elements per staged node plane (rows+1 rows + slack)
+    uint32_t wpr;            // 256-cell segments per cell row
+    uint32_t zchunk;         // cell planes per warp task
+    uint64_t task_begin;     // first warp task of this group in its launch
+    uint64_t unit_base;      // first element of its (unit, isolevel) counters
+    uint32_t plane_begin;    // first unit-scan block of this group (one per z)
+    uint32_t seg_elems;      // staged elements per node row (16-byte multiple)
+    uint32_t seg_copy_bytes; // bytes copied per node row (last segment: fewer)
+    uint32_t warp_smem_bytes;
+    uint32_t warp_smem_offset;
+    float bt0, bscale;       // bucket(v) = clamp(floor((v - bt0) * bscale), -1, kStreamBuckets + 1)
 };
 
-size_t stream_shared_bytes(size_t plane_bytes, bool emit);
-cudaError_t launch_stream(bool emit, int dtype, const StreamGroup* d_groups, int ngroups, uint32_t nctas,
-                          size_t smem_bytes, const StreamIso* d_isos, uint32_t* d_counts, const uint64_t* d_offsets,
-                          int* d_status, const Launch& L);
-cudaError_t launch_iso_totals(const StreamIso* d_isos, int n, const uint64_t* d_offsets, const uint64_t* d_total,
+size_t stream_shared_bytes(int dtype, bool emit);
+size_t stream_warp_smem_bytes(int dtype, bool emit);
+size_t stream_warp_smem_offset();
+size_t stream_row_elems(int dtype);
+cudaError_t launch_stream(bool emit, int dtype, const StreamGroup* d_groups, int ngroups, uint64_t ntasks,
+                          const StreamIso* d_isos, uint16_t* d_unit_counts, const uint32_t* d_unit_offsets,
+                          const uint64_t* d_plane_base, int* d_status, const Launch& L);
+cudaError_t launch_unit_scan(const StreamGroup* d_groups, int ngroups, uint32_t nplanes, const StreamIso* d_isos,
+                             const uint16_t* d_unit_counts, uint32_t* d_unit_offsets, uint32_t* d_plane_totals,
+                             const Launch& L);
+cudaError_t launch_iso_totals(const StreamIso* d_isos, int n, const uint64_t* d_plane_base, const uint64_t* d_total,
                               uint64_t* d_totals, const Launch& L);
 
 // ---- diagnostics (selftest.cu)

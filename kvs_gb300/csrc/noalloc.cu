@@ -13,7 +13,8 @@
 // g_noalloc_scratch, a file-scope __device__ array of kNoAllocScratchBytes
 // (4 MiB).  Every GPU that loads this library holds that array until the
 // process exits.  A request whose intermediates do not fit is refused with
-// KVSMC_ERR_TOO_LARGE (the limit covers volumes up to about 1024^3 float32).
+// KVSMC_ERR_TOO_LARGE (the limit covers volumes up to about 512^3: one u16
+// count and one u32 offset per 256-cell row piece).
 //
 // In host code the name g_noalloc_scratch is only a host-side stand-in, not
 // a device address, so the device address is looked up with
@@ -87,7 +88,7 @@ extern "C" kvsmc_status kvsmc_extract_noalloc(const void* d_values, kvsmc_dtype 
         return KVSMC_ERR_UNSUPPORTED_DTYPE;
     const size_t es = dtype_size(dtype);
     // rows are staged with bulk copies: they must start on 16-byte boundaries
-    if (nx < 2 || ny < 2 || nz < 2 || nx - 1 > (uint32_t)(kStreamMaxWarpsPerRow * kStreamSegCells) ||
+    if (nx < 2 || ny < 2 || nz < 2 || nx - 1 > (uint32_t)(kStreamMaxSegments * kStreamSegCells) ||
         (reinterpret_cast<uintptr_t>(d_values) & 15u) || ((size_t)nx * es) % 16 != 0 || !std::isfinite(p->isolevel) ||
         std::fabs(p->isolevel) > 1.0e30)
         return KVSMC_ERR_INVALID_ARGUMENT;
@@ -111,25 +112,32 @@ extern "C" kvsmc_status kvsmc_extract_noalloc(const void* d_values, kvsmc_dtype 
     StreamGroup g;
     std::memset(&g, 0, sizeof g);
     g.vol = v;
-    kvsmc_host::tiling(v, g.wpr, g.rows, g.plane_elems);
-    const size_t smem_emit = stream_shared_bytes(g.plane_elems * es, true);
-    if (smem_emit > (size_t)227 * 1024) return KVSMC_ERR_TOO_LARGE;
+    g.wpr = (nx - 1 + kStreamSegCells - 1) / kStreamSegCells;
+    if (stream_shared_bytes(dtype, true) > (size_t)227 * 1024 ||
+        (double)(nx - 1) * (double)(ny - 1) * 5.0 >= 4294967295.0)
+        return KVSMC_ERR_TOO_LARGE;
     const uint32_t cy = ny - 1, cz = nz - 1;
-    g.ytiles = (cy + g.rows - 1) / g.rows;
-    const uint32_t want = (uint32_t)((2 * num_sms + g.ytiles - 1) / g.ytiles);
-    uint32_t zc = (cz + (want ? want : 1) - 1) / (want ? want : 1);
-    g.zchunk = zc < 4 ? 4 : (zc > 32 ? 32 : zc);
-    const uint32_t nctas = g.ytiles * ((cz + g.zchunk - 1) / g.zchunk);
-    const uint64_t tiles = (uint64_t)cz * g.ytiles;
+    g.zchunk = kvsmc_host::stream_zchunk(v, g.wpr, num_sms);
+    const uint64_t ntasks = (uint64_t)cy * g.wpr * ((cz + g.zchunk - 1) / g.zchunk);
+    const uint64_t units = (uint64_t)cz * cy * g.wpr;   // one isolevel: one counter per unit
+    g.task_begin = 0;
+    g.unit_base = 0;
+    g.plane_begin = 0;
+    g.seg_elems = (uint32_t)stream_row_elems(dtype);
+    g.seg_copy_bytes = g.seg_elems * (uint32_t)es;
+    g.warp_smem_bytes = (uint32_t)stream_warp_smem_bytes(dtype, true);
+    g.warp_smem_offset = (uint32_t)stream_warp_smem_offset();
 
     // carve the static array
     size_t off = 0;
     auto take = [&](size_t bytes) { char* q = scratch + off; off = align_up(off + bytes, 256); return q; };
     StreamGroup* d_group = reinterpret_cast<StreamGroup*>(take(sizeof(StreamGroup)));
     StreamIso* d_iso = reinterpret_cast<StreamIso*>(take(sizeof(StreamIso)));
-    uint32_t* d_counts = reinterpret_cast<uint32_t*>(take(tiles * 4));
-    uint64_t* d_offsets = reinterpret_cast<uint64_t*>(take(tiles * 8));
-    void* d_scan = take(scan_scratch_bytes(tiles));
+    uint16_t* d_unit_counts = reinterpret_cast<uint16_t*>(take(units * 2));
+    uint32_t* d_unit_offsets = reinterpret_cast<uint32_t*>(take(units * 4));
+    uint32_t* d_plane_totals = reinterpret_cast<uint32_t*>(take((size_t)cz * 4));
+    uint64_t* d_plane_base = reinterpret_cast<uint64_t*>(take((size_t)cz * 8));
+    void* d_scan = take(scan_scratch_bytes(cz));
     uint64_t* d_totals = reinterpret_cast<uint64_t*>(take(8));
     uint64_t* d_total = reinterpret_cast<uint64_t*>(take(8));
     int* d_status = reinterpret_cast<int*>(take(sizeof(int)));
@@ -160,25 +168,23 @@ extern "C" kvsmc_status kvsmc_extract_noalloc(const void* d_values, kvsmc_dtype 
     iso.ip.vmin = vmin;
     iso.ip.vmax = vmax;
     for (int k = 0; k < 3; ++k) { iso.ip.min_coord[k] = p->min_coord[k]; iso.ip.scale[k] = p->scale[k]; }
-    iso.count_base = 0;
+    iso.plane_index = 0;
     g.iso_begin = 0;
     g.niso = 1;
-    g.cta_begin = 0;
-    g.bt0 = iso.f.f_thr;
-    g.bscale = 1.0f / (1.0f + std::fabs(g.bt0));
-    if (!(g.bscale > 0.0f) || !std::isfinite(g.bscale)) g.bscale = 1.0f;
+    kvsmc_host::bucket_params(iso.f.f_thr, iso.f.f_thr, g.bt0, g.bscale);
 
-    // count -> scan -> total
+    // count -> unit scan -> plane scan -> total
     const int zero = 0;
     uint64_t total = 0;
     int status = 0;
     if (cudaMemcpyAsync(d_group, &g, sizeof g, cudaMemcpyHostToDevice, s) != cudaSuccess ||
         cudaMemcpyAsync(d_iso, &iso, sizeof iso, cudaMemcpyHostToDevice, s) != cudaSuccess ||
         cudaMemcpyAsync(d_status, &zero, sizeof zero, cudaMemcpyHostToDevice, s) != cudaSuccess ||
-        launch_stream(false, dtype, d_group, 1, nctas, stream_shared_bytes(g.plane_elems * es, false), d_iso,
-                      d_counts, d_offsets, d_status, L) != cudaSuccess ||
-        launch_scan(d_counts, d_offsets, tiles, d_scan, d_total, L) != cudaSuccess ||
-        launch_iso_totals(d_iso, 1, d_offsets, d_total, d_totals, L) != cudaSuccess ||
+        launch_stream(false, dtype, d_group, 1, ntasks, d_iso, d_unit_counts, nullptr, nullptr, d_status, L) !=
+            cudaSuccess ||
+        launch_unit_scan(d_group, 1, cz, d_iso, d_unit_counts, d_unit_offsets, d_plane_totals, L) != cudaSuccess ||
+        launch_scan(d_plane_totals, d_plane_base, cz, d_scan, d_total, L) != cudaSuccess ||
+        launch_iso_totals(d_iso, 1, d_plane_base, d_total, d_totals, L) != cudaSuccess ||
         cudaMemcpyAsync(&total, d_totals, sizeof total, cudaMemcpyDeviceToHost, s) != cudaSuccess ||
         cudaMemcpyAsync(&status, d_status, sizeof status, cudaMemcpyDeviceToHost, s) != cudaSuccess ||
         cudaStreamSynchronize(s) != cudaSuccess)
@@ -196,7 +202,7 @@ extern "C" kvsmc_status kvsmc_extract_noalloc(const void* d_values, kvsmc_dtype 
     iso.coords = d_coords;
     iso.normals = d_normals;
     if (cudaMemcpyAsync(d_iso, &iso, sizeof iso, cudaMemcpyHostToDevice, s) != cudaSuccess ||
-        launch_stream(true, dtype, d_group, 1, nctas, smem_emit, d_iso, nullptr, d_offsets, d_status, L) !=
+        launch_stream(true, dtype, d_group, 1, ntasks, d_iso, nullptr, d_unit_offsets, d_plane_base, d_status, L) !=
             cudaSuccess ||
         cudaMemcpyAsync(&status, d_status, sizeof status, cudaMemcpyDeviceToHost, s) != cudaSuccess ||
         cudaStreamSynchronize(s) != cudaSuccess)
