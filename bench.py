@@ -8,7 +8,7 @@ volume: the fused count launch, the scan, the fused emit launch, with output
 written to HBM.  `value` = cells x isovalues / s (Mcells/s).
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
-                    [--workload sweep1024|blobs128]
+                    [--workload sweep1024|sweep384|blobs128]
 
 --impl reference times the reference's CPU algorithm on this host's cores: the
 C restatement under oracle/ (the reference sources are not present on the GPU
@@ -33,6 +33,9 @@ WORKLOADS = {
     "sweep1024": dict(shape=(1024, 1024, 1024), kind="fbm", isos=[0.2 + 0.04 * k for k in range(16)],
                       desc="1024^3 float32 fBm gradient noise (5 octaves, base freq 1/128, gain 0.5, in [0,1]), "
                            "16 isovalues 0.2..0.8 in one batched call, duplication=true, PolygonNormal"),
+    "sweep384": dict(shape=(384, 384, 384), kind="fbm", isos=[0.2 + 0.04 * k for k in range(16)],
+                     desc="384^3 float32 fBm gradient noise (as sweep1024), 16 isovalues 0.2..0.8 in one batched "
+                          "call, duplication=true, PolygonNormal (the profiling case)"),
     "blobs128": dict(shape=(128, 128, 128), kind="blobs", isos=[0.5],
                      desc="128^3 float32, 4 Gaussian blobs (sigma 8..24) + U[-0.01,0.01] noise, iso 0.5, "
                           "duplication=true, PolygonNormal"),
@@ -245,7 +248,8 @@ def run_ours(args, rank, world, local):
         "data": "synthetic (seeded fBm generated on the device)",
         "config": {"workload": w["desc"], "volume": [nx, ny, nz], "isovalues": n,
                    "mode": "duplication+PolygonNormal", "cache": "inputs larger than L2 (4 GiB volume, "
-                   "outputs ~48 B/triangle)" if args.workload == "sweep1024" else "input smaller than L2"},
+                   "outputs ~48 B/triangle)" if args.workload == "sweep1024" else (
+                   "inputs larger than L2 (216 MiB volume)" if args.workload == "sweep384" else "input smaller than L2")},
         "mtris_per_s": round(ntri * world / (step_ms * 1e-3) / 1e6, 1),
         "triangles_per_step": int(ntri),
         "roofline": roofline,
@@ -340,7 +344,7 @@ def run_reference(args, rank, world):
         return None
     w = WORKLOADS[args.workload]
     threads = os.cpu_count() or 1
-    planes = 65 if args.workload == "sweep1024" else w["shape"][0]
+    planes = min(65, w["shape"][0]) if w["kind"] == "fbm" else w["shape"][0]
     isos = w["isos"]
     vals = []
     sample = ""
@@ -384,9 +388,9 @@ def main():
     else:
         line = run_ours(args, rank, world, local)
         if rank == 0 and world == 1 and not args.no_cpu:
-            planes = 65 if args.workload == "sweep1024" else WORKLOADS[args.workload]["shape"][0]
-            isos = WORKLOADS[args.workload]["isos"] if args.workload == "sweep1024" else \
-                WORKLOADS[args.workload]["isos"] * 50
+            w = WORKLOADS[args.workload]
+            planes = min(65, w["shape"][0]) if w["kind"] == "fbm" else w["shape"][0]
+            isos = w["isos"] if w["kind"] == "fbm" else w["isos"] * 50
             v, t, sample = run_cpu(args, 1, planes, isos)
             line["cpu_baseline"] = {"value": round(v, 1), "unit": "Mcells/s", "cores": 1, "kind": "port",
                                     "sample": sample + f"; {t:.1f} s on 1 host core; oracle/mc_oracle.c"}

@@ -55,12 +55,22 @@ kvsmc::FastIso make_fast(double iso, double vmin, double vmax, int dtype)
     return f;
 }
 
-void bucket_params(float t0, float t1, float& bt0, float& bscale)
+void bucket_params(float t0, float t1, float& bs, float& bo)
 {
-    const float span = t1 - t0;
-    bt0 = t0;
-    bscale = (span > 0.0f && std::isfinite(span)) ? (float)kvsmc::kStreamBuckets / span : 1.0f / (1.0f + std::fabs(t0));
-    if (!(bscale > 0.0f) || !std::isfinite(bscale)) bscale = 1.0f;
+    // Any finite bs > 0 and finite bo give a monotone bucket map (which is all
+    // the kernels rely on); these spread the thresholds [t0, t1] over buckets
+    // 1 .. kStreamBuckets - 1.
+    const double nb = (double)kvsmc::kStreamBuckets;
+    const double span = (double)t1 - (double)t0;
+    double s = (span > 0.0 && std::isfinite(span)) ? (1.0 - 2.0 / nb) / span : 1.0 / (1.0 + std::fabs((double)t0));
+    if (!(s > 1.0e-30) || !(s < 1.0e30)) s = 1.0 / (1.0 + std::fabs((double)t0));
+    double o = 1.0 / nb - (double)t0 * s;
+    bs = (float)s;
+    bo = (float)o;
+    if (!(bs > 0.0f) || !std::isfinite(bs) || !std::isfinite(bo)) {
+        bs = 1.0f;
+        bo = 0.0f;
+    }
 }
 
 uint32_t stream_zchunk(const kvsmc::VolumeView& v, uint32_t wpr, int num_sms)
@@ -141,7 +151,7 @@ kvsmc_status StreamBatch::plan()
                              [](const std::pair<float, Item*>& a, const std::pair<float, Item*>& b) { return a.first < b.first; });
             g.iso_begin = (int32_t)isos.size();
             g.niso = (int32_t)sorted.size();
-            bucket_params(sorted.front().first, sorted.back().first, g.bt0, g.bscale);
+            bucket_params(sorted.front().first, sorted.back().first, g.bs, g.bo);
             g.unit_base = unit_elems;
             unit_elems += (uint64_t)cz * cy * g.wpr * g.niso;
             g.plane_begin = scan_blocks;

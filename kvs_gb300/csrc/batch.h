@@ -9,7 +9,7 @@ namespace kvsmc_host {
 kvsmc::FastIso make_fast(double iso, double vmin, double vmax, int dtype);
 
 // Bucket parameters of a group's sorted thresholds.
-void bucket_params(float t0, float t1, float& bt0, float& bscale);
+void bucket_params(float t0, float t1, float& bs, float& bo);
 
 // Cell planes per warp task for a volume (enough tasks to fill the GPU, at
 // most 64 planes so the one-plane halo of a task stays small).

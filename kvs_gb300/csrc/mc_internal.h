@@ -74,7 +74,7 @@ struct StreamGroup {
     uint32_t seg_copy_bytes; // bytes copied per node row (last segment: fewer)
     uint32_t warp_smem_bytes;
     uint32_t warp_smem_offset;
-    float bt0, bscale;       // bucket(v) = clamp(floor((v - bt0) * bscale), -1, kStreamBuckets + 1)
+    float bs, bo;            // bucket(v) = floor(kStreamBuckets * sat(v * bs + bo)), in [0, kStreamBuckets]
 };
 
 size_t stream_shared_bytes(int dtype, bool emit);

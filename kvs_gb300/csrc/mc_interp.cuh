@@ -125,6 +125,14 @@ __device__ __forceinline__ bool fast_axis(float v0, float v1, float a, float b, 
     return true;
 }
 
+// The FP64 sequence, kept out of line: it runs for about one vertex in 10^5
+// and would otherwise hold FP64 registers in the hot loop.
+static __device__ __noinline__ float3 interpolate_exact_slow(const Interp& j, float va, float vb, float ax, float ay,
+                                                             float az, float bx, float by, float bz)
+{
+    return interpolate_exact(j, (double)va, (double)vb, ax, ay, az, bx, by, bz);
+}
+
 // Vertex of an edge whose endpoints differ along `axis` (0, 1, 2): A = (ax,
 // ay, az) with value va, B with value vb (both raw values as float).  `j`
 // carries the FP64 constants for the fallback.  Output after the
@@ -133,27 +141,27 @@ __device__ __forceinline__ float3 edge_vertex_fast(const Interp& j, const FastIs
                                                    float ax, float ay, float az, float bx, float by, float bz,
                                                    int axis)
 {
-    float px = ax, py = ay, pz = az;
     bool ok = f.fast_ok != 0;
+    float r = 0.0f;
     if (ok) {
         const float v0 = clampf_ref(va, f.vmin_f, f.vmax_f);
         const float v1 = clampf_ref(vb, f.vmin_f, f.vmax_f);
         ok = (v0 > f.f_thr) != (v1 > f.f_thr);
-        if (ok) {
-            float r;
-            if (axis == 0) ok = fast_axis(v0, v1, ax, bx, f, r), px = r;
-            else if (axis == 1) ok = fast_axis(v0, v1, ay, by, f, r), py = r;
-            else ok = fast_axis(v0, v1, az, bz, f, r), pz = r;
-        }
+        // one inlined copy of the varying-axis computation for all three axes
+        // (lanes of a warp interpolate edges of different directions)
+        const float a = axis == 0 ? ax : (axis == 1 ? ay : az);
+        const float b = axis == 0 ? bx : (axis == 1 ? by : bz);
+        if (ok) ok = fast_axis(v0, v1, a, b, f, r);
     }
     if (ok) {
+        const float px = axis == 0 ? r : ax, py = axis == 1 ? r : ay, pz = axis == 2 ? r : az;
         float3 o;
         o.x = __fmul_rn(__fadd_rn(px, j.min_coord[0]), j.scale[0]);
         o.y = __fmul_rn(__fadd_rn(py, j.min_coord[1]), j.scale[1]);
         o.z = __fmul_rn(__fadd_rn(pz, j.min_coord[2]), j.scale[2]);
         return o;
     }
-    return interpolate_exact(j, (double)va, (double)vb, ax, ay, az, bx, by, bz);
+    return interpolate_exact_slow(j, va, vb, ax, ay, az, bx, by, bz);
 }
 
 }  // namespace kvsmc

@@ -9,11 +9,13 @@
 //     a per-buffer mbarrier), so a plane is read from HBM once per pass and
 //     the next one is in flight while the warp works.  No CTA-wide barrier:
 //     warps never wait for each other.
-//   * Each lane owns 8 consecutive cells.  Per cell: min/max of the 8 corners
-//     and the range [lo, hi) of isolevels (sorted by threshold) for which
-//     min <= t < max -- exactly the isolevels for which the cell has a
-//     surface -- from a monotone bucket table plus exact compares.  Only
-//     active (cell, isolevel) pairs are classified further.
+//   * Classification works on each node's isolevel index q = #{thresholds < v}
+//     (isolevels sorted by threshold; a monotone bucket table plus exact
+//     compares in the rare shared bucket).  Since v > t_k exactly when q > k,
+//     a cell is active for isolevel k exactly when min(q) <= k < max(q) over
+//     its 8 corners, and its case bits are (q_c > k).  Each lane owns 8
+//     consecutive cells; q of the new plane's nodes is computed once per
+//     step and carried (packed bytes) to the next step.
 //   * A "unit" = (z, y, segment): a contiguous piece of the reference's linear
 //     cell order.  The count kernel writes one u16 triangle count per (unit,
 //     isolevel); the unit-scan kernel turns them into u32 offsets inside each
@@ -21,12 +23,14 @@
 //     gives each plane's first triangle.  So an emitting warp knows where its
 //     unit's triangles start for every isolevel without talking to any other
 //     warp.
-//   * Emit: the warp compacts its active pairs (warp scan), groups lanes by
-//     isolevel with __match_any_sync (per-isolevel offsets from bit-sliced
-//     ballots), interpolates each pair's edges once (one lane per edge, the
-//     exact FP32 path of mc_interp.cuh), then writes each triangle (one lane
-//     per triangle) at its position: cells in linear order, table order
-//     inside a cell, each isolevel into its own arrays.
+//   * Emit: the warp compacts its active pairs in (cell, isolevel) order (warp
+//     scan), then takes them 32 at a time, one pair per lane: lanes of the
+//     same isolevel are grouped with __match_any_sync and bit-sliced ballots
+//     give each pair's output position; each lane interpolates its pair's
+//     edges once (the exact FP32 path of mc_interp.cuh) into its own column
+//     of a shared-memory vertex table and writes the pair's triangles, cells
+//     in linear order, table order inside a cell, each isolevel into its own
+//     arrays.
 #include <cuda_runtime.h>
 
 #include "mc_internal.h"
@@ -40,8 +44,6 @@ constexpr int kWarps = kStreamThreads / 32;
 constexpr int kLaneCells = 8;
 constexpr int kSegCells = 32 * kLaneCells;
 constexpr int kPairCap = 128;   // pair buffer entries per warp
-constexpr int kEdgeCap = 96;    // vertex slots per warp and round
-constexpr int kTriCap = 160;    // triangles per round (32 pairs x 5)
 constexpr unsigned FULL = 0xffffffffu;
 
 __constant__ uint64_t c_tri_packed[256] = MC_TRI_PACKED_INIT;
@@ -150,9 +152,17 @@ template <> __device__ __forceinline__ void load8<int8_t>(const int8_t* row, uin
 
 // ------------------------------------------------------------ shared layout
 
-// Per-CTA tables (filled once, read-only afterwards).
+constexpr int kLut = kStreamBuckets + 1;   // bucket indices 0 .. kStreamBuckets
+constexpr uint32_t kHasThr = 1u << 16;     // LUT flag: a threshold lies in this bucket
+constexpr int kMaxVerts = 32 * 12;         // vertex items of one round (12 edges per pair at most)
+constexpr int kMaxTris = 32 * 5;           // triangle items of one round (5 per pair at most)
+
+// Per-CTA tables, indexed by the corner code of case_code() (not by the
+// reference's case number: the code -> case permutation is applied when the
+// tables are filled).
 struct Tables {
-    uint64_t tri_packed[256];
+    uint64_t tri_packed[256];   // edges per triangle, emission order, 4 bits each
+    uint64_t edge_list[256];    // the used edges in increasing order, 4 bits each
     uint16_t edge_mask[256];
     uint8_t ntri[256];
     uint8_t edge_packed[16];
@@ -165,47 +175,97 @@ struct WarpState {
     int32_t thr_bucket[kStreamMaxIso];
     uint32_t cnt[kStreamMaxIso];             // count: triangles of the current unit
     uint32_t add[kStreamMaxIso];             // emit: per-isolevel advance of the current round
-    uint8_t bucket[kStreamBuckets + 3];
+    // bucket -> thermometer mask of the thresholds in lower buckets, plus kHasThr
+    uint32_t lut[kLut];
 };
 
+// Per-warp emit buffers: the unit's pairs, and for one round the vertex pool
+// (one entry per (pair, used edge)) and the item -> pair maps.
 struct WarpEmit {
     uint32_t pairs[kPairCap];
-    uint16_t edge_map[kEdgeCap];             // vertex slot -> pair lane | edge rank << 5
-    uint8_t tri_map[kTriCap];                // triangle of the round -> pair lane | index << 5
-    float3 vtx[kEdgeCap];
+    float px[kMaxVerts], py[kMaxVerts], pz[kMaxVerts];
+    uint8_t item_v[kMaxVerts];
+    uint8_t item_t[kMaxTris];
 };
 
 __host__ __device__ __forceinline__ size_t align128(size_t v) { return (v + 127) / 128 * 128; }
 
-// Monotone (non-decreasing) bucket of a value; thresholds and cell values go
-// through exactly this function, so #{t < v} = #{t in lower buckets} + the
-// exact compares inside v's own bucket.
-__device__ __forceinline__ int bucket_of(const StreamGroup& G, float v)
+// Monotone (non-decreasing) bucket of a value in [0, kStreamBuckets]:
+// floor(kStreamBuckets * sat(v * bs + bo)).  Thresholds and node values go
+// through exactly this function, so a threshold in a lower bucket than v is
+// below v, one in a higher bucket is not, and only a shared bucket needs an
+// exact compare.  NaN saturates to 0 (the fma's .sat flushes NaN to +0): it
+// is above no threshold, as in the reference's double compare.
+__device__ __forceinline__ uint32_t bucket_index(float v, float bs, float bo)
 {
-    float fb = floorf(__fmul_rn(__fsub_rn(v, G.bt0), G.bscale));
-    if (!(fb >= -1.0f)) fb = -1.0f;
-    if (fb > (float)(kStreamBuckets + 1)) fb = (float)(kStreamBuckets + 1);
-    return (int)fb;
+    float u;
+    asm("fma.rn.sat.f32 %0, %1, %2, %3;" : "=f"(u) : "f"(v), "f"(bs), "f"(bo));
+    // u * NB + 2^23 rounded down: 2^23 + floor(u * NB) exactly
+    const float t = __fmaf_rd(u, (float)kStreamBuckets, 8388608.0f);
+    return (uint32_t)__float_as_int(t) - 0x4B000000u;
 }
 
-// Number of thresholds strictly below v.
-__device__ __forceinline__ int count_below(const WarpState& W, int niso, const StreamGroup& G, float v)
+// Thermometer masks of the 9 nodes x0 .. x0+8 of a staged row: bit k set when
+// the value is above isolevel k's threshold (v > t_k; thresholds sorted, so
+// the set bits are 0 .. q-1), packed two nodes per word (node 2m in the low
+// half of word m, node 2m+1 in the high half; word 4 holds node 8).
+template <typename T>
+__device__ __forceinline__ void row_masks(const T* row, uint32_t x0, const WarpState& W, int niso, float bs, float bo,
+                                          uint32_t* P)
 {
-    const int b = bucket_of(G, v);
-    const unsigned e = W.bucket[b + 1];
-    int k = (int)(e & 0x3fu);
-    if (e & 0x80u) {
-        while (k < niso && W.thr_bucket[k] == b && W.thr[k] < v) ++k;
+    float v[9];
+    load8<T>(row, x0, v);
+    v[8] = (float)row[x0 + 8];
+    uint32_t e[9];
+    uint32_t any = 0;
+#pragma unroll
+    for (int i = 0; i < 9; ++i) {
+        e[i] = W.lut[bucket_index(v[i], bs, bo)];
+        any |= e[i];
     }
-    return k;
+    if (any & kHasThr) {
+        // a node shares its bucket with a threshold: exact compares there
+#pragma unroll
+        for (int i = 0; i < 9; ++i) {
+            if (e[i] & kHasThr) {
+                const int b = (int)bucket_index(v[i], bs, bo);
+                int k = __popc(e[i] & 0xffffu);
+                while (k < niso && W.thr_bucket[k] == b && W.thr[k] < v[i]) ++k;
+                e[i] = (1u << k) - 1u;
+            }
+        }
+    }
+    P[0] = __byte_perm(e[0], e[1], 0x5410);
+    P[1] = __byte_perm(e[2], e[3], 0x5410);
+    P[2] = __byte_perm(e[4], e[5], 0x5410);
+    P[3] = __byte_perm(e[6], e[7], 0x5410);
+    P[4] = e[8];
 }
 
-__device__ __forceinline__ unsigned case_of(const float* a0, const float* a1, const float* b0, const float* b1, int i,
-                                            float t)
+// The row word of cell i (0..7): node i in the low half, node i+1 in the high half.
+__device__ __forceinline__ uint32_t cell_word(const uint32_t* P, int i)
 {
-    return (a0[i] > t ? 1u : 0u) | (a0[i + 1] > t ? 2u : 0u) | (a1[i + 1] > t ? 4u : 0u) | (a1[i] > t ? 8u : 0u) |
-           (b0[i] > t ? 16u : 0u) | (b0[i + 1] > t ? 32u : 0u) | (b1[i + 1] > t ? 64u : 0u) |
-           (b1[i] > t ? 128u : 0u);
+    return (i & 1) ? __funnelshift_r(P[i >> 1], P[(i >> 1) + 1], 16) : P[i >> 1];
+}
+
+// Corner code of a cell for isolevel k from its four row words (plane z rows
+// y, y+1 = a0, a1; plane z+1 = b0, b1): bit r = row r's node i above, bit
+// 4 + r = row r's node i+1 above.
+__device__ __forceinline__ uint32_t case_code(uint32_t a0, uint32_t a1, uint32_t b0, uint32_t b1, uint32_t k)
+{
+    const uint32_t m0 = (a0 >> k) & 0x10001u, m1 = (a1 >> k) & 0x10001u;
+    const uint32_t m2 = (b0 >> k) & 0x10001u, m3 = (b1 >> k) & 0x10001u;
+    const uint32_t x = m0 | (m1 << 1) | (m2 << 2) | (m3 << 3);
+    return (x & 0xfu) | ((x >> 12) & 0xf0u);
+}
+
+// The reference's case number of a corner code: bit c = corner c above, with
+// corners (x,y,z) 0:(0,0,0) 1:(1,0,0) 2:(1,1,0) 3:(0,1,0) 4:(0,0,1) 5:(1,0,1)
+// 6:(1,1,1) 7:(0,1,1) (MarchingCubes.cpp:187-194).
+__device__ __forceinline__ uint32_t code_to_case(uint32_t c)
+{
+    return (c & 1u) | (((c >> 4) & 1u) << 1) | (((c >> 5) & 1u) << 2) | (((c >> 1) & 1u) << 3) |
+           (((c >> 2) & 1u) << 4) | (((c >> 6) & 1u) << 5) | (((c >> 7) & 1u) << 6) | (((c >> 3) & 1u) << 7);
 }
 
 __device__ __forceinline__ uint32_t warp_inclusive_scan(uint32_t v, unsigned lane)
@@ -230,7 +290,7 @@ __device__ __forceinline__ int find_group(const StreamGroup* groups, int ngroups
 }
 
 template <typename T, bool EMIT>
-__global__ void __launch_bounds__(kStreamThreads)
+__global__ void __launch_bounds__(kStreamThreads, EMIT ? 2 : 3)
     k_stream(const StreamGroup* __restrict__ groups, int ngroups, uint64_t ntasks, const StreamIso* __restrict__ isos,
              uint16_t* __restrict__ unit_counts, const uint32_t* __restrict__ unit_offsets,
              const uint64_t* __restrict__ plane_base, int* __restrict__ status)
@@ -238,11 +298,20 @@ __global__ void __launch_bounds__(kStreamThreads)
     extern __shared__ __align__(128) unsigned char smem_raw[];
     const unsigned tid = threadIdx.x, lane = tid & 31u, warp = tid >> 5;
     Tables& TB = *reinterpret_cast<Tables*>(smem_raw);
-    for (unsigned i = tid; i < 256; i += blockDim.x) {
-        TB.tri_packed[i] = c_tri_packed[i];
-        TB.ntri[i] = c_ntri[i];
-        TB.edge_mask[i] = c_edge_mask[i];
-        if (i < 12) TB.edge_packed[i] = c_edge_packed[i];
+    for (unsigned code = tid; code < 256; code += blockDim.x) {
+        const uint32_t cs = code_to_case(code);
+        TB.ntri[code] = c_ntri[cs];
+        const uint32_t em = c_edge_mask[cs];
+        TB.edge_mask[code] = (uint16_t)em;
+        if (EMIT) {
+            TB.tri_packed[code] = c_tri_packed[cs];
+            uint64_t list = 0;
+            int n = 0;
+            for (int e = 0; e < 12; ++e)
+                if ((em >> e) & 1u) list |= (uint64_t)e << (4 * n++);
+            TB.edge_list[code] = list;
+        }
+        if (code < 12) TB.edge_packed[code] = c_edge_packed[code];
     }
     __syncthreads();   // the only CTA-wide barrier: tables are read-only from here on
 
@@ -251,45 +320,50 @@ __global__ void __launch_bounds__(kStreamThreads)
     const StreamGroup& G = groups[find_group(groups, ngroups, task)];
     const uint64_t local = task - G.task_begin;
     const uint32_t cx = G.vol.nx - 1, cy = G.vol.ny - 1, cz = G.vol.nz - 1;
-    const uint32_t seg = (uint32_t)(local % G.wpr);
-    const uint32_t y = (uint32_t)((local / G.wpr) % cy);
-    const uint32_t zc = (uint32_t)(local / ((uint64_t)G.wpr * cy));
+    const uint32_t wpr = G.wpr;
+    const uint32_t seg = (uint32_t)(local % wpr);
+    const uint32_t y = (uint32_t)((local / wpr) % cy);
+    const uint32_t zc = (uint32_t)(local / ((uint64_t)wpr * cy));
     const uint32_t z0 = zc * G.zchunk;
     const uint32_t z1 = (z0 + G.zchunk < cz) ? z0 + G.zchunk : cz;   // cell planes [z0, z1)
     const int niso = G.niso;
+    const float bs = G.bs, bo = G.bo;
+    const int iso_begin = G.iso_begin;
+    const uint64_t unit_base = G.unit_base;
 
     // per-warp shared memory: state, then (emit) buffers, then the row ring
     // (the same layout as stream_warp_smem_bytes on the host)
+    const uint32_t row_elems = G.seg_elems;              // staged elements per row
     const size_t wstride = align128(sizeof(WarpState)) + (EMIT ? align128(sizeof(WarpEmit)) : 0) +
-                           align128((size_t)3 * 2 * G.seg_elems * sizeof(T));
+                           align128((size_t)3 * 2 * row_elems * sizeof(T));
     unsigned char* wbase = smem_raw + align128(sizeof(Tables)) + (size_t)warp * wstride;
     WarpState& W = *reinterpret_cast<WarpState*>(wbase);
     WarpEmit* WE = reinterpret_cast<WarpEmit*>(wbase + align128(sizeof(WarpState)));
     T* ring = reinterpret_cast<T*>(wbase + align128(sizeof(WarpState)) + (EMIT ? align128(sizeof(WarpEmit)) : 0));
     const uint64_t pitch = G.vol.pitch;
+    const uint64_t slice = G.vol.slice;
     const uint64_t xoff = (uint64_t)seg * kSegCells;
-    const uint32_t row_elems = G.seg_elems;              // staged elements per row
     // bytes copied per row: 257 values rounded up to 16 bytes, or up to the end
     // of the (16-byte padded) row for the last segment
     const uint64_t avail = (pitch - xoff) * sizeof(T);
     const uint32_t row_bytes = (uint32_t)(avail < G.seg_copy_bytes ? avail : G.seg_copy_bytes);
+    const T* vol = static_cast<const T*>(G.vol.data);
 
     if (lane < (unsigned)niso) {
-        const float t = isos[G.iso_begin + lane].f.f_thr;
+        const float t = isos[iso_begin + lane].f.f_thr;
         W.thr[lane] = t;
-        W.thr_bucket[lane] = bucket_of(G, t);
+        W.thr_bucket[lane] = (int32_t)bucket_index(t, bs, bo);
         W.cnt[lane] = 0;
         W.add[lane] = 0;
     }
     __syncwarp();
-    for (unsigned i = lane; i < kStreamBuckets + 3; i += 32) {
-        const int b = (int)i - 1;
-        unsigned below = 0, has = 0;
+    for (unsigned b = lane; b < (unsigned)kLut; b += 32) {
+        uint32_t below = 0, has = 0;
         for (int k = 0; k < niso; ++k) {
-            below += W.thr_bucket[k] < b ? 1u : 0u;
-            has |= W.thr_bucket[k] == b ? 1u : 0u;
+            below += (uint32_t)W.thr_bucket[k] < b ? 1u : 0u;
+            has |= (uint32_t)W.thr_bucket[k] == b ? 1u : 0u;
         }
-        W.bucket[i] = (uint8_t)(below | (has << 7));
+        W.lut[b] = ((1u << below) - 1u) | (has ? kHasThr : 0u);
     }
     if (lane == 0) {
         for (int b = 0; b < 3; ++b) mbar_init(&W.bar[b], 1);
@@ -297,12 +371,11 @@ __global__ void __launch_bounds__(kStreamThreads)
     }
     __syncwarp();
 
-    const T* vol = static_cast<const T*>(G.vol.data);
     auto issue = [&](uint32_t plane) {
         const uint32_t i = plane - z0;
         const int b = (int)(i % 3u);
         T* dst = ring + (size_t)b * 2 * row_elems;
-        const T* src = vol + (uint64_t)plane * G.vol.slice + (uint64_t)y * pitch + xoff;
+        const T* src = vol + (uint64_t)plane * slice + (uint64_t)y * pitch + xoff;
         mbar_arrive_expect_tx(&W.bar[b], 2 * row_bytes);
         bulk_copy_g2s(dst, src, row_bytes, &W.bar[b]);
         bulk_copy_g2s(dst + row_elems, src + pitch, row_bytes, &W.bar[b]);
@@ -312,10 +385,11 @@ __global__ void __launch_bounds__(kStreamThreads)
     }
 
     const uint32_t xl = lane * kLaneCells;              // first cell of this lane inside the segment
-    const uint32_t xb = (uint32_t)xoff + xl;            // its x
+    const int lim = (int)cx - (int)((uint32_t)xoff + xl);   // cells of this lane inside the volume (if < 8)
     const unsigned lt = (1u << lane) - 1u;
     bool dead = false;
     uint32_t s_break = 0;
+    uint32_t PA0[5], PA1[5];   // masks of plane z, rows y and y+1 (carried from the previous step)
 
     for (uint32_t z = z0; z < z1; ++z) {
         const uint32_t s = z - z0;
@@ -331,183 +405,213 @@ __global__ void __launch_bounds__(kStreamThreads)
         const T* ra1 = ra0 + row_elems;
         const T* rb0 = ring + (size_t)((s + 1) % 3u) * 2 * row_elems;
         const T* rb1 = rb0 + row_elems;
-        const uint64_t unit = ((uint64_t)z * cy + y) * G.wpr + seg;
+        const uint64_t unit = ((uint64_t)z * cy + y) * wpr + seg;
 
-        // ---------------- phase 1: classify (lo/hi isolevel range per cell)
-        float a0[9], a1[9], b0[9], b1[9];
-        load8<T>(ra0, xl, a0);
-        load8<T>(ra1, xl, a1);
-        load8<T>(rb0, xl, b0);
-        load8<T>(rb1, xl, b1);
-        a0[8] = (float)ra0[xl + 8];
-        a1[8] = (float)ra1[xl + 8];
-        b0[8] = (float)rb0[xl + 8];
-        b1[8] = (float)rb1[xl + 8];
-        if constexpr (std::is_same<T, float>::value) {
-            // NaN classifies as "not above" for every threshold, like -inf
-#pragma unroll
-            for (int i = 0; i < 9; ++i) {
-                a0[i] = a0[i] != a0[i] ? -INFINITY : a0[i];
-                a1[i] = a1[i] != a1[i] ? -INFINITY : a1[i];
-                b0[i] = b0[i] != b0[i] ? -INFINITY : b0[i];
-                b1[i] = b1[i] != b1[i] ? -INFINITY : b1[i];
-            }
+        // ---------------- phase 1: node masks, per-cell active isolevels
+        if (s == 0) {
+            row_masks<T>(ra0, xl, W, niso, bs, bo, PA0);
+            row_masks<T>(ra1, xl, W, niso, bs, bo, PA1);
         }
-        uint32_t lohi[kLaneCells / 2] = {0, 0, 0, 0};
+        uint32_t PB0[5], PB1[5];
+        row_masks<T>(rb0, xl, W, niso, bs, bo, PB0);
+        row_masks<T>(rb1, xl, W, niso, bs, bo, PB1);
+        // per node column: OR / AND of the 4 corners' masks (thermometer codes:
+        // OR = the highest, AND = the lowest); per cell: the isolevels whose
+        // threshold lies between its lowest and highest corner
+        uint32_t co[5], ca[5];
+#pragma unroll
+        for (int w = 0; w < 5; ++w) {
+            co[w] = PA0[w] | PA1[w] | PB0[w] | PB1[w];
+            ca[w] = PA0[w] & PA1[w] & PB0[w] & PB1[w];
+        }
+        uint32_t act[4];
         uint32_t m = 0;
 #pragma unroll
-        for (int i = 0; i < kLaneCells; ++i) {
-            if (xb + i >= cx) continue;
-            const float mn = fminf(fminf(fminf(a0[i], a0[i + 1]), fminf(a1[i], a1[i + 1])),
-                                   fminf(fminf(b0[i], b0[i + 1]), fminf(b1[i], b1[i + 1])));
-            const float mx = fmaxf(fmaxf(fmaxf(a0[i], a0[i + 1]), fmaxf(a1[i], a1[i + 1])),
-                                   fmaxf(fmaxf(b0[i], b0[i + 1]), fmaxf(b1[i], b1[i + 1])));
-            const int lo = count_below(W, niso, G, mn);
-            const int hi = count_below(W, niso, G, mx);
-            lohi[i >> 1] |= (uint32_t)(lo | (hi << 8)) << (16 * (i & 1));
-            m += (uint32_t)(hi - lo);
-            if (!EMIT) {
-                for (int k = lo; k < hi; ++k) atomicAdd(&W.cnt[k], (uint32_t)TB.ntri[case_of(a0, a1, b0, b1, i, W.thr[k])]);
+        for (int w = 0; w < 4; ++w) {
+            const uint32_t o = co[w] | __funnelshift_r(co[w], co[w + 1], 16);
+            const uint32_t a = ca[w] & __funnelshift_r(ca[w], ca[w + 1], 16);
+            act[w] = o & ~a;
+        }
+        if (lim < kLaneCells) {
+            // cells past the last one of the row: none
+#pragma unroll
+            for (int w = 0; w < 4; ++w) {
+                const uint32_t keep = (2 * w < lim ? 0xffffu : 0u) | (2 * w + 1 < lim ? 0xffff0000u : 0u);
+                act[w] &= keep;
             }
         }
+#pragma unroll
+        for (int w = 0; w < 4; ++w) m += __popc(act[w]);
 
         if (!EMIT) {
-            __syncwarp();
-            if (lane < (unsigned)niso) {
-                unit_counts[G.unit_base + unit * niso + lane] = (uint16_t)W.cnt[lane];
-                W.cnt[lane] = 0;
-            }
-        } else {
-            // ---------------- phase 2: positions, compaction, vertices, triangles
-            // lane k holds the next output triangle of isolevel k for this unit
-            uint64_t run = 0;
-            if (lane < (unsigned)niso) {
-                const StreamIso& I = isos[G.iso_begin + lane];
-                run = plane_base[I.plane_index + z] - plane_base[I.plane_index] +
-                      unit_offsets[G.unit_base + unit * niso + lane];
-            }
-            const uint32_t inc = warp_inclusive_scan(m, lane);
-            const uint32_t npairs = __shfl_sync(FULL, inc, 31);
-            const uint32_t my_first = inc - m;
-            uint32_t* pbuf = WE->pairs;
-            for (uint32_t fill0 = 0; fill0 < npairs; fill0 += kPairCap) {
-                // this lane's pairs that fall into [fill0, fill0 + kPairCap)
-                uint32_t slot = my_first;
+            // count: one u16 per (unit, isolevel)
+            if (__any_sync(FULL, m != 0)) {
 #pragma unroll
                 for (int i = 0; i < kLaneCells; ++i) {
-                    const uint32_t e = (lohi[i >> 1] >> (16 * (i & 1))) & 0xffffu;
-                    for (uint32_t k = e & 0xffu; k < (e >> 8); ++k, ++slot) {
-                        if (slot >= fill0 && slot < fill0 + kPairCap) {
-                            const unsigned c = case_of(a0, a1, b0, b1, i, W.thr[k]);
-                            pbuf[slot - fill0] = (uint32_t)(xl + i) | (k << 8) | (c << 16);
-                        }
+                    uint32_t am = (act[i >> 1] >> (16 * (i & 1))) & 0xffffu;
+                    if (am) {
+                        const uint32_t w0 = cell_word(PA0, i), w1 = cell_word(PA1, i);
+                        const uint32_t w2 = cell_word(PB0, i), w3 = cell_word(PB1, i);
+                        do {
+                            const uint32_t k = __ffs(am) - 1;
+                            am &= am - 1;
+                            atomicAdd(&W.cnt[k], (uint32_t)TB.ntri[case_code(w0, w1, w2, w3, k)]);
+                        } while (am);
                     }
                 }
                 __syncwarp();
-                const uint32_t nfill = (npairs - fill0 < (uint32_t)kPairCap) ? npairs - fill0 : (uint32_t)kPairCap;
-                for (uint32_t r0 = 0; r0 < nfill;) {
-                    const uint32_t p = r0 + lane;
-                    const bool has = p < nfill;
-                    const uint32_t pe = has ? pbuf[p] : 0u;
-                    const uint32_t cell = pe & 0xffu, k = (pe >> 8) & 0xffu, cs = pe >> 16;
-                    uint32_t em = has ? TB.edge_mask[cs] : 0u;
-                    uint32_t ne = __popc(em);
-                    const uint32_t einc = warp_inclusive_scan(ne, lane);
-                    const bool join = has && einc <= (uint32_t)kEdgeCap;
-                    const uint32_t nround = __popc(__ballot_sync(FULL, join));
-                    const uint32_t nt = join ? TB.ntri[cs] : 0u;
-                    if (!join) { ne = 0; em = 0; }
-                    const uint32_t ebase = einc - ne;
-                    const uint32_t tinc = warp_inclusive_scan(nt, lane);
-                    const uint32_t tbase = tinc - nt;
-                    const uint32_t ttot = __shfl_sync(FULL, tinc, nround - 1);
-                    const uint32_t etot = __shfl_sync(FULL, einc, nround - 1);
-                    // per-isolevel position of this pair's first triangle (cell order)
-                    const int key = join ? (int)k : 64 + (int)lane;
-                    const uint32_t grp = __match_any_sync(FULL, key);
-                    uint32_t pre = 0, gtot = 0;
+            }
+            if (lane < (unsigned)niso) {
+                unit_counts[unit_base + unit * niso + lane] = (uint16_t)W.cnt[lane];
+                W.cnt[lane] = 0;
+            }
+        } else {
+            // ---------------- phase 2: pairs, positions, vertices, triangles
+            const uint32_t inc = warp_inclusive_scan(m, lane);
+            const uint32_t npairs = __shfl_sync(FULL, inc, 31);
+            if (npairs) {
+                // lane k holds the next output triangle of isolevel k for this unit
+                uint64_t run = 0;
+                if (lane < (unsigned)niso) {
+                    const StreamIso& I = isos[iso_begin + lane];
+                    run = plane_base[I.plane_index + z] - plane_base[I.plane_index] +
+                          unit_offsets[unit_base + unit * niso + lane];
+                }
+                const uint32_t my_first = inc - m;
+                uint32_t* pbuf = WE->pairs;
+                for (uint32_t fill0 = 0; fill0 < npairs; fill0 += kPairCap) {
+                    // this lane's pairs (cell order, then isolevel) that fall into
+                    // [fill0, fill0 + kPairCap): cell | isolevel << 8 | code << 16
+                    if (m && my_first < fill0 + kPairCap && my_first + m > fill0) {
+                        uint32_t slot = my_first;
 #pragma unroll
-                    for (int bit = 0; bit < 3; ++bit) {
-                        const uint32_t bm = __ballot_sync(FULL, (nt >> bit) & 1u);
-                        pre += (uint32_t)__popc(bm & grp & lt) << bit;
-                        gtot += (uint32_t)__popc(bm & grp) << bit;
-                    }
-                    const uint64_t run_k = __shfl_sync(FULL, run, k & 31u);
-                    const uint64_t obase = run_k + pre;
-                    if (join && (31 - __clz(grp)) == (int)lane) W.add[k] = gtot;
-                    // expansion maps: vertex slot -> (pair, edge rank), triangle -> (pair, index)
-                    for (uint32_t j = 0; j < ne; ++j) WE->edge_map[ebase + j] = (uint16_t)(lane | (j << 5));
-                    for (uint32_t j = 0; j < nt; ++j) WE->tri_map[tbase + j] = (uint8_t)(lane | (j << 5));
-                    __syncwarp();
-                    if (lane < (unsigned)niso) {
-                        run += W.add[lane];
-                        W.add[lane] = 0;
-                    }
-                    // vertices: one lane per (pair, edge)
-                    for (uint32_t b = 0; b < etot; b += 32) {
-                        const uint32_t it = b + lane;
-                        const bool v = it < etot;
-                        const uint32_t mp = v ? (uint32_t)WE->edge_map[it] : 0u;
-                        const uint32_t q = mp & 31u, j = mp >> 5;
-                        const uint32_t em_q = __shfl_sync(FULL, em, q);
-                        const uint32_t cell_q = __shfl_sync(FULL, cell, q);
-                        const uint32_t k_q = __shfl_sync(FULL, k, q);
-                        if (v) {
-                            const int e = __fns(em_q, 0, (int)j + 1);
-                            const unsigned ep = TB.edge_packed[e];
-                            const unsigned ca = ep & 7u, cb = ep >> 3;
-                            const T* sa = ((ca >> 2) ? rb0 : ra0) + ((ca >> 1) & 1u) * row_elems + cell_q + (ca & 1u);
-                            const T* sb = ((cb >> 2) ? rb0 : ra0) + ((cb >> 1) & 1u) * row_elems + cell_q + (cb & 1u);
-                            const unsigned d = ca ^ cb;
-                            const int axis = d == 1u ? 0 : (d == 2u ? 1 : 2);
-                            const uint32_t x = (uint32_t)xoff + cell_q;
-                            const StreamIso& I = isos[G.iso_begin + k_q];
-                            WE->vtx[it] = edge_vertex_fast(
-                                I.ip, I.f, (float)*sa, (float)*sb, __uint2float_rn(x + (ca & 1u)),
-                                __uint2float_rn(y + ((ca >> 1) & 1u)), __uint2float_rn(z + (ca >> 2)),
-                                __uint2float_rn(x + (cb & 1u)), __uint2float_rn(y + ((cb >> 1) & 1u)),
-                                __uint2float_rn(z + (cb >> 2)), axis);
-                        }
-                    }
-                    __syncwarp();
-                    // triangles: one lane per triangle
-                    for (uint32_t b = 0; b < ttot; b += 32) {
-                        const uint32_t it = b + lane;
-                        const bool v = it < ttot;
-                        const uint32_t mp = v ? (uint32_t)WE->tri_map[it] : 0u;
-                        const uint32_t q = mp & 31u, ti = mp >> 5;
-                        const uint32_t em_q = __shfl_sync(FULL, em, q);
-                        const uint32_t eb_q = __shfl_sync(FULL, ebase, q);
-                        const uint32_t cs_q = __shfl_sync(FULL, cs, q);
-                        const uint32_t k_q = __shfl_sync(FULL, k, q);
-                        const uint64_t ob_q = __shfl_sync(FULL, obase, q);
-                        if (v) {
-                            const uint64_t pk = TB.tri_packed[cs_q] >> (12 * ti);
-                            const uint32_t e0 = (uint32_t)pk & 15u, e1 = (uint32_t)(pk >> 4) & 15u,
-                                           e2 = (uint32_t)(pk >> 8) & 15u;
-                            const float3 A = WE->vtx[eb_q + __popc(em_q & ((1u << e0) - 1u))];
-                            const float3 B = WE->vtx[eb_q + __popc(em_q & ((1u << e1) - 1u))];
-                            const float3 C = WE->vtx[eb_q + __popc(em_q & ((1u << e2) - 1u))];
-                            const float3 n = tri_normal(A, B, C);
-                            const StreamIso& I = isos[G.iso_begin + k_q];
-                            float* pc = I.coords;
-                            if (pc) {
-                                const uint64_t o = ob_q + ti;
-                                float* oc = pc + 9 * o;
-                                oc[0] = A.x; oc[1] = A.y; oc[2] = A.z;
-                                oc[3] = B.x; oc[4] = B.y; oc[5] = B.z;
-                                oc[6] = C.x; oc[7] = C.y; oc[8] = C.z;
-                                float* on = I.normals + 3 * o;
-                                on[0] = n.x; on[1] = n.y; on[2] = n.z;
+                        for (int i = 0; i < kLaneCells; ++i) {
+                            uint32_t am = (act[i >> 1] >> (16 * (i & 1))) & 0xffffu;
+                            if (am) {
+                                const uint32_t w0 = cell_word(PA0, i), w1 = cell_word(PA1, i);
+                                const uint32_t w2 = cell_word(PB0, i), w3 = cell_word(PB1, i);
+                                do {
+                                    const uint32_t k = __ffs(am) - 1;
+                                    am &= am - 1;
+                                    if (slot >= fill0 && slot < fill0 + kPairCap)
+                                        pbuf[slot - fill0] = (xl + i) | (k << 8) | (case_code(w0, w1, w2, w3, k) << 16);
+                                    ++slot;
+                                } while (am);
                             }
                         }
                     }
                     __syncwarp();
-                    r0 += nround;
+                    const uint32_t nfill = (npairs - fill0 < (uint32_t)kPairCap) ? npairs - fill0 : (uint32_t)kPairCap;
+                    for (uint32_t r0 = 0; r0 < nfill; r0 += 32) {
+                        // ---- one pair per lane
+                        const uint32_t p = r0 + lane;
+                        const bool has = p < nfill;
+                        const uint32_t pe = has ? pbuf[p] : 0u;
+                        const uint32_t k = (pe >> 8) & 0xffu, code = pe >> 16;
+                        const uint32_t nt = has ? TB.ntri[code] : 0u;
+                        const uint32_t ne = has ? (uint32_t)__popc(TB.edge_mask[code]) : 0u;
+                        // output position of the pair's first triangle: pairs are in
+                        // cell order, so it is the isolevel's running count plus the
+                        // triangles of the earlier lanes of the same isolevel
+                        const int key = has ? (int)k : 64 + (int)lane;
+                        const uint32_t grp = __match_any_sync(FULL, key);
+                        uint32_t pre = 0, gtot = 0, tpre = 0, ntr = 0;
+#pragma unroll
+                        for (int bit = 0; bit < 3; ++bit) {
+                            const uint32_t bm = __ballot_sync(FULL, (nt >> bit) & 1u);
+                            pre += (uint32_t)__popc(bm & grp & lt) << bit;
+                            gtot += (uint32_t)__popc(bm & grp) << bit;
+                            tpre += (uint32_t)__popc(bm & lt) << bit;
+                            ntr += (uint32_t)__popc(bm) << bit;
+                        }
+                        uint32_t vpre = 0, nv = 0;
+#pragma unroll
+                        for (int bit = 0; bit < 4; ++bit) {
+                            const uint32_t bm = __ballot_sync(FULL, (ne >> bit) & 1u);
+                            vpre += (uint32_t)__popc(bm & lt) << bit;
+                            nv += (uint32_t)__popc(bm) << bit;
+                        }
+                        const uint64_t obase = __shfl_sync(FULL, run, k & 31u) + pre;
+                        if (has && (31 - __clz(grp)) == (int)lane) W.add[k] = gtot;
+                        // item -> pair maps of this round
+                        for (uint32_t r = 0; r < ne; ++r) WE->item_v[vpre + r] = (uint8_t)lane;
+                        for (uint32_t t = 0; t < nt; ++t) WE->item_t[tpre + t] = (uint8_t)lane;
+                        __syncwarp();
+                        if (lane < (unsigned)niso) {
+                            run += W.add[lane];
+                            W.add[lane] = 0;
+                        }
+                        // ---- vertices: one (pair, used edge) per lane, edges in increasing order
+                        for (uint32_t j0 = 0; j0 < nv; j0 += 32) {
+                            const uint32_t j = j0 + lane;
+                            const bool hv = j < nv;
+                            const uint32_t q = hv ? WE->item_v[j] : 0u;
+                            const uint32_t qe = __shfl_sync(FULL, pe, q);
+                            const uint32_t qv = __shfl_sync(FULL, vpre, q);
+                            if (hv) {
+                                const uint32_t cell = qe & 0xffu, qk = (qe >> 8) & 0xffu, qc = qe >> 16;
+                                const uint32_t e = (uint32_t)(TB.edge_list[qc] >> (4 * (j - qv))) & 15u;
+                                const unsigned ep = TB.edge_packed[e];
+                                const unsigned c0 = ep & 7u, c1 = ep >> 3;
+                                const T* sa = ((c0 >> 2) ? rb0 : ra0) + ((c0 >> 1) & 1u) * row_elems + cell + (c0 & 1u);
+                                const T* sb = ((c1 >> 2) ? rb0 : ra0) + ((c1 >> 1) & 1u) * row_elems + cell + (c1 & 1u);
+                                const unsigned d = c0 ^ c1;
+                                const int axis = d == 1u ? 0 : (d == 2u ? 1 : 2);
+                                const uint32_t x = (uint32_t)xoff + cell;
+                                const StreamIso& I = isos[iso_begin + qk];
+                                const float3 v = edge_vertex_fast(
+                                    I.ip, I.f, (float)*sa, (float)*sb, __uint2float_rn(x + (c0 & 1u)),
+                                    __uint2float_rn(y + ((c0 >> 1) & 1u)), __uint2float_rn(z + (c0 >> 2)),
+                                    __uint2float_rn(x + (c1 & 1u)), __uint2float_rn(y + ((c1 >> 1) & 1u)),
+                                    __uint2float_rn(z + (c1 >> 2)), axis);
+                                WE->px[j] = v.x;
+                                WE->py[j] = v.y;
+                                WE->pz[j] = v.z;
+                            }
+                        }
+                        __syncwarp();
+                        // ---- triangles: one (pair, triangle) per lane, table order
+                        for (uint32_t j0 = 0; j0 < ntr; j0 += 32) {
+                            const uint32_t j = j0 + lane;
+                            const bool ht = j < ntr;
+                            const uint32_t q = ht ? WE->item_t[j] : 0u;
+                            const uint32_t qe = __shfl_sync(FULL, pe, q);
+                            const uint32_t qv = __shfl_sync(FULL, vpre, q);
+                            const uint32_t qt = __shfl_sync(FULL, tpre, q);
+                            const uint64_t qo = __shfl_sync(FULL, obase, q);
+                            if (ht) {
+                                const uint32_t qk = (qe >> 8) & 0xffu, qc = qe >> 16;
+                                const uint32_t t = j - qt;
+                                const uint32_t emq = TB.edge_mask[qc];
+                                const uint32_t pk = (uint32_t)(TB.tri_packed[qc] >> (12 * t));
+                                const uint32_t s0 = qv + __popc(emq & ((1u << (pk & 15u)) - 1u));
+                                const uint32_t s1 = qv + __popc(emq & ((1u << ((pk >> 4) & 15u)) - 1u));
+                                const uint32_t s2 = qv + __popc(emq & ((1u << ((pk >> 8) & 15u)) - 1u));
+                                const float3 A = make_float3(WE->px[s0], WE->py[s0], WE->pz[s0]);
+                                const float3 B = make_float3(WE->px[s1], WE->py[s1], WE->pz[s1]);
+                                const float3 C = make_float3(WE->px[s2], WE->py[s2], WE->pz[s2]);
+                                const float3 n = tri_normal(A, B, C);
+                                const StreamIso& I = isos[iso_begin + qk];
+                                float* const pc = I.coords;
+                                if (pc) {
+                                    float* oc = pc + 9 * (qo + t);
+                                    float* on = I.normals + 3 * (qo + t);
+                                    oc[0] = A.x; oc[1] = A.y; oc[2] = A.z;
+                                    oc[3] = B.x; oc[4] = B.y; oc[5] = B.z;
+                                    oc[6] = C.x; oc[7] = C.y; oc[8] = C.z;
+                                    on[0] = n.x; on[1] = n.y; on[2] = n.z;
+                                }
+                            }
+                        }
+                        __syncwarp();
+                    }
+                    __syncwarp();
                 }
-                __syncwarp();
             }
         }
+        // plane z+1's masks are plane z's at the next step
+#pragma unroll
+        for (int w = 0; w < 5; ++w) { PA0[w] = PB0[w]; PA1[w] = PB1[w]; }
         // plane z is consumed: refill its buffer with plane z + 3
         __syncwarp();
         if (lane == 0 && z + 3 <= z1) {
@@ -619,6 +723,9 @@ cudaError_t launch_stream(bool emit, int dtype, const StreamGroup* d_groups, int
     KVSMC_STREAM_SWITCH(dtype, {
         auto kern = emit ? k_stream<T, true> : k_stream<T, false>;
         cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        if (e == cudaSuccess)
+            e = cudaFuncSetAttribute(kern, cudaFuncAttributePreferredSharedMemoryCarveout,
+                                     (int)cudaSharedmemCarveoutMaxShared);
         if (e != cudaSuccess) return e;
         prof_begin(L, emit ? "stream_emit" : "stream_count");
         kern<<<(unsigned)nctas, kStreamThreads, smem, L.stream>>>(d_groups, ngroups, ntasks, d_isos, d_unit_counts,

@@ -171,7 +171,7 @@ extern "C" kvsmc_status kvsmc_extract_noalloc(const void* d_values, kvsmc_dtype 
     iso.plane_index = 0;
     g.iso_begin = 0;
     g.niso = 1;
-    kvsmc_host::bucket_params(iso.f.f_thr, iso.f.f_thr, g.bt0, g.bscale);
+    kvsmc_host::bucket_params(iso.f.f_thr, iso.f.f_thr, g.bs, g.bo);
 
     // count -> unit scan -> plane scan -> total
     const int zero = 0;
