@@ -46,7 +46,7 @@ cudaError_t launch_vertex_normals(const Job& j, const Launch& L);
 // ---- streaming kernels (mc_stream.cu): duplicated mode, batched
 constexpr int kStreamThreads = 256;   // 8 independent warps per CTA
 constexpr int kStreamMaxIso = 16;     // isolevels of one volume per group
-constexpr int kStreamBuckets = 256;   // threshold lookup buckets
+constexpr int kStreamBuckets = 128;   // threshold lookup buckets
 constexpr int kStreamSegCells = 256;  // cells per warp segment
 constexpr int kStreamMaxSegments = 16;  // segments per row (width <= 4096 cells)
 

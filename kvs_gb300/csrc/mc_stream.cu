@@ -153,7 +153,7 @@ template <> __device__ __forceinline__ void load8<int8_t>(const int8_t* row, uin
 // ------------------------------------------------------------ shared layout
 
 constexpr int kLut = kStreamBuckets + 1;   // bucket indices 0 .. kStreamBuckets
-constexpr uint32_t kHasThr = 1u << 16;     // LUT flag: a threshold lies in this bucket
+constexpr uint32_t kMultiThr = 1u << 31;   // LUT flag: two or more thresholds lie in this bucket
 constexpr int kMaxVerts = 32 * 12;         // vertex items of one round (12 edges per pair at most)
 constexpr int kMaxTris = 32 * 5;           // triangle items of one round (5 per pair at most)
 
@@ -175,8 +175,9 @@ struct WarpState {
     int32_t thr_bucket[kStreamMaxIso];
     uint32_t cnt[kStreamMaxIso];             // count: triangles of the current unit
     uint32_t add[kStreamMaxIso];             // emit: per-isolevel advance of the current round
-    // bucket -> thermometer mask of the thresholds in lower buckets, plus kHasThr
-    uint32_t lut[kLut];
+    // bucket -> (thermometer mask of the thresholds in lower buckets | kMultiThr,
+    //            bits of the bucket's first threshold, +inf when it has none)
+    uint2 lut[kLut];
 };
 
 // Per-warp emit buffers: the unit's pairs, and for one round the vertex pool
@@ -208,7 +209,9 @@ __device__ __forceinline__ uint32_t bucket_index(float v, float bs, float bo)
 // Thermometer masks of the 9 nodes x0 .. x0+8 of a staged row: bit k set when
 // the value is above isolevel k's threshold (v > t_k; thresholds sorted, so
 // the set bits are 0 .. q-1), packed two nodes per word (node 2m in the low
-// half of word m, node 2m+1 in the high half; word 4 holds node 8).
+// half of word m, node 2m+1 in the high half; word 4 holds node 8).  A bucket
+// holding one threshold needs one compare (branch-free); only a bucket holding
+// several takes the exact loop.
 template <typename T>
 __device__ __forceinline__ void row_masks(const T* row, uint32_t x0, const WarpState& W, int niso, float bs, float bo,
                                           uint32_t* P)
@@ -220,17 +223,18 @@ __device__ __forceinline__ void row_masks(const T* row, uint32_t x0, const WarpS
     uint32_t any = 0;
 #pragma unroll
     for (int i = 0; i < 9; ++i) {
-        e[i] = W.lut[bucket_index(v[i], bs, bo)];
-        any |= e[i];
+        const uint2 l = W.lut[bucket_index(v[i], bs, bo)];
+        e[i] = (v[i] > __int_as_float((int)l.y)) ? 2u * l.x + 1u : l.x;
+        any |= l.x;
     }
-    if (any & kHasThr) {
-        // a node shares its bucket with a threshold: exact compares there
+    if (any & kMultiThr) {
 #pragma unroll
         for (int i = 0; i < 9; ++i) {
-            if (e[i] & kHasThr) {
-                const int b = (int)bucket_index(v[i], bs, bo);
-                int k = __popc(e[i] & 0xffffu);
-                while (k < niso && W.thr_bucket[k] == b && W.thr[k] < v[i]) ++k;
+            const uint32_t b = bucket_index(v[i], bs, bo);
+            const uint32_t lx = W.lut[b].x;
+            if (lx & kMultiThr) {
+                int k = __popc(lx & 0xffffu);
+                while (k < niso && (uint32_t)W.thr_bucket[k] == b && W.thr[k] < v[i]) ++k;
                 e[i] = (1u << k) - 1u;
             }
         }
@@ -358,12 +362,13 @@ __global__ void __launch_bounds__(kStreamThreads, EMIT ? 2 : 3)
     }
     __syncwarp();
     for (unsigned b = lane; b < (unsigned)kLut; b += 32) {
-        uint32_t below = 0, has = 0;
+        uint32_t below = 0, in = 0;
         for (int k = 0; k < niso; ++k) {
             below += (uint32_t)W.thr_bucket[k] < b ? 1u : 0u;
-            has |= (uint32_t)W.thr_bucket[k] == b ? 1u : 0u;
+            in += (uint32_t)W.thr_bucket[k] == b ? 1u : 0u;
         }
-        W.lut[b] = ((1u << below) - 1u) | (has ? kHasThr : 0u);
+        const float first = in ? W.thr[below] : __int_as_float(0x7f800000);
+        W.lut[b] = make_uint2(((1u << below) - 1u) | (in > 1 ? kMultiThr : 0u), (uint32_t)__float_as_int(first));
     }
     if (lane == 0) {
         for (int b = 0; b < 3; ++b) mbar_init(&W.bar[b], 1);

@@ -148,3 +148,24 @@ def test_capacity_error_reports_sizes(kvsmc_ctx):
                                             c.data_ptr(), 3, None, 0, C.byref(s))
     assert st == _abi.ERR_CAPACITY
     assert s.ntriangles > 1 and s.ncoords == 9 * s.ntriangles
+
+
+def test_clustered_isolevels(kvsmc_ctx):
+    """Equal and nearly equal isolevels in one batch (several thresholds in one
+    lookup bucket) and node values exactly on thresholds."""
+    v = (np.round(S.to_numpy(S.fbm((24, 37, 290), seed=21)) * 64.0) / 64.0).astype(np.float32)
+    vol = _abi.DeviceVolume.upload(kvsmc_ctx, v)
+    isos = [0.5, 0.5, 0.5 + 1e-7, 0.5 + 1e-4, 0.5 + 2e-4, 0.25, 0.25 + 1 / 64, 0.75, 0.75, 31 / 64, 33 / 64]
+    ps = [_abi.make_params(i, 0) for i in isos]
+    a = extract_batch(kvsmc_ctx, [vol] * len(ps), ps, _abi.PATH_AUTO)
+    b = extract_batch(kvsmc_ctx, [vol] * len(ps), ps, _abi.PATH_GATHER)
+    for i, iso in enumerate(isos):
+        compare(a[i], b[i], f"f32 iso={iso}")
+    u = S.to_numpy(S.ellipsoid_phantom((21, 33, 100), np.uint8, seed=22))
+    uvol = _abi.DeviceVolume.upload(kvsmc_ctx, u)
+    isos = [100.0, 100.0, 100.5, 101.0, 99.9, 100.25, 20.0, 21.0]
+    ps = [_abi.make_params(i, 0) for i in isos]
+    a = extract_batch(kvsmc_ctx, [uvol] * len(ps), ps, _abi.PATH_AUTO)
+    b = extract_batch(kvsmc_ctx, [uvol] * len(ps), ps, _abi.PATH_GATHER)
+    for i, iso in enumerate(isos):
+        compare(a[i], b[i], f"u8 iso={iso}")
