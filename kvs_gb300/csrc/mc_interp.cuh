@@ -23,9 +23,13 @@
 //    arithmetic, |X - (a + (b-a) R)| <= 2^-51 (max(|a|,|b|) + 1)   (E_D).
 //    The double-float Y approximates a + (b-a) R within
 //        E_Y = 2^-40 |q| + err(num)/|den| + 2^-23 |y_lo|
-//    (the quotient error is below 26 u^2 |R| < 2^-43 |R|, u = 2^-24; the
-//    bound keeps a factor 8 of slack).  If every real in [Y - E, Y + E],
-//    E = E_Y + E_D, rounds to the same float, that float is RN32(X) = F.
+//    The quotient starts from the hardware reciprocal approximation
+//    (rcp.approx, relative error below 2^-22 assumed, twice its documented
+//    1 ulp), q1 = nh * inv, and takes one residual correction q2 = rho * inv
+//    with rho = num - q1 * den formed from exact FMA products; then
+//    |q1 + q2 - num/den| < 1.5 * 2^-43 |R|, below the 2^-40 |q| term with a
+//    factor 5 of slack.  If every real in [Y - E, Y + E], E = E_Y + E_D,
+//    rounds to the same float, that float is RN32(X) = F.
 #pragma once
 #include <cstdint>
 #include <cuda_runtime.h>
@@ -56,16 +60,6 @@ __device__ __forceinline__ float clampf_ref(float a, float lo, float hi)
     return a <= lo ? lo : (a <= hi ? a : hi);
 }
 
-// Half the distance from y (>= 0, finite) to the next float above / below.
-__device__ __forceinline__ float half_gap_up(float y)
-{
-    return __fmul_rn(__fsub_rn(__int_as_float(__float_as_int(y) + 1), y), 0.5f);
-}
-__device__ __forceinline__ float half_gap_down(float y)
-{
-    return __fmul_rn(__fsub_rn(y, __int_as_float(__float_as_int(y) - 1)), 0.5f);
-}
-
 // The varying-axis coordinate RN32(X) for an edge from coordinate a (value
 // v0) to b = a + d (value v1), d = +-1.  Returns false when the FP32 path
 // cannot decide; `out` is then unspecified.
@@ -88,8 +82,9 @@ __device__ __forceinline__ bool fast_axis(float v0, float v1, float a, float b, 
     two_sum(v1, -v0, dh, dl);
     const float adh = fabsf(dh);
     if (!(adh >= 8.67361738e-19f) || !(adh <= 1.15292150e+18f)) return false;  // 2^-60 .. 2^60
-    // q = num / den: q1 from the reciprocal, then one residual correction.
-    const float inv = __frcp_rn(dh);
+    // q = num / den: q1 from the approximate reciprocal, then one residual correction.
+    float inv;
+    asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(inv) : "f"(dh));
     const float q1 = __fmul_rn(nh, inv);
     const float p = __fmul_rn(q1, dh);
     const float pe = __fmaf_rn(q1, dh, -p);
@@ -110,7 +105,7 @@ __device__ __forceinline__ bool fast_axis(float v0, float v1, float a, float b, 
     // E = E_R + rounding of yb2 + E_D, each with slack.
     const float m = fmaxf(a, b);
     float E = __fmul_rn(aq, 9.09494702e-13f);                                   // 2^-40 |q|
-    E = __fadd_rn(E, __fmul_rn(__fmul_rn(err_num, __frcp_ru(adh)), 1.0001f));  // err(num)/|den|
+    E = __fadd_rn(E, __fmul_rn(__fmul_rn(err_num, fabsf(inv)), 1.0001f));      // err(num)/|den| (inv within 2^-22)
     E = __fadd_rn(E, __fmul_rn(fabsf(yb2), 1.1920929e-07f));                    // 2^-23 |yb2|
     E = __fadd_rn(E, __fmul_rn(__fadd_rn(m, 1.0f), 8.8817842e-16f));            // 2^-50 (M + 1)
     E = __fmul_rn(E, 1.001f);
@@ -119,7 +114,10 @@ __device__ __forceinline__ bool fast_axis(float v0, float v1, float a, float b, 
         if (yh == 0.0f && yl == 0.0f && E < 1.0e-30f) { out = 0.0f; return true; }
         return false;
     }
-    const float dist = (yl >= 0.0f) ? __fsub_rn(half_gap_up(yh), yl) : __fadd_rn(half_gap_down(yh), yl);
+    // distance to the nearest rounding boundary on yl's side: half the gap to
+    // the neighbouring float there, less |yl| (yh > 0 and normal here)
+    const float nb = __int_as_float(__float_as_int(yh) + (yl >= 0.0f ? 1 : -1));
+    const float dist = __fsub_rn(__fmul_rn(fabsf(__fsub_rn(nb, yh)), 0.5f), fabsf(yl));
     if (!(dist > E)) return false;
     out = yh;
     return true;
@@ -131,6 +129,33 @@ static __device__ __noinline__ float3 interpolate_exact_slow(const Interp& j, fl
                                                              float az, float bx, float by, float bz)
 {
     return interpolate_exact(j, (double)va, (double)vb, ax, ay, az, bx, by, bz);
+}
+
+// Vertex of an edge from corner A = (ax, ay, az) (value va) to the corner one
+// step along `axis` (0, 1, 2), whose coordinate there is `b` (a +- 1).  Same
+// result as edge_vertex_fast; the callers pass integer coordinates as floats.
+__device__ __forceinline__ float3 edge_vertex_axis(const Interp& j, const FastIso& f, float va, float vb, float ax,
+                                                   float ay, float az, int axis, float b)
+{
+    bool ok = f.fast_ok != 0;
+    float r = 0.0f;
+    const float a = axis == 0 ? ax : (axis == 1 ? ay : az);
+    if (ok) {
+        const float v0 = clampf_ref(va, f.vmin_f, f.vmax_f);
+        const float v1 = clampf_ref(vb, f.vmin_f, f.vmax_f);
+        ok = (v0 > f.f_thr) != (v1 > f.f_thr);
+        if (ok) ok = fast_axis(v0, v1, a, b, f, r);
+    }
+    if (ok) {
+        const float px = axis == 0 ? r : ax, py = axis == 1 ? r : ay, pz = axis == 2 ? r : az;
+        float3 o;
+        o.x = __fmul_rn(__fadd_rn(px, j.min_coord[0]), j.scale[0]);
+        o.y = __fmul_rn(__fadd_rn(py, j.min_coord[1]), j.scale[1]);
+        o.z = __fmul_rn(__fadd_rn(pz, j.min_coord[2]), j.scale[2]);
+        return o;
+    }
+    const float bx = axis == 0 ? b : ax, by = axis == 1 ? b : ay, bz = axis == 2 ? b : az;
+    return interpolate_exact_slow(j, va, vb, ax, ay, az, bx, by, bz);
 }
 
 // Vertex of an edge whose endpoints differ along `axis` (0, 1, 2): A = (ax,

@@ -392,6 +392,7 @@ __global__ void __launch_bounds__(kStreamThreads, EMIT ? 2 : 3)
     const uint32_t xl = lane * kLaneCells;              // first cell of this lane inside the segment
     const int lim = (int)cx - (int)((uint32_t)xoff + xl);   // cells of this lane inside the volume (if < 8)
     const unsigned lt = (1u << lane) - 1u;
+    const float fy = __uint2float_rn(y);
     bool dead = false;
     uint32_t s_break = 0;
     uint32_t PA0[5], PA1[5];   // masks of plane z, rows y and y+1 (carried from the previous step)
@@ -411,6 +412,7 @@ __global__ void __launch_bounds__(kStreamThreads, EMIT ? 2 : 3)
         const T* rb0 = ring + (size_t)((s + 1) % 3u) * 2 * row_elems;
         const T* rb1 = rb0 + row_elems;
         const uint64_t unit = ((uint64_t)z * cy + y) * wpr + seg;
+        const float fz = __uint2float_rn(z);
 
         // ---------------- phase 1: node masks, per-cell active isolevels
         if (s == 0) {
@@ -562,13 +564,16 @@ __global__ void __launch_bounds__(kStreamThreads, EMIT ? 2 : 3)
                                 const T* sb = ((c1 >> 2) ? rb0 : ra0) + ((c1 >> 1) & 1u) * row_elems + cell + (c1 & 1u);
                                 const unsigned d = c0 ^ c1;
                                 const int axis = d == 1u ? 0 : (d == 2u ? 1 : 2);
-                                const uint32_t x = (uint32_t)xoff + cell;
+                                // corner coordinates: integers below 2^24, exact as floats
+                                const float fx = __uint2float_rn((uint32_t)xoff + cell);
+                                const float ax = __fadd_rn(fx, (c0 & 1u) ? 1.0f : 0.0f);
+                                const float ay = __fadd_rn(fy, (c0 & 2u) ? 1.0f : 0.0f);
+                                const float az = __fadd_rn(fz, (c0 & 4u) ? 1.0f : 0.0f);
+                                const float bcoord = __fadd_rn(axis == 0 ? fx : (axis == 1 ? fy : fz),
+                                                               (c1 & d) ? 1.0f : 0.0f);
                                 const StreamIso& I = isos[iso_begin + qk];
-                                const float3 v = edge_vertex_fast(
-                                    I.ip, I.f, (float)*sa, (float)*sb, __uint2float_rn(x + (c0 & 1u)),
-                                    __uint2float_rn(y + ((c0 >> 1) & 1u)), __uint2float_rn(z + (c0 >> 2)),
-                                    __uint2float_rn(x + (c1 & 1u)), __uint2float_rn(y + ((c1 >> 1) & 1u)),
-                                    __uint2float_rn(z + (c1 >> 2)), axis);
+                                const float3 v =
+                                    edge_vertex_axis(I.ip, I.f, (float)*sa, (float)*sb, ax, ay, az, axis, bcoord);
                                 WE->px[j] = v.x;
                                 WE->py[j] = v.y;
                                 WE->pz[j] = v.z;
@@ -636,7 +641,10 @@ __global__ void __launch_bounds__(kStreamThreads, EMIT ? 2 : 3)
 
 // One CTA per (group, z): for every isolevel of the group, the exclusive scan
 // of its unit counts over the plane's units (rows y, segments x) -> u32
-// offsets inside the plane, and the plane's total.
+// offsets inside the plane, and the plane's total.  Counts are stored
+// [unit][isolevel]; the plane is walked in tiles of 256 units, each staged
+// through shared memory with coalesced loads and stores, one unit per thread
+// and all isolevels scanned at once.
 constexpr int kScanUnitThreads = 256;
 
 __global__ void __launch_bounds__(kScanUnitThreads)
@@ -644,9 +652,13 @@ __global__ void __launch_bounds__(kScanUnitThreads)
                 const uint16_t* __restrict__ unit_counts, uint32_t* __restrict__ unit_offsets,
                 uint32_t* __restrict__ plane_totals)
 {
-    __shared__ uint32_t ws[33];
+    constexpr int NT = kScanUnitThreads, NW = NT / 32;
+    __shared__ uint16_t sc[NT * kStreamMaxIso];
+    __shared__ uint32_t so[NT * kStreamMaxIso];
+    __shared__ uint32_t wsum[NW][kStreamMaxIso];
     __shared__ int s_g;
-    if (threadIdx.x == 0) {
+    const unsigned tid = threadIdx.x, lane = tid & 31u, warp = tid >> 5;
+    if (tid == 0) {
         int lo = 0, hi = ngroups - 1;
         while (lo < hi) {
             const int mid = (lo + hi + 1) >> 1;
@@ -660,17 +672,53 @@ __global__ void __launch_bounds__(kScanUnitThreads)
     const uint64_t U = (uint64_t)(G.vol.ny - 1) * G.wpr;
     const int niso = G.niso;
     const uint64_t base = G.unit_base + (uint64_t)z * U * niso;
-    for (int k = 0; k < niso; ++k) {
-        uint32_t running = 0;
-        for (uint64_t u0 = 0; u0 < U; u0 += blockDim.x) {
-            const uint64_t u = u0 + threadIdx.x;
-            const uint32_t c = u < U ? unit_counts[base + u * niso + k] : 0u;
-            uint32_t tot;
-            const uint32_t e = block_exclusive_scan(c, ws, &tot);
-            if (u < U) unit_offsets[base + u * niso + k] = running + e;
-            running += tot;
+
+    uint32_t carry[kStreamMaxIso];
+#pragma unroll
+    for (int k = 0; k < kStreamMaxIso; ++k) carry[k] = 0;
+    for (uint64_t t0 = 0; t0 < U; t0 += NT) {
+        const uint32_t n = (uint32_t)(U - t0 < (uint64_t)NT ? U - t0 : (uint64_t)NT);
+        const uint32_t nel = n * (uint32_t)niso;
+        const uint16_t* src = unit_counts + base + t0 * niso;
+        for (uint32_t i = tid; i < nel; i += NT) sc[i] = src[i];
+        __syncthreads();
+        uint32_t c[kStreamMaxIso], ex[kStreamMaxIso];
+#pragma unroll
+        for (int k = 0; k < kStreamMaxIso; ++k) {
+            c[k] = (k < niso && tid < n) ? sc[tid * niso + k] : 0u;
+            uint32_t v = c[k];
+#pragma unroll
+            for (int o = 1; o < 32; o <<= 1) {
+                const uint32_t t = __shfl_up_sync(0xffffffffu, v, o);
+                if (lane >= (unsigned)o) v += t;
+            }
+            if (lane == 31) wsum[warp][k] = v;
+            ex[k] = v - c[k];
         }
-        if (threadIdx.x == 0) plane_totals[isos[G.iso_begin + k].plane_index + z] = running;
+        __syncthreads();
+#pragma unroll
+        for (int k = 0; k < kStreamMaxIso; ++k) {
+            if (k < niso) {
+                uint32_t before = 0, all = 0;
+#pragma unroll
+                for (int w = 0; w < NW; ++w) {
+                    const uint32_t x = wsum[w][k];
+                    before += (w < (int)warp) ? x : 0u;
+                    all += x;
+                }
+                if (tid < n) so[tid * niso + k] = carry[k] + before + ex[k];
+                carry[k] += all;
+            }
+        }
+        __syncthreads();
+        uint32_t* dst = unit_offsets + base + t0 * niso;
+        for (uint32_t i = tid; i < nel; i += NT) dst[i] = so[i];
+        __syncthreads();
+    }
+    if (tid < (unsigned)niso) {
+#pragma unroll
+        for (int k = 0; k < kStreamMaxIso; ++k)
+            if (k == (int)tid) plane_totals[isos[G.iso_begin + k].plane_index + z] = carry[k];
     }
 }
 

@@ -110,7 +110,8 @@ def fbm(shape, octaves=5, base_freq=1.0 / 128.0, gain=0.5, lacunarity=2.0, seed=
         out = torch.empty((nz, ny, nx), dtype=torch.float32, device=device)
     x = torch.arange(nx, device=device, dtype=torch.float32)
     y = torch.arange(ny, device=device, dtype=torch.float32)
-    slab = max(1, (1 << 22) // max(1, nx * ny))
+    # elements per generated slab: large on a GPU (fewer launches), small on the CPU
+    slab = max(1, (1 << (26 if str(device).startswith("cuda") else 22)) // max(1, nx * ny))
     for z0 in range(0, nz, slab):
         z1 = min(nz, z0 + slab)
         z = torch.arange(z0, z1, device=device, dtype=torch.float32)
