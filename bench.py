@@ -8,7 +8,12 @@ volume: the fused count launch, the scan, the fused emit launch, with output
 written to HBM.  `value` = cells x isovalues / s (Mcells/s).
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
-                    [--workload sweep1024|sweep384|blobs128]
+                    [--workload sweep1024|sweep384|uneven200|blobs128]
+
+--workload uneven200 times the same 200-request batch three ways: one plain
+kvsmc_extract_device call per request (count, host sync, emit, host sync),
+one kvsmc_extract_batch call, and one replay of a kvsmc_plan (the whole batch
+captured in a CUDA graph); `value` is the plan replay.
 
 --impl reference times the reference's CPU algorithm on this host's cores: the
 C restatement under oracle/ (the reference sources are not present on the GPU
@@ -36,6 +41,10 @@ WORKLOADS = {
     "sweep384": dict(shape=(384, 384, 384), kind="fbm", isos=[0.2 + 0.04 * k for k in range(16)],
                      desc="384^3 float32 fBm gradient noise (as sweep1024), 16 isovalues 0.2..0.8 in one batched "
                           "call, duplication=true, PolygonNormal (the profiling case)"),
+    "uneven200": dict(kind="batch", n=200, dims=(32, 384), seed=2024,
+                      desc="200 volumes, each axis U[32,384], dtype U{uint8,uint16,float32}, ellipsoid phantoms "
+                           "(3-6 nested rotated shells + N(0, 2% range) noise), one isovalue per volume U over the "
+                           "central 60% of its range, duplication=true, PolygonNormal"),
     "blobs128": dict(shape=(128, 128, 128), kind="blobs", isos=[0.5],
                      desc="128^3 float32, 4 Gaussian blobs (sigma 8..24) + U[-0.01,0.01] noise, iso 0.5, "
                           "duplication=true, PolygonNormal"),
@@ -296,6 +305,179 @@ def run_e2e(ctx, host_field, isos, reqs, args, stream):
             "api": "kvsmc_extract_batch_host", "steps": steps}
 
 
+# ----------------------------------------------------------------- uneven batch
+
+def run_batch(args, rank, world, local):
+    """The uneven multi-volume batch: plain per-call vs batched vs graph replay."""
+    import ctypes as C
+
+    import torch
+
+    from kvs_gb300 import _abi
+    from kvs_gb300 import synthetic as S
+
+    torch.cuda.set_device(local)
+    w = WORKLOADS[args.workload]
+    ctx = _abi.Context(local)
+    stream = torch.cuda.Stream()
+    ctx.set_stream(stream.cuda_stream)
+    rng = np.random.default_rng(w["seed"])
+    dts = [np.uint8, np.uint16, np.float32]
+    vols, params, hosts, shapes = [], [], [], []
+    cells = 0
+    in_bytes = 0
+    sample = []
+    for i in range(w["n"]):
+        nz, ny, nx = (int(d) for d in rng.integers(w["dims"][0], w["dims"][1] + 1, 3))
+        dt = dts[int(rng.integers(0, 3))]
+        f = S.ellipsoid_phantom((nz, ny, nx), dt, seed=w["seed"] + 1 + i, device="cuda")
+        torch.cuda.synchronize()
+        dv = _abi.DeviceVolume.from_device(ctx, f.data_ptr(), dt, (nz, ny, nx))
+        if not args.no_e2e:
+            h = torch.empty(f.shape, dtype=f.dtype, pin_memory=True)
+            h.copy_(f)
+            hosts.append(h)
+        if rank == 0 and len(sample) < 4:
+            sample.append(S.to_numpy(f))
+        del f
+        mn, mx = dv.minmax()
+        iso = mn + rng.uniform(0.2, 0.8) * (mx - mn)
+        vols.append(dv)
+        params.append(_abi.make_params(iso, _abi.MODE_DUP_POLYGON_NORMAL))
+        shapes.append((nz, ny, nx, np.dtype(dt)))
+        cells += (nx - 1) * (ny - 1) * (nz - 1)
+        in_bytes += nx * ny * nz * np.dtype(dt).itemsize
+    torch.cuda.empty_cache()
+    n = len(vols)
+    reqs = (_abi.Request * n)()
+    for i in range(n):
+        reqs[i].volume = vols[i].handle
+        reqs[i].params = params[i]
+    ctx.check(ctx.lib.kvsmc_count_batch(ctx.handle, reqs, n), "count")
+    outs = []
+    for i in range(n):
+        s = reqs[i].sizes
+        c = torch.empty(max(1, s.ncoords), dtype=torch.float32, device="cuda")
+        nn = torch.empty(max(1, s.nnormals), dtype=torch.float32, device="cuda")
+        outs.append((c, nn))
+        reqs[i].d_coords, reqs[i].coords_capacity = c.data_ptr(), s.ncoords
+        reqs[i].d_normals, reqs[i].normals_capacity = nn.data_ptr(), s.nnormals
+    ntri = sum(reqs[i].sizes.ntriangles for i in range(n))
+    sizes = _abi.Sizes()
+
+    def per_call():
+        for i in range(n):
+            ctx.check(ctx.lib.kvsmc_extract_device(ctx.handle, vols[i].handle, C.byref(reqs[i].params),
+                                                   reqs[i].d_coords, reqs[i].coords_capacity, reqs[i].d_normals,
+                                                   reqs[i].normals_capacity, None, 0, C.byref(sizes)),
+                      "extract_device")
+
+    def batched():
+        ctx.check(ctx.lib.kvsmc_extract_batch(ctx.handle, reqs, n), "extract_batch")
+
+    plan = _abi.Plan(ctx, reqs)
+
+    def replay():
+        plan.launch()
+        plan.wait()
+
+    def timed(fn, steps):
+        for _ in range(args.warmup):
+            fn()
+        torch.cuda.synchronize()
+        if world > 1:
+            import torch.distributed as dist
+            dist.barrier()
+        launches0 = ctx.kernel_launches
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        for _ in range(steps):
+            fn()
+        e1.record(stream)
+        torch.cuda.synchronize()
+        return barrier_max(e0.elapsed_time(e1), world) / steps, (ctx.kernel_launches - launches0) // steps
+
+    ms_call, l_call = timed(per_call, max(1, args.steps // 2))
+    ms_batch, l_batch = timed(batched, args.steps)
+    clocks = Clocks(local)
+    clocks.start()
+    ms_graph, l_graph = timed(replay, args.steps)
+    clk = clocks.stop()
+    # kernel times of one batch (same kernels as the replay) for the roofline
+    ctx.profile_enable(True)
+    batched()
+    torch.cuda.synchronize()
+    prof = ctx.profile_read()
+    ctx.profile_enable(False)
+    hbm, peak_kind = peaks()
+    algo = in_bytes + 48 * ntri
+    emit_ms = sum(v[1] for k, v in prof.items() if k == "stream_emit")
+    count_ms = sum(v[1] for k, v in prof.items() if k == "stream_count")
+    roofline = {"kernel": "stream_emit", "bound": "hbm", "achieved": round(algo / (emit_ms * 1e-3) / 1e9, 1),
+                "peak": hbm, "peak_kind": peak_kind, "unit": "GB/s",
+                "frac": round(algo / (emit_ms * 1e-3) / 1e9 / hbm, 4), "algorithmic_bytes_per_launch": int(algo),
+                "launch_ms": round(emit_ms, 4), "traffic": None,
+                "note": "one emit launch per dtype present (3), summed"}
+    mc = lambda ms: round(cells * world / (ms * 1e-3) / 1e6, 1)
+    e2e = None
+    if hosts:
+        host_out = [(torch.empty(c.shape, dtype=c.dtype, pin_memory=True),
+                     torch.empty(nn.shape, dtype=nn.dtype, pin_memory=True)) for c, nn in outs]
+
+        def e2e_step():
+            for i in range(n):
+                ctx.check(ctx.lib.kvsmc_volume_update(ctx.handle, vols[i].handle, hosts[i].data_ptr()), "update")
+            plan.launch()
+            with torch.cuda.stream(stream):
+                for (c, nn), (hc, hn) in zip(outs, host_out):
+                    hc.copy_(c, non_blocking=True)
+                    hn.copy_(nn, non_blocking=True)
+            plan.wait()
+            stream.synchronize()
+
+        ms_e2e, _ = timed(e2e_step, max(1, args.steps // 2))
+        e2e = {"value": mc(ms_e2e), "unit": "Mcells/s", "h2d_bytes_per_step": int(in_bytes),
+               "d2h_bytes_per_step": int(sum(4 * (c.numel() + nn.numel()) for c, nn in outs)),
+               "api": "kvsmc_volume_update x200 + kvsmc_plan_launch/wait + device-to-host copies", "ms_per_step": round(ms_e2e, 3)}
+    plan.close()
+    args.batch_sample = sample
+    args.batch_params = [(params[i].isolevel, reqs[i].sizes.min_value, reqs[i].sizes.max_value) for i in range(4)]
+    return {
+        "metric": "Mcells/s", "value": mc(ms_graph), "unit": "Mcells/s", "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": round(ms_graph, 4), "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "u8/u16/f32", "data": "synthetic (seeded phantoms generated on the device)",
+        "config": {"workload": w["desc"], "requests": n, "cells": int(cells), "input_bytes": int(in_bytes),
+                   "cache": "inputs larger than L2 (%.1f GB of volumes)" % (in_bytes / 1e9)},
+        "mtris_per_s": round(ntri * world / (ms_graph * 1e-3) / 1e6, 1), "triangles_per_step": int(ntri),
+        "forms": {"per_call": {"api": "kvsmc_extract_device x%d" % n, "ms_per_step": round(ms_call, 3),
+                               "value": mc(ms_call), "gpu_launches": int(l_call)},
+                  "batched": {"api": "kvsmc_extract_batch", "ms_per_step": round(ms_batch, 3),
+                              "value": mc(ms_batch), "gpu_launches": int(l_batch)},
+                  "graph": {"api": "kvsmc_plan_launch + kvsmc_plan_wait", "ms_per_step": round(ms_graph, 3),
+                            "value": mc(ms_graph), "gpu_launches": int(l_graph)}},
+        "speedup_vs_per_call": round(ms_call / ms_graph, 2),
+        "roofline": roofline,
+        "kernels": {k: {"launches": v[0], "ms": round(v[1], 3)} for k, v in prof.items()},
+        "e2e": e2e, "gpu_launches": int(l_graph), "clocks": clk,
+    }
+
+
+def run_batch_cpu(args):
+    """The oracle on the first sample volumes of the batch, one core."""
+    from oracle import oracle
+    oracle.build()
+    done, t = 0, 0.0
+    for v, (iso, mn, mx) in zip(args.batch_sample, args.batch_params):
+        nz, ny, nx = v.shape
+        t0 = time.perf_counter()
+        oracle.extract(v, iso, 0, mn, mx)
+        t += time.perf_counter() - t0
+        done += (nx - 1) * (ny - 1) * (nz - 1)
+    return done / t / 1e6, t, "%d volumes of the batch (%s), %.0f M cells" % (
+        len(args.batch_sample), ", ".join("x".join(str(d) for d in v.shape[::-1]) + " " + str(v.dtype)
+                                          for v in args.batch_sample), done / 1e6)
+
+
 # ----------------------------------------------------------------- CPU side
 
 def cpu_slab_sample(args, slab_planes):
@@ -339,11 +521,64 @@ def run_cpu(args, threads, planes, isos):
     return done / t / 1e6, t, f"{len(isos)} isovalues x {nx}x{ny}x{nz} slab ({done / 1e6:.0f} M cell-isovalues)"
 
 
+def batch_reference_sample(w, count):
+    """The first `count` requests of a batch workload, generated on the CPU
+    with the same generator, shapes, dtypes and isovalues as the GPU run."""
+    from kvs_gb300 import synthetic as S
+    rng = np.random.default_rng(w["seed"])
+    dts = [np.uint8, np.uint16, np.float32]
+    out = []
+    for i in range(count):
+        nz, ny, nx = (int(d) for d in rng.integers(w["dims"][0], w["dims"][1] + 1, 3))
+        dt = dts[int(rng.integers(0, 3))]
+        v = S.to_numpy(S.ellipsoid_phantom((nz, ny, nx), dt, seed=w["seed"] + 1 + i, device="cpu"))
+        mn, mx = float(v.min()), float(v.max())
+        iso = mn + rng.uniform(0.2, 0.8) * (mx - mn)
+        out.append((v, iso, mn, mx))
+    return out
+
+
+def run_reference_batch(args, world, threads):
+    from oracle import oracle
+    oracle.build()
+    w = WORKLOADS[args.workload]
+    reqs = batch_reference_sample(w, 12)
+    cells = sum((v.shape[0] - 1) * (v.shape[1] - 1) * (v.shape[2] - 1) for v, _, _, _ in reqs)
+
+    def one(r):
+        v, iso, mn, mx = r
+        oracle.extract(v, iso, 0, mn, mx)
+
+    vals = []
+    for i in range(args.warmup + args.steps):
+        t0 = time.perf_counter()
+        with cf.ThreadPoolExecutor(max_workers=threads) as ex:
+            list(ex.map(one, reqs))
+        t = time.perf_counter() - t0
+        if i >= args.warmup:
+            vals.append(t)
+    t = statistics.median(vals)
+    value = cells / t / 1e6
+    sample = f"first {len(reqs)} requests of the batch ({cells / 1e6:.0f} M cells), one request per thread"
+    return {
+        "impl": "reference", "metric": "Mcells/s", "value": round(value, 1), "unit": "Mcells/s",
+        "n_gpus": world, "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(t * 1e3, 1),
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "u8/u16/f32", "data": "synthetic",
+        "config": {"workload": w["desc"], "sample": sample},
+        "cpu_baseline": {"value": round(value, 1), "unit": "Mcells/s", "cores": threads, "kind": "port",
+                         "sample": sample + "; oracle/mc_oracle.c (C restatement of kvs::MarchingCubes, "
+                         "-O3 -ffp-contract=off)"},
+        "e2e": {"value": round(value, 1), "unit": "Mcells/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+
+
 def run_reference(args, rank, world):
     if rank != 0:
         return None
     w = WORKLOADS[args.workload]
     threads = os.cpu_count() or 1
+    if w["kind"] == "batch":
+        return run_reference_batch(args, world, threads)
     planes = min(65, w["shape"][0]) if w["kind"] == "fbm" else w["shape"][0]
     isos = w["isos"]
     vals = []
@@ -385,6 +620,12 @@ def main():
         dist.init_process_group("nccl")
     if args.impl == "reference":
         line = run_reference(args, rank, world)
+    elif WORKLOADS[args.workload]["kind"] == "batch":
+        line = run_batch(args, rank, world, local)
+        if rank == 0 and world == 1 and not args.no_cpu:
+            v, t, sample = run_batch_cpu(args)
+            line["cpu_baseline"] = {"value": round(v, 1), "unit": "Mcells/s", "cores": 1, "kind": "port",
+                                    "sample": sample + f"; {t:.1f} s on 1 host core; oracle/mc_oracle.c"}
     else:
         line = run_ours(args, rank, world, local)
         if rank == 0 and world == 1 and not args.no_cpu:

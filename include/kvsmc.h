@@ -189,6 +189,36 @@ kvsmc_status kvsmc_count_batch(kvsmc_context* ctx, kvsmc_request* reqs, int32_t 
  * volume is read once per pass however many isolevels share it. */
 kvsmc_status kvsmc_extract_batch(kvsmc_context* ctx, kvsmc_request* reqs, int32_t n);
 
+/* ------------------------------------------------------- replayable plans */
+
+/* A fixed batch extracted again and again (the same volumes, isolevels and
+ * output buffers; the volume contents may change in place): the work tables
+ * are planned and uploaded once and every launch of one extraction (count,
+ * unit scan, plane scan, totals, emit, for every value type present) plus
+ * the read-back of the totals is captured into ONE CUDA graph, so a replay
+ * costs one cudaGraphLaunch and no host round trip between the passes.
+ * No counterpart in the reference (one kvs::MarchingCubes per request).
+ *   - every extracted request must be one the streaming kernels take
+ *     (duplicated mode, int8/uint8/int16/uint16/float32, width <= 4097),
+ *     else KVSMC_ERR_INVALID_ARGUMENT;
+ *   - min/max are decided at creation (preset, or the volume's cache, filled
+ *     by a min/max pass if needed) and frozen in the plan;
+ *   - outputs are bound by address: each request writes at most
+ *     min(coords_capacity / 9, normals_capacity / 3) triangles (checked on the
+ *     device), and kvsmc_plan_wait reports KVSMC_ERR_CAPACITY with the full
+ *     sizes for a request whose result did not fit;
+ *   - volumes and outputs must outlive the plan; one replay in flight per plan. */
+typedef struct kvsmc_plan kvsmc_plan;
+kvsmc_status kvsmc_plan_create(kvsmc_context* ctx, const kvsmc_request* reqs, int32_t n, kvsmc_plan** out);
+/* Enqueue one replay on `cuda_stream` (NULL: the context's stream); returns at once. */
+kvsmc_status kvsmc_plan_launch(kvsmc_plan* plan, void* cuda_stream);
+/* Wait for the last replay and fill reqs[i].sizes / reqs[i].status (n = the
+ * plan's request count, same order as at creation); returns the first error. */
+kvsmc_status kvsmc_plan_wait(kvsmc_plan* plan, kvsmc_request* reqs, int32_t n);
+/* Kernel launches one replay performs. */
+uint64_t kvsmc_plan_kernels(const kvsmc_plan* plan);
+void kvsmc_plan_destroy(kvsmc_plan* plan);
+
 /* ------------------------------------------------- no-allocation variant */
 
 /* For callers that may not allocate device memory: a plugin whose host

@@ -41,6 +41,7 @@ EXPORTS = [
     "kvsmc_count_batch", "kvsmc_extract_batch", "kvsmc_set_kernel_path",
     "kvsmc_selftest_interpolation", "kvsmc_profile_enable", "kvsmc_profile_read",
     "kvsmc_extract_batch_host", "kvsmc_extract_noalloc",
+    "kvsmc_plan_create", "kvsmc_plan_launch", "kvsmc_plan_wait", "kvsmc_plan_kernels", "kvsmc_plan_destroy",
 ]
 
 PATH_AUTO = 0      # streaming kernels where eligible
@@ -125,6 +126,11 @@ def load(path=LIB_PATH):
                                                HOST_ALLOC, vp, C.POINTER(Sizes)]),
         "kvsmc_extract_noalloc": (C.c_int, [vp, C.c_int, u32, u32, u32, C.POINTER(Params), vp, u64, vp, u64,
                                             vp, C.POINTER(Sizes)]),
+        "kvsmc_plan_create": (C.c_int, [vp, C.POINTER(Request), i32, C.POINTER(vp)]),
+        "kvsmc_plan_launch": (C.c_int, [vp, vp]),
+        "kvsmc_plan_wait": (C.c_int, [vp, C.POINTER(Request), i32]),
+        "kvsmc_plan_kernels": (u64, [vp]),
+        "kvsmc_plan_destroy": (None, [vp]),
         "kvsmc_profile_enable": (C.c_int, [vp, i32]),
         "kvsmc_profile_read": (i32, [vp, i32, C.POINTER(C.c_char_p), C.POINTER(u64), C.POINTER(C.c_double)]),
     }
@@ -241,6 +247,41 @@ class DeviceVolume:
         try:
             if self.ctx.handle:
                 self.free()
+        except Exception:
+            pass
+
+
+class Plan:
+    """A replayable batch (kvsmc_plan_*): created once for a request array,
+    then launch() + wait() per extraction."""
+
+    def __init__(self, ctx, reqs):
+        self.ctx, self.reqs = ctx, reqs
+        h = C.c_void_p()
+        ctx.check(ctx.lib.kvsmc_plan_create(ctx.handle, reqs, len(reqs), C.byref(h)), "plan_create")
+        self.handle = h
+
+    @property
+    def kernels(self):
+        return int(self.ctx.lib.kvsmc_plan_kernels(self.handle))
+
+    def launch(self, cuda_stream_ptr=None):
+        self.ctx.check(self.ctx.lib.kvsmc_plan_launch(self.handle, cuda_stream_ptr), "plan_launch")
+
+    def wait(self, check=True):
+        st = self.ctx.lib.kvsmc_plan_wait(self.handle, self.reqs, len(self.reqs))
+        if check:
+            self.ctx.check(st, "plan_wait")
+        return st
+
+    def close(self):
+        if self.handle:
+            self.ctx.lib.kvsmc_plan_destroy(self.handle)
+            self.handle = None
+
+    def __del__(self):
+        try:
+            self.close()
         except Exception:
             pass
 

@@ -98,6 +98,49 @@ Classifier make_classifier(double iso)
     return c;
 }
 
+kvsmc_status volume_bricks(kvsmc_context* ctx, kvsmc_volume* v)
+{
+    v->bricks_valid = false;
+    const int dt = v->view.dtype;
+    const bool ok = (dt == KVSMC_I8 || dt == KVSMC_I16 || dt == KVSMC_U8 || dt == KVSMC_U16 || dt == KVSMC_F32) &&
+                    v->view.nx - 1 <= (uint32_t)kvsmc::kStreamMaxCells;
+    if (!ok) return KVSMC_OK;
+    const int rows = stream_rows(v->view.nx - 1);
+    const size_t bytes = kvsmc::brick_count(v->view, rows) * sizeof(float2);
+    if (bytes > v->brick_bytes) {
+        if (v->bricks) cudaFree(v->bricks);
+        v->bricks = nullptr;
+        v->brick_bytes = 0;
+        KVSMC_CUDA(ctx, cudaMalloc(&v->bricks, bytes));
+        v->brick_bytes = bytes;
+    }
+    KVSMC_CUDA(ctx, kvsmc::launch_bricks(v->view, rows, v->bricks, launch_of(ctx)));
+    v->brick_rows = rows;
+    v->bricks_valid = true;
+    return KVSMC_OK;
+}
+
+// Decide min/max (MapperBase::setRange) and the Equal early exit.
+kvsmc_status prepare(kvsmc_context* ctx, Item& it)
+{
+    if (!it.vol) return fail(ctx, KVSMC_ERR_INVALID_ARGUMENT, "null volume");
+    if (it.params.mode < 0 || it.params.mode > 2) return fail(ctx, KVSMC_ERR_INVALID_ARGUMENT, "bad mode %d", it.params.mode);
+    if (it.params.has_minmax) {
+        it.vmin = it.params.min_value;
+        it.vmax = it.params.max_value;
+    } else {
+        kvsmc_status st = volume_minmax(ctx, it.vol);
+        if (st) return st;
+        it.vmin = it.vol->vmin;
+        it.vmax = it.vol->vmax;
+    }
+    it.extracted = !equal_ref(it.vmin, it.vmax);
+    std::memset(&it.sizes, 0, sizeof it.sizes);
+    it.sizes.min_value = it.vmin;
+    it.sizes.max_value = it.vmax;
+    return KVSMC_OK;
+}
+
 }  // namespace kvsmc_host
 
 using namespace kvsmc_host;
@@ -270,27 +313,6 @@ kvsmc_status gather_emit(kvsmc_context* ctx, Plan& pl, float* coords, float* nor
 }
 
 // ------------------------------------------------------------ request setup
-
-// Decide min/max (MapperBase::setRange) and the Equal early exit.
-kvsmc_status prepare(kvsmc_context* ctx, Item& it)
-{
-    if (!it.vol) return fail(ctx, KVSMC_ERR_INVALID_ARGUMENT, "null volume");
-    if (it.params.mode < 0 || it.params.mode > 2) return fail(ctx, KVSMC_ERR_INVALID_ARGUMENT, "bad mode %d", it.params.mode);
-    if (it.params.has_minmax) {
-        it.vmin = it.params.min_value;
-        it.vmax = it.params.max_value;
-    } else {
-        kvsmc_status st = volume_minmax(ctx, it.vol);
-        if (st) return st;
-        it.vmin = it.vol->vmin;
-        it.vmax = it.vol->vmax;
-    }
-    it.extracted = !equal_ref(it.vmin, it.vmax);
-    std::memset(&it.sizes, 0, sizeof it.sizes);
-    it.sizes.min_value = it.vmin;
-    it.sizes.max_value = it.vmax;
-    return KVSMC_OK;
-}
 
 bool capacity_ok(const Item& it)
 {
@@ -469,7 +491,8 @@ kvsmc_status kvsmc_volume_upload(kvsmc_context* ctx, const void* host, kvsmc_dty
     if (!host || !out) return fail(ctx, KVSMC_ERR_INVALID_ARGUMENT, "null pointer");
     if ((st = check_shape(ctx, dtype, nx, ny, nz))) return st;
     kvsmc_volume* v = new kvsmc_volume();
-    if ((st = volume_alloc(ctx, dtype, nx, ny, nz, v)) || (st = volume_copy_in(ctx, v, host, cudaMemcpyHostToDevice))) {
+    if ((st = volume_alloc(ctx, dtype, nx, ny, nz, v)) || (st = volume_copy_in(ctx, v, host, cudaMemcpyHostToDevice)) ||
+        (st = volume_bricks(ctx, v))) {
         if (v->dev) cudaFree(v->dev);
         delete v;
         return st;
@@ -486,7 +509,8 @@ kvsmc_status kvsmc_volume_from_device(kvsmc_context* ctx, const void* dev, kvsmc
     if (!dev || !out) return fail(ctx, KVSMC_ERR_INVALID_ARGUMENT, "null pointer");
     if ((st = check_shape(ctx, dtype, nx, ny, nz))) return st;
     kvsmc_volume* v = new kvsmc_volume();
-    if ((st = volume_alloc(ctx, dtype, nx, ny, nz, v)) || (st = volume_copy_in(ctx, v, dev, cudaMemcpyDeviceToDevice))) {
+    if ((st = volume_alloc(ctx, dtype, nx, ny, nz, v)) || (st = volume_copy_in(ctx, v, dev, cudaMemcpyDeviceToDevice)) ||
+        (st = volume_bricks(ctx, v))) {
         if (v->dev) cudaFree(v->dev);
         delete v;
         return st;
@@ -500,7 +524,8 @@ kvsmc_status kvsmc_volume_update(kvsmc_context* ctx, kvsmc_volume* v, const void
     kvsmc_status st = use_device(ctx);
     if (st) return st;
     if (!v || !host) return fail(ctx, KVSMC_ERR_INVALID_ARGUMENT, "null pointer");
-    return volume_copy_in(ctx, v, host, cudaMemcpyHostToDevice);
+    if ((st = volume_copy_in(ctx, v, host, cudaMemcpyHostToDevice))) return st;
+    return v->bricks_valid ? volume_bricks(ctx, v) : KVSMC_OK;
 }
 
 void kvsmc_volume_free(kvsmc_context* ctx, kvsmc_volume* v)
@@ -511,6 +536,7 @@ void kvsmc_volume_free(kvsmc_context* ctx, kvsmc_volume* v)
         cudaStreamSynchronize(ctx->stream);
     }
     if (v->dev) cudaFree(v->dev);
+    if (v->bricks) cudaFree(v->bricks);
     delete v;
 }
 

@@ -18,9 +18,10 @@ namespace {
 
 bool stream_dtype(int dt) { return dt == KVSMC_I8 || dt == KVSMC_I16 || dt == KVSMC_U8 || dt == KVSMC_U16 || dt == KVSMC_F32; }
 
-uint32_t segments_per_row(const kvsmc::VolumeView& v)
+uint32_t segments_per_row(const kvsmc::VolumeView& v, int rows)
 {
-    return (v.nx - 1 + kvsmc::kStreamSegCells - 1) / kvsmc::kStreamSegCells;
+    const uint32_t seg = kvsmc::kStreamSegCells / rows;
+    return (v.nx - 1 + seg - 1) / seg;
 }
 
 }  // namespace
@@ -73,9 +74,23 @@ void bucket_params(float t0, float t1, float& bs, float& bo)
     }
 }
 
-uint32_t stream_zchunk(const kvsmc::VolumeView& v, uint32_t wpr, int num_sms)
+uint64_t cap_triangles(const Item& it)
 {
-    const uint64_t warp_steps = (uint64_t)(v.nz - 1) * (v.ny - 1) * wpr;
+    const uint64_t a = it.d_coords ? it.coords_cap / 9 : 0, b = it.d_normals ? it.normals_cap / 3 : 0;
+    return a < b ? a : b;
+}
+
+int stream_rows(uint32_t cx)
+{
+    // two 128-cell rows per warp when that leaves fewer idle lanes than one
+    // 256-cell row (narrow volumes, or a last segment of at most 128 cells);
+    // on a tie one row (fewer, longer units)
+    const uint32_t w1 = (cx + 255) / 256 * 256, w2 = (cx + 127) / 128 * 128;
+    return w2 < w1 ? 2 : 1;
+}
+
+uint32_t stream_zchunk(uint64_t warp_steps, int num_sms)
+{
     const uint64_t want_tasks = (uint64_t)num_sms * 24 * 4;
     uint64_t zc = (warp_steps + want_tasks - 1) / want_tasks;
     if (zc < 4) zc = 4;
@@ -90,15 +105,15 @@ bool stream_eligible(const kvsmc_context* ctx, const Item& it)
     const kvsmc::VolumeView& v = it.vol->view;
     if (!stream_dtype(v.dtype)) return false;
     if (v.nx < 2 || v.ny < 2 || v.nz < 2) return false;
-    if (segments_per_row(v) > (uint32_t)kvsmc::kStreamMaxSegments) return false;
+    if (v.nx - 1 > (uint32_t)kvsmc::kStreamMaxCells) return false;
     // triangles of one (isolevel, z) plane must fit the u32 plane offsets
     if ((double)(v.nx - 1) * (double)(v.ny - 1) * 5.0 >= 4294967295.0) return false;
     const double iso = it.params.isolevel;
     if (!std::isfinite(iso) || std::fabs(iso) > 1.0e30) return false;
-    return kvsmc::stream_shared_bytes(v.dtype, true) <= (size_t)227 * 1024;
+    return kvsmc::stream_shared_bytes(v.dtype, true, stream_rows(v.nx - 1)) <= (size_t)227 * 1024;
 }
 
-kvsmc_status StreamBatch::plan()
+void StreamBatch::plan_tables()
 {
     // group by volume in request order, at most kStreamMaxIso per group
     std::vector<std::vector<Item*>> lists;
@@ -112,10 +127,14 @@ kvsmc_status StreamBatch::plan()
         }
         lists[f->second].push_back(it);
     }
-    std::vector<int> dtypes;
+    // one launch per (value type, rows per warp) present
+    std::vector<std::pair<int, int>> kinds;
+    auto kind_of = [](const std::vector<Item*>& l) {
+        const kvsmc::VolumeView& v = l[0]->vol->view;
+        return std::make_pair((int)v.dtype, stream_rows(v.nx - 1));
+    };
     for (auto& l : lists)
-        if (std::find(dtypes.begin(), dtypes.end(), l[0]->vol->view.dtype) == dtypes.end())
-            dtypes.push_back(l[0]->vol->view.dtype);
+        if (std::find(kinds.begin(), kinds.end(), kind_of(l)) == kinds.end()) kinds.push_back(kind_of(l));
     groups.clear();
     isos.clear();
     iso_item.clear();
@@ -123,26 +142,40 @@ kvsmc_status StreamBatch::plan()
     unit_elems = 0;
     scan_blocks = 0;
     iso_planes = 0;
-    for (int dt : dtypes) {
+    for (const auto& kd : kinds) {
+        const int dt = kd.first, rows = kd.second;
         Launch1 L;
         L.dtype = dt;
+        L.rows = rows;
         L.g0 = (int)groups.size();
         L.ntasks = 0;
+        // one z-chunk for the whole launch: sized by all its warp steps, so a
+        // batch of small volumes gets long tasks rather than many short ones
+        uint64_t steps = 0;
         for (auto& l : lists) {
-            if (l[0]->vol->view.dtype != dt) continue;
+            if (kind_of(l) != kd) continue;
+            const kvsmc::VolumeView& v = l[0]->vol->view;
+            steps += (uint64_t)(v.nz - 1) * ((v.ny - 1 + rows - 1) / rows) * segments_per_row(v, rows);
+        }
+        const uint32_t zchunk = stream_zchunk(steps, ctx->num_sms);
+        for (auto& l : lists) {
+            if (kind_of(l) != kd) continue;
             const kvsmc::VolumeView v = l[0]->vol->view;
             StreamGroup g;
             std::memset(&g, 0, sizeof g);
             g.vol = v;
-            g.wpr = segments_per_row(v);
-            g.zchunk = stream_zchunk(v, g.wpr, ctx->num_sms);
+            g.rows = (uint32_t)rows;
+            const kvsmc_volume* vol = l[0]->vol;
+            g.bricks = (vol->bricks_valid && vol->brick_rows == rows) ? vol->bricks : nullptr;
+            g.wpr = segments_per_row(v, rows);
+            g.zchunk = zchunk;
             const uint32_t cy = v.ny - 1, cz = v.nz - 1;
             const uint32_t zchunks = (cz + g.zchunk - 1) / g.zchunk;
             g.task_begin = L.ntasks;
-            L.ntasks += (uint64_t)cy * g.wpr * zchunks;
-            g.seg_elems = (uint32_t)kvsmc::stream_row_elems(dt);
+            L.ntasks += (uint64_t)((cy + rows - 1) / rows) * g.wpr * zchunks;
+            g.seg_elems = (uint32_t)kvsmc::stream_row_elems(dt, rows);
             g.seg_copy_bytes = g.seg_elems * (uint32_t)kvsmc::dtype_size(dt);
-            g.warp_smem_bytes = (uint32_t)kvsmc::stream_warp_smem_bytes(dt, true);
+            g.warp_smem_bytes = (uint32_t)kvsmc::stream_warp_smem_bytes(dt, true, rows);
             g.warp_smem_offset = (uint32_t)kvsmc::stream_warp_smem_offset();
             // isolevels sorted by threshold
             std::vector<std::pair<float, Item*>> sorted;
@@ -175,16 +208,21 @@ kvsmc_status StreamBatch::plan()
         L.ng = (int)groups.size() - L.g0;
         launches.push_back(L);
     }
+}
 
-    // device scratch
+size_t StreamBatch::scratch_bytes() const
+{
     const size_t niso = isos.size();
-    const size_t need = 16 * 256 + align_up(groups.size() * sizeof(StreamGroup), 256) +
-                        align_up(niso * sizeof(StreamIso), 256) + align_up(unit_elems * 2, 256) +
-                        align_up(unit_elems * 4, 256) + align_up(iso_planes * 4, 256) + align_up(iso_planes * 8, 256) +
-                        align_up(kvsmc::scan_scratch_bytes(iso_planes), 256) + align_up(niso * 8, 256) + 4 * 256;
-    kvsmc_status st = ensure_scratch(ctx, need);
-    if (st) return st;
-    Carve cv{static_cast<char*>(ctx->scratch)};
+    return 16 * 256 + align_up(groups.size() * sizeof(StreamGroup), 256) + align_up(niso * sizeof(StreamIso), 256) +
+           align_up(unit_elems * 2, 256) + align_up(unit_elems * 4, 256) + align_up(iso_planes * 4, 256) +
+           align_up(iso_planes * 8, 256) + align_up(kvsmc::scan_scratch_bytes(iso_planes), 256) +
+           align_up(niso * 8, 256) + 4 * 256;
+}
+
+void StreamBatch::carve(char* base)
+{
+    const size_t niso = isos.size();
+    Carve cv{base};
     d_groups = cv.take<StreamGroup>(groups.size() * sizeof(StreamGroup));
     d_isos = cv.take<StreamIso>(niso * sizeof(StreamIso));
     d_unit_counts = cv.take<uint16_t>(unit_elems * 2);
@@ -195,6 +233,14 @@ kvsmc_status StreamBatch::plan()
     d_totals = cv.take<uint64_t>(niso * 8);
     d_total = cv.take<uint64_t>(256);
     d_status = cv.take<int>(256);
+}
+
+kvsmc_status StreamBatch::plan()
+{
+    plan_tables();
+    kvsmc_status st = ensure_scratch(ctx, scratch_bytes());
+    if (st) return st;
+    carve(static_cast<char*>(ctx->scratch));
     return upload_tables();
 }
 
@@ -215,8 +261,10 @@ kvsmc_status StreamBatch::count()
 {
     const kvsmc::Launch L = launch_of(ctx);
     KVSMC_CUDA(ctx, cudaMemsetAsync(d_status, 0, sizeof(int), ctx->stream));
+    // units the kernels skip as empty space keep these zeros
+    KVSMC_CUDA(ctx, cudaMemsetAsync(d_unit_counts, 0, unit_elems * sizeof(uint16_t), ctx->stream));
     for (const Launch1& l : launches)
-        KVSMC_CUDA(ctx, kvsmc::launch_stream(false, l.dtype, d_groups + l.g0, l.ng, l.ntasks, d_isos, d_unit_counts,
+        KVSMC_CUDA(ctx, kvsmc::launch_stream(false, l.dtype, l.rows, d_groups + l.g0, l.ng, l.ntasks, d_isos, d_unit_counts,
                                              nullptr, nullptr, d_status, L));
     KVSMC_CUDA(ctx, kvsmc::launch_unit_scan(d_groups, (int)groups.size(), scan_blocks, d_isos, d_unit_counts,
                                             d_unit_offsets, d_plane_totals, L));
@@ -256,6 +304,7 @@ kvsmc_status StreamBatch::emit()
         const bool ok = it->emit && it->status == KVSMC_OK && it->sizes.ntriangles > 0;
         isos[i].coords = ok ? it->d_coords : nullptr;
         isos[i].normals = ok ? it->d_normals : nullptr;
+        isos[i].cap_tris = ok ? cap_triangles(*it) : 0;
         any = any || ok;
     }
     if (!any) return KVSMC_OK;
@@ -263,7 +312,7 @@ kvsmc_status StreamBatch::emit()
     if (st) return st;
     const kvsmc::Launch L = launch_of(ctx);
     for (const Launch1& l : launches)
-        KVSMC_CUDA(ctx, kvsmc::launch_stream(true, l.dtype, d_groups + l.g0, l.ng, l.ntasks, d_isos, nullptr,
+        KVSMC_CUDA(ctx, kvsmc::launch_stream(true, l.dtype, l.rows, d_groups + l.g0, l.ng, l.ntasks, d_isos, nullptr,
                                              d_unit_offsets, d_plane_base, d_status, L));
     return KVSMC_OK;
 }

@@ -11,9 +11,14 @@ kvsmc::FastIso make_fast(double iso, double vmin, double vmax, int dtype);
 // Bucket parameters of a group's sorted thresholds.
 void bucket_params(float t0, float t1, float& bs, float& bo);
 
-// Cell planes per warp task for a volume (enough tasks to fill the GPU, at
-// most 64 planes so the one-plane halo of a task stays small).
-uint32_t stream_zchunk(const kvsmc::VolumeView& v, uint32_t wpr, int num_sms);
+// Cell planes per warp task for a launch of `warp_steps` (row segment, plane)
+// steps in all: enough tasks to fill the GPU, 4 to 64 planes per task (the
+// one-plane halo a task re-reads stays small).
+uint32_t stream_zchunk(uint64_t warp_steps, int num_sms);
+
+// Cell rows per warp task for rows of cx cells: 2 (128-cell segments) when
+// that idles fewer lanes than 256-cell segments, else 1.
+int stream_rows(uint32_t cx);
 
 // A batch of streaming-eligible requests.  plan() builds the work tables,
 // count() fills every item's sizes, emit() writes the outputs of the items
@@ -25,6 +30,7 @@ struct StreamBatch {
 
     struct Launch1 {
         int dtype;
+        int rows;
         int g0, ng;
         uint64_t ntasks;
     };
@@ -52,8 +58,15 @@ struct StreamBatch {
     kvsmc_status emit();
     kvsmc_status finish();
 
-  private:
+    // The pieces of plan(): host tables, their device footprint, and the
+    // device pointers carved from a region of scratch_bytes().
+    void plan_tables();
+    size_t scratch_bytes() const;
+    void carve(char* base);
     kvsmc_status upload_tables();
 };
+
+// Triangles an item's output buffers hold (coords / 9, normals / 3).
+uint64_t cap_triangles(const Item& it);
 
 }  // namespace kvsmc_host

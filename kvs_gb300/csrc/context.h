@@ -13,6 +13,12 @@ struct kvsmc_volume {
     size_t bytes = 0;
     bool has_minmax = false;
     double vmin = 0.0, vmax = 0.0;
+    // brick min/max table (streaming kernels' empty-space skip), rebuilt after
+    // every copy into a resident volume; valid for brick_rows rows per task
+    float2* bricks = nullptr;
+    size_t brick_bytes = 0;
+    int brick_rows = 0;
+    bool bricks_valid = false;
 };
 
 struct kvsmc_context {
@@ -81,6 +87,14 @@ struct Item {
     kvsmc_sizes sizes{};
     kvsmc_status status = KVSMC_OK;
 };
+
+// (Re)build a resident volume's brick min/max table on the context's stream
+// (no-op for value types or widths the streaming kernels do not take).
+kvsmc_status volume_bricks(kvsmc_context* ctx, kvsmc_volume* v);
+
+// Decide min/max (MapperBase::setRange, the volume's cache or a preset) and
+// the Math::Equal early exit; fills it.vmin/vmax/extracted and clears sizes.
+kvsmc_status prepare(kvsmc_context* ctx, Item& it);
 
 // Requests the streaming kernels can take (duplicated mode, 8/16-bit and
 // float32 data, finite isolevel, width <= 4096 cells).

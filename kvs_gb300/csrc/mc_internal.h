@@ -47,8 +47,8 @@ cudaError_t launch_vertex_normals(const Job& j, const Launch& L);
 constexpr int kStreamThreads = 256;   // 8 independent warps per CTA
 constexpr int kStreamMaxIso = 16;     // isolevels of one volume per group
 constexpr int kStreamBuckets = 128;   // threshold lookup buckets
-constexpr int kStreamSegCells = 256;  // cells per warp segment
-constexpr int kStreamMaxSegments = 16;  // segments per row (width <= 4096 cells)
+constexpr int kStreamSegCells = 256;  // cells per warp step (one 256-cell row segment, or two of 128)
+constexpr int kStreamMaxCells = 4096; // cells per row (width <= 4097 nodes)
 
 // One isolevel request inside a streaming launch.
 struct StreamIso {
@@ -57,6 +57,7 @@ struct StreamIso {
     uint64_t plane_index;  // its first (isolevel, z) plane in the plane arrays
     float* coords;         // outputs (null: not written)
     float* normals;
+    uint64_t cap_tris;     // triangles the outputs hold: later ones are not written
 };
 
 // One volume with up to kStreamMaxIso isolevels, sorted by threshold.
@@ -65,7 +66,8 @@ struct StreamIso {
 struct StreamGroup {
     VolumeView vol;
     int32_t iso_begin, niso;
-    uint32_t wpr;            // 256-cell segments per cell row
+    uint32_t rows;           // cell rows per warp task: 1 (256-cell segments) or 2 (128-cell segments)
+    uint32_t wpr;            // segments per cell row
     uint32_t zchunk;         // cell planes per warp task
     uint64_t task_begin;     // first warp task of this group in its launch
     uint64_t unit_base;      // first element of its (unit, isolevel) counters
@@ -75,13 +77,22 @@ struct StreamGroup {
     uint32_t warp_smem_bytes;
     uint32_t warp_smem_offset;
     float bs, bo;            // bucket(v) = floor(kStreamBuckets * sat(v * bs + bo)), in [0, kStreamBuckets]
+    const float2* bricks;    // per brick (8 cell planes x 2 cell rows x one segment) node min/max, or null
 };
 
-size_t stream_shared_bytes(int dtype, bool emit);
-size_t stream_warp_smem_bytes(int dtype, bool emit);
+// Brick min/max table of a volume for `rows` cell rows per warp task: one
+// float2 per (8 cell planes, 2 cell rows, one row segment) brick, the min and
+// max of its node box ((-inf, +inf) when it holds a NaN), bricks numbered
+// segment fastest, then row pair, then plane group.
+constexpr int kBrickPlanes = 8;
+uint64_t brick_count(const VolumeView& v, int rows);
+cudaError_t launch_bricks(const VolumeView& v, int rows, float2* out, const Launch& L);
+
+size_t stream_shared_bytes(int dtype, bool emit, int rows);
+size_t stream_warp_smem_bytes(int dtype, bool emit, int rows);
 size_t stream_warp_smem_offset();
-size_t stream_row_elems(int dtype);
-cudaError_t launch_stream(bool emit, int dtype, const StreamGroup* d_groups, int ngroups, uint64_t ntasks,
+size_t stream_row_elems(int dtype, int rows);
+cudaError_t launch_stream(bool emit, int dtype, int rows, const StreamGroup* d_groups, int ngroups, uint64_t ntasks,
                           const StreamIso* d_isos, uint16_t* d_unit_counts, const uint32_t* d_unit_offsets,
                           const uint64_t* d_plane_base, int* d_status, const Launch& L);
 cudaError_t launch_unit_scan(const StreamGroup* d_groups, int ngroups, uint32_t nplanes, const StreamIso* d_isos,

@@ -173,8 +173,8 @@ struct WarpState {
     uint64_t bar[3];
     float thr[kStreamMaxIso];
     int32_t thr_bucket[kStreamMaxIso];
-    uint32_t cnt[kStreamMaxIso];             // count: triangles of the current unit
-    uint32_t add[kStreamMaxIso];             // emit: per-isolevel advance of the current round
+    uint32_t cnt[32];                        // count: triangles of the current units, [row][isolevel]
+    uint32_t add[32];                        // emit: per-(row, isolevel) advance of the current round
     // bucket -> (thermometer mask of the thresholds in lower buckets | kMultiThr,
     //            bits of the bucket's first threshold, +inf when it has none)
     uint2 lut[kLut];
@@ -246,6 +246,20 @@ __device__ __forceinline__ void row_masks(const T* row, uint32_t x0, const WarpS
     P[4] = e[8];
 }
 
+// Thermometer mask of one value (the per-node rule of row_masks).
+__device__ __forceinline__ uint32_t value_mask(const WarpState& W, int niso, float bs, float bo, float v)
+{
+    const uint32_t b = bucket_index(v, bs, bo);
+    const uint2 l = W.lut[b];
+    uint32_t e = (v > __int_as_float((int)l.y)) ? 2u * l.x + 1u : l.x;
+    if (l.x & kMultiThr) {
+        int k = __popc(l.x & 0xffffu);
+        while (k < niso && (uint32_t)W.thr_bucket[k] == b && W.thr[k] < v) ++k;
+        e = (1u << k) - 1u;
+    }
+    return e & 0xffffu;
+}
+
 // The row word of cell i (0..7): node i in the low half, node i+1 in the high half.
 __device__ __forceinline__ uint32_t cell_word(const uint32_t* P, int i)
 {
@@ -293,12 +307,18 @@ __device__ __forceinline__ int find_group(const StreamGroup* groups, int ngroups
     return lo;
 }
 
-template <typename T, bool EMIT>
+// R = cell rows per warp task (1 or 2).  With R = 2, lanes 0-15 take row y
+// and lanes 16-31 row y+1, each over a 128-cell segment, so narrow volumes
+// keep every lane busy and a node row is staged for 1.5 cell rows, not 2.
+template <typename T, bool EMIT, int R>
 __global__ void __launch_bounds__(kStreamThreads, EMIT ? 2 : 3)
     k_stream(const StreamGroup* __restrict__ groups, int ngroups, uint64_t ntasks, const StreamIso* __restrict__ isos,
              uint16_t* __restrict__ unit_counts, const uint32_t* __restrict__ unit_offsets,
              const uint64_t* __restrict__ plane_base, int* __restrict__ status)
 {
+    constexpr int LPR = 32 / R;                 // lanes per cell row
+    constexpr int SEG = kSegCells / R;          // cells per row segment
+    constexpr int SEG_SHIFT = R == 1 ? 8 : 7;   // log2(SEG)
     extern __shared__ __align__(128) unsigned char smem_raw[];
     const unsigned tid = threadIdx.x, lane = tid & 31u, warp = tid >> 5;
     Tables& TB = *reinterpret_cast<Tables*>(smem_raw);
@@ -325,30 +345,33 @@ __global__ void __launch_bounds__(kStreamThreads, EMIT ? 2 : 3)
     const uint64_t local = task - G.task_begin;
     const uint32_t cx = G.vol.nx - 1, cy = G.vol.ny - 1, cz = G.vol.nz - 1;
     const uint32_t wpr = G.wpr;
+    const uint32_t cyr = (cy + R - 1) / R;   // row groups
     const uint32_t seg = (uint32_t)(local % wpr);
-    const uint32_t y = (uint32_t)((local / wpr) % cy);
-    const uint32_t zc = (uint32_t)(local / ((uint64_t)wpr * cy));
+    const uint32_t y = (uint32_t)((local / wpr) % cyr) * R;
+    const uint32_t zc = (uint32_t)(local / ((uint64_t)wpr * cyr));
     const uint32_t z0 = zc * G.zchunk;
     const uint32_t z1 = (z0 + G.zchunk < cz) ? z0 + G.zchunk : cz;   // cell planes [z0, z1)
     const int niso = G.niso;
     const float bs = G.bs, bo = G.bo;
     const int iso_begin = G.iso_begin;
     const uint64_t unit_base = G.unit_base;
+    const uint32_t nrows = (y + R + 1 <= G.vol.ny) ? R + 1 : G.vol.ny - y;   // node rows staged per plane
 
     // per-warp shared memory: state, then (emit) buffers, then the row ring
     // (the same layout as stream_warp_smem_bytes on the host)
     const uint32_t row_elems = G.seg_elems;              // staged elements per row
+    const uint32_t plane_elems = (R + 1) * row_elems;
     const size_t wstride = align128(sizeof(WarpState)) + (EMIT ? align128(sizeof(WarpEmit)) : 0) +
-                           align128((size_t)3 * 2 * row_elems * sizeof(T));
+                           align128((size_t)3 * plane_elems * sizeof(T));
     unsigned char* wbase = smem_raw + align128(sizeof(Tables)) + (size_t)warp * wstride;
     WarpState& W = *reinterpret_cast<WarpState*>(wbase);
     WarpEmit* WE = reinterpret_cast<WarpEmit*>(wbase + align128(sizeof(WarpState)));
     T* ring = reinterpret_cast<T*>(wbase + align128(sizeof(WarpState)) + (EMIT ? align128(sizeof(WarpEmit)) : 0));
     const uint64_t pitch = G.vol.pitch;
     const uint64_t slice = G.vol.slice;
-    const uint64_t xoff = (uint64_t)seg * kSegCells;
-    // bytes copied per row: 257 values rounded up to 16 bytes, or up to the end
-    // of the (16-byte padded) row for the last segment
+    const uint64_t xoff = (uint64_t)seg * SEG;
+    // bytes copied per row: SEG + 1 values rounded up to 16 bytes, or up to the
+    // end of the (16-byte padded) row for the last segment
     const uint64_t avail = (pitch - xoff) * sizeof(T);
     const uint32_t row_bytes = (uint32_t)(avail < G.seg_copy_bytes ? avail : G.seg_copy_bytes);
     const T* vol = static_cast<const T*>(G.vol.data);
@@ -357,9 +380,9 @@ __global__ void __launch_bounds__(kStreamThreads, EMIT ? 2 : 3)
         const float t = isos[iso_begin + lane].f.f_thr;
         W.thr[lane] = t;
         W.thr_bucket[lane] = (int32_t)bucket_index(t, bs, bo);
-        W.cnt[lane] = 0;
-        W.add[lane] = 0;
     }
+    W.cnt[lane] = 0;
+    W.add[lane] = 0;
     __syncwarp();
     for (unsigned b = lane; b < (unsigned)kLut; b += 32) {
         uint32_t below = 0, in = 0;
@@ -376,26 +399,44 @@ __global__ void __launch_bounds__(kStreamThreads, EMIT ? 2 : 3)
     }
     __syncwarp();
 
+    // empty space: a brick whose node min and max have the same mask (no
+    // threshold between them) holds no active cell for any isolevel
+    const float2* bricks = G.bricks;
+    const uint32_t nby = (cy + 1) / 2;
+    auto brick_empty = [&](uint32_t z) -> bool {
+        const float2 mm = bricks[((uint64_t)(z / kBrickPlanes) * nby + (y >> 1)) * wpr + seg];
+        return value_mask(W, niso, bs, bo, mm.x) == value_mask(W, niso, bs, bo, mm.y);
+    };
+    if (bricks) {
+        bool all_empty = true;
+        for (uint32_t z = z0; z < z1 && all_empty; z = (z / kBrickPlanes + 1) * kBrickPlanes) all_empty = brick_empty(z);
+        if (all_empty) return;   // nothing to count or emit (counts are zeroed before the count pass)
+    }
+
     auto issue = [&](uint32_t plane) {
         const uint32_t i = plane - z0;
         const int b = (int)(i % 3u);
-        T* dst = ring + (size_t)b * 2 * row_elems;
+        T* dst = ring + (size_t)b * plane_elems;
         const T* src = vol + (uint64_t)plane * slice + (uint64_t)y * pitch + xoff;
-        mbar_arrive_expect_tx(&W.bar[b], 2 * row_bytes);
-        bulk_copy_g2s(dst, src, row_bytes, &W.bar[b]);
-        bulk_copy_g2s(dst + row_elems, src + pitch, row_bytes, &W.bar[b]);
+        mbar_arrive_expect_tx(&W.bar[b], nrows * row_bytes);
+        for (uint32_t r = 0; r < nrows; ++r) bulk_copy_g2s(dst + r * row_elems, src + r * pitch, row_bytes, &W.bar[b]);
     };
     if (lane == 0) {
         for (uint32_t p = z0; p <= z1 && p < z0 + 3; ++p) issue(p);
     }
 
-    const uint32_t xl = lane * kLaneCells;              // first cell of this lane inside the segment
-    const int lim = (int)cx - (int)((uint32_t)xoff + xl);   // cells of this lane inside the volume (if < 8)
+    const uint32_t half = lane / LPR;                     // this lane's row: y + half
+    const uint32_t xl = (lane % LPR) * kLaneCells;        // first cell of this lane inside the segment
+    const bool row_ok = y + half < cy;
+    // cells of this lane inside the volume (if < 8)
+    const int lim = row_ok ? (int)cx - (int)((uint32_t)xoff + xl) : 0;
     const unsigned lt = (1u << lane) - 1u;
     const float fy = __uint2float_rn(y);
     bool dead = false;
     uint32_t s_break = 0;
-    uint32_t PA0[5], PA1[5];   // masks of plane z, rows y and y+1 (carried from the previous step)
+    uint32_t PA0[5], PA1[5];   // masks of plane z, this lane's rows (carried from the previous step)
+    bool pa_valid = false;
+    bool skip = false;         // the current brick is empty
 
     for (uint32_t z = z0; z < z1; ++z) {
         const uint32_t s = z - z0;
@@ -407,15 +448,26 @@ __global__ void __launch_bounds__(kStreamThreads, EMIT ? 2 : 3)
             s_break = s;
             break;
         }
-        const T* ra0 = ring + (size_t)(s % 3u) * 2 * row_elems;
+        const T* pa = ring + (size_t)(s % 3u) * plane_elems;         // plane z
+        const T* pb = ring + (size_t)((s + 1) % 3u) * plane_elems;   // plane z + 1
+        const T* ra0 = pa + half * row_elems;
         const T* ra1 = ra0 + row_elems;
-        const T* rb0 = ring + (size_t)((s + 1) % 3u) * 2 * row_elems;
+        const T* rb0 = pb + half * row_elems;
         const T* rb1 = rb0 + row_elems;
-        const uint64_t unit = ((uint64_t)z * cy + y) * wpr + seg;
         const float fz = __uint2float_rn(z);
+        if (bricks && (s == 0 || z % kBrickPlanes == 0)) skip = brick_empty(z);
+        if (skip) {
+            pa_valid = false;
+            __syncwarp();
+            if (lane == 0 && z + 3 <= z1) {
+                fence_proxy_async();
+                issue(z + 3);
+            }
+            continue;
+        }
 
         // ---------------- phase 1: node masks, per-cell active isolevels
-        if (s == 0) {
+        if (!pa_valid) {
             row_masks<T>(ra0, xl, W, niso, bs, bo, PA0);
             row_masks<T>(ra1, xl, W, niso, bs, bo, PA1);
         }
@@ -440,7 +492,7 @@ __global__ void __launch_bounds__(kStreamThreads, EMIT ? 2 : 3)
             act[w] = o & ~a;
         }
         if (lim < kLaneCells) {
-            // cells past the last one of the row: none
+            // cells past the last one of the row, or rows past the last: none
 #pragma unroll
             for (int w = 0; w < 4; ++w) {
                 const uint32_t keep = (2 * w < lim ? 0xffffu : 0u) | (2 * w + 1 < lim ? 0xffff0000u : 0u);
@@ -451,7 +503,7 @@ __global__ void __launch_bounds__(kStreamThreads, EMIT ? 2 : 3)
         for (int w = 0; w < 4; ++w) m += __popc(act[w]);
 
         if (!EMIT) {
-            // count: one u16 per (unit, isolevel)
+            // count: one u16 per (unit, isolevel); counters [row][isolevel]
             if (__any_sync(FULL, m != 0)) {
 #pragma unroll
                 for (int i = 0; i < kLaneCells; ++i) {
@@ -462,14 +514,16 @@ __global__ void __launch_bounds__(kStreamThreads, EMIT ? 2 : 3)
                         do {
                             const uint32_t k = __ffs(am) - 1;
                             am &= am - 1;
-                            atomicAdd(&W.cnt[k], (uint32_t)TB.ntri[case_code(w0, w1, w2, w3, k)]);
+                            atomicAdd(&W.cnt[half * 16 + k], (uint32_t)TB.ntri[case_code(w0, w1, w2, w3, k)]);
                         } while (am);
                     }
                 }
                 __syncwarp();
             }
-            if (lane < (unsigned)niso) {
-                unit_counts[unit_base + unit * niso + lane] = (uint16_t)W.cnt[lane];
+            const uint32_t h = lane >> 4, k = lane & 15u;
+            if (h < (uint32_t)R && k < (uint32_t)niso && y + h < cy) {
+                const uint64_t unit = ((uint64_t)z * cy + y + h) * wpr + seg;
+                unit_counts[unit_base + unit * niso + k] = (uint16_t)W.cnt[lane];
                 W.cnt[lane] = 0;
             }
         } else {
@@ -477,18 +531,23 @@ __global__ void __launch_bounds__(kStreamThreads, EMIT ? 2 : 3)
             const uint32_t inc = warp_inclusive_scan(m, lane);
             const uint32_t npairs = __shfl_sync(FULL, inc, 31);
             if (npairs) {
-                // lane k holds the next output triangle of isolevel k for this unit
+                // lane 16 h + k holds the next output triangle of isolevel k in row y + h
                 uint64_t run = 0;
-                if (lane < (unsigned)niso) {
-                    const StreamIso& I = isos[iso_begin + lane];
-                    run = plane_base[I.plane_index + z] - plane_base[I.plane_index] +
-                          unit_offsets[unit_base + unit * niso + lane];
+                {
+                    const uint32_t h = lane >> 4, k = lane & 15u;
+                    if (h < (uint32_t)R && k < (uint32_t)niso && y + h < cy) {
+                        const StreamIso& I = isos[iso_begin + k];
+                        const uint64_t unit = ((uint64_t)z * cy + y + h) * wpr + seg;
+                        run = plane_base[I.plane_index + z] - plane_base[I.plane_index] +
+                              unit_offsets[unit_base + unit * niso + k];
+                    }
                 }
                 const uint32_t my_first = inc - m;
                 uint32_t* pbuf = WE->pairs;
                 for (uint32_t fill0 = 0; fill0 < npairs; fill0 += kPairCap) {
                     // this lane's pairs (cell order, then isolevel) that fall into
-                    // [fill0, fill0 + kPairCap): cell | isolevel << 8 | code << 16
+                    // [fill0, fill0 + kPairCap): warp cell | isolevel << 8 | code << 16
+                    // (warp cell = lane * 8 + i: row half in its high bit when R = 2)
                     if (m && my_first < fill0 + kPairCap && my_first + m > fill0) {
                         uint32_t slot = my_first;
 #pragma unroll
@@ -501,7 +560,8 @@ __global__ void __launch_bounds__(kStreamThreads, EMIT ? 2 : 3)
                                     const uint32_t k = __ffs(am) - 1;
                                     am &= am - 1;
                                     if (slot >= fill0 && slot < fill0 + kPairCap)
-                                        pbuf[slot - fill0] = (xl + i) | (k << 8) | (case_code(w0, w1, w2, w3, k) << 16);
+                                        pbuf[slot - fill0] = (lane * kLaneCells + i) | (k << 8) |
+                                                             (case_code(w0, w1, w2, w3, k) << 16);
                                     ++slot;
                                 } while (am);
                             }
@@ -515,12 +575,13 @@ __global__ void __launch_bounds__(kStreamThreads, EMIT ? 2 : 3)
                         const bool has = p < nfill;
                         const uint32_t pe = has ? pbuf[p] : 0u;
                         const uint32_t k = (pe >> 8) & 0xffu, code = pe >> 16;
+                        const uint32_t rk = ((pe & 0xffu) >> SEG_SHIFT) * 16 + k;   // (row, isolevel) slot
                         const uint32_t nt = has ? TB.ntri[code] : 0u;
                         const uint32_t ne = has ? (uint32_t)__popc(TB.edge_mask[code]) : 0u;
                         // output position of the pair's first triangle: pairs are in
-                        // cell order, so it is the isolevel's running count plus the
-                        // triangles of the earlier lanes of the same isolevel
-                        const int key = has ? (int)k : 64 + (int)lane;
+                        // cell order, so it is the (row, isolevel)'s running count plus
+                        // the triangles of the earlier lanes of the same (row, isolevel)
+                        const int key = has ? (int)rk : 64 + (int)lane;
                         const uint32_t grp = __match_any_sync(FULL, key);
                         uint32_t pre = 0, gtot = 0, tpre = 0, ntr = 0;
 #pragma unroll
@@ -538,16 +599,14 @@ __global__ void __launch_bounds__(kStreamThreads, EMIT ? 2 : 3)
                             vpre += (uint32_t)__popc(bm & lt) << bit;
                             nv += (uint32_t)__popc(bm) << bit;
                         }
-                        const uint64_t obase = __shfl_sync(FULL, run, k & 31u) + pre;
-                        if (has && (31 - __clz(grp)) == (int)lane) W.add[k] = gtot;
+                        const uint64_t obase = __shfl_sync(FULL, run, rk & 31u) + pre;
+                        if (has && (31 - __clz(grp)) == (int)lane) W.add[rk] = gtot;
                         // item -> pair maps of this round
                         for (uint32_t r = 0; r < ne; ++r) WE->item_v[vpre + r] = (uint8_t)lane;
                         for (uint32_t t = 0; t < nt; ++t) WE->item_t[tpre + t] = (uint8_t)lane;
                         __syncwarp();
-                        if (lane < (unsigned)niso) {
-                            run += W.add[lane];
-                            W.add[lane] = 0;
-                        }
+                        run += W.add[lane];
+                        W.add[lane] = 0;
                         // ---- vertices: one (pair, used edge) per lane, edges in increasing order
                         for (uint32_t j0 = 0; j0 < nv; j0 += 32) {
                             const uint32_t j = j0 + lane;
@@ -556,20 +615,22 @@ __global__ void __launch_bounds__(kStreamThreads, EMIT ? 2 : 3)
                             const uint32_t qe = __shfl_sync(FULL, pe, q);
                             const uint32_t qv = __shfl_sync(FULL, vpre, q);
                             if (hv) {
-                                const uint32_t cell = qe & 0xffu, qk = (qe >> 8) & 0xffu, qc = qe >> 16;
+                                const uint32_t qh = (qe & 0xffu) >> SEG_SHIFT, cell = qe & (SEG - 1);
+                                const uint32_t qk = (qe >> 8) & 0xffu, qc = qe >> 16;
                                 const uint32_t e = (uint32_t)(TB.edge_list[qc] >> (4 * (j - qv))) & 15u;
                                 const unsigned ep = TB.edge_packed[e];
                                 const unsigned c0 = ep & 7u, c1 = ep >> 3;
-                                const T* sa = ((c0 >> 2) ? rb0 : ra0) + ((c0 >> 1) & 1u) * row_elems + cell + (c0 & 1u);
-                                const T* sb = ((c1 >> 2) ? rb0 : ra0) + ((c1 >> 1) & 1u) * row_elems + cell + (c1 & 1u);
+                                const T* sa = ((c0 >> 2) ? pb : pa) + (qh + ((c0 >> 1) & 1u)) * row_elems + cell + (c0 & 1u);
+                                const T* sb = ((c1 >> 2) ? pb : pa) + (qh + ((c1 >> 1) & 1u)) * row_elems + cell + (c1 & 1u);
                                 const unsigned d = c0 ^ c1;
                                 const int axis = d == 1u ? 0 : (d == 2u ? 1 : 2);
                                 // corner coordinates: integers below 2^24, exact as floats
                                 const float fx = __uint2float_rn((uint32_t)xoff + cell);
+                                const float fyh = __fadd_rn(fy, qh ? 1.0f : 0.0f);
                                 const float ax = __fadd_rn(fx, (c0 & 1u) ? 1.0f : 0.0f);
-                                const float ay = __fadd_rn(fy, (c0 & 2u) ? 1.0f : 0.0f);
+                                const float ay = __fadd_rn(fyh, (c0 & 2u) ? 1.0f : 0.0f);
                                 const float az = __fadd_rn(fz, (c0 & 4u) ? 1.0f : 0.0f);
-                                const float bcoord = __fadd_rn(axis == 0 ? fx : (axis == 1 ? fy : fz),
+                                const float bcoord = __fadd_rn(axis == 0 ? fx : (axis == 1 ? fyh : fz),
                                                                (c1 & d) ? 1.0f : 0.0f);
                                 const StreamIso& I = isos[iso_begin + qk];
                                 const float3 v =
@@ -603,7 +664,7 @@ __global__ void __launch_bounds__(kStreamThreads, EMIT ? 2 : 3)
                                 const float3 n = tri_normal(A, B, C);
                                 const StreamIso& I = isos[iso_begin + qk];
                                 float* const pc = I.coords;
-                                if (pc) {
+                                if (pc && qo + t < I.cap_tris) {
                                     float* oc = pc + 9 * (qo + t);
                                     float* on = I.normals + 3 * (qo + t);
                                     oc[0] = A.x; oc[1] = A.y; oc[2] = A.z;
@@ -622,6 +683,7 @@ __global__ void __launch_bounds__(kStreamThreads, EMIT ? 2 : 3)
         // plane z+1's masks are plane z's at the next step
 #pragma unroll
         for (int w = 0; w < 5; ++w) { PA0[w] = PB0[w]; PA1[w] = PB1[w]; }
+        pa_valid = true;
         // plane z is consumed: refill its buffer with plane z + 3
         __syncwarp();
         if (lane == 0 && z + 3 <= z1) {
@@ -637,6 +699,44 @@ __global__ void __launch_bounds__(kStreamThreads, EMIT ? 2 : 3)
         for (uint32_t i = s_break; i <= last && i < s_break + 3; ++i)
             mbar_wait(&W.bar[i % 3u], (i / 3u) & 1u, 1u << 16);
     }
+}
+
+// Brick min/max: one warp per brick, lanes across its node rows.
+template <typename T>
+__global__ void __launch_bounds__(256)
+    k_bricks(VolumeView v, uint32_t seg_cells, uint32_t wpr, uint32_t nby, uint64_t nbricks, float2* __restrict__ out)
+{
+    const uint64_t b = ((uint64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const unsigned lane = threadIdx.x & 31u;
+    if (b >= nbricks) return;
+    const uint32_t seg = (uint32_t)(b % wpr);
+    const uint32_t by = (uint32_t)((b / wpr) % nby);
+    const uint32_t bz = (uint32_t)(b / ((uint64_t)wpr * nby));
+    const uint32_t cx = v.nx - 1, cy = v.ny - 1, cz = v.nz - 1;
+    const uint32_t x0 = seg * seg_cells, x1 = min(x0 + seg_cells, cx);
+    const uint32_t y0 = 2 * by, y1 = min(y0 + 2, cy);
+    const uint32_t z0 = bz * kBrickPlanes, z1 = min(z0 + kBrickPlanes, cz);
+    const T* d = static_cast<const T*>(v.data);
+    float lo = __int_as_float(0x7f800000), hi = __int_as_float(0xff800000);
+    bool nan = false;
+    for (uint32_t z = z0; z <= z1; ++z)
+        for (uint32_t y = y0; y <= y1; ++y) {
+            const T* row = d + (uint64_t)z * v.slice + (uint64_t)y * v.pitch;
+            for (uint32_t x = x0 + lane; x <= x1; x += 32) {
+                const float f = (float)row[x];
+                nan |= f != f;
+                lo = fminf(lo, f);
+                hi = fmaxf(hi, f);
+            }
+        }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        lo = fminf(lo, __shfl_xor_sync(FULL, lo, o));
+        hi = fmaxf(hi, __shfl_xor_sync(FULL, hi, o));
+    }
+    nan = __any_sync(FULL, nan);
+    if (lane == 0)
+        out[b] = nan ? make_float2(__int_as_float(0xff800000), __int_as_float(0x7f800000)) : make_float2(lo, hi);
 }
 
 // One CTA per (group, z): for every isolevel of the group, the exclusive scan
@@ -736,24 +836,31 @@ __global__ void k_iso_totals(const StreamIso* isos, int n, const uint64_t* plane
 
 }  // namespace
 
-size_t stream_warp_smem_bytes(int dtype, bool emit)
+size_t stream_row_elems(int dtype, int rows)
 {
     const size_t es = dtype_size(dtype);
-    const size_t row = ((257 * es + 15) / 16) * 16;
-    return align128(sizeof(WarpState)) + (emit ? align128(sizeof(WarpEmit)) : 0) + align128(3 * 2 * row);
+    return ((((size_t)kSegCells / rows + 1) * es + 15) / 16) * 16 / es;
 }
 
-size_t stream_row_elems(int dtype)
+size_t stream_warp_smem_bytes(int dtype, bool emit, int rows)
 {
-    const size_t es = dtype_size(dtype);
-    return ((257 * es + 15) / 16) * 16 / es;
+    const size_t plane = (size_t)(rows + 1) * stream_row_elems(dtype, rows) * dtype_size(dtype);
+    return align128(sizeof(WarpState)) + (emit ? align128(sizeof(WarpEmit)) : 0) + align128(3 * plane);
 }
 
 size_t stream_warp_smem_offset() { return align128(sizeof(Tables)); }
 
-size_t stream_shared_bytes(int dtype, bool emit)
+size_t stream_shared_bytes(int dtype, bool emit, int rows)
 {
-    return stream_warp_smem_offset() + (size_t)kWarps * stream_warp_smem_bytes(dtype, emit);
+    return stream_warp_smem_offset() + (size_t)kWarps * stream_warp_smem_bytes(dtype, emit, rows);
+}
+
+uint64_t brick_count(const VolumeView& v, int rows)
+{
+    const uint64_t seg = (uint64_t)kSegCells / rows;
+    const uint64_t wpr = (v.nx - 1 + seg - 1) / seg;
+    const uint64_t nby = (v.ny - 1 + 1) / 2, nbz = (v.nz - 1 + kBrickPlanes - 1) / kBrickPlanes;
+    return wpr * nby * nbz;
 }
 
 #define KVSMC_STREAM_SWITCH(DT, ...)                    \
@@ -766,15 +873,17 @@ size_t stream_shared_bytes(int dtype, bool emit)
     default: return cudaErrorInvalidValue;              \
     }
 
-cudaError_t launch_stream(bool emit, int dtype, const StreamGroup* d_groups, int ngroups, uint64_t ntasks,
+cudaError_t launch_stream(bool emit, int dtype, int rows, const StreamGroup* d_groups, int ngroups, uint64_t ntasks,
                           const StreamIso* d_isos, uint16_t* d_unit_counts, const uint32_t* d_unit_offsets,
                           const uint64_t* d_plane_base, int* d_status, const Launch& L)
 {
     if (ntasks == 0) return cudaSuccess;
-    const size_t smem = stream_shared_bytes(dtype, emit);
+    if (rows != 1 && rows != 2) return cudaErrorInvalidValue;
+    const size_t smem = stream_shared_bytes(dtype, emit, rows);
     const uint64_t nctas = (ntasks + kWarps - 1) / kWarps;
     KVSMC_STREAM_SWITCH(dtype, {
-        auto kern = emit ? k_stream<T, true> : k_stream<T, false>;
+        auto kern = emit ? (rows == 1 ? k_stream<T, true, 1> : k_stream<T, true, 2>)
+                         : (rows == 1 ? k_stream<T, false, 1> : k_stream<T, false, 2>);
         cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
         if (e == cudaSuccess)
             e = cudaFuncSetAttribute(kern, cudaFuncAttributePreferredSharedMemoryCarveout,
@@ -783,6 +892,22 @@ cudaError_t launch_stream(bool emit, int dtype, const StreamGroup* d_groups, int
         prof_begin(L, emit ? "stream_emit" : "stream_count");
         kern<<<(unsigned)nctas, kStreamThreads, smem, L.stream>>>(d_groups, ngroups, ntasks, d_isos, d_unit_counts,
                                                                    d_unit_offsets, d_plane_base, d_status);
+        prof_end(L);
+    });
+    *L.counter += 1;
+    return cudaGetLastError();
+}
+
+cudaError_t launch_bricks(const VolumeView& v, int rows, float2* out, const Launch& L)
+{
+    const uint64_t n = brick_count(v, rows);
+    if (n == 0) return cudaSuccess;
+    const uint32_t seg = (uint32_t)(kSegCells / rows);
+    const uint32_t wpr = (v.nx - 1 + seg - 1) / seg, nby = (v.ny - 1 + 1) / 2;
+    const unsigned blocks = (unsigned)((n * 32 + 255) / 256);
+    KVSMC_STREAM_SWITCH(v.dtype, {
+        prof_begin(L, "bricks");
+        k_bricks<T><<<blocks, 256, 0, L.stream>>>(v, seg, wpr, nby, n, out);
         prof_end(L);
     });
     *L.counter += 1;

@@ -88,7 +88,7 @@ extern "C" kvsmc_status kvsmc_extract_noalloc(const void* d_values, kvsmc_dtype 
         return KVSMC_ERR_UNSUPPORTED_DTYPE;
     const size_t es = dtype_size(dtype);
     // rows are staged with bulk copies: they must start on 16-byte boundaries
-    if (nx < 2 || ny < 2 || nz < 2 || nx - 1 > (uint32_t)(kStreamMaxSegments * kStreamSegCells) ||
+    if (nx < 2 || ny < 2 || nz < 2 || nx - 1 > (uint32_t)kStreamMaxCells ||
         (reinterpret_cast<uintptr_t>(d_values) & 15u) || ((size_t)nx * es) % 16 != 0 || !std::isfinite(p->isolevel) ||
         std::fabs(p->isolevel) > 1.0e30)
         return KVSMC_ERR_INVALID_ARGUMENT;
@@ -112,20 +112,24 @@ extern "C" kvsmc_status kvsmc_extract_noalloc(const void* d_values, kvsmc_dtype 
     StreamGroup g;
     std::memset(&g, 0, sizeof g);
     g.vol = v;
-    g.wpr = (nx - 1 + kStreamSegCells - 1) / kStreamSegCells;
-    if (stream_shared_bytes(dtype, true) > (size_t)227 * 1024 ||
+    const int rows = kvsmc_host::stream_rows(nx - 1);
+    const uint32_t seg_cells = (uint32_t)(kStreamSegCells / rows);
+    g.rows = (uint32_t)rows;
+    g.wpr = (nx - 1 + seg_cells - 1) / seg_cells;
+    if (stream_shared_bytes(dtype, true, rows) > (size_t)227 * 1024 ||
         (double)(nx - 1) * (double)(ny - 1) * 5.0 >= 4294967295.0)
         return KVSMC_ERR_TOO_LARGE;
     const uint32_t cy = ny - 1, cz = nz - 1;
-    g.zchunk = kvsmc_host::stream_zchunk(v, g.wpr, num_sms);
-    const uint64_t ntasks = (uint64_t)cy * g.wpr * ((cz + g.zchunk - 1) / g.zchunk);
+    const uint32_t cyr = (cy + rows - 1) / rows;
+    g.zchunk = kvsmc_host::stream_zchunk((uint64_t)cz * cyr * g.wpr, num_sms);
+    const uint64_t ntasks = (uint64_t)cyr * g.wpr * ((cz + g.zchunk - 1) / g.zchunk);
     const uint64_t units = (uint64_t)cz * cy * g.wpr;   // one isolevel: one counter per unit
     g.task_begin = 0;
     g.unit_base = 0;
     g.plane_begin = 0;
-    g.seg_elems = (uint32_t)stream_row_elems(dtype);
+    g.seg_elems = (uint32_t)stream_row_elems(dtype, rows);
     g.seg_copy_bytes = g.seg_elems * (uint32_t)es;
-    g.warp_smem_bytes = (uint32_t)stream_warp_smem_bytes(dtype, true);
+    g.warp_smem_bytes = (uint32_t)stream_warp_smem_bytes(dtype, true, rows);
     g.warp_smem_offset = (uint32_t)stream_warp_smem_offset();
 
     // carve the static array
@@ -180,7 +184,8 @@ extern "C" kvsmc_status kvsmc_extract_noalloc(const void* d_values, kvsmc_dtype 
     if (cudaMemcpyAsync(d_group, &g, sizeof g, cudaMemcpyHostToDevice, s) != cudaSuccess ||
         cudaMemcpyAsync(d_iso, &iso, sizeof iso, cudaMemcpyHostToDevice, s) != cudaSuccess ||
         cudaMemcpyAsync(d_status, &zero, sizeof zero, cudaMemcpyHostToDevice, s) != cudaSuccess ||
-        launch_stream(false, dtype, d_group, 1, ntasks, d_iso, d_unit_counts, nullptr, nullptr, d_status, L) !=
+        cudaMemsetAsync(d_unit_counts, 0, units * sizeof(uint16_t), s) != cudaSuccess ||
+        launch_stream(false, dtype, rows, d_group, 1, ntasks, d_iso, d_unit_counts, nullptr, nullptr, d_status, L) !=
             cudaSuccess ||
         launch_unit_scan(d_group, 1, cz, d_iso, d_unit_counts, d_unit_offsets, d_plane_totals, L) != cudaSuccess ||
         launch_scan(d_plane_totals, d_plane_base, cz, d_scan, d_total, L) != cudaSuccess ||
@@ -201,8 +206,9 @@ extern "C" kvsmc_status kvsmc_extract_noalloc(const void* d_values, kvsmc_dtype 
     // emit
     iso.coords = d_coords;
     iso.normals = d_normals;
+    iso.cap_tris = total;
     if (cudaMemcpyAsync(d_iso, &iso, sizeof iso, cudaMemcpyHostToDevice, s) != cudaSuccess ||
-        launch_stream(true, dtype, d_group, 1, ntasks, d_iso, nullptr, d_unit_offsets, d_plane_base, d_status, L) !=
+        launch_stream(true, dtype, rows, d_group, 1, ntasks, d_iso, nullptr, d_unit_offsets, d_plane_base, d_status, L) !=
             cudaSuccess ||
         cudaMemcpyAsync(&status, d_status, sizeof status, cudaMemcpyDeviceToHost, s) != cudaSuccess ||
         cudaStreamSynchronize(s) != cudaSuccess)

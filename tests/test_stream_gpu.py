@@ -72,6 +72,18 @@ def _fields():
     yield "noise i16", rng.integers(-3000, 3000, (17, 19, 520)).astype(np.int16), [0.0, 100.5]
     yield "wide f32", S.to_numpy(S.fbm((6, 9, 1100), seed=5)), [0.5]
     yield "nan f32", _with_nan(S.to_numpy(S.gaussian_blobs((20, 30, 40), seed=6))), [0.4]
+    # mostly empty space (one small feature): most bricks are skipped
+    yield "sparse f32", _sparse(), [0.5, 0.1]
+    # widths that keep one 256-cell row per warp (199 and 449 cells), odd and even row counts
+    yield "one-row f32", S.to_numpy(S.gaussian_blobs((21, 33, 200), seed=7)), [0.5, 0.2]
+    yield "one-row u8", S.to_numpy(S.ellipsoid_phantom((15, 22, 450), np.uint8, seed=8)), [90.5, 160.0]
+
+
+def _sparse():
+    v = np.zeros((70, 45, 300), np.float32)
+    b = S.to_numpy(S.gaussian_blobs((12, 10, 30), seed=9))
+    v[40:52, 20:30, 200:230] = b
+    return v
 
 
 def _with_nan(v):
