@@ -413,11 +413,14 @@ def run_batch(args, rank, world, local):
     algo = in_bytes + 48 * ntri
     emit_ms = sum(v[1] for k, v in prof.items() if k == "stream_emit")
     count_ms = sum(v[1] for k, v in prof.items() if k == "stream_count")
-    roofline = {"kernel": "stream_emit", "bound": "hbm", "achieved": round(algo / (emit_ms * 1e-3) / 1e9, 1),
+    # the per-kind launches overlap, so the roofline is taken over the whole
+    # replayed step (count + scans + emit): algorithmic bytes / step time
+    roofline = {"kernel": "whole plan replay", "bound": "hbm", "achieved": round(algo / (ms_graph * 1e-3) / 1e9, 1),
                 "peak": hbm, "peak_kind": peak_kind, "unit": "GB/s",
-                "frac": round(algo / (emit_ms * 1e-3) / 1e9 / hbm, 4), "algorithmic_bytes_per_launch": int(algo),
-                "launch_ms": round(emit_ms, 4), "traffic": None,
-                "note": "one emit launch per dtype present (3), summed"}
+                "frac": round(algo / (ms_graph * 1e-3) / 1e9 / hbm, 4), "algorithmic_bytes_per_launch": int(algo),
+                "launch_ms": round(ms_graph, 4), "traffic": None,
+                "note": "per-kind count and emit launches run side by side; kernel ms below are summed per family "
+                        "(emit %.2f, count %.2f) and overlap" % (emit_ms, count_ms)}
     mc = lambda ms: round(cells * world / (ms * 1e-3) / 1e6, 1)
     e2e = None
     if hosts:

@@ -98,6 +98,30 @@ Classifier make_classifier(double iso)
     return c;
 }
 
+cudaError_t fan_out(kvsmc_context* ctx, cudaStream_t origin, size_t n,
+                    const std::function<cudaError_t(size_t, cudaStream_t)>& fn)
+{
+    if (n == 0) return cudaSuccess;
+    if (n == 1) return fn(0, origin);
+    cudaError_t e = cudaSuccess;
+    if (!ctx->aux_ready) {
+        for (int i = 0; i < kvsmc_context::kAux && e == cudaSuccess; ++i) {
+            e = cudaStreamCreateWithFlags(&ctx->aux[i], cudaStreamNonBlocking);
+            if (e == cudaSuccess) e = cudaEventCreateWithFlags(&ctx->join_ev[i], cudaEventDisableTiming);
+        }
+        if (e == cudaSuccess) e = cudaEventCreateWithFlags(&ctx->fork_ev, cudaEventDisableTiming);
+        if (e != cudaSuccess) return e;
+        ctx->aux_ready = true;
+    }
+    e = cudaEventRecord(ctx->fork_ev, origin);
+    const size_t used = n < (size_t)kvsmc_context::kAux ? n : (size_t)kvsmc_context::kAux;
+    for (size_t j = 0; j < used && e == cudaSuccess; ++j) e = cudaStreamWaitEvent(ctx->aux[j], ctx->fork_ev, 0);
+    for (size_t i = 0; i < n && e == cudaSuccess; ++i) e = fn(i, ctx->aux[i % kvsmc_context::kAux]);
+    for (size_t j = 0; j < used && e == cudaSuccess; ++j) e = cudaEventRecord(ctx->join_ev[j], ctx->aux[j]);
+    for (size_t j = 0; j < used && e == cudaSuccess; ++j) e = cudaStreamWaitEvent(origin, ctx->join_ev[j], 0);
+    return e;
+}
+
 kvsmc_status volume_bricks(kvsmc_context* ctx, kvsmc_volume* v)
 {
     v->bricks_valid = false;
@@ -451,6 +475,14 @@ void kvsmc_destroy(kvsmc_context* ctx)
     if (ctx->h_small) cudaFreeHost(ctx->h_small);
     if (ctx->h_stage) cudaFreeHost(ctx->h_stage);
     profiler_destroy(ctx->prof);
+    if (ctx->aux_ready) {
+        for (int i = 0; i < kvsmc_context::kAux; ++i) {
+            cudaStreamSynchronize(ctx->aux[i]);
+            cudaStreamDestroy(ctx->aux[i]);
+            cudaEventDestroy(ctx->join_ev[i]);
+        }
+        cudaEventDestroy(ctx->fork_ev);
+    }
     if (ctx->own_stream) cudaStreamDestroy(ctx->own_stream);
     delete ctx;
 }

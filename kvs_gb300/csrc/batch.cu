@@ -216,7 +216,7 @@ size_t StreamBatch::scratch_bytes() const
     return 16 * 256 + align_up(groups.size() * sizeof(StreamGroup), 256) + align_up(niso * sizeof(StreamIso), 256) +
            align_up(unit_elems * 2, 256) + align_up(unit_elems * 4, 256) + align_up(iso_planes * 4, 256) +
            align_up(iso_planes * 8, 256) + align_up(kvsmc::scan_scratch_bytes(iso_planes), 256) +
-           align_up(niso * 8, 256) + 4 * 256;
+           align_up(niso * 8, 256) + align_up(launches.size() * 16, 256) + 4 * 256;
 }
 
 void StreamBatch::carve(char* base)
@@ -233,6 +233,7 @@ void StreamBatch::carve(char* base)
     d_totals = cv.take<uint64_t>(niso * 8);
     d_total = cv.take<uint64_t>(256);
     d_status = cv.take<int>(256);
+    d_next = cv.take<unsigned long long>(launches.size() * 16);
 }
 
 kvsmc_status StreamBatch::plan()
@@ -263,9 +264,15 @@ kvsmc_status StreamBatch::count()
     KVSMC_CUDA(ctx, cudaMemsetAsync(d_status, 0, sizeof(int), ctx->stream));
     // units the kernels skip as empty space keep these zeros
     KVSMC_CUDA(ctx, cudaMemsetAsync(d_unit_counts, 0, unit_elems * sizeof(uint16_t), ctx->stream));
-    for (const Launch1& l : launches)
-        KVSMC_CUDA(ctx, kvsmc::launch_stream(false, l.dtype, l.rows, d_groups + l.g0, l.ng, l.ntasks, d_isos, d_unit_counts,
-                                             nullptr, nullptr, d_status, L));
+    KVSMC_CUDA(ctx, cudaMemsetAsync(d_next, 0, launches.size() * 16, ctx->stream));
+    // one count launch per (value type, rows) kind, side by side
+    KVSMC_CUDA(ctx, fan_out(ctx, ctx->stream, launches.size(), [&](size_t i, cudaStream_t st) {
+        const Launch1& l = launches[i];
+        kvsmc::Launch Li = L;
+        Li.stream = st;
+        return kvsmc::launch_stream(false, l.dtype, l.rows, d_groups + l.g0, l.ng, l.ntasks, d_isos, d_unit_counts,
+                                    nullptr, nullptr, d_status, d_next + 2 * i, Li);
+    }));
     KVSMC_CUDA(ctx, kvsmc::launch_unit_scan(d_groups, (int)groups.size(), scan_blocks, d_isos, d_unit_counts,
                                             d_unit_offsets, d_plane_totals, L));
     KVSMC_CUDA(ctx, kvsmc::launch_scan(d_plane_totals, d_plane_base, iso_planes, d_scan, d_total, L));
@@ -311,9 +318,13 @@ kvsmc_status StreamBatch::emit()
     kvsmc_status st = upload_tables();
     if (st) return st;
     const kvsmc::Launch L = launch_of(ctx);
-    for (const Launch1& l : launches)
-        KVSMC_CUDA(ctx, kvsmc::launch_stream(true, l.dtype, l.rows, d_groups + l.g0, l.ng, l.ntasks, d_isos, nullptr,
-                                             d_unit_offsets, d_plane_base, d_status, L));
+    KVSMC_CUDA(ctx, fan_out(ctx, ctx->stream, launches.size(), [&](size_t i, cudaStream_t st) {
+        const Launch1& l = launches[i];
+        kvsmc::Launch Li = L;
+        Li.stream = st;
+        return kvsmc::launch_stream(true, l.dtype, l.rows, d_groups + l.g0, l.ng, l.ntasks, d_isos, d_unit_counts,
+                                    d_unit_offsets, d_plane_base, d_status, d_next + 2 * i + 1, Li);
+    }));
     return KVSMC_OK;
 }
 

@@ -52,6 +52,7 @@ struct StreamBatch {
     uint64_t* d_totals = nullptr;
     uint64_t* d_total = nullptr;
     int* d_status = nullptr;
+    unsigned long long* d_next = nullptr;   // per launch: [2 i] count, [2 i + 1] emit task counter
 
     kvsmc_status plan();
     kvsmc_status count();

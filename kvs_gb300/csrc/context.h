@@ -1,6 +1,7 @@
 // context.h -- host-side state of libkvsmc shared by api.cu and batch.cu.
 #pragma once
 #include <cstdint>
+#include <functional>
 #include <string>
 #include <vector>
 
@@ -38,6 +39,12 @@ struct kvsmc_context {
     int path = 0;                // 0: streaming kernels where eligible, 1: gather kernels only
     kvsmc::Profiler* prof = nullptr;
     std::string last_error;
+    // auxiliary streams for launches that may run side by side (created on first use)
+    static constexpr int kAux = 6;
+    cudaStream_t aux[kAux] = {};
+    cudaEvent_t fork_ev = nullptr;
+    cudaEvent_t join_ev[kAux] = {};
+    bool aux_ready = false;
 };
 
 namespace kvsmc {
@@ -91,6 +98,11 @@ struct Item {
 // (Re)build a resident volume's brick min/max table on the context's stream
 // (no-op for value types or widths the streaming kernels do not take).
 kvsmc_status volume_bricks(kvsmc_context* ctx, kvsmc_volume* v);
+
+// Run fn(i, stream) for i < n side by side on the context's auxiliary streams,
+// forked from and joined back into `origin` (also inside a stream capture).
+cudaError_t fan_out(kvsmc_context* ctx, cudaStream_t origin, size_t n,
+                    const std::function<cudaError_t(size_t, cudaStream_t)>& fn);
 
 // Decide min/max (MapperBase::setRange, the volume's cache or a preset) and
 // the Math::Equal early exit; fills it.vmin/vmax/extracted and clears sizes.

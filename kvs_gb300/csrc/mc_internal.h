@@ -92,9 +92,13 @@ size_t stream_shared_bytes(int dtype, bool emit, int rows);
 size_t stream_warp_smem_bytes(int dtype, bool emit, int rows);
 size_t stream_warp_smem_offset();
 size_t stream_row_elems(int dtype, int rows);
+// d_next_task: a zeroed u64 per launch (the persistent warps' task counter).
+// d_unit_counts: written by the count launch; read by the emit launch to skip
+// steps without triangles.
 cudaError_t launch_stream(bool emit, int dtype, int rows, const StreamGroup* d_groups, int ngroups, uint64_t ntasks,
                           const StreamIso* d_isos, uint16_t* d_unit_counts, const uint32_t* d_unit_offsets,
-                          const uint64_t* d_plane_base, int* d_status, const Launch& L);
+                          const uint64_t* d_plane_base, int* d_status, unsigned long long* d_next_task,
+                          const Launch& L);
 cudaError_t launch_unit_scan(const StreamGroup* d_groups, int ngroups, uint32_t nplanes, const StreamIso* d_isos,
                              const uint16_t* d_unit_counts, uint32_t* d_unit_offsets, uint32_t* d_plane_totals,
                              const Launch& L);

@@ -310,11 +310,18 @@ __device__ __forceinline__ int find_group(const StreamGroup* groups, int ngroups
 // R = cell rows per warp task (1 or 2).  With R = 2, lanes 0-15 take row y
 // and lanes 16-31 row y+1, each over a 128-cell segment, so narrow volumes
 // keep every lane busy and a node row is staged for 1.5 cell rows, not 2.
+//
+// Persistent: the grid holds as many CTAs as fit on the GPU and every warp
+// takes tasks from `next_task` (one atomicAdd per task) until they run out,
+// so warps that skip empty tasks go on at once instead of idling in a CTA
+// whose other warps still run.  Tasks come out in increasing order; the
+// group's isolevel tables are rebuilt when a warp crosses a group boundary.
 template <typename T, bool EMIT, int R>
 __global__ void __launch_bounds__(kStreamThreads, EMIT ? 2 : 3)
     k_stream(const StreamGroup* __restrict__ groups, int ngroups, uint64_t ntasks, const StreamIso* __restrict__ isos,
              uint16_t* __restrict__ unit_counts, const uint32_t* __restrict__ unit_offsets,
-             const uint64_t* __restrict__ plane_base, int* __restrict__ status)
+             const uint64_t* __restrict__ plane_base, int* __restrict__ status,
+             unsigned long long* __restrict__ next_task)
 {
     constexpr int LPR = 32 / R;                 // lanes per cell row
     constexpr int SEG = kSegCells / R;          // cells per row segment
@@ -339,9 +346,36 @@ __global__ void __launch_bounds__(kStreamThreads, EMIT ? 2 : 3)
     }
     __syncthreads();   // the only CTA-wide barrier: tables are read-only from here on
 
-    const uint64_t task = (uint64_t)blockIdx.x * kWarps + warp;
-    if (task >= ntasks) return;
-    const StreamGroup& G = groups[find_group(groups, ngroups, task)];
+    // per-warp shared memory: state, then (emit) buffers, then the row ring
+    // (the same layout as stream_warp_smem_bytes on the host; one value type
+    // and one rows-per-task per launch, so one layout for all groups)
+    const uint32_t row_elems = groups[0].seg_elems;      // staged elements per row
+    const uint32_t plane_elems = (R + 1) * row_elems;
+    const size_t wstride = align128(sizeof(WarpState)) + (EMIT ? align128(sizeof(WarpEmit)) : 0) +
+                           align128((size_t)3 * plane_elems * sizeof(T));
+    unsigned char* wbase = smem_raw + align128(sizeof(Tables)) + (size_t)warp * wstride;
+    WarpState& W = *reinterpret_cast<WarpState*>(wbase);
+    WarpEmit* WE = reinterpret_cast<WarpEmit*>(wbase + align128(sizeof(WarpState)));
+    T* ring = reinterpret_cast<T*>(wbase + align128(sizeof(WarpState)) + (EMIT ? align128(sizeof(WarpEmit)) : 0));
+    if (lane == 0) {
+        for (int b = 0; b < 3; ++b) mbar_init(&W.bar[b], 1);
+        fence_barrier_init();
+    }
+    W.cnt[lane] = 0;
+    W.add[lane] = 0;
+    __syncwarp();
+
+    uint32_t ph = 0;     // per ring buffer: parity of its next completion
+    int gcur = -1;       // group whose tables are in W
+    for (;;) {
+    unsigned long long tk = 0;
+    if (lane == 0) tk = atomicAdd(next_task, 1ull);
+    const uint64_t task = __shfl_sync(FULL, tk, 0);
+    if (task >= ntasks) break;
+    int gi = gcur;
+    if (gi < 0 || task < groups[gi].task_begin || (gi + 1 < ngroups && task >= groups[gi + 1].task_begin))
+        gi = find_group(groups, ngroups, task);
+    const StreamGroup& G = groups[gi];
     const uint64_t local = task - G.task_begin;
     const uint32_t cx = G.vol.nx - 1, cy = G.vol.ny - 1, cz = G.vol.nz - 1;
     const uint32_t wpr = G.wpr;
@@ -356,17 +390,6 @@ __global__ void __launch_bounds__(kStreamThreads, EMIT ? 2 : 3)
     const int iso_begin = G.iso_begin;
     const uint64_t unit_base = G.unit_base;
     const uint32_t nrows = (y + R + 1 <= G.vol.ny) ? R + 1 : G.vol.ny - y;   // node rows staged per plane
-
-    // per-warp shared memory: state, then (emit) buffers, then the row ring
-    // (the same layout as stream_warp_smem_bytes on the host)
-    const uint32_t row_elems = G.seg_elems;              // staged elements per row
-    const uint32_t plane_elems = (R + 1) * row_elems;
-    const size_t wstride = align128(sizeof(WarpState)) + (EMIT ? align128(sizeof(WarpEmit)) : 0) +
-                           align128((size_t)3 * plane_elems * sizeof(T));
-    unsigned char* wbase = smem_raw + align128(sizeof(Tables)) + (size_t)warp * wstride;
-    WarpState& W = *reinterpret_cast<WarpState*>(wbase);
-    WarpEmit* WE = reinterpret_cast<WarpEmit*>(wbase + align128(sizeof(WarpState)));
-    T* ring = reinterpret_cast<T*>(wbase + align128(sizeof(WarpState)) + (EMIT ? align128(sizeof(WarpEmit)) : 0));
     const uint64_t pitch = G.vol.pitch;
     const uint64_t slice = G.vol.slice;
     const uint64_t xoff = (uint64_t)seg * SEG;
@@ -376,28 +399,26 @@ __global__ void __launch_bounds__(kStreamThreads, EMIT ? 2 : 3)
     const uint32_t row_bytes = (uint32_t)(avail < G.seg_copy_bytes ? avail : G.seg_copy_bytes);
     const T* vol = static_cast<const T*>(G.vol.data);
 
-    if (lane < (unsigned)niso) {
-        const float t = isos[iso_begin + lane].f.f_thr;
-        W.thr[lane] = t;
-        W.thr_bucket[lane] = (int32_t)bucket_index(t, bs, bo);
-    }
-    W.cnt[lane] = 0;
-    W.add[lane] = 0;
-    __syncwarp();
-    for (unsigned b = lane; b < (unsigned)kLut; b += 32) {
-        uint32_t below = 0, in = 0;
-        for (int k = 0; k < niso; ++k) {
-            below += (uint32_t)W.thr_bucket[k] < b ? 1u : 0u;
-            in += (uint32_t)W.thr_bucket[k] == b ? 1u : 0u;
+    if (gi != gcur) {
+        // the group's thresholds and bucket table
+        if (lane < (unsigned)niso) {
+            const float t = isos[iso_begin + lane].f.f_thr;
+            W.thr[lane] = t;
+            W.thr_bucket[lane] = (int32_t)bucket_index(t, bs, bo);
         }
-        const float first = in ? W.thr[below] : __int_as_float(0x7f800000);
-        W.lut[b] = make_uint2(((1u << below) - 1u) | (in > 1 ? kMultiThr : 0u), (uint32_t)__float_as_int(first));
+        __syncwarp();
+        for (unsigned b = lane; b < (unsigned)kLut; b += 32) {
+            uint32_t below = 0, in = 0;
+            for (int k = 0; k < niso; ++k) {
+                below += (uint32_t)W.thr_bucket[k] < b ? 1u : 0u;
+                in += (uint32_t)W.thr_bucket[k] == b ? 1u : 0u;
+            }
+            const float first = in ? W.thr[below] : __int_as_float(0x7f800000);
+            W.lut[b] = make_uint2(((1u << below) - 1u) | (in > 1 ? kMultiThr : 0u), (uint32_t)__float_as_int(first));
+        }
+        __syncwarp();
+        gcur = gi;
     }
-    if (lane == 0) {
-        for (int b = 0; b < 3; ++b) mbar_init(&W.bar[b], 1);
-        fence_barrier_init();
-    }
-    __syncwarp();
 
     // empty space: a brick whose node min and max have the same mask (no
     // threshold between them) holds no active cell for any isolevel
@@ -410,21 +431,30 @@ __global__ void __launch_bounds__(kStreamThreads, EMIT ? 2 : 3)
     if (bricks) {
         bool all_empty = true;
         for (uint32_t z = z0; z < z1 && all_empty; z = (z / kBrickPlanes + 1) * kBrickPlanes) all_empty = brick_empty(z);
-        if (all_empty) return;   // nothing to count or emit (counts are zeroed before the count pass)
+        if (all_empty) continue;   // nothing to count or emit (counts are zeroed before the count pass)
     }
 
-    auto issue = [&](uint32_t plane) {
-        const uint32_t i = plane - z0;
+    // plane i of this task goes to ring buffer i % 3
+    auto issue = [&](uint32_t i) {
         const int b = (int)(i % 3u);
         T* dst = ring + (size_t)b * plane_elems;
-        const T* src = vol + (uint64_t)plane * slice + (uint64_t)y * pitch + xoff;
+        const T* src = vol + (uint64_t)(z0 + i) * slice + (uint64_t)y * pitch + xoff;
         mbar_arrive_expect_tx(&W.bar[b], nrows * row_bytes);
         for (uint32_t r = 0; r < nrows; ++r) bulk_copy_g2s(dst + r * row_elems, src + r * pitch, row_bytes, &W.bar[b]);
     };
+    // wait (bounded) for plane i; on success the buffer's parity advances
+    auto acquire = [&](uint32_t i) -> bool {
+        const uint32_t b = i % 3u;
+        const bool ok = mbar_wait(&W.bar[b], (ph >> b) & 1u, 1u << 22);
+        if (ok) ph ^= 1u << b;
+        return ok;
+    };
+    const uint32_t nplanes = z1 - z0 + 1;
+    __syncwarp();   // the previous task's reads of the ring are done
     if (lane == 0) {
-        for (uint32_t p = z0; p <= z1 && p < z0 + 3; ++p) issue(p);
+        fence_proxy_async();
+        for (uint32_t i = 0; i < nplanes && i < 3; ++i) issue(i);
     }
-
     const uint32_t half = lane / LPR;                     // this lane's row: y + half
     const uint32_t xl = (lane % LPR) * kLaneCells;        // first cell of this lane inside the segment
     const bool row_ok = y + half < cy;
@@ -433,19 +463,24 @@ __global__ void __launch_bounds__(kStreamThreads, EMIT ? 2 : 3)
     const unsigned lt = (1u << lane) - 1u;
     const float fy = __uint2float_rn(y);
     bool dead = false;
-    uint32_t s_break = 0;
+    uint32_t acq = 0;          // planes of this task acquired so far
+    uint32_t issued = 0;       // planes of this task issued when a wait timed out
     uint32_t PA0[5], PA1[5];   // masks of plane z, this lane's rows (carried from the previous step)
     bool pa_valid = false;
-    bool skip = false;         // the current brick is empty
+    bool brick_skip = false;   // the current brick is empty
 
     for (uint32_t z = z0; z < z1; ++z) {
         const uint32_t s = z - z0;
-        bool ok = mbar_wait(&W.bar[s % 3u], (s / 3u) & 1u, 1u << 22);
-        ok = ok && mbar_wait(&W.bar[(s + 1) % 3u], ((s + 1) / 3u) & 1u, 1u << 22);
+        // step s needs planes s and s + 1
+        bool ok = true;
+        while (ok && acq <= s + 1) {
+            ok = acquire(acq);
+            if (ok) ++acq;
+        }
         if (__any_sync(FULL, !ok)) {
             if (lane == 0) atomicExch(status, 1);
             dead = true;
-            s_break = s;
+            issued = (s + 3 < nplanes) ? s + 3 : nplanes;   // 3 at the start + one per finished step
             break;
         }
         const T* pa = ring + (size_t)(s % 3u) * plane_elems;         // plane z
@@ -455,13 +490,22 @@ __global__ void __launch_bounds__(kStreamThreads, EMIT ? 2 : 3)
         const T* rb0 = pb + half * row_elems;
         const T* rb1 = rb0 + row_elems;
         const float fz = __uint2float_rn(z);
-        if (bricks && (s == 0 || z % kBrickPlanes == 0)) skip = brick_empty(z);
+        if (bricks && (s == 0 || z % kBrickPlanes == 0)) brick_skip = brick_empty(z);
+        bool skip = brick_skip;
+        if (EMIT && !skip) {
+            // the count pass found no triangle in this step's units: nothing to emit
+            const uint32_t h = lane >> 4, k = lane & 15u;
+            bool any = false;
+            if (h < (uint32_t)R && k < (uint32_t)niso && y + h < cy)
+                any = unit_counts[unit_base + (((uint64_t)z * cy + y + h) * wpr + seg) * niso + k] != 0;
+            skip = !__any_sync(FULL, any);
+        }
         if (skip) {
             pa_valid = false;
             __syncwarp();
-            if (lane == 0 && z + 3 <= z1) {
+            if (lane == 0 && s + 3 < nplanes) {
                 fence_proxy_async();
-                issue(z + 3);
+                issue(s + 3);
             }
             continue;
         }
@@ -686,19 +730,23 @@ __global__ void __launch_bounds__(kStreamThreads, EMIT ? 2 : 3)
         pa_valid = true;
         // plane z is consumed: refill its buffer with plane z + 3
         __syncwarp();
-        if (lane == 0 && z + 3 <= z1) {
+        if (lane == 0 && s + 3 < nplanes) {
             fence_proxy_async();
-            issue(z + 3);
+            issue(s + 3);
         }
     }
-    // After a normal walk every issued plane has been waited for.  After a
-    // timeout, wait (bounded) for the copies still in flight before leaving,
-    // so no bulk copy lands in shared memory this warp no longer owns.
-    if (dead && lane == 0) {
-        const uint32_t last = z1 - z0;
-        for (uint32_t i = s_break; i <= last && i < s_break + 3; ++i)
-            mbar_wait(&W.bar[i % 3u], (i / 3u) & 1u, 1u << 16);
+    if (dead) {
+        // After a timeout, wait (bounded) for the copies still in flight before
+        // leaving, so no bulk copy lands in shared memory this warp no longer
+        // uses; then stop taking tasks.  (A normal walk acquires every plane it
+        // issued.)
+        for (uint32_t i = acq; i < issued; ++i) {
+            const uint32_t b = i % 3u;
+            if (mbar_wait(&W.bar[b], (ph >> b) & 1u, 1u << 16)) ph ^= 1u << b;
+        }
+        break;
     }
+    }   // task loop
 }
 
 // Brick min/max: one warp per brick, lanes across its node rows.
@@ -875,12 +923,13 @@ uint64_t brick_count(const VolumeView& v, int rows)
 
 cudaError_t launch_stream(bool emit, int dtype, int rows, const StreamGroup* d_groups, int ngroups, uint64_t ntasks,
                           const StreamIso* d_isos, uint16_t* d_unit_counts, const uint32_t* d_unit_offsets,
-                          const uint64_t* d_plane_base, int* d_status, const Launch& L)
+                          const uint64_t* d_plane_base, int* d_status, unsigned long long* d_next_task,
+                          const Launch& L)
 {
     if (ntasks == 0) return cudaSuccess;
     if (rows != 1 && rows != 2) return cudaErrorInvalidValue;
     const size_t smem = stream_shared_bytes(dtype, emit, rows);
-    const uint64_t nctas = (ntasks + kWarps - 1) / kWarps;
+    const uint64_t need = (ntasks + kWarps - 1) / kWarps;
     KVSMC_STREAM_SWITCH(dtype, {
         auto kern = emit ? (rows == 1 ? k_stream<T, true, 1> : k_stream<T, true, 2>)
                          : (rows == 1 ? k_stream<T, false, 1> : k_stream<T, false, 2>);
@@ -888,10 +937,16 @@ cudaError_t launch_stream(bool emit, int dtype, int rows, const StreamGroup* d_g
         if (e == cudaSuccess)
             e = cudaFuncSetAttribute(kern, cudaFuncAttributePreferredSharedMemoryCarveout,
                                      (int)cudaSharedmemCarveoutMaxShared);
+        int per_sm = 0;
+        if (e == cudaSuccess) e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, kStreamThreads, smem);
         if (e != cudaSuccess) return e;
+        // persistent: as many CTAs as are resident at once (never more than the tasks need)
+        const uint64_t resident = (uint64_t)(per_sm > 0 ? per_sm : 1) * (uint64_t)L.num_sms;
+        const uint64_t nctas = need < resident ? need : resident;
         prof_begin(L, emit ? "stream_emit" : "stream_count");
         kern<<<(unsigned)nctas, kStreamThreads, smem, L.stream>>>(d_groups, ngroups, ntasks, d_isos, d_unit_counts,
-                                                                   d_unit_offsets, d_plane_base, d_status);
+                                                                   d_unit_offsets, d_plane_base, d_status,
+                                                                   d_next_task);
         prof_end(L);
     });
     *L.counter += 1;

@@ -145,6 +145,7 @@ extern "C" kvsmc_status kvsmc_extract_noalloc(const void* d_values, kvsmc_dtype 
     uint64_t* d_totals = reinterpret_cast<uint64_t*>(take(8));
     uint64_t* d_total = reinterpret_cast<uint64_t*>(take(8));
     int* d_status = reinterpret_cast<int*>(take(sizeof(int)));
+    unsigned long long* d_next = reinterpret_cast<unsigned long long*>(take(2 * sizeof(unsigned long long)));
     double* d_mm = reinterpret_cast<double*>(take(2 * sizeof(double)));
     void* d_mm_part = take(minmax_scratch_bytes(num_sms));
     if (off > kNoAllocScratchBytes) return KVSMC_ERR_TOO_LARGE;
@@ -185,7 +186,8 @@ extern "C" kvsmc_status kvsmc_extract_noalloc(const void* d_values, kvsmc_dtype 
         cudaMemcpyAsync(d_iso, &iso, sizeof iso, cudaMemcpyHostToDevice, s) != cudaSuccess ||
         cudaMemcpyAsync(d_status, &zero, sizeof zero, cudaMemcpyHostToDevice, s) != cudaSuccess ||
         cudaMemsetAsync(d_unit_counts, 0, units * sizeof(uint16_t), s) != cudaSuccess ||
-        launch_stream(false, dtype, rows, d_group, 1, ntasks, d_iso, d_unit_counts, nullptr, nullptr, d_status, L) !=
+        cudaMemsetAsync(d_next, 0, 2 * sizeof(unsigned long long), s) != cudaSuccess ||
+        launch_stream(false, dtype, rows, d_group, 1, ntasks, d_iso, d_unit_counts, nullptr, nullptr, d_status, d_next, L) !=
             cudaSuccess ||
         launch_unit_scan(d_group, 1, cz, d_iso, d_unit_counts, d_unit_offsets, d_plane_totals, L) != cudaSuccess ||
         launch_scan(d_plane_totals, d_plane_base, cz, d_scan, d_total, L) != cudaSuccess ||
@@ -208,7 +210,7 @@ extern "C" kvsmc_status kvsmc_extract_noalloc(const void* d_values, kvsmc_dtype 
     iso.normals = d_normals;
     iso.cap_tris = total;
     if (cudaMemcpyAsync(d_iso, &iso, sizeof iso, cudaMemcpyHostToDevice, s) != cudaSuccess ||
-        launch_stream(true, dtype, rows, d_group, 1, ntasks, d_iso, nullptr, d_unit_offsets, d_plane_base, d_status, L) !=
+        launch_stream(true, dtype, rows, d_group, 1, ntasks, d_iso, d_unit_counts, d_unit_offsets, d_plane_base, d_status, d_next + 1, L) !=
             cudaSuccess ||
         cudaMemcpyAsync(&status, d_status, sizeof status, cudaMemcpyDeviceToHost, s) != cudaSuccess ||
         cudaStreamSynchronize(s) != cudaSuccess)

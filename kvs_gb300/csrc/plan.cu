@@ -49,22 +49,29 @@ void plan_free(kvsmc_plan* p)
 cudaError_t record(kvsmc_host::StreamBatch& b, cudaStream_t s, int num_sms, uint64_t* counter, uint64_t* h_out)
 {
     const kvsmc::Launch L{s, num_sms, counter, nullptr};
+    // the per-kind launches of a pass run side by side (parallel graph branches)
+    auto per_kind = [&](bool emit) {
+        return kvsmc_host::fan_out(b.ctx, s, b.launches.size(), [&](size_t i, cudaStream_t st) {
+            const auto& l = b.launches[i];
+            kvsmc::Launch Li = L;
+            Li.stream = st;
+            return kvsmc::launch_stream(emit, l.dtype, l.rows, b.d_groups + l.g0, l.ng, l.ntasks, b.d_isos,
+                                        b.d_unit_counts, emit ? b.d_unit_offsets : nullptr,
+                                        emit ? b.d_plane_base : nullptr, b.d_status, b.d_next + 2 * i + (emit ? 1 : 0),
+                                        Li);
+        });
+    };
     cudaError_t e = cudaMemsetAsync(b.d_status, 0, sizeof(int), s);
     if (e == cudaSuccess) e = cudaMemsetAsync(b.d_unit_counts, 0, b.unit_elems * sizeof(uint16_t), s);
-    for (const auto& l : b.launches)
-        if (e == cudaSuccess)
-            e = kvsmc::launch_stream(false, l.dtype, l.rows, b.d_groups + l.g0, l.ng, l.ntasks, b.d_isos, b.d_unit_counts,
-                                     nullptr, nullptr, b.d_status, L);
+    if (e == cudaSuccess) e = cudaMemsetAsync(b.d_next, 0, b.launches.size() * 16, s);
+    if (e == cudaSuccess) e = per_kind(false);
     if (e == cudaSuccess)
         e = kvsmc::launch_unit_scan(b.d_groups, (int)b.groups.size(), b.scan_blocks, b.d_isos, b.d_unit_counts,
                                     b.d_unit_offsets, b.d_plane_totals, L);
     if (e == cudaSuccess) e = kvsmc::launch_scan(b.d_plane_totals, b.d_plane_base, b.iso_planes, b.d_scan, b.d_total, L);
     if (e == cudaSuccess)
         e = kvsmc::launch_iso_totals(b.d_isos, (int)b.isos.size(), b.d_plane_base, b.d_total, b.d_totals, L);
-    for (const auto& l : b.launches)
-        if (e == cudaSuccess)
-            e = kvsmc::launch_stream(true, l.dtype, l.rows, b.d_groups + l.g0, l.ng, l.ntasks, b.d_isos, nullptr,
-                                     b.d_unit_offsets, b.d_plane_base, b.d_status, L);
+    if (e == cudaSuccess) e = per_kind(true);
     if (e == cudaSuccess) e = cudaMemcpyAsync(h_out, b.d_status, sizeof(int), cudaMemcpyDeviceToHost, s);
     if (e == cudaSuccess)
         e = cudaMemcpyAsync(h_out + 1, b.d_totals, b.isos.size() * sizeof(uint64_t), cudaMemcpyDeviceToHost, s);
