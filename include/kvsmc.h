@@ -219,6 +219,68 @@ kvsmc_status kvsmc_plan_wait(kvsmc_plan* plan, kvsmc_request* reqs, int32_t n);
 uint64_t kvsmc_plan_kernels(const kvsmc_plan* plan);
 void kvsmc_plan_destroy(kvsmc_plan* plan);
 
+/* ---------------------------------------------------------------- serving */
+
+/* A request loop over resident volumes with continuous batching.  No
+ * counterpart in the reference (one kvs::MarchingCubes call at a time on the
+ * caller's thread).  Clients submit (volume, params) requests from any
+ * thread; `workers` worker threads, each with its own context and stream,
+ * take every pending request (up to `max_batch`) as soon as they are free,
+ * count them in one fused pass, admit them against the output budget (48
+ * bytes per triangle of device memory held until the client releases the
+ * result), allocate their outputs stream-ordered, and emit them in one fused
+ * pass; batches of different workers overlap on the GPU, so requests that
+ * arrive while others run start without waiting for them.  A request whose
+ * output alone exceeds the budget completes with KVSMC_ERR_BUDGET.  Served
+ * requests: duplicated vertices + polygon normals on int8/uint8/int16/uint16/
+ * float32 volumes of width <= 4097 (the streaming kernels); others are refused
+ * at submit.  Results are identical to kvsmc_extract_device's. */
+typedef struct kvsmc_server kvsmc_server;
+
+typedef struct kvsmc_server_config {
+    uint64_t output_budget_bytes;  /* device memory for results not yet released (0: 40 GiB) */
+    int32_t max_batch;             /* requests per batch (0: 256) */
+    int32_t workers;               /* batches in flight at once (0: 3) */
+} kvsmc_server_config;
+
+typedef struct kvsmc_completion {
+    uint64_t ticket;
+    kvsmc_status status;
+    int32_t batch_size;            /* requests in the batch it ran in */
+    kvsmc_sizes sizes;
+    const float* d_coords;         /* device; valid until kvsmc_server_release(ticket) */
+    const float* d_normals;
+    double submit_s, start_s, done_s;  /* host clock, seconds since the server was created:
+                                        * submitted, its batch started counting, results ready */
+} kvsmc_completion;
+
+/* The server runs on ctx's device; volumes must stay alive and unchanged
+ * while requests on them are pending.  The first request on a volume waits
+ * for ctx's stream (so an upload on ctx is complete); a volume uploaded on
+ * another context must be complete before it is submitted. */
+kvsmc_status kvsmc_server_create(kvsmc_context* ctx, const kvsmc_server_config* cfg, kvsmc_server** out);
+/* Queue one request; never blocks on the GPU beyond the first-use wait above
+ * (the volume's min/max is filled first if not cached).  *ticket identifies
+ * its completion. */
+kvsmc_status kvsmc_server_submit(kvsmc_server* s, kvsmc_volume* vol, const kvsmc_params* p, uint64_t* ticket);
+/* Up to `max` completions, waiting up to `timeout_ms` (0: do not wait) for
+ * the first one; returns how many were written. */
+int32_t kvsmc_server_poll(kvsmc_server* s, kvsmc_completion* out, int32_t max, int32_t timeout_ms);
+/* Free a completed result's device outputs and return its bytes to the budget. */
+kvsmc_status kvsmc_server_release(kvsmc_server* s, uint64_t ticket);
+/* Counters: [0] requests submitted, [1] completed, [2] batches, [3] kernel
+ * launches, [4] output bytes held now, [5] peak bytes held, [6] times a batch
+ * waited for budget. */
+kvsmc_status kvsmc_server_stats(kvsmc_server* s, uint64_t* out7);
+/* Drain (every submitted request completes), stop the workers, free every
+ * result still held. */
+void kvsmc_server_destroy(kvsmc_server* s);
+
+/* Copy `bytes` of device memory (a result's d_coords / d_normals) to host
+ * memory on the context's stream and wait; for callers without a CUDA
+ * runtime of their own. */
+kvsmc_status kvsmc_copy_to_host(kvsmc_context* ctx, void* host, const void* device, uint64_t bytes);
+
 /* ------------------------------------------------- no-allocation variant */
 
 /* For callers that may not allocate device memory: a plugin whose host

@@ -42,6 +42,8 @@ EXPORTS = [
     "kvsmc_selftest_interpolation", "kvsmc_profile_enable", "kvsmc_profile_read",
     "kvsmc_extract_batch_host", "kvsmc_extract_noalloc",
     "kvsmc_plan_create", "kvsmc_plan_launch", "kvsmc_plan_wait", "kvsmc_plan_kernels", "kvsmc_plan_destroy",
+    "kvsmc_server_create", "kvsmc_server_submit", "kvsmc_server_poll", "kvsmc_server_release",
+    "kvsmc_server_stats", "kvsmc_server_destroy", "kvsmc_copy_to_host",
 ]
 
 PATH_AUTO = 0      # streaming kernels where eligible
@@ -67,6 +69,16 @@ class Sizes(C.Structure):
                 ("nnormals", C.c_uint64), ("nconnections", C.c_uint64),
                 ("min_value", C.c_double), ("max_value", C.c_double),
                 ("extracted", C.c_int32), ("reserved", C.c_int32)]
+
+
+class ServerConfig(C.Structure):
+    _fields_ = [("output_budget_bytes", C.c_uint64), ("max_batch", C.c_int32), ("workers", C.c_int32)]
+
+
+class Completion(C.Structure):
+    _fields_ = [("ticket", C.c_uint64), ("status", C.c_int), ("batch_size", C.c_int32), ("sizes", Sizes),
+                ("d_coords", C.c_void_p), ("d_normals", C.c_void_p),
+                ("submit_s", C.c_double), ("start_s", C.c_double), ("done_s", C.c_double)]
 
 
 class Request(C.Structure):
@@ -126,6 +138,13 @@ def load(path=LIB_PATH):
                                                HOST_ALLOC, vp, C.POINTER(Sizes)]),
         "kvsmc_extract_noalloc": (C.c_int, [vp, C.c_int, u32, u32, u32, C.POINTER(Params), vp, u64, vp, u64,
                                             vp, C.POINTER(Sizes)]),
+        "kvsmc_server_create": (C.c_int, [vp, C.POINTER(ServerConfig), C.POINTER(vp)]),
+        "kvsmc_server_submit": (C.c_int, [vp, vp, C.POINTER(Params), C.POINTER(u64)]),
+        "kvsmc_server_poll": (i32, [vp, C.POINTER(Completion), i32, i32]),
+        "kvsmc_server_release": (C.c_int, [vp, u64]),
+        "kvsmc_server_stats": (C.c_int, [vp, C.POINTER(u64)]),
+        "kvsmc_server_destroy": (None, [vp]),
+        "kvsmc_copy_to_host": (C.c_int, [vp, vp, vp, u64]),
         "kvsmc_plan_create": (C.c_int, [vp, C.POINTER(Request), i32, C.POINTER(vp)]),
         "kvsmc_plan_launch": (C.c_int, [vp, vp]),
         "kvsmc_plan_wait": (C.c_int, [vp, C.POINTER(Request), i32]),
@@ -247,6 +266,59 @@ class DeviceVolume:
         try:
             if self.ctx.handle:
                 self.free()
+        except Exception:
+            pass
+
+
+class Server:
+    """The request loop (kvsmc_server_*): submit() from any thread, poll()
+    completions, fetch() a result to host memory, release() it to return its
+    bytes to the budget."""
+
+    def __init__(self, ctx, budget_bytes=0, max_batch=0, workers=0):
+        self.ctx = ctx
+        cfg = ServerConfig(budget_bytes, max_batch, workers)
+        h = C.c_void_p()
+        ctx.check(ctx.lib.kvsmc_server_create(ctx.handle, C.byref(cfg), C.byref(h)), "server_create")
+        self.handle = h
+        self._buf = (Completion * 256)()
+
+    def submit(self, volume, params):
+        t = C.c_uint64()
+        self.ctx.check(self.ctx.lib.kvsmc_server_submit(self.handle, volume.handle, C.byref(params), C.byref(t)),
+                       "server_submit")
+        return t.value
+
+    def poll(self, timeout_ms=0):
+        k = self.ctx.lib.kvsmc_server_poll(self.handle, self._buf, len(self._buf), int(timeout_ms))
+        return [Completion.from_buffer_copy(self._buf[i]) for i in range(k)]
+
+    def fetch(self, c):
+        """(coords, normals) of a completion as host float32 arrays."""
+        coords = np.empty(c.sizes.ncoords, np.float32)
+        normals = np.empty(c.sizes.nnormals, np.float32)
+        for a, ptr in ((coords, c.d_coords), (normals, c.d_normals)):
+            if a.size:
+                self.ctx.check(self.ctx.lib.kvsmc_copy_to_host(self.ctx.handle, a.ctypes.data, ptr, a.nbytes), "copy")
+        return coords, normals
+
+    def release(self, ticket):
+        self.ctx.check(self.ctx.lib.kvsmc_server_release(self.handle, ticket), "server_release")
+
+    def stats(self):
+        v = (C.c_uint64 * 7)()
+        self.ctx.check(self.ctx.lib.kvsmc_server_stats(self.handle, v), "server_stats")
+        keys = ("submitted", "completed", "batches", "kernel_launches", "held_bytes", "peak_bytes", "budget_waits")
+        return dict(zip(keys, (int(x) for x in v)))
+
+    def close(self):
+        if self.handle:
+            self.ctx.lib.kvsmc_server_destroy(self.handle)
+            self.handle = None
+
+    def __del__(self):
+        try:
+            self.close()
         except Exception:
             pass
 
