@@ -8,7 +8,10 @@ volume: the fused count launch, the scan, the fused emit launch, with output
 written to HBM.  `value` = cells x isovalues / s (Mcells/s).
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
-                    [--workload sweep1024|sweep384|uneven200|blobs128]
+                    [--workload sweep1024|sweep384|uneven200|serve|blobs128]
+
+--workload serve runs the request loop (kvsmc_server_*) under Poisson
+arrivals at each offered rate and reports p50/p99 latency and throughput.
 
 --workload uneven200 times the same 200-request batch three ways: one plain
 kvsmc_extract_device call per request (count, host sync, emit, host sync),
@@ -45,6 +48,13 @@ WORKLOADS = {
                       desc="200 volumes, each axis U[32,384], dtype U{uint8,uint16,float32}, ellipsoid phantoms "
                            "(3-6 nested rotated shells + N(0, 2% range) noise), one isovalue per volume U over the "
                            "central 60% of its range, duplication=true, PolygonNormal"),
+    "serve": dict(kind="serve", seed=77, rates=[100, 500, 2000], seconds=3.0,
+                  volumes=[("fbm", (256, 256, 256), np.float32)] * 4 + [("phantom", (512, 512, 512), np.uint16)] * 2
+                  + [("blobs", (768, 768, 768), np.float32)] * 2,
+                  desc="serving loop: 8 resident volumes (4x 256^3 f32 fBm, 2x 512^3 u16 phantoms, 2x 768^3 f32 "
+                       "Gaussian blobs); Poisson arrivals at 100, 500, 2000 req/s, each request a uniform volume and "
+                       "an isovalue uniform in its 10th-90th value percentiles; 40 GiB output budget; "
+                       "duplication=true, PolygonNormal"),
     "blobs128": dict(shape=(128, 128, 128), kind="blobs", isos=[0.5],
                      desc="128^3 float32, 4 Gaussian blobs (sigma 8..24) + U[-0.01,0.01] noise, iso 0.5, "
                           "duplication=true, PolygonNormal"),
@@ -481,6 +491,109 @@ def run_batch_cpu(args):
                                           for v in args.batch_sample), done / 1e6)
 
 
+# ----------------------------------------------------------------- serving
+
+def run_serve(args, rank, world, local):
+    """The request loop under Poisson arrivals: p50/p99 latency and throughput."""
+    import threading
+
+    import torch
+
+    from kvs_gb300 import _abi
+    from kvs_gb300 import synthetic as S
+
+    torch.cuda.set_device(local)
+    w = WORKLOADS[args.workload]
+    ctx = _abi.Context(local)
+    rng = np.random.default_rng(w["seed"])
+    vols, pct, cells = [], [], []
+    for i, (kind, shape, dt) in enumerate(w["volumes"]):
+        if kind == "fbm":
+            f = S.fbm(shape, seed=w["seed"] + i, device="cuda")
+        elif kind == "phantom":
+            f = S.ellipsoid_phantom(shape, dt, seed=w["seed"] + i, device="cuda")
+        else:
+            f = S.gaussian_blobs(shape, seed=w["seed"] + i, device="cuda")
+        torch.cuda.synchronize()
+        vols.append(_abi.DeviceVolume.from_device(ctx, f.data_ptr(), dt, shape))
+        g = torch.Generator(device="cuda").manual_seed(i)
+        sample = f.flatten()[torch.randint(0, f.numel(), (1 << 20,), device="cuda", generator=g)].double()
+        pct.append((float(torch.quantile(sample, 0.10)), float(torch.quantile(sample, 0.90))))
+        cells.append((shape[0] - 1) * (shape[1] - 1) * (shape[2] - 1))
+        del f, sample
+    torch.cuda.empty_cache()
+    for v in vols:
+        v.minmax()
+    srv = _abi.Server(ctx, budget_bytes=40 << 30, max_batch=256, workers=3)
+
+    def run_rate(rate, seconds, warm=False):
+        n = max(20, int(rate * seconds))
+        gaps = rng.exponential(1.0 / rate, n)
+        picks = rng.integers(0, len(vols), n)
+        fr = rng.uniform(0.0, 1.0, n)
+        reqs = [(int(picks[k]), _abi.make_params(pct[picks[k]][0] + fr[k] * (pct[picks[k]][1] - pct[picks[k]][0]),
+                                                 _abi.MODE_DUP_POLYGON_NORMAL)) for k in range(n)]
+        done = []
+
+        def poller():
+            t_end = time.time() + 600
+            while len(done) < n and time.time() < t_end:
+                for c in srv.poll(timeout_ms=50):
+                    done.append((c.ticket, c.status, c.submit_s, c.start_s, c.done_s, c.sizes.ntriangles,
+                                 c.batch_size))
+                    srv.release(c.ticket)
+
+        th = threading.Thread(target=poller)
+        th.start()
+        vol_of = {}
+        t_next = time.perf_counter()
+        for k in range(n):
+            t_next += gaps[k]
+            while True:
+                d = t_next - time.perf_counter()
+                if d <= 0:
+                    break
+                if d > 0.0003:
+                    time.sleep(d - 0.0002)
+            vol_of[srv.submit(vols[reqs[k][0]], reqs[k][1])] = reqs[k][0]
+        th.join()
+        if warm:
+            return None
+        lat = np.array([d[4] - d[2] for d in done]) * 1e3
+        span = max(d[4] for d in done) - min(d[2] for d in done)
+        tri = sum(d[5] for d in done)
+        cel = sum(cells[vol_of[d[0]]] for d in done)
+        return {"rate_req_s": rate, "requests": n, "completed": len(done), "ok": sum(1 for d in done if d[1] == 0),
+                "p50_ms": round(float(np.percentile(lat, 50)), 3), "p99_ms": round(float(np.percentile(lat, 99)), 3),
+                "mean_ms": round(float(lat.mean()), 3),
+                "queue_p50_ms": round(float(np.percentile([(d[3] - d[2]) * 1e3 for d in done], 50)), 3),
+                "throughput_req_s": round(len(done) / span, 1), "mcells_per_s": round(cel / span / 1e6, 1),
+                "mtris_per_s": round(tri / span / 1e6, 1),
+                "mean_batch": round(float(np.mean([d[6] for d in done])), 2)}
+
+    run_rate(200, 0.5, warm=True)
+    clocks = Clocks(local)
+    clocks.start()
+    launches0 = srv.stats()["kernel_launches"]
+    results = [run_rate(r, w["seconds"]) for r in w["rates"]]
+    clk = clocks.stop()
+    st = srv.stats()
+    srv.close()
+    top = results[-1]
+    return {
+        "metric": "Mcells/s", "value": top["mcells_per_s"], "unit": "Mcells/s", "n_gpus": world,
+        "steps": len(results), "warmup": 1, "ms_per_step": None, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "u16/f32", "data": "synthetic (seeded fields generated on the device)",
+        "config": {"workload": w["desc"], "budget_bytes": 40 << 30, "max_batch": 256, "workers": 3,
+                   "cache": "volumes 4.2 GB in all, larger than L2"},
+        "value_at": "%d req/s offered" % top["rate_req_s"],
+        "serving": results,
+        "p50_ms": top["p50_ms"], "p99_ms": top["p99_ms"],
+        "server_stats": st, "gpu_launches": int(st["kernel_launches"] - launches0), "clocks": clk,
+        "e2e": None,
+    }
+
+
 # ----------------------------------------------------------------- CPU side
 
 def cpu_slab_sample(args, slab_planes):
@@ -582,6 +695,10 @@ def run_reference(args, rank, world):
     threads = os.cpu_count() or 1
     if w["kind"] == "batch":
         return run_reference_batch(args, world, threads)
+    if w["kind"] == "serve":
+        return {"impl": "reference", "unavailable": "the reference has no request loop (one kvs::MarchingCubes call "
+                "at a time on the caller's thread); its per-request CPU cost is the uneven200 / sweep1024 reference "
+                "arms"}
     planes = min(65, w["shape"][0]) if w["kind"] == "fbm" else w["shape"][0]
     isos = w["isos"]
     vals = []
@@ -623,6 +740,8 @@ def main():
         dist.init_process_group("nccl")
     if args.impl == "reference":
         line = run_reference(args, rank, world)
+    elif WORKLOADS[args.workload]["kind"] == "serve":
+        line = run_serve(args, rank, world, local)
     elif WORKLOADS[args.workload]["kind"] == "batch":
         line = run_batch(args, rank, world, local)
         if rank == 0 and world == 1 and not args.no_cpu:
