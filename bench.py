@@ -517,10 +517,11 @@ def run_serve(args, rank, world, local):
         torch.cuda.synchronize()
         vols.append(_abi.DeviceVolume.from_device(ctx, f.data_ptr(), dt, shape))
         g = torch.Generator(device="cuda").manual_seed(i)
-        sample = f.flatten()[torch.randint(0, f.numel(), (1 << 20,), device="cuda", generator=g)].double()
+        src = f.to(torch.int32) if f.dtype == torch.uint16 else f   # no uint16 indexing on every torch
+        sample = src.flatten()[torch.randint(0, f.numel(), (1 << 20,), device="cuda", generator=g)].double()
         pct.append((float(torch.quantile(sample, 0.10)), float(torch.quantile(sample, 0.90))))
         cells.append((shape[0] - 1) * (shape[1] - 1) * (shape[2] - 1))
-        del f, sample
+        del f, src, sample
     torch.cuda.empty_cache()
     for v in vols:
         v.minmax()
