@@ -228,7 +228,8 @@ void kvsmc_plan_destroy(kvsmc_plan* plan);
  * take every pending request (up to `max_batch`) as soon as they are free,
  * count them in one fused pass, admit them against the output budget (48
  * bytes per triangle of device memory held until the client releases the
- * result), allocate their outputs stream-ordered, and emit them in one fused
+ * result), carve their outputs from a device arena of the budget's size
+ * (allocated once, at creation), and emit them in one fused
  * pass; batches of different workers overlap on the GPU, so requests that
  * arrive while others run start without waiting for them.  A request whose
  * output alone exceeds the budget completes with KVSMC_ERR_BUDGET.  Served

@@ -5,17 +5,21 @@
 // context (its own stream, scratch and auxiliary streams) and loops: take
 // every pending request up to max_batch, count them in one fused pass,
 // admit them against the output budget, allocate their outputs from the
-// server's stream-ordered memory pool, emit them in one fused pass, publish
-// the completions.  With several workers, one batch counts while another
+// server's output arena, emit them in one fused pass, publish the
+// completions.  With several workers, one batch counts while another
 // emits, so new arrivals never wait for a whole batch in flight.  The
 // budget counts the bytes of results the clients have not released yet; a
 // batch that does not fit waits for releases (its requests that could
-// never fit alone complete with KVSMC_ERR_BUDGET).
+// never fit alone complete with KVSMC_ERR_BUDGET).  The budget is laid out
+// once, at creation, as one device arena; results are carved from it by a
+// host-side best-fit free list, so admitting and releasing a result costs no
+// CUDA allocation call.
 #include <algorithm>
 #include <chrono>
 #include <condition_variable>
 #include <cstring>
 #include <deque>
+#include <map>
 #include <mutex>
 #include <thread>
 #include <unordered_map>
@@ -34,12 +38,49 @@ struct Pending {
 };
 
 struct Held {
-    float* coords;
-    float* normals;
+    uint64_t coords_off, coords_len, normals_off, normals_len;
     uint64_t bytes;
 };
 
 constexpr uint64_t kBytesPerTriangle = 48;   // 9 coords + 3 normals, float
+constexpr uint64_t kArenaAlign = 256;
+
+// Best-fit free list over [0, size): offset -> length, neighbours coalesced.
+struct FreeList {
+    std::map<uint64_t, uint64_t> free_;
+    void reset(uint64_t size) { free_.clear(); if (size) free_[0] = size; }
+    bool take(uint64_t len, uint64_t* off)
+    {
+        auto best = free_.end();
+        for (auto it = free_.begin(); it != free_.end(); ++it)
+            if (it->second >= len && (best == free_.end() || it->second < best->second)) best = it;
+        if (best == free_.end()) return false;
+        *off = best->first;
+        const uint64_t rest = best->second - len;
+        const uint64_t at = best->first + len;
+        free_.erase(best);
+        if (rest) free_[at] = rest;
+        return true;
+    }
+    void give(uint64_t off, uint64_t len)
+    {
+        auto next = free_.lower_bound(off);
+        if (next != free_.end() && off + len == next->first) {
+            len += next->second;
+            next = free_.erase(next);
+        }
+        if (next != free_.begin()) {
+            auto prev = std::prev(next);
+            if (prev->first + prev->second == off) {
+                prev->second += len;
+                return;
+            }
+        }
+        free_[off] = len;
+    }
+};
+
+uint64_t arena_len(uint64_t bytes) { return (bytes + kArenaAlign - 1) / kArenaAlign * kArenaAlign; }
 
 }  // namespace
 
@@ -48,8 +89,9 @@ struct kvsmc_server {
     kvsmc_server_config cfg{};
     std::vector<kvsmc_context*> wctx;   // one per worker
     std::vector<std::thread> threads;
-    cudaMemPool_t pool = nullptr;       // outputs of admitted requests
-    cudaStream_t free_stream = nullptr; // stream-ordered frees on release
+    char* arena = nullptr;              // outputs of admitted requests (the budget, laid out once)
+    uint64_t arena_bytes = 0;
+    FreeList free_list;                 // guarded by mu
     std::mutex mu;                      // queues, budget, counters
     std::mutex mm_mu;                   // min/max passes and first-use waits on the owner context
     std::condition_variable cv_work, cv_done, cv_budget;
@@ -73,10 +115,11 @@ namespace {
 using kvsmc_host::Item;
 using kvsmc_host::StreamBatch;
 
-void free_outputs(kvsmc_server* S, float* coords, float* normals)
+// Give a held result's blocks back (caller holds mu).
+void give_back(kvsmc_server* S, const Held& h)
 {
-    if (coords) cudaFreeAsync(coords, S->free_stream);
-    if (normals) cudaFreeAsync(normals, S->free_stream);
+    if (h.coords_len) S->free_list.give(h.coords_off, h.coords_len);
+    if (h.normals_len) S->free_list.give(h.normals_off, h.normals_len);
 }
 
 void worker(kvsmc_server* S, int w)
@@ -133,31 +176,64 @@ void worker(kvsmc_server* S, int w)
                 }
             }
         }
+        // outputs: carved from the arena once the budget (and a block of each
+        // size) is free; with nothing held the arena is whole, so a batch that
+        // fits the budget always gets its blocks eventually
+        std::vector<Held> blocks(n, Held{0, 0, 0, 0, 0});
+        std::vector<float*> coords(n, nullptr), normals(n, nullptr);
         if (need) {
             std::unique_lock<std::mutex> lk(S->mu);
-            if (S->in_use + need > budget) ++S->budget_waits;
-            S->cv_budget.wait(lk, [&] { return S->in_use + need <= budget || S->stop; });
+            bool waited = false;
+            for (;;) {
+                bool ok = S->in_use + need <= budget;
+                size_t taken = 0;
+                for (; ok && taken < admit.size(); ++taken) {
+                    Item* it = admit[taken];
+                    const size_t i = (size_t)(it - items.data());
+                    const uint64_t t = it->sizes.ntriangles;
+                    Held& h = blocks[i];
+                    h = Held{0, 0, 0, 0, t * kBytesPerTriangle};
+                    if (t == 0) continue;
+                    h.coords_len = arena_len(36 * t);
+                    h.normals_len = arena_len(12 * t);
+                    if (!S->free_list.take(h.coords_len, &h.coords_off)) { h.coords_len = h.normals_len = 0; ok = false; break; }
+                    if (!S->free_list.take(h.normals_len, &h.normals_off)) {
+                        S->free_list.give(h.coords_off, h.coords_len);
+                        h.coords_len = h.normals_len = 0;
+                        ok = false;
+                        break;
+                    }
+                }
+                if (ok) break;
+                for (size_t j = 0; j < taken; ++j) {
+                    Held& h = blocks[(size_t)(admit[j] - items.data())];
+                    give_back(S, h);
+                    h.coords_len = h.normals_len = 0;
+                }
+                if (S->stop) {
+                    for (Item* it : admit)
+                        it->status = kvsmc_host::fail(ctx, KVSMC_ERR_BUDGET, "server stopping before the budget freed");
+                    admit.clear();
+                    need = 0;
+                    break;
+                }
+                if (!waited) {
+                    ++S->budget_waits;
+                    waited = true;
+                }
+                S->cv_budget.wait(lk);
+            }
             S->in_use += need;
             S->peak = std::max(S->peak, S->in_use);
         }
-
-        // outputs (stream-ordered) and emit, in one fused pass
-        std::vector<float*> coords(n, nullptr), normals(n, nullptr);
         uint64_t granted = need;
         for (Item* it : admit) {
             const size_t i = (size_t)(it - items.data());
             const uint64_t t = it->sizes.ntriangles;
             it->emit = true;
             if (t == 0) continue;
-            cudaError_t e = cudaMallocFromPoolAsync(reinterpret_cast<void**>(&coords[i]), 36 * t, S->pool, ctx->stream);
-            if (e == cudaSuccess)
-                e = cudaMallocFromPoolAsync(reinterpret_cast<void**>(&normals[i]), 12 * t, S->pool, ctx->stream);
-            if (e != cudaSuccess) {
-                cudaGetLastError();
-                it->status = kvsmc_host::fail(ctx, KVSMC_ERR_OUT_OF_MEMORY, "output allocation: %s",
-                                              cudaGetErrorString(e));
-                continue;
-            }
+            coords[i] = reinterpret_cast<float*>(S->arena + blocks[i].coords_off);
+            normals[i] = reinterpret_cast<float*>(S->arena + blocks[i].normals_off);
             it->d_coords = coords[i];
             it->coords_cap = 9 * t;
             it->d_normals = normals[i];
@@ -187,14 +263,13 @@ void worker(kvsmc_server* S, int w)
             c.submit_s = reqs[i].t_submit;
             c.start_s = t_start;
             c.done_s = t_done;
-            const uint64_t bytes = coords[i] ? items[i].sizes.ntriangles * kBytesPerTriangle : 0;
             if (c.status || !coords[i]) {
-                free_outputs(S, coords[i], normals[i]);
+                give_back(S, blocks[i]);
             } else {
                 c.d_coords = coords[i];
                 c.d_normals = normals[i];
-                S->held[c.ticket] = Held{coords[i], normals[i], bytes};
-                granted -= bytes;
+                S->held[c.ticket] = blocks[i];
+                granted -= blocks[i].bytes;
             }
             S->done.push_back(c);
             ++S->completed;
@@ -202,7 +277,7 @@ void worker(kvsmc_server* S, int w)
         // budget reserved for requests that hold nothing (failed, empty) goes back now
         S->in_use -= granted;
         S->cv_done.notify_all();
-        if (granted) S->cv_budget.notify_all();
+        S->cv_budget.notify_all();
         if (!later.empty()) S->cv_work.notify_one();
     }
 }
@@ -223,19 +298,13 @@ kvsmc_status kvsmc_server_create(kvsmc_context* ctx, const kvsmc_server_config* 
     if (S->cfg.max_batch <= 0) S->cfg.max_batch = 256;
     if (S->cfg.workers <= 0) S->cfg.workers = 3;
     S->t0 = std::chrono::steady_clock::now();
-    cudaMemPoolProps props;
-    std::memset(&props, 0, sizeof props);
-    props.allocType = cudaMemAllocationTypePinned;
-    props.location.type = cudaMemLocationTypeDevice;
-    props.location.id = ctx->device;
-    cudaError_t e = cudaMemPoolCreate(&S->pool, &props);
-    if (e == cudaSuccess) {
-        // keep freed blocks mapped for reuse, up to the budget
-        uint64_t keep = S->cfg.output_budget_bytes;
-        e = cudaMemPoolSetAttribute(S->pool, cudaMemPoolAttrReleaseThreshold, &keep);
-    }
-    if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&S->free_stream, cudaStreamNonBlocking);
-    kvsmc_status st = e == cudaSuccess ? KVSMC_OK : KVSMC_ERR_CUDA;
+    // the arena: the budget plus room for the 256-byte rounding of every block
+    // of a full batch in each worker
+    S->arena_bytes = S->cfg.output_budget_bytes + 2 * kArenaAlign * (uint64_t)S->cfg.max_batch * S->cfg.workers;
+    cudaError_t e = cudaMalloc(reinterpret_cast<void**>(&S->arena), S->arena_bytes);
+    S->free_list.reset(e == cudaSuccess ? S->arena_bytes : 0);
+    kvsmc_status st = e == cudaSuccess ? KVSMC_OK
+                                       : (e == cudaErrorMemoryAllocation ? KVSMC_ERR_OUT_OF_MEMORY : KVSMC_ERR_CUDA);
     for (int w = 0; w < S->cfg.workers && !st; ++w) {
         kvsmc_context* c = nullptr;
         st = kvsmc_create(ctx->device, &c);
@@ -243,8 +312,7 @@ kvsmc_status kvsmc_server_create(kvsmc_context* ctx, const kvsmc_server_config* 
     }
     if (st) {
         for (kvsmc_context* c : S->wctx) kvsmc_destroy(c);
-        if (S->free_stream) cudaStreamDestroy(S->free_stream);
-        if (S->pool) cudaMemPoolDestroy(S->pool);
+        if (S->arena) cudaFree(S->arena);
         cudaGetLastError();
         delete S;
         return kvsmc_host::fail(ctx, st, "server: set-up failed");
@@ -307,8 +375,7 @@ kvsmc_status kvsmc_server_release(kvsmc_server* S, uint64_t ticket)
     std::lock_guard<std::mutex> lk(S->mu);
     auto f = S->held.find(ticket);
     if (f == S->held.end()) return KVSMC_OK;   // nothing held (empty, failed or already released)
-    cudaSetDevice(S->ctx->device);
-    free_outputs(S, f->second.coords, f->second.normals);
+    give_back(S, f->second);
     S->in_use -= f->second.bytes;
     S->held.erase(f);
     S->cv_budget.notify_all();
@@ -347,12 +414,9 @@ void kvsmc_server_destroy(kvsmc_server* S)
     S->cv_budget.notify_all();
     for (std::thread& t : S->threads) t.join();
     cudaSetDevice(S->ctx->device);
-    for (auto& h : S->held) free_outputs(S, h.second.coords, h.second.normals);
     S->held.clear();
-    cudaStreamSynchronize(S->free_stream);
     for (kvsmc_context* c : S->wctx) kvsmc_destroy(c);
-    cudaStreamDestroy(S->free_stream);
-    cudaMemPoolDestroy(S->pool);
+    cudaFree(S->arena);
     delete S;
 }
 
