@@ -315,6 +315,11 @@ kvsmc_status StreamBatch::emit()
         any = any || ok;
     }
     if (!any) return KVSMC_OK;
+    for (StreamGroup& g : groups) {
+        g.skip_emit = 1;
+        for (int k = 0; k < g.niso; ++k)
+            if (isos[g.iso_begin + k].coords) g.skip_emit = 0;
+    }
     kvsmc_status st = upload_tables();
     if (st) return st;
     const kvsmc::Launch L = launch_of(ctx);

@@ -78,6 +78,8 @@ struct StreamGroup {
     uint32_t warp_smem_offset;
     float bs, bo;            // bucket(v) = floor(kStreamBuckets * sat(v * bs + bo)), in [0, kStreamBuckets]
     const float2* bricks;    // per brick (8 cell planes x 2 cell rows x one segment) node min/max, or null
+    int32_t skip_emit;       // 1: no isolevel of the group is written by this emit launch
+    int32_t pad_;
 };
 
 // Brick min/max table of a volume for `rows` cell rows per warp task: one

@@ -399,6 +399,7 @@ __global__ void __launch_bounds__(kStreamThreads, EMIT ? 2 : 3)
     const uint32_t row_bytes = (uint32_t)(avail < G.seg_copy_bytes ? avail : G.seg_copy_bytes);
     const T* vol = static_cast<const T*>(G.vol.data);
 
+    if (EMIT && G.skip_emit) continue;   // nothing of this group is written in this launch
     if (gi != gcur) {
         // the group's thresholds and bucket table
         if (lane < (unsigned)niso) {

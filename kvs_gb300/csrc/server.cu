@@ -159,126 +159,147 @@ void worker(kvsmc_server* S, int w)
             if (!st) st = b.count();
         }
 
-        // admission: what this batch's results will hold until released
-        uint64_t need = 0;
-        std::vector<Item*> admit, later;
-        if (!st) {
-            for (Item* it : live) {
-                const uint64_t bytes = it->sizes.ntriangles * kBytesPerTriangle;
-                if (bytes > budget) {
-                    it->status = kvsmc_host::fail(ctx, KVSMC_ERR_BUDGET, "result of %llu bytes exceeds the budget",
-                                                  (unsigned long long)bytes);
-                } else if (need + bytes > budget) {
-                    later.push_back(it);   // the batch alone would exceed the budget: run it again later
-                } else {
+        // Emit in rounds reusing this one count: each round admits the next
+        // requests (in order) whose results fit the budget together, waits
+        // until the budget and arena blocks are free, emits just those, and
+        // publishes them.  A request whose result alone exceeds the budget
+        // completes with KVSMC_ERR_BUDGET.
+        std::vector<char> published(n, 0);
+        size_t next = 0;
+        bool first_round = true;
+        for (;;) {
+            std::vector<Item*> admit;
+            uint64_t need = 0;
+            if (!st) {
+                while (next < live.size()) {
+                    Item* it = live[next];
+                    const uint64_t bytes = it->sizes.ntriangles * kBytesPerTriangle;
+                    if (bytes > budget) {
+                        it->status = kvsmc_host::fail(ctx, KVSMC_ERR_BUDGET, "result of %llu bytes exceeds the budget",
+                                                      (unsigned long long)bytes);
+                        ++next;
+                        continue;
+                    }
+                    if (need + bytes > budget) break;
                     need += bytes;
                     admit.push_back(it);
+                    ++next;
                 }
             }
-        }
-        // outputs: carved from the arena once the budget (and a block of each
-        // size) is free; with nothing held the arena is whole, so a batch that
-        // fits the budget always gets its blocks eventually
-        std::vector<Held> blocks(n, Held{0, 0, 0, 0, 0});
-        std::vector<float*> coords(n, nullptr), normals(n, nullptr);
-        if (need) {
-            std::unique_lock<std::mutex> lk(S->mu);
-            bool waited = false;
-            for (;;) {
-                bool ok = S->in_use + need <= budget;
-                size_t taken = 0;
-                for (; ok && taken < admit.size(); ++taken) {
-                    Item* it = admit[taken];
-                    const size_t i = (size_t)(it - items.data());
-                    const uint64_t t = it->sizes.ntriangles;
-                    Held& h = blocks[i];
-                    h = Held{0, 0, 0, 0, t * kBytesPerTriangle};
-                    if (t == 0) continue;
-                    h.coords_len = arena_len(36 * t);
-                    h.normals_len = arena_len(12 * t);
-                    if (!S->free_list.take(h.coords_len, &h.coords_off)) { h.coords_len = h.normals_len = 0; ok = false; break; }
-                    if (!S->free_list.take(h.normals_len, &h.normals_off)) {
-                        S->free_list.give(h.coords_off, h.coords_len);
+            // outputs: carved from the arena once the budget (and a block of
+            // each size) is free; with nothing held the arena is whole, so a
+            // round that fits the budget always gets its blocks eventually
+            std::vector<Held> blocks(n, Held{0, 0, 0, 0, 0});
+            std::vector<float*> coords(n, nullptr), normals(n, nullptr);
+            if (need) {
+                std::unique_lock<std::mutex> lk(S->mu);
+                bool waited = false;
+                for (;;) {
+                    bool ok = S->in_use + need <= budget;
+                    size_t taken = 0;
+                    for (; ok && taken < admit.size(); ++taken) {
+                        Item* it = admit[taken];
+                        const size_t i = (size_t)(it - items.data());
+                        const uint64_t t = it->sizes.ntriangles;
+                        Held& h = blocks[i];
+                        h = Held{0, 0, 0, 0, t * kBytesPerTriangle};
+                        if (t == 0) continue;
+                        h.coords_len = arena_len(36 * t);
+                        h.normals_len = arena_len(12 * t);
+                        if (!S->free_list.take(h.coords_len, &h.coords_off)) {
+                            h.coords_len = h.normals_len = 0;
+                            ok = false;
+                            break;
+                        }
+                        if (!S->free_list.take(h.normals_len, &h.normals_off)) {
+                            S->free_list.give(h.coords_off, h.coords_len);
+                            h.coords_len = h.normals_len = 0;
+                            ok = false;
+                            break;
+                        }
+                    }
+                    if (ok) break;
+                    for (size_t j = 0; j < taken; ++j) {
+                        Held& h = blocks[(size_t)(admit[j] - items.data())];
+                        give_back(S, h);
                         h.coords_len = h.normals_len = 0;
-                        ok = false;
+                    }
+                    if (S->stop) {
+                        for (Item* it : admit)
+                            it->status = kvsmc_host::fail(ctx, KVSMC_ERR_BUDGET, "server stopping before the budget freed");
+                        admit.clear();
+                        need = 0;
                         break;
                     }
+                    if (!waited) {
+                        ++S->budget_waits;
+                        waited = true;
+                    }
+                    S->cv_budget.wait(lk);
                 }
-                if (ok) break;
-                for (size_t j = 0; j < taken; ++j) {
-                    Held& h = blocks[(size_t)(admit[j] - items.data())];
-                    give_back(S, h);
-                    h.coords_len = h.normals_len = 0;
-                }
-                if (S->stop) {
-                    for (Item* it : admit)
-                        it->status = kvsmc_host::fail(ctx, KVSMC_ERR_BUDGET, "server stopping before the budget freed");
-                    admit.clear();
-                    need = 0;
-                    break;
-                }
-                if (!waited) {
-                    ++S->budget_waits;
-                    waited = true;
-                }
-                S->cv_budget.wait(lk);
+                S->in_use += need;
+                S->peak = std::max(S->peak, S->in_use);
             }
-            S->in_use += need;
-            S->peak = std::max(S->peak, S->in_use);
-        }
-        uint64_t granted = need;
-        for (Item* it : admit) {
-            const size_t i = (size_t)(it - items.data());
-            const uint64_t t = it->sizes.ntriangles;
-            it->emit = true;
-            if (t == 0) continue;
-            coords[i] = reinterpret_cast<float*>(S->arena + blocks[i].coords_off);
-            normals[i] = reinterpret_cast<float*>(S->arena + blocks[i].normals_off);
-            it->d_coords = coords[i];
-            it->coords_cap = 9 * t;
-            it->d_normals = normals[i];
-            it->normals_cap = 3 * t;
-        }
-        if (!st && !admit.empty()) {
-            st = b.emit();
-            if (!st) st = b.finish();
-        }
-        if (st)
-            for (Item* it : live)
-                if (!it->status) it->status = st;
+            for (Item* it : live) it->emit = false;
+            for (Item* it : admit) {
+                const size_t i = (size_t)(it - items.data());
+                const uint64_t t = it->sizes.ntriangles;
+                it->emit = true;
+                if (t == 0) continue;
+                coords[i] = reinterpret_cast<float*>(S->arena + blocks[i].coords_off);
+                normals[i] = reinterpret_cast<float*>(S->arena + blocks[i].normals_off);
+                it->d_coords = coords[i];
+                it->coords_cap = 9 * t;
+                it->d_normals = normals[i];
+                it->normals_cap = 3 * t;
+            }
+            if (!st && !admit.empty()) {
+                st = b.emit();
+                if (!st) st = b.finish();
+            }
+            if (st)
+                for (Item* it : live)
+                    if (!it->status) it->status = st;
 
-        // publish
-        const double t_done = S->now();
-        std::unique_lock<std::mutex> lk(S->mu);
-        // deferred requests go back to the front, in order, for a later batch
-        for (auto r = later.rbegin(); r != later.rend(); ++r) S->pending.push_front(reqs[(size_t)(*r - items.data())]);
-        for (size_t i = 0; i < n; ++i) {
-            if (std::find(later.begin(), later.end(), &items[i]) != later.end()) continue;
-            kvsmc_completion c;
-            std::memset(&c, 0, sizeof c);
-            c.ticket = reqs[i].ticket;
-            c.status = items[i].status;
-            c.batch_size = (int32_t)n;
-            c.sizes = items[i].sizes;
-            c.submit_s = reqs[i].t_submit;
-            c.start_s = t_start;
-            c.done_s = t_done;
-            if (c.status || !coords[i]) {
-                give_back(S, blocks[i]);
-            } else {
-                c.d_coords = coords[i];
-                c.d_normals = normals[i];
-                S->held[c.ticket] = blocks[i];
-                granted -= blocks[i].bytes;
+            // publish this round: the admitted requests, and (first round) the
+            // ones that failed or had nothing to extract; on an error, all
+            const double t_done = S->now();
+            uint64_t granted = need;
+            std::unique_lock<std::mutex> lk(S->mu);
+            for (size_t i = 0; i < n; ++i) {
+                if (published[i]) continue;
+                const bool in_round = std::find(admit.begin(), admit.end(), &items[i]) != admit.end();
+                const bool settled = items[i].status != KVSMC_OK || !items[i].extracted ||
+                                     (first_round && std::find(live.begin(), live.end(), &items[i]) == live.end());
+                if (!in_round && !settled && !st) continue;
+                published[i] = 1;
+                kvsmc_completion c;
+                std::memset(&c, 0, sizeof c);
+                c.ticket = reqs[i].ticket;
+                c.status = items[i].status;
+                c.batch_size = (int32_t)n;
+                c.sizes = items[i].sizes;
+                c.submit_s = reqs[i].t_submit;
+                c.start_s = t_start;
+                c.done_s = t_done;
+                if (in_round && !c.status && coords[i]) {
+                    c.d_coords = coords[i];
+                    c.d_normals = normals[i];
+                    S->held[c.ticket] = blocks[i];
+                    granted -= blocks[i].bytes;
+                } else if (in_round) {
+                    give_back(S, blocks[i]);
+                }
+                S->done.push_back(c);
+                ++S->completed;
             }
-            S->done.push_back(c);
-            ++S->completed;
+            // budget reserved for requests that hold nothing (failed, empty) goes back now
+            S->in_use -= granted;
+            S->cv_done.notify_all();
+            S->cv_budget.notify_all();
+            first_round = false;
+            if (st || next >= live.size()) break;
         }
-        // budget reserved for requests that hold nothing (failed, empty) goes back now
-        S->in_use -= granted;
-        S->cv_done.notify_all();
-        S->cv_budget.notify_all();
-        if (!later.empty()) S->cv_work.notify_one();
     }
 }
 
