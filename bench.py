@@ -8,7 +8,7 @@ volume: the fused count launch, the scan, the fused emit launch, with output
 written to HBM.  `value` = cells x isovalues / s (Mcells/s).
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
-                    [--workload sweep1024|sweep384|uneven200|serve|blobs128]
+                    [--workload sweep1024|sweep384|uneven200|serve|heavy|blobs128]
 
 --workload serve runs the request loop (kvsmc_server_*) under Poisson
 arrivals at each offered rate and reports p50/p99 latency and throughput.
@@ -55,6 +55,10 @@ WORKLOADS = {
                        "Gaussian blobs); Poisson arrivals at 100, 500, 2000 req/s, each request a uniform volume and "
                        "an isovalue uniform in its 10th-90th value percentiles; 40 GiB output budget; "
                        "duplication=true, PolygonNormal"),
+    "heavy": dict(shape=(1024, 2048, 2048), kind="boxnoise", dtype=np.uint16, pcts=[0.45, 0.50, 0.55, 0.60],
+                  desc="output-heavy stress: 2048x2048x1024 uint16 white noise U[0,65535] box-filtered (3 taps per "
+                       "axis), 4 isovalues at the 45/50/55/60th percentiles in one batched call, duplication=true, "
+                       "PolygonNormal"),
     "blobs128": dict(shape=(128, 128, 128), kind="blobs", isos=[0.5],
                      desc="128^3 float32, 4 Gaussian blobs (sigma 8..24) + U[-0.01,0.01] noise, iso 0.5, "
                           "duplication=true, PolygonNormal"),
@@ -90,7 +94,17 @@ def make_field(w, device, seed=42):
     from kvs_gb300 import synthetic as S
     if w["kind"] == "fbm":
         return S.fbm(w["shape"], seed=seed, device=device)
+    if w["kind"] == "boxnoise":
+        return S.box_filtered_noise(w["shape"], w["dtype"], seed=seed, device=device)
     return S.gaussian_blobs(w["shape"], seed=seed, device=device)
+
+
+def workload_isos(w, sample):
+    """The workload's isovalues: fixed, or percentiles of a value sample
+    (a flat float64 array)."""
+    if "pcts" in w:
+        return [float(np.quantile(sample, q)) for q in w["pcts"]]
+    return list(w["isos"])
 
 
 class Clocks:
@@ -180,18 +194,28 @@ def run_ours(args, rank, world, local):
     ctx = _abi.Context(local)
     stream = torch.cuda.Stream()
     ctx.set_stream(stream.cuda_stream)
+    from kvs_gb300 import synthetic as S
+    dt = np.dtype(w.get("dtype", np.float32))
     field = make_field(w, "cuda")
     torch.cuda.synchronize()
-    vol = _abi.DeviceVolume.from_device(ctx, field.data_ptr(), np.float32, field.shape)
+    vol = _abi.DeviceVolume.from_device(ctx, field.data_ptr(), dt, field.shape)
     host_field = None
     if not args.no_e2e:
-        host_field = torch.empty(field.shape, dtype=torch.float32, pin_memory=True)
+        host_field = torch.empty(field.shape, dtype=field.dtype, pin_memory=True)
         host_field.copy_(field)
     # the CPU baseline's sample: the first z-slab of this same field
-    args.cpu_slab = field[:min(nz, 65)].cpu().numpy() if rank == 0 else None
+    args.cpu_slab = S.to_numpy(field[:min(nz, 65)]) if rank == 0 else None
+    sample = None
+    if "pcts" in w:
+        g = torch.Generator(device="cuda").manual_seed(7)
+        src = field.to(torch.int32) if field.dtype == torch.uint16 else field
+        sample = src.flatten()[torch.randint(0, field.numel(), (1 << 22,), device="cuda", generator=g)].double()
+        sample = sample.cpu().numpy()
+        del src
     del field
     torch.cuda.empty_cache()
-    isos = w["isos"]
+    isos = workload_isos(w, sample)
+    args.isos = isos
     n = len(isos)
     reqs = (_abi.Request * n)()
     for i, iso in enumerate(isos):
@@ -241,7 +265,7 @@ def run_ours(args, rank, world, local):
     value = cells * world / (step_ms * 1e-3) / 1e6
     # roofline of the dominant kernel (the fused emit launch)
     hbm, peak_kind = peaks()
-    algo_bytes = nx * ny * nz * 4 + 48 * ntri
+    algo_bytes = nx * ny * nz * dt.itemsize + 48 * ntri
     dom = max(prof.items(), key=lambda kv: kv[1][1])
     emit_launches, emit_ms = prof.get("stream_emit", (0, 0.0))
     roofline = None
@@ -263,11 +287,13 @@ def run_ours(args, rank, world, local):
     line = {
         "metric": "Mcells/s", "value": round(value, 1), "unit": "Mcells/s", "n_gpus": world,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(step_ms, 4),
-        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
-        "data": "synthetic (seeded fBm generated on the device)",
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": {"float32": "f32", "uint16": "u16"}.get(dt.name, dt.name),
+        "data": "synthetic (seeded field generated on the device)",
         "config": {"workload": w["desc"], "volume": [nx, ny, nz], "isovalues": n,
+                   "isolevels": [round(x, 6) for x in isos],
                    "mode": "duplication+PolygonNormal", "cache": "inputs larger than L2 (4 GiB volume, "
-                   "outputs ~48 B/triangle)" if args.workload == "sweep1024" else (
+                   "outputs ~48 B/triangle)" if args.workload in ("sweep1024", "heavy") else (
                    "inputs larger than L2 (216 MiB volume)" if args.workload == "sweep384" else "input smaller than L2")},
         "mtris_per_s": round(ntri * world / (step_ms * 1e-3) / 1e6, 1),
         "triangles_per_step": int(ntri),
@@ -611,9 +637,12 @@ def cpu_slab_sample(args, slab_planes):
         # same field: generate the full-depth statistics on a slab (rescaled
         # per slab; the sample only sets the cost per cell)
         f = S.fbm((slab_planes, ny, nx), seed=42, device="cpu")
+    elif w["kind"] == "boxnoise":
+        # box-filtered noise is statistically the same in every slab
+        f = S.box_filtered_noise((min(slab_planes, nz), ny, nx), w["dtype"], seed=42, device="cpu")
     else:
         f = S.gaussian_blobs((min(slab_planes, nz), ny, nx), seed=42, device="cpu")
-    return f.numpy()
+    return S.to_numpy(f)
 
 
 def run_cpu(args, threads, planes, isos):
@@ -704,8 +733,12 @@ def run_reference(args, rank, world):
         return {"impl": "reference", "unavailable": "the reference has no request loop (one kvs::MarchingCubes call "
                 "at a time on the caller's thread); its per-request CPU cost is the uneven200 / sweep1024 reference "
                 "arms"}
-    planes = min(65, w["shape"][0]) if w["kind"] == "fbm" else w["shape"][0]
-    isos = w["isos"]
+    planes = min(65, w["shape"][0]) if w["kind"] in ("fbm", "boxnoise") else w["shape"][0]
+    if "pcts" in w:
+        args.cpu_slab = cpu_slab_sample(args, planes)
+        isos = workload_isos(w, args.cpu_slab.astype(np.float64).ravel())
+    else:
+        isos = w["isos"]
     vals = []
     sample = ""
     for i in range(args.warmup + args.steps):
@@ -757,8 +790,8 @@ def main():
         line = run_ours(args, rank, world, local)
         if rank == 0 and world == 1 and not args.no_cpu:
             w = WORKLOADS[args.workload]
-            planes = min(65, w["shape"][0]) if w["kind"] == "fbm" else w["shape"][0]
-            isos = w["isos"] if w["kind"] == "fbm" else w["isos"] * 50
+            planes = min(65, w["shape"][0]) if w["kind"] in ("fbm", "boxnoise") else w["shape"][0]
+            isos = args.isos if w["kind"] in ("fbm", "boxnoise") else w["isos"] * 50
             v, t, sample = run_cpu(args, 1, planes, isos)
             line["cpu_baseline"] = {"value": round(v, 1), "unit": "Mcells/s", "cores": 1, "kind": "port",
                                     "sample": sample + f"; {t:.1f} s on 1 host core; oracle/mc_oracle.c"}
