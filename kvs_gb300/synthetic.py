@@ -6,7 +6,8 @@ with the shapes, dtypes and value distributions of the workloads:
   gaussian_blobs       sum of isotropic Gaussians + uniform noise (float32)
   fbm                  fractal Brownian motion of 3-D gradient noise in [0, 1]
   ellipsoid_phantom    nested rotated ellipsoidal shells + Gaussian noise
-  box_filtered_noise   white noise low-passed by a 3-tap box filter per axis
+  box_filtered_noise   white noise low-passed by a box filter per axis
+  lattice_noise        white noise on a coarse lattice, trilinearly interpolated
 
 All return arrays shaped (nz, ny, nx) (x fastest, as the mapper expects).
 They run with torch on any device, so the large fields are made on the GPU
@@ -166,9 +167,23 @@ def ellipsoid_phantom(shape, dtype, seed=0, device="cpu"):
     return _cast(out, dtype)
 
 
-def box_filtered_noise(shape, dtype=np.uint16, seed=0, device="cpu"):
-    """White noise uniform over the dtype's range, box-filtered (3 taps, edge
-    replicated) along x, y and z, rounded back to the dtype."""
+def _box_wide(f, dim, taps):
+    """Box filter of odd width `taps` along one dimension (edges replicated),
+    through a running sum."""
+    h = taps // 2
+    n = f.shape[dim]
+    g = torch.cat([f.narrow(dim, 0, 1).expand(*[h if d == dim else -1 for d in range(f.dim())]), f,
+                   f.narrow(dim, n - 1, 1).expand(*[h if d == dim else -1 for d in range(f.dim())])], dim)
+    c = torch.cumsum(g, dim)
+    del g
+    zero = torch.zeros_like(c.narrow(dim, 0, 1))
+    c = torch.cat([zero, c], dim)
+    return (c.narrow(dim, taps, n) - c.narrow(dim, 0, n)) / taps
+
+
+def box_filtered_noise(shape, dtype=np.uint16, seed=0, device="cpu", taps=3):
+    """White noise uniform over the dtype's range, box-filtered (`taps` taps,
+    odd, edge replicated) along x, y and z, rounded back to the dtype."""
     nz, ny, nx = shape
     lo, hi = _dtype_range(dtype)
     gen = torch.Generator(device=device).manual_seed(seed)
@@ -177,10 +192,43 @@ def box_filtered_noise(shape, dtype=np.uint16, seed=0, device="cpu"):
         n = f.shape[dim]
         if n < 2:
             continue
-        idx = torch.arange(n, device=device)
-        left = f.index_select(dim, torch.clamp(idx - 1, 0, n - 1))
-        right = f.index_select(dim, torch.clamp(idx + 1, 0, n - 1))
-        f = (left + f + right) / 3.0
+        if taps == 3:
+            idx = torch.arange(n, device=device)
+            left = f.index_select(dim, torch.clamp(idx - 1, 0, n - 1))
+            right = f.index_select(dim, torch.clamp(idx + 1, 0, n - 1))
+            f = (left + f + right) / 3.0
+        else:
+            f = _box_wide(f, dim, taps)
+    return _cast(f, dtype)
+
+
+def lattice_noise(shape, dtype=np.uint16, seed=0, device="cpu", spacing=32):
+    """White noise uniform over the dtype's range on a lattice of the given
+    spacing (in cells), trilinearly interpolated to the full grid (a low-pass
+    of white noise whose isosurfaces cross about 2/spacing of the cells per
+    isovalue), rounded back to the dtype."""
+    nz, ny, nx = shape
+    lo, hi = _dtype_range(dtype)
+    gen = torch.Generator(device=device).manual_seed(seed)
+    cz, cy, cx = ((n - 1 + spacing - 1) // spacing + 1 for n in shape)
+    c = torch.rand((1, 1, cz, cy, cx), generator=gen, device=device, dtype=torch.float32) * (hi - lo) + lo
+    # sample the coarse grid at the fine nodes (node i at coarse coordinate i / spacing)
+    f = torch.empty((nz, ny, nx), dtype=torch.float32, device=device)
+    zs = torch.arange(nz, device=device, dtype=torch.float32) / spacing
+    ys = torch.arange(ny, device=device, dtype=torch.float32) / spacing
+    xs = torch.arange(nx, device=device, dtype=torch.float32) / spacing
+    cc = c[0, 0]
+    y0 = ys.floor().long().clamp(max=cy - 2)
+    x0 = xs.floor().long().clamp(max=cx - 2)
+    wy = (ys - y0.float())[:, None]
+    wx = (xs - x0.float())[None, :]
+    for z in range(nz):
+        z0 = min(int(zs[z].floor().item()), cz - 2)
+        wz = float(zs[z].item()) - z0
+        plane = cc[z0] * (1.0 - wz) + cc[z0 + 1] * wz
+        a = plane[y0][:, x0] * (1.0 - wx) + plane[y0][:, x0 + 1] * wx
+        b = plane[y0 + 1][:, x0] * (1.0 - wx) + plane[y0 + 1][:, x0 + 1] * wx
+        f[z] = a * (1.0 - wy) + b * wy
     return _cast(f, dtype)
 
 
