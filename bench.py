@@ -8,7 +8,7 @@ volume: the fused count launch, the scan, the fused emit launch, with output
 written to HBM.  `value` = cells x isovalues / s (Mcells/s).
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
-                    [--workload sweep1024|sweep384|uneven200|serve|heavy|blobs128]
+                    [--workload sweep1024|sweep512|uneven200|serve|heavy|blobs128]
 
 --workload serve runs the request loop (kvsmc_server_*) under Poisson
 arrivals at each offered rate and reports p50/p99 latency and throughput.
@@ -41,9 +41,10 @@ WORKLOADS = {
     "sweep1024": dict(shape=(1024, 1024, 1024), kind="fbm", isos=[0.2 + 0.04 * k for k in range(16)],
                       desc="1024^3 float32 fBm gradient noise (5 octaves, base freq 1/128, gain 0.5, in [0,1]), "
                            "16 isovalues 0.2..0.8 in one batched call, duplication=true, PolygonNormal"),
-    "sweep384": dict(shape=(384, 384, 384), kind="fbm", isos=[0.2 + 0.04 * k for k in range(16)],
-                     desc="384^3 float32 fBm gradient noise (as sweep1024), 16 isovalues 0.2..0.8 in one batched "
-                          "call, duplication=true, PolygonNormal (the profiling case)"),
+    "sweep512": dict(shape=(512, 512, 512), kind="fbm", isos=[0.2 + 0.04 * k for k in range(16)],
+                     desc="512^3 float32 fBm gradient noise (as sweep1024), 16 isovalues 0.2..0.8 in one batched "
+                          "call, duplication=true, PolygonNormal (the profiling case: same kernel instance as "
+                          "sweep1024)"),
     "uneven200": dict(kind="batch", n=200, dims=(32, 384), seed=2024,
                       desc="200 volumes, each axis U[32,384], dtype U{uint8,uint16,float32}, ellipsoid phantoms "
                            "(3-6 nested rotated shells + N(0, 2% range) noise), one isovalue per volume U over the "
@@ -297,7 +298,7 @@ def run_ours(args, rank, world, local):
                    "isolevels": [round(x, 6) for x in isos],
                    "mode": "duplication+PolygonNormal", "cache": "inputs larger than L2 (4 GiB volume, "
                    "outputs ~48 B/triangle)" if args.workload in ("sweep1024", "heavy") else (
-                   "inputs larger than L2 (216 MiB volume)" if args.workload == "sweep384" else "input smaller than L2")},
+                   "inputs larger than L2 (512 MiB volume)" if args.workload == "sweep512" else "input smaller than L2")},
         "mtris_per_s": round(ntri * world / (step_ms * 1e-3) / 1e6, 1),
         "triangles_per_step": int(ntri),
         "roofline": roofline,
