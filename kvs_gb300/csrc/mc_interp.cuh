@@ -133,9 +133,12 @@ static __device__ __noinline__ float3 interpolate_exact_slow(const Interp& j, fl
 
 // Vertex of an edge from corner A = (ax, ay, az) (value va) to the corner one
 // step along `axis` (0, 1, 2), whose coordinate there is `b` (a +- 1).  Same
-// result as edge_vertex_fast; the callers pass integer coordinates as floats.
-__device__ __forceinline__ float3 edge_vertex_axis(const Interp& j, const FastIso& f, float va, float vb, float ax,
-                                                   float ay, float az, int axis, float b)
+// result as edge_vertex_fast; the callers pass integer coordinates as floats
+// and the fast path's constants (f, min_coord, scale) from wherever they keep
+// them.
+__device__ __forceinline__ float3 edge_vertex_axis(const FastIso& f, const float* min_coord, const float* scale,
+                                                   const Interp& j, float va, float vb, float ax, float ay, float az,
+                                                   int axis, float b)
 {
     bool ok = f.fast_ok != 0;
     float r = 0.0f;
@@ -149,11 +152,12 @@ __device__ __forceinline__ float3 edge_vertex_axis(const Interp& j, const FastIs
     if (ok) {
         const float px = axis == 0 ? r : ax, py = axis == 1 ? r : ay, pz = axis == 2 ? r : az;
         float3 o;
-        o.x = __fmul_rn(__fadd_rn(px, j.min_coord[0]), j.scale[0]);
-        o.y = __fmul_rn(__fadd_rn(py, j.min_coord[1]), j.scale[1]);
-        o.z = __fmul_rn(__fadd_rn(pz, j.min_coord[2]), j.scale[2]);
+        o.x = __fmul_rn(__fadd_rn(px, min_coord[0]), scale[0]);
+        o.y = __fmul_rn(__fadd_rn(py, min_coord[1]), scale[1]);
+        o.z = __fmul_rn(__fadd_rn(pz, min_coord[2]), scale[2]);
         return o;
     }
+    // j (the FP64 constants, same min_coord and scale) is read only here
     const float bx = axis == 0 ? b : ax, by = axis == 1 ? b : ay, bz = axis == 2 ? b : az;
     return interpolate_exact_slow(j, va, vb, ax, ay, az, bx, by, bz);
 }

@@ -154,7 +154,7 @@ template <> __device__ __forceinline__ void load8<int8_t>(const int8_t* row, uin
 
 constexpr int kLut = kStreamBuckets + 1;   // bucket indices 0 .. kStreamBuckets
 constexpr uint32_t kMultiThr = 1u << 31;   // LUT flag: two or more thresholds lie in this bucket
-constexpr int kMaxVerts = 32 * 12;         // vertex items of one round (12 edges per pair at most)
+constexpr int kMaxVerts = 256;             // vertex items of one round (rounds end before it is exceeded)
 constexpr int kMaxTris = 32 * 5;           // triangle items of one round (5 per pair at most)
 
 // Per-CTA tables, indexed by the corner code of case_code() (not by the
@@ -182,7 +182,18 @@ struct WarpState {
 
 // Per-warp emit buffers: the unit's pairs, and for one round the vertex pool
 // (one entry per (pair, used edge)) and the item -> pair maps.
+// An isolevel's constants as the emit loops read them (copied from the
+// group's StreamIso entries when a warp starts on a group).
+struct IsoConst {
+    FastIso f;
+    float mc[3], sc[3];   // min_coord, scale
+    float* coords;
+    float* normals;
+    uint64_t cap_tris;
+};
+
 struct WarpEmit {
+    IsoConst ic[kStreamMaxIso];
     uint32_t pairs[kPairCap];
     float px[kMaxVerts], py[kMaxVerts], pz[kMaxVerts];
     uint8_t item_v[kMaxVerts];
@@ -403,9 +414,18 @@ __global__ void __launch_bounds__(kStreamThreads, EMIT ? 2 : 3)
     if (gi != gcur) {
         // the group's thresholds and bucket table
         if (lane < (unsigned)niso) {
-            const float t = isos[iso_begin + lane].f.f_thr;
+            const StreamIso& I = isos[iso_begin + lane];
+            const float t = I.f.f_thr;
             W.thr[lane] = t;
             W.thr_bucket[lane] = (int32_t)bucket_index(t, bs, bo);
+            if (EMIT) {
+                IsoConst& c = WE->ic[lane];
+                c.f = I.f;
+                for (int a = 0; a < 3; ++a) { c.mc[a] = I.ip.min_coord[a]; c.sc[a] = I.ip.scale[a]; }
+                c.coords = I.coords;
+                c.normals = I.normals;
+                c.cap_tris = I.cap_tris;
+            }
         }
         __syncwarp();
         for (unsigned b = lane; b < (unsigned)kLut; b += 32) {
@@ -614,15 +634,24 @@ __global__ void __launch_bounds__(kStreamThreads, EMIT ? 2 : 3)
                     }
                     __syncwarp();
                     const uint32_t nfill = (npairs - fill0 < (uint32_t)kPairCap) ? npairs - fill0 : (uint32_t)kPairCap;
-                    for (uint32_t r0 = 0; r0 < nfill; r0 += 32) {
-                        // ---- one pair per lane
+                    for (uint32_t r0 = 0, taken = 0; r0 < nfill; r0 += taken) {
+                        // ---- one pair per lane, as many as the vertex pool holds
                         const uint32_t p = r0 + lane;
-                        const bool has = p < nfill;
-                        const uint32_t pe = has ? pbuf[p] : 0u;
+                        bool has = p < nfill;
+                        const uint32_t pe0 = has ? pbuf[p] : 0u;
+                        const uint32_t ne0 = has ? (uint32_t)__popc(TB.edge_mask[pe0 >> 16]) : 0u;
+                        uint32_t vpre = 0;
+#pragma unroll
+                        for (int bit = 0; bit < 4; ++bit)
+                            vpre += (uint32_t)__popc(__ballot_sync(FULL, (ne0 >> bit) & 1u) & lt) << bit;
+                        has = has && vpre + ne0 <= (uint32_t)kMaxVerts;   // a suffix of lanes waits
+                        taken = (uint32_t)__popc(__ballot_sync(FULL, has));
+                        const uint32_t nv = __shfl_sync(FULL, vpre + ne0, taken - 1);
+                        const uint32_t pe = has ? pe0 : 0u;
                         const uint32_t k = (pe >> 8) & 0xffu, code = pe >> 16;
                         const uint32_t rk = ((pe & 0xffu) >> SEG_SHIFT) * 16 + k;   // (row, isolevel) slot
                         const uint32_t nt = has ? TB.ntri[code] : 0u;
-                        const uint32_t ne = has ? (uint32_t)__popc(TB.edge_mask[code]) : 0u;
+                        const uint32_t ne = has ? ne0 : 0u;
                         // output position of the pair's first triangle: pairs are in
                         // cell order, so it is the (row, isolevel)'s running count plus
                         // the triangles of the earlier lanes of the same (row, isolevel)
@@ -636,13 +665,6 @@ __global__ void __launch_bounds__(kStreamThreads, EMIT ? 2 : 3)
                             gtot += (uint32_t)__popc(bm & grp) << bit;
                             tpre += (uint32_t)__popc(bm & lt) << bit;
                             ntr += (uint32_t)__popc(bm) << bit;
-                        }
-                        uint32_t vpre = 0, nv = 0;
-#pragma unroll
-                        for (int bit = 0; bit < 4; ++bit) {
-                            const uint32_t bm = __ballot_sync(FULL, (ne >> bit) & 1u);
-                            vpre += (uint32_t)__popc(bm & lt) << bit;
-                            nv += (uint32_t)__popc(bm) << bit;
                         }
                         const uint64_t obase = __shfl_sync(FULL, run, rk & 31u) + pre;
                         if (has && (31 - __clz(grp)) == (int)lane) W.add[rk] = gtot;
@@ -677,9 +699,9 @@ __global__ void __launch_bounds__(kStreamThreads, EMIT ? 2 : 3)
                                 const float az = __fadd_rn(fz, (c0 & 4u) ? 1.0f : 0.0f);
                                 const float bcoord = __fadd_rn(axis == 0 ? fx : (axis == 1 ? fyh : fz),
                                                                (c1 & d) ? 1.0f : 0.0f);
-                                const StreamIso& I = isos[iso_begin + qk];
-                                const float3 v =
-                                    edge_vertex_axis(I.ip, I.f, (float)*sa, (float)*sb, ax, ay, az, axis, bcoord);
+                                const IsoConst& IC = WE->ic[qk];
+                                const float3 v = edge_vertex_axis(IC.f, IC.mc, IC.sc, isos[iso_begin + qk].ip,
+                                                                  (float)*sa, (float)*sb, ax, ay, az, axis, bcoord);
                                 WE->px[j] = v.x;
                                 WE->py[j] = v.y;
                                 WE->pz[j] = v.z;
@@ -707,11 +729,11 @@ __global__ void __launch_bounds__(kStreamThreads, EMIT ? 2 : 3)
                                 const float3 B = make_float3(WE->px[s1], WE->py[s1], WE->pz[s1]);
                                 const float3 C = make_float3(WE->px[s2], WE->py[s2], WE->pz[s2]);
                                 const float3 n = tri_normal(A, B, C);
-                                const StreamIso& I = isos[iso_begin + qk];
-                                float* const pc = I.coords;
-                                if (pc && qo + t < I.cap_tris) {
+                                const IsoConst& IC = WE->ic[qk];
+                                float* const pc = IC.coords;
+                                if (pc && qo + t < IC.cap_tris) {
                                     float* oc = pc + 9 * (qo + t);
-                                    float* on = I.normals + 3 * (qo + t);
+                                    float* on = IC.normals + 3 * (qo + t);
                                     oc[0] = A.x; oc[1] = A.y; oc[2] = A.z;
                                     oc[3] = B.x; oc[4] = B.y; oc[5] = B.z;
                                     oc[6] = C.x; oc[7] = C.y; oc[8] = C.z;
