@@ -123,6 +123,73 @@ __device__ __forceinline__ bool fast_axis(float v0, float v1, float a, float b, 
     return true;
 }
 
+// fast_axis without branches: every step is computed and the result is
+// selected, so independent edges' arithmetic can interleave in one thread.
+// Same accepted results as fast_axis (the cases it returns early on come out
+// as selects; out is meaningless when the result is false).
+__device__ __forceinline__ bool fast_axis_bf(float v0, float v1, float a, float b, const FastIso& f, float& out)
+{
+    float s, e;
+    two_sum(f.ih, -v0, s, e);
+    const float e2 = __fadd_rn(e, f.il);
+    float nh, nl;
+    two_sum(s, e2, nh, nl);
+    const bool at_v0 = nh == 0.0f && nl == 0.0f && f.iso_err == 0.0f;   // iso == v0: r = 0, X = a
+    const float err_num = __fadd_rn(f.iso_err, __fmul_rn(fabsf(e2), 1.1920929e-07f));
+    float dh, dl;
+    two_sum(v1, -v0, dh, dl);
+    const float adh = fabsf(dh);
+    const bool den_ok = adh >= 8.67361738e-19f && adh <= 1.15292150e+18f;   // 2^-60 .. 2^60
+    float inv;
+    asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(inv) : "f"(dh));
+    const float q1 = __fmul_rn(nh, inv);
+    const float p = __fmul_rn(q1, dh);
+    const float pe = __fmaf_rn(q1, dh, -p);
+    const float p2 = __fmul_rn(q1, dl);
+    const float pe2 = __fmaf_rn(q1, dl, -p2);
+    const float rho = __fsub_rn(__fadd_rn(__fsub_rn(__fsub_rn(nh, p), pe), __fsub_rn(nl, p2)), pe2);
+    const float q2 = __fmul_rn(rho, inv);
+    const float aq = fabsf(q1);
+    const bool up = b > a;
+    const float dq1 = up ? q1 : -q1, dq2 = up ? q2 : -q2;
+    float ya, yb;
+    two_sum(a, dq1, ya, yb);
+    const float yb2 = __fadd_rn(yb, dq2);
+    float yh, yl;
+    two_sum(ya, yb2, yh, yl);
+    const float m = fmaxf(a, b);
+    float E = __fmul_rn(aq, 9.09494702e-13f);
+    E = __fadd_rn(E, __fmul_rn(__fmul_rn(err_num, fabsf(inv)), 1.0001f));
+    E = __fadd_rn(E, __fmul_rn(fabsf(yb2), 1.1920929e-07f));
+    E = __fadd_rn(E, __fmul_rn(__fadd_rn(m, 1.0f), 8.8817842e-16f));
+    E = __fmul_rn(E, 1.001f);
+    const float nb = __int_as_float(__float_as_int(yh) + (yl >= 0.0f ? 1 : -1));
+    const float dist = __fsub_rn(__fmul_rn(fabsf(__fsub_rn(nb, yh)), 0.5f), fabsf(yl));
+    const bool pos_ok = yh > 0.0f && yh < 3.0e7f && dist > E;
+    const bool zero_ok = yh == 0.0f && yl == 0.0f && E < 1.0e-30f;
+    const bool ok = at_v0 || (den_ok && aq <= 1.5f && (pos_ok || zero_ok));
+    out = at_v0 ? a : (zero_ok ? 0.0f : yh);
+    return ok;
+}
+
+// The fast path of edge_vertex_axis without branches: the vertex, and
+// whether it is certain (false: run edge_vertex_axis for this edge).
+__device__ __forceinline__ bool edge_vertex_axis_try(const FastIso& f, const float* min_coord, const float* scale,
+                                                     float va, float vb, float ax, float ay, float az, int axis,
+                                                     float b, float3& o)
+{
+    const float a = axis == 0 ? ax : (axis == 1 ? ay : az);
+    const float v0 = clampf_ref(va, f.vmin_f, f.vmax_f);
+    const float v1 = clampf_ref(vb, f.vmin_f, f.vmax_f);
+    float r;
+    const bool ok = fast_axis_bf(v0, v1, a, b, f, r) && f.fast_ok != 0 && ((v0 > f.f_thr) != (v1 > f.f_thr));
+    const float px = axis == 0 ? r : ax, py = axis == 1 ? r : ay, pz = axis == 2 ? r : az;
+    o.x = __fmul_rn(__fadd_rn(px, min_coord[0]), scale[0]);
+    o.y = __fmul_rn(__fadd_rn(py, min_coord[1]), scale[1]);
+    o.z = __fmul_rn(__fadd_rn(pz, min_coord[2]), scale[2]);
+    return ok;
+}
+
 // The FP64 sequence, kept out of line: it runs for about one vertex in 10^5
 // and would otherwise hold FP64 registers in the hot loop.
 static __device__ __noinline__ float3 interpolate_exact_slow(const Interp& j, float va, float vb, float ax, float ay,

@@ -36,6 +36,10 @@
 #include "mc_internal.h"
 #include "mc_interp.cuh"
 
+#ifndef KVSMC_VERTS_PER_LANE
+#define KVSMC_VERTS_PER_LANE 1
+#endif
+
 namespace kvsmc {
 
 namespace {
@@ -156,6 +160,7 @@ constexpr int kLut = kStreamBuckets + 1;   // bucket indices 0 .. kStreamBuckets
 constexpr uint32_t kMultiThr = 1u << 31;   // LUT flag: two or more thresholds lie in this bucket
 constexpr int kMaxVerts = 256;             // vertex items of one round (rounds end before it is exceeded)
 constexpr int kMaxTris = 32 * 5;           // triangle items of one round (5 per pair at most)
+constexpr int kVertsPerLane = KVSMC_VERTS_PER_LANE;   // vertex items per lane per pass
 
 // Per-CTA tables, indexed by the corner code of case_code() (not by the
 // reference's case number: the code -> case permutation is applied when the
@@ -194,6 +199,8 @@ struct IsoConst {
 
 struct WarpEmit {
     IsoConst ic[kStreamMaxIso];
+    uint32_t pairs_round[32];   // this round's pair entry and vertex base per lane
+    uint32_t vpre_round[32];
     uint32_t pairs[kPairCap];
     float px[kMaxVerts], py[kMaxVerts], pz[kMaxVerts];
     uint8_t item_v[kMaxVerts];
@@ -669,22 +676,29 @@ __global__ void __launch_bounds__(kStreamThreads, EMIT ? 2 : 3)
                         const uint64_t obase = __shfl_sync(FULL, run, rk & 31u) + pre;
                         if (has && (31 - __clz(grp)) == (int)lane) W.add[rk] = gtot;
                         // item -> pair maps of this round
+                        WE->pairs_round[lane] = pe;
+                        WE->vpre_round[lane] = vpre;
                         for (uint32_t r = 0; r < ne; ++r) WE->item_v[vpre + r] = (uint8_t)lane;
                         for (uint32_t t = 0; t < nt; ++t) WE->item_t[tpre + t] = (uint8_t)lane;
                         __syncwarp();
                         run += W.add[lane];
                         W.add[lane] = 0;
-                        // ---- vertices: one (pair, used edge) per lane, edges in increasing order
-                        for (uint32_t j0 = 0; j0 < nv; j0 += 32) {
-                            const uint32_t j = j0 + lane;
-                            const bool hv = j < nv;
-                            const uint32_t q = hv ? WE->item_v[j] : 0u;
-                            const uint32_t qe = __shfl_sync(FULL, pe, q);
-                            const uint32_t qv = __shfl_sync(FULL, vpre, q);
-                            if (hv) {
+                        // ---- vertices: one (pair, used edge) per lane, edges in increasing order;
+                        // kVertsPerLane items per lane per pass, their arithmetic branch-free so
+                        // it interleaves; an edge the FP32 path cannot certify (rare) takes the
+                        // exact FP64 sequence afterwards
+                        for (uint32_t j0 = 0; j0 < nv; j0 += 32 * kVertsPerLane) {
+                            uint32_t fail = 0;   // bit u: item u of this lane needs the FP64 path
+#pragma unroll
+                            for (int u = 0; u < kVertsPerLane; ++u) {
+                                const uint32_t j = j0 + 32 * u + lane;
+                                const bool hv = j < nv;
+                                const uint32_t q = hv ? WE->item_v[j] : 0u;
+                                const uint32_t qe = __shfl_sync(FULL, pe, q);
+                                const uint32_t qv = __shfl_sync(FULL, vpre, q);
                                 const uint32_t qh = (qe & 0xffu) >> SEG_SHIFT, cell = qe & (SEG - 1);
                                 const uint32_t qk = (qe >> 8) & 0xffu, qc = qe >> 16;
-                                const uint32_t e = (uint32_t)(TB.edge_list[qc] >> (4 * (j - qv))) & 15u;
+                                const uint32_t e = (uint32_t)(TB.edge_list[qc] >> (4 * ((j - qv) & 15u))) & 15u;
                                 const unsigned ep = TB.edge_packed[e];
                                 const unsigned c0 = ep & 7u, c1 = ep >> 3;
                                 const T* sa = ((c0 >> 2) ? pb : pa) + (qh + ((c0 >> 1) & 1u)) * row_elems + cell + (c0 & 1u);
@@ -700,11 +714,45 @@ __global__ void __launch_bounds__(kStreamThreads, EMIT ? 2 : 3)
                                 const float bcoord = __fadd_rn(axis == 0 ? fx : (axis == 1 ? fyh : fz),
                                                                (c1 & d) ? 1.0f : 0.0f);
                                 const IsoConst& IC = WE->ic[qk];
-                                const float3 v = edge_vertex_axis(IC.f, IC.mc, IC.sc, isos[iso_begin + qk].ip,
-                                                                  (float)*sa, (float)*sb, ax, ay, az, axis, bcoord);
-                                WE->px[j] = v.x;
-                                WE->py[j] = v.y;
-                                WE->pz[j] = v.z;
+                                float3 v;
+                                const bool ok = edge_vertex_axis_try(IC.f, IC.mc, IC.sc, (float)*sa, (float)*sb, ax,
+                                                                     ay, az, axis, bcoord, v);
+                                if (hv) {
+                                    WE->px[j] = v.x;
+                                    WE->py[j] = v.y;
+                                    WE->pz[j] = v.z;
+                                    if (!ok) fail |= 1u << u;
+                                }
+                            }
+                            if (__any_sync(FULL, fail != 0)) {
+                                for (int u = 0; u < kVertsPerLane; ++u) {
+                                    if (!((fail >> u) & 1u)) continue;
+                                    const uint32_t j = j0 + 32 * u + lane;
+                                    const uint32_t q = WE->item_v[j];
+                                    const uint32_t qe = WE->pairs_round[q], qv = WE->vpre_round[q];
+                                    const uint32_t qh = (qe & 0xffu) >> SEG_SHIFT, cell = qe & (SEG - 1);
+                                    const uint32_t qk = (qe >> 8) & 0xffu, qc = qe >> 16;
+                                    const uint32_t e = (uint32_t)(TB.edge_list[qc] >> (4 * (j - qv))) & 15u;
+                                    const unsigned ep = TB.edge_packed[e];
+                                    const unsigned c0 = ep & 7u, c1 = ep >> 3;
+                                    const T* sa = ((c0 >> 2) ? pb : pa) + (qh + ((c0 >> 1) & 1u)) * row_elems + cell + (c0 & 1u);
+                                    const T* sb = ((c1 >> 2) ? pb : pa) + (qh + ((c1 >> 1) & 1u)) * row_elems + cell + (c1 & 1u);
+                                    const unsigned d = c0 ^ c1;
+                                    const int axis = d == 1u ? 0 : (d == 2u ? 1 : 2);
+                                    const float fx = __uint2float_rn((uint32_t)xoff + cell);
+                                    const float fyh = __fadd_rn(fy, qh ? 1.0f : 0.0f);
+                                    const float ax = __fadd_rn(fx, (c0 & 1u) ? 1.0f : 0.0f);
+                                    const float ay = __fadd_rn(fyh, (c0 & 2u) ? 1.0f : 0.0f);
+                                    const float az = __fadd_rn(fz, (c0 & 4u) ? 1.0f : 0.0f);
+                                    const float bcoord = __fadd_rn(axis == 0 ? fx : (axis == 1 ? fyh : fz),
+                                                                   (c1 & d) ? 1.0f : 0.0f);
+                                    const IsoConst& IC = WE->ic[qk];
+                                    const float3 v = edge_vertex_axis(IC.f, IC.mc, IC.sc, isos[iso_begin + qk].ip,
+                                                                      (float)*sa, (float)*sb, ax, ay, az, axis, bcoord);
+                                    WE->px[j] = v.x;
+                                    WE->py[j] = v.y;
+                                    WE->pz[j] = v.z;
+                                }
                             }
                         }
                         __syncwarp();
