@@ -173,17 +173,6 @@ struct Tables {
     uint8_t edge_packed[16];
 };
 
-// A pair entry: warp cell [0,8) | isolevel [8,16) | corner code [16,24) |
-// distance back to the pair of the same isolevel in the cell to the left
-// [24,30) (0: none in this warp) | bit 30: that pair is in this round, so
-// this pair takes its x = 0 face z-edges (8 and 11) from it.  Those are the
-// left cell's edges 9 and 10, walked in the same direction (z increasing),
-// so the interpolation is the same arithmetic and the bits are identical.
-constexpr uint32_t kDelegEdges = (1u << 8) | (1u << 11);
-__device__ __forceinline__ uint32_t pe_code(uint32_t pe) { return (pe >> 16) & 0xffu; }
-__device__ __forceinline__ uint32_t pe_dist(uint32_t pe) { return (pe >> 24) & 63u; }
-__device__ __forceinline__ bool pe_deleg(uint32_t pe) { return (pe >> 30) & 1u; }
-
 // Per-warp state.
 struct WarpState {
     uint64_t bar[3];
@@ -217,24 +206,6 @@ struct WarpEmit {
     uint8_t item_v[kMaxVerts];
     uint8_t item_t[kMaxTris];
 };
-
-// The edges whose vertices a pair computes itself (its used edges less the
-// delegated ones), and the r-th of them in increasing order.
-__device__ __forceinline__ uint32_t own_edges(const Tables& TB, uint32_t pe)
-{
-    return TB.edge_mask[pe_code(pe)] & (pe_deleg(pe) ? ~kDelegEdges : 0xfffu);
-}
-__device__ __forceinline__ uint32_t own_edge(const Tables& TB, uint32_t pe, uint32_t r)
-{
-    const uint32_t code = pe_code(pe), em = TB.edge_mask[code];
-    uint32_t idx = r;
-    if (pe_deleg(pe)) {
-        // skip 8 and 11 in the list of used edges (8 comes first)
-        if (((em >> 8) & 1u) && idx >= (uint32_t)__popc(em & 0xffu)) ++idx;
-        if (((em >> 11) & 1u) && idx >= (uint32_t)__popc(em & 0x7ffu)) ++idx;
-    }
-    return (uint32_t)(TB.edge_list[code] >> (4 * (idx & 15u))) & 15u;
-}
 
 __host__ __device__ __forceinline__ size_t align128(size_t v) { return (v + 127) / 128 * 128; }
 
@@ -645,7 +616,6 @@ __global__ void __launch_bounds__(kStreamThreads, EMIT ? 2 : 3)
                 }
                 const uint32_t my_first = inc - m;
                 uint32_t* pbuf = WE->pairs;
-                const uint32_t prev7 = __shfl_up_sync(FULL, act[3] >> 16, 1);   // the left lane's last cell
                 for (uint32_t fill0 = 0; fill0 < npairs; fill0 += kPairCap) {
                     // this lane's pairs (cell order, then isolevel) that fall into
                     // [fill0, fill0 + kPairCap): warp cell | isolevel << 8 | code << 16
@@ -658,22 +628,12 @@ __global__ void __launch_bounds__(kStreamThreads, EMIT ? 2 : 3)
                             if (am) {
                                 const uint32_t w0 = cell_word(PA0, i), w1 = cell_word(PA1, i);
                                 const uint32_t w2 = cell_word(PB0, i), w3 = cell_word(PB1, i);
-                                const uint32_t am0 = am;
-                                // the cell to the left (none at the start of a row segment)
-                                const bool row_start = i == 0 && (lane % LPR) == 0;
-                                const uint32_t am_left =
-                                    i == 0 ? (row_start ? 0u : prev7)
-                                           : (act[(i - 1) >> 1] >> (16 * ((i - 1) & 1))) & 0xffffu;
                                 do {
                                     const uint32_t k = __ffs(am) - 1;
                                     am &= am - 1;
-                                    const uint32_t below = (1u << k) - 1u;
-                                    const uint32_t d = ((am_left >> k) & 1u)
-                                                           ? (uint32_t)(__popc(am_left & ~below) + __popc(am0 & below))
-                                                           : 0u;
                                     if (slot >= fill0 && slot < fill0 + kPairCap)
                                         pbuf[slot - fill0] = (lane * kLaneCells + i) | (k << 8) |
-                                                             (case_code(w0, w1, w2, w3, k) << 16) | (d << 24);
+                                                             (case_code(w0, w1, w2, w3, k) << 16);
                                     ++slot;
                                 } while (am);
                             }
@@ -685,11 +645,8 @@ __global__ void __launch_bounds__(kStreamThreads, EMIT ? 2 : 3)
                         // ---- one pair per lane, as many as the vertex pool holds
                         const uint32_t p = r0 + lane;
                         bool has = p < nfill;
-                        uint32_t pe0 = has ? pbuf[p] : 0u;
-                        // the left cell's pair of the same isolevel is in this round: take its edges
-                        const uint32_t dd = pe_dist(pe0);
-                        if (dd != 0 && dd <= lane) pe0 |= 1u << 30;
-                        const uint32_t ne0 = has ? (uint32_t)__popc(own_edges(TB, pe0)) : 0u;
+                        const uint32_t pe0 = has ? pbuf[p] : 0u;
+                        const uint32_t ne0 = has ? (uint32_t)__popc(TB.edge_mask[pe0 >> 16]) : 0u;
                         uint32_t vpre = 0;
 #pragma unroll
                         for (int bit = 0; bit < 4; ++bit)
@@ -698,7 +655,7 @@ __global__ void __launch_bounds__(kStreamThreads, EMIT ? 2 : 3)
                         taken = (uint32_t)__popc(__ballot_sync(FULL, has));
                         const uint32_t nv = __shfl_sync(FULL, vpre + ne0, taken - 1);
                         const uint32_t pe = has ? pe0 : 0u;
-                        const uint32_t k = (pe >> 8) & 0xffu, code = pe_code(pe);
+                        const uint32_t k = (pe >> 8) & 0xffu, code = pe >> 16;
                         const uint32_t rk = ((pe & 0xffu) >> SEG_SHIFT) * 16 + k;   // (row, isolevel) slot
                         const uint32_t nt = has ? TB.ntri[code] : 0u;
                         const uint32_t ne = has ? ne0 : 0u;
@@ -740,8 +697,8 @@ __global__ void __launch_bounds__(kStreamThreads, EMIT ? 2 : 3)
                                 const uint32_t qe = __shfl_sync(FULL, pe, q);
                                 const uint32_t qv = __shfl_sync(FULL, vpre, q);
                                 const uint32_t qh = (qe & 0xffu) >> SEG_SHIFT, cell = qe & (SEG - 1);
-                                const uint32_t qk = (qe >> 8) & 0xffu;
-                                const uint32_t e = own_edge(TB, qe, j - qv);
+                                const uint32_t qk = (qe >> 8) & 0xffu, qc = qe >> 16;
+                                const uint32_t e = (uint32_t)(TB.edge_list[qc] >> (4 * ((j - qv) & 15u))) & 15u;
                                 const unsigned ep = TB.edge_packed[e];
                                 const unsigned c0 = ep & 7u, c1 = ep >> 3;
                                 const T* sa = ((c0 >> 2) ? pb : pa) + (qh + ((c0 >> 1) & 1u)) * row_elems + cell + (c0 & 1u);
@@ -774,8 +731,8 @@ __global__ void __launch_bounds__(kStreamThreads, EMIT ? 2 : 3)
                                     const uint32_t q = WE->item_v[j];
                                     const uint32_t qe = WE->pairs_round[q], qv = WE->vpre_round[q];
                                     const uint32_t qh = (qe & 0xffu) >> SEG_SHIFT, cell = qe & (SEG - 1);
-                                    const uint32_t qk = (qe >> 8) & 0xffu;
-                                    const uint32_t e = own_edge(TB, qe, j - qv);
+                                    const uint32_t qk = (qe >> 8) & 0xffu, qc = qe >> 16;
+                                    const uint32_t e = (uint32_t)(TB.edge_list[qc] >> (4 * (j - qv))) & 15u;
                                     const unsigned ep = TB.edge_packed[e];
                                     const unsigned c0 = ep & 7u, c1 = ep >> 3;
                                     const T* sa = ((c0 >> 2) ? pb : pa) + (qh + ((c0 >> 1) & 1u)) * row_elems + cell + (c0 & 1u);
@@ -809,22 +766,13 @@ __global__ void __launch_bounds__(kStreamThreads, EMIT ? 2 : 3)
                             const uint32_t qt = __shfl_sync(FULL, tpre, q);
                             const uint64_t qo = __shfl_sync(FULL, obase, q);
                             if (ht) {
-                                const uint32_t qk = (qe >> 8) & 0xffu, qc = pe_code(qe);
+                                const uint32_t qk = (qe >> 8) & 0xffu, qc = qe >> 16;
                                 const uint32_t t = j - qt;
-                                const uint32_t emq = own_edges(TB, qe);
+                                const uint32_t emq = TB.edge_mask[qc];
                                 const uint32_t pk = (uint32_t)(TB.tri_packed[qc] >> (12 * t));
-                                // a vertex's pool slot: its own, or (edges 8, 11 delegated) the
-                                // left pair's edge 9 / 10
-                                auto slot_of = [&](uint32_t ev) -> uint32_t {
-                                    if ((emq >> ev) & 1u) return qv + __popc(emq & ((1u << ev) - 1u));
-                                    const uint32_t q2 = q - pe_dist(qe);
-                                    const uint32_t pe2 = WE->pairs_round[q2];
-                                    const uint32_t e2 = ev == 8u ? 9u : 10u;
-                                    return WE->vpre_round[q2] + __popc(own_edges(TB, pe2) & ((1u << e2) - 1u));
-                                };
-                                const uint32_t s0 = slot_of(pk & 15u);
-                                const uint32_t s1 = slot_of((pk >> 4) & 15u);
-                                const uint32_t s2 = slot_of((pk >> 8) & 15u);
+                                const uint32_t s0 = qv + __popc(emq & ((1u << (pk & 15u)) - 1u));
+                                const uint32_t s1 = qv + __popc(emq & ((1u << ((pk >> 4) & 15u)) - 1u));
+                                const uint32_t s2 = qv + __popc(emq & ((1u << ((pk >> 8) & 15u)) - 1u));
                                 const float3 A = make_float3(WE->px[s0], WE->py[s0], WE->pz[s0]);
                                 const float3 B = make_float3(WE->px[s1], WE->py[s1], WE->pz[s1]);
                                 const float3 C = make_float3(WE->px[s2], WE->py[s2], WE->pz[s2]);
