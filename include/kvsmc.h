@@ -311,6 +311,68 @@ kvsmc_status kvsmc_extract_noalloc(const void* d_values, kvsmc_dtype dtype, uint
                                    uint64_t coords_capacity, float* d_normals, uint64_t normals_capacity,
                                    void* cuda_stream, kvsmc_sizes* sizes);
 
+/* ------------------------------------------------------------- autotuning */
+
+/* Launch shape of the streaming kernels for one (value type, volume size
+ * class).  Every field 0 = the built-in rule for that field.  Results are
+ * identical under every shape; only the speed differs.  The reference has one
+ * CPU loop and nothing to tune. */
+typedef struct kvsmc_tune_choice {
+    int32_t rows;          /* cell rows per warp task: 1 (256-cell row segments) or 2 (two 128-cell rows) */
+    int32_t tasks_per_sm;  /* warp tasks per SM a launch is cut into (sets cell planes per task, 4..64) */
+    int32_t ctas_per_sm;   /* resident CTAs per SM of the persistent launches (capped by what fits) */
+    int32_t scan_threads;  /* unit-scan tile: 64, 128 or 256 units per CTA pass */
+} kvsmc_tune_choice;
+
+/* One row of a tuning table. */
+typedef struct kvsmc_tune_entry {
+    int32_t dtype;            /* kvsmc_dtype */
+    int32_t size_class;       /* kvsmc_size_class() of the volumes it applies to */
+    kvsmc_tune_choice choice;
+    double tuned_ms;          /* measured count + emit time of the choice (0: not measured) */
+    double default_ms;        /* measured time of the built-in rule on the same work */
+} kvsmc_tune_entry;
+
+#define KVSMC_SIZE_CLASSES 5
+
+/* Size class of a volume by its cell count C = (nx-1)(ny-1)(nz-1):
+ * 0: C < 2^18, 1: < 2^21, 2: < 2^24, 3: < 2^27, 4: larger. */
+int32_t kvsmc_size_class(uint32_t nx, uint32_t ny, uint32_t nz);
+
+/* The launch shape a streaming batch uses for a volume, given a tuning table
+ * (NULL / 0 rows: built-in rules): the entry for (dtype, size class) with
+ * its zero fields filled by the built-in rules.  Pure host function.
+ * KVSMC_ERR_INVALID_ARGUMENT when a table entry holds an invalid value. */
+kvsmc_status kvsmc_tune_resolve(const kvsmc_tune_entry* table, int32_t n, kvsmc_dtype dtype, uint32_t nx,
+                                uint32_t ny, uint32_t nz, kvsmc_tune_choice* out);
+
+/* Install a tuning table on a context (copied; n = 0 clears it).  Every
+ * later streaming batch, plan and server round of the context follows it. */
+kvsmc_status kvsmc_tuning_set(kvsmc_context* ctx, const kvsmc_tune_entry* table, int32_t n);
+/* Copy out the installed table; returns its length (fills at most cap rows). */
+int32_t kvsmc_tuning_get(const kvsmc_context* ctx, kvsmc_tune_entry* out, int32_t cap);
+/* Use one launch shape for every volume (NULL: back to the table). */
+kvsmc_status kvsmc_tuning_force(kvsmc_context* ctx, const kvsmc_tune_choice* choice);
+
+typedef struct kvsmc_autotune_config {
+    const int32_t* dtypes;    /* value types to tune (NULL: uint8, uint16, float32, int8, int16) */
+    int32_t ndtypes;
+    int32_t max_class;        /* tune size classes 0 .. max_class (<= 4) */
+    int32_t isovalues;        /* isovalues per batch on the tuning volumes (1..16) */
+    int32_t reps;             /* timed runs per candidate; the median counts */
+    uint64_t seed;            /* seed of the synthetic tuning volumes */
+} kvsmc_autotune_config;
+
+/* The autotuner: for every (dtype, size class) asked for, build a seeded
+ * synthetic volume of that class on the device, time count + emit of a
+ * batch of isovalues under candidate launch shapes (coordinate descent over
+ * rows x tasks per SM, then CTAs per SM, then the scan tile), and keep a
+ * shape only where it beats the built-in rules by more than 3 %.  Installs
+ * the table on the context and copies it to out (at most cap rows, *nout
+ * rows written).  Takes seconds; allocates and frees its own buffers. */
+kvsmc_status kvsmc_autotune(kvsmc_context* ctx, const kvsmc_autotune_config* cfg, kvsmc_tune_entry* out,
+                            int32_t cap, int32_t* nout);
+
 /* ------------------------------------------------------------ diagnostics */
 
 /* Per-kernel timing: with profiling on, every kernel family launched by this

@@ -44,6 +44,8 @@ EXPORTS = [
     "kvsmc_plan_create", "kvsmc_plan_launch", "kvsmc_plan_wait", "kvsmc_plan_kernels", "kvsmc_plan_destroy",
     "kvsmc_server_create", "kvsmc_server_submit", "kvsmc_server_poll", "kvsmc_server_release",
     "kvsmc_server_stats", "kvsmc_server_destroy", "kvsmc_copy_to_host",
+    "kvsmc_size_class", "kvsmc_tune_resolve", "kvsmc_tuning_set", "kvsmc_tuning_get",
+    "kvsmc_tuning_force", "kvsmc_autotune",
 ]
 
 PATH_AUTO = 0      # streaming kernels where eligible
@@ -88,6 +90,23 @@ class Request(C.Structure):
                 ("d_connections", C.c_void_p), ("connections_capacity", C.c_uint64),
                 ("sizes", Sizes), ("status", C.c_int)]
 
+
+class TuneChoice(C.Structure):
+    _fields_ = [("rows", C.c_int32), ("tasks_per_sm", C.c_int32), ("ctas_per_sm", C.c_int32),
+                ("scan_threads", C.c_int32)]
+
+
+class TuneEntry(C.Structure):
+    _fields_ = [("dtype", C.c_int32), ("size_class", C.c_int32), ("choice", TuneChoice),
+                ("tuned_ms", C.c_double), ("default_ms", C.c_double)]
+
+
+class AutotuneConfig(C.Structure):
+    _fields_ = [("dtypes", C.POINTER(C.c_int32)), ("ndtypes", C.c_int32), ("max_class", C.c_int32),
+                ("isovalues", C.c_int32), ("reps", C.c_int32), ("seed", C.c_uint64)]
+
+
+SIZE_CLASSES = 5
 
 HOST_ALLOC = C.CFUNCTYPE(C.c_void_p, C.c_void_p, C.c_int32, C.c_uint64)
 
@@ -150,6 +169,13 @@ def load(path=LIB_PATH):
         "kvsmc_plan_wait": (C.c_int, [vp, C.POINTER(Request), i32]),
         "kvsmc_plan_kernels": (u64, [vp]),
         "kvsmc_plan_destroy": (None, [vp]),
+        "kvsmc_size_class": (i32, [u32, u32, u32]),
+        "kvsmc_tune_resolve": (C.c_int, [C.POINTER(TuneEntry), i32, C.c_int, u32, u32, u32,
+                                         C.POINTER(TuneChoice)]),
+        "kvsmc_tuning_set": (C.c_int, [vp, C.POINTER(TuneEntry), i32]),
+        "kvsmc_tuning_get": (i32, [vp, C.POINTER(TuneEntry), i32]),
+        "kvsmc_tuning_force": (C.c_int, [vp, C.POINTER(TuneChoice)]),
+        "kvsmc_autotune": (C.c_int, [vp, C.POINTER(AutotuneConfig), C.POINTER(TuneEntry), i32, C.POINTER(i32)]),
         "kvsmc_profile_enable": (C.c_int, [vp, i32]),
         "kvsmc_profile_read": (i32, [vp, i32, C.POINTER(C.c_char_p), C.POINTER(u64), C.POINTER(C.c_double)]),
     }

@@ -129,8 +129,7 @@ kvsmc_status volume_bricks(kvsmc_context* ctx, kvsmc_volume* v)
     const bool ok = (dt == KVSMC_I8 || dt == KVSMC_I16 || dt == KVSMC_U8 || dt == KVSMC_U16 || dt == KVSMC_F32) &&
                     v->view.nx - 1 <= (uint32_t)kvsmc::kStreamMaxCells;
     if (!ok) return KVSMC_OK;
-    const int rows = stream_rows(v->view.nx - 1);
-    const size_t bytes = kvsmc::brick_count(v->view, rows) * sizeof(float2);
+    const size_t bytes = kvsmc::brick_count(v->view) * sizeof(float2);
     if (bytes > v->brick_bytes) {
         if (v->bricks) cudaFree(v->bricks);
         v->bricks = nullptr;
@@ -138,8 +137,7 @@ kvsmc_status volume_bricks(kvsmc_context* ctx, kvsmc_volume* v)
         KVSMC_CUDA(ctx, cudaMalloc(&v->bricks, bytes));
         v->brick_bytes = bytes;
     }
-    KVSMC_CUDA(ctx, kvsmc::launch_bricks(v->view, rows, v->bricks, launch_of(ctx)));
-    v->brick_rows = rows;
+    KVSMC_CUDA(ctx, kvsmc::launch_bricks(v->view, v->bricks, launch_of(ctx)));
     v->bricks_valid = true;
     return KVSMC_OK;
 }

@@ -89,9 +89,26 @@ int stream_rows(uint32_t cx)
     return w2 < w1 ? 2 : 1;
 }
 
-uint32_t stream_zchunk(uint64_t warp_steps, int num_sms)
+kvsmc_tune_choice stream_shape(const kvsmc_context* ctx, const kvsmc::VolumeView& v)
 {
-    const uint64_t want_tasks = (uint64_t)num_sms * 24 * 4;
+    kvsmc_tune_choice c{};
+    if (ctx->tune_forced) {
+        c = ctx->tune_force;
+        kvsmc_tune_entry e{};
+        e.choice = c;
+        e.dtype = v.dtype;
+        e.size_class = kvsmc_size_class(v.nx, v.ny, v.nz);
+        if (kvsmc_tune_resolve(&e, 1, (kvsmc_dtype)v.dtype, v.nx, v.ny, v.nz, &c) == KVSMC_OK) return c;
+    }
+    if (kvsmc_tune_resolve(ctx->tuning.data(), (int32_t)ctx->tuning.size(), (kvsmc_dtype)v.dtype, v.nx, v.ny, v.nz,
+                           &c) != KVSMC_OK)
+        kvsmc_tune_resolve(nullptr, 0, (kvsmc_dtype)v.dtype, v.nx, v.ny, v.nz, &c);
+    return c;
+}
+
+uint32_t stream_zchunk(uint64_t warp_steps, int num_sms, int tasks_per_sm)
+{
+    const uint64_t want_tasks = (uint64_t)num_sms * (uint64_t)(tasks_per_sm > 0 ? tasks_per_sm : kDefaultTasksPerSm);
     uint64_t zc = (warp_steps + want_tasks - 1) / want_tasks;
     if (zc < 4) zc = 4;
     if (zc > 64) zc = 64;
@@ -110,7 +127,8 @@ bool stream_eligible(const kvsmc_context* ctx, const Item& it)
     if ((double)(v.nx - 1) * (double)(v.ny - 1) * 5.0 >= 4294967295.0) return false;
     const double iso = it.params.isolevel;
     if (!std::isfinite(iso) || std::fabs(iso) > 1.0e30) return false;
-    return kvsmc::stream_shared_bytes(v.dtype, true, stream_rows(v.nx - 1)) <= (size_t)227 * 1024;
+    return kvsmc::stream_shared_bytes(v.dtype, true, 1) <= (size_t)227 * 1024 &&
+           kvsmc::stream_shared_bytes(v.dtype, true, 2) <= (size_t)227 * 1024;
 }
 
 void StreamBatch::plan_tables()
@@ -127,12 +145,20 @@ void StreamBatch::plan_tables()
         }
         lists[f->second].push_back(it);
     }
-    // one launch per (value type, rows per warp) present
+    // one launch per (value type, rows per warp) present; the launch shape
+    // of each volume from the context's tuning
     std::vector<std::pair<int, int>> kinds;
-    auto kind_of = [](const std::vector<Item*>& l) {
-        const kvsmc::VolumeView& v = l[0]->vol->view;
-        return std::make_pair((int)v.dtype, stream_rows(v.nx - 1));
+    std::map<const kvsmc_volume*, kvsmc_tune_choice> shape;
+    for (auto& l : lists) shape[l[0]->vol] = stream_shape(ctx, l[0]->vol->view);
+    auto kind_of = [&](const std::vector<Item*>& l) {
+        return std::make_pair((int)l[0]->vol->view.dtype, (int)shape[l[0]->vol].rows);
     };
+    // the largest volume (in cells) decides the launch-wide fields
+    auto cells_of = [](const kvsmc::VolumeView& v) { return (uint64_t)(v.nx - 1) * (v.ny - 1) * (v.nz - 1); };
+    const kvsmc_volume* largest = nullptr;
+    for (auto& l : lists)
+        if (!largest || cells_of(l[0]->vol->view) > cells_of(largest->view)) largest = l[0]->vol;
+    scan_threads = largest ? shape[largest].scan_threads : 256;
     for (auto& l : lists)
         if (std::find(kinds.begin(), kinds.end(), kind_of(l)) == kinds.end()) kinds.push_back(kind_of(l));
     groups.clear();
@@ -152,12 +178,16 @@ void StreamBatch::plan_tables()
         // one z-chunk for the whole launch: sized by all its warp steps, so a
         // batch of small volumes gets long tasks rather than many short ones
         uint64_t steps = 0;
+        const kvsmc_volume* big = nullptr;
         for (auto& l : lists) {
             if (kind_of(l) != kd) continue;
             const kvsmc::VolumeView& v = l[0]->vol->view;
             steps += (uint64_t)(v.nz - 1) * ((v.ny - 1 + rows - 1) / rows) * segments_per_row(v, rows);
+            if (!big || cells_of(v) > cells_of(big->view)) big = l[0]->vol;
         }
-        const uint32_t zchunk = stream_zchunk(steps, ctx->num_sms);
+        const kvsmc_tune_choice& bs_shape = shape[big];
+        L.ctas_per_sm = bs_shape.ctas_per_sm;
+        const uint32_t zchunk = stream_zchunk(steps, ctx->num_sms, bs_shape.tasks_per_sm);
         for (auto& l : lists) {
             if (kind_of(l) != kd) continue;
             const kvsmc::VolumeView v = l[0]->vol->view;
@@ -166,7 +196,8 @@ void StreamBatch::plan_tables()
             g.vol = v;
             g.rows = (uint32_t)rows;
             const kvsmc_volume* vol = l[0]->vol;
-            g.bricks = (vol->bricks_valid && vol->brick_rows == rows) ? vol->bricks : nullptr;
+            g.bricks = vol->bricks_valid ? vol->bricks : nullptr;
+            g.brick_wpr = (v.nx - 1 + kvsmc::kBrickCells - 1) / kvsmc::kBrickCells;
             g.wpr = segments_per_row(v, rows);
             g.zchunk = zchunk;
             const uint32_t cy = v.ny - 1, cz = v.nz - 1;
@@ -271,10 +302,10 @@ kvsmc_status StreamBatch::count()
         kvsmc::Launch Li = L;
         Li.stream = st;
         return kvsmc::launch_stream(false, l.dtype, l.rows, d_groups + l.g0, l.ng, l.ntasks, d_isos, d_unit_counts,
-                                    nullptr, nullptr, d_status, d_next + 2 * i, Li);
+                                    nullptr, nullptr, d_status, d_next + 2 * i, Li, l.ctas_per_sm);
     }));
     KVSMC_CUDA(ctx, kvsmc::launch_unit_scan(d_groups, (int)groups.size(), scan_blocks, d_isos, d_unit_counts,
-                                            d_unit_offsets, d_plane_totals, L));
+                                            d_unit_offsets, d_plane_totals, L, scan_threads));
     KVSMC_CUDA(ctx, kvsmc::launch_scan(d_plane_totals, d_plane_base, iso_planes, d_scan, d_total, L));
     KVSMC_CUDA(ctx, kvsmc::launch_iso_totals(d_isos, (int)isos.size(), d_plane_base, d_total, d_totals, L));
     // read back: status word, then one total per isolevel
@@ -328,7 +359,7 @@ kvsmc_status StreamBatch::emit()
         kvsmc::Launch Li = L;
         Li.stream = st;
         return kvsmc::launch_stream(true, l.dtype, l.rows, d_groups + l.g0, l.ng, l.ntasks, d_isos, d_unit_counts,
-                                    d_unit_offsets, d_plane_base, d_status, d_next + 2 * i + 1, Li);
+                                    d_unit_offsets, d_plane_base, d_status, d_next + 2 * i + 1, Li, l.ctas_per_sm);
     }));
     return KVSMC_OK;
 }

@@ -12,9 +12,10 @@ kvsmc::FastIso make_fast(double iso, double vmin, double vmax, int dtype);
 void bucket_params(float t0, float t1, float& bs, float& bo);
 
 // Cell planes per warp task for a launch of `warp_steps` (row segment, plane)
-// steps in all: enough tasks to fill the GPU, 4 to 64 planes per task (the
-// one-plane halo a task re-reads stays small).
-uint32_t stream_zchunk(uint64_t warp_steps, int num_sms);
+// steps in all: about tasks_per_sm tasks per SM (the built-in rule: 96),
+// 4 to 64 planes per task (the one-plane halo a task re-reads stays small).
+constexpr int kDefaultTasksPerSm = 96;
+uint32_t stream_zchunk(uint64_t warp_steps, int num_sms, int tasks_per_sm = kDefaultTasksPerSm);
 
 // Cell rows per warp task for rows of cx cells: 2 (128-cell segments) when
 // that idles fewer lanes than 256-cell segments, else 1.
@@ -33,6 +34,7 @@ struct StreamBatch {
         int rows;
         int g0, ng;
         uint64_t ntasks;
+        int ctas_per_sm;   // 0: as many as fit
     };
     std::vector<kvsmc::StreamGroup> groups;
     std::vector<kvsmc::StreamIso> isos;
@@ -40,6 +42,7 @@ struct StreamBatch {
     std::vector<Launch1> launches;
     uint64_t unit_elems = 0;     // (unit, isolevel) counters
     uint32_t scan_blocks = 0;    // unit-scan blocks: one per (group, z)
+    int scan_threads = 256;      // unit-scan tile
     uint64_t iso_planes = 0;     // (isolevel, z) planes
 
     kvsmc::StreamGroup* d_groups = nullptr;

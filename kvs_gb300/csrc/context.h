@@ -15,10 +15,9 @@ struct kvsmc_volume {
     bool has_minmax = false;
     double vmin = 0.0, vmax = 0.0;
     // brick min/max table (streaming kernels' empty-space skip), rebuilt after
-    // every copy into a resident volume; valid for brick_rows rows per task
+    // every copy into a resident volume
     float2* bricks = nullptr;
     size_t brick_bytes = 0;
-    int brick_rows = 0;
     bool bricks_valid = false;
 };
 
@@ -45,6 +44,10 @@ struct kvsmc_context {
     cudaEvent_t fork_ev = nullptr;
     cudaEvent_t join_ev[kAux] = {};
     bool aux_ready = false;
+    // streaming launch shapes: the tuning table, or one forced shape
+    std::vector<kvsmc_tune_entry> tuning;
+    bool tune_forced = false;
+    kvsmc_tune_choice tune_force{};
 };
 
 namespace kvsmc {
@@ -107,6 +110,10 @@ cudaError_t fan_out(kvsmc_context* ctx, cudaStream_t origin, size_t n,
 // Decide min/max (MapperBase::setRange, the volume's cache or a preset) and
 // the Math::Equal early exit; fills it.vmin/vmax/extracted and clears sizes.
 kvsmc_status prepare(kvsmc_context* ctx, Item& it);
+
+// The streaming launch shape for a volume under the context's tuning (zero
+// fields resolved by the built-in rules).
+kvsmc_tune_choice stream_shape(const kvsmc_context* ctx, const kvsmc::VolumeView& v);
 
 // Requests the streaming kernels can take (duplicated mode, 8/16-bit and
 // float32 data, finite isolevel, width <= 4096 cells).

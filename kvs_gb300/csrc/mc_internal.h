@@ -77,18 +77,20 @@ struct StreamGroup {
     uint32_t warp_smem_bytes;
     uint32_t warp_smem_offset;
     float bs, bo;            // bucket(v) = floor(kStreamBuckets * sat(v * bs + bo)), in [0, kStreamBuckets]
-    const float2* bricks;    // per brick (8 cell planes x 2 cell rows x one segment) node min/max, or null
+    const float2* bricks;    // the volume's brick min/max table, or null
     int32_t skip_emit;       // 1: no isolevel of the group is written by this emit launch
-    int32_t pad_;
+    uint32_t brick_wpr;      // bricks per row pair (128-cell brick segments per row)
 };
 
-// Brick min/max table of a volume for `rows` cell rows per warp task: one
-// float2 per (8 cell planes, 2 cell rows, one row segment) brick, the min and
-// max of its node box ((-inf, +inf) when it holds a NaN), bricks numbered
-// segment fastest, then row pair, then plane group.
+// Brick min/max table of a volume: one float2 per (8 cell planes, 2 cell
+// rows, 128 cells) brick, the min and max of its node box ((-inf, +inf) when
+// it holds a NaN), bricks numbered segment fastest, then row pair, then plane
+// group.  A two-row warp task covers one brick per plane group, a one-row
+// task (256 cells) two neighbouring bricks; the table serves both.
 constexpr int kBrickPlanes = 8;
-uint64_t brick_count(const VolumeView& v, int rows);
-cudaError_t launch_bricks(const VolumeView& v, int rows, float2* out, const Launch& L);
+constexpr uint32_t kBrickCells = 128;
+uint64_t brick_count(const VolumeView& v);
+cudaError_t launch_bricks(const VolumeView& v, float2* out, const Launch& L);
 
 size_t stream_shared_bytes(int dtype, bool emit, int rows);
 size_t stream_warp_smem_bytes(int dtype, bool emit, int rows);
@@ -96,14 +98,16 @@ size_t stream_warp_smem_offset();
 size_t stream_row_elems(int dtype, int rows);
 // d_next_task: a zeroed u64 per launch (the persistent warps' task counter).
 // d_unit_counts: written by the count launch; read by the emit launch to skip
-// steps without triangles.
+// steps without triangles.  ctas_per_sm: resident CTAs per SM of the
+// persistent grid (0: as many as fit; never more than fit).
 cudaError_t launch_stream(bool emit, int dtype, int rows, const StreamGroup* d_groups, int ngroups, uint64_t ntasks,
                           const StreamIso* d_isos, uint16_t* d_unit_counts, const uint32_t* d_unit_offsets,
                           const uint64_t* d_plane_base, int* d_status, unsigned long long* d_next_task,
-                          const Launch& L);
+                          const Launch& L, int ctas_per_sm = 0);
+// scan_threads: units per CTA pass (64, 128 or 256; 0 = 256).
 cudaError_t launch_unit_scan(const StreamGroup* d_groups, int ngroups, uint32_t nplanes, const StreamIso* d_isos,
                              const uint16_t* d_unit_counts, uint32_t* d_unit_offsets, uint32_t* d_plane_totals,
-                             const Launch& L);
+                             const Launch& L, int scan_threads = 0);
 cudaError_t launch_iso_totals(const StreamIso* d_isos, int n, const uint64_t* d_plane_base, const uint64_t* d_total,
                               uint64_t* d_totals, const Launch& L);
 

@@ -453,7 +453,19 @@ __global__ void __launch_bounds__(kStreamThreads, EMIT ? 2 : 3)
     const float2* bricks = G.bricks;
     const uint32_t nby = (cy + 1) / 2;
     auto brick_empty = [&](uint32_t z) -> bool {
-        const float2 mm = bricks[((uint64_t)(z / kBrickPlanes) * nby + (y >> 1)) * wpr + seg];
+        const float2* row = bricks + ((uint64_t)(z / kBrickPlanes) * nby + (y >> 1)) * G.brick_wpr;
+        float2 mm;
+        if (R == 2) {
+            mm = row[seg];   // a 128-cell segment is one brick
+        } else {
+            const uint32_t b0 = 2 * seg;   // a 256-cell segment spans bricks b0 and b0 + 1
+            mm = row[b0];
+            if (b0 + 1 < G.brick_wpr) {
+                const float2 m1 = row[b0 + 1];
+                mm.x = fminf(mm.x, m1.x);
+                mm.y = fmaxf(mm.y, m1.y);
+            }
+        }
         return value_mask(W, niso, bs, bo, mm.x) == value_mask(W, niso, bs, bo, mm.y);
     };
     if (bricks) {
@@ -861,17 +873,16 @@ __global__ void __launch_bounds__(256)
 // One CTA per (group, z): for every isolevel of the group, the exclusive scan
 // of its unit counts over the plane's units (rows y, segments x) -> u32
 // offsets inside the plane, and the plane's total.  Counts are stored
-// [unit][isolevel]; the plane is walked in tiles of 256 units, each staged
+// [unit][isolevel]; the plane is walked in tiles of NT units, each staged
 // through shared memory with coalesced loads and stores, one unit per thread
 // and all isolevels scanned at once.
-constexpr int kScanUnitThreads = 256;
-
-__global__ void __launch_bounds__(kScanUnitThreads)
+template <int NT>
+__global__ void __launch_bounds__(NT)
     k_unit_scan(const StreamGroup* __restrict__ groups, int ngroups, const StreamIso* __restrict__ isos,
                 const uint16_t* __restrict__ unit_counts, uint32_t* __restrict__ unit_offsets,
                 uint32_t* __restrict__ plane_totals)
 {
-    constexpr int NT = kScanUnitThreads, NW = NT / 32;
+    constexpr int NW = NT / 32;
     __shared__ uint16_t sc[NT * kStreamMaxIso];
     __shared__ uint32_t so[NT * kStreamMaxIso];
     __shared__ uint32_t wsum[NW][kStreamMaxIso];
@@ -974,9 +985,9 @@ size_t stream_shared_bytes(int dtype, bool emit, int rows)
     return stream_warp_smem_offset() + (size_t)kWarps * stream_warp_smem_bytes(dtype, emit, rows);
 }
 
-uint64_t brick_count(const VolumeView& v, int rows)
+uint64_t brick_count(const VolumeView& v)
 {
-    const uint64_t seg = (uint64_t)kSegCells / rows;
+    const uint64_t seg = kBrickCells;
     const uint64_t wpr = (v.nx - 1 + seg - 1) / seg;
     const uint64_t nby = (v.ny - 1 + 1) / 2, nbz = (v.nz - 1 + kBrickPlanes - 1) / kBrickPlanes;
     return wpr * nby * nbz;
@@ -995,7 +1006,7 @@ uint64_t brick_count(const VolumeView& v, int rows)
 cudaError_t launch_stream(bool emit, int dtype, int rows, const StreamGroup* d_groups, int ngroups, uint64_t ntasks,
                           const StreamIso* d_isos, uint16_t* d_unit_counts, const uint32_t* d_unit_offsets,
                           const uint64_t* d_plane_base, int* d_status, unsigned long long* d_next_task,
-                          const Launch& L)
+                          const Launch& L, int ctas_per_sm)
 {
     if (ntasks == 0) return cudaSuccess;
     if (rows != 1 && rows != 2) return cudaErrorInvalidValue;
@@ -1011,6 +1022,7 @@ cudaError_t launch_stream(bool emit, int dtype, int rows, const StreamGroup* d_g
         int per_sm = 0;
         if (e == cudaSuccess) e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, kStreamThreads, smem);
         if (e != cudaSuccess) return e;
+        if (ctas_per_sm > 0 && ctas_per_sm < per_sm) per_sm = ctas_per_sm;
         // persistent: as many CTAs as are resident at once (never more than the tasks need)
         const uint64_t resident = (uint64_t)(per_sm > 0 ? per_sm : 1) * (uint64_t)L.num_sms;
         const uint64_t nctas = need < resident ? need : resident;
@@ -1024,11 +1036,11 @@ cudaError_t launch_stream(bool emit, int dtype, int rows, const StreamGroup* d_g
     return cudaGetLastError();
 }
 
-cudaError_t launch_bricks(const VolumeView& v, int rows, float2* out, const Launch& L)
+cudaError_t launch_bricks(const VolumeView& v, float2* out, const Launch& L)
 {
-    const uint64_t n = brick_count(v, rows);
+    const uint64_t n = brick_count(v);
     if (n == 0) return cudaSuccess;
-    const uint32_t seg = (uint32_t)(kSegCells / rows);
+    const uint32_t seg = kBrickCells;
     const uint32_t wpr = (v.nx - 1 + seg - 1) / seg, nby = (v.ny - 1 + 1) / 2;
     const unsigned blocks = (unsigned)((n * 32 + 255) / 256);
     KVSMC_STREAM_SWITCH(v.dtype, {
@@ -1042,12 +1054,28 @@ cudaError_t launch_bricks(const VolumeView& v, int rows, float2* out, const Laun
 
 cudaError_t launch_unit_scan(const StreamGroup* d_groups, int ngroups, uint32_t nplanes, const StreamIso* d_isos,
                              const uint16_t* d_unit_counts, uint32_t* d_unit_offsets, uint32_t* d_plane_totals,
-                             const Launch& L)
+                             const Launch& L, int scan_threads)
 {
     if (nplanes == 0) return cudaSuccess;
     prof_begin(L, "unit_scan");
-    k_unit_scan<<<nplanes, kScanUnitThreads, 0, L.stream>>>(d_groups, ngroups, d_isos, d_unit_counts, d_unit_offsets,
-                                                            d_plane_totals);
+    switch (scan_threads) {
+    case 64:
+        k_unit_scan<64><<<nplanes, 64, 0, L.stream>>>(d_groups, ngroups, d_isos, d_unit_counts, d_unit_offsets,
+                                                      d_plane_totals);
+        break;
+    case 128:
+        k_unit_scan<128><<<nplanes, 128, 0, L.stream>>>(d_groups, ngroups, d_isos, d_unit_counts, d_unit_offsets,
+                                                        d_plane_totals);
+        break;
+    case 0:
+    case 256:
+        k_unit_scan<256><<<nplanes, 256, 0, L.stream>>>(d_groups, ngroups, d_isos, d_unit_counts, d_unit_offsets,
+                                                        d_plane_totals);
+        break;
+    default:
+        prof_end(L);
+        return cudaErrorInvalidValue;
+    }
     prof_end(L);
     *L.counter += 1;
     return cudaGetLastError();

@@ -58,7 +58,7 @@ cudaError_t record(kvsmc_host::StreamBatch& b, cudaStream_t s, int num_sms, uint
             return kvsmc::launch_stream(emit, l.dtype, l.rows, b.d_groups + l.g0, l.ng, l.ntasks, b.d_isos,
                                         b.d_unit_counts, emit ? b.d_unit_offsets : nullptr,
                                         emit ? b.d_plane_base : nullptr, b.d_status, b.d_next + 2 * i + (emit ? 1 : 0),
-                                        Li);
+                                        Li, l.ctas_per_sm);
         });
     };
     cudaError_t e = cudaMemsetAsync(b.d_status, 0, sizeof(int), s);
@@ -67,7 +67,7 @@ cudaError_t record(kvsmc_host::StreamBatch& b, cudaStream_t s, int num_sms, uint
     if (e == cudaSuccess) e = per_kind(false);
     if (e == cudaSuccess)
         e = kvsmc::launch_unit_scan(b.d_groups, (int)b.groups.size(), b.scan_blocks, b.d_isos, b.d_unit_counts,
-                                    b.d_unit_offsets, b.d_plane_totals, L);
+                                    b.d_unit_offsets, b.d_plane_totals, L, b.scan_threads);
     if (e == cudaSuccess) e = kvsmc::launch_scan(b.d_plane_totals, b.d_plane_base, b.iso_planes, b.d_scan, b.d_total, L);
     if (e == cudaSuccess)
         e = kvsmc::launch_iso_totals(b.d_isos, (int)b.isos.size(), b.d_plane_base, b.d_total, b.d_totals, L);

@@ -329,7 +329,13 @@ kvsmc_status kvsmc_server_create(kvsmc_context* ctx, const kvsmc_server_config* 
     for (int w = 0; w < S->cfg.workers && !st; ++w) {
         kvsmc_context* c = nullptr;
         st = kvsmc_create(ctx->device, &c);
-        if (!st) S->wctx.push_back(c);
+        if (!st) {
+            // the workers follow the owner's launch shapes
+            c->tuning = ctx->tuning;
+            c->tune_forced = ctx->tune_forced;
+            c->tune_force = ctx->tune_force;
+            S->wctx.push_back(c);
+        }
     }
     if (st) {
         for (kvsmc_context* c : S->wctx) kvsmc_destroy(c);
