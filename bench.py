@@ -8,7 +8,10 @@ volume: the fused count launch, the scan, the fused emit launch, with output
 written to HBM.  `value` = cells x isovalues / s (Mcells/s).
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
-                    [--workload sweep1024|sweep512|uneven200|serve|heavy|blobs128]
+                    [--workload sweep1024|sweep512|uneven200|serve|heavy|blobs128] [--tune]
+
+--tune runs the launch-shape autotuner (kvsmc_autotune, a few seconds) on the
+bench's context before measuring; without it the built-in rules decide.
 
 --workload serve runs the request loop (kvsmc_server_*) under Poisson
 arrivals at each offered rate and reports p50/p99 latency and throughput.
@@ -185,6 +188,21 @@ def traffic_per_launch(workload):
 
 # ----------------------------------------------------------------- our arm
 
+def maybe_tune(args, ctx):
+    """--tune: run the launch-shape autotuner on this context first; returns
+    a summary for the JSON line (None without --tune)."""
+    if not args.tune:
+        return None
+    import time
+
+    from kvs_gb300 import autotune as T
+    t0 = time.time()
+    table = T.autotune(ctx, max_class=4, isovalues=4, reps=3)
+    changed = [r for r in table if any(r[f] for f in T.FIELDS)]
+    return {"seconds": round(time.time() - t0, 2), "entries": len(table), "entries_changed": len(changed),
+            "changed": [{k: r[k] for k in ("dtype", "size_class") + T.FIELDS} for r in changed]}
+
+
 def run_ours(args, rank, world, local):
     import ctypes as C
 
@@ -198,6 +216,7 @@ def run_ours(args, rank, world, local):
     ctx = _abi.Context(local)
     stream = torch.cuda.Stream()
     ctx.set_stream(stream.cuda_stream)
+    tuning = maybe_tune(args, ctx)
     from kvs_gb300 import synthetic as S
     dt = np.dtype(w.get("dtype", np.float32))
     field = make_field(w, "cuda")
@@ -298,7 +317,9 @@ def run_ours(args, rank, world, local):
                    "isolevels": [round(x, 6) for x in isos],
                    "mode": "duplication+PolygonNormal", "cache": "inputs larger than L2 (4 GiB volume, "
                    "outputs ~48 B/triangle)" if args.workload in ("sweep1024", "heavy") else (
-                   "inputs larger than L2 (512 MiB volume)" if args.workload == "sweep512" else "input smaller than L2")},
+                   "inputs larger than L2 (512 MiB volume)" if args.workload == "sweep512" else "input smaller than L2"),
+                   "launch_shapes": "autotuned (--tune)" if tuning else "built-in rules"},
+        "tuning": tuning,
         "mtris_per_s": round(ntri * world / (step_ms * 1e-3) / 1e6, 1),
         "triangles_per_step": int(ntri),
         "roofline": roofline,
@@ -361,6 +382,7 @@ def run_batch(args, rank, world, local):
     ctx = _abi.Context(local)
     stream = torch.cuda.Stream()
     ctx.set_stream(stream.cuda_stream)
+    tuning = maybe_tune(args, ctx)
     rng = np.random.default_rng(w["seed"])
     dts = [np.uint8, np.uint16, np.float32]
     vols, params, hosts, shapes = [], [], [], []
@@ -490,7 +512,9 @@ def run_batch(args, rank, world, local):
         "warmup": args.warmup, "ms_per_step": round(ms_graph, 4), "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "u8/u16/f32", "data": "synthetic (seeded phantoms generated on the device)",
         "config": {"workload": w["desc"], "requests": n, "cells": int(cells), "input_bytes": int(in_bytes),
-                   "cache": "inputs larger than L2 (%.1f GB of volumes)" % (in_bytes / 1e9)},
+                   "cache": "inputs larger than L2 (%.1f GB of volumes)" % (in_bytes / 1e9),
+                   "launch_shapes": "autotuned (--tune)" if tuning else "built-in rules"},
+        "tuning": tuning,
         "mtris_per_s": round(ntri * world / (ms_graph * 1e-3) / 1e6, 1), "triangles_per_step": int(ntri),
         "forms": {"per_call": {"api": "kvsmc_extract_device x%d" % n, "ms_per_step": round(ms_call, 3),
                                "value": mc(ms_call), "gpu_launches": int(l_call)},
@@ -772,6 +796,7 @@ def main():
     ap.add_argument("--workload", default="sweep1024", choices=sorted(WORKLOADS))
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--tune", action="store_true", help="run the launch-shape autotuner before measuring")
     args = ap.parse_args()
     args.warmup = max(3, args.warmup)
     rank, world, local = dist_env()
