@@ -1,0 +1,213 @@
+/*****************************************************************************/
+/**
+ *  @file   Isosurface.cpp
+ *  @brief  kvs::cuda::Isosurface on kvs::cuda::MarchingCubes.
+ *
+ *  The flow is the reference's (Source/Core/Visualization/Mapper/Isosurface.cpp):
+ *  the constructors (:23-96) set the normal type, take the default isolevel
+ *  (max + min) * 0.5 from the volume's min/max cache and make VertexNormal
+ *  imply shared vertices; exec (:104-124) checks the input; mapping
+ *  (:132-258) builds the per-grid mapper and shallow-copies its arrays.
+ *  What changes: the structured branch's mapper is kvs::cuda::MarchingCubes,
+ *  the min/max scan behind the default isolevel runs on the GPU, and a GPU
+ *  failure is reported and ends exec with nullptr instead of leaving empty
+ *  arrays behind.  As in the reference, this mapper never sets isSuccess()
+ *  true (MapperBase's initial false, MapperBase.cpp:23).
+ */
+/*****************************************************************************/
+#include "Isosurface.h"
+
+#include <kvs/MarchingHexahedra>
+#include <kvs/MarchingPrism>
+#include <kvs/MarchingPyramid>
+#include <kvs/MarchingTetrahedra>
+#include <kvs/Message>
+#include <kvs/StructuredVolumeObject>
+#include <kvs/UnstructuredVolumeObject>
+
+#include "Context.h"
+#include "MarchingCubes.h"
+
+namespace
+{
+
+// StructuredVolumeObject::updateMinMaxValues (StructuredVolumeObject.cpp:431-450)
+// by the device scan (GetMinMaxValues' rules); the cache is mutable in the
+// reference too (VolumeObjectBase.h:51-53).
+bool DeviceMinMax( const kvs::StructuredVolumeObject* volume, int device )
+{
+    const int dtype = kvs::cuda::DType( volume->values() );
+    if ( dtype < 0 ) return false;
+    kvsmc_status st = KVSMC_OK;
+    kvsmc_context* ctx = kvs::cuda::DeviceContext( device, &st );
+    if ( !ctx )
+    {
+        kvsMessageError("libkvsmc: %s.", kvsmc_status_string( st ) );
+        return false;
+    }
+    const auto res = volume->resolution();
+    kvsmc_volume* v = nullptr;
+    double mn = 0, mx = 0;
+    st = kvsmc_volume_upload( ctx, volume->values().data(), kvsmc_dtype( dtype ), res.x(), res.y(), res.z(), &v );
+    if ( st == KVSMC_OK ) st = kvsmc_volume_minmax( ctx, v, &mn, &mx );
+    if ( v ) kvsmc_volume_free( ctx, v );
+    if ( st != KVSMC_OK )
+    {
+        kvsMessageError("libkvsmc: %s: %s", kvsmc_status_string( st ), kvsmc_last_error( ctx ) );
+        return false;
+    }
+    volume->setMinMaxValues( mn, mx );
+    return true;
+}
+
+} // end of namespace
+
+namespace kvs
+{
+
+namespace cuda
+{
+
+Isosurface::Isosurface(
+    const kvs::VolumeObjectBase* volume,
+    const SuperClass::NormalType normal_type ):
+    kvs::MapperBase(),
+    kvs::PolygonObject()
+{
+    SuperClass::setNormalType( normal_type );
+    if ( !volume->hasMinMaxValues() )
+    {
+        const auto* svolume = kvs::StructuredVolumeObject::DownCast( volume );
+        if ( svolume ) { if ( !DeviceMinMax( svolume, m_device ) ) return; }
+        else { volume->updateMinMaxValues(); }   // unstructured: the reference's own scan
+    }
+    this->setIsolevel( ( volume->maxValue() + volume->minValue() ) * 0.5 );
+    if ( normal_type == kvs::PolygonObject::VertexNormal ) { m_duplication = false; }
+    this->exec( volume );
+}
+
+Isosurface::Isosurface(
+    const kvs::VolumeObjectBase* volume,
+    const double isolevel,
+    const NormalType normal_type ):
+    kvs::MapperBase(),
+    kvs::PolygonObject(),
+    m_isolevel( isolevel )
+{
+    SuperClass::setNormalType( normal_type );
+    if ( normal_type == kvs::PolygonObject::VertexNormal ) { m_duplication = false; }
+    this->exec( volume );
+}
+
+Isosurface::Isosurface(
+    const kvs::VolumeObjectBase* volume,
+    const double isolevel,
+    const NormalType normal_type,
+    const bool duplication,
+    const kvs::TransferFunction& transfer_function ):
+    kvs::MapperBase( transfer_function ),
+    kvs::PolygonObject(),
+    m_isolevel( isolevel ),
+    m_duplication( duplication )
+{
+    SuperClass::setNormalType( normal_type );
+    if ( normal_type == kvs::PolygonObject::VertexNormal ) { m_duplication = false; }
+    this->exec( volume );
+}
+
+Isosurface::SuperClass* Isosurface::exec( const kvs::ObjectBase* object )
+{
+    if ( !object )
+    {
+        BaseClass::setSuccess( false );
+        kvsMessageError("Input object is NULL.");
+        return nullptr;
+    }
+
+    const auto* volume = kvs::VolumeObjectBase::DownCast( object );
+    if ( !volume )
+    {
+        BaseClass::setSuccess( false );
+        kvsMessageError("Input object is not volume dat.");
+        return nullptr;
+    }
+
+    if ( !this->mapping( volume ) ) { return nullptr; }
+    return this;
+}
+
+void Isosurface::shallowCopy( const kvs::PolygonObject* polygon )
+{
+    SuperClass::setCoords( polygon->coords() );
+    SuperClass::setColors( polygon->colors() );
+    SuperClass::setNormals( polygon->normals() );
+    SuperClass::setConnections( polygon->connections() );
+    SuperClass::setOpacities( polygon->opacities() );
+    SuperClass::setPolygonType( polygon->polygonType() );
+    SuperClass::setColorType( polygon->colorType() );
+    SuperClass::setNormalType( polygon->normalType() );
+    SuperClass::setMinMaxObjectCoords( polygon->minObjectCoord(), polygon->maxObjectCoord() );
+    SuperClass::setMinMaxExternalCoords( polygon->minExternalCoord(), polygon->maxExternalCoord() );
+}
+
+bool Isosurface::mapping( const kvs::VolumeObjectBase* volume )
+{
+    if ( volume->veclen() != 1 )
+    {
+        BaseClass::setSuccess( false );
+        kvsMessageError("Input object is not scalar field dat.");
+        return true;   // the reference returns `this` here
+    }
+
+    const auto ntype = SuperClass::normalType();
+    const auto tfunc = BaseClass::transferFunction();
+
+    if ( volume->volumeType() == kvs::VolumeObjectBase::Structured )
+    {
+        const auto* svolume = kvs::StructuredVolumeObject::DownCast( volume );
+        kvs::cuda::MarchingCubes polygon;
+        polygon.setDevice( m_device );
+        polygon.setNormalType( ntype );
+        polygon.setTransferFunction( tfunc );
+        polygon.setDuplication( m_duplication );
+        polygon.setIsolevel( m_isolevel );
+        if ( !polygon.exec( svolume ) )
+        {
+            BaseClass::setSuccess( false );
+            kvsMessageError("Cannot create isosurfaces.");
+            return false;
+        }
+        this->shallowCopy( &polygon );
+        return true;
+    }
+
+    // unstructured grids: the reference's own mappers (Isosurface.cpp:193-258)
+    const auto* uvolume = kvs::UnstructuredVolumeObject::DownCast( volume );
+    kvs::PolygonObject* polygon = nullptr;
+    switch ( uvolume->cellType() )
+    {
+    case kvs::UnstructuredVolumeObject::Tetrahedra:
+        polygon = new kvs::MarchingTetrahedra( uvolume, m_isolevel, ntype, m_duplication, tfunc );
+        break;
+    case kvs::UnstructuredVolumeObject::Hexahedra:
+        polygon = new kvs::MarchingHexahedra( uvolume, m_isolevel, ntype, m_duplication, tfunc );
+        break;
+    case kvs::UnstructuredVolumeObject::Pyramid:
+        polygon = new kvs::MarchingPyramid( uvolume, m_isolevel, ntype, m_duplication, tfunc );
+        break;
+    case kvs::UnstructuredVolumeObject::Prism:
+        polygon = new kvs::MarchingPrism( uvolume, m_isolevel, ntype, m_duplication, tfunc );
+        break;
+    default: break;
+    }
+    if ( polygon )
+    {
+        this->shallowCopy( polygon );
+        delete polygon;
+    }
+    return true;
+}
+
+} // end of namespace cuda
+
+} // end of namespace kvs

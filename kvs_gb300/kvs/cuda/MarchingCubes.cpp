@@ -20,6 +20,7 @@
 #include <kvs/Message>
 #include <kvs/ValueArray>
 
+#include "Context.h"
 #include "kvsmc.h"
 
 namespace
@@ -46,6 +47,15 @@ kvsmc_context* Context( int device, kvsmc_status* status )
     return ctx;
 }
 
+} // end of namespace
+
+namespace kvs
+{
+namespace cuda
+{
+
+kvsmc_context* DeviceContext( int device, kvsmc_status* status ) { return Context( device, status ); }
+
 // kvs::Type::TypeID -> kvsmc_dtype (the reference's type switch, :113-124)
 int DType( const kvs::AnyValueArray& values )
 {
@@ -64,6 +74,14 @@ int DType( const kvs::AnyValueArray& values )
     default: return -1;
     }
 }
+
+} // end of namespace cuda
+} // end of namespace kvs
+
+namespace
+{
+
+using kvs::cuda::DType;
 
 // The arrays the C call asks for, allocated as the PolygonObject's own.
 struct Outputs

@@ -49,6 +49,8 @@ public:
 
     void setIsolevel( const double isolevel ) { m_isolevel = isolevel; }
     void setDevice( const int device ) { m_device = device; }
+    /// the constructor's duplication flag, for the pipeline-module form
+    void setDuplication( const bool duplication ) { m_duplication = duplication; }
 
     SuperClass* exec( const kvs::ObjectBase* object );
 

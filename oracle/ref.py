@@ -1,4 +1,5 @@
-"""ctypes binding to the reference kvs::MarchingCubes built by oracle/Makefile.ref.
+"""ctypes binding to the reference kvs::MarchingCubes and kvs::Isosurface built by
+oracle/Makefile.ref.
 
 Test infrastructure only (parity anchor).  The library exists only where the
 reference sources were available to compile it; `available()` says whether it
@@ -78,6 +79,11 @@ def lib():
             C.c_int, C.c_void_p, C.c_void_p,
             C.c_int, C.c_int, C.c_float, C.c_float,
             C.c_int, C.POINTER(_Result)]
+        _lib.kvsref_isosurface.restype = C.c_int
+        _lib.kvsref_isosurface.argtypes = [
+            C.c_int, C.c_int, C.c_void_p, C.c_uint, C.c_uint, C.c_uint,
+            C.c_double, C.c_int, C.c_int, C.c_int, C.c_double, C.c_double,
+            C.c_int, C.c_int, C.c_float, C.c_float, C.POINTER(_Result)]
         _lib.kvsref_free.argtypes = [C.POINTER(_Result)]
         _lib.kvsref_hydrogen.argtypes = [C.c_uint, C.c_void_p]
         _lib.kvsref_default_colormap.argtypes = [C.c_int, C.c_void_p]
@@ -133,6 +139,44 @@ def marching_cubes(values, isolevel, normal_type="polygon", duplication=True,
         seconds=r.seconds)
     lib().kvsref_free(C.byref(r))
     return out
+
+
+def _collect(r):
+    out = dict(
+        success=bool(r.success),
+        coords=_arr(r.coords, r.ncoords, np.float32),
+        normals=_arr(r.normals, r.nnormals, np.float32),
+        connections=_arr(r.connections, r.nconnections, np.uint32),
+        colors=_arr(r.colors, r.ncolors, np.uint8),
+        opacities=_arr(r.opacities, r.nopacities, np.uint8),
+        polygon_type=r.polygon_type, normal_type=r.normal_type, color_type=r.color_type,
+        vol_has_minmax=bool(r.vol_has_minmax), vol_min=r.vol_min, vol_max=r.vol_max,
+        min_obj=np.array(r.min_obj[:], np.float32), max_obj=np.array(r.max_obj[:], np.float32),
+        min_ext=np.array(r.min_ext[:], np.float32), max_ext=np.array(r.max_ext[:], np.float32))
+    lib().kvsref_free(C.byref(r))
+    return out
+
+
+def isosurface(values, form, isolevel=0.0, normal_type="polygon", duplication=True, minmax=None,
+               tf_resolution=256, tf_range=None):
+    """The reference kvs::Isosurface through constructor `form` (0: volume,
+    normal type -- isolevel from the min/max; 1: + isolevel; 2: + duplication
+    and transfer function) on a uniform volume shaped (nz, ny, nx)."""
+    v = np.ascontiguousarray(values)
+    nz, ny, nx = v.shape
+    r = _Result()
+    st = lib().kvsref_isosurface(
+        int(form), dtype_code(v.dtype), v.ctypes.data, nx, ny, nz, float(isolevel),
+        0 if normal_type == "polygon" else 1, 1 if duplication else 0,
+        1 if minmax is not None else 0,
+        float(minmax[0]) if minmax is not None else 0.0,
+        float(minmax[1]) if minmax is not None else 0.0,
+        tf_resolution, 1 if tf_range is not None else 0,
+        float(tf_range[0]) if tf_range is not None else 0.0,
+        float(tf_range[1]) if tf_range is not None else 0.0, C.byref(r))
+    if st != 0:
+        raise RuntimeError("kvsref_isosurface failed")
+    return _collect(r)
 
 
 def hydrogen(res):

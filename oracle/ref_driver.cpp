@@ -11,6 +11,7 @@
 #include <kvs/StructuredVolumeObject>
 #include <kvs/PolygonObject>
 #include <kvs/MarchingCubes>
+#include <kvs/Isosurface>
 #include <kvs/TransferFunction>
 #include <kvs/HydrogenVolumeData>
 #include <kvs/ValueArray>
@@ -87,6 +88,29 @@ T* CopyOut( const kvs::ValueArray<T>& a, unsigned long long* n )
 
 void Copy3( float* dst, const kvs::Vec3& v ) { dst[0] = v.x(); dst[1] = v.y(); dst[2] = v.z(); }
 
+// The arrays, types and bounding box of a mapper's PolygonObject, and the
+// volume's min/max cache afterwards.
+void Fill( const kvs::MapperBase* mapper, const kvs::PolygonObject* p, const kvs::StructuredVolumeObject* vol,
+           kvsref_result* out )
+{
+    out->success = mapper->isSuccess() ? 1 : 0;
+    out->coords = CopyOut( p->coords(), &out->ncoords );
+    out->normals = CopyOut( p->normals(), &out->nnormals );
+    out->connections = CopyOut( p->connections(), &out->nconnections );
+    out->colors = CopyOut( p->colors(), &out->ncolors );
+    out->opacities = CopyOut( p->opacities(), &out->nopacities );
+    out->polygon_type = int( p->polygonType() );
+    out->normal_type = int( p->normalType() );
+    out->color_type = int( p->colorType() );
+    out->vol_has_minmax = vol->hasMinMaxValues() ? 1 : 0;
+    out->vol_min = vol->minValue();
+    out->vol_max = vol->maxValue();
+    Copy3( out->min_obj, p->minObjectCoord() );
+    Copy3( out->max_obj, p->maxObjectCoord() );
+    Copy3( out->min_ext, p->minExternalCoord() );
+    Copy3( out->max_ext, p->maxExternalCoord() );
+}
+
 } // namespace
 
 extern "C" {
@@ -152,24 +176,44 @@ int kvsref_marching_cubes(
         if ( s < best ) best = s;
     }
 
-    out->success = mc->isSuccess() ? 1 : 0;
-    out->coords = CopyOut( mc->coords(), &out->ncoords );
-    out->normals = CopyOut( mc->normals(), &out->nnormals );
-    out->connections = CopyOut( mc->connections(), &out->nconnections );
-    out->colors = CopyOut( mc->colors(), &out->ncolors );
-    out->opacities = CopyOut( mc->opacities(), &out->nopacities );
-    out->polygon_type = int( mc->polygonType() );
-    out->normal_type = int( mc->normalType() );
-    out->color_type = int( mc->colorType() );
-    out->vol_has_minmax = vol->hasMinMaxValues() ? 1 : 0;
-    out->vol_min = vol->minValue();
-    out->vol_max = vol->maxValue();
-    Copy3( out->min_obj, mc->minObjectCoord() );
-    Copy3( out->max_obj, mc->maxObjectCoord() );
-    Copy3( out->min_ext, mc->minExternalCoord() );
-    Copy3( out->max_ext, mc->maxExternalCoord() );
+    Fill( mc, mc, vol, out );
     out->seconds = best;
     delete mc;
+    delete vol;
+    return 0;
+}
+
+/*
+ * The reference kvs::Isosurface (Source/Core/Visualization/Mapper/Isosurface.cpp)
+ * on a uniform structured volume, through one of its three constructors:
+ *   form 0: Isosurface( volume, normal_type )   -- isolevel = (max + min) * 0.5
+ *   form 1: Isosurface( volume, isolevel, normal_type )
+ *   form 2: Isosurface( volume, isolevel, normal_type, duplication, tfunc )
+ */
+int kvsref_isosurface(
+    int form, int dtype, const void* values, unsigned nx, unsigned ny, unsigned nz,
+    double isolevel, int normal_type, int duplication, int has_minmax, double vmin, double vmax,
+    int tf_resolution, int tf_has_range, float tf_min, float tf_max, kvsref_result* out )
+{
+    std::memset( out, 0, sizeof( *out ) );
+    const size_t n = size_t( nx ) * ny * nz;
+    kvs::AnyValueArray vals = Values( dtype, values, n );
+    if ( vals.size() != n ) return -1;
+    kvs::TransferFunction tfunc( tf_resolution > 0 ? tf_resolution : 256 );
+    if ( tf_has_range ) tfunc.setRange( tf_min, tf_max );
+    const auto ntype = normal_type == 0 ? kvs::PolygonObject::PolygonNormal : kvs::PolygonObject::VertexNormal;
+    auto* vol = new kvs::StructuredVolumeObject();
+    vol->setVeclen( 1 );
+    vol->setResolution( kvs::Vec3ui( nx, ny, nz ) );
+    vol->setValues( vals );
+    vol->setGridTypeToUniform();
+    if ( has_minmax ) vol->setMinMaxValues( vmin, vmax );
+    kvs::Isosurface* iso = nullptr;
+    if ( form == 0 ) iso = new kvs::Isosurface( vol, ntype );
+    else if ( form == 1 ) iso = new kvs::Isosurface( vol, isolevel, ntype );
+    else iso = new kvs::Isosurface( vol, isolevel, ntype, duplication != 0, tfunc );
+    Fill( iso, iso, vol, out );
+    delete iso;
     delete vol;
     return 0;
 }

@@ -1,12 +1,14 @@
-"""Generate the golden fixtures from the reference kvs::MarchingCubes.
+"""Generate the golden fixtures from the reference kvs::MarchingCubes and
+kvs::Isosurface.
 
-Runs the reference mapper compiled from its own sources (oracle/_ref, built by
-oracle/Makefile.ref) on small seeded inputs and stores inputs + outputs in
-tests/golden/golden.npz, with the case list in tests/golden/cases.json.  The
-reference ships no tests or golden vectors of its own, so these fixtures pin the
-oracle restatement and the CUDA path on hosts where the reference is absent.
+Runs the reference mappers compiled from their own sources (oracle/_ref, built
+by oracle/Makefile.ref) on small seeded inputs and stores inputs + outputs in
+tests/golden/golden.npz (case list tests/golden/cases.json) and
+tests/golden/isosurface.npz (tests/golden/isosurface.json).  The reference
+ships no tests or golden vectors of its own, so these fixtures pin the oracle
+restatement and the CUDA path on hosts where the reference is absent.
 
-    python tests/golden/make_golden.py
+    python tests/golden/make_golden.py [marching_cubes] [isosurface]   (default: both)
 """
 import json
 import os
@@ -60,9 +62,61 @@ def cases():
     return out
 
 
+def isosurface_cases():
+    """(name, volume, [(form, isolevel, normal_type, duplication, minmax, tf_range), ...])"""
+    rng = np.random.default_rng(77)
+    h = ref.hydrogen(32)
+    x, y, z = np.meshgrid(np.arange(26), np.arange(24), np.arange(22), indexing="xy")
+    blob = np.exp(-((x - 12.3) ** 2 + (y - 11.1) ** 2 + (z - 10.7) ** 2) / (2 * 6.0 ** 2)).transpose(2, 0, 1)
+    blob = np.ascontiguousarray(blob).astype(np.float32)
+    f = rng.random((9, 10, 11)).astype(np.float32)
+    w = f.copy()
+    w[2, 3, 4] = np.nan
+    return [
+        ("hydrogen32", h, [(0, 0.0, "polygon", True, None, None), (0, 0.0, "vertex", True, None, None),
+                           (1, 100.5, "polygon", True, None, None), (1, 100.5, "vertex", True, None, None),
+                           (2, 60.0, "polygon", False, None, (0.0, 200.0)), (2, 60.0, "polygon", True, None, None)]),
+        ("blob_f32", blob, [(0, 0.0, "polygon", True, None, None), (1, 0.3, "vertex", True, None, None),
+                            (2, 0.5, "polygon", False, None, None)]),
+        ("random_i16", rng.integers(-300, 300, (9, 10, 11)).astype(np.int16), [(0, 0.0, "polygon", True, None, None)]),
+        ("random_u16", rng.integers(0, 60000, (6, 7, 33)).astype(np.uint16), [(0, 0.0, "polygon", True, None, None)]),
+        ("random_f64", rng.random((9, 10, 11)), [(0, 0.0, "polygon", True, None, None),
+                                                 (2, 0.5, "vertex", True, None, None)]),
+        ("constant_f32", np.full((4, 5, 6), 2.0, np.float32), [(0, 0.0, "polygon", True, None, None)]),
+        ("nan_f32", w, [(0, 0.0, "polygon", True, None, None)]),
+        ("preset_f32", f, [(0, 0.0, "polygon", True, (0.2, 0.6), None), (1, 0.5, "polygon", True, (0.2, 0.6), None)]),
+    ]
+
+
+def write_isosurface():
+    arrays, manifest = {}, []
+    for name, v, runs in isosurface_cases():
+        arrays[f"{name}__input"] = v
+        for i, (form, iso, nt, dup, minmax, tfr) in enumerate(runs):
+            key = f"{name}__{i}"
+            r = ref.isosurface(v, form, iso, nt, dup, minmax=minmax, tf_range=tfr)
+            for fld in ("coords", "normals", "connections", "colors", "opacities"):
+                arrays[f"{key}__{fld}"] = r[fld]
+            manifest.append(dict(key=key, case=name, form=form, isolevel=iso, normal_type=nt, duplication=dup,
+                                 minmax=minmax, tf_range=tfr, success=r["success"], vol_min=r["vol_min"],
+                                 vol_max=r["vol_max"], polygon_type=r["polygon_type"],
+                                 normal_type_out=r["normal_type"], color_type=r["color_type"],
+                                 min_obj=r["min_obj"].tolist(), max_obj=r["max_obj"].tolist(),
+                                 min_ext=r["min_ext"].tolist(), max_ext=r["max_ext"].tolist()))
+    np.savez_compressed(os.path.join(HERE, "isosurface.npz"), **arrays)
+    with open(os.path.join(HERE, "isosurface.json"), "w") as f:
+        json.dump(manifest, f, indent=0)
+    print(f"{len(manifest)} isosurface cases")
+
+
 def main():
     if not ref.available():
         ref.build()
+    parts = sys.argv[1:] or ["marching_cubes", "isosurface"]
+    if "isosurface" in parts:
+        write_isosurface()
+    if "marching_cubes" not in parts:
+        return
     arrays = {}
     manifest = []
     for name, v, isos, opts in cases():

@@ -6,6 +6,7 @@
 #include <kvs/HydrogenVolumeData>
 #include <kvs/TransferFunction>
 #include "kvs/cuda/MarchingCubes.h"
+#include "kvs/cuda/Isosurface.h"
 
 int main()
 {
@@ -27,6 +28,16 @@ int main()
 
     kvs::ObjectBase* none = m.exec( nullptr );
     std::printf( "null success=%d returned=%d\n", m.isSuccess() ? 1 : 0, none ? 1 : 0 );
+
+    // kvs::Isosurface's forms (Isosurface.h:35-48) on the drop-in
+    kvs::cuda::Isosurface* s = new kvs::cuda::Isosurface( volume, iso, kvs::PolygonObject::PolygonNormal, true, tf );
+    std::printf( "isosurface vertices=%zu connections=%zu module=%s\n", s->numberOfVertices(),
+                 s->numberOfConnections(), s->moduleName() );
+    kvs::cuda::Isosurface t;
+    kvs::ObjectBase* u = t.exec( volume );
+    std::printf( "isosurface exec returned=%d vertices=%zu\n", u ? 1 : 0, t.numberOfVertices() );
+    std::printf( "isosurface null returned=%d\n", t.exec( nullptr ) ? 1 : 0 );
+    delete s;
     delete a;
     return 0;
 }

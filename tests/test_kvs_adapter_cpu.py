@@ -37,4 +37,8 @@ def test_adapter_builds_and_fails_loudly_without_gpu(tmp_path):
     assert "ctor success=0 vertices=0" in r.stdout
     assert "exec success=0 returned=0 module=kvs::cuda::MarchingCubes" in r.stdout
     assert "null success=0 returned=0" in r.stdout
+    assert "isosurface vertices=0 connections=0 module=kvs::cuda::Isosurface" in r.stdout
+    assert "isosurface exec returned=0 vertices=0" in r.stdout
+    assert "isosurface null returned=0" in r.stdout
+    assert "Cannot create isosurfaces." in r.stdout + r.stderr
     assert "no CUDA device" in r.stdout + r.stderr
