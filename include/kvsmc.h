@@ -311,6 +311,41 @@ kvsmc_status kvsmc_extract_noalloc(const void* d_values, kvsmc_dtype dtype, uint
                                    uint64_t coords_capacity, float* d_normals, uint64_t normals_capacity,
                                    void* cuda_stream, kvsmc_sizes* sizes);
 
+/* ---------------------------------------------------------- polygon export */
+
+/* Binary STL records of a triangle mesh in device memory: what
+ * kvs::PolygonExporter<kvs::Stl>::exec (PolygonExporter.cpp:78-176) and
+ * kvs::Stl::write_binary (Stl.cpp:490-540) write after the 84-byte header --
+ * per triangle its normal (3 floats; with vertex normals the mean
+ * (n0 + n1 + n2) / 3 of its vertices' normals), its 3 vertices (9 floats)
+ * and 2 zero bytes: 50 bytes, little-endian.  mode is the kvsmc_mode the mesh
+ * was extracted with:
+ *   KVSMC_DUP_POLYGON_NORMAL:    d_coords 9T floats, d_normals 3T (d_connections unused);
+ *   KVSMC_SHARED_POLYGON_NORMAL: d_coords 3V, d_connections 3T, d_normals 3T;
+ *   KVSMC_SHARED_VERTEX_NORMAL:  d_coords 3V, d_connections 3T, d_normals 3V.
+ * d_out: 50 * ntriangles bytes of 16-byte aligned device memory.  Runs on the
+ * context's stream and waits for it.  A connection index >= nvertices is
+ * KVSMC_ERR_INVALID_ARGUMENT (checked on the device; nothing is read out of
+ * range). */
+kvsmc_status kvsmc_stl_records(kvsmc_context* ctx, int32_t mode, const float* d_coords, const float* d_normals,
+                               const uint32_t* d_connections, uint64_t nvertices, uint64_t ntriangles,
+                               void* d_out);
+/* The binary STL file of a device mesh, written to `path`: the 80-byte header
+ * "Generated by KVS" (zero-padded), the uint32 triangle count, the records --
+ * serialised on the GPU in chunks of 2^20 triangles, each copied to pinned
+ * memory and written while the next is serialised.  The reference's
+ * kvs::Stl defaults to ASCII; this is its Binary file type.  More than
+ * 2^32 - 1 triangles is KVSMC_ERR_TOO_LARGE (the format's count would wrap). */
+kvsmc_status kvsmc_write_stl(kvsmc_context* ctx, const char* path, int32_t mode, const float* d_coords,
+                             const float* d_normals, const uint32_t* d_connections, uint64_t nvertices,
+                             uint64_t ntriangles);
+/* Same for a mesh in HOST memory (a PolygonObject's arrays; sizes in
+ * elements): uploaded, then serialised on the GPU as above.  Triangles:
+ * ncoords / 9 (duplicated) or nconnections / 3. */
+kvsmc_status kvsmc_write_stl_host(kvsmc_context* ctx, const char* path, int32_t mode, const float* coords,
+                                  uint64_t ncoords, const float* normals, uint64_t nnormals,
+                                  const uint32_t* connections, uint64_t nconnections);
+
 /* ------------------------------------------------------------- autotuning */
 
 /* Launch shape of the streaming kernels for one (value type, volume size

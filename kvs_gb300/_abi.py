@@ -45,7 +45,8 @@ EXPORTS = [
     "kvsmc_server_create", "kvsmc_server_submit", "kvsmc_server_poll", "kvsmc_server_release",
     "kvsmc_server_stats", "kvsmc_server_destroy", "kvsmc_copy_to_host",
     "kvsmc_size_class", "kvsmc_tune_resolve", "kvsmc_tuning_set", "kvsmc_tuning_get",
-    "kvsmc_tuning_force", "kvsmc_autotune",
+    "kvsmc_tuning_force", "kvsmc_autotune", "kvsmc_stl_records", "kvsmc_write_stl",
+    "kvsmc_write_stl_host",
 ]
 
 PATH_AUTO = 0      # streaming kernels where eligible
@@ -169,6 +170,9 @@ def load(path=LIB_PATH):
         "kvsmc_plan_wait": (C.c_int, [vp, C.POINTER(Request), i32]),
         "kvsmc_plan_kernels": (u64, [vp]),
         "kvsmc_plan_destroy": (None, [vp]),
+        "kvsmc_stl_records": (C.c_int, [vp, i32, vp, vp, vp, u64, u64, vp]),
+        "kvsmc_write_stl": (C.c_int, [vp, C.c_char_p, i32, vp, vp, vp, u64, u64]),
+        "kvsmc_write_stl_host": (C.c_int, [vp, C.c_char_p, i32, vp, u64, vp, u64, vp, u64]),
         "kvsmc_size_class": (i32, [u32, u32, u32]),
         "kvsmc_tune_resolve": (C.c_int, [C.POINTER(TuneEntry), i32, C.c_int, u32, u32, u32,
                                          C.POINTER(TuneChoice)]),

@@ -469,6 +469,7 @@ void kvsmc_destroy(kvsmc_context* ctx)
     cudaStreamSynchronize(ctx->stream);
     if (ctx->host_vol) { cudaFree(ctx->host_vol->dev); delete ctx->host_vol; }
     if (ctx->scratch) cudaFree(ctx->scratch);
+    if (ctx->d_flag) cudaFree(ctx->d_flag);
     if (ctx->out_arena) cudaFree(ctx->out_arena);
     if (ctx->h_small) cudaFreeHost(ctx->h_small);
     if (ctx->h_stage) cudaFreeHost(ctx->h_stage);

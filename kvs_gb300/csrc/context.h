@@ -44,6 +44,7 @@ struct kvsmc_context {
     cudaEvent_t fork_ev = nullptr;
     cudaEvent_t join_ev[kAux] = {};
     bool aux_ready = false;
+    int* d_flag = nullptr;       // device word for checks of export calls (created on first use)
     // streaming launch shapes: the tuning table, or one forced shape
     std::vector<kvsmc_tune_entry> tuning;
     bool tune_forced = false;

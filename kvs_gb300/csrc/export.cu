@@ -1,0 +1,293 @@
+// export.cu -- binary STL serialisation of a device triangle mesh.
+//
+// The records are what kvs::PolygonExporter<kvs::Stl>::exec
+// (Source/Core/Visualization/Exporter/PolygonExporter.cpp:78-176) and
+// kvs::Stl::write_binary (Source/Core/FileFormat/STL/Stl.cpp:490-540) write:
+// per triangle its normal (3 floats), its three vertices (9 floats) and two
+// zero bytes, 50 bytes, little-endian, after an 84-byte header (80 bytes
+// "Generated by KVS" zero-padded, the uint32 triangle count).  Shared-vertex
+// meshes are expanded through their connections; with vertex normals the
+// triangle's normal is (n0 + n1 + n2) / 3 in float, in that order
+// (PolygonExporter.cpp:133-152, kvs::Vector3 operator+ and operator/).
+//
+// One CTA per tile of 256 triangles: coalesced loads of the tile's coords
+// and normals (or gathers through its connections) into shared memory, the
+// 12,800 record bytes composed there, then written with 16-byte stores (a
+// tile's records start at a multiple of 12,800 bytes, so every store is
+// aligned).  HBM-bound: 48 bytes read and 50 written per triangle for a
+// duplicated mesh.
+#include <cstdio>
+#include <cstring>
+#include <vector>
+
+#include "context.h"
+
+namespace kvsmc {
+
+namespace {
+
+constexpr int kStlTile = 256;
+constexpr int kStlRecord = 50;
+
+__device__ __forceinline__ void put_float(uint16_t* r, int slot, float f)
+{
+    const uint32_t b = __float_as_uint(f);
+    r[2 * slot] = (uint16_t)(b & 0xffffu);
+    r[2 * slot + 1] = (uint16_t)(b >> 16);
+}
+
+// mode: KVSMC_DUP_POLYGON_NORMAL / KVSMC_SHARED_POLYGON_NORMAL / KVSMC_SHARED_VERTEX_NORMAL.
+__global__ void __launch_bounds__(kStlTile)
+    k_stl_records(const float* __restrict__ coords, const float* __restrict__ normals,
+                  const uint32_t* __restrict__ conn, uint64_t nverts, uint64_t ntri, int mode,
+                  uint8_t* __restrict__ out, int* __restrict__ bad_index)
+{
+    __shared__ float sc[kStlTile * 9];
+    __shared__ float sn[kStlTile * 3];
+    __shared__ __align__(16) uint16_t rec[kStlTile * kStlRecord / 2];
+    const unsigned tid = threadIdx.x;
+    for (uint64_t tile = blockIdx.x; tile * kStlTile < ntri; tile += gridDim.x) {
+        const uint64_t t0 = tile * kStlTile;
+        const uint32_t n = (uint32_t)(ntri - t0 < (uint64_t)kStlTile ? ntri - t0 : (uint64_t)kStlTile);
+        if (mode == KVSMC_DUP_POLYGON_NORMAL) {
+            const float* cs = coords + 9 * t0;
+            for (uint32_t i = tid; i < 9 * n; i += kStlTile) sc[i] = cs[i];
+            const float* ns = normals + 3 * t0;
+            for (uint32_t i = tid; i < 3 * n; i += kStlTile) sn[i] = ns[i];
+        } else {
+            // one (triangle, corner) per thread pass: its vertex through the connections
+            const uint32_t* cn = conn + 3 * t0;
+            for (uint32_t i = tid; i < 3 * n; i += kStlTile) {
+                uint64_t v = cn[i];
+                if (v >= nverts) {
+                    atomicExch(bad_index, 1);
+                    v = 0;
+                }
+                sc[3 * i + 0] = coords[3 * v + 0];
+                sc[3 * i + 1] = coords[3 * v + 1];
+                sc[3 * i + 2] = coords[3 * v + 2];
+            }
+            if (mode == KVSMC_SHARED_POLYGON_NORMAL) {
+                const float* ns = normals + 3 * t0;
+                for (uint32_t i = tid; i < 3 * n; i += kStlTile) sn[i] = ns[i];
+            } else if (tid < n) {
+                // ( normal0 + normal1 + normal2 ) / 3.0f, component by component
+                uint64_t v0 = cn[3 * tid], v1 = cn[3 * tid + 1], v2 = cn[3 * tid + 2];
+                v0 = v0 < nverts ? v0 : 0;
+                v1 = v1 < nverts ? v1 : 0;
+                v2 = v2 < nverts ? v2 : 0;
+#pragma unroll
+                for (int k = 0; k < 3; ++k) {
+                    const float s = __fadd_rn(__fadd_rn(normals[3 * v0 + k], normals[3 * v1 + k]), normals[3 * v2 + k]);
+                    sn[3 * tid + k] = __fdiv_rn(s, 3.0f);
+                }
+            }
+        }
+        __syncthreads();
+        if (tid < n) {
+            uint16_t* r = rec + tid * (kStlRecord / 2);
+#pragma unroll
+            for (int k = 0; k < 3; ++k) put_float(r, k, sn[3 * tid + k]);
+#pragma unroll
+            for (int k = 0; k < 9; ++k) put_float(r, 3 + k, sc[9 * tid + k]);
+            r[24] = 0;   // the unused 2-byte attribute
+        }
+        __syncthreads();
+        const uint32_t bytes = (uint32_t)kStlRecord * n;
+        uint8_t* dst = out + (uint64_t)kStlRecord * t0;
+        const uint4* src4 = reinterpret_cast<const uint4*>(rec);
+        uint4* dst4 = reinterpret_cast<uint4*>(dst);
+        for (uint32_t i = tid; i < bytes / 16; i += kStlTile) dst4[i] = src4[i];
+        const uint8_t* src1 = reinterpret_cast<const uint8_t*>(rec);
+        for (uint32_t i = bytes / 16 * 16 + tid; i < bytes; i += kStlTile) dst[i] = src1[i];
+        __syncthreads();
+    }
+}
+
+}  // namespace
+
+cudaError_t launch_stl_records(const float* coords, const float* normals, const uint32_t* conn, uint64_t nverts,
+                               uint64_t ntri, int mode, uint8_t* out, int* bad_index, const Launch& L)
+{
+    if (ntri == 0) return cudaSuccess;
+    const uint64_t tiles = (ntri + kStlTile - 1) / kStlTile;
+    // resident CTAs: 25 KB of shared memory and 256 threads each, a few per SM
+    const uint64_t cap = (uint64_t)L.num_sms * 8;
+    const unsigned grid = (unsigned)(tiles < cap ? tiles : cap);
+    prof_begin(L, "stl_records");
+    k_stl_records<<<grid, kStlTile, 0, L.stream>>>(coords, normals, conn, nverts, ntri, mode, out, bad_index);
+    prof_end(L);
+    *L.counter += 1;
+    return cudaGetLastError();
+}
+
+}  // namespace kvsmc
+
+namespace {
+
+using kvsmc_host::fail;
+
+kvsmc_status check_mesh(kvsmc_context* ctx, int32_t mode, const float* d_coords, const float* d_normals,
+                        const uint32_t* d_connections, uint64_t ntriangles)
+{
+    if (mode != KVSMC_DUP_POLYGON_NORMAL && mode != KVSMC_SHARED_POLYGON_NORMAL && mode != KVSMC_SHARED_VERTEX_NORMAL)
+        return fail(ctx, KVSMC_ERR_INVALID_ARGUMENT, "stl: bad mode %d", (int)mode);
+    if (ntriangles && (!d_coords || !d_normals || (mode != KVSMC_DUP_POLYGON_NORMAL && !d_connections)))
+        return fail(ctx, KVSMC_ERR_INVALID_ARGUMENT, "stl: null mesh array");
+    return KVSMC_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+kvsmc_status kvsmc_stl_records(kvsmc_context* ctx, int32_t mode, const float* d_coords, const float* d_normals,
+                               const uint32_t* d_connections, uint64_t nvertices, uint64_t ntriangles, void* d_out)
+{
+    if (!ctx) return KVSMC_ERR_INVALID_ARGUMENT;
+    kvsmc_status st = check_mesh(ctx, mode, d_coords, d_normals, d_connections, ntriangles);
+    if (st) return st;
+    if (ntriangles == 0) return KVSMC_OK;
+    if (!d_out || (reinterpret_cast<uintptr_t>(d_out) & 15u))
+        return fail(ctx, KVSMC_ERR_INVALID_ARGUMENT, "stl: output must be 16-byte aligned device memory");
+    KVSMC_CUDA(ctx, cudaSetDevice(ctx->device));
+    if (!ctx->d_flag) KVSMC_CUDA(ctx, cudaMalloc(&ctx->d_flag, sizeof(int)));
+    int* bad = ctx->d_flag;
+    KVSMC_CUDA(ctx, cudaMemsetAsync(bad, 0, sizeof(int), ctx->stream));
+    KVSMC_CUDA(ctx, kvsmc::launch_stl_records(d_coords, d_normals, d_connections, nvertices, ntriangles, mode,
+                                              static_cast<uint8_t*>(d_out), bad, kvsmc_host::launch_of(ctx)));
+    int h_bad = 0;
+    KVSMC_CUDA(ctx, cudaMemcpyAsync(&h_bad, bad, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
+    KVSMC_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    if (h_bad) return fail(ctx, KVSMC_ERR_INVALID_ARGUMENT, "stl: a connection index is >= nvertices");
+    return KVSMC_OK;
+}
+
+kvsmc_status kvsmc_write_stl(kvsmc_context* ctx, const char* path, int32_t mode, const float* d_coords,
+                             const float* d_normals, const uint32_t* d_connections, uint64_t nvertices,
+                             uint64_t ntriangles)
+{
+    if (!ctx || !path) return KVSMC_ERR_INVALID_ARGUMENT;
+    kvsmc_status st = check_mesh(ctx, mode, d_coords, d_normals, d_connections, ntriangles);
+    if (st) return st;
+    if (ntriangles > 0xffffffffull)
+        return fail(ctx, KVSMC_ERR_TOO_LARGE, "stl: %llu triangles do not fit the format's 32-bit count",
+                    (unsigned long long)ntriangles);
+    KVSMC_CUDA(ctx, cudaSetDevice(ctx->device));
+    FILE* f = std::fopen(path, "wb");
+    if (!f) return fail(ctx, KVSMC_ERR_INVALID_ARGUMENT, "stl: cannot open %s", path);
+    char header[84];
+    std::memset(header, 0, sizeof header);
+    std::snprintf(header, 80, "Generated by KVS");
+    const uint32_t count = (uint32_t)ntriangles;
+    std::memcpy(header + 80, &count, 4);   // little-endian host (x86-64, aarch64)
+    bool ok = std::fwrite(header, 1, 84, f) == 84;
+    // chunks of 2^20 triangles, double-buffered: chunk i is serialised and
+    // copied while chunk i - 1 is written
+    const uint64_t chunk = 1ull << 20;
+    const uint64_t nchunks = (ntriangles + chunk - 1) / chunk;
+    uint8_t* d_buf[2] = {nullptr, nullptr};
+    uint8_t* h_buf[2] = {nullptr, nullptr};
+    cudaEvent_t done[2] = {nullptr, nullptr};
+    int* bad = nullptr;
+    int* h_bad = nullptr;
+    cudaError_t e = cudaSuccess;
+    if (nchunks) {
+        const size_t bytes = (size_t)(ntriangles < chunk ? ntriangles : chunk) * kvsmc::kStlRecordBytes;
+        for (int b = 0; b < 2 && e == cudaSuccess; ++b) {
+            e = cudaMalloc(&d_buf[b], bytes);
+            if (e == cudaSuccess) e = cudaMallocHost(&h_buf[b], bytes);
+            if (e == cudaSuccess) e = cudaEventCreateWithFlags(&done[b], cudaEventDisableTiming);
+        }
+        if (e == cudaSuccess) e = cudaMalloc(&bad, sizeof(int));
+        if (e == cudaSuccess) e = cudaMallocHost(&h_bad, sizeof(int));
+        if (e == cudaSuccess) e = cudaMemsetAsync(bad, 0, sizeof(int), ctx->stream);
+    }
+    const kvsmc::Launch L = kvsmc_host::launch_of(ctx);
+    auto chunk_tris = [&](uint64_t i) { return (i + 1) * chunk <= ntriangles ? chunk : ntriangles - i * chunk; };
+    for (uint64_t i = 0; i <= nchunks && e == cudaSuccess && ok; ++i) {
+        if (i < nchunks) {
+            const int b = (int)(i & 1);
+            const uint64_t t0 = i * chunk, nt = chunk_tris(i);
+            const float* c = mode == KVSMC_DUP_POLYGON_NORMAL ? d_coords + 9 * t0 : d_coords;
+            const float* nrm = mode == KVSMC_SHARED_VERTEX_NORMAL ? d_normals : d_normals + 3 * t0;
+            const uint32_t* cn = mode == KVSMC_DUP_POLYGON_NORMAL ? nullptr : d_connections + 3 * t0;
+            // the host buffer of this parity was written out before (chunk i - 2)
+            e = kvsmc::launch_stl_records(c, nrm, cn, nvertices, nt, mode, d_buf[b], bad, L);
+            if (e == cudaSuccess)
+                e = cudaMemcpyAsync(h_buf[b], d_buf[b], nt * kvsmc::kStlRecordBytes, cudaMemcpyDeviceToHost,
+                                    ctx->stream);
+            if (e == cudaSuccess) e = cudaEventRecord(done[b], ctx->stream);
+        }
+        if (i > 0 && e == cudaSuccess) {
+            const int b = (int)((i - 1) & 1);
+            e = cudaEventSynchronize(done[b]);
+            if (e == cudaSuccess) {
+                const size_t nb = chunk_tris(i - 1) * kvsmc::kStlRecordBytes;
+                ok = std::fwrite(h_buf[b], 1, nb, f) == nb;
+            }
+        }
+    }
+    if (e == cudaSuccess && nchunks) {
+        e = cudaMemcpyAsync(h_bad, bad, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream);
+        if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
+    }
+    const bool closed = std::fclose(f) == 0;
+    const int was_bad = (e == cudaSuccess && h_bad) ? *h_bad : 0;
+    for (int b = 0; b < 2; ++b) {
+        if (d_buf[b]) cudaFree(d_buf[b]);
+        if (h_buf[b]) cudaFreeHost(h_buf[b]);
+        if (done[b]) cudaEventDestroy(done[b]);
+    }
+    if (bad) cudaFree(bad);
+    if (h_bad) cudaFreeHost(h_bad);
+    if (e != cudaSuccess)
+        return fail(ctx, e == cudaErrorMemoryAllocation ? KVSMC_ERR_OUT_OF_MEMORY : KVSMC_ERR_CUDA, "stl: %s",
+                    cudaGetErrorString(e));
+    if (!ok || !closed) return fail(ctx, KVSMC_ERR_INVALID_ARGUMENT, "stl: writing %s failed", path);
+    if (was_bad) return fail(ctx, KVSMC_ERR_INVALID_ARGUMENT, "stl: a connection index is >= nvertices");
+    return KVSMC_OK;
+}
+
+kvsmc_status kvsmc_write_stl_host(kvsmc_context* ctx, const char* path, int32_t mode, const float* coords,
+                                  uint64_t ncoords, const float* normals, uint64_t nnormals,
+                                  const uint32_t* connections, uint64_t nconnections)
+{
+    if (!ctx || !path) return KVSMC_ERR_INVALID_ARGUMENT;
+    if (mode != KVSMC_DUP_POLYGON_NORMAL && mode != KVSMC_SHARED_POLYGON_NORMAL && mode != KVSMC_SHARED_VERTEX_NORMAL)
+        return fail(ctx, KVSMC_ERR_INVALID_ARGUMENT, "stl: bad mode %d", (int)mode);
+    const bool dup = mode == KVSMC_DUP_POLYGON_NORMAL;
+    const uint64_t ntri = dup ? ncoords / 9 : nconnections / 3;
+    const uint64_t nverts = ncoords / 3;
+    const uint64_t need_normals = mode == KVSMC_SHARED_VERTEX_NORMAL ? 3 * nverts : 3 * ntri;
+    if (nnormals < need_normals || (ntri && (!coords || !normals || (!dup && !connections))))
+        return fail(ctx, KVSMC_ERR_INVALID_ARGUMENT, "stl: mesh arrays of inconsistent sizes");
+    KVSMC_CUDA(ctx, cudaSetDevice(ctx->device));
+    float* d_c = nullptr;
+    float* d_n = nullptr;
+    uint32_t* d_k = nullptr;
+    cudaError_t e = cudaSuccess;
+    if (ntri) {
+        e = cudaMalloc(&d_c, ncoords * sizeof(float));
+        if (e == cudaSuccess) e = cudaMalloc(&d_n, need_normals * sizeof(float));
+        if (e == cudaSuccess && !dup) e = cudaMalloc(&d_k, 3 * ntri * sizeof(uint32_t));
+        if (e == cudaSuccess) e = cudaMemcpyAsync(d_c, coords, ncoords * sizeof(float), cudaMemcpyHostToDevice, ctx->stream);
+        if (e == cudaSuccess)
+            e = cudaMemcpyAsync(d_n, normals, need_normals * sizeof(float), cudaMemcpyHostToDevice, ctx->stream);
+        if (e == cudaSuccess && !dup)
+            e = cudaMemcpyAsync(d_k, connections, 3 * ntri * sizeof(uint32_t), cudaMemcpyHostToDevice, ctx->stream);
+    }
+    kvsmc_status st = KVSMC_OK;
+    if (e != cudaSuccess)
+        st = fail(ctx, e == cudaErrorMemoryAllocation ? KVSMC_ERR_OUT_OF_MEMORY : KVSMC_ERR_CUDA, "stl: %s",
+                  cudaGetErrorString(e));
+    else
+        st = kvsmc_write_stl(ctx, path, mode, d_c, d_n, d_k, nverts, ntri);
+    cudaStreamSynchronize(ctx->stream);
+    if (d_c) cudaFree(d_c);
+    if (d_n) cudaFree(d_n);
+    if (d_k) cudaFree(d_k);
+    return st;
+}
+
+}  // extern "C"

@@ -111,6 +111,13 @@ cudaError_t launch_unit_scan(const StreamGroup* d_groups, int ngroups, uint32_t 
 cudaError_t launch_iso_totals(const StreamIso* d_isos, int n, const uint64_t* d_plane_base, const uint64_t* d_total,
                               uint64_t* d_totals, const Launch& L);
 
+// ---- binary STL records (export.cu): 50 bytes per triangle; bad_index: a
+// device word set to 1 when a connection index is >= nverts (that vertex
+// then reads as vertex 0)
+constexpr uint64_t kStlRecordBytes = 50;
+cudaError_t launch_stl_records(const float* coords, const float* normals, const uint32_t* conn, uint64_t nverts,
+                               uint64_t ntri, int mode, uint8_t* out, int* bad_index, const Launch& L);
+
 // ---- diagnostics (selftest.cu)
 cudaError_t launch_selftest(uint64_t n, uint64_t seed, unsigned long long* d_counters, const Launch& L);
 

@@ -84,6 +84,9 @@ def lib():
             C.c_int, C.c_int, C.c_void_p, C.c_uint, C.c_uint, C.c_uint,
             C.c_double, C.c_int, C.c_int, C.c_int, C.c_double, C.c_double,
             C.c_int, C.c_int, C.c_float, C.c_float, C.POINTER(_Result)]
+        _lib.kvsref_marching_cubes_stl.restype = C.c_int
+        _lib.kvsref_marching_cubes_stl.argtypes = [
+            C.c_int, C.c_void_p, C.c_uint, C.c_uint, C.c_uint, C.c_double, C.c_int, C.c_int, C.c_char_p]
         _lib.kvsref_free.argtypes = [C.POINTER(_Result)]
         _lib.kvsref_hydrogen.argtypes = [C.c_uint, C.c_void_p]
         _lib.kvsref_default_colormap.argtypes = [C.c_int, C.c_void_p]
@@ -177,6 +180,29 @@ def isosurface(values, form, isolevel=0.0, normal_type="polygon", duplication=Tr
     if st != 0:
         raise RuntimeError("kvsref_isosurface failed")
     return _collect(r)
+
+
+def marching_cubes_stl(values, isolevel, normal_type="polygon", duplication=True, path=None):
+    """The reference MarchingCubes result exported by PolygonExporter<kvs::Stl>
+    as a binary STL file; returns the file's bytes."""
+    import tempfile
+    v = np.ascontiguousarray(values)
+    nz, ny, nx = v.shape
+    own = path is None
+    if own:
+        fd, path = tempfile.mkstemp(suffix=".stl")
+        os.close(fd)
+    try:
+        st = lib().kvsref_marching_cubes_stl(dtype_code(v.dtype), v.ctypes.data, nx, ny, nz, float(isolevel),
+                                             0 if normal_type == "polygon" else 1, 1 if duplication else 0,
+                                             path.encode())
+        if st != 0:
+            raise RuntimeError(f"kvsref_marching_cubes_stl failed ({st})")
+        with open(path, "rb") as f:
+            return f.read()
+    finally:
+        if own:
+            os.remove(path)
 
 
 def hydrogen(res):

@@ -12,6 +12,8 @@
 #include <kvs/PolygonObject>
 #include <kvs/MarchingCubes>
 #include <kvs/Isosurface>
+#include <kvs/PolygonExporter>
+#include <kvs/Stl>
 #include <kvs/TransferFunction>
 #include <kvs/HydrogenVolumeData>
 #include <kvs/ValueArray>
@@ -181,6 +183,39 @@ int kvsref_marching_cubes(
     delete mc;
     delete vol;
     return 0;
+}
+
+/*
+ * kvs::MarchingCubes on a uniform volume, then the reference's binary STL export
+ * of the result: PolygonExporter<kvs::Stl>::exec (PolygonExporter.cpp:78-176)
+ * and Stl::write with the Binary file type (Stl.cpp:170-199, 490-540).
+ * Returns 0 when the file was written.
+ */
+int kvsref_marching_cubes_stl(
+    int dtype, const void* values, unsigned nx, unsigned ny, unsigned nz,
+    double isolevel, int normal_type, int duplication, const char* path )
+{
+    const size_t n = size_t( nx ) * ny * nz;
+    kvs::AnyValueArray vals = Values( dtype, values, n );
+    if ( vals.size() != n ) return -1;
+    kvs::TransferFunction tfunc( 256 );
+    const auto ntype = normal_type == 0 ? kvs::PolygonObject::PolygonNormal : kvs::PolygonObject::VertexNormal;
+    auto* vol = new kvs::StructuredVolumeObject();
+    vol->setVeclen( 1 );
+    vol->setResolution( kvs::Vec3ui( nx, ny, nz ) );
+    vol->setValues( vals );
+    vol->setGridTypeToUniform();
+    auto* mc = new kvs::MarchingCubes( vol, isolevel, ntype, duplication != 0, tfunc );
+    kvs::PolygonExporter<kvs::Stl> exporter( mc );   // the exporter's one constructor runs exec
+    int rc = -2;
+    if ( exporter.kvs::ExporterBase::isSuccess() )
+    {
+        exporter.setFileType( kvs::Stl::Binary );
+        rc = exporter.write( path ) ? 0 : -3;
+    }
+    delete mc;
+    delete vol;
+    return rc;
 }
 
 /*

@@ -4,11 +4,13 @@ kvs::Isosurface.
 Runs the reference mappers compiled from their own sources (oracle/_ref, built
 by oracle/Makefile.ref) on small seeded inputs and stores inputs + outputs in
 tests/golden/golden.npz (case list tests/golden/cases.json) and
-tests/golden/isosurface.npz (tests/golden/isosurface.json).  The reference
+tests/golden/isosurface.npz (tests/golden/isosurface.json), and binary STL
+files written by the reference PolygonExporter<kvs::Stl> in tests/golden/stl.npz
+(tests/golden/stl.json).  The reference
 ships no tests or golden vectors of its own, so these fixtures pin the oracle
 restatement and the CUDA path on hosts where the reference is absent.
 
-    python tests/golden/make_golden.py [marching_cubes] [isosurface]   (default: both)
+    python tests/golden/make_golden.py [marching_cubes] [isosurface] [stl]   (default: all)
 """
 import json
 import os
@@ -109,12 +111,50 @@ def write_isosurface():
     print(f"{len(manifest)} isosurface cases")
 
 
+def stl_cases():
+    """(name, volume, isolevel, normal_type, duplication) for the binary STL fixtures."""
+    rng = np.random.default_rng(88)
+    h = ref.hydrogen(32)
+    x, y, z = np.meshgrid(np.arange(20), np.arange(18), np.arange(16), indexing="xy")
+    blob = np.exp(-((x - 9.3) ** 2 + (y - 8.1) ** 2 + (z - 7.7) ** 2) / (2 * 5.0 ** 2)).transpose(2, 0, 1)
+    blob = np.ascontiguousarray(blob).astype(np.float32)
+    noise = rng.integers(0, 255, (9, 10, 11)).astype(np.uint8)
+    return [
+        ("hydrogen32_dup", h, 100.5, "polygon", True),
+        ("hydrogen32_shared", h, 100.5, "polygon", False),
+        ("hydrogen32_vertex", h, 100.5, "vertex", False),
+        ("blob_f32_dup", blob, 0.5, "polygon", True),
+        ("blob_f32_vertex", blob, 0.37, "vertex", True),
+        ("noise_u8_dup", noise, 127.5, "polygon", True),
+        ("noise_u8_vertex", noise, 127.5, "vertex", False),
+        ("constant_f32", np.full((4, 5, 6), 2.0, np.float32), 2.0, "polygon", True),
+    ]
+
+
+def write_stl():
+    arrays, manifest = {}, []
+    for name, v, iso, nt, dup in stl_cases():
+        arrays[f"{name}__input"] = v
+        r = ref.marching_cubes(v, iso, nt, dup)
+        for fld in ("coords", "normals", "connections"):
+            arrays[f"{name}__{fld}"] = r[fld]
+        arrays[f"{name}__stl"] = np.frombuffer(ref.marching_cubes_stl(v, iso, nt, dup), np.uint8)
+        manifest.append(dict(case=name, isolevel=iso, normal_type=nt, duplication=dup,
+                             normal_type_out=r["normal_type"], ntriangles=int(arrays[f"{name}__stl"][80:84].view("<u4")[0])))
+    np.savez_compressed(os.path.join(HERE, "stl.npz"), **arrays)
+    with open(os.path.join(HERE, "stl.json"), "w") as f:
+        json.dump(manifest, f, indent=0)
+    print(f"{len(manifest)} stl cases")
+
+
 def main():
     if not ref.available():
         ref.build()
-    parts = sys.argv[1:] or ["marching_cubes", "isosurface"]
+    parts = sys.argv[1:] or ["marching_cubes", "isosurface", "stl"]
     if "isosurface" in parts:
         write_isosurface()
+    if "stl" in parts:
+        write_stl()
     if "marching_cubes" not in parts:
         return
     arrays = {}
