@@ -186,7 +186,7 @@ class PolygonObject(ObjectBase):
         self._coords = np.zeros(0, np.float32)
         self._normals = np.zeros(0, np.float32)
         self._connections = np.zeros(0, np.uint32)
-        self._colors = np.array([255, 255, 255], np.uint8)
+        self._colors = np.zeros(0, np.uint8)           # no colour until a mapper sets one
         self._opacities = np.array([255], np.uint8)   # PolygonObject.cpp:154-157
         self._polygon_type = 5                         # UnknownPolygonType
         self._normal_type = 2                          # UnknownNormalType
