@@ -8,7 +8,7 @@ volume: the fused count launch, the scan, the fused emit launch, with output
 written to HBM.  `value` = cells x isovalues / s (Mcells/s).
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
-                    [--workload sweep1024|sweep512|uneven200|serve|heavy|blobs128] [--tune]
+                    [--workload sweep1024|sweep512|uneven200|serve|heavy|stl512|stl384|blobs128] [--tune]
 
 --tune runs the launch-shape autotuner (kvsmc_autotune, a few seconds) on the
 bench's context before measuring; without it the built-in rules decide.
@@ -66,6 +66,13 @@ WORKLOADS = {
                        "2.8e10 triangles / 1.3 TB for 4 isovalues, against the stated ~1e9), 4 isovalues at the "
                        "45/50/55/60th percentiles in one batched call (~1.1e9 triangles), duplication=true, "
                        "PolygonNormal"),
+    "stl512": dict(shape=(512, 512, 512), kind="stl", isos=[0.2 + 0.04 * k for k in range(16)],
+                   desc="binary STL serialisation on the GPU of the 16 duplicated-vertex meshes of the 512^3 "
+                        "float32 fBm sweep (80 M triangles, 3.9 GB in, 4.0 GB of 50-byte records out per step); "
+                        "e2e = kvsmc_write_stl of all 16 to /dev/null (GPU records, copy to pinned memory, fwrite)"),
+    "stl384": dict(shape=(384, 384, 384), kind="stl", isos=[0.2 + 0.04 * k for k in range(16)],
+                   desc="binary STL serialisation of the 16 meshes of a 384^3 float32 fBm sweep (the profiling "
+                        "case of stl512: same kernel, ~3.5 GB on the device, each launch larger than L2)"),
     "blobs128": dict(shape=(128, 128, 128), kind="blobs", isos=[0.5],
                      desc="128^3 float32, 4 Gaussian blobs (sigma 8..24) + U[-0.01,0.01] noise, iso 0.5, "
                           "duplication=true, PolygonNormal"),
@@ -201,6 +208,119 @@ def maybe_tune(args, ctx):
     changed = [r for r in table if any(r[f] for f in T.FIELDS)]
     return {"seconds": round(time.time() - t0, 2), "entries": len(table), "entries_changed": len(changed),
             "changed": [{k: r[k] for k in ("dtype", "size_class") + T.FIELDS} for r in changed]}
+
+
+def run_stl(args, rank, world, local):
+    """kvsmc_stl_records over the device meshes of a multi-isovalue sweep."""
+    import time
+
+    import torch
+
+    from kvs_gb300 import _abi
+    from kvs_gb300.export import stl_records_device, write_stl_device
+
+    torch.cuda.set_device(local)
+    w = WORKLOADS[args.workload]
+    ctx = _abi.Context(local)
+    stream = torch.cuda.Stream()
+    ctx.set_stream(stream.cuda_stream)
+    field = make_field(dict(w, kind="fbm"), "cuda")
+    torch.cuda.synchronize()
+    vol = _abi.DeviceVolume.from_device(ctx, field.data_ptr(), np.float32, field.shape)
+    del field
+    torch.cuda.empty_cache()
+    n = len(w["isos"])
+    reqs = (_abi.Request * n)()
+    for i, iso in enumerate(w["isos"]):
+        reqs[i].volume = vol.handle
+        reqs[i].params = _abi.make_params(iso, _abi.MODE_DUP_POLYGON_NORMAL)
+    ctx.check(ctx.lib.kvsmc_count_batch(ctx.handle, reqs, n), "count")
+    meshes = []
+    for i in range(n):
+        s = reqs[i].sizes
+        c = torch.empty(max(1, s.ncoords), dtype=torch.float32, device="cuda")
+        nn = torch.empty(max(1, s.nnormals), dtype=torch.float32, device="cuda")
+        meshes.append((c, nn, s.ntriangles))
+        reqs[i].d_coords, reqs[i].coords_capacity = c.data_ptr(), s.ncoords
+        reqs[i].d_normals, reqs[i].normals_capacity = nn.data_ptr(), s.nnormals
+    ctx.check(ctx.lib.kvsmc_extract_batch(ctx.handle, reqs, n), "extract")
+    ntri = sum(m[2] for m in meshes)
+    offs = np.cumsum([0] + [50 * m[2] for m in meshes])
+    out = torch.empty(int(offs[-1]) + 16 * n, dtype=torch.uint8, device="cuda")
+    base = out.data_ptr()
+    dst = [base + ((int(o) + 15) // 16) * 16 + 16 * i for i, o in enumerate(offs[:-1])]   # 16-byte aligned
+
+    def step():
+        for (c, nn, t), d in zip(meshes, dst):
+            stl_records_device(ctx, _abi.MODE_DUP_POLYGON_NORMAL, c.data_ptr(), nn.data_ptr(), None, 3 * t, t, d)
+
+    for _ in range(args.warmup):
+        step()
+    torch.cuda.synchronize()
+    clocks = Clocks(local)
+    clocks.start()
+    ctx.profile_enable(True)
+    launches0 = ctx.kernel_launches
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for _ in range(args.steps):
+        step()
+    e1.record(stream)
+    torch.cuda.synchronize()
+    ms = barrier_max(e0.elapsed_time(e1), world) / args.steps
+    prof = ctx.profile_read()
+    ctx.profile_enable(False)
+    launches = ctx.kernel_launches - launches0
+    clk = clocks.stop()
+    hbm, peak_kind = peaks()
+    algo = 98 * ntri                      # 48 B of coords + normals read, 50 B of records written
+    k_launches, k_ms = prof.get("stl_records", (0, 0.0))
+    k_ms_step = k_ms / args.steps
+    achieved = algo / (k_ms_step * 1e-3) / 1e9
+    e2e = None
+    if not args.no_e2e:
+        steps = max(1, min(args.steps, 3))
+        write_stl_device(ctx, "/dev/null", 0, meshes[0][0].data_ptr(), meshes[0][1].data_ptr(), None,
+                         3 * meshes[0][2], meshes[0][2])
+        t0 = time.perf_counter()
+        for _ in range(steps):
+            for c, nn, t in meshes:
+                write_stl_device(ctx, "/dev/null", 0, c.data_ptr(), nn.data_ptr(), None, 3 * t, t)
+        t_e2e = (time.perf_counter() - t0) / steps
+        e2e = {"value": round(ntri / t_e2e / 1e6, 1), "unit": "Mtris/s", "h2d_bytes_per_step": 0,
+               "d2h_bytes_per_step": int(50 * ntri + 84 * n), "api": "kvsmc_write_stl x%d (to /dev/null)" % n,
+               "ms_per_step": round(t_e2e * 1e3, 2)}
+    return {
+        "metric": "Mtris/s", "value": round(ntri * world / (ms * 1e-3) / 1e6, 1), "unit": "Mtris/s",
+        "n_gpus": world, "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(ms, 4),
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32 -> bytes",
+        "data": "synthetic (seeded fBm meshes extracted on the device)",
+        "config": {"workload": w["desc"], "meshes": n, "triangles": int(ntri),
+                   "cache": "inputs larger than L2 (%.1f GB of meshes)" % (48 * ntri / 1e9)},
+        "roofline": {"kernel": "stl_records", "bound": "hbm", "achieved": round(achieved, 1), "peak": hbm,
+                     "peak_kind": peak_kind, "unit": "GB/s", "frac": round(achieved / hbm, 4),
+                     "algorithmic_bytes_per_launch": int(algo / max(1, k_launches / args.steps)),
+                     "launch_ms": round(k_ms / max(1, k_launches), 4), "traffic": None},
+        "kernels": {k: {"launches": v[0], "ms": round(v[1], 3)} for k, v in prof.items()},
+        "e2e": e2e, "gpu_launches": int(launches), "clocks": clk,
+        "_sample_mesh": (meshes[0][0][:9 * min(meshes[0][2], 1 << 20)].cpu().numpy(),
+                         meshes[0][1][:3 * min(meshes[0][2], 1 << 20)].cpu().numpy()),
+    }
+
+
+def run_stl_cpu(mesh):
+    """The STL restatement (oracle/export.py) on one host core, on a 1 M-triangle sample."""
+    import time
+
+    from oracle import export as E
+    coords, normals = mesh
+    t0 = time.perf_counter()
+    reps = 0
+    while time.perf_counter() - t0 < 3.0 or reps < 1:
+        E.stl_binary(coords, normals, np.zeros(0, np.uint32), E.POLYGON_NORMAL)
+        reps += 1
+    t = (time.perf_counter() - t0) / reps
+    return normals.size // 3 / t / 1e6, t * reps, normals.size // 3
 
 
 def run_ours(args, rank, world, local):
@@ -807,6 +927,15 @@ def main():
         dist.init_process_group("nccl")
     if args.impl == "reference":
         line = run_reference(args, rank, world)
+    elif WORKLOADS[args.workload]["kind"] == "stl":
+        line = run_stl(args, rank, world, local)
+        mesh = line.pop("_sample_mesh")
+        if rank == 0 and world == 1 and not args.no_cpu:
+            v, t, nt = run_stl_cpu(mesh)
+            line["cpu_baseline"] = {"value": round(v, 1), "unit": "Mtris/s", "cores": 1, "kind": "port",
+                                    "sample": f"{nt} triangles of the first mesh, oracle/export.py (numpy "
+                                              f"restatement of PolygonExporter<Stl> + Stl::write_binary), "
+                                              f"{t:.1f} s on 1 host core"}
     elif WORKLOADS[args.workload]["kind"] == "serve":
         line = run_serve(args, rank, world, local)
     elif WORKLOADS[args.workload]["kind"] == "batch":

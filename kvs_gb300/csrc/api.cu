@@ -470,6 +470,12 @@ void kvsmc_destroy(kvsmc_context* ctx)
     if (ctx->host_vol) { cudaFree(ctx->host_vol->dev); delete ctx->host_vol; }
     if (ctx->scratch) cudaFree(ctx->scratch);
     if (ctx->d_flag) cudaFree(ctx->d_flag);
+    if (ctx->h_flag) cudaFreeHost(ctx->h_flag);
+    for (int b = 0; b < 2; ++b) {
+        if (ctx->stl_dbuf[b]) cudaFree(ctx->stl_dbuf[b]);
+        if (ctx->stl_hbuf[b]) cudaFreeHost(ctx->stl_hbuf[b]);
+        if (ctx->stl_ev[b]) cudaEventDestroy(ctx->stl_ev[b]);
+    }
     if (ctx->out_arena) cudaFree(ctx->out_arena);
     if (ctx->h_small) cudaFreeHost(ctx->h_small);
     if (ctx->h_stage) cudaFreeHost(ctx->h_stage);

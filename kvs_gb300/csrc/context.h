@@ -45,6 +45,12 @@ struct kvsmc_context {
     cudaEvent_t join_ev[kAux] = {};
     bool aux_ready = false;
     int* d_flag = nullptr;       // device word for checks of export calls (created on first use)
+    int* h_flag = nullptr;       // pinned copy of it
+    // export staging: two device record buffers, two pinned host buffers (grow-only)
+    uint8_t* stl_dbuf[2] = {};
+    uint8_t* stl_hbuf[2] = {};
+    size_t stl_buf_bytes = 0;
+    cudaEvent_t stl_ev[2] = {};
     // streaming launch shapes: the tuning table, or one forced shape
     std::vector<kvsmc_tune_entry> tuning;
     bool tune_forced = false;

@@ -174,6 +174,32 @@ kvsmc_status kvsmc_write_stl(kvsmc_context* ctx, const char* path, int32_t mode,
         return fail(ctx, KVSMC_ERR_TOO_LARGE, "stl: %llu triangles do not fit the format's 32-bit count",
                     (unsigned long long)ntriangles);
     KVSMC_CUDA(ctx, cudaSetDevice(ctx->device));
+    // chunks of 2^20 triangles, double-buffered through the context's staging
+    // buffers: chunk i is serialised and copied while chunk i - 1 is written
+    const uint64_t chunk = 1ull << 20;
+    const uint64_t nchunks = (ntriangles + chunk - 1) / chunk;
+    if (nchunks) {
+        const size_t bytes = (size_t)(ntriangles < chunk ? ntriangles : chunk) * kvsmc::kStlRecordBytes;
+        if (bytes > ctx->stl_buf_bytes) {
+            KVSMC_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+            for (int b = 0; b < 2; ++b) {
+                if (ctx->stl_dbuf[b]) cudaFree(ctx->stl_dbuf[b]);
+                if (ctx->stl_hbuf[b]) cudaFreeHost(ctx->stl_hbuf[b]);
+                ctx->stl_dbuf[b] = nullptr;
+                ctx->stl_hbuf[b] = nullptr;
+            }
+            ctx->stl_buf_bytes = 0;
+            for (int b = 0; b < 2; ++b) {
+                KVSMC_CUDA(ctx, cudaMalloc(&ctx->stl_dbuf[b], bytes));
+                KVSMC_CUDA(ctx, cudaMallocHost(&ctx->stl_hbuf[b], bytes));
+                if (!ctx->stl_ev[b]) KVSMC_CUDA(ctx, cudaEventCreateWithFlags(&ctx->stl_ev[b], cudaEventDisableTiming));
+            }
+            ctx->stl_buf_bytes = bytes;
+        }
+        if (!ctx->d_flag) KVSMC_CUDA(ctx, cudaMalloc(&ctx->d_flag, sizeof(int)));
+        if (!ctx->h_flag) KVSMC_CUDA(ctx, cudaMallocHost(&ctx->h_flag, sizeof(int)));
+        KVSMC_CUDA(ctx, cudaMemsetAsync(ctx->d_flag, 0, sizeof(int), ctx->stream));
+    }
     FILE* f = std::fopen(path, "wb");
     if (!f) return fail(ctx, KVSMC_ERR_INVALID_ARGUMENT, "stl: cannot open %s", path);
     char header[84];
@@ -182,29 +208,9 @@ kvsmc_status kvsmc_write_stl(kvsmc_context* ctx, const char* path, int32_t mode,
     const uint32_t count = (uint32_t)ntriangles;
     std::memcpy(header + 80, &count, 4);   // little-endian host (x86-64, aarch64)
     bool ok = std::fwrite(header, 1, 84, f) == 84;
-    // chunks of 2^20 triangles, double-buffered: chunk i is serialised and
-    // copied while chunk i - 1 is written
-    const uint64_t chunk = 1ull << 20;
-    const uint64_t nchunks = (ntriangles + chunk - 1) / chunk;
-    uint8_t* d_buf[2] = {nullptr, nullptr};
-    uint8_t* h_buf[2] = {nullptr, nullptr};
-    cudaEvent_t done[2] = {nullptr, nullptr};
-    int* bad = nullptr;
-    int* h_bad = nullptr;
-    cudaError_t e = cudaSuccess;
-    if (nchunks) {
-        const size_t bytes = (size_t)(ntriangles < chunk ? ntriangles : chunk) * kvsmc::kStlRecordBytes;
-        for (int b = 0; b < 2 && e == cudaSuccess; ++b) {
-            e = cudaMalloc(&d_buf[b], bytes);
-            if (e == cudaSuccess) e = cudaMallocHost(&h_buf[b], bytes);
-            if (e == cudaSuccess) e = cudaEventCreateWithFlags(&done[b], cudaEventDisableTiming);
-        }
-        if (e == cudaSuccess) e = cudaMalloc(&bad, sizeof(int));
-        if (e == cudaSuccess) e = cudaMallocHost(&h_bad, sizeof(int));
-        if (e == cudaSuccess) e = cudaMemsetAsync(bad, 0, sizeof(int), ctx->stream);
-    }
     const kvsmc::Launch L = kvsmc_host::launch_of(ctx);
     auto chunk_tris = [&](uint64_t i) { return (i + 1) * chunk <= ntriangles ? chunk : ntriangles - i * chunk; };
+    cudaError_t e = cudaSuccess;
     for (uint64_t i = 0; i <= nchunks && e == cudaSuccess && ok; ++i) {
         if (i < nchunks) {
             const int b = (int)(i & 1);
@@ -213,38 +219,36 @@ kvsmc_status kvsmc_write_stl(kvsmc_context* ctx, const char* path, int32_t mode,
             const float* nrm = mode == KVSMC_SHARED_VERTEX_NORMAL ? d_normals : d_normals + 3 * t0;
             const uint32_t* cn = mode == KVSMC_DUP_POLYGON_NORMAL ? nullptr : d_connections + 3 * t0;
             // the host buffer of this parity was written out before (chunk i - 2)
-            e = kvsmc::launch_stl_records(c, nrm, cn, nvertices, nt, mode, d_buf[b], bad, L);
+            e = kvsmc::launch_stl_records(c, nrm, cn, nvertices, nt, mode, ctx->stl_dbuf[b], ctx->d_flag, L);
             if (e == cudaSuccess)
-                e = cudaMemcpyAsync(h_buf[b], d_buf[b], nt * kvsmc::kStlRecordBytes, cudaMemcpyDeviceToHost,
-                                    ctx->stream);
-            if (e == cudaSuccess) e = cudaEventRecord(done[b], ctx->stream);
+                e = cudaMemcpyAsync(ctx->stl_hbuf[b], ctx->stl_dbuf[b], nt * kvsmc::kStlRecordBytes,
+                                    cudaMemcpyDeviceToHost, ctx->stream);
+            if (e == cudaSuccess) e = cudaEventRecord(ctx->stl_ev[b], ctx->stream);
         }
         if (i > 0 && e == cudaSuccess) {
             const int b = (int)((i - 1) & 1);
-            e = cudaEventSynchronize(done[b]);
+            e = cudaEventSynchronize(ctx->stl_ev[b]);
             if (e == cudaSuccess) {
                 const size_t nb = chunk_tris(i - 1) * kvsmc::kStlRecordBytes;
-                ok = std::fwrite(h_buf[b], 1, nb, f) == nb;
+                ok = std::fwrite(ctx->stl_hbuf[b], 1, nb, f) == nb;
             }
         }
     }
+    int was_bad = 0;
     if (e == cudaSuccess && nchunks) {
-        e = cudaMemcpyAsync(h_bad, bad, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream);
+        e = cudaMemcpyAsync(ctx->h_flag, ctx->d_flag, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream);
         if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
+        if (e == cudaSuccess) was_bad = *ctx->h_flag;
     }
     const bool closed = std::fclose(f) == 0;
-    const int was_bad = (e == cudaSuccess && h_bad) ? *h_bad : 0;
-    for (int b = 0; b < 2; ++b) {
-        if (d_buf[b]) cudaFree(d_buf[b]);
-        if (h_buf[b]) cudaFreeHost(h_buf[b]);
-        if (done[b]) cudaEventDestroy(done[b]);
+    if (e != cudaSuccess) {
+        cudaStreamSynchronize(ctx->stream);
+        return fail(ctx, KVSMC_ERR_CUDA, "stl: %s", cudaGetErrorString(e));
     }
-    if (bad) cudaFree(bad);
-    if (h_bad) cudaFreeHost(h_bad);
-    if (e != cudaSuccess)
-        return fail(ctx, e == cudaErrorMemoryAllocation ? KVSMC_ERR_OUT_OF_MEMORY : KVSMC_ERR_CUDA, "stl: %s",
-                    cudaGetErrorString(e));
-    if (!ok || !closed) return fail(ctx, KVSMC_ERR_INVALID_ARGUMENT, "stl: writing %s failed", path);
+    if (!ok || !closed) {
+        cudaStreamSynchronize(ctx->stream);
+        return fail(ctx, KVSMC_ERR_INVALID_ARGUMENT, "stl: writing %s failed", path);
+    }
     if (was_bad) return fail(ctx, KVSMC_ERR_INVALID_ARGUMENT, "stl: a connection index is >= nvertices");
     return KVSMC_OK;
 }
