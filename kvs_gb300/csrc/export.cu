@@ -10,17 +10,22 @@
 // triangle's normal is (n0 + n1 + n2) / 3 in float, in that order
 // (PolygonExporter.cpp:133-152, kvs::Vector3 operator+ and operator/).
 //
-// One CTA per tile of 256 triangles: coalesced loads of the tile's coords
-// and normals (or gathers through its connections) into shared memory, the
-// 12,800 record bytes composed there, then written with 16-byte stores (a
-// tile's records start at a multiple of 12,800 bytes, so every store is
-// aligned).  HBM-bound: 48 bytes read and 50 written per triangle for a
-// duplicated mesh.
+// Duplicated meshes with 16-byte aligned arrays: a persistent CTA walks tiles
+// of 256 triangles through a two-stage pipeline of bulk asynchronous copies
+// (TMA): the next tile's 9,216 coordinate and 3,072 normal bytes load into
+// shared memory (mbarrier completion) while the current tile's 12,800 record
+// bytes are composed there and leave by one bulk shared-to-global copy.  The
+// last partial tile, shared-vertex meshes (gathers through the connections)
+// and unaligned arrays take the plain kernel: coalesced loads, the records
+// composed in shared memory, 16-byte stores (a tile's records start at a
+// multiple of 12,800 bytes, so every store is aligned).  HBM-bound: 48 bytes
+// read and 50 written per triangle for a duplicated mesh.
 #include <cstdio>
 #include <cstring>
 #include <vector>
 
 #include "context.h"
+#include "tma.cuh"
 
 namespace kvsmc {
 
@@ -104,21 +109,126 @@ __global__ void __launch_bounds__(kStlTile)
     }
 }
 
+// Shared memory of the pipelined kernel: two stages of tile inputs and of
+// composed records, and one mbarrier per input stage.
+struct StlPipe {
+    float c[2][kStlTile * 9];
+    float n[2][kStlTile * 3];
+    uint16_t rec[2][kStlTile * kStlRecord / 2];
+    uint64_t bar[2];
+};
+
+constexpr uint32_t kStlPollLimit = 1u << 22;
+
+// Full tiles [0, ntiles) of a duplicated mesh; coords, normals, out 16-byte
+// aligned.  status: set to 2 when a load did not complete within the poll
+// limit (the CTA then drains its own copies and stops).
+__global__ void __launch_bounds__(kStlTile)
+    k_stl_records_tma(const float* __restrict__ coords, const float* __restrict__ normals, uint64_t ntiles,
+                      uint8_t* __restrict__ out, int* __restrict__ status)
+{
+    extern __shared__ __align__(128) unsigned char smem_raw[];
+    StlPipe& P = *reinterpret_cast<StlPipe*>(smem_raw);
+    const unsigned tid = threadIdx.x;
+    constexpr uint32_t kInBytes = kStlTile * 12 * sizeof(float);
+    auto issue = [&](uint64_t tile, int b) {
+        mbar_arrive_expect_tx(&P.bar[b], kInBytes);
+        bulk_copy_g2s(P.c[b], coords + (uint64_t)kStlTile * 9 * tile, kStlTile * 9 * sizeof(float), &P.bar[b]);
+        bulk_copy_g2s(P.n[b], normals + (uint64_t)kStlTile * 3 * tile, kStlTile * 3 * sizeof(float), &P.bar[b]);
+    };
+    if (tid == 0) {
+        mbar_init(&P.bar[0], 1);
+        mbar_init(&P.bar[1], 1);
+        fence_barrier_init();
+    }
+    __syncthreads();
+    uint64_t tile = blockIdx.x;
+    if (tid == 0 && tile < ntiles) issue(tile, 0);
+    uint32_t ph = 0;            // per input stage: parity of its next completion
+    uint32_t pending = 0;       // per input stage: a load was issued and not yet waited for
+    if (tile < ntiles) pending = 1u;
+    for (uint32_t k = 0; tile < ntiles; tile += gridDim.x, ++k) {
+        const int b = (int)(k & 1u);
+        const uint64_t next = tile + gridDim.x;
+        if (tid == 0 && next < ntiles) {
+            fence_proxy_async();   // the stage was read by every thread in the previous step
+            issue(next, b ^ 1);
+        }
+        if (next < ntiles) pending |= 1u << (b ^ 1);
+        const bool ok = mbar_wait(&P.bar[b], (ph >> b) & 1u, kStlPollLimit);
+        if (!__syncthreads_and(ok)) {
+            if (tid == 0) atomicExch(status, 2);
+            break;
+        }
+        ph ^= 1u << b;
+        pending &= ~(1u << b);
+        // this stage's records were handed to a bulk store two steps ago
+        if (tid == 0) bulk_wait_read<1>();
+        __syncthreads();
+        uint16_t* r = P.rec[b] + tid * (kStlRecord / 2);
+#pragma unroll
+        for (int j = 0; j < 3; ++j) put_float(r, j, P.n[b][3 * tid + j]);
+#pragma unroll
+        for (int j = 0; j < 9; ++j) put_float(r, 3 + j, P.c[b][9 * tid + j]);
+        r[24] = 0;
+        fence_proxy_async();   // the records, written by this thread, are read by the async proxy
+        __syncthreads();
+        if (tid == 0) {
+            bulk_copy_s2g(out + (uint64_t)kStlTile * kStlRecord * tile, P.rec[b], kStlTile * kStlRecord);
+            bulk_commit();
+        }
+    }
+    if (tid == 0) {
+        // after a timeout: the loads still in flight land (bounded) before the CTA exits
+        for (int b = 0; b < 2; ++b)
+            if ((pending >> b) & 1u) mbar_wait(&P.bar[b], (ph >> b) & 1u, kStlPollLimit);
+        bulk_wait<0>();
+    }
+}
+
 }  // namespace
 
 cudaError_t launch_stl_records(const float* coords, const float* normals, const uint32_t* conn, uint64_t nverts,
                                uint64_t ntri, int mode, uint8_t* out, int* bad_index, const Launch& L)
 {
     if (ntri == 0) return cudaSuccess;
-    const uint64_t tiles = (ntri + kStlTile - 1) / kStlTile;
-    // resident CTAs: 25 KB of shared memory and 256 threads each, a few per SM
-    const uint64_t cap = (uint64_t)L.num_sms * 8;
-    const unsigned grid = (unsigned)(tiles < cap ? tiles : cap);
     prof_begin(L, "stl_records");
-    k_stl_records<<<grid, kStlTile, 0, L.stream>>>(coords, normals, conn, nverts, ntri, mode, out, bad_index);
+    uint64_t done = 0;
+    cudaError_t e = cudaSuccess;
+    const bool aligned = ((reinterpret_cast<uintptr_t>(coords) | reinterpret_cast<uintptr_t>(normals) |
+                           reinterpret_cast<uintptr_t>(out)) & 15u) == 0;
+    if (mode == KVSMC_DUP_POLYGON_NORMAL && aligned && ntri >= (uint64_t)kStlTile) {
+        const uint64_t full = ntri / kStlTile;
+        const int smem = (int)sizeof(StlPipe);
+        e = cudaFuncSetAttribute(k_stl_records_tma, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+        int per_sm = 0;
+        if (e == cudaSuccess) e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_stl_records_tma, kStlTile, smem);
+        if (e == cudaSuccess) {
+            const uint64_t cap = (uint64_t)(per_sm > 0 ? per_sm : 1) * L.num_sms;
+            k_stl_records_tma<<<(unsigned)(full < cap ? full : cap), kStlTile, smem, L.stream>>>(coords, normals, full,
+                                                                                              out, bad_index);
+            e = cudaGetLastError();
+            *L.counter += 1;
+        }
+        done = full * kStlTile;
+    }
+    if (e == cudaSuccess && done < ntri) {
+        const uint64_t rest = ntri - done;
+        const uint64_t tiles = (rest + kStlTile - 1) / kStlTile;
+        // resident CTAs: 25 KB of shared memory and 256 threads each, a few per SM
+        const uint64_t cap = (uint64_t)L.num_sms * 8;
+        const unsigned grid = (unsigned)(tiles < cap ? tiles : cap);
+        const bool dup = mode == KVSMC_DUP_POLYGON_NORMAL;
+        k_stl_records<<<grid, kStlTile, 0, L.stream>>>(dup ? coords + 9 * done : coords,
+                                                       (mode == KVSMC_SHARED_VERTEX_NORMAL) ? normals
+                                                                                            : normals + 3 * done,
+                                                       dup ? conn : conn + 3 * done, nverts, rest, mode,
+                                                       out + kStlRecord * done, bad_index);
+        e = cudaGetLastError();
+        *L.counter += 1;
+    }
     prof_end(L);
-    *L.counter += 1;
-    return cudaGetLastError();
+    return e;
 }
 
 }  // namespace kvsmc
@@ -159,6 +269,7 @@ kvsmc_status kvsmc_stl_records(kvsmc_context* ctx, int32_t mode, const float* d_
     int h_bad = 0;
     KVSMC_CUDA(ctx, cudaMemcpyAsync(&h_bad, bad, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
     KVSMC_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    if (h_bad == 2) return fail(ctx, KVSMC_ERR_TIMEOUT, "stl: a shared-memory load did not complete");
     if (h_bad) return fail(ctx, KVSMC_ERR_INVALID_ARGUMENT, "stl: a connection index is >= nvertices");
     return KVSMC_OK;
 }
@@ -249,6 +360,7 @@ kvsmc_status kvsmc_write_stl(kvsmc_context* ctx, const char* path, int32_t mode,
         cudaStreamSynchronize(ctx->stream);
         return fail(ctx, KVSMC_ERR_INVALID_ARGUMENT, "stl: writing %s failed", path);
     }
+    if (was_bad == 2) return fail(ctx, KVSMC_ERR_TIMEOUT, "stl: a shared-memory load did not complete");
     if (was_bad) return fail(ctx, KVSMC_ERR_INVALID_ARGUMENT, "stl: a connection index is >= nvertices");
     return KVSMC_OK;
 }
