@@ -127,6 +127,8 @@ kvsmc_status kvsmc_volume_from_device(kvsmc_context* ctx, const void* dev_values
 /* Overwrite the values of an existing volume from host memory (same shape/type). */
 kvsmc_status kvsmc_volume_update(kvsmc_context* ctx, kvsmc_volume* vol, const void* host_values);
 void kvsmc_volume_free(kvsmc_context* ctx, kvsmc_volume* vol);
+/* Copy a volume's values back to host memory (dense, x fastest). */
+kvsmc_status kvsmc_volume_download(kvsmc_context* ctx, const kvsmc_volume* vol, void* host_values);
 /* Min/max of the values, computed on the device once and cached
  * (StructuredVolumeObject::updateMinMaxValues, StructuredVolumeObject.cpp:431-450). */
 kvsmc_status kvsmc_volume_minmax(kvsmc_context* ctx, kvsmc_volume* vol, double* min_value, double* max_value);
@@ -310,6 +312,38 @@ kvsmc_status kvsmc_extract_noalloc(const void* d_values, kvsmc_dtype dtype, uint
                                    uint32_t nz, const kvsmc_params* p, float* d_coords,
                                    uint64_t coords_capacity, float* d_normals, uint64_t normals_capacity,
                                    void* cuda_stream, kvsmc_sizes* sizes);
+
+/* ------------------------------------------------------------ volume ingest */
+
+/* A KVSML structured volume (.kvsml) as the reference reads it
+ * (StructuredVolumeObject::read, StructuredVolumeObject.cpp:171-229). */
+typedef struct kvsmc_kvsml_info {
+    int32_t dtype;                  /* kvsmc_dtype of <DataArray type> */
+    uint32_t nx, ny, nz;            /* resolution */
+    uint32_t veclen;
+    int32_t grid_uniform;           /* 1: grid_type="uniform" */
+    int32_t data_format;            /* 0: inline ASCII, 1: external ASCII, 2: external binary */
+    int32_t byte_swap;              /* external binary of the other endianness */
+    int32_t has_min_value, has_max_value;
+    double min_value, max_value;    /* the file's <Value min_value max_value> */
+    double volume_min, volume_max;  /* the loaded volume's min/max (set by the load) */
+    int32_t has_object_coord, has_external_coord;
+    float min_object_coord[3], max_object_coord[3];     /* the file's, or [0, res - 1] */
+    float min_external_coord[3], max_external_coord[3]; /* the file's, or the object coords */
+} kvsmc_kvsml_info;
+
+/* The header of a .kvsml file (no data read, no GPU needed). */
+kvsmc_status kvsmc_kvsml_read_info(const char* path, kvsmc_kvsml_info* info);
+/* Load a .kvsml uniform scalar volume straight into a resident device volume:
+ * external binary values stream from the file through pinned memory into the
+ * padded device rows (byte-swapped on the GPU when the file's endianness
+ * differs); ASCII values are parsed as the reference does (atof, cast).  The
+ * volume's min/max cache is set as StructuredVolumeObject::read sets it, the
+ * brick table is built.  Non-uniform grids and veclen != 1 are
+ * KVSMC_ERR_INVALID_ARGUMENT; fewer values than nodes too (the reference
+ * leaves them uninitialised). */
+kvsmc_status kvsmc_volume_load_kvsml(kvsmc_context* ctx, const char* path, kvsmc_volume** vol,
+                                     kvsmc_kvsml_info* info);
 
 /* ---------------------------------------------------------- polygon export */
 

@@ -46,7 +46,7 @@ EXPORTS = [
     "kvsmc_server_stats", "kvsmc_server_destroy", "kvsmc_copy_to_host",
     "kvsmc_size_class", "kvsmc_tune_resolve", "kvsmc_tuning_set", "kvsmc_tuning_get",
     "kvsmc_tuning_force", "kvsmc_autotune", "kvsmc_stl_records", "kvsmc_write_stl",
-    "kvsmc_write_stl_host",
+    "kvsmc_write_stl_host", "kvsmc_volume_download", "kvsmc_kvsml_read_info", "kvsmc_volume_load_kvsml",
 ]
 
 PATH_AUTO = 0      # streaming kernels where eligible
@@ -90,6 +90,16 @@ class Request(C.Structure):
                 ("d_normals", C.c_void_p), ("normals_capacity", C.c_uint64),
                 ("d_connections", C.c_void_p), ("connections_capacity", C.c_uint64),
                 ("sizes", Sizes), ("status", C.c_int)]
+
+
+class KvsmlInfo(C.Structure):
+    _fields_ = [("dtype", C.c_int32), ("nx", C.c_uint32), ("ny", C.c_uint32), ("nz", C.c_uint32),
+                ("veclen", C.c_uint32), ("grid_uniform", C.c_int32), ("data_format", C.c_int32),
+                ("byte_swap", C.c_int32), ("has_min_value", C.c_int32), ("has_max_value", C.c_int32),
+                ("min_value", C.c_double), ("max_value", C.c_double), ("volume_min", C.c_double),
+                ("volume_max", C.c_double), ("has_object_coord", C.c_int32), ("has_external_coord", C.c_int32),
+                ("min_object_coord", C.c_float * 3), ("max_object_coord", C.c_float * 3),
+                ("min_external_coord", C.c_float * 3), ("max_external_coord", C.c_float * 3)]
 
 
 class TuneChoice(C.Structure):
@@ -171,6 +181,9 @@ def load(path=LIB_PATH):
         "kvsmc_plan_kernels": (u64, [vp]),
         "kvsmc_plan_destroy": (None, [vp]),
         "kvsmc_stl_records": (C.c_int, [vp, i32, vp, vp, vp, u64, u64, vp]),
+        "kvsmc_volume_download": (C.c_int, [vp, vp, vp]),
+        "kvsmc_kvsml_read_info": (C.c_int, [C.c_char_p, C.POINTER(KvsmlInfo)]),
+        "kvsmc_volume_load_kvsml": (C.c_int, [vp, C.c_char_p, C.POINTER(vp), C.POINTER(KvsmlInfo)]),
         "kvsmc_write_stl": (C.c_int, [vp, C.c_char_p, i32, vp, vp, vp, u64, u64]),
         "kvsmc_write_stl_host": (C.c_int, [vp, C.c_char_p, i32, vp, u64, vp, u64, vp, u64]),
         "kvsmc_size_class": (i32, [u32, u32, u32]),
@@ -280,6 +293,13 @@ class DeviceVolume:
         ctx.check(ctx.lib.kvsmc_volume_from_device(ctx.handle, C.c_void_p(ptr), dtype_code(dtype), nx, ny, nz,
                                                    C.byref(h)), "kvsmc_volume_from_device")
         return cls(ctx, h, dtype, tuple(shape))
+
+    def download(self):
+        """The values as a host array shaped (nz, ny, nx)."""
+        out = np.empty(self.shape, self.dtype)
+        self.ctx.check(self.ctx.lib.kvsmc_volume_download(self.ctx.handle, self.handle, out.ctypes.data),
+                       "kvsmc_volume_download")
+        return out
 
     def minmax(self):
         mn, mx = C.c_double(), C.c_double()

@@ -577,6 +577,19 @@ void kvsmc_volume_free(kvsmc_context* ctx, kvsmc_volume* v)
     delete v;
 }
 
+kvsmc_status kvsmc_volume_download(kvsmc_context* ctx, const kvsmc_volume* v, void* host_values)
+{
+    kvsmc_status st = use_device(ctx);
+    if (st) return st;
+    if (!v || !host_values) return fail(ctx, KVSMC_ERR_INVALID_ARGUMENT, "null pointer");
+    const size_t es = dtype_size(v->view.dtype);
+    const size_t row = (size_t)v->view.nx * es;
+    KVSMC_CUDA(ctx, cudaMemcpy2DAsync(host_values, row, v->dev, v->view.pitch * es, row,
+                                      (size_t)v->view.ny * v->view.nz, cudaMemcpyDeviceToHost, ctx->stream));
+    KVSMC_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    return KVSMC_OK;
+}
+
 kvsmc_status kvsmc_volume_minmax(kvsmc_context* ctx, kvsmc_volume* v, double* mn, double* mx)
 {
     kvsmc_status st = use_device(ctx);
@@ -850,3 +863,22 @@ kvsmc_status kvsmc_selftest_interpolation(kvsmc_context* ctx, uint64_t n, uint64
 }
 
 }  // extern "C"
+
+namespace kvsmc_host {
+
+kvsmc_status volume_create(kvsmc_context* ctx, kvsmc_dtype dtype, uint32_t nx, uint32_t ny, uint32_t nz,
+                           kvsmc_volume** out)
+{
+    kvsmc_status st = check_shape(ctx, dtype, nx, ny, nz);
+    if (st) return st;
+    kvsmc_volume* v = new kvsmc_volume();
+    if ((st = volume_alloc(ctx, dtype, nx, ny, nz, v))) {
+        if (v->dev) cudaFree(v->dev);
+        delete v;
+        return st;
+    }
+    *out = v;
+    return KVSMC_OK;
+}
+
+}  // namespace kvsmc_host

@@ -105,6 +105,11 @@ struct Item {
     kvsmc_status status = KVSMC_OK;
 };
 
+// A resident volume of the given shape with uninitialised values (row-padded
+// like the uploads); the caller fills it and then calls volume_bricks.
+kvsmc_status volume_create(kvsmc_context* ctx, kvsmc_dtype dtype, uint32_t nx, uint32_t ny, uint32_t nz,
+                           kvsmc_volume** out);
+
 // (Re)build a resident volume's brick min/max table on the context's stream
 // (no-op for value types or widths the streaming kernels do not take).
 kvsmc_status volume_bricks(kvsmc_context* ctx, kvsmc_volume* v);

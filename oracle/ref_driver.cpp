@@ -186,6 +186,80 @@ int kvsref_marching_cubes(
 }
 
 /*
+ * KVSML structured volumes through the reference's own reader and writer
+ * (StructuredVolumeObject::read / write, StructuredVolumeObject.cpp:171-270,
+ * KVSMLStructuredVolumeObject).  write: writing type from (ascii, external).
+ */
+int kvsref_write_kvsml( int dtype, const void* values, unsigned nx, unsigned ny, unsigned nz, const char* path,
+                        int ascii, int external, int has_minmax, double vmin, double vmax,
+                        int has_obj, const float* min_obj, const float* max_obj )
+{
+    const size_t n = size_t( nx ) * ny * nz;
+    kvs::StructuredVolumeObject vol;
+    vol.setVeclen( 1 );
+    vol.setResolution( kvs::Vec3ui( nx, ny, nz ) );
+    vol.setValues( Values( dtype, values, n ) );
+    vol.setGridTypeToUniform();
+    if ( has_obj )
+    {
+        vol.setMinMaxObjectCoords( kvs::Vec3( min_obj[0], min_obj[1], min_obj[2] ),
+                                   kvs::Vec3( max_obj[0], max_obj[1], max_obj[2] ) );
+        vol.setMinMaxExternalCoords( kvs::Vec3( min_obj[0], min_obj[1], min_obj[2] ),
+                                     kvs::Vec3( max_obj[0], max_obj[1], max_obj[2] ) );
+    }
+    else
+    {
+        vol.updateMinMaxCoords();
+    }
+    if ( has_minmax ) vol.setMinMaxValues( vmin, vmax );
+    else vol.updateMinMaxValues();
+    return vol.write( path, ascii != 0, external != 0 ) ? 0 : -1;
+}
+
+struct kvsref_volume
+{
+    int success;
+    int dtype;               // -1: a type outside the ten of the mapper's switch
+    unsigned nx, ny, nz;
+    unsigned veclen;
+    int grid_type;
+    double vmin, vmax;
+    float min_obj[3], max_obj[3], min_ext[3], max_ext[3];
+    unsigned long long nbytes;
+    unsigned char* values;   // malloc'ed copy, nbytes
+};
+
+int kvsref_read_kvsml( const char* path, kvsref_volume* out )
+{
+    std::memset( out, 0, sizeof( *out ) );
+    kvs::StructuredVolumeObject vol;
+    if ( !vol.read( path ) ) return -1;
+    out->success = 1;
+    const auto t = vol.values().typeID();
+    static const kvs::Type::TypeID order[10] = {
+        kvs::Type::TypeInt8, kvs::Type::TypeInt16, kvs::Type::TypeInt32, kvs::Type::TypeInt64,
+        kvs::Type::TypeUInt8, kvs::Type::TypeUInt16, kvs::Type::TypeUInt32, kvs::Type::TypeUInt64,
+        kvs::Type::TypeReal32, kvs::Type::TypeReal64 };
+    out->dtype = -1;
+    for ( int i = 0; i < 10; ++i ) if ( order[i] == t ) out->dtype = i;
+    out->nx = vol.resolution().x(); out->ny = vol.resolution().y(); out->nz = vol.resolution().z();
+    out->veclen = vol.veclen();
+    out->grid_type = int( vol.gridType() );
+    out->vmin = vol.minValue();
+    out->vmax = vol.maxValue();
+    Copy3( out->min_obj, vol.minObjectCoord() );
+    Copy3( out->max_obj, vol.maxObjectCoord() );
+    Copy3( out->min_ext, vol.minExternalCoord() );
+    Copy3( out->max_ext, vol.maxExternalCoord() );
+    out->nbytes = vol.values().byteSize();
+    out->values = static_cast<unsigned char*>( std::malloc( out->nbytes ? out->nbytes : 1 ) );
+    std::memcpy( out->values, vol.values().data(), out->nbytes );
+    return 0;
+}
+
+void kvsref_free_volume( kvsref_volume* v ) { std::free( v->values ); std::memset( v, 0, sizeof( *v ) ); }
+
+/*
  * kvs::MarchingCubes on a uniform volume, then the reference's binary STL export
  * of the result: PolygonExporter<kvs::Stl>::exec (PolygonExporter.cpp:78-176)
  * and Stl::write with the Binary file type (Stl.cpp:170-199, 490-540).
