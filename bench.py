@@ -8,7 +8,8 @@ volume: the fused count launch, the scan, the fused emit launch, with output
 written to HBM.  `value` = cells x isovalues / s (Mcells/s).
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
-                    [--workload sweep1024|sweep512|uneven200|serve|heavy|stl512|stl384|blobs128] [--tune]
+                    [--workload sweep1024|sweep512|uneven200|serve|heavy|stl512|stl384|kvsml512|blobs128]
+                    [--tune]
 
 --tune runs the launch-shape autotuner (kvsmc_autotune, a few seconds) on the
 bench's context before measuring; without it the built-in rules decide.
@@ -73,6 +74,10 @@ WORKLOADS = {
     "stl384": dict(shape=(384, 384, 384), kind="stl", isos=[0.2 + 0.04 * k for k in range(16)],
                    desc="binary STL serialisation of the 16 meshes of a 384^3 float32 fBm sweep (the profiling "
                         "case of stl512: same kernel, ~3.5 GB on the device, each launch larger than L2)"),
+    "kvsml512": dict(shape=(512, 512, 512), kind="ingest",
+                     desc="KVSML ingest: a 512^3 float32 structured volume (external binary, 512 MiB, page cache "
+                          "under /dev/shm) loaded straight into a padded device volume by kvsmc_volume_load_kvsml "
+                          "(header parse, chunked pinned reads + cudaMemcpy2DAsync, min/max scan, brick table)"),
     "blobs128": dict(shape=(128, 128, 128), kind="blobs", isos=[0.5],
                      desc="128^3 float32, 4 Gaussian blobs (sigma 8..24) + U[-0.01,0.01] noise, iso 0.5, "
                           "duplication=true, PolygonNormal"),
@@ -208,6 +213,74 @@ def maybe_tune(args, ctx):
     changed = [r for r in table if any(r[f] for f in T.FIELDS)]
     return {"seconds": round(time.time() - t0, 2), "entries": len(table), "entries_changed": len(changed),
             "changed": [{k: r[k] for k in ("dtype", "size_class") + T.FIELDS} for r in changed]}
+
+
+def run_ingest(args, rank, world, local):
+    """kvsmc_volume_load_kvsml of a 512^3 float32 external-binary KVSML file."""
+    import shutil
+    import tempfile
+    import time
+
+    import torch
+
+    from kvs_gb300 import _abi
+    from kvs_gb300 import ingest
+
+    torch.cuda.set_device(local)
+    w = WORKLOADS[args.workload]
+    ctx = _abi.Context(local)
+    nz, ny, nx = w["shape"]
+    base = "/dev/shm" if os.path.isdir("/dev/shm") else None
+    d = tempfile.mkdtemp(dir=base)
+    try:
+        field = make_field(dict(w, kind="fbm"), "cuda").cpu().numpy()
+        field.astype("<f4").tofile(os.path.join(d, "vol_value.dat"))
+        with open(os.path.join(d, "vol.kvsml"), "w") as f:
+            f.write('<?xml version="1.0" ?>\n<KVSML>\n<Object type="StructuredVolumeObject">\n'
+                    f'<StructuredVolumeObject grid_type="uniform" resolution="{nx} {ny} {nz}">\n<Node>\n'
+                    '<Value veclen="1">\n<DataArray type="float" format="binary" file="vol_value.dat" '
+                    'endian="little" />\n</Value>\n</Node>\n</StructuredVolumeObject>\n</Object>\n</KVSML>\n')
+        path = os.path.join(d, "vol.kvsml")
+        nbytes = field.nbytes
+        del field
+        for _ in range(args.warmup):
+            v, _info = ingest.load_kvsml(ctx, path)
+            v.free()
+        launches0 = ctx.kernel_launches
+        times = []
+        for _ in range(args.steps):
+            t0 = time.perf_counter()
+            v, info = ingest.load_kvsml(ctx, path)
+            times.append(time.perf_counter() - t0)
+            v.free()
+        launches = ctx.kernel_launches - launches0
+        t = sorted(times)[len(times) // 2]
+        gbs = nbytes / t / 1e9
+        cpu = None
+        if rank == 0 and not args.no_cpu:
+            t0 = time.perf_counter()
+            reps = 0
+            while time.perf_counter() - t0 < 3.0 or reps < 1:
+                np.fromfile(os.path.join(d, "vol_value.dat"), "<f4")
+                reps += 1
+            tc = (time.perf_counter() - t0) / reps
+            cpu = {"value": round(nbytes / tc / 1e9, 2), "unit": "GB/s", "cores": 1, "kind": "port",
+                   "sample": "the same 512 MiB value file read into host memory (numpy.fromfile: the fread of "
+                             "DataArray::ReadExternalData, DataArray.h:175-190), %.1f s on 1 host core" % (tc * reps)}
+    finally:
+        shutil.rmtree(d, ignore_errors=True)
+    return {
+        "metric": "GB/s", "value": round(gbs, 2), "unit": "GB/s", "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": round(t * 1e3, 2), "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded fBm written as KVSML)",
+        "config": {"workload": w["desc"], "bytes": int(nbytes), "timing": "host clock, median of steps"},
+        "roofline": {"kernel": "host-to-device link", "bound": "link", "achieved": round(gbs, 2), "peak": None,
+                     "unit": "GB/s", "frac": None, "traffic": None,
+                     "note": "file (page cache) -> pinned -> HBM; no kernel dominates"},
+        "e2e": {"value": round(gbs, 2), "unit": "GB/s", "h2d_bytes_per_step": int(nbytes), "d2h_bytes_per_step": 16,
+                "api": "kvsmc_volume_load_kvsml"},
+        "gpu_launches": int(launches // max(1, args.steps)), "cpu_baseline": cpu,
+    }
 
 
 def run_stl(args, rank, world, local):
@@ -927,6 +1000,8 @@ def main():
         dist.init_process_group("nccl")
     if args.impl == "reference":
         line = run_reference(args, rank, world)
+    elif WORKLOADS[args.workload]["kind"] == "ingest":
+        line = run_ingest(args, rank, world, local)
     elif WORKLOADS[args.workload]["kind"] == "stl":
         line = run_stl(args, rank, world, local)
         mesh = line.pop("_sample_mesh")

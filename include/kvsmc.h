@@ -344,6 +344,14 @@ kvsmc_status kvsmc_kvsml_read_info(const char* path, kvsmc_kvsml_info* info);
  * leaves them uninitialised). */
 kvsmc_status kvsmc_volume_load_kvsml(kvsmc_context* ctx, const char* path, kvsmc_volume** vol,
                                      kvsmc_kvsml_info* info);
+/* The same for an AVS field file (.fld, kvs::AVSField, FileFormat/AVSField/
+ * AVSField.cpp, imported as StructuredVolumeImporter.cpp:155-189 does):
+ * uniform fields of byte/short/integer/float/double, the values after the
+ * header's "\f\f" streamed into the device rows; min/max by the device scan;
+ * info->data_format is 2 (binary). */
+kvsmc_status kvsmc_avs_read_info(const char* path, kvsmc_kvsml_info* info);
+kvsmc_status kvsmc_volume_load_avs(kvsmc_context* ctx, const char* path, kvsmc_volume** vol,
+                                   kvsmc_kvsml_info* info);
 
 /* ---------------------------------------------------------- polygon export */
 

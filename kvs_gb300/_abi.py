@@ -47,6 +47,7 @@ EXPORTS = [
     "kvsmc_size_class", "kvsmc_tune_resolve", "kvsmc_tuning_set", "kvsmc_tuning_get",
     "kvsmc_tuning_force", "kvsmc_autotune", "kvsmc_stl_records", "kvsmc_write_stl",
     "kvsmc_write_stl_host", "kvsmc_volume_download", "kvsmc_kvsml_read_info", "kvsmc_volume_load_kvsml",
+    "kvsmc_avs_read_info", "kvsmc_volume_load_avs",
 ]
 
 PATH_AUTO = 0      # streaming kernels where eligible
@@ -184,6 +185,8 @@ def load(path=LIB_PATH):
         "kvsmc_volume_download": (C.c_int, [vp, vp, vp]),
         "kvsmc_kvsml_read_info": (C.c_int, [C.c_char_p, C.POINTER(KvsmlInfo)]),
         "kvsmc_volume_load_kvsml": (C.c_int, [vp, C.c_char_p, C.POINTER(vp), C.POINTER(KvsmlInfo)]),
+        "kvsmc_avs_read_info": (C.c_int, [C.c_char_p, C.POINTER(KvsmlInfo)]),
+        "kvsmc_volume_load_avs": (C.c_int, [vp, C.c_char_p, C.POINTER(vp), C.POINTER(KvsmlInfo)]),
         "kvsmc_write_stl": (C.c_int, [vp, C.c_char_p, i32, vp, vp, vp, u64, u64]),
         "kvsmc_write_stl_host": (C.c_int, [vp, C.c_char_p, i32, vp, u64, vp, u64, vp, u64]),
         "kvsmc_size_class": (i32, [u32, u32, u32]),

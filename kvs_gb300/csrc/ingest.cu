@@ -1,5 +1,5 @@
-// ingest.cu -- KVSML structured volumes read straight into resident device
-// volumes.
+// ingest.cu -- KVSML structured volumes and AVS fields read straight into
+// resident device volumes.
 //
 // The reference reads a .kvsml file into a host kvs::StructuredVolumeObject
 // (StructuredVolumeObject::read, Object/StructuredVolumeObject.cpp:171-229,
@@ -367,8 +367,9 @@ __global__ void k_byteswap(uint8_t* p, uint64_t n, int es)
     }
 }
 
-// External binary values streamed into the device rows.
-kvsmc_status load_binary(kvsmc_context* ctx, const std::string& file, kvsmc_volume* v)
+// External binary values (from byte `offset` of the file) streamed into the
+// device rows.
+kvsmc_status load_binary(kvsmc_context* ctx, const std::string& file, kvsmc_volume* v, long offset = 0)
 {
     const size_t es = dsize(v->view.dtype);
     const size_t row = (size_t)v->view.nx * es;
@@ -376,6 +377,10 @@ kvsmc_status load_binary(kvsmc_context* ctx, const std::string& file, kvsmc_volu
     const size_t chunk_rows = std::max<size_t>(1, (64u << 20) / std::max<size_t>(row, 1));
     FILE* f = std::fopen(file.c_str(), "rb");
     if (!f) return fail(ctx, KVSMC_ERR_INVALID_ARGUMENT, "kvsml: Cannot open '%s'.", file.c_str());
+    if (offset && std::fseek(f, offset, SEEK_SET) != 0) {
+        std::fclose(f);
+        return fail(ctx, KVSMC_ERR_INVALID_ARGUMENT, "Cannot read '%s'.", file.c_str());
+    }
     uint8_t* h[2] = {nullptr, nullptr};
     cudaEvent_t ev[2] = {nullptr, nullptr};
     cudaError_t e = cudaSuccess;
@@ -439,9 +444,127 @@ kvsmc_status load_ascii(kvsmc_context* ctx, const Header& hd, kvsmc_volume* v)
     return KVSMC_OK;
 }
 
+// ------------------------------------------------------------ AVS field
+//
+// kvs::AVSField::read (FileFormat/AVSField/AVSField.cpp): the first line
+// starts "# AVS"; then "key = value" lines (tokens split at " ,\t\n", lines
+// starting '#' skipped) up to a line starting with a form feed; the values
+// follow the first "\f\f" of the file, raw, in the host's byte order.
+// StructuredVolumeImporter::import(const AVSField*) (:155-189) takes only
+// uniform fields; object coords [0, dim - 1]; external coords min_ext /
+// max_ext when either is given (defaults (0,0,0) / (1,1,1)), else the object
+// coords; min/max by the scan.
+struct AvsHeader {
+    kvsmc_kvsml_info info;
+    long data_offset = -1;
+    bool uniform = false;
+};
+
+kvsmc_status read_avs_header(const char* path, AvsHeader& h, std::string& err)
+{
+    std::memset(&h.info, 0, sizeof h.info);
+    std::string doc;
+    if (!read_file(path, doc)) { err = std::string("Cannot open ") + path; return KVSMC_ERR_INVALID_ARGUMENT; }
+    if (doc.compare(0, 5, "# AVS") != 0) { err = "not an AVS field file"; return KVSMC_ERR_INVALID_ARGUMENT; }
+    kvsmc_kvsml_info& in = h.info;
+    in.veclen = 1;
+    in.nx = in.ny = in.nz = 1;
+    float min_ext[3] = {0, 0, 0}, max_ext[3] = {1, 1, 1};
+    bool has_ext = false;
+    int data = -1;
+    std::string field;
+    size_t pos = doc.find('\n') == std::string::npos ? doc.size() : doc.find('\n') + 1;
+    while (pos < doc.size()) {
+        if (doc[pos] == '\f') break;   // the data separator
+        const size_t eol = doc.find('\n', pos);
+        const size_t end = eol == std::string::npos ? doc.size() : eol;
+        const std::string line = doc.substr(pos, end - pos);
+        pos = end + 1;
+        if (line.empty() || line[0] == '#') continue;
+        std::vector<std::string> t;
+        tokens(line.data(), line.size(), " ,\t\n", [&](const char* s, size_t n) { t.emplace_back(s, n); return true; });
+        if (t.size() < 3 || t[1] != "=") continue;
+        const std::string& key = t[0];
+        const char* val = t[2].c_str();
+        if (key == "veclen") in.veclen = (uint32_t)std::atoi(val);
+        else if (key == "dim1") in.nx = (uint32_t)std::atoi(val);
+        else if (key == "dim2") in.ny = (uint32_t)std::atoi(val);
+        else if (key == "dim3") in.nz = (uint32_t)std::atoi(val);
+        else if (key == "field") field = t[2];
+        else if (key == "data") {
+            data = t[2] == "byte" ? KVSMC_U8 : t[2] == "short" ? KVSMC_I16 : t[2] == "integer" ? KVSMC_I32
+                 : t[2] == "float" ? KVSMC_F32 : t[2] == "double" ? KVSMC_F64 : -1;
+        } else if ((key == "min_ext" || key == "max_ext") && t.size() >= 5) {
+            float* e = key == "min_ext" ? min_ext : max_ext;
+            for (int k = 0; k < 3; ++k) e[k] = (float)std::atof(t[2 + k].c_str());
+            has_ext = true;
+        }
+    }
+    const size_t ff = doc.find("\f\f");
+    if (ff == std::string::npos) { err = "no data separator"; return KVSMC_ERR_INVALID_ARGUMENT; }
+    h.data_offset = (long)(ff + 2);
+    h.uniform = field == "uniform";
+    in.grid_uniform = h.uniform ? 1 : 0;
+    in.dtype = data;
+    in.data_format = 2;
+    if (data < 0) { err = "unknown 'data' type"; return KVSMC_ERR_UNSUPPORTED_DTYPE; }
+    in.has_object_coord = 1;
+    in.max_object_coord[0] = (float)in.nx - 1.0f;
+    in.max_object_coord[1] = (float)in.ny - 1.0f;
+    in.max_object_coord[2] = (float)in.nz - 1.0f;
+    in.has_external_coord = 1;
+    for (int k = 0; k < 3; ++k) {
+        in.min_external_coord[k] = has_ext ? min_ext[k] : in.min_object_coord[k];
+        in.max_external_coord[k] = has_ext ? max_ext[k] : in.max_object_coord[k];
+    }
+    return KVSMC_OK;
+}
+
 }  // namespace
 
 extern "C" {
+
+kvsmc_status kvsmc_avs_read_info(const char* path, kvsmc_kvsml_info* info)
+{
+    if (!path || !info) return KVSMC_ERR_INVALID_ARGUMENT;
+    AvsHeader h;
+    std::string err;
+    const kvsmc_status st = read_avs_header(path, h, err);
+    *info = h.info;
+    return st;
+}
+
+kvsmc_status kvsmc_volume_load_avs(kvsmc_context* ctx, const char* path, kvsmc_volume** vol, kvsmc_kvsml_info* info)
+{
+    if (!ctx || !path || !vol) return KVSMC_ERR_INVALID_ARGUMENT;
+    *vol = nullptr;
+    KVSMC_CUDA(ctx, cudaSetDevice(ctx->device));
+    AvsHeader h;
+    std::string err;
+    kvsmc_status st = read_avs_header(path, h, err);
+    if (info) *info = h.info;
+    if (st) return fail(ctx, st, "avs: %s: %s", path, err.c_str());
+    if (!h.uniform) return fail(ctx, KVSMC_ERR_INVALID_ARGUMENT, "'Uniform' type in kvs::AVSField format is only supported.");
+    if (h.info.veclen != 1)
+        return fail(ctx, KVSMC_ERR_INVALID_ARGUMENT, "avs: veclen %u: the device volumes are scalar fields",
+                    h.info.veclen);
+    kvsmc_volume* v = nullptr;
+    if ((st = kvsmc_host::volume_create(ctx, (kvsmc_dtype)h.info.dtype, h.info.nx, h.info.ny, h.info.nz, &v)))
+        return st;
+    st = load_binary(ctx, path, v, h.data_offset);
+    if (!st) st = kvsmc_volume_minmax(ctx, v, &v->vmin, &v->vmax);
+    if (!st) st = kvsmc_host::volume_bricks(ctx, v);
+    if (st) {
+        kvsmc_volume_free(ctx, v);
+        return st;
+    }
+    if (info) {
+        info->volume_min = v->vmin;
+        info->volume_max = v->vmax;
+    }
+    *vol = v;
+    return KVSMC_OK;
+}
 
 kvsmc_status kvsmc_kvsml_read_info(const char* path, kvsmc_kvsml_info* info)
 {

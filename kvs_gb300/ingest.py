@@ -1,5 +1,6 @@
-"""KVSML structured volumes loaded straight into resident device volumes
-(kvsmc_kvsml_read_info, kvsmc_volume_load_kvsml).
+"""KVSML structured volumes and AVS fields loaded straight into resident
+device volumes (kvsmc_kvsml_read_info / kvsmc_volume_load_kvsml,
+kvsmc_avs_read_info / kvsmc_volume_load_avs).
 
 The reference reads a .kvsml file into a host kvs::StructuredVolumeObject
 (StructuredVolumeObject::read, Object/StructuredVolumeObject.cpp:171-229);
@@ -38,6 +39,26 @@ def read_info(path):
     if st:
         raise _abi.KvsmcError(st, f"kvsml header of {path}: {_abi.status_string(st)}")
     return _info_dict(info)
+
+
+def read_avs_info(path):
+    """The header of an AVS field file (.fld)."""
+    info = _abi.KvsmlInfo()
+    st = _abi.load().kvsmc_avs_read_info(str(path).encode(), C.byref(info))
+    if st:
+        raise _abi.KvsmcError(st, f"AVS header of {path}: {_abi.status_string(st)}")
+    return _info_dict(info)
+
+
+def load_avs(ctx, path):
+    """(DeviceVolume, info) of a uniform scalar AVS field (.fld)."""
+    info = _abi.KvsmlInfo()
+    h = C.c_void_p()
+    ctx.check(ctx.lib.kvsmc_volume_load_avs(ctx.handle, str(path).encode(), C.byref(h), C.byref(info)),
+              "kvsmc_volume_load_avs")
+    d = _info_dict(info)
+    nx, ny, nz = d["resolution"]
+    return _abi.DeviceVolume(ctx, h, d["dtype"], (nz, ny, nx)), d
 
 
 def load_kvsml(ctx, path):

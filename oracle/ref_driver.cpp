@@ -14,6 +14,7 @@
 #include <kvs/Isosurface>
 #include <kvs/PolygonExporter>
 #include <kvs/Stl>
+#include <kvs/AVSField>
 #include <kvs/TransferFunction>
 #include <kvs/HydrogenVolumeData>
 #include <kvs/ValueArray>
@@ -258,6 +259,55 @@ int kvsref_read_kvsml( const char* path, kvsref_volume* out )
 }
 
 void kvsref_free_volume( kvsref_volume* v ) { std::free( v->values ); std::memset( v, 0, sizeof( *v ) ); }
+
+/*
+ * An AVS field file read by kvs::AVSField (FileFormat/AVSField/AVSField.cpp)
+ * and turned into a volume the way StructuredVolumeImporter::import(const
+ * AVSField*) does (Visualization/Importer/StructuredVolumeImporter.cpp:155-189;
+ * restated here because the importer's other formats pull in DICOM and more):
+ * uniform fields only, object coords [0, dim - 1], external coords min_ext /
+ * max_ext or the object coords, min/max by updateMinMaxValues.
+ */
+int kvsref_read_avs( const char* path, kvsref_volume* out )
+{
+    std::memset( out, 0, sizeof( *out ) );
+    kvs::AVSField field( path );
+    if ( field.isFailure() ) return -1;
+    if ( field.fieldType() != kvs::AVSField::Uniform ) return -2;
+    kvs::StructuredVolumeObject vol;
+    const kvs::Vec3 min_obj( 0.0f, 0.0f, 0.0f );
+    const kvs::Vec3 max_obj( float( field.dim().x() ) - 1.0f, float( field.dim().y() ) - 1.0f,
+                             float( field.dim().z() ) - 1.0f );
+    vol.setMinMaxObjectCoords( min_obj, max_obj );
+    if ( field.hasMinMaxExt() ) vol.setMinMaxExternalCoords( field.minExt(), field.maxExt() );
+    else vol.setMinMaxExternalCoords( min_obj, max_obj );
+    vol.setGridType( kvs::StructuredVolumeObject::Uniform );
+    vol.setVeclen( field.veclen() );
+    vol.setResolution( field.dim() );
+    vol.setValues( field.values() );
+    vol.updateMinMaxValues();
+    out->success = 1;
+    const auto t = vol.values().typeID();
+    static const kvs::Type::TypeID order[10] = {
+        kvs::Type::TypeInt8, kvs::Type::TypeInt16, kvs::Type::TypeInt32, kvs::Type::TypeInt64,
+        kvs::Type::TypeUInt8, kvs::Type::TypeUInt16, kvs::Type::TypeUInt32, kvs::Type::TypeUInt64,
+        kvs::Type::TypeReal32, kvs::Type::TypeReal64 };
+    out->dtype = -1;
+    for ( int i = 0; i < 10; ++i ) if ( order[i] == t ) out->dtype = i;
+    out->nx = vol.resolution().x(); out->ny = vol.resolution().y(); out->nz = vol.resolution().z();
+    out->veclen = vol.veclen();
+    out->grid_type = int( vol.gridType() );
+    out->vmin = vol.minValue();
+    out->vmax = vol.maxValue();
+    Copy3( out->min_obj, vol.minObjectCoord() );
+    Copy3( out->max_obj, vol.maxObjectCoord() );
+    Copy3( out->min_ext, vol.minExternalCoord() );
+    Copy3( out->max_ext, vol.maxExternalCoord() );
+    out->nbytes = vol.values().byteSize();
+    out->values = static_cast<unsigned char*>( std::malloc( out->nbytes ? out->nbytes : 1 ) );
+    std::memcpy( out->values, vol.values().data(), out->nbytes );
+    return 0;
+}
 
 /*
  * kvs::MarchingCubes on a uniform volume, then the reference's binary STL export

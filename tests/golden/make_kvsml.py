@@ -1,4 +1,4 @@
-"""Generate the KVSML ingest fixtures from the reference.
+"""Generate the KVSML and AVS-field ingest fixtures from the reference.
 
 Small structured volumes are written by the reference's own writer
 (StructuredVolumeObject::write: inline ASCII, external ASCII, external
@@ -8,7 +8,9 @@ attributes, inline values separated by commas, tabs and newlines).  Every
 file is then read back by the reference reader (StructuredVolumeObject::read)
 and what it produced -- values, type, resolution, min/max, coordinates -- is
 stored in tests/golden/kvsml/expected.npz with the case list in
-tests/golden/kvsml/cases.json.
+tests/golden/kvsml/cases.json.  AVS field files (.fld: header lines, "\f\f",
+raw values) are written here and read by the reference kvs::AVSField with the
+StructuredVolumeImporter rules (the driver's kvsref_read_avs).
 
     python tests/golden/make_kvsml.py
 """
@@ -42,7 +44,24 @@ def lib():
     L.kvsref_read_kvsml.restype = C.c_int
     L.kvsref_read_kvsml.argtypes = [C.c_char_p, C.POINTER(RefVolume)]
     L.kvsref_free_volume.argtypes = [C.POINTER(RefVolume)]
+    L.kvsref_read_avs.restype = C.c_int
+    L.kvsref_read_avs.argtypes = [C.c_char_p, C.POINTER(RefVolume)]
     return L
+
+
+def write_avs(name, v, data, ext=None, extra=""):
+    """An AVS field file as the format defines it: '# AVS' line, key = value
+    lines, two form feeds, the raw values (little-endian)."""
+    nz, ny, nx = v.shape
+    head = ["# AVS field file", "# written for the ingest fixtures", "#", "nspace = 3", "veclen = 1", "ndim   = 3",
+            f"dim1   = {nx}", f"dim2   = {ny}", f"dim3   = {nz}", f"data   = {data}", "field  = uniform"]
+    if ext:
+        head += ["min_ext = %r %r %r" % tuple(ext[0]), "max_ext = %r %r %r" % tuple(ext[1])]
+    head += ["label  = value"] + ([extra] if extra else [])
+    with open(os.path.join(OUT, name + ".fld"), "wb") as f:
+        f.write(("\n".join(head) + "\n").encode())
+        f.write(b"\f\f")
+        f.write(np.ascontiguousarray(v).astype(v.dtype.newbyteorder("<")).tobytes())
 
 
 def write(name, v, ascii, external, minmax=None, obj=None):
@@ -108,23 +127,30 @@ def main():
     start = text.index('<DataArray type="float">') + len('<DataArray type="float">')
     end = text.index("</DataArray>")
     open(os.path.join(OUT, "f32_commas.kvsml"), "w").write(text[:start] + vals + "\n" + text[end:])
+    # AVS fields
+    write_avs("avs_f32", f32, "float", ext=([0.5, -1.0, 2.0], [7.5, 4.0, 6.0]))
+    write_avs("avs_u8", u8, "byte")
+    write_avs("avs_i16", i16, "short", extra="# comment after the keys")
+    write_avs("avs_i32", i32, "integer")
+    write_avs("avs_f64", f64, "double", extra="unknown_key = 12")
     # what the reference reader makes of every file
     arrays, cases = {}, []
-    for fn in sorted(f for f in os.listdir(OUT) if f.endswith(".kvsml")):
-        name = fn[:-6]
+    for fn in sorted(f for f in os.listdir(OUT) if f.endswith(".kvsml") or f.endswith(".fld")):
+        name = fn.rsplit(".", 1)[0]
         r = RefVolume()
-        assert lib().kvsref_read_kvsml(os.path.join(OUT, fn).encode(), C.byref(r)) == 0, fn
+        read = lib().kvsref_read_avs if fn.endswith(".fld") else lib().kvsref_read_kvsml
+        assert read(os.path.join(OUT, fn).encode(), C.byref(r)) == 0, fn
         dt = np.dtype(ref.DTYPES[r.dtype])
         vals = np.ctypeslib.as_array(r.values, shape=(r.nbytes,)).copy().view(dt).reshape(r.nz, r.ny, r.nx)
         arrays[name] = vals
-        cases.append(dict(name=name, dtype=dt.name, resolution=[r.nx, r.ny, r.nz], veclen=r.veclen,
+        cases.append(dict(name=name, file=fn, dtype=dt.name, resolution=[r.nx, r.ny, r.nz], veclen=r.veclen,
                           vmin=r.vmin, vmax=r.vmax, min_obj=list(r.min_obj), max_obj=list(r.max_obj),
                           min_ext=list(r.min_ext), max_ext=list(r.max_ext)))
         lib().kvsref_free_volume(C.byref(r))
     np.savez_compressed(os.path.join(OUT, "expected.npz"), **arrays)
     with open(os.path.join(OUT, "cases.json"), "w") as f:
         json.dump(cases, f, indent=0)
-    print(f"{len(cases)} kvsml cases, {sum(os.path.getsize(os.path.join(OUT, x)) for x in os.listdir(OUT))} bytes")
+    print(f"{len(cases)} kvsml/avs cases, {sum(os.path.getsize(os.path.join(OUT, x)) for x in os.listdir(OUT))} bytes")
 
 
 if __name__ == "__main__":

@@ -1,6 +1,7 @@
-"""KVSML headers (kvsmc_kvsml_read_info, a pure host function) against what
-the reference reader (StructuredVolumeObject::read) made of the same files,
-tests/golden/kvsml/ (tests/golden/make_kvsml.py)."""
+"""KVSML and AVS-field headers (kvsmc_kvsml_read_info, kvsmc_avs_read_info:
+pure host functions) against what the reference readers
+(StructuredVolumeObject::read; kvs::AVSField with the importer's rules) made
+of the same files, tests/golden/kvsml/ (tests/golden/make_kvsml.py)."""
 import json
 import os
 
@@ -19,11 +20,16 @@ def kvsml_cases():
     return json.load(open(os.path.join(KDIR, "cases.json"))), np.load(os.path.join(KDIR, "expected.npz"))
 
 
+def header(c):
+    p = os.path.join(KDIR, c["file"])
+    return ingest.read_avs_info(p) if p.endswith(".fld") else ingest.read_info(p)
+
+
 def test_headers_match_reference_reader():
     cases, arr = kvsml_cases()
-    assert len(cases) >= 15
+    assert len(cases) >= 20
     for c in cases:
-        info = ingest.read_info(os.path.join(KDIR, c["name"] + ".kvsml"))
+        info = header(c)
         n = c["name"]
         assert info["dtype"] == np.dtype(c["dtype"]), n
         assert list(info["resolution"]) == c["resolution"] and info["veclen"] == c["veclen"], n
@@ -38,7 +44,7 @@ def test_headers_match_reference_reader():
             assert info["min_value"] == c["vmin"], n
         if info["max_value"] is not None:
             assert info["max_value"] == c["vmax"], n
-    fmt = {c["name"]: ingest.read_info(os.path.join(KDIR, c["name"] + ".kvsml"))["format"] for c in cases}
+    fmt = {c["name"]: header(c)["format"] for c in cases}
     assert fmt["f32_ascii"] == "ascii" and fmt["f32_extascii"] == "external ascii" and fmt["f32_binary"] == "external binary"
     assert ingest.read_info(os.path.join(KDIR, "f32_big.kvsml"))["byte_swap"]
 
