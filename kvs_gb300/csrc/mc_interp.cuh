@@ -60,6 +60,18 @@ __device__ __forceinline__ float clampf_ref(float a, float lo, float hi)
     return a <= lo ? lo : (a <= hi ? a : hi);
 }
 
+// Distance from x + e (x > 0 a normal float, |e| below half its gaps) to the
+// nearer of x's two rounding boundaries: half the gap to the next float above
+// less e, or half the gap to the next float below plus e.  Both sides count:
+// at a power of two the gap below is half the gap above.
+__device__ __forceinline__ float rounding_margin(float x, float e)
+{
+    const int ib = __float_as_int(x);
+    const float hi = __fmul_rn(__fsub_rn(__int_as_float(ib + 1), x), 0.5f);
+    const float lo = __fmul_rn(__fsub_rn(x, __int_as_float(ib - 1)), 0.5f);
+    return fminf(__fsub_rn(hi, e), __fadd_rn(lo, e));
+}
+
 // The varying-axis coordinate RN32(X) for an edge from coordinate a (value
 // v0) to b = a + d (value v1), d = +-1.  Returns false when the FP32 path
 // cannot decide; `out` is then unspecified.
@@ -114,10 +126,7 @@ __device__ __forceinline__ bool fast_axis(float v0, float v1, float a, float b, 
         if (yh == 0.0f && yl == 0.0f && E < 1.0e-30f) { out = 0.0f; return true; }
         return false;
     }
-    // distance to the nearest rounding boundary on yl's side: half the gap to
-    // the neighbouring float there, less |yl| (yh > 0 and normal here)
-    const float nb = __int_as_float(__float_as_int(yh) + (yl >= 0.0f ? 1 : -1));
-    const float dist = __fsub_rn(__fmul_rn(fabsf(__fsub_rn(nb, yh)), 0.5f), fabsf(yl));
+    const float dist = rounding_margin(yh, yl);
     if (!(dist > E)) return false;
     out = yh;
     return true;
@@ -163,8 +172,7 @@ __device__ __forceinline__ bool fast_axis_bf(float v0, float v1, float a, float 
     E = __fadd_rn(E, __fmul_rn(fabsf(yb2), 1.1920929e-07f));
     E = __fadd_rn(E, __fmul_rn(__fadd_rn(m, 1.0f), 8.8817842e-16f));
     E = __fmul_rn(E, 1.001f);
-    const float nb = __int_as_float(__float_as_int(yh) + (yl >= 0.0f ? 1 : -1));
-    const float dist = __fsub_rn(__fmul_rn(fabsf(__fsub_rn(nb, yh)), 0.5f), fabsf(yl));
+    const float dist = rounding_margin(yh, yl);
     const bool pos_ok = yh > 0.0f && yh < 3.0e7f && dist > E;
     const bool zero_ok = yh == 0.0f && yl == 0.0f && E < 1.0e-30f;
     const bool ok = at_v0 || (den_ok && aq <= 1.5f && (pos_ok || zero_ok));

@@ -26,7 +26,7 @@ __global__ void k_selftest(uint64_t n, uint64_t seed, unsigned long long* counte
     for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < n; i += (uint64_t)gridDim.x * blockDim.x) {
         const uint64_t h0 = mix64(seed * 0x9e3779b97f4a7c15ull + i);
         const uint64_t h1 = mix64(h0 + 1), h2 = mix64(h0 + 2), h3 = mix64(h0 + 3);
-        const int kind = (int)(h0 & 7);
+        const int kind = (int)(h0 % 10);
         double iso;
         float va, vb;
         if (kind == 0) {          // float data in [0,1], double isolevel
@@ -45,8 +45,16 @@ __global__ void k_selftest(uint64_t n, uint64_t seed, unsigned long long* counte
             iso = (double)fminf(va, vb) + unit(h3) * 1e-9;
         } else if (kind == 6) {   // wide dynamic range
             va = (float)((unit(h1) - 0.5) * 2e6); vb = (float)((unit(h2) - 0.5) * 2e6); iso = (unit(h3) - 0.5) * 2e6;
-        } else {                  // ratio near 1/2 (midpoint-prone)
+        } else if (kind == 7) {   // ratio near 1/2 (midpoint-prone)
             va = (float)(h1 & 1023); vb = va + 1.0f; iso = (double)va + 0.5 + (unit(h3) - 0.5) * 1e-12;
+        } else if (kind == 8) {   // close values, ratio near 0 or 1 (vertices on power-of-two coordinates below)
+            va = (float)unit(h1); vb = __int_as_float(__float_as_int(va) + (int)(h2 & 3) + 1);
+            const double t = unit(h3) * 1e-6;
+            iso = ((h3 >> 60) & 1) ? (double)va + ((double)vb - (double)va) * t
+                                   : (double)vb - ((double)vb - (double)va) * t;
+        } else {                  // isolevel a double just off a float value, close values
+            va = (float)unit(h1); vb = __int_as_float(__float_as_int(va) + 1);
+            iso = (double)va + ((double)vb - (double)va) * unit(h3) * 1e-3;
         }
         const float f_iso = (float)iso;
         float thr = f_iso;
@@ -66,7 +74,9 @@ __global__ void k_selftest(uint64_t n, uint64_t seed, unsigned long long* counte
         j.vmin = -3.0e38; j.vmax = 3.0e38;
         for (int k = 0; k < 3; ++k) { j.min_coord[k] = 0.0f; j.scale[k] = 1.0f; }
         const int axis = (int)((h3 >> 20) % 3);
-        const float a = (float)((h3 >> 24) & 2047);
+        // kinds 8 and 9: the edge starts or ends on a power of two
+        const float a = kind >= 8 ? (float)(1u << ((h3 >> 24) & 10)) - (((h3 >> 50) & 1) ? 1.0f : 0.0f)
+                                  : (float)((h3 >> 24) & 2047);
         const bool rev = (h3 >> 40) & 1;
         float ax = (float)((h2 >> 30) & 2047), ay = (float)((h2 >> 41) & 2047), az = (float)((h1 >> 30) & 2047);
         float bx = ax, by = ay, bz = az;
@@ -75,15 +85,20 @@ __global__ void k_selftest(uint64_t n, uint64_t seed, unsigned long long* counte
         *pa = rev ? a + 1.0f : a;
         *pb = rev ? a : a + 1.0f;
         const float3 ex = interpolate_exact(j, (double)va, (double)vb, ax, ay, az, bx, by, bz);
-        // the fast path alone (no fallback) to count fallbacks
-        float r;
+        // every certified FP32 path must agree with the FP64 sequence where it
+        // claims certainty: fast_axis (and edge_vertex_fast, which falls back)
+        // and fast_axis_bf (the streaming kernels' branch-free form)
+        const float want = axis == 0 ? ex.x : (axis == 1 ? ex.y : ex.z);
+        float r, rb;
         const float v0 = va, v1 = vb;
         const bool ok = fast_axis(v0, v1, *pa, *pb, f, r);
+        const bool okb = fast_axis_bf(v0, v1, *pa, *pb, f, rb);
         const float3 fv = edge_vertex_fast(j, f, va, vb, ax, ay, az, bx, by, bz, axis);
         ++tested;
-        if (!ok) ++fall;
+        if (!okb) ++fall;
         if (__float_as_int(ex.x) != __float_as_int(fv.x) || __float_as_int(ex.y) != __float_as_int(fv.y) ||
-            __float_as_int(ex.z) != __float_as_int(fv.z))
+            __float_as_int(ex.z) != __float_as_int(fv.z) ||
+            (ok && __float_as_int(r) != __float_as_int(want)) || (okb && __float_as_int(rb) != __float_as_int(want)))
             ++mism;
     }
     atomicAdd(&counters[0], tested);
