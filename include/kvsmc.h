@@ -148,7 +148,8 @@ kvsmc_status kvsmc_extract_device(kvsmc_context* ctx, kvsmc_volume* vol, const k
                                   kvsmc_sizes* sizes);
 
 /* Host-side allocator for the output arrays: which = 0 coords (float),
- * 1 normals (float), 2 connections (uint32); count = elements (> 0).
+ * 1 normals (float), 2 connections (uint32), 3 colours (uint8, slice plane);
+ * count = elements (> 0).
  * Return NULL to fail the call with KVSMC_ERR_OUT_OF_MEMORY. */
 typedef void* (*kvsmc_host_alloc_fn)(void* user, int32_t which, uint64_t count);
 
@@ -312,6 +313,39 @@ kvsmc_status kvsmc_extract_noalloc(const void* d_values, kvsmc_dtype dtype, uint
                                    uint32_t nz, const kvsmc_params* p, float* d_coords,
                                    uint64_t coords_capacity, float* d_normals, uint64_t normals_capacity,
                                    void* cuda_stream, kvsmc_sizes* sizes);
+
+/* -------------------------------------------------------------- slice plane */
+
+/* kvs::SlicePlane on a structured volume (Source/Core/Visualization/Mapper/
+ * SlicePlane.cpp): marching cubes on the plane a x + b y + c z + d (cases
+ * from its sign at the corners), one RGB colour per vertex from the
+ * transfer function at the interpolated volume value, one normal per
+ * triangle; duplicated vertices, coords float[9T], colours uint8[9T],
+ * normals float[3T], in the reference's cell and table order, same bits.
+ * The host decides what MapperBase decides (the colour map range, the
+ * coordinate transform) and passes it here. */
+typedef struct kvsmc_slice_params {
+    float coefficients[4];      /* a, b, c, d (SlicePlane::setPlane; point p, normal n -> (n, -p.n)) */
+    float min_coord[3];         /* volume->minObjectCoord() */
+    float scale[3];             /* (max_coord - min_coord) / ncells */
+    float tf_min, tf_max;       /* the colour map's range (MapperBase::setRange) */
+    int32_t tf_resolution;      /* colour table entries */
+    const uint8_t* tf_table;    /* host, tf_resolution x RGB */
+} kvsmc_slice_params;
+
+/* Triangles of the slice (count pass only). */
+kvsmc_status kvsmc_slice_count(kvsmc_context* ctx, kvsmc_volume* vol, const kvsmc_slice_params* p,
+                               uint64_t* ntriangles);
+/* Count + emit into DEVICE buffers (capacities in elements); on
+ * KVSMC_ERR_CAPACITY nothing is written and *ntriangles holds the need. */
+kvsmc_status kvsmc_slice_extract_device(kvsmc_context* ctx, kvsmc_volume* vol, const kvsmc_slice_params* p,
+                                        float* d_coords, uint64_t coords_capacity, uint8_t* d_colors,
+                                        uint64_t colors_capacity, float* d_normals, uint64_t normals_capacity,
+                                        uint64_t* ntriangles);
+/* Count + emit into host arrays from `alloc` (which: 0 coords, 1 normals,
+ * 3 colours (uint8)); nothing is allocated for an empty slice. */
+kvsmc_status kvsmc_slice_plane(kvsmc_context* ctx, kvsmc_volume* vol, const kvsmc_slice_params* p,
+                               kvsmc_host_alloc_fn alloc, void* user, uint64_t* ntriangles);
 
 /* ------------------------------------------------------------ volume ingest */
 

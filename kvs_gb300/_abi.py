@@ -48,6 +48,7 @@ EXPORTS = [
     "kvsmc_tuning_force", "kvsmc_autotune", "kvsmc_stl_records", "kvsmc_write_stl",
     "kvsmc_write_stl_host", "kvsmc_volume_download", "kvsmc_kvsml_read_info", "kvsmc_volume_load_kvsml",
     "kvsmc_avs_read_info", "kvsmc_volume_load_avs",
+    "kvsmc_slice_count", "kvsmc_slice_extract_device", "kvsmc_slice_plane",
 ]
 
 PATH_AUTO = 0      # streaming kernels where eligible
@@ -101,6 +102,12 @@ class KvsmlInfo(C.Structure):
                 ("volume_max", C.c_double), ("has_object_coord", C.c_int32), ("has_external_coord", C.c_int32),
                 ("min_object_coord", C.c_float * 3), ("max_object_coord", C.c_float * 3),
                 ("min_external_coord", C.c_float * 3), ("max_external_coord", C.c_float * 3)]
+
+
+class SliceParams(C.Structure):
+    _fields_ = [("coefficients", C.c_float * 4), ("min_coord", C.c_float * 3), ("scale", C.c_float * 3),
+                ("tf_min", C.c_float), ("tf_max", C.c_float), ("tf_resolution", C.c_int32),
+                ("tf_table", C.c_void_p)]
 
 
 class TuneChoice(C.Structure):
@@ -183,6 +190,10 @@ def load(path=LIB_PATH):
         "kvsmc_plan_destroy": (None, [vp]),
         "kvsmc_stl_records": (C.c_int, [vp, i32, vp, vp, vp, u64, u64, vp]),
         "kvsmc_volume_download": (C.c_int, [vp, vp, vp]),
+        "kvsmc_slice_count": (C.c_int, [vp, vp, C.POINTER(SliceParams), C.POINTER(u64)]),
+        "kvsmc_slice_extract_device": (C.c_int, [vp, vp, C.POINTER(SliceParams), vp, u64, vp, u64, vp, u64,
+                                                 C.POINTER(u64)]),
+        "kvsmc_slice_plane": (C.c_int, [vp, vp, C.POINTER(SliceParams), HOST_ALLOC, vp, C.POINTER(u64)]),
         "kvsmc_kvsml_read_info": (C.c_int, [C.c_char_p, C.POINTER(KvsmlInfo)]),
         "kvsmc_volume_load_kvsml": (C.c_int, [vp, C.c_char_p, C.POINTER(vp), C.POINTER(KvsmlInfo)]),
         "kvsmc_avs_read_info": (C.c_int, [C.c_char_p, C.POINTER(KvsmlInfo)]),

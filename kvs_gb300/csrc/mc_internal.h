@@ -111,6 +111,27 @@ cudaError_t launch_unit_scan(const StreamGroup* d_groups, int ngroups, uint32_t 
 cudaError_t launch_iso_totals(const StreamIso* d_isos, int n, const uint64_t* d_plane_base, const uint64_t* d_total,
                               uint64_t* d_totals, const Launch& L);
 
+// ---- SlicePlane on structured volumes (slice.cu): tiles of up to `rows`
+// cell rows of one plane z, numbered row group fastest
+struct SliceJob {
+    VolumeView vol;
+    float coef[4];            // a x + b y + c z + d
+    float min_coord[3], scale[3];
+    float tf_min, tf_max;     // colour map range
+    int32_t tf_res;
+    const uint8_t* table;     // device colour table, tf_res x RGB
+    uint32_t rows, ytiles;
+    uint64_t tiles;
+    uint32_t* tile_counts;    // count pass: triangles per tile
+    uint64_t* tile_offsets;   // emit pass: exclusive scan of tile_counts
+    float* coords;            // 9 T
+    uint8_t* colors;          // 9 T (RGB per vertex)
+    float* normals;           // 3 T
+    uint64_t cap_tris;        // triangles the outputs hold
+};
+cudaError_t launch_slice_count(const SliceJob& j, const Launch& L);
+cudaError_t launch_slice_emit(const SliceJob& j, const Launch& L);
+
 // ---- binary STL records (export.cu): 50 bytes per triangle; bad_index: a
 // device word set to 1 when a connection index is >= nverts (that vertex
 // then reads as vertex 0)

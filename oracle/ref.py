@@ -84,6 +84,10 @@ def lib():
             C.c_int, C.c_int, C.c_void_p, C.c_uint, C.c_uint, C.c_uint,
             C.c_double, C.c_int, C.c_int, C.c_int, C.c_double, C.c_double,
             C.c_int, C.c_int, C.c_float, C.c_float, C.POINTER(_Result)]
+        _lib.kvsref_slice_plane.restype = C.c_int
+        _lib.kvsref_slice_plane.argtypes = [
+            C.c_int, C.c_int, C.c_void_p, C.c_uint, C.c_uint, C.c_uint, C.c_void_p,
+            C.c_int, C.c_double, C.c_double, C.c_int, C.c_int, C.c_float, C.c_float, C.POINTER(_Result)]
         _lib.kvsref_marching_cubes_stl.restype = C.c_int
         _lib.kvsref_marching_cubes_stl.argtypes = [
             C.c_int, C.c_void_p, C.c_uint, C.c_uint, C.c_uint, C.c_double, C.c_int, C.c_int, C.c_char_p]
@@ -179,6 +183,30 @@ def isosurface(values, form, isolevel=0.0, normal_type="polygon", duplication=Tr
         float(tf_range[1]) if tf_range is not None else 0.0, C.byref(r))
     if st != 0:
         raise RuntimeError("kvsref_isosurface failed")
+    return _collect(r)
+
+
+def slice_plane(values, coefficients=None, point=None, normal=None, minmax=None, tf_resolution=256,
+                tf_range=None):
+    """The reference kvs::SlicePlane on a uniform volume shaped (nz, ny, nx):
+    by plane coefficients (a, b, c, d), or by a point and a normal."""
+    v = np.ascontiguousarray(values)
+    nz, ny, nx = v.shape
+    if coefficients is not None:
+        form, plane = 0, np.ascontiguousarray(coefficients, np.float32)
+    else:
+        form, plane = 1, np.ascontiguousarray(list(point) + list(normal), np.float32)
+    r = _Result()
+    st = lib().kvsref_slice_plane(
+        form, dtype_code(v.dtype), v.ctypes.data, nx, ny, nz, plane.ctypes.data,
+        1 if minmax is not None else 0,
+        float(minmax[0]) if minmax is not None else 0.0,
+        float(minmax[1]) if minmax is not None else 0.0,
+        tf_resolution, 1 if tf_range is not None else 0,
+        float(tf_range[0]) if tf_range is not None else 0.0,
+        float(tf_range[1]) if tf_range is not None else 0.0, C.byref(r))
+    if st != 0:
+        raise RuntimeError("kvsref_slice_plane failed")
     return _collect(r)
 
 

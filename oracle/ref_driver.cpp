@@ -15,6 +15,7 @@
 #include <kvs/PolygonExporter>
 #include <kvs/Stl>
 #include <kvs/AVSField>
+#include <kvs/SlicePlane>
 #include <kvs/TransferFunction>
 #include <kvs/HydrogenVolumeData>
 #include <kvs/ValueArray>
@@ -182,6 +183,39 @@ int kvsref_marching_cubes(
     Fill( mc, mc, vol, out );
     out->seconds = best;
     delete mc;
+    delete vol;
+    return 0;
+}
+
+/*
+ * The reference kvs::SlicePlane (Source/Core/Visualization/Mapper/SlicePlane.cpp)
+ * on a uniform structured volume: form 0 SlicePlane( volume, coefficients, tf ),
+ * form 1 SlicePlane( volume, point, normal, tf ) (plane[0..2] point,
+ * plane[3..5] normal).
+ */
+int kvsref_slice_plane(
+    int form, int dtype, const void* values, unsigned nx, unsigned ny, unsigned nz, const float* plane,
+    int has_minmax, double vmin, double vmax, int tf_resolution, int tf_has_range, float tf_min, float tf_max,
+    kvsref_result* out )
+{
+    std::memset( out, 0, sizeof( *out ) );
+    const size_t n = size_t( nx ) * ny * nz;
+    kvs::AnyValueArray vals = Values( dtype, values, n );
+    if ( vals.size() != n ) return -1;
+    kvs::TransferFunction tfunc( tf_resolution > 0 ? tf_resolution : 256 );
+    if ( tf_has_range ) tfunc.setRange( tf_min, tf_max );
+    auto* vol = new kvs::StructuredVolumeObject();
+    vol->setVeclen( 1 );
+    vol->setResolution( kvs::Vec3ui( nx, ny, nz ) );
+    vol->setValues( vals );
+    vol->setGridTypeToUniform();
+    if ( has_minmax ) vol->setMinMaxValues( vmin, vmax );
+    kvs::SlicePlane* s = nullptr;
+    if ( form == 0 ) s = new kvs::SlicePlane( vol, kvs::Vec4( plane[0], plane[1], plane[2], plane[3] ), tfunc );
+    else s = new kvs::SlicePlane( vol, kvs::Vec3( plane[0], plane[1], plane[2] ),
+                                  kvs::Vec3( plane[3], plane[4], plane[5] ), tfunc );
+    Fill( s, s, vol, out );
+    delete s;
     delete vol;
     return 0;
 }

@@ -6,11 +6,12 @@ by oracle/Makefile.ref) on small seeded inputs and stores inputs + outputs in
 tests/golden/golden.npz (case list tests/golden/cases.json) and
 tests/golden/isosurface.npz (tests/golden/isosurface.json), and binary STL
 files written by the reference PolygonExporter<kvs::Stl> in tests/golden/stl.npz
-(tests/golden/stl.json).  The reference
+(tests/golden/stl.json), and kvs::SlicePlane results in tests/golden/slice.npz
+(tests/golden/slice.json).  The reference
 ships no tests or golden vectors of its own, so these fixtures pin the oracle
 restatement and the CUDA path on hosts where the reference is absent.
 
-    python tests/golden/make_golden.py [marching_cubes] [isosurface] [stl]   (default: all)
+    python tests/golden/make_golden.py [marching_cubes] [isosurface] [stl] [slice]   (default: all)
 """
 import json
 import os
@@ -147,10 +148,58 @@ def write_stl():
     print(f"{len(manifest)} stl cases")
 
 
+def slice_cases():
+    """(name, volume, [(coefficients or None, point, normal, tf_range), ...])"""
+    rng = np.random.default_rng(55)
+    h = ref.hydrogen(16)
+    x, y, z = np.meshgrid(np.arange(20), np.arange(18), np.arange(16), indexing="xy")
+    blob = np.exp(-((x - 9.3) ** 2 + (y - 8.1) ** 2 + (z - 7.7) ** 2) / (2 * 5.0 ** 2)).transpose(2, 0, 1)
+    blob = np.ascontiguousarray(blob).astype(np.float32)
+    shape = (9, 10, 11)
+    obl = (None, (5.3, 4.7, 3.9), (0.31, -0.52, 0.79), None)
+    return [
+        ("hydrogen16", h, [((0, 0, 1, -7.5), None, None, None), obl, ((0, 0, 1, -7), None, None, None),
+                           ((1, 1, 1, -20), None, None, None), ((0, 0, 1, 100), None, None, None),
+                           (None, (7.3, 7.7, 8.1), (0.3, -0.5, 0.8), (10.0, 200.0))]),
+        ("blob_f32", blob, [obl, ((0.2, 0.9, -0.4, -3.3), None, None, None)]),
+        ("random_i8", rng.integers(-128, 128, shape).astype(np.int8), [((0, 0, 1, -4.25), None, None, None)]),
+        ("random_u16", rng.integers(0, 65536, shape).astype(np.uint16), [((1, 0, 0, -5.5), None, None, None)]),
+        ("random_i16", rng.integers(-3000, 3000, shape).astype(np.int16), [obl]),
+        ("random_i32", rng.integers(-2 ** 30, 2 ** 30, shape).astype(np.int32), [obl]),
+        ("random_u32", rng.integers(0, 2 ** 32 - 1, shape, dtype=np.uint64).astype(np.uint32), [obl]),
+        ("random_i64", rng.integers(-2 ** 60, 2 ** 60, shape).astype(np.int64), [obl]),
+        ("random_u64", rng.integers(0, 2 ** 63, shape, dtype=np.uint64), [obl]),
+        ("random_f64", rng.standard_normal(shape), [obl]),
+        ("constant_f32", np.full((4, 5, 6), 2.0, np.float32), [((0, 1, 0, -1.5), None, None, None)]),
+    ]
+
+
+def write_slice():
+    arrays, manifest = {}, []
+    for name, v, runs in slice_cases():
+        arrays[f"{name}__input"] = v
+        for i, (coef, point, normal, tfr) in enumerate(runs):
+            key = f"{name}__{i}"
+            r = ref.slice_plane(v, coefficients=coef, point=point, normal=normal, tf_range=tfr)
+            for fld in ("coords", "normals", "colors", "opacities"):
+                arrays[f"{key}__{fld}"] = r[fld]
+            manifest.append(dict(key=key, case=name, coefficients=coef, point=point, normal=normal, tf_range=tfr,
+                                 success=r["success"], polygon_type=r["polygon_type"], color_type=r["color_type"],
+                                 normal_type=r["normal_type"], min_obj=r["min_obj"].tolist(),
+                                 max_obj=r["max_obj"].tolist(), min_ext=r["min_ext"].tolist(),
+                                 max_ext=r["max_ext"].tolist(), ntriangles=int(r["coords"].size // 9)))
+    np.savez_compressed(os.path.join(HERE, "slice.npz"), **arrays)
+    with open(os.path.join(HERE, "slice.json"), "w") as f:
+        json.dump(manifest, f, indent=0)
+    print(f"{len(manifest)} slice cases")
+
+
 def main():
     if not ref.available():
         ref.build()
-    parts = sys.argv[1:] or ["marching_cubes", "isosurface", "stl"]
+    parts = sys.argv[1:] or ["marching_cubes", "isosurface", "stl", "slice"]
+    if "slice" in parts:
+        write_slice()
     if "isosurface" in parts:
         write_isosurface()
     if "stl" in parts:
