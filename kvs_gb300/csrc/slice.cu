@@ -177,6 +177,25 @@ __device__ __forceinline__ void slice_tile(const SliceJob& j, uint64_t tile, uin
     rows = (cy - y0) < j.rows ? (cy - y0) : j.rows;
 }
 
+// True when every node of the tile's cells (x in [0, cx], y in [y0, y0 + rows],
+// z in [z, z + 1]) evaluates to the same side of the plane in float, so no
+// cell of the tile is cut.  The plane is linear: its exact range over the box
+// is taken at the box corners in double (the float products of the
+// coefficients with integers below 2^24 are exact there); the float
+// evaluation ((a x + b y) + c z) + d differs from the exact value by less
+// than 2^-21 (|a| x_max + |b| y_max + |c| z_max + |d|) (four roundings of
+// 2^-24 each), so a range beyond that margin decides every node's sign.
+__device__ __forceinline__ bool tile_uncut(const SliceJob& j, uint32_t cx, uint32_t y0, uint32_t rows, uint32_t z)
+{
+    const double a = j.coef[0], b = j.coef[1], c = j.coef[2], d = j.coef[3];
+    const double x0 = 0.0, x1 = (double)cx, ya = (double)y0, yb = (double)(y0 + rows), za = (double)z,
+                 zb = (double)(z + 1);
+    const double lo = (a < 0 ? a * x1 : a * x0) + (b < 0 ? b * yb : b * ya) + (c < 0 ? c * zb : c * za) + d;
+    const double hi = (a < 0 ? a * x0 : a * x1) + (b < 0 ? b * ya : b * yb) + (c < 0 ? c * za : c * zb) + d;
+    const double m = 4.76837158203125e-07 * (fabs(a) * x1 + fabs(b) * yb + fabs(c) * zb + fabs(d)) + 1e-30;
+    return lo > m || hi < -m;
+}
+
 __device__ __forceinline__ uint32_t block_sum_u32(uint32_t v, uint32_t* ws)
 {
     for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
@@ -217,6 +236,10 @@ __global__ void __launch_bounds__(kSliceThreads) k_slice_count(SliceJob j)
     for (uint64_t tile = blockIdx.x; tile < j.tiles; tile += gridDim.x) {
         uint32_t z, y0, rows;
         slice_tile(j, tile, z, y0, rows);
+        if (tile_uncut(j, cx, y0, rows, z)) {   // uniform across the block
+            if (threadIdx.x == 0) j.tile_counts[tile] = 0;
+            continue;
+        }
         uint32_t sum = 0;
         for (uint32_t r = 0; r < rows; ++r)
             for (uint32_t x = threadIdx.x; x < cx; x += blockDim.x) sum += c_slice_ntri[slice_case(j, x, y0 + r, z)];
@@ -234,6 +257,7 @@ __global__ void __launch_bounds__(kSliceThreads) k_slice_emit(SliceJob j)
     for (uint64_t tile = blockIdx.x; tile < j.tiles; tile += gridDim.x) {
         uint32_t z, y0, rows;
         slice_tile(j, tile, z, y0, rows);
+        if (tile_uncut(j, cx, y0, rows, z)) continue;   // uniform across the block
         uint64_t running = j.tile_offsets[tile];
         for (uint32_t r = 0; r < rows; ++r) {
             const uint32_t y = y0 + r;
