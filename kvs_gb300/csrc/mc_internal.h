@@ -111,8 +111,8 @@ cudaError_t launch_unit_scan(const StreamGroup* d_groups, int ngroups, uint32_t 
 cudaError_t launch_iso_totals(const StreamIso* d_isos, int n, const uint64_t* d_plane_base, const uint64_t* d_total,
                               uint64_t* d_totals, const Launch& L);
 
-// ---- SlicePlane on structured volumes (slice.cu): tiles of up to `rows`
-// cell rows of one plane z, numbered row group fastest
+// ---- SlicePlane on structured volumes (slice.cu): one warp per cell row
+// (y, z), rows numbered y fastest
 struct SliceJob {
     VolumeView vol;
     float coef[4];            // a x + b y + c z + d
@@ -120,10 +120,9 @@ struct SliceJob {
     float tf_min, tf_max;     // colour map range
     int32_t tf_res;
     const uint8_t* table;     // device colour table, tf_res x RGB
-    uint32_t rows, ytiles;
-    uint64_t tiles;
-    uint32_t* tile_counts;    // count pass: triangles per tile
-    uint64_t* tile_offsets;   // emit pass: exclusive scan of tile_counts
+    uint64_t nrows;           // (ny - 1) (nz - 1)
+    uint32_t* row_counts;     // count pass: triangles per row
+    uint64_t* row_offsets;    // emit pass: exclusive scan of row_counts
     float* coords;            // 9 T
     uint8_t* colors;          // 9 T (RGB per vertex)
     float* normals;           // 3 T

@@ -13,10 +13,11 @@
 // 1043-1054, RGBColor::Mix, RGBColor(Vec3) rounding); one normal per triangle
 // -((v2 - v0) x (v1 - v0)).  Cells in z, y, x order.
 //
-// Two passes over tiles of cell rows (one plane z, up to a few rows): count
-// (cases from the plane alone, no volume read), an exclusive scan of the tile
-// counts, then emit (block-wide scan of each cell's triangle count, the
-// volume read only at the corners of cut edges).
+// Two passes, one warp per cell row (y, z): count (cases from the plane
+// alone, only over the x-interval of cells the plane can cut, bounded
+// conservatively in double), an exclusive scan of the row counts, then emit
+// (a warp scan of each cell's triangle count; the volume read only at the
+// corners of cut edges).
 #include <cuda_runtime.h>
 
 #include <cstring>
@@ -121,7 +122,10 @@ __device__ __forceinline__ uchar3 color_at(const SliceJob& j, float value)
         float m = __fadd_rn(__fmul_rn(a, __fsub_rn(1.0f, t)), __fmul_rn(b, t));
         m = m <= 0.0f ? 0.0f : (m <= 1.0f ? m : 1.0f);
         const float x = __fmul_rn(m, 255.0f);
-        out[k] = (uint8_t)__double2int_rz(__dadd_rn((double)x, 0.5));
+        // Math::Round: (int)(x + 0.5) in double for x in [0, 255], i.e. the
+        // integer part plus one when the (exact) fraction is at least 1/2
+        const float ip = truncf(x);
+        out[k] = (uint8_t)((int)ip + (__fsub_rn(x, ip) >= 0.5f ? 1 : 0));
     }
     return make_uchar3(out[0], out[1], out[2]);
 }
@@ -169,142 +173,136 @@ __device__ __forceinline__ float3 slice_normal(float3 a, float3 b, float3 c)
     return n;
 }
 
-__device__ __forceinline__ void slice_tile(const SliceJob& j, uint64_t tile, uint32_t& z, uint32_t& y0, uint32_t& rows)
-{
-    z = (uint32_t)(tile / j.ytiles);
-    y0 = (uint32_t)(tile - (uint64_t)z * j.ytiles) * j.rows;
-    const uint32_t cy = j.vol.ny - 1;
-    rows = (cy - y0) < j.rows ? (cy - y0) : j.rows;
-}
-
-// True when every node of the tile's cells (x in [0, cx], y in [y0, y0 + rows],
-// z in [z, z + 1]) evaluates to the same side of the plane in float, so no
-// cell of the tile is cut.  The plane is linear: its exact range over the box
-// is taken at the box corners in double (the float products of the
-// coefficients with integers below 2^24 are exact there); the float
-// evaluation ((a x + b y) + c z) + d differs from the exact value by less
-// than 2^-21 (|a| x_max + |b| y_max + |c| z_max + |d|) (four roundings of
-// 2^-24 each), so a range beyond that margin decides every node's sign.
-__device__ __forceinline__ bool tile_uncut(const SliceJob& j, uint32_t cx, uint32_t y0, uint32_t rows, uint32_t z)
+// The cells of row (y, z) the plane can cut: an interval [x0, x1] of x (x0 >
+// x1: none).  Over a cell the plane ranges over [a x + min(0, a) + Bmin + Cmin
+// + d, a x + max(0, a) + Bmax + Cmax + d] (B, C: b y', c z' over the cell's
+// y', z'), exactly, in double (the products of float coefficients with
+// integers below 2^24 are exact there).  The float evaluation
+// ((a x + b y) + c z) + d of a node is within 2^-21 (|a| cx + |b| (y + 1) +
+// |c| (z + 1) + |d|) of the exact value (four roundings of 2^-24 each, times
+// 2), so a cell whose exact range lies beyond that margin on one side has
+// all its corners on that side in float: case 0 or 255, no triangle.  The
+// interval is padded by one cell for the double arithmetic of its ends.
+__device__ __forceinline__ void row_interval(const SliceJob& j, uint32_t cx, uint32_t y, uint32_t z, int64_t& x0,
+                                             int64_t& x1)
 {
     const double a = j.coef[0], b = j.coef[1], c = j.coef[2], d = j.coef[3];
-    const double x0 = 0.0, x1 = (double)cx, ya = (double)y0, yb = (double)(y0 + rows), za = (double)z,
-                 zb = (double)(z + 1);
-    const double lo = (a < 0 ? a * x1 : a * x0) + (b < 0 ? b * yb : b * ya) + (c < 0 ? c * zb : c * za) + d;
-    const double hi = (a < 0 ? a * x0 : a * x1) + (b < 0 ? b * ya : b * yb) + (c < 0 ? c * za : c * zb) + d;
-    const double m = 4.76837158203125e-07 * (fabs(a) * x1 + fabs(b) * yb + fabs(c) * zb + fabs(d)) + 1e-30;
-    return lo > m || hi < -m;
-}
-
-__device__ __forceinline__ uint32_t block_sum_u32(uint32_t v, uint32_t* ws)
-{
-    for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
-    const unsigned lane = threadIdx.x & 31u, warp = threadIdx.x >> 5;
-    __syncthreads();
-    if (lane == 0) ws[warp] = v;
-    __syncthreads();
-    uint32_t t = 0;
-    for (unsigned w = 0; w < blockDim.x / 32; ++w) t += ws[w];
-    return t;
-}
-
-// Exclusive scan over the block; *total = the block's sum.
-__device__ __forceinline__ uint32_t block_excl_u32(uint32_t v, uint32_t* ws, uint32_t* total)
-{
-    const unsigned lane = threadIdx.x & 31u, warp = threadIdx.x >> 5;
-    uint32_t inc = v;
-    for (int o = 1; o < 32; o <<= 1) {
-        const uint32_t t = __shfl_up_sync(0xffffffffu, inc, o);
-        if (lane >= (unsigned)o) inc += t;
+    const double by0 = b * (double)y, by1 = b * (double)(y + 1), cz0 = c * (double)z, cz1 = c * (double)(z + 1);
+    const double m = 4.76837158203125e-07 * (fabs(a) * (double)cx + fabs(b) * (double)(y + 1) +
+                                             fabs(c) * (double)(z + 1) + fabs(d)) + 1e-30;
+    const double k1 = fmin(0.0, a) + fmin(by0, by1) + fmin(cz0, cz1) + d - m;   // low end <= margin: a x + k1 <= 0
+    const double k2 = fmax(0.0, a) + fmax(by0, by1) + fmax(cz0, cz1) + d + m;   // high end > -margin: a x + k2 > 0
+    x0 = 0;
+    x1 = (int64_t)cx - 1;
+    if (!(k1 == k1) || !(k2 == k2) || !(a == a)) return;   // NaN plane: every cell is evaluated
+    if (a == 0.0) {
+        if (!(k1 <= 0.0 && k2 > 0.0)) x1 = -1;
+        return;
     }
-    __syncthreads();
-    if (lane == 31) ws[warp] = inc;
-    __syncthreads();
-    uint32_t before = 0, all = 0;
-    for (unsigned w = 0; w < blockDim.x / 32; ++w) {
-        before += w < warp ? ws[w] : 0u;
-        all += ws[w];
-    }
-    *total = all;
-    return before + inc - v;
+    double lo, hi;   // x in [lo, hi] (open ends widened below)
+    if (a > 0.0) { lo = -k2 / a; hi = -k1 / a; }
+    else { lo = -k1 / a; hi = -k2 / a; }
+    if (!(lo <= hi)) { x1 = -1; return; }
+    const double cap = (double)cx;
+    lo = fmax(lo, -2.0);
+    hi = fmin(hi, cap + 1.0);
+    const int64_t l = (int64_t)floor(lo) - 1, h = (int64_t)ceil(hi) + 1;
+    x0 = l > 0 ? l : 0;
+    x1 = h < (int64_t)cx - 1 ? h : (int64_t)cx - 1;
 }
 
+// One thread per cell row (y, z), rows in z, y order: the triangles of the
+// cells of its interval (the interval's double arithmetic once per row).
 __global__ void __launch_bounds__(kSliceThreads) k_slice_count(SliceJob j)
 {
-    __shared__ uint32_t ws[32];
-    const uint32_t cx = j.vol.nx - 1;
-    for (uint64_t tile = blockIdx.x; tile < j.tiles; tile += gridDim.x) {
-        uint32_t z, y0, rows;
-        slice_tile(j, tile, z, y0, rows);
-        if (tile_uncut(j, cx, y0, rows, z)) {   // uniform across the block
-            if (threadIdx.x == 0) j.tile_counts[tile] = 0;
-            continue;
-        }
+    const uint32_t cx = j.vol.nx - 1, cy = j.vol.ny - 1;
+    for (uint64_t row = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; row < j.nrows;
+         row += (uint64_t)gridDim.x * blockDim.x) {
+        const uint32_t z = (uint32_t)(row / cy), y = (uint32_t)(row - (uint64_t)z * cy);
+        int64_t x0, x1;
+        row_interval(j, cx, y, z, x0, x1);
         uint32_t sum = 0;
-        for (uint32_t r = 0; r < rows; ++r)
-            for (uint32_t x = threadIdx.x; x < cx; x += blockDim.x) sum += c_slice_ntri[slice_case(j, x, y0 + r, z)];
-        const uint32_t t = block_sum_u32(sum, ws);
-        if (threadIdx.x == 0) j.tile_counts[tile] = t;
+        for (int64_t x = x0; x <= x1; ++x) sum += c_slice_ntri[slice_case(j, (uint32_t)x, y, z)];
+        j.row_counts[row] = sum;
     }
 }
 
 template <typename T>
 __global__ void __launch_bounds__(kSliceThreads) k_slice_emit(SliceJob j)
 {
-    __shared__ uint32_t ws[32];
     const T* vol = static_cast<const T*>(j.vol.data);
-    const uint32_t cx = j.vol.nx - 1;
-    for (uint64_t tile = blockIdx.x; tile < j.tiles; tile += gridDim.x) {
-        uint32_t z, y0, rows;
-        slice_tile(j, tile, z, y0, rows);
-        if (tile_uncut(j, cx, y0, rows, z)) continue;   // uniform across the block
-        uint64_t running = j.tile_offsets[tile];
-        for (uint32_t r = 0; r < rows; ++r) {
-            const uint32_t y = y0 + r;
-            for (uint32_t xc = 0; xc < cx; xc += blockDim.x) {
-                const uint32_t x = xc + threadIdx.x;
-                const unsigned c = x < cx ? slice_case(j, x, y, z) : 0u;
-                const uint32_t n = c_slice_ntri[c];
-                uint32_t tot;
-                const uint32_t excl = block_excl_u32(n, ws, &tot);
-                uint64_t t = running + excl;
-                uint64_t pk = c_slice_tri[c];
-                for (uint32_t k = 0; k < n; ++k, ++t, pk >>= 12) {
-                    if (t >= j.cap_tris) break;   // never past the outputs
-                    const SliceVertex a = slice_vertex<T>(j, vol, x, y, z, (int)(pk & 15u));
-                    const SliceVertex b = slice_vertex<T>(j, vol, x, y, z, (int)((pk >> 4) & 15u));
-                    const SliceVertex d = slice_vertex<T>(j, vol, x, y, z, (int)((pk >> 8) & 15u));
-                    float* o = j.coords + 9 * t;
-                    o[0] = a.p.x; o[1] = a.p.y; o[2] = a.p.z;
-                    o[3] = b.p.x; o[4] = b.p.y; o[5] = b.p.z;
-                    o[6] = d.p.x; o[7] = d.p.y; o[8] = d.p.z;
-                    uint8_t* col = j.colors + 9 * t;
-                    col[0] = a.rgb.x; col[1] = a.rgb.y; col[2] = a.rgb.z;
-                    col[3] = b.rgb.x; col[4] = b.rgb.y; col[5] = b.rgb.z;
-                    col[6] = d.rgb.x; col[7] = d.rgb.y; col[8] = d.rgb.z;
-                    const float3 nn = slice_normal(a.p, b.p, d.p);
-                    float* q = j.normals + 3 * t;
-                    q[0] = nn.x; q[1] = nn.y; q[2] = nn.z;
-                }
-                running += tot;
+    const uint32_t cx = j.vol.nx - 1, cy = j.vol.ny - 1;
+    const unsigned lane = threadIdx.x & 31u;
+    const uint64_t warps = (uint64_t)gridDim.x * (blockDim.x / 32);
+    // each warp takes 32 consecutive rows: every lane works out one row's
+    // interval and offset, then the warp walks the rows one after another
+    for (uint64_t r0 = ((uint64_t)blockIdx.x * (blockDim.x / 32) + (threadIdx.x >> 5)) * 32; r0 < j.nrows;
+         r0 += warps * 32) {
+        const uint64_t my = r0 + lane;
+        int64_t mx0 = 0, mx1 = -1;
+        uint64_t moff = 0;
+        if (my < j.nrows) {
+            const uint32_t mz = (uint32_t)(my / cy), myy = (uint32_t)(my - (uint64_t)mz * cy);
+            row_interval(j, cx, myy, mz, mx0, mx1);
+            moff = j.row_offsets[my];
+        }
+        const uint32_t nr = (uint32_t)(j.nrows - r0 < 32 ? j.nrows - r0 : 32);
+        for (uint32_t i = 0; i < nr; ++i) {
+        const uint64_t row = r0 + i;
+        const uint32_t z = (uint32_t)(row / cy), y = (uint32_t)(row - (uint64_t)z * cy);
+        const int64_t x0 = __shfl_sync(0xffffffffu, mx0, i), x1 = __shfl_sync(0xffffffffu, mx1, i);
+        uint64_t running = __shfl_sync(0xffffffffu, moff, i);
+        for (int64_t xc = x0; xc <= x1; xc += 32) {
+            const int64_t xs = xc + lane;
+            const uint32_t x = (uint32_t)xs;
+            const unsigned c = xs <= x1 ? slice_case(j, x, y, z) : 0u;
+            const uint32_t n = c_slice_ntri[c];
+            uint32_t inc = n;
+            for (int o = 1; o < 32; o <<= 1) {
+                const uint32_t t = __shfl_up_sync(0xffffffffu, inc, o);
+                if (lane >= (unsigned)o) inc += t;
             }
+            const uint32_t tot = __shfl_sync(0xffffffffu, inc, 31);
+            uint64_t t = running + inc - n;
+            uint64_t pk = c_slice_tri[c];
+            for (uint32_t k = 0; k < n; ++k, ++t, pk >>= 12) {
+                if (t >= j.cap_tris) break;   // never past the outputs
+                const SliceVertex va = slice_vertex<T>(j, vol, x, y, z, (int)(pk & 15u));
+                const SliceVertex vb = slice_vertex<T>(j, vol, x, y, z, (int)((pk >> 4) & 15u));
+                const SliceVertex vd = slice_vertex<T>(j, vol, x, y, z, (int)((pk >> 8) & 15u));
+                float* o = j.coords + 9 * t;
+                o[0] = va.p.x; o[1] = va.p.y; o[2] = va.p.z;
+                o[3] = vb.p.x; o[4] = vb.p.y; o[5] = vb.p.z;
+                o[6] = vd.p.x; o[7] = vd.p.y; o[8] = vd.p.z;
+                uint8_t* col = j.colors + 9 * t;
+                col[0] = va.rgb.x; col[1] = va.rgb.y; col[2] = va.rgb.z;
+                col[3] = vb.rgb.x; col[4] = vb.rgb.y; col[5] = vb.rgb.z;
+                col[6] = vd.rgb.x; col[7] = vd.rgb.y; col[8] = vd.rgb.z;
+                const float3 nn = slice_normal(va.p, vb.p, vd.p);
+                float* q = j.normals + 3 * t;
+                q[0] = nn.x; q[1] = nn.y; q[2] = nn.z;
+            }
+            running += tot;
+        }
         }
     }
 }
 
-unsigned slice_grid(uint64_t tiles, const Launch& L)
+// blocks for `units` work items of `per_block` each, at most 16 per SM
+unsigned slice_grid(uint64_t units, uint64_t per_block, const Launch& L)
 {
+    const uint64_t blocks = (units + per_block - 1) / per_block;
     const uint64_t cap = (uint64_t)L.num_sms * 16;
-    return (unsigned)(tiles < cap ? (tiles ? tiles : 1) : cap);
+    return (unsigned)(blocks < cap ? (blocks ? blocks : 1) : cap);
 }
 
 }  // namespace
 
 cudaError_t launch_slice_count(const SliceJob& j, const Launch& L)
 {
-    if (j.tiles == 0) return cudaSuccess;
+    if (j.nrows == 0) return cudaSuccess;
     prof_begin(L, "slice_count");
-    k_slice_count<<<slice_grid(j.tiles, L), kSliceThreads, 0, L.stream>>>(j);
+    k_slice_count<<<slice_grid(j.nrows, kSliceThreads, L), kSliceThreads, 0, L.stream>>>(j);
     prof_end(L);
     *L.counter += 1;
     return cudaGetLastError();
@@ -312,19 +310,19 @@ cudaError_t launch_slice_count(const SliceJob& j, const Launch& L)
 
 cudaError_t launch_slice_emit(const SliceJob& j, const Launch& L)
 {
-    if (j.tiles == 0) return cudaSuccess;
+    if (j.nrows == 0) return cudaSuccess;
     prof_begin(L, "slice_emit");
     switch (j.vol.dtype) {
-    case 0: k_slice_emit<int8_t><<<slice_grid(j.tiles, L), kSliceThreads, 0, L.stream>>>(j); break;
-    case 1: k_slice_emit<int16_t><<<slice_grid(j.tiles, L), kSliceThreads, 0, L.stream>>>(j); break;
-    case 2: k_slice_emit<int32_t><<<slice_grid(j.tiles, L), kSliceThreads, 0, L.stream>>>(j); break;
-    case 3: k_slice_emit<long long><<<slice_grid(j.tiles, L), kSliceThreads, 0, L.stream>>>(j); break;
-    case 4: k_slice_emit<uint8_t><<<slice_grid(j.tiles, L), kSliceThreads, 0, L.stream>>>(j); break;
-    case 5: k_slice_emit<uint16_t><<<slice_grid(j.tiles, L), kSliceThreads, 0, L.stream>>>(j); break;
-    case 6: k_slice_emit<uint32_t><<<slice_grid(j.tiles, L), kSliceThreads, 0, L.stream>>>(j); break;
-    case 7: k_slice_emit<unsigned long long><<<slice_grid(j.tiles, L), kSliceThreads, 0, L.stream>>>(j); break;
-    case 8: k_slice_emit<float><<<slice_grid(j.tiles, L), kSliceThreads, 0, L.stream>>>(j); break;
-    case 9: k_slice_emit<double><<<slice_grid(j.tiles, L), kSliceThreads, 0, L.stream>>>(j); break;
+    case 0: k_slice_emit<int8_t><<<slice_grid(j.nrows, (kSliceThreads / 32) * 32, L), kSliceThreads, 0, L.stream>>>(j); break;
+    case 1: k_slice_emit<int16_t><<<slice_grid(j.nrows, (kSliceThreads / 32) * 32, L), kSliceThreads, 0, L.stream>>>(j); break;
+    case 2: k_slice_emit<int32_t><<<slice_grid(j.nrows, (kSliceThreads / 32) * 32, L), kSliceThreads, 0, L.stream>>>(j); break;
+    case 3: k_slice_emit<long long><<<slice_grid(j.nrows, (kSliceThreads / 32) * 32, L), kSliceThreads, 0, L.stream>>>(j); break;
+    case 4: k_slice_emit<uint8_t><<<slice_grid(j.nrows, (kSliceThreads / 32) * 32, L), kSliceThreads, 0, L.stream>>>(j); break;
+    case 5: k_slice_emit<uint16_t><<<slice_grid(j.nrows, (kSliceThreads / 32) * 32, L), kSliceThreads, 0, L.stream>>>(j); break;
+    case 6: k_slice_emit<uint32_t><<<slice_grid(j.nrows, (kSliceThreads / 32) * 32, L), kSliceThreads, 0, L.stream>>>(j); break;
+    case 7: k_slice_emit<unsigned long long><<<slice_grid(j.nrows, (kSliceThreads / 32) * 32, L), kSliceThreads, 0, L.stream>>>(j); break;
+    case 8: k_slice_emit<float><<<slice_grid(j.nrows, (kSliceThreads / 32) * 32, L), kSliceThreads, 0, L.stream>>>(j); break;
+    case 9: k_slice_emit<double><<<slice_grid(j.nrows, (kSliceThreads / 32) * 32, L), kSliceThreads, 0, L.stream>>>(j); break;
     default: prof_end(L); return cudaErrorInvalidValue;
     }
     prof_end(L);
@@ -338,39 +336,35 @@ namespace {
 
 using kvsmc_host::fail;
 
-// Plan, count and (when outputs are given) emit one slice on a resident
-// volume; *ntri = the triangle count.  Outputs: device arrays of at least
-// cap triangles (the emit never writes past them).
-kvsmc_status slice_run(kvsmc_context* ctx, kvsmc_volume* v, const kvsmc_slice_params* p, float* d_coords,
-                       uint8_t* d_colors, float* d_normals, uint64_t cap, bool emit, uint64_t* ntri)
+// Count one slice on a resident volume (plan, count, scan; *ntri = total)
+// into the context's scratch; slice_emit then writes it.  The job stays
+// valid until the scratch is next used.
+kvsmc_status slice_count_pass(kvsmc_context* ctx, kvsmc_volume* v, const kvsmc_slice_params* p, kvsmc::SliceJob& j,
+                              uint64_t* ntri)
 {
     using namespace kvsmc_host;
     *ntri = 0;
-    if (!p || (p->tf_resolution > 0 && !p->tf_table) || p->tf_resolution < 1)
+    std::memset(&j, 0, sizeof j);
+    if (!p || !p->tf_table || p->tf_resolution < 1)
         return fail(ctx, KVSMC_ERR_INVALID_ARGUMENT, "slice: bad parameters (colour table)");
     const kvsmc::VolumeView& vv = v->view;
     if (vv.nx < 2 || vv.ny < 2 || vv.nz < 2) return KVSMC_OK;   // no cells
-    kvsmc::SliceJob j;
-    std::memset(&j, 0, sizeof j);
     j.vol = vv;
     for (int k = 0; k < 4; ++k) j.coef[k] = p->coefficients[k];
     for (int k = 0; k < 3; ++k) { j.min_coord[k] = p->min_coord[k]; j.scale[k] = p->scale[k]; }
     j.tf_min = p->tf_min;
     j.tf_max = p->tf_max;
     j.tf_res = p->tf_resolution;
-    const uint32_t cx = vv.nx - 1, cy = vv.ny - 1, cz = vv.nz - 1;
-    j.rows = std::max<uint32_t>(1, std::min<uint32_t>(cy, (2048 + cx - 1) / cx));
-    j.ytiles = (cy + j.rows - 1) / j.rows;
-    j.tiles = (uint64_t)cz * j.ytiles;
-    const size_t bt = align_up((size_t)3 * j.tf_res, 256), bc = align_up(j.tiles * 4, 256),
-                 bo = align_up(j.tiles * 8, 256), bs = align_up(kvsmc::scan_scratch_bytes(j.tiles), 256);
+    j.nrows = (uint64_t)(vv.ny - 1) * (vv.nz - 1);
+    const size_t bt = align_up((size_t)3 * j.tf_res, 256), bc = align_up(j.nrows * 4, 256),
+                 bo = align_up(j.nrows * 8, 256), bs = align_up(kvsmc::scan_scratch_bytes(j.nrows), 256);
     kvsmc_status st = ensure_scratch(ctx, bt + bc + bo + bs + 256);
     if (st) return st;
     char* base = static_cast<char*>(ctx->scratch);
     uint8_t* d_table = reinterpret_cast<uint8_t*>(base);
     j.table = d_table;
-    j.tile_counts = reinterpret_cast<uint32_t*>(base + bt);
-    j.tile_offsets = reinterpret_cast<uint64_t*>(base + bt + bc);
+    j.row_counts = reinterpret_cast<uint32_t*>(base + bt);
+    j.row_offsets = reinterpret_cast<uint64_t*>(base + bt + bc);
     void* d_scan = base + bt + bc + bo;
     uint64_t* d_total = reinterpret_cast<uint64_t*>(base + bt + bc + bo + bs);
     if ((st = ensure_stage(ctx, (size_t)3 * j.tf_res))) return st;
@@ -378,16 +372,23 @@ kvsmc_status slice_run(kvsmc_context* ctx, kvsmc_volume* v, const kvsmc_slice_pa
     KVSMC_CUDA(ctx, cudaMemcpyAsync(d_table, ctx->h_stage, (size_t)3 * j.tf_res, cudaMemcpyHostToDevice, ctx->stream));
     const kvsmc::Launch L = launch_of(ctx);
     KVSMC_CUDA(ctx, kvsmc::launch_slice_count(j, L));
-    KVSMC_CUDA(ctx, kvsmc::launch_scan(j.tile_counts, j.tile_offsets, j.tiles, d_scan, d_total, L));
+    KVSMC_CUDA(ctx, kvsmc::launch_scan(j.row_counts, j.row_offsets, j.nrows, d_scan, d_total, L));
     KVSMC_CUDA(ctx, cudaMemcpyAsync(ctx->h_small, d_total, sizeof(uint64_t), cudaMemcpyDeviceToHost, ctx->stream));
     KVSMC_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
     *ntri = ctx->h_small[0];
-    if (!emit || *ntri == 0) return KVSMC_OK;
+    return KVSMC_OK;
+}
+
+kvsmc_status slice_emit(kvsmc_context* ctx, kvsmc::SliceJob& j, float* d_coords, uint8_t* d_colors, float* d_normals,
+                        uint64_t cap)
+{
+    using namespace kvsmc_host;
+    if (j.nrows == 0) return KVSMC_OK;
     j.coords = d_coords;
     j.colors = d_colors;
     j.normals = d_normals;
     j.cap_tris = cap;
-    KVSMC_CUDA(ctx, kvsmc::launch_slice_emit(j, L));
+    KVSMC_CUDA(ctx, kvsmc::launch_slice_emit(j, launch_of(ctx)));
     return KVSMC_OK;
 }
 
@@ -400,7 +401,8 @@ kvsmc_status kvsmc_slice_count(kvsmc_context* ctx, kvsmc_volume* vol, const kvsm
 {
     if (!ctx || !vol || !ntriangles) return KVSMC_ERR_INVALID_ARGUMENT;
     KVSMC_CUDA(ctx, cudaSetDevice(ctx->device));
-    return slice_run(ctx, vol, p, nullptr, nullptr, nullptr, 0, false, ntriangles);
+    kvsmc::SliceJob j;
+    return slice_count_pass(ctx, vol, p, j, ntriangles);
 }
 
 kvsmc_status kvsmc_slice_extract_device(kvsmc_context* ctx, kvsmc_volume* vol, const kvsmc_slice_params* p,
@@ -411,13 +413,14 @@ kvsmc_status kvsmc_slice_extract_device(kvsmc_context* ctx, kvsmc_volume* vol, c
     if (!ctx || !vol || !ntriangles) return KVSMC_ERR_INVALID_ARGUMENT;
     KVSMC_CUDA(ctx, cudaSetDevice(ctx->device));
     uint64_t n = 0;
-    kvsmc_status st = slice_run(ctx, vol, p, nullptr, nullptr, nullptr, 0, false, &n);
+    kvsmc::SliceJob j;
+    kvsmc_status st = slice_count_pass(ctx, vol, p, j, &n);
     *ntriangles = n;
     if (st || n == 0) return st;
     const uint64_t cap = std::min(std::min(coords_capacity / 9, colors_capacity / 9), normals_capacity / 3);
     if (!d_coords || !d_colors || !d_normals || cap < n)
         return fail(ctx, KVSMC_ERR_CAPACITY, "slice: %llu triangles do not fit the outputs", (unsigned long long)n);
-    st = slice_run(ctx, vol, p, d_coords, d_colors, d_normals, cap, true, &n);
+    st = slice_emit(ctx, j, d_coords, d_colors, d_normals, cap);
     if (!st) KVSMC_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
     return st;
 }
@@ -429,7 +432,8 @@ kvsmc_status kvsmc_slice_plane(kvsmc_context* ctx, kvsmc_volume* vol, const kvsm
     if (!ctx || !vol || !alloc || !ntriangles) return KVSMC_ERR_INVALID_ARGUMENT;
     KVSMC_CUDA(ctx, cudaSetDevice(ctx->device));
     uint64_t n = 0;
-    kvsmc_status st = slice_run(ctx, vol, p, nullptr, nullptr, nullptr, 0, false, &n);
+    kvsmc::SliceJob j;
+    kvsmc_status st = slice_count_pass(ctx, vol, p, j, &n);
     *ntriangles = n;
     if (st || n == 0) return st;
     const size_t bc = align_up(n * 36, 256), bn = align_up(n * 12, 256), bk = align_up(n * 9, 256);
@@ -446,7 +450,7 @@ kvsmc_status kvsmc_slice_plane(kvsmc_context* ctx, kvsmc_volume* vol, const kvsm
     float* dc = reinterpret_cast<float*>(base);
     float* dn = reinterpret_cast<float*>(base + bc);
     uint8_t* dk = reinterpret_cast<uint8_t*>(base + bc + bn);
-    if ((st = slice_run(ctx, vol, p, dc, dk, dn, n, true, &n))) return st;
+    if ((st = slice_emit(ctx, j, dc, dk, dn, n))) return st;
     void* hc = alloc(user, 0, 9 * n);
     void* hn = hc ? alloc(user, 1, 3 * n) : nullptr;
     void* hk = hn ? alloc(user, 3, 9 * n) : nullptr;
