@@ -7,6 +7,7 @@
 #include <kvs/TransferFunction>
 #include "kvs/cuda/MarchingCubes.h"
 #include "kvs/cuda/Isosurface.h"
+#include "kvs/cuda/SlicePlane.h"
 
 int main()
 {
@@ -37,6 +38,13 @@ int main()
     kvs::ObjectBase* u = t.exec( volume );
     std::printf( "isosurface exec returned=%d vertices=%zu\n", u ? 1 : 0, t.numberOfVertices() );
     std::printf( "isosurface null returned=%d\n", t.exec( nullptr ) ? 1 : 0 );
+    // kvs::SlicePlane's forms (SlicePlane.h:39-48) on the drop-in
+    kvs::cuda::SlicePlane* sp = new kvs::cuda::SlicePlane( volume, kvs::Vec4( 0, 0, 1, -15.5f ), tf );
+    std::printf( "slice vertices=%zu module=%s\n", sp->numberOfVertices(), sp->moduleName() );
+    kvs::cuda::SlicePlane sq;
+    sq.setPlane( kvs::Vec3( 15.0f, 15.0f, 15.0f ), kvs::Vec3( 0.3f, -0.5f, 0.8f ) );
+    std::printf( "slice exec returned=%d\n", sq.exec( volume ) ? 1 : 0 );
+    delete sp;
     delete s;
     delete a;
     return 0;

@@ -41,4 +41,6 @@ def test_adapter_builds_and_fails_loudly_without_gpu(tmp_path):
     assert "isosurface exec returned=0 vertices=0" in r.stdout
     assert "isosurface null returned=0" in r.stdout
     assert "Cannot create isosurfaces." in r.stdout + r.stderr
+    assert "slice vertices=0 module=kvs::cuda::SlicePlane" in r.stdout
+    assert "slice exec returned=0" in r.stdout
     assert "no CUDA device" in r.stdout + r.stderr
