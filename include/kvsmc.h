@@ -61,6 +61,12 @@ typedef enum kvsmc_mode {
     KVSMC_SHARED_VERTEX_NORMAL = 2   /* VertexNormal (either duplication) */
 } kvsmc_mode;
 
+/* Unstructured cell types of the marching mappers (the reference's
+ * UnstructuredVolumeObject::CellType Tetrahedra, Hexahedra, Pyramid, Prism). */
+typedef enum kvsmc_cell_type {
+    KVSMC_TETRAHEDRA = 0, KVSMC_HEXAHEDRA = 1, KVSMC_PYRAMID = 2, KVSMC_PRISM = 3
+} kvsmc_cell_type;
+
 typedef struct kvsmc_context kvsmc_context;
 typedef struct kvsmc_volume kvsmc_volume;
 
@@ -313,6 +319,26 @@ kvsmc_status kvsmc_extract_noalloc(const void* d_values, kvsmc_dtype dtype, uint
                                    uint32_t nz, const kvsmc_params* p, float* d_coords,
                                    uint64_t coords_capacity, float* d_normals, uint64_t normals_capacity,
                                    void* cuda_stream, kvsmc_sizes* sizes);
+
+/* ------------------------------------------------------ unstructured volumes */
+
+/* kvs::MarchingTetrahedra / MarchingHexahedra / MarchingPyramid /
+ * MarchingPrism (Source/Core/Visualization/Mapper/) on an unstructured volume
+ * in host memory: nnodes values and float coords[3 nnodes], ncells cells of
+ * 4 / 8 / 5 / 6 connections each.  Duplicated vertices, one normal per
+ * triangle (the reference builds nothing in shared-vertex mode), cells in
+ * order, table order inside a cell, same bits.  The isolevel and the clamp
+ * range (has_minmax: min/max given, else the device scan of the values,
+ * StructuredVolumeObject's rules) decide as in the reference; the
+ * Math::Equal(min, max) early exit gives sizes->extracted = 0.  Outputs come
+ * from `alloc` (which: 0 coords, 1 normals).  A connection index >= nnodes is
+ * KVSMC_ERR_INVALID_ARGUMENT (checked on the device, nothing read out of
+ * range). */
+kvsmc_status kvsmc_marching_cells_host(kvsmc_context* ctx, kvsmc_cell_type cell_type, const void* values,
+                                       kvsmc_dtype dtype, uint64_t nnodes, const float* coords,
+                                       const uint32_t* connections, uint64_t ncells, double isolevel,
+                                       int32_t has_minmax, double min_value, double max_value,
+                                       kvsmc_host_alloc_fn alloc, void* user, kvsmc_sizes* sizes);
 
 /* -------------------------------------------------------------- slice plane */
 

@@ -6,6 +6,9 @@ in include/kvsmc.h).  This package holds the Python host layer over that ABI.
 from . import _abi  # noqa: F401
 from .marching_cubes import (MarchingCubes, PolygonObject, StructuredVolumeObject,  # noqa: F401
                              TransferFunction, default_context)
+from .marching_cells import (MarchingHexahedra, MarchingPrism, MarchingPyramid,  # noqa: F401
+                             MarchingTetrahedra, UnstructuredVolumeObject)
 
 __all__ = ["MarchingCubes", "PolygonObject", "StructuredVolumeObject", "TransferFunction",
-           "default_context"]
+           "default_context", "UnstructuredVolumeObject", "MarchingTetrahedra", "MarchingHexahedra",
+           "MarchingPyramid", "MarchingPrism"]

@@ -49,6 +49,7 @@ EXPORTS = [
     "kvsmc_write_stl_host", "kvsmc_volume_download", "kvsmc_kvsml_read_info", "kvsmc_volume_load_kvsml",
     "kvsmc_avs_read_info", "kvsmc_volume_load_avs",
     "kvsmc_slice_count", "kvsmc_slice_extract_device", "kvsmc_slice_plane",
+    "kvsmc_marching_cells_host",
 ]
 
 PATH_AUTO = 0      # streaming kernels where eligible
@@ -194,6 +195,8 @@ def load(path=LIB_PATH):
         "kvsmc_slice_extract_device": (C.c_int, [vp, vp, C.POINTER(SliceParams), vp, u64, vp, u64, vp, u64,
                                                  C.POINTER(u64)]),
         "kvsmc_slice_plane": (C.c_int, [vp, vp, C.POINTER(SliceParams), HOST_ALLOC, vp, C.POINTER(u64)]),
+        "kvsmc_marching_cells_host": (C.c_int, [vp, C.c_int, vp, C.c_int, u64, vp, vp, u64, C.c_double, i32,
+                                                C.c_double, C.c_double, HOST_ALLOC, vp, C.POINTER(Sizes)]),
         "kvsmc_kvsml_read_info": (C.c_int, [C.c_char_p, C.POINTER(KvsmlInfo)]),
         "kvsmc_volume_load_kvsml": (C.c_int, [vp, C.c_char_p, C.POINTER(vp), C.POINTER(KvsmlInfo)]),
         "kvsmc_avs_read_info": (C.c_int, [C.c_char_p, C.POINTER(KvsmlInfo)]),
@@ -459,6 +462,35 @@ def marching_cubes_host(ctx, values, params):
               "kvsmc_marching_cubes_host")
     empty_f = np.zeros(0, np.float32)
     return (bufs.get(0, empty_f), bufs.get(1, empty_f), bufs.get(2, np.zeros(0, np.uint32)), sizes_dict(s))
+
+
+CELL_NODES = (4, 8, 5, 6)   # kvsmc_cell_type: tetrahedra, hexahedra, pyramid, prism
+
+
+def marching_cells_host(ctx, cell_type, values, coords, connections, isolevel, minmax=None):
+    """kvsmc_marching_cells_host: (coords, normals, sizes) of one unstructured volume."""
+    v = np.ascontiguousarray(values).reshape(-1)
+    c = np.ascontiguousarray(coords, np.float32).reshape(-1)
+    k = np.ascontiguousarray(connections, np.uint32).reshape(-1)
+    npc = CELL_NODES[int(cell_type)]
+    if c.size != 3 * v.size or k.size % npc:
+        raise ValueError("coords / connections do not match the node count / cell type")
+    bufs = {}
+
+    def alloc(user, which, count):
+        a = np.empty(count, dtype=np.float32)
+        bufs[which] = a
+        return a.ctypes.data
+
+    cb = HOST_ALLOC(alloc)
+    s = Sizes()
+    ctx.check(ctx.lib.kvsmc_marching_cells_host(
+        ctx.handle, int(cell_type), v.ctypes.data, dtype_code(v.dtype), v.size, c.ctypes.data,
+        k.ctypes.data if k.size else None, k.size // npc, float(isolevel), 1 if minmax is not None else 0,
+        float(minmax[0]) if minmax is not None else 0.0, float(minmax[1]) if minmax is not None else 0.0,
+        cb, None, C.byref(s)), "kvsmc_marching_cells_host")
+    empty_f = np.zeros(0, np.float32)
+    return bufs.get(0, empty_f), bufs.get(1, empty_f), sizes_dict(s)
 
 
 def extract_batch_host(ctx, values, params_list, buffer_for=None):

@@ -1,0 +1,535 @@
+// cells.cu -- marching tetrahedra / hexahedra / pyramids / prisms on
+// unstructured volumes, on the GPU.
+//
+// The reference mappers (Source/Core/Visualization/Mapper/MarchingTetrahedra.cpp,
+// MarchingHexahedra.cpp, MarchingPyramid.cpp, MarchingPrism.cpp) share one
+// structure, restated here once: cells in order; a cell's case has bit k set
+// iff double(value of local node k) > isolevel (calculate_table_index), the
+// local nodes being the cell's connections (hexahedra take connections 4-7
+// then 0-3, MarchingHexahedra.cpp:105-112); pyramid cases 10, 11, 20, 21 are
+// resolved by the sign of (iso - A) D + B C over the base's four values
+// (calculate_special_table_index, MarchingPyramid.cpp:293-315); triangles
+// come from the cell type's table in the mapper's vertex order (cell_tables.h);
+// a vertex on the edge (n0, n1) is, in double, c0 + r (c1 - c0) per axis with
+// r = |(iso - v0) / (v1 - v0)|, v clamped to the volume's [min, max], c1 - c0
+// a float difference, then rounded to float (interpolate_vertex); one normal
+// per triangle (v1 - v0) x (v2 - v0).  Duplicated vertices only (the
+// reference's shared-vertex branch is not built, :164-206).
+//
+// Two passes over tiles of 256 cells: count, an exclusive scan of the tile
+// counts, emit (a block-wide scan of each cell's triangle count).  A
+// connection index outside the nodes sets a flag and reads node 0 instead.
+#include <cuda_runtime.h>
+
+#include <cstring>
+
+#include "cell_tables.h"
+#include "context.h"
+#include "mc_device.cuh"
+
+namespace kvsmc {
+
+namespace {
+
+__constant__ uint8_t c_tet_ntri[CELL_TETRA_CASES] = CELL_TETRA_NTRI_INIT;
+__constant__ uint64_t c_tet_tri[CELL_TETRA_CASES] = CELL_TETRA_TRI_INIT;
+__constant__ uint8_t c_tet_edge[CELL_TETRA_EDGES] = CELL_TETRA_EDGE_INIT;
+__constant__ uint8_t c_hex_ntri[CELL_HEXA_CASES] = CELL_HEXA_NTRI_INIT;
+__constant__ uint64_t c_hex_tri[CELL_HEXA_CASES] = CELL_HEXA_TRI_INIT;
+__constant__ uint8_t c_hex_edge[CELL_HEXA_EDGES] = CELL_HEXA_EDGE_INIT;
+__constant__ uint8_t c_pyr_ntri[CELL_PYRAMID_CASES] = CELL_PYRAMID_NTRI_INIT;
+__constant__ uint64_t c_pyr_tri[CELL_PYRAMID_CASES] = CELL_PYRAMID_TRI_INIT;
+__constant__ uint8_t c_pyr_edge[CELL_PYRAMID_EDGES] = CELL_PYRAMID_EDGE_INIT;
+__constant__ uint8_t c_pri_ntri[CELL_PRISM_CASES] = CELL_PRISM_NTRI_INIT;
+__constant__ uint64_t c_pri_tri[CELL_PRISM_CASES] = CELL_PRISM_TRI_INIT;
+__constant__ uint8_t c_pri_edge[CELL_PRISM_EDGES] = CELL_PRISM_EDGE_INIT;
+
+constexpr int kCellThreads = 256;
+
+template <int CT> struct CellTraits;
+template <> struct CellTraits<KVSMC_TETRAHEDRA> {
+    static constexpr int kNodes = 4;
+    __device__ static int node(int k) { return k; }
+    __device__ static uint32_t ntri(unsigned c) { return c_tet_ntri[c]; }
+    __device__ static uint64_t tri(unsigned c) { return c_tet_tri[c]; }
+    __device__ static unsigned edge(int e) { return c_tet_edge[e]; }
+};
+template <> struct CellTraits<KVSMC_HEXAHEDRA> {
+    static constexpr int kNodes = 8;
+    __device__ static int node(int k) { return k < 4 ? k + 4 : k - 4; }   // MarchingHexahedra.cpp:105-112
+    __device__ static uint32_t ntri(unsigned c) { return c_hex_ntri[c]; }
+    __device__ static uint64_t tri(unsigned c) { return c_hex_tri[c]; }
+    __device__ static unsigned edge(int e) { return c_hex_edge[e]; }
+};
+template <> struct CellTraits<KVSMC_PYRAMID> {
+    static constexpr int kNodes = 5;
+    __device__ static int node(int k) { return k; }
+    __device__ static uint32_t ntri(unsigned c) { return c < CELL_PYRAMID_CASES ? c_pyr_ntri[c] : 0u; }
+    __device__ static uint64_t tri(unsigned c) { return c < CELL_PYRAMID_CASES ? c_pyr_tri[c] : 0ull; }
+    __device__ static unsigned edge(int e) { return c_pyr_edge[e]; }
+};
+template <> struct CellTraits<KVSMC_PRISM> {
+    static constexpr int kNodes = 6;
+    __device__ static int node(int k) { return k; }
+    __device__ static uint32_t ntri(unsigned c) { return c_pri_ntri[c]; }
+    __device__ static uint64_t tri(unsigned c) { return c_pri_tri[c]; }
+    __device__ static unsigned edge(int e) { return c_pri_edge[e]; }
+};
+
+template <typename T> __device__ __forceinline__ double dval(const void* v, uint64_t i)
+{
+    return to_double(static_cast<const T*>(v)[i]);
+}
+
+// The cell's local node indices (checked against the node count) and case.
+template <int CT, typename T>
+__device__ __forceinline__ unsigned cell_case(const CellJob& j, uint64_t cell, uint64_t* nodes)
+{
+    using Tr = CellTraits<CT>;
+    const uint32_t* conn = j.conn + (uint64_t)Tr::kNodes * cell;
+#pragma unroll
+    for (int k = 0; k < Tr::kNodes; ++k) {
+        uint64_t n = conn[Tr::node(k)];
+        if (n >= j.nnodes) {
+            atomicExch(j.bad_index, 1);
+            n = 0;
+        }
+        nodes[k] = n;
+    }
+    unsigned c = 0;
+#pragma unroll
+    for (int k = 0; k < Tr::kNodes; ++k) c |= (dval<T>(j.values, nodes[k]) > j.iso) ? (1u << k) : 0u;
+    if (CT == KVSMC_PYRAMID && (c == 10u || c == 11u || c == 20u || c == 21u)) {
+        const double v1 = dval<T>(j.values, nodes[1]), v2 = dval<T>(j.values, nodes[2]);
+        const double v3 = dval<T>(j.values, nodes[3]), v4 = dval<T>(j.values, nodes[4]);
+        const double A = __ddiv_rn(__dadd_rn(__dadd_rn(__dadd_rn(v1, v2), v3), v4), 4.0);
+        const double B = __ddiv_rn(__dsub_rn(__dadd_rn(__dadd_rn(-v1, v2), v3), v4), 4.0);
+        const double C = __ddiv_rn(__dadd_rn(__dadd_rn(__dsub_rn(-v1, v2), v3), v4), 4.0);
+        const double D = __ddiv_rn(__dsub_rn(__dadd_rn(__dsub_rn(v1, v2), v3), v4), 4.0);
+        const double E = __dadd_rn(__dmul_rn(__dsub_rn(j.iso, A), D), __dmul_rn(B, C));
+        if (c == 10u && E < 0) c = 32u;
+        else if (c == 11u && E >= 0) c = 33u;
+        else if (c == 20u && E >= 0) c = 34u;
+        else if (c == 21u && E < 0) c = 35u;
+    }
+    return c;
+}
+
+template <typename T>
+__device__ __forceinline__ float3 cell_vertex(const CellJob& j, uint64_t n0, uint64_t n1)
+{
+    const double lo = j.vmin, hi = j.vmax;
+    double v0 = dval<T>(j.values, n0), v1 = dval<T>(j.values, n1);
+    v0 = v0 <= lo ? lo : (v0 <= hi ? v0 : hi);   // Math::Clamp
+    v1 = v1 <= lo ? lo : (v1 <= hi ? v1 : hi);
+    const double q = __ddiv_rn(__dsub_rn(j.iso, v0), __dsub_rn(v1, v0));
+    const double r = q < 0.0 ? -q : q;
+    const float* c0 = j.coords + 3 * n0;
+    const float* c1 = j.coords + 3 * n1;
+    float3 o;
+    o.x = __double2float_rn(__dadd_rn((double)c0[0], __dmul_rn(r, (double)__fsub_rn(c1[0], c0[0]))));
+    o.y = __double2float_rn(__dadd_rn((double)c0[1], __dmul_rn(r, (double)__fsub_rn(c1[1], c0[1]))));
+    o.z = __double2float_rn(__dadd_rn((double)c0[2], __dmul_rn(r, (double)__fsub_rn(c1[2], c0[2]))));
+    return o;
+}
+
+__device__ __forceinline__ uint32_t cell_block_sum(uint32_t v, uint32_t* ws)
+{
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+    const unsigned lane = threadIdx.x & 31u, warp = threadIdx.x >> 5;
+    __syncthreads();
+    if (lane == 0) ws[warp] = v;
+    __syncthreads();
+    uint32_t t = 0;
+    for (unsigned w = 0; w < blockDim.x / 32; ++w) t += ws[w];
+    return t;
+}
+
+__device__ __forceinline__ uint32_t cell_block_excl(uint32_t v, uint32_t* ws)
+{
+    const unsigned lane = threadIdx.x & 31u, warp = threadIdx.x >> 5;
+    uint32_t inc = v;
+    for (int o = 1; o < 32; o <<= 1) {
+        const uint32_t t = __shfl_up_sync(0xffffffffu, inc, o);
+        if (lane >= (unsigned)o) inc += t;
+    }
+    __syncthreads();
+    if (lane == 31) ws[warp] = inc;
+    __syncthreads();
+    uint32_t before = 0;
+    for (unsigned w = 0; w < warp; ++w) before += ws[w];
+    return before + inc - v;
+}
+
+template <int CT, typename T>
+__global__ void __launch_bounds__(kCellThreads) k_cells_count(CellJob j)
+{
+    __shared__ uint32_t ws[32];
+    using Tr = CellTraits<CT>;
+    for (uint64_t tile = blockIdx.x; tile * kCellThreads < j.ncells; tile += gridDim.x) {
+        const uint64_t cell = tile * kCellThreads + threadIdx.x;
+        uint32_t n = 0;
+        if (cell < j.ncells) {
+            uint64_t nodes[Tr::kNodes];
+            n = Tr::ntri(cell_case<CT, T>(j, cell, nodes));
+        }
+        const uint32_t t = cell_block_sum(n, ws);
+        if (threadIdx.x == 0) j.tile_counts[tile] = t;
+    }
+}
+
+template <int CT, typename T>
+__global__ void __launch_bounds__(kCellThreads) k_cells_emit(CellJob j)
+{
+    __shared__ uint32_t ws[32];
+    using Tr = CellTraits<CT>;
+    for (uint64_t tile = blockIdx.x; tile * kCellThreads < j.ncells; tile += gridDim.x) {
+        const uint64_t cell = tile * kCellThreads + threadIdx.x;
+        uint64_t nodes[Tr::kNodes];
+        unsigned c = 0;
+        uint32_t n = 0;
+        if (cell < j.ncells) {
+            c = cell_case<CT, T>(j, cell, nodes);
+            n = Tr::ntri(c);
+        }
+        uint64_t t = j.tile_offsets[tile] + cell_block_excl(n, ws);
+        uint64_t pk = Tr::tri(c);
+        for (uint32_t k = 0; k < n; ++k, ++t, pk >>= 12) {
+            if (t >= j.cap_tris) break;   // never past the outputs
+            float3 v[3];
+#pragma unroll
+            for (int s = 0; s < 3; ++s) {
+                const unsigned ed = Tr::edge((int)((pk >> (4 * s)) & 15u));
+                v[s] = cell_vertex<T>(j, nodes[ed & 15u], nodes[ed >> 4]);
+            }
+            float* o = j.out_coords + 9 * t;
+            o[0] = v[0].x; o[1] = v[0].y; o[2] = v[0].z;
+            o[3] = v[1].x; o[4] = v[1].y; o[5] = v[1].z;
+            o[6] = v[2].x; o[7] = v[2].y; o[8] = v[2].z;
+            const float3 nn = tri_normal(v[0], v[1], v[2]);
+            float* q = j.out_normals + 3 * t;
+            q[0] = nn.x; q[1] = nn.y; q[2] = nn.z;
+        }
+    }
+}
+
+
+// ---- min/max over the cells' nodes (GetMinMaxValues with connections,
+// UnstructuredVolumeObject.cpp:123-143): the scan starts at values[0] and
+// then visits values[conn[p]] for every connection p in order; Min/Max keep
+// the earlier value on ties and never take a NaN (a NaN values[0] stays).
+template <typename T> struct CellMinMax {
+    T lo, hi;
+    unsigned long long ilo, ihi;   // scan positions (values[0] is position 0)
+    int any;
+};
+
+template <typename T> __device__ __forceinline__ void cmm_combine(CellMinMax<T>& a, const CellMinMax<T>& b)
+{
+    if (!b.any) return;
+    if (!a.any) { a = b; return; }
+    if (b.lo < a.lo || (b.lo == a.lo && b.ilo < a.ilo)) { a.lo = b.lo; a.ilo = b.ilo; }
+    if (b.hi > a.hi || (b.hi == a.hi && b.ihi < a.ihi)) { a.hi = b.hi; a.ihi = b.ihi; }
+}
+
+template <typename T> __device__ void cmm_block(CellMinMax<T>& m, CellMinMax<T>* sm)
+{
+    sm[threadIdx.x] = m;
+    __syncthreads();
+    for (unsigned s = blockDim.x / 2; s > 0; s >>= 1) {
+        if (threadIdx.x < s) {
+            CellMinMax<T> a = sm[threadIdx.x];
+            cmm_combine(a, sm[threadIdx.x + s]);
+            sm[threadIdx.x] = a;
+        }
+        __syncthreads();
+    }
+    m = sm[0];
+}
+
+template <typename T>
+__global__ void __launch_bounds__(kCellThreads) k_cells_minmax_partial(CellJob j, uint64_t nconn, CellMinMax<T>* partial)
+{
+    __shared__ CellMinMax<T> sm[kCellThreads];
+    const T* vals = static_cast<const T*>(j.values);
+    CellMinMax<T> m;
+    m.any = 0; m.lo = T(0); m.hi = T(0); m.ilo = m.ihi = 0;
+    const uint64_t per = (nconn + gridDim.x - 1) / gridDim.x;
+    const uint64_t p0 = (uint64_t)blockIdx.x * per, p1 = p0 + per < nconn ? p0 + per : nconn;
+    for (uint64_t p = p0 + threadIdx.x; p < p1; p += blockDim.x) {
+        const uint32_t n = j.conn[p];
+        if (n >= j.nnodes) { atomicExch(j.bad_index, 1); continue; }
+        const T v = vals[n];
+        if (v != v) continue;
+        const unsigned long long pos = p + 1;
+        if (!m.any) { m.lo = m.hi = v; m.ilo = m.ihi = pos; m.any = 1; continue; }
+        if (v < m.lo) { m.lo = v; m.ilo = pos; }
+        if (v > m.hi) { m.hi = v; m.ihi = pos; }
+    }
+    cmm_block(m, sm);
+    if (threadIdx.x == 0) partial[blockIdx.x] = m;
+}
+
+template <typename T>
+__global__ void __launch_bounds__(kCellThreads) k_cells_minmax_final(CellJob j, const CellMinMax<T>* partial, int n, double* out)
+{
+    __shared__ CellMinMax<T> sm[kCellThreads];
+    CellMinMax<T> m;
+    m.any = 0; m.lo = T(0); m.hi = T(0); m.ilo = m.ihi = 0;
+    for (int i = threadIdx.x; i < n; i += blockDim.x) cmm_combine(m, partial[i]);
+    cmm_block(m, sm);
+    if (threadIdx.x == 0) {
+        const T first = static_cast<const T*>(j.values)[0];
+        if (first != first) {
+            out[0] = out[1] = to_double(first);
+            return;
+        }
+        CellMinMax<T> f;
+        f.lo = f.hi = first; f.ilo = f.ihi = 0; f.any = 1;
+        cmm_combine(f, m);
+        out[0] = to_double(f.lo);
+        out[1] = to_double(f.hi);
+    }
+}
+
+unsigned cell_grid(uint64_t tiles, const Launch& L)
+{
+    const uint64_t cap = (uint64_t)L.num_sms * 8;
+    return (unsigned)(tiles < cap ? (tiles ? tiles : 1) : cap);
+}
+
+#define KVSMC_CELL_SWITCH(CTV, DT, ...)                                                     \
+    switch (CTV) {                                                                          \
+    case KVSMC_TETRAHEDRA: { constexpr int CT = KVSMC_TETRAHEDRA; KVSMC_VALUE_SWITCH(DT, __VA_ARGS__); } break; \
+    case KVSMC_HEXAHEDRA: { constexpr int CT = KVSMC_HEXAHEDRA; KVSMC_VALUE_SWITCH(DT, __VA_ARGS__); } break;   \
+    case KVSMC_PYRAMID: { constexpr int CT = KVSMC_PYRAMID; KVSMC_VALUE_SWITCH(DT, __VA_ARGS__); } break;       \
+    case KVSMC_PRISM: { constexpr int CT = KVSMC_PRISM; KVSMC_VALUE_SWITCH(DT, __VA_ARGS__); } break;           \
+    default: return cudaErrorInvalidValue;                                                  \
+    }
+
+#define KVSMC_VALUE_SWITCH(DT, ...)                                 \
+    switch (DT) {                                                   \
+    case 0: { using T = int8_t; __VA_ARGS__; } break;               \
+    case 1: { using T = int16_t; __VA_ARGS__; } break;              \
+    case 2: { using T = int32_t; __VA_ARGS__; } break;              \
+    case 3: { using T = long long; __VA_ARGS__; } break;            \
+    case 4: { using T = uint8_t; __VA_ARGS__; } break;              \
+    case 5: { using T = uint16_t; __VA_ARGS__; } break;             \
+    case 6: { using T = uint32_t; __VA_ARGS__; } break;             \
+    case 7: { using T = unsigned long long; __VA_ARGS__; } break;   \
+    case 8: { using T = float; __VA_ARGS__; } break;                \
+    case 9: { using T = double; __VA_ARGS__; } break;               \
+    default: return cudaErrorInvalidValue;                          \
+    }
+
+}  // namespace
+
+cudaError_t launch_cells_count(const CellJob& j, const Launch& L)
+{
+    if (j.ncells == 0) return cudaSuccess;
+    const uint64_t tiles = (j.ncells + kCellThreads - 1) / kCellThreads;
+    prof_begin(L, "cells_count");
+    KVSMC_CELL_SWITCH(j.cell_type, j.dtype,
+                      { k_cells_count<CT, T><<<cell_grid(tiles, L), kCellThreads, 0, L.stream>>>(j); });
+    prof_end(L);
+    *L.counter += 1;
+    return cudaGetLastError();
+}
+
+cudaError_t launch_cells_emit(const CellJob& j, const Launch& L)
+{
+    if (j.ncells == 0) return cudaSuccess;
+    const uint64_t tiles = (j.ncells + kCellThreads - 1) / kCellThreads;
+    prof_begin(L, "cells_emit");
+    KVSMC_CELL_SWITCH(j.cell_type, j.dtype,
+                      { k_cells_emit<CT, T><<<cell_grid(tiles, L), kCellThreads, 0, L.stream>>>(j); });
+    prof_end(L);
+    *L.counter += 1;
+    return cudaGetLastError();
+}
+
+
+size_t cells_minmax_scratch_bytes(int num_sms) { return (size_t)num_sms * 4 * 64; }
+
+cudaError_t launch_cells_minmax(const CellJob& j, void* scratch, double* d_out, const Launch& L)
+{
+    const uint64_t nconn = j.ncells * (uint64_t)(j.cell_type == KVSMC_TETRAHEDRA ? 4 : j.cell_type == KVSMC_HEXAHEDRA ? 8
+                                                 : j.cell_type == KVSMC_PYRAMID ? 5 : 6);
+    const int nb = L.num_sms * 4;
+    prof_begin(L, "cells_minmax");
+    KVSMC_VALUE_SWITCH(j.dtype, {
+        static_assert(sizeof(CellMinMax<T>) <= 64, "partial slot");
+        CellMinMax<T>* part = static_cast<CellMinMax<T>*>(scratch);
+        k_cells_minmax_partial<T><<<nb, kCellThreads, 0, L.stream>>>(j, nconn, part);
+        k_cells_minmax_final<T><<<1, kCellThreads, 0, L.stream>>>(j, part, nb, d_out);
+    });
+    prof_end(L);
+    *L.counter += 2;
+    return cudaGetLastError();
+}
+
+uint64_t cells_tiles(uint64_t ncells) { return (ncells + kCellThreads - 1) / kCellThreads; }
+
+}  // namespace kvsmc
+
+namespace {
+
+using kvsmc_host::fail;
+
+int nodes_per_cell(int ct)
+{
+    return ct == KVSMC_TETRAHEDRA ? 4 : ct == KVSMC_HEXAHEDRA ? 8 : ct == KVSMC_PYRAMID ? 5 : ct == KVSMC_PRISM ? 6 : 0;
+}
+
+// kvs::Math::Equal (Utility/Math.h:135-138)
+bool equal_abs(double a, double b)
+{
+    const double d = a - b;
+    return (d < 0 ? -d : d) < 1.e-6;
+}
+
+}  // namespace
+
+extern "C" {
+
+kvsmc_status kvsmc_marching_cells_host(kvsmc_context* ctx, kvsmc_cell_type cell_type, const void* values,
+                                       kvsmc_dtype dtype, uint64_t nnodes, const float* coords,
+                                       const uint32_t* connections, uint64_t ncells, double isolevel,
+                                       int32_t has_minmax, double min_value, double max_value,
+                                       kvsmc_host_alloc_fn alloc, void* user, kvsmc_sizes* sizes)
+{
+    using namespace kvsmc_host;
+    if (!ctx || !alloc || !sizes) return KVSMC_ERR_INVALID_ARGUMENT;
+    std::memset(sizes, 0, sizeof *sizes);
+    const int npc = nodes_per_cell(cell_type);
+    if (npc == 0) return fail(ctx, KVSMC_ERR_INVALID_ARGUMENT, "cells: unknown cell type %d", (int)cell_type);
+    if (kvsmc::dtype_size(dtype) == 0) return fail(ctx, KVSMC_ERR_UNSUPPORTED_DTYPE, "cells: data type %d", (int)dtype);
+    if (nnodes == 0 || !values || !coords || (ncells && !connections))
+        return fail(ctx, KVSMC_ERR_INVALID_ARGUMENT, "cells: empty or null volume arrays");
+    // the mappers hold node ids in int and loop cells with a UInt32 counter
+    if (nnodes > 0x7fffffffull || ncells > 0xffffffffull)
+        return fail(ctx, KVSMC_ERR_TOO_LARGE, "cells: %llu nodes / %llu cells beyond the 32-bit ids",
+                    (unsigned long long)nnodes, (unsigned long long)ncells);
+    KVSMC_CUDA(ctx, cudaSetDevice(ctx->device));
+    const size_t es = kvsmc::dtype_size(dtype);
+    void* d_values = nullptr;
+    float* d_coords = nullptr;
+    uint32_t* d_conn = nullptr;
+    float* d_out = nullptr;
+    int* d_bad = nullptr;
+    auto done = [&](kvsmc_status s) {
+        cudaStreamSynchronize(ctx->stream);
+        cudaFree(d_values);
+        cudaFree(d_coords);
+        cudaFree(d_conn);
+        cudaFree(d_out);
+        cudaFree(d_bad);
+        return s;
+    };
+    auto cuda_fail = [&](cudaError_t e) {
+        return done(fail(ctx, e == cudaErrorMemoryAllocation ? KVSMC_ERR_OUT_OF_MEMORY : KVSMC_ERR_CUDA, "cells: %s",
+                         cudaGetErrorString(e)));
+    };
+    cudaError_t e = cudaMalloc(&d_values, nnodes * es);
+    if (e == cudaSuccess) e = cudaMalloc(&d_coords, nnodes * 3 * sizeof(float));
+    if (e == cudaSuccess) e = cudaMalloc(&d_conn, (ncells ? ncells * npc : 1) * sizeof(uint32_t));
+    if (e == cudaSuccess) e = cudaMalloc(&d_bad, sizeof(int));
+    if (e == cudaSuccess) e = cudaMemcpyAsync(d_values, values, nnodes * es, cudaMemcpyHostToDevice, ctx->stream);
+    if (e == cudaSuccess)
+        e = cudaMemcpyAsync(d_coords, coords, nnodes * 3 * sizeof(float), cudaMemcpyHostToDevice, ctx->stream);
+    if (e == cudaSuccess && ncells)
+        e = cudaMemcpyAsync(d_conn, connections, ncells * npc * sizeof(uint32_t), cudaMemcpyHostToDevice, ctx->stream);
+    if (e == cudaSuccess) e = cudaMemsetAsync(d_bad, 0, sizeof(int), ctx->stream);
+    if (e != cudaSuccess) return cuda_fail(e);
+
+    kvsmc::CellJob j;
+    std::memset(&j, 0, sizeof j);
+    j.cell_type = cell_type;
+    j.dtype = dtype;
+    j.values = d_values;
+    j.nnodes = nnodes;
+    j.coords = d_coords;
+    j.conn = d_conn;
+    j.ncells = ncells;
+    j.iso = isolevel;
+    j.bad_index = d_bad;
+    const uint64_t tiles = kvsmc::cells_tiles(ncells);
+    const size_t bc = align_up(tiles * 4, 256), bo = align_up(tiles * 8, 256),
+                 bs = align_up(std::max(kvsmc::scan_scratch_bytes(tiles), kvsmc::cells_minmax_scratch_bytes(ctx->num_sms)), 256);
+    kvsmc_status st = ensure_scratch(ctx, bc + bo + bs + 256);
+    if (st) return done(st);
+    char* base = static_cast<char*>(ctx->scratch);
+    j.tile_counts = reinterpret_cast<uint32_t*>(base);
+    j.tile_offsets = reinterpret_cast<uint64_t*>(base + bc);
+    void* d_scan = base + bc + bo;
+    uint64_t* d_tail = reinterpret_cast<uint64_t*>(base + bc + bo + bs);   // total, or min/max as doubles
+    const kvsmc::Launch L = launch_of(ctx);
+
+    // MapperBase::setRange: the volume's min/max, computed when not set
+    double vmin = min_value, vmax = max_value;
+    if (!has_minmax) {
+        if (ncells) {
+            e = kvsmc::launch_cells_minmax(j, d_scan, reinterpret_cast<double*>(d_tail), L);
+        } else {
+            // no connections: the scan runs over the nodes (UnstructuredVolumeObject.cpp:88-102)
+            kvsmc::VolumeView v1;
+            std::memset(&v1, 0, sizeof v1);
+            v1.data = d_values;
+            v1.dtype = dtype;
+            v1.nx = (uint32_t)nnodes;
+            v1.ny = v1.nz = 1;
+            v1.pitch = nnodes;
+            v1.slice = nnodes;
+            const size_t need = kvsmc::minmax_scratch_bytes(ctx->num_sms);
+            if (need > bs) return done(fail(ctx, KVSMC_ERR_CUDA, "cells: min/max scratch"));
+            e = kvsmc::launch_minmax(v1, d_scan, reinterpret_cast<double*>(d_tail), L);
+        }
+        if (e == cudaSuccess) e = cudaMemcpyAsync(ctx->h_small, d_tail, 2 * sizeof(double), cudaMemcpyDeviceToHost, ctx->stream);
+        if (e == cudaSuccess) e = cudaMemcpyAsync(ctx->h_small + 2, d_bad, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream);
+        if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
+        if (e != cudaSuccess) return cuda_fail(e);
+        std::memcpy(&vmin, ctx->h_small, sizeof(double));
+        std::memcpy(&vmax, ctx->h_small + 1, sizeof(double));
+        int bad = 0;
+        std::memcpy(&bad, ctx->h_small + 2, sizeof(int));
+        if (bad) return done(fail(ctx, KVSMC_ERR_INVALID_ARGUMENT, "cells: a connection index is >= nnodes"));
+    }
+    sizes->min_value = vmin;
+    sizes->max_value = vmax;
+    if (equal_abs(vmin, vmax)) return done(KVSMC_OK);   // MarchingTetrahedra.cpp:118-119
+    sizes->extracted = 1;
+    if (ncells == 0) return done(KVSMC_OK);
+    j.vmin = vmin;
+    j.vmax = vmax;
+
+    e = kvsmc::launch_cells_count(j, L);
+    if (e == cudaSuccess) e = kvsmc::launch_scan(j.tile_counts, j.tile_offsets, tiles, d_scan, d_tail, L);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(ctx->h_small, d_tail, sizeof(uint64_t), cudaMemcpyDeviceToHost, ctx->stream);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(ctx->h_small + 1, d_bad, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
+    if (e != cudaSuccess) return cuda_fail(e);
+    int bad = 0;
+    std::memcpy(&bad, ctx->h_small + 1, sizeof(int));
+    if (bad) return done(fail(ctx, KVSMC_ERR_INVALID_ARGUMENT, "cells: a connection index is >= nnodes"));
+    const uint64_t t = ctx->h_small[0];
+    sizes->ntriangles = t;
+    sizes->nvertices = 3 * t;
+    sizes->ncoords = 9 * t;
+    sizes->nnormals = 3 * t;
+    if (t == 0) return done(KVSMC_OK);
+    if ((e = cudaMalloc(&d_out, t * 12 * sizeof(float))) != cudaSuccess) return cuda_fail(e);
+    j.out_coords = d_out;
+    j.out_normals = d_out + 9 * t;
+    j.cap_tris = t;
+    if ((e = kvsmc::launch_cells_emit(j, L)) != cudaSuccess) return cuda_fail(e);
+    void* hc = alloc(user, 0, 9 * t);
+    void* hn = hc ? alloc(user, 1, 3 * t) : nullptr;
+    if (!hc || !hn) return done(fail(ctx, KVSMC_ERR_OUT_OF_MEMORY, "cells: host alloc"));
+    e = cudaMemcpyAsync(hc, d_out, t * 9 * sizeof(float), cudaMemcpyDeviceToHost, ctx->stream);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(hn, d_out + 9 * t, t * 3 * sizeof(float), cudaMemcpyDeviceToHost, ctx->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
+    if (e != cudaSuccess) return cuda_fail(e);
+    return done(KVSMC_OK);
+}
+
+}  // extern "C"

@@ -131,6 +131,30 @@ struct SliceJob {
 cudaError_t launch_slice_count(const SliceJob& j, const Launch& L);
 cudaError_t launch_slice_emit(const SliceJob& j, const Launch& L);
 
+// ---- marching cells on unstructured volumes (cells.cu)
+struct CellJob {
+    int32_t cell_type;        // kvsmc_cell_type
+    int32_t dtype;
+    const void* values;
+    uint64_t nnodes;
+    const float* coords;      // 3 nnodes
+    const uint32_t* conn;     // nodes-per-cell x ncells
+    uint64_t ncells;
+    double iso, vmin, vmax;
+    uint32_t* tile_counts;    // per 256-cell tile
+    uint64_t* tile_offsets;
+    float* out_coords;        // 9 T
+    float* out_normals;       // 3 T
+    uint64_t cap_tris;
+    int* bad_index;           // set to 1 by a connection index >= nnodes
+};
+cudaError_t launch_cells_count(const CellJob& j, const Launch& L);
+cudaError_t launch_cells_emit(const CellJob& j, const Launch& L);
+uint64_t cells_tiles(uint64_t ncells);
+// min/max over values[0] and the connected nodes' values, as doubles in d_out[0..1]
+size_t cells_minmax_scratch_bytes(int num_sms);
+cudaError_t launch_cells_minmax(const CellJob& j, void* scratch, double* d_out, const Launch& L);
+
 // ---- binary STL records (export.cu): 50 bytes per triangle; bad_index: a
 // device word set to 1 when a connection index is >= nverts (that vertex
 // then reads as vertex 0)

@@ -20,13 +20,15 @@ As in the reference:
     false.
 Unlike the reference, a failure of the GPU mapper is not swallowed: exec
 reports "Cannot create isosurfaces." with the cause and returns None (the
-reference tests `new` for null and carries on with empty arrays).  Volumes
-other than StructuredVolumeObject (the unstructured branch,
-Isosurface.cpp:193-258) are not handled by this package.
+reference tests `new` for null and carries on with empty arrays).  An
+UnstructuredVolumeObject goes, by its cell type, to this package's
+MarchingTetrahedra / MarchingHexahedra / MarchingPyramid / MarchingPrism
+(Isosurface.cpp:193-258); other cell types give an empty result, as there.
 """
 import numpy as np
 
 from . import _abi
+from .marching_cells import MAPPERS, UnstructuredVolumeObject
 from .marching_cubes import (MarchingCubes, PolygonObject, StructuredVolumeObject, TransferFunction,
                              default_context, message_error)
 
@@ -56,8 +58,21 @@ class Isosurface(PolygonObject):
 
     def _update_min_max(self, volume):
         """StructuredVolumeObject::updateMinMaxValues (StructuredVolumeObject.cpp:431-450)
+        or UnstructuredVolumeObject::updateMinMaxValues (UnstructuredVolumeObject.cpp:469-487)
         by the device scan."""
         ctx = self._ctx or default_context()
+        if isinstance(volume, UnstructuredVolumeObject):
+            # isolevel NaN: no node is above it, so only the min/max scan and an
+            # empty count pass run
+            ct = {c: m.ABI_CELL for c, m in MAPPERS.items()}.get(volume.cellType())
+            if ct is None:
+                raise ValueError("min/max of an unstructured volume needs a marching cell type")
+            n = volume.numberOfNodes()
+            conn = volume.connections()[:volume.numberOfCells() * volume.numberOfCellNodes()]
+            _, _, sizes = _abi.marching_cells_host(ctx, ct, volume.values()[:n], volume.coords()[:3 * n], conn,
+                                                   float("nan"))
+            volume.setMinMaxValues(sizes["min_value"], sizes["max_value"])
+            return
         dv = _abi.DeviceVolume.upload(ctx, volume.volume_array())
         try:
             mn, mx = dv.minmax()
@@ -90,7 +105,7 @@ class Isosurface(PolygonObject):
             self._success = False
             message_error("Input object is NULL.")
             return None
-        if not isinstance(obj, StructuredVolumeObject):
+        if not isinstance(obj, (StructuredVolumeObject, UnstructuredVolumeObject)):
             self._success = False
             message_error("Input object is not volume dat.")
             return None
@@ -99,14 +114,25 @@ class Isosurface(PolygonObject):
         return self
 
     def _mapping(self, volume):
-        """Isosurface::mapping (Isosurface.cpp:132-191), structured branch."""
+        """Isosurface::mapping (Isosurface.cpp:142-258)."""
         if volume.veclen() != 1:
             self._success = False
             message_error("Input object is not scalar field dat.")
             return True
-        mc = MarchingCubes(volume, self._isolevel, self.normalType(), self._duplication, self._tfunc,
-                           context=self._ctx)
-        if mc.isFailure():
+        if isinstance(volume, UnstructuredVolumeObject):
+            mapper = MAPPERS.get(volume.cellType())
+            if mapper is None:
+                return True            # default: break (Isosurface.cpp:256)
+            mc = mapper(None, self._isolevel, self.normalType(), self._duplication, self._tfunc,
+                        context=self._ctx)
+            if mc.exec(volume) is None:
+                self._success = False
+                message_error("Cannot create isosurfaces.")
+                return False
+        else:
+            mc = MarchingCubes(volume, self._isolevel, self.normalType(), self._duplication, self._tfunc,
+                               context=self._ctx)
+        if isinstance(volume, StructuredVolumeObject) and mc.isFailure():
             self._success = False
             message_error("Cannot create isosurfaces.")
             return False

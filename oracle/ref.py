@@ -91,6 +91,11 @@ def lib():
         _lib.kvsref_marching_cubes_stl.restype = C.c_int
         _lib.kvsref_marching_cubes_stl.argtypes = [
             C.c_int, C.c_void_p, C.c_uint, C.c_uint, C.c_uint, C.c_double, C.c_int, C.c_int, C.c_char_p]
+        _lib.kvsref_marching_cells.restype = C.c_int
+        _lib.kvsref_marching_cells.argtypes = [
+            C.c_int, C.c_int, C.c_int, C.c_void_p, C.c_ulonglong, C.c_void_p, C.c_void_p, C.c_ulonglong,
+            C.c_double, C.c_int, C.c_int, C.c_int, C.c_double, C.c_double, C.c_int, C.c_int, C.c_float,
+            C.c_float, C.c_int, C.POINTER(_Result)]
         _lib.kvsref_free.argtypes = [C.POINTER(_Result)]
         _lib.kvsref_hydrogen.argtypes = [C.c_uint, C.c_void_p]
         _lib.kvsref_default_colormap.argtypes = [C.c_int, C.c_void_p]
@@ -184,6 +189,39 @@ def isosurface(values, form, isolevel=0.0, normal_type="polygon", duplication=Tr
     if st != 0:
         raise RuntimeError("kvsref_isosurface failed")
     return _collect(r)
+
+
+CELL_NODES = {0: 4, 1: 8, 2: 5, 3: 6}   # tetrahedra, hexahedra, pyramid, prism
+
+
+def marching_cells(cell_type, values, coords, connections, isolevel, form=0, normal_type="polygon",
+                   duplication=True, minmax=None, tf_resolution=256, tf_range=None, repeat=1):
+    """The reference unstructured marching mapper of `cell_type` (0 tetrahedra,
+    1 hexahedra, 2 pyramid, 3 prism) -- form 0 -- or kvs::Isosurface routing to
+    it -- form 1 -- on an UnstructuredVolumeObject of nnodes values, float32
+    coords (3 per node) and uint32 connections (nodes per cell x ncells)."""
+    v = np.ascontiguousarray(values).reshape(-1)
+    c = np.ascontiguousarray(coords, np.float32).reshape(-1)
+    k = np.ascontiguousarray(connections, np.uint32).reshape(-1)
+    npc = CELL_NODES[int(cell_type)]
+    if c.size != 3 * v.size or k.size % npc:
+        raise ValueError("coords / connections do not match the node count / cell type")
+    r = _Result()
+    st = lib().kvsref_marching_cells(
+        int(form), int(cell_type), dtype_code(v.dtype), v.ctypes.data, v.size, c.ctypes.data, k.ctypes.data,
+        k.size // npc, float(isolevel), 0 if normal_type == "polygon" else 1, 1 if duplication else 0,
+        1 if minmax is not None else 0,
+        float(minmax[0]) if minmax is not None else 0.0,
+        float(minmax[1]) if minmax is not None else 0.0,
+        tf_resolution, 1 if tf_range is not None else 0,
+        float(tf_range[0]) if tf_range is not None else 0.0,
+        float(tf_range[1]) if tf_range is not None else 0.0, int(repeat), C.byref(r))
+    if st != 0:
+        raise RuntimeError("kvsref_marching_cells failed")
+    seconds = r.seconds
+    out = _collect(r)
+    out["seconds"] = seconds
+    return out
 
 
 def slice_plane(values, coefficients=None, point=None, normal=None, minmax=None, tf_resolution=256,

@@ -9,6 +9,11 @@
  * with the C restatement and write golden fixtures.
  */
 #include <kvs/StructuredVolumeObject>
+#include <kvs/UnstructuredVolumeObject>
+#include <kvs/MarchingTetrahedra>
+#include <kvs/MarchingHexahedra>
+#include <kvs/MarchingPyramid>
+#include <kvs/MarchingPrism>
 #include <kvs/PolygonObject>
 #include <kvs/MarchingCubes>
 #include <kvs/Isosurface>
@@ -94,7 +99,7 @@ void Copy3( float* dst, const kvs::Vec3& v ) { dst[0] = v.x(); dst[1] = v.y(); d
 
 // The arrays, types and bounding box of a mapper's PolygonObject, and the
 // volume's min/max cache afterwards.
-void Fill( const kvs::MapperBase* mapper, const kvs::PolygonObject* p, const kvs::StructuredVolumeObject* vol,
+void Fill( const kvs::MapperBase* mapper, const kvs::PolygonObject* p, const kvs::VolumeObjectBase* vol,
            kvsref_result* out )
 {
     out->success = mapper->isSuccess() ? 1 : 0;
@@ -419,6 +424,86 @@ void kvsref_free( kvsref_result* r )
     std::free( r->colors );
     std::free( r->opacities );
     std::memset( r, 0, sizeof( *r ) );
+}
+
+/*
+ * The unstructured marching mappers (MarchingTetrahedra, MarchingHexahedra,
+ * MarchingPyramid, MarchingPrism) on an UnstructuredVolumeObject built from
+ * raw arrays.  cell_type: 0 tetrahedra, 1 hexahedra, 2 pyramid, 3 prism.
+ * form 0: the cell type's mapper (volume, isolevel, normal_type, duplication,
+ * tfunc); form 1: Isosurface( volume, isolevel, normal_type, duplication,
+ * tfunc ), which routes by cell type (Isosurface.cpp:193-258).
+ * repeat: run this many times on fresh volumes, report the fastest.
+ */
+int kvsref_marching_cells(
+    int form, int cell_type, int dtype, const void* values, unsigned long long nnodes, const float* coords,
+    const unsigned int* connections, unsigned long long ncells, double isolevel, int normal_type,
+    int duplication, int has_minmax, double vmin, double vmax, int tf_resolution, int tf_has_range,
+    float tf_min, float tf_max, int repeat, kvsref_result* out )
+{
+    std::memset( out, 0, sizeof( *out ) );
+    static const kvs::UnstructuredVolumeObject::CellType types[4] = {
+        kvs::UnstructuredVolumeObject::Tetrahedra, kvs::UnstructuredVolumeObject::Hexahedra,
+        kvs::UnstructuredVolumeObject::Pyramid, kvs::UnstructuredVolumeObject::Prism };
+    static const size_t npc[4] = { 4, 8, 5, 6 };
+    if ( cell_type < 0 || cell_type > 3 ) return -1;
+    kvs::AnyValueArray vals = Values( dtype, values, nnodes );
+    if ( vals.size() != nnodes ) return -1;
+    kvs::TransferFunction tfunc( tf_resolution > 0 ? tf_resolution : 256 );
+    if ( tf_has_range ) tfunc.setRange( tf_min, tf_max );
+    const auto ntype = normal_type == 0 ? kvs::PolygonObject::PolygonNormal : kvs::PolygonObject::VertexNormal;
+    double best = 1e300;
+    for ( int r = 0; r < ( repeat > 0 ? repeat : 1 ); ++r )
+    {
+        auto* vol = new kvs::UnstructuredVolumeObject();
+        vol->setCellType( types[cell_type] );
+        vol->setVeclen( 1 );
+        vol->setNumberOfNodes( nnodes );
+        vol->setNumberOfCells( ncells );
+        vol->setCoords( kvs::ValueArray<kvs::Real32>( coords, 3 * nnodes ) );
+        vol->setConnections( kvs::ValueArray<kvs::UInt32>( connections, npc[cell_type] * ncells ) );
+        vol->setValues( vals );
+        if ( has_minmax ) vol->setMinMaxValues( vmin, vmax );
+        const auto t0 = std::chrono::steady_clock::now();
+        kvs::PolygonObject* poly = nullptr;
+        kvs::MapperBase* mapper = nullptr;
+        if ( form == 1 )
+        {
+            auto* m = new kvs::Isosurface( vol, isolevel, ntype, duplication != 0, tfunc );
+            poly = m; mapper = m;
+        }
+        else if ( cell_type == 0 )
+        {
+            auto* m = new kvs::MarchingTetrahedra( vol, isolevel, ntype, duplication != 0, tfunc );
+            poly = m; mapper = m;
+        }
+        else if ( cell_type == 1 )
+        {
+            auto* m = new kvs::MarchingHexahedra( vol, isolevel, ntype, duplication != 0, tfunc );
+            poly = m; mapper = m;
+        }
+        else if ( cell_type == 2 )
+        {
+            auto* m = new kvs::MarchingPyramid( vol, isolevel, ntype, duplication != 0, tfunc );
+            poly = m; mapper = m;
+        }
+        else
+        {
+            auto* m = new kvs::MarchingPrism( vol, isolevel, ntype, duplication != 0, tfunc );
+            poly = m; mapper = m;
+        }
+        const double dt = std::chrono::duration<double>( std::chrono::steady_clock::now() - t0 ).count();
+        if ( dt < best ) best = dt;
+        if ( r + 1 == ( repeat > 0 ? repeat : 1 ) )
+        {
+            kvsref_free( out );
+            Fill( mapper, poly, vol, out );
+            out->seconds = best;
+        }
+        delete poly;
+        delete vol;
+    }
+    return 0;
 }
 
 /* HydrogenVolumeData (Source/Core/Visualization/Data/HydrogenVolumeData.cpp):

@@ -6,12 +6,14 @@ by oracle/Makefile.ref) on small seeded inputs and stores inputs + outputs in
 tests/golden/golden.npz (case list tests/golden/cases.json) and
 tests/golden/isosurface.npz (tests/golden/isosurface.json), and binary STL
 files written by the reference PolygonExporter<kvs::Stl> in tests/golden/stl.npz
-(tests/golden/stl.json), and kvs::SlicePlane results in tests/golden/slice.npz
-(tests/golden/slice.json).  The reference
+(tests/golden/stl.json), kvs::SlicePlane results in tests/golden/slice.npz
+(tests/golden/slice.json), and the unstructured marching mappers
+(MarchingTetrahedra / Hexahedra / Pyramid / Prism, directly and through
+kvs::Isosurface) in tests/golden/cells.npz (tests/golden/cells.json).  The reference
 ships no tests or golden vectors of its own, so these fixtures pin the oracle
 restatement and the CUDA path on hosts where the reference is absent.
 
-    python tests/golden/make_golden.py [marching_cubes] [isosurface] [stl] [slice]   (default: all)
+    python tests/golden/make_golden.py [marching_cubes] [isosurface] [stl] [slice] [cells]   (default: all)
 """
 import json
 import os
@@ -24,6 +26,7 @@ ROOT = os.path.dirname(os.path.dirname(HERE))
 sys.path.insert(0, ROOT)
 
 from oracle import ref  # noqa: E402
+from tests import cell_meshes as cm  # noqa: E402
 
 MODES = [("polygon", True), ("polygon", False), ("vertex", True)]
 
@@ -194,10 +197,102 @@ def write_slice():
     print(f"{len(manifest)} slice cases")
 
 
+def cells_cases():
+    """(name, cell_type, values, coords, connections, [run options, ...]); a run
+    is dict(iso, form, normal_type, duplication, minmax, tf_range)."""
+    out = []
+    base = dict(form=0, normal_type="polygon", duplication=True, minmax=None, tf_range=None)
+
+    def run(**kw):
+        r = dict(base)
+        r.update(kw)
+        return r
+
+    for ct, tag in ((0, "tet"), (1, "hex"), (2, "pyr"), (3, "pri")):
+        seed = 100 + ct
+        rng = np.random.default_rng(seed)
+        xyz, conn = cm.grid(ct, 7, 6, 5, seed=seed)
+        v = cm.sphere_values(xyz)
+        out.append((f"{tag}_grid_f32", ct, v, xyz, conn,
+                    [run(iso=1.7), run(iso=2.45), run(iso=1.7, normal_type="vertex"),
+                     run(iso=1.7, duplication=False), run(iso=1.7, form=1), run(iso=2.0, tf_range=(0.5, 3.0)),
+                     run(iso=1.7, minmax=(1.2, 2.2))]))
+        xyz, conn = cm.random_mesh(ct, 120, (300, 120, 200, 160)[ct], seed=seed)
+        n = xyz.shape[0]
+        out.append((f"{tag}_random_f64", ct, rng.standard_normal(n), xyz, conn,
+                    [run(iso=0.1), run(iso=-0.35, minmax=(-0.5, 0.5)), run(iso=0.1, form=1, duplication=False)]))
+        small = rng.integers(-2, 3, n)
+        out.append((f"{tag}_random_i8", ct, small.astype(np.int8), xyz, conn,
+                    [run(iso=0.0), run(iso=0.5), run(iso=1.0)]))
+        out.append((f"{tag}_random_u8", ct, rng.integers(0, 256, n).astype(np.uint8), xyz, conn,
+                    [run(iso=100.5)]))
+        out.append((f"{tag}_random_i16", ct, rng.integers(-3000, 3000, n).astype(np.int16), xyz, conn,
+                    [run(iso=17.0)]))
+        out.append((f"{tag}_random_u16", ct, rng.integers(0, 65536, n).astype(np.uint16), xyz, conn,
+                    [run(iso=30000.25)]))
+        out.append((f"{tag}_random_i32", ct, rng.integers(-2 ** 30, 2 ** 30, n).astype(np.int32), xyz, conn,
+                    [run(iso=12345.5)]))
+        out.append((f"{tag}_random_u32", ct, rng.integers(0, 2 ** 32 - 1, n, dtype=np.uint64).astype(np.uint32),
+                    xyz, conn, [run(iso=2.0 ** 31)]))
+        out.append((f"{tag}_random_i64", ct, rng.integers(-2 ** 60, 2 ** 60, n).astype(np.int64), xyz, conn,
+                    [run(iso=3.0 ** 30)]))
+        out.append((f"{tag}_random_u64", ct, rng.integers(0, 2 ** 63, n, dtype=np.uint64), xyz, conn,
+                    [run(iso=2.0 ** 62)]))
+        vn = rng.standard_normal(n).astype(np.float32)
+        vn[rng.choice(np.arange(1, n), 6, replace=False)] = np.nan
+        out.append((f"{tag}_nan_f32", ct, vn, xyz, conn, [run(iso=0.2)]))
+        v0 = rng.standard_normal(n).astype(np.float32)
+        v0[0] = np.nan
+        # (a NaN min/max with no transfer-function range makes the reference
+        # index its colour table with a NaN, undefined behaviour: give a range)
+        out.append((f"{tag}_nan0_f32", ct, v0, xyz, conn, [run(iso=0.2, tf_range=(-1.0, 1.0))]))
+        out.append((f"{tag}_constant_f32", ct, np.full(n, 1.5, np.float32), xyz, conn, [run(iso=1.5)]))
+        # node 0 off the cells with the largest value (min/max scan starts there)
+        conn1 = np.where(conn == 0, 1, conn).astype(np.uint32)
+        vz = rng.standard_normal(n).astype(np.float32)
+        vz[0] = 50.0
+        out.append((f"{tag}_unref0_f32", ct, vz, xyz, conn1, [run(iso=0.3)]))
+        # signed zeros: the first occurrence decides the sign of min/max
+        vs = np.where(rng.random(n) < 0.5, np.float32(-0.0), np.float32(0.0)).astype(np.float32)
+        vs[rng.choice(n, n // 3, replace=False)] = np.float32(1.0)
+        out.append((f"{tag}_zeros_f32", ct, vs, xyz, conn, [run(iso=0.5), run(iso=0.0)]))
+        # no cells: min/max over the nodes, nothing extracted
+        out.append((f"{tag}_nocells_f32", ct, rng.standard_normal(n).astype(np.float32), xyz,
+                    np.zeros((0, cm.NODES[ct]), np.uint32), [run(iso=0.0)]))
+    return out
+
+
+def write_cells():
+    arrays, manifest = {}, []
+    for name, ct, v, xyz, conn, runs in cells_cases():
+        arrays[f"{name}__values"] = v
+        arrays[f"{name}__coords"] = xyz
+        arrays[f"{name}__connections"] = conn
+        for i, o in enumerate(runs):
+            key = f"{name}__{i}"
+            r = ref.marching_cells(ct, v, xyz, conn, o["iso"], form=o["form"], normal_type=o["normal_type"],
+                                   duplication=o["duplication"], minmax=o["minmax"], tf_range=o["tf_range"])
+            for fld in ("coords", "normals", "connections", "colors", "opacities"):
+                arrays[f"{key}__{fld}"] = r[fld]
+            arrays[f"{key}__vol_minmax"] = np.array([r["vol_min"], r["vol_max"]], np.float64)
+            manifest.append(dict(key=key, case=name, cell_type=ct, **{k: o[k] for k in o},
+                                 success=r["success"], vol_has_minmax=r["vol_has_minmax"],
+                                 polygon_type=r["polygon_type"], color_type=r["color_type"],
+                                 normal_type_out=r["normal_type"], min_obj=r["min_obj"].tolist(),
+                                 max_obj=r["max_obj"].tolist(), min_ext=r["min_ext"].tolist(),
+                                 max_ext=r["max_ext"].tolist(), ntriangles=int(r["coords"].size // 9)))
+    np.savez_compressed(os.path.join(HERE, "cells.npz"), **arrays)
+    with open(os.path.join(HERE, "cells.json"), "w") as f:
+        json.dump(manifest, f, indent=0)
+    print(f"{len(manifest)} cells cases")
+
+
 def main():
     if not ref.available():
         ref.build()
-    parts = sys.argv[1:] or ["marching_cubes", "isosurface", "stl", "slice"]
+    parts = sys.argv[1:] or ["marching_cubes", "isosurface", "stl", "slice", "cells"]
+    if "cells" in parts:
+        write_cells()
     if "slice" in parts:
         write_slice()
     if "isosurface" in parts:

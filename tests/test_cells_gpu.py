@@ -1,0 +1,128 @@
+"""The unstructured marching mappers on the GPU (kvsmc_marching_cells_host
+through kvs_gb300.marching_cells and kvs_gb300.isosurface) against the
+fixtures made from the reference MarchingTetrahedra / Hexahedra / Pyramid /
+Prism, bit for bit (coordinates, normals, colour, types, the volume's min/max
+cache, bounding box), and against the numpy restatement on grids of a
+million and more cells."""
+import numpy as np
+import pytest
+
+from kvs_gb300 import _abi
+from kvs_gb300 import marching_cells as mcells
+from kvs_gb300.isosurface import Isosurface
+from kvs_gb300.marching_cubes import PolygonObject, TransferFunction
+from oracle import cells as ocells
+
+from . import cell_meshes as cm
+from .helpers import first_diff, same_bits
+from .test_cells_cpu import case_inputs, cells_fixtures
+
+pytestmark = pytest.mark.gpu
+
+torch = pytest.importorskip("torch")
+
+
+def _volume(ct, v, xyz, conn):
+    return mcells.UnstructuredVolumeObject(mcells.MAPPERS_BY_ABI[ct].CELL, v.size, conn.shape[0], 1, xyz, conn, v)
+
+
+def _run(e, arr, ctx):
+    v, xyz, conn = case_inputs(arr, e)
+    vol = _volume(e["cell_type"], v, xyz, conn)
+    if e["minmax"] is not None:
+        vol.setMinMaxValues(*e["minmax"])
+    tf = TransferFunction(256)
+    if e["tf_range"]:
+        tf.setRange(*e["tf_range"])
+    nt = PolygonObject.PolygonNormal if e["normal_type"] == "polygon" else PolygonObject.VertexNormal
+    if e["form"] == 1:
+        m = Isosurface(vol, e["iso"], nt, e["duplication"], tf, context=ctx)
+    else:
+        m = mcells.MAPPERS_BY_ABI[e["cell_type"]](vol, e["iso"], nt, e["duplication"], tf, context=ctx)
+    return m, vol
+
+
+def test_mappers_match_reference_fixtures(kvsmc_ctx):
+    man, arr = cells_fixtures()
+    for e in man:
+        k = e["key"]
+        m, vol = _run(e, arr, kvsmc_ctx)
+        assert m.isSuccess() == e["success"], k
+        for f, got in (("coords", m.coords()), ("normals", m.normals())):
+            want = arr[f"{k}__{f}"]
+            assert same_bits(got, want), (k, f, first_diff(got, want))
+        assert np.array_equal(m.colors(), arr[f"{k}__colors"]), k
+        assert np.array_equal(m.opacities(), arr[f"{k}__opacities"]), k
+        assert m.connections().size == 0, k
+        assert (m.polygonType(), m.colorType(), m.normalType()) == (
+            e["polygon_type"], e["color_type"], e["normal_type_out"]), k
+        assert vol.hasMinMaxValues() == e["vol_has_minmax"], k
+        assert same_bits(np.array([vol.minValue(), vol.maxValue()]), arr[f"{k}__vol_minmax"]), k
+        assert np.array_equal(m.minObjectCoord(), np.float32(e["min_obj"])), k
+        assert np.array_equal(m.maxObjectCoord(), np.float32(e["max_obj"])), k
+        assert np.array_equal(m.maxExternalCoord(), np.float32(e["max_ext"])), k
+
+
+@pytest.mark.parametrize("ct", [0, 1, 2, 3])
+def test_large_grids_match_oracle(kvsmc_ctx, ct):
+    """About 1.5 M tetrahedra, 250 k hexahedra, 1.5 M pyramids, 500 k prisms."""
+    xyz, conn = cm.grid(ct, 64, 64, 64, jitter=0.3, seed=40 + ct)
+    v = cm.sphere_values(xyz, (30.3, 31.7, 29.1))
+    for iso in (12.5, 27.0):
+        got_c, got_n, sizes = _abi.marching_cells_host(kvsmc_ctx, ct, v, xyz, conn, iso)
+        o = ocells.marching_cells(ct, v, xyz, conn, iso)
+        assert sizes["ntriangles"] * 9 == o["coords"].size > 0
+        assert (sizes["min_value"], sizes["max_value"]) == (o["vmin"], o["vmax"])
+        assert same_bits(got_c, o["coords"]), (ct, iso, first_diff(got_c, o["coords"]))
+        assert same_bits(got_n, o["normals"]), (ct, iso, first_diff(got_n, o["normals"]))
+
+
+def test_all_value_types_on_random_meshes(kvsmc_ctx):
+    """Random connectivity (every table case) at a size the fixtures do not
+    reach, all ten value types, with and without a preset min/max."""
+    rng = np.random.default_rng(5)
+    for ct in range(4):
+        xyz, conn = cm.random_mesh(ct, 5000, 200000, seed=ct)
+        for dt in _abi.DTYPES:
+            info = np.iinfo(dt) if np.dtype(dt).kind in "iu" else None
+            if info is None:
+                v = rng.standard_normal(5000).astype(dt)
+                iso = 0.25
+            else:
+                lo, hi = max(info.min, -1000), min(info.max, 1000)
+                v = rng.integers(lo, hi, 5000).astype(dt)
+                iso = (lo + hi) / 2 + 0.5
+            for mm in (None, (float(v.min()) / 2, float(v.max()) / 2)):
+                got_c, got_n, sizes = _abi.marching_cells_host(kvsmc_ctx, ct, v, xyz, conn, iso, mm)
+                o = ocells.marching_cells(ct, v, xyz, conn, iso, mm)
+                assert same_bits(got_c, o["coords"]), (ct, dt, mm, first_diff(got_c, o["coords"]))
+                assert same_bits(got_n, o["normals"]), (ct, dt, mm)
+
+
+def test_isosurface_default_isolevel_on_unstructured(kvsmc_ctx):
+    """Isosurface(volume, normal_type): the isolevel is (max + min) / 2 from the
+    device min/max over the cells' nodes."""
+    xyz, conn = cm.grid(0, 20, 18, 16, seed=3)
+    v = cm.sphere_values(xyz, (9.1, 8.3, 7.7))
+    v[0] = 100.0           # node 0 is always in the scan
+    vol = _volume(0, v, xyz, conn)
+    iso = Isosurface(vol, normal_type=PolygonObject.PolygonNormal, context=kvsmc_ctx)
+    lo, hi = ocells.minmax(v, conn, 0)
+    assert (vol.minValue(), vol.maxValue()) == (lo, hi) and hi == 100.0
+    o = ocells.marching_cells(0, v, xyz, conn, (hi + lo) * 0.5)
+    assert o["coords"].size > 0 and same_bits(iso.coords(), o["coords"])
+
+
+def test_bad_connection_index_is_an_error(kvsmc_ctx):
+    xyz, conn = cm.grid(1, 6, 6, 6, seed=1)
+    v = cm.sphere_values(xyz)
+    bad = conn.copy()
+    bad[7, 3] = xyz.shape[0]          # one past the last node
+    with pytest.raises(_abi.KvsmcError, match="connection index"):
+        _abi.marching_cells_host(kvsmc_ctx, 1, v, xyz, bad, 1.5)
+    # with a preset min/max the count pass finds it
+    with pytest.raises(_abi.KvsmcError, match="connection index"):
+        _abi.marching_cells_host(kvsmc_ctx, 1, v, xyz, bad, 1.5, (0.0, 5.0))
+    # the context stays usable
+    c, n, s = _abi.marching_cells_host(kvsmc_ctx, 1, v, xyz, conn, 1.5)
+    assert same_bits(c, ocells.marching_cells(1, v, xyz, conn, 1.5)["coords"])
