@@ -82,6 +82,11 @@ WORKLOADS = {
                       desc="kvs::SlicePlane of the 1024^3 float32 fBm field by the oblique plane through its "
                            "centre with normal (0.31, -0.52, 0.79): count + emit (coords, per-vertex colours from "
                            "the default colour map, normals) into device buffers through kvsmc_slice_extract_device"),
+    "tet160": dict(kind="cells", n=161, radii=[30.0, 50.0, 70.0, 90.0], seed=9,
+                   desc="kvs::MarchingTetrahedra on an unstructured volume: a 161^3-node grid (unit spacing, "
+                        "nodes jittered U[-0.2,0.2]) split into 6 tetrahedra per hexahedron (24.6 M cells, 4.17 M "
+                        "nodes), float32 values = distance to (80.3, 79.6, 80.9) + 1.5 sin(x/7) sin(y/9) sin(z/11), "
+                        "one isolevel per step cycling 30/50/70/90, duplication=true, PolygonNormal"),
     "blobs128": dict(shape=(128, 128, 128), kind="blobs", isos=[0.5],
                      desc="128^3 float32, 4 Gaussian blobs (sigma 8..24) + U[-0.01,0.01] noise, iso 0.5, "
                           "duplication=true, PolygonNormal"),
@@ -466,6 +471,194 @@ def run_stl(args, rank, world, local):
         "_sample_mesh": (meshes[0][0][:9 * min(meshes[0][2], 1 << 20)].cpu().numpy(),
                          meshes[0][1][:3 * min(meshes[0][2], 1 << 20)].cpu().numpy()),
     }
+
+
+def tet_grid(n, seed, device):
+    """The tet160 mesh: (values f32[N], coords f32[N, 3], connections int32[C, 4])."""
+    import torch
+    g = torch.Generator(device=device).manual_seed(seed)
+    ar = torch.arange(n, device=device, dtype=torch.float32)
+    z, y, x = torch.meshgrid(ar, ar, ar, indexing="ij")
+    xyz = torch.stack([x, y, z], -1).reshape(-1, 3)
+    xyz = xyz + (torch.rand(xyz.shape, generator=g, device=device) * 0.4 - 0.2)
+    c = torch.tensor([80.3, 79.6, 80.9], device=device)
+    vals = (torch.sqrt(((xyz - c) ** 2).sum(-1)) + 1.5 * torch.sin(xyz[:, 0] / 7) * torch.sin(xyz[:, 1] / 9)
+            * torch.sin(xyz[:, 2] / 11)).float().contiguous()
+    m = n - 1
+    ai = torch.arange(m, device=device, dtype=torch.int64)
+    cz, cy, cx = torch.meshgrid(ai, ai, ai, indexing="ij")
+    base = (cx + n * (cy + n * cz)).reshape(-1, 1)
+    off = torch.tensor([0, 1, 1 + n, n, n * n, n * n + 1, n * n + 1 + n, n * n + n], device=device)
+    hexa = base + off
+    del base
+    tets = torch.tensor([(0, 1, 2, 6), (0, 2, 3, 6), (0, 3, 7, 6), (0, 7, 4, 6), (0, 4, 5, 6), (0, 5, 1, 6)],
+                        device=device)
+    conn = hexa[:, tets].reshape(-1, 4).to(torch.int32).contiguous()
+    return vals, xyz.contiguous(), conn
+
+
+def run_cells(args, rank, world, local):
+    """kvsmc_marching_cells_device on a resident tetrahedral mesh (value), and
+    the mapper's host call kvsmc_marching_cells_host from pinned host arrays
+    (e2e)."""
+    import ctypes as C
+
+    import torch
+
+    from kvs_gb300 import _abi
+
+    torch.cuda.set_device(local)
+    w = WORKLOADS[args.workload]
+    ctx = _abi.Context(local)
+    stream = torch.cuda.Stream()
+    ctx.set_stream(stream.cuda_stream)
+    vals, xyz, conn = tet_grid(w["n"], w["seed"] + rank, "cuda")
+    nnodes, ncells = vals.numel(), conn.shape[0]
+    lo, hi = float(vals.min()), float(vals.max())
+    torch.cuda.synchronize()
+    s = _abi.Sizes()
+    fn = ctx.lib.kvsmc_marching_cells_device
+
+    def call(iso, oc, on, cap):
+        return fn(ctx.handle, 0, vals.data_ptr(), 8, nnodes, xyz.data_ptr(), conn.data_ptr(), ncells, iso, 1, lo, hi,
+                  oc, 9 * cap, on, 3 * cap, C.byref(s))
+
+    cap = 0
+    for r in w["radii"]:
+        st = call(r, None, None, 0)
+        if st not in (_abi.OK, 6):
+            ctx.check(st, "marching_cells_device")
+        cap = max(cap, s.ntriangles)
+    oc = torch.empty(max(1, 9 * cap), dtype=torch.float32, device="cuda")
+    on = torch.empty(max(1, 3 * cap), dtype=torch.float32, device="cuda")
+    tris = []
+
+    def step(i):
+        ctx.check(call(w["radii"][i % len(w["radii"])], oc.data_ptr(), on.data_ptr(), cap), "marching_cells_device")
+        tris.append(s.ntriangles)
+
+    for i in range(args.warmup):
+        step(i)
+    torch.cuda.synchronize()
+    tris.clear()
+    clocks = Clocks(local)
+    clocks.start()
+    ctx.profile_enable(True)
+    launches0 = ctx.kernel_launches
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for i in range(args.steps):
+        step(i)
+    e1.record(stream)
+    torch.cuda.synchronize()
+    ms = barrier_max(e0.elapsed_time(e1), world) / args.steps
+    prof = ctx.profile_read()
+    ctx.profile_enable(False)
+    launches = ctx.kernel_launches - launches0
+    clk = clocks.stop()
+    hbm, peak_kind = peaks()
+    t_avg = sum(tris) / len(tris)
+    # algorithmic bytes of one extraction: the connections once, the values and
+    # the coordinates once, the outputs (36 + 12 B per triangle)
+    algo = ncells * 16 + nnodes * 4 + nnodes * 12 + 48 * t_avg
+    count_ms = prof.get("cells_count", (0, 0.0))[1] / args.steps
+    emit_ms = prof.get("cells_emit", (0, 0.0))[1] / args.steps
+    line = {
+        "metric": "Mcells/s", "value": round(ncells * world / (ms * 1e-3) / 1e6, 1), "unit": "Mcells/s",
+        "n_gpus": world, "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(ms, 4),
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+        "data": "synthetic (seeded mesh and field generated on the device)",
+        "config": {"workload": w["desc"], "cells": ncells, "nodes": nnodes, "triangles_per_step": int(t_avg),
+                   "cache": "inputs larger than L2 (394 MB of connections per step)"},
+        "roofline": {"kernel": "cells_count + cells_emit + scan (whole step)", "bound": "hbm",
+                     "achieved": round(algo / (ms * 1e-3) / 1e9, 1), "peak": hbm, "peak_kind": peak_kind,
+                     "unit": "GB/s", "frac": round(algo / (ms * 1e-3) / 1e9 / hbm, 4),
+                     "algorithmic_bytes_per_step": int(algo), "count_ms": round(count_ms, 4),
+                     "emit_ms": round(emit_ms, 4), "traffic": None},
+        "kernels": {kk: {"launches": vv[0], "ms": round(vv[1], 3)} for kk, vv in prof.items()},
+        "gpu_launches": int(launches // max(1, args.steps)), "clocks": clk,
+    }
+    if not args.no_e2e:
+        hv = torch.empty(vals.shape, dtype=vals.dtype, pin_memory=True)
+        hx = torch.empty(xyz.shape, dtype=xyz.dtype, pin_memory=True)
+        hk = torch.empty(conn.shape, dtype=conn.dtype, pin_memory=True)
+        hv.copy_(vals)
+        hx.copy_(xyz)
+        hk.copy_(conn)
+        del vals, xyz, conn, oc, on
+        torch.cuda.empty_cache()
+        nv, nx, nk = hv.numpy(), hx.numpy(), hk.numpy().view(np.uint32)
+        e2e_tris = []
+
+        def e2e_step(i):
+            c, n, sz = _abi.marching_cells_host(ctx, 0, nv, nx, nk, w["radii"][i % len(w["radii"])], (lo, hi))
+            e2e_tris.append(sz["ntriangles"])
+
+        for i in range(args.warmup):
+            e2e_step(i)
+        e2e_tris.clear()
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        for i in range(args.steps):
+            e2e_step(i)
+        torch.cuda.synchronize()
+        e_ms = barrier_max((time.perf_counter() - t0) * 1e3, world) / args.steps
+        line["e2e"] = {"value": round(ncells * world / (e_ms * 1e-3) / 1e6, 1), "unit": "Mcells/s",
+                       "ms_per_step": round(e_ms, 3),
+                       "h2d_bytes_per_step": int(nv.nbytes + nx.nbytes + nk.nbytes),
+                       "d2h_bytes_per_step": int(48 * sum(e2e_tris) / len(e2e_tris)),
+                       "path": "kvsmc_marching_cells_host (the kvs::cuda::MarchingTetrahedra call) from pinned "
+                               "host arrays: upload, count, emit, copy back"}
+    return line
+
+
+def cells_cpu_sample(w, planes):
+    """A z-slab of the tet160 mesh (full x/y extent, `planes` node planes),
+    generated on the CPU with the same formula."""
+    vals, xyz, conn = tet_grid(w["n"], w["seed"], "cpu")
+    n = w["n"]
+    z0 = (n - planes) // 2                      # through the centre: every isolevel cuts it
+    nodes = slice(z0 * n * n, (z0 + planes) * n * n)
+    cells_per_plane = (n - 1) * (n - 1) * 6
+    cells = slice(z0 * cells_per_plane, (z0 + planes - 1) * cells_per_plane)
+    return (vals[nodes].numpy(), xyz[nodes].numpy(), (conn[cells] - z0 * n * n).numpy().view(np.uint32))
+
+
+def run_cells_cpu(w, reference, min_seconds=10.0):
+    """The CPU mapper on a 17-plane slab through the centre (2.5 M tetrahedra), one host core,
+    cycling the isolevels for at least `min_seconds`: the reference
+    MarchingTetrahedra (oracle/_ref) when built, else the numpy restatement
+    (oracle/cells.py); returns (Mcells/s, seconds, sample, kind)."""
+    vals, xyz, conn = cells_cpu_sample(w, 17)
+    ncells = conn.shape[0]
+    lo, hi = float(vals.min()), float(vals.max())
+    kind = "port"
+    if reference:
+        from oracle import ref
+        if ref.available():
+            kind = "reference"
+    t0 = time.perf_counter()
+    done = 0
+    calls = 0
+    t = 0.0
+    while calls < len(w["radii"]) or time.perf_counter() - t0 < min_seconds:
+        r = w["radii"][calls % len(w["radii"])]
+        calls += 1
+        if kind == "reference":
+            from oracle import ref
+            # the mapper constructor alone, timed inside the driver (the
+            # volume object's setup copies are left out)
+            t += ref.marching_cells(0, vals, xyz, conn, r, minmax=(lo, hi))["seconds"]
+        else:
+            from oracle import cells as OC
+            t1 = time.perf_counter()
+            OC.marching_cells(0, vals, xyz, conn, r, (lo, hi))
+            t += time.perf_counter() - t1
+        done += ncells
+    what = ("the reference kvs::MarchingTetrahedra (oracle/_ref)" if kind == "reference"
+            else "oracle/cells.py (numpy restatement of kvs::MarchingTetrahedra)")
+    return (done / t / 1e6, t, f"{calls} calls (isolevels 30/50/70/90 in turn) on the central 17-plane slab "
+            f"({ncells / 1e6:.2f} M tetrahedra), {what}", kind)
 
 
 def run_stl_cpu(mesh):
@@ -1037,6 +1230,23 @@ def run_reference(args, rank, world):
     threads = os.cpu_count() or 1
     if w["kind"] == "batch":
         return run_reference_batch(args, world, threads)
+    if w["kind"] == "cells":
+        vals = []
+        for i in range(args.warmup + args.steps):
+            v, t, sample, kind = run_cells_cpu(w, reference=True, min_seconds=3.0)
+            if i >= args.warmup:
+                vals.append((v, t))
+        value = statistics.median(v for v, _ in vals)
+        ms = statistics.median(t for _, t in vals) * 1e3
+        return {
+            "impl": "reference", "metric": "Mcells/s", "value": round(value, 1), "unit": "Mcells/s",
+            "n_gpus": world, "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(ms, 1),
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+            "config": {"workload": w["desc"], "sample": sample},
+            "cpu_baseline": {"value": round(value, 1), "unit": "Mcells/s", "cores": 1, "kind": kind,
+                             "sample": sample},
+            "e2e": {"value": round(value, 1), "unit": "Mcells/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+        }
     if w["kind"] == "serve":
         return {"impl": "reference", "unavailable": "the reference has no request loop (one kvs::MarchingCubes call "
                 "at a time on the caller's thread); its per-request CPU cost is the uneven200 / sweep1024 reference "
@@ -1089,6 +1299,12 @@ def main():
         line = run_reference(args, rank, world)
     elif WORKLOADS[args.workload]["kind"] == "slice":
         line = run_slice(args, rank, world, local)
+    elif WORKLOADS[args.workload]["kind"] == "cells":
+        line = run_cells(args, rank, world, local)
+        if rank == 0 and world == 1 and not args.no_cpu:
+            v, t, sample, kind = run_cells_cpu(WORKLOADS[args.workload], reference=False)
+            line["cpu_baseline"] = {"value": round(v, 1), "unit": "Mcells/s", "cores": 1, "kind": kind,
+                                    "sample": sample + f"; {t:.1f} s on 1 host core"}
     elif WORKLOADS[args.workload]["kind"] == "ingest":
         line = run_ingest(args, rank, world, local)
     elif WORKLOADS[args.workload]["kind"] == "stl":

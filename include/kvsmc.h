@@ -328,17 +328,30 @@ kvsmc_status kvsmc_extract_noalloc(const void* d_values, kvsmc_dtype dtype, uint
  * 4 / 8 / 5 / 6 connections each.  Duplicated vertices, one normal per
  * triangle (the reference builds nothing in shared-vertex mode), cells in
  * order, table order inside a cell, same bits.  The isolevel and the clamp
- * range (has_minmax: min/max given, else the device scan of the values,
- * StructuredVolumeObject's rules) decide as in the reference; the
- * Math::Equal(min, max) early exit gives sizes->extracted = 0.  Outputs come
- * from `alloc` (which: 0 coords, 1 normals).  A connection index >= nnodes is
- * KVSMC_ERR_INVALID_ARGUMENT (checked on the device, nothing read out of
- * range). */
+ * range (has_minmax: min/max given, else the device scan over values[0] and
+ * the cells' nodes, UnstructuredVolumeObject.cpp:82-143, or over the nodes
+ * when there are no cells) decide as in the reference; sizes->min_value /
+ * max_value return the range used; the Math::Equal(min, max) early exit
+ * gives sizes->extracted = 0.  Outputs come from `alloc` (which: 0 coords,
+ * 1 normals).  A connection index >= nnodes is KVSMC_ERR_INVALID_ARGUMENT
+ * (checked on the device, nothing read out of range); more than 2^31 - 1
+ * nodes or 2^32 - 1 cells is KVSMC_ERR_TOO_LARGE (the reference's int node
+ * ids and UInt32 cell counter).  An isolevel of NaN classifies every node
+ * below it: only the min/max scan and an empty count run. */
 kvsmc_status kvsmc_marching_cells_host(kvsmc_context* ctx, kvsmc_cell_type cell_type, const void* values,
                                        kvsmc_dtype dtype, uint64_t nnodes, const float* coords,
                                        const uint32_t* connections, uint64_t ncells, double isolevel,
                                        int32_t has_minmax, double min_value, double max_value,
                                        kvsmc_host_alloc_fn alloc, void* user, kvsmc_sizes* sizes);
+/* The same on DEVICE arrays (values, coords, connections) into caller-provided
+ * device outputs (capacities in floats: 9 T coords, 3 T normals); on
+ * KVSMC_ERR_CAPACITY nothing is written and *sizes holds the need. */
+kvsmc_status kvsmc_marching_cells_device(kvsmc_context* ctx, kvsmc_cell_type cell_type, const void* d_values,
+                                         kvsmc_dtype dtype, uint64_t nnodes, const float* d_coords,
+                                         const uint32_t* d_connections, uint64_t ncells, double isolevel,
+                                         int32_t has_minmax, double min_value, double max_value,
+                                         float* d_out_coords, uint64_t coords_capacity, float* d_out_normals,
+                                         uint64_t normals_capacity, kvsmc_sizes* sizes);
 
 /* -------------------------------------------------------------- slice plane */
 
@@ -528,6 +541,11 @@ int32_t kvsmc_profile_read(kvsmc_context* ctx, int32_t max, const char** names, 
  * and how many fell back to FP64.  No counterpart in the reference. */
 kvsmc_status kvsmc_selftest_interpolation(kvsmc_context* ctx, uint64_t n, uint64_t seed, uint64_t* tested,
                                           uint64_t* mismatches, uint64_t* fallbacks);
+/* The same for the unstructured mappers' vertex on random float endpoints
+ * (interpolate_vertex, MarchingTetrahedra.cpp:325-346): the FP32 certificate
+ * of the cells' emit pass against the FP64 sequence. */
+kvsmc_status kvsmc_selftest_cells(kvsmc_context* ctx, uint64_t n, uint64_t seed, uint64_t* tested,
+                                  uint64_t* mismatches, uint64_t* fallbacks);
 
 #ifdef __cplusplus
 }

@@ -49,7 +49,7 @@ EXPORTS = [
     "kvsmc_write_stl_host", "kvsmc_volume_download", "kvsmc_kvsml_read_info", "kvsmc_volume_load_kvsml",
     "kvsmc_avs_read_info", "kvsmc_volume_load_avs",
     "kvsmc_slice_count", "kvsmc_slice_extract_device", "kvsmc_slice_plane",
-    "kvsmc_marching_cells_host",
+    "kvsmc_marching_cells_host", "kvsmc_marching_cells_device", "kvsmc_selftest_cells",
 ]
 
 PATH_AUTO = 0      # streaming kernels where eligible
@@ -173,6 +173,7 @@ def load(path=LIB_PATH):
         "kvsmc_set_kernel_path": (C.c_int, [vp, i32]),
         "kvsmc_selftest_interpolation": (C.c_int, [vp, u64, u64, C.POINTER(u64), C.POINTER(u64),
                                                    C.POINTER(u64)]),
+        "kvsmc_selftest_cells": (C.c_int, [vp, u64, u64, C.POINTER(u64), C.POINTER(u64), C.POINTER(u64)]),
         "kvsmc_extract_batch_host": (C.c_int, [vp, vp, C.c_int, u32, u32, u32, C.POINTER(Params), i32,
                                                HOST_ALLOC, vp, C.POINTER(Sizes)]),
         "kvsmc_extract_noalloc": (C.c_int, [vp, C.c_int, u32, u32, u32, C.POINTER(Params), vp, u64, vp, u64,
@@ -197,6 +198,8 @@ def load(path=LIB_PATH):
         "kvsmc_slice_plane": (C.c_int, [vp, vp, C.POINTER(SliceParams), HOST_ALLOC, vp, C.POINTER(u64)]),
         "kvsmc_marching_cells_host": (C.c_int, [vp, C.c_int, vp, C.c_int, u64, vp, vp, u64, C.c_double, i32,
                                                 C.c_double, C.c_double, HOST_ALLOC, vp, C.POINTER(Sizes)]),
+        "kvsmc_marching_cells_device": (C.c_int, [vp, C.c_int, vp, C.c_int, u64, vp, vp, u64, C.c_double, i32,
+                                                  C.c_double, C.c_double, vp, u64, vp, u64, C.POINTER(Sizes)]),
         "kvsmc_kvsml_read_info": (C.c_int, [C.c_char_p, C.POINTER(KvsmlInfo)]),
         "kvsmc_volume_load_kvsml": (C.c_int, [vp, C.c_char_p, C.POINTER(vp), C.POINTER(KvsmlInfo)]),
         "kvsmc_avs_read_info": (C.c_int, [C.c_char_p, C.POINTER(KvsmlInfo)]),
@@ -274,6 +277,12 @@ class Context:
         t, m, f = C.c_uint64(), C.c_uint64(), C.c_uint64()
         self.check(self.lib.kvsmc_selftest_interpolation(self.handle, int(n), int(seed), C.byref(t), C.byref(m),
                                                          C.byref(f)), "kvsmc_selftest_interpolation")
+        return t.value, m.value, f.value
+
+    def selftest_cells(self, n, seed=1):
+        t, m, f = C.c_uint64(), C.c_uint64(), C.c_uint64()
+        self.check(self.lib.kvsmc_selftest_cells(self.handle, int(n), int(seed), C.byref(t), C.byref(m),
+                                                 C.byref(f)), "kvsmc_selftest_cells")
         return t.value, m.value, f.value
 
     def close(self):

@@ -845,21 +845,34 @@ kvsmc_status kvsmc_extract_batch(kvsmc_context* ctx, kvsmc_request* reqs, int32_
     return batch_items(ctx, reqs, n, true);
 }
 
-kvsmc_status kvsmc_selftest_interpolation(kvsmc_context* ctx, uint64_t n, uint64_t seed, uint64_t* tested,
-                                          uint64_t* mismatches, uint64_t* fallbacks)
+static kvsmc_status selftest_run(kvsmc_context* ctx, bool cells, uint64_t n, uint64_t seed, uint64_t* tested,
+                                 uint64_t* mismatches, uint64_t* fallbacks)
 {
     kvsmc_status st = use_device(ctx);
     if (st) return st;
     if ((st = ensure_scratch(ctx, 256))) return st;
     unsigned long long* d = static_cast<unsigned long long*>(ctx->scratch);
     KVSMC_CUDA(ctx, cudaMemsetAsync(d, 0, 3 * sizeof(unsigned long long), ctx->stream));
-    KVSMC_CUDA(ctx, launch_selftest(n, seed, d, launch_of(ctx)));
+    if (cells) KVSMC_CUDA(ctx, launch_selftest_cells(n, seed, d, launch_of(ctx)));
+    else KVSMC_CUDA(ctx, launch_selftest(n, seed, d, launch_of(ctx)));
     KVSMC_CUDA(ctx, cudaMemcpyAsync(ctx->h_small, d, 3 * sizeof(unsigned long long), cudaMemcpyDeviceToHost, ctx->stream));
     KVSMC_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
     if (tested) *tested = ctx->h_small[0];
     if (mismatches) *mismatches = ctx->h_small[1];
     if (fallbacks) *fallbacks = ctx->h_small[2];
     return KVSMC_OK;
+}
+
+kvsmc_status kvsmc_selftest_interpolation(kvsmc_context* ctx, uint64_t n, uint64_t seed, uint64_t* tested,
+                                          uint64_t* mismatches, uint64_t* fallbacks)
+{
+    return selftest_run(ctx, false, n, seed, tested, mismatches, fallbacks);
+}
+
+kvsmc_status kvsmc_selftest_cells(kvsmc_context* ctx, uint64_t n, uint64_t seed, uint64_t* tested,
+                                  uint64_t* mismatches, uint64_t* fallbacks)
+{
+    return selftest_run(ctx, true, n, seed, tested, mismatches, fallbacks);
 }
 
 }  // extern "C"

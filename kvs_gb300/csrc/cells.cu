@@ -12,20 +12,28 @@
 // come from the cell type's table in the mapper's vertex order (cell_tables.h);
 // a vertex on the edge (n0, n1) is, in double, c0 + r (c1 - c0) per axis with
 // r = |(iso - v0) / (v1 - v0)|, v clamped to the volume's [min, max], c1 - c0
-// a float difference, then rounded to float (interpolate_vertex); one normal
-// per triangle (v1 - v0) x (v2 - v0).  Duplicated vertices only (the
+// a float difference, then rounded to float (interpolate_vertex) -- here
+// computed in FP32 double-float arithmetic with a rigorous error bound and
+// taken only when no float rounding boundary lies within it (cell_axis),
+// else by the FP64 sequence, so the bits are the reference's either way; one
+// normal per triangle (v1 - v0) x (v2 - v0).  Duplicated vertices only (the
 // reference's shared-vertex branch is not built, :164-206).
 //
-// Two passes over tiles of 256 cells: count, an exclusive scan of the tile
-// counts, emit (a block-wide scan of each cell's triangle count).  A
+// Two passes over groups of 32 cells, a warp per group: count, an exclusive
+// scan of the group counts, emit (a warp scan of each cell's triangle
+// count); the emit pass skips the groups that counted no triangle without
+// reading their cells.  A
 // connection index outside the nodes sets a flag and reads node 0 instead.
 #include <cuda_runtime.h>
 
+#include <algorithm>
 #include <cstring>
 
 #include "cell_tables.h"
 #include "context.h"
+#include "batch.h"
 #include "mc_device.cuh"
+#include "mc_interp.cuh"
 
 namespace kvsmc {
 
@@ -81,31 +89,55 @@ template <typename T> __device__ __forceinline__ double dval(const void* v, uint
     return to_double(static_cast<const T*>(v)[i]);
 }
 
-// The cell's local node indices (checked against the node count) and case.
-template <int CT, typename T>
-__device__ __forceinline__ unsigned cell_case(const CellJob& j, uint64_t cell, uint64_t* nodes)
+// The cell's local node indices (checked against the node count): one or two
+// 16-byte loads per cell when the connections allow it (tetrahedra,
+// hexahedra on a 16-byte aligned array), else 32-bit loads.
+template <int CT>
+__device__ __forceinline__ void cell_nodes(const CellJob& j, uint64_t cell, uint32_t* nodes)
 {
     using Tr = CellTraits<CT>;
     const uint32_t* conn = j.conn + (uint64_t)Tr::kNodes * cell;
+    uint32_t raw[Tr::kNodes];
+    if ((CT == KVSMC_TETRAHEDRA || CT == KVSMC_HEXAHEDRA) && j.conn_vec16) {
+#pragma unroll
+        for (int q = 0; q < Tr::kNodes / 4; ++q) {
+            const uint4 w = __ldg(reinterpret_cast<const uint4*>(conn) + q);
+            raw[4 * q] = w.x; raw[4 * q + 1] = w.y; raw[4 * q + 2] = w.z; raw[4 * q + 3] = w.w;
+        }
+    } else {
+#pragma unroll
+        for (int k = 0; k < Tr::kNodes; ++k) raw[k] = __ldg(conn + k);
+    }
 #pragma unroll
     for (int k = 0; k < Tr::kNodes; ++k) {
-        uint64_t n = conn[Tr::node(k)];
+        uint32_t n = raw[Tr::node(k)];
         if (n >= j.nnodes) {
             atomicExch(j.bad_index, 1);
             n = 0;
         }
         nodes[k] = n;
     }
+}
+
+// The case: bit k iff double(value of local node k) > isolevel, decided
+// without FP64 for float and up-to-32-bit integer values (Classifier).
+template <int CT, typename T>
+__device__ __forceinline__ unsigned cell_case(const CellJob& j, uint64_t cell, uint32_t* nodes)
+{
+    using Tr = CellTraits<CT>;
+    cell_nodes<CT>(j, cell, nodes);
+    const T* vals = static_cast<const T*>(j.values);
     unsigned c = 0;
 #pragma unroll
-    for (int k = 0; k < Tr::kNodes; ++k) c |= (dval<T>(j.values, nodes[k]) > j.iso) ? (1u << k) : 0u;
+    for (int k = 0; k < Tr::kNodes; ++k) c |= above(j.cls, __ldg(vals + nodes[k])) ? (1u << k) : 0u;
     if (CT == KVSMC_PYRAMID && (c == 10u || c == 11u || c == 20u || c == 21u)) {
-        const double v1 = dval<T>(j.values, nodes[1]), v2 = dval<T>(j.values, nodes[2]);
-        const double v3 = dval<T>(j.values, nodes[3]), v4 = dval<T>(j.values, nodes[4]);
-        const double A = __ddiv_rn(__dadd_rn(__dadd_rn(__dadd_rn(v1, v2), v3), v4), 4.0);
-        const double B = __ddiv_rn(__dsub_rn(__dadd_rn(__dadd_rn(-v1, v2), v3), v4), 4.0);
-        const double C = __ddiv_rn(__dadd_rn(__dadd_rn(__dsub_rn(-v1, v2), v3), v4), 4.0);
-        const double D = __ddiv_rn(__dsub_rn(__dadd_rn(__dsub_rn(v1, v2), v3), v4), 4.0);
+        // x / 4 as x * 0.25: the same correctly rounded result
+        const double v1 = to_double(vals[nodes[1]]), v2 = to_double(vals[nodes[2]]);
+        const double v3 = to_double(vals[nodes[3]]), v4 = to_double(vals[nodes[4]]);
+        const double A = __dmul_rn(__dadd_rn(__dadd_rn(__dadd_rn(v1, v2), v3), v4), 0.25);
+        const double B = __dmul_rn(__dsub_rn(__dadd_rn(__dadd_rn(-v1, v2), v3), v4), 0.25);
+        const double C = __dmul_rn(__dadd_rn(__dadd_rn(__dsub_rn(-v1, v2), v3), v4), 0.25);
+        const double D = __dmul_rn(__dsub_rn(__dadd_rn(__dsub_rn(v1, v2), v3), v4), 0.25);
         const double E = __dadd_rn(__dmul_rn(__dsub_rn(j.iso, A), D), __dmul_rn(B, C));
         if (c == 10u && E < 0) c = 32u;
         else if (c == 11u && E >= 0) c = 33u;
@@ -115,8 +147,10 @@ __device__ __forceinline__ unsigned cell_case(const CellJob& j, uint64_t cell, u
     return c;
 }
 
+// The reference's FP64 sequence, out of line (it runs for the vertices the
+// FP32 certificate cannot decide, and for 32/64-bit integer and double values).
 template <typename T>
-__device__ __forceinline__ float3 cell_vertex(const CellJob& j, uint64_t n0, uint64_t n1)
+static __device__ __noinline__ float3 cell_vertex_exact(const CellJob& j, uint32_t n0, uint32_t n1)
 {
     const double lo = j.vmin, hi = j.vmax;
     double v0 = dval<T>(j.values, n0), v1 = dval<T>(j.values, n1);
@@ -124,8 +158,8 @@ __device__ __forceinline__ float3 cell_vertex(const CellJob& j, uint64_t n0, uin
     v1 = v1 <= lo ? lo : (v1 <= hi ? v1 : hi);
     const double q = __ddiv_rn(__dsub_rn(j.iso, v0), __dsub_rn(v1, v0));
     const double r = q < 0.0 ? -q : q;
-    const float* c0 = j.coords + 3 * n0;
-    const float* c1 = j.coords + 3 * n1;
+    const float* c0 = j.coords + 3 * (uint64_t)n0;
+    const float* c1 = j.coords + 3 * (uint64_t)n1;
     float3 o;
     o.x = __double2float_rn(__dadd_rn((double)c0[0], __dmul_rn(r, (double)__fsub_rn(c1[0], c0[0]))));
     o.y = __double2float_rn(__dadd_rn((double)c0[1], __dmul_rn(r, (double)__fsub_rn(c1[1], c0[1]))));
@@ -133,66 +167,81 @@ __device__ __forceinline__ float3 cell_vertex(const CellJob& j, uint64_t n0, uin
     return o;
 }
 
-__device__ __forceinline__ uint32_t cell_block_sum(uint32_t v, uint32_t* ws)
-{
-    for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
-    const unsigned lane = threadIdx.x & 31u, warp = threadIdx.x >> 5;
-    __syncthreads();
-    if (lane == 0) ws[warp] = v;
-    __syncthreads();
-    uint32_t t = 0;
-    for (unsigned w = 0; w < blockDim.x / 32; ++w) t += ws[w];
-    return t;
-}
+// Value types whose values are floats exactly (the FP32 certificate applies).
+template <typename T> struct CellFast { static constexpr bool value = false; };
+template <> struct CellFast<float> { static constexpr bool value = true; };
+template <> struct CellFast<int8_t> { static constexpr bool value = true; };
+template <> struct CellFast<int16_t> { static constexpr bool value = true; };
+template <> struct CellFast<uint8_t> { static constexpr bool value = true; };
+template <> struct CellFast<uint16_t> { static constexpr bool value = true; };
 
-__device__ __forceinline__ uint32_t cell_block_excl(uint32_t v, uint32_t* ws)
+// interpolate_vertex: the FP32 certificate (cell_ratio / cell_axis), else FP64.
+template <typename T>
+__device__ __forceinline__ float3 cell_vertex(const CellJob& j, uint32_t n0, uint32_t n1)
 {
-    const unsigned lane = threadIdx.x & 31u, warp = threadIdx.x >> 5;
-    uint32_t inc = v;
-    for (int o = 1; o < 32; o <<= 1) {
-        const uint32_t t = __shfl_up_sync(0xffffffffu, inc, o);
-        if (lane >= (unsigned)o) inc += t;
+    if constexpr (CellFast<T>::value) {
+        const T* vals = static_cast<const T*>(j.values);
+        const float v0 = clampf_ref((float)__ldg(vals + n0), j.f.vmin_f, j.f.vmax_f);
+        const float v1 = clampf_ref((float)__ldg(vals + n1), j.f.vmin_f, j.f.vmax_f);
+        const CellRatio c = cell_ratio(v0, v1, j.f);
+        const float* c0 = j.coords + 3 * (uint64_t)n0;
+        const float* c1 = j.coords + 3 * (uint64_t)n1;
+        float3 o;
+        const bool ox = cell_axis(c, __ldg(c0), __ldg(c1), o.x);
+        const bool oy = cell_axis(c, __ldg(c0 + 1), __ldg(c1 + 1), o.y);
+        const bool oz = cell_axis(c, __ldg(c0 + 2), __ldg(c1 + 2), o.z);
+        if (ox && oy && oz) return o;
     }
-    __syncthreads();
-    if (lane == 31) ws[warp] = inc;
-    __syncthreads();
-    uint32_t before = 0;
-    for (unsigned w = 0; w < warp; ++w) before += ws[w];
-    return before + inc - v;
+    return cell_vertex_exact<T>(j, n0, n1);
 }
 
+// Both passes work on groups of 32 consecutive cells, one warp per group
+// (grid-stride over groups): the count pass writes each group's triangle
+// count, the emit pass skips the groups that counted none without reading
+// their cells and places the others' triangles by a warp scan.
 template <int CT, typename T>
 __global__ void __launch_bounds__(kCellThreads) k_cells_count(CellJob j)
 {
-    __shared__ uint32_t ws[32];
     using Tr = CellTraits<CT>;
-    for (uint64_t tile = blockIdx.x; tile * kCellThreads < j.ncells; tile += gridDim.x) {
-        const uint64_t cell = tile * kCellThreads + threadIdx.x;
+    const unsigned lane = threadIdx.x & 31u;
+    const uint64_t warps = (uint64_t)gridDim.x * (kCellThreads / 32);
+    const uint64_t groups = (j.ncells + 31) / 32;
+    for (uint64_t g = (uint64_t)blockIdx.x * (kCellThreads / 32) + (threadIdx.x >> 5); g < groups; g += warps) {
+        const uint64_t cell = g * 32 + lane;
         uint32_t n = 0;
         if (cell < j.ncells) {
-            uint64_t nodes[Tr::kNodes];
+            uint32_t nodes[Tr::kNodes];
             n = Tr::ntri(cell_case<CT, T>(j, cell, nodes));
         }
-        const uint32_t t = cell_block_sum(n, ws);
-        if (threadIdx.x == 0) j.tile_counts[tile] = t;
+        const uint32_t t = __reduce_add_sync(0xffffffffu, n);
+        if (lane == 0) j.tile_counts[g] = t;
     }
 }
 
 template <int CT, typename T>
 __global__ void __launch_bounds__(kCellThreads) k_cells_emit(CellJob j)
 {
-    __shared__ uint32_t ws[32];
     using Tr = CellTraits<CT>;
-    for (uint64_t tile = blockIdx.x; tile * kCellThreads < j.ncells; tile += gridDim.x) {
-        const uint64_t cell = tile * kCellThreads + threadIdx.x;
-        uint64_t nodes[Tr::kNodes];
+    const unsigned lane = threadIdx.x & 31u;
+    const uint64_t warps = (uint64_t)gridDim.x * (kCellThreads / 32);
+    const uint64_t groups = (j.ncells + 31) / 32;
+    for (uint64_t g = (uint64_t)blockIdx.x * (kCellThreads / 32) + (threadIdx.x >> 5); g < groups; g += warps) {
+        if (j.tile_counts[g] == 0) continue;   // warp-uniform: no triangle in these 32 cells
+        const uint64_t cell = g * 32 + lane;
+        uint32_t nodes[Tr::kNodes];
         unsigned c = 0;
         uint32_t n = 0;
         if (cell < j.ncells) {
             c = cell_case<CT, T>(j, cell, nodes);
             n = Tr::ntri(c);
         }
-        uint64_t t = j.tile_offsets[tile] + cell_block_excl(n, ws);
+        uint32_t inc = n;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const uint32_t y = __shfl_up_sync(0xffffffffu, inc, o);
+            if (lane >= (unsigned)o) inc += y;
+        }
+        uint64_t t = j.tile_offsets[g] + (inc - n);
         uint64_t pk = Tr::tri(c);
         for (uint32_t k = 0; k < n; ++k, ++t, pk >>= 12) {
             if (t >= j.cap_tris) break;   // never past the outputs
@@ -212,7 +261,6 @@ __global__ void __launch_bounds__(kCellThreads) k_cells_emit(CellJob j)
         }
     }
 }
-
 
 // ---- min/max over the cells' nodes (GetMinMaxValues with connections,
 // UnstructuredVolumeObject.cpp:123-143): the scan starts at values[0] and
@@ -292,10 +340,12 @@ __global__ void __launch_bounds__(kCellThreads) k_cells_minmax_final(CellJob j, 
     }
 }
 
-unsigned cell_grid(uint64_t tiles, const Launch& L)
+// Blocks of 8 warps, one warp per 32-cell group, at most 8 blocks per SM.
+unsigned cell_grid(uint64_t groups, const Launch& L)
 {
+    const uint64_t blocks = (groups + kCellThreads / 32 - 1) / (kCellThreads / 32);
     const uint64_t cap = (uint64_t)L.num_sms * 8;
-    return (unsigned)(tiles < cap ? (tiles ? tiles : 1) : cap);
+    return (unsigned)(blocks < cap ? (blocks ? blocks : 1) : cap);
 }
 
 #define KVSMC_CELL_SWITCH(CTV, DT, ...)                                                     \
@@ -327,7 +377,7 @@ unsigned cell_grid(uint64_t tiles, const Launch& L)
 cudaError_t launch_cells_count(const CellJob& j, const Launch& L)
 {
     if (j.ncells == 0) return cudaSuccess;
-    const uint64_t tiles = (j.ncells + kCellThreads - 1) / kCellThreads;
+    const uint64_t tiles = cells_tiles(j.ncells);
     prof_begin(L, "cells_count");
     KVSMC_CELL_SWITCH(j.cell_type, j.dtype,
                       { k_cells_count<CT, T><<<cell_grid(tiles, L), kCellThreads, 0, L.stream>>>(j); });
@@ -339,7 +389,7 @@ cudaError_t launch_cells_count(const CellJob& j, const Launch& L)
 cudaError_t launch_cells_emit(const CellJob& j, const Launch& L)
 {
     if (j.ncells == 0) return cudaSuccess;
-    const uint64_t tiles = (j.ncells + kCellThreads - 1) / kCellThreads;
+    const uint64_t tiles = cells_tiles(j.ncells);
     prof_begin(L, "cells_emit");
     KVSMC_CELL_SWITCH(j.cell_type, j.dtype,
                       { k_cells_emit<CT, T><<<cell_grid(tiles, L), kCellThreads, 0, L.stream>>>(j); });
@@ -368,7 +418,7 @@ cudaError_t launch_cells_minmax(const CellJob& j, void* scratch, double* d_out, 
     return cudaGetLastError();
 }
 
-uint64_t cells_tiles(uint64_t ncells) { return (ncells + kCellThreads - 1) / kCellThreads; }
+uint64_t cells_tiles(uint64_t ncells) { return (ncells + 31) / 32; }
 
 }  // namespace kvsmc
 
@@ -388,9 +438,144 @@ bool equal_abs(double a, double b)
     return (d < 0 ? -d : d) < 1.e-6;
 }
 
+kvsmc_status check_args(kvsmc_context* ctx, int cell_type, int dtype, uint64_t nnodes, const void* values,
+                        const float* coords, const uint32_t* connections, uint64_t ncells)
+{
+    if (nodes_per_cell(cell_type) == 0)
+        return fail(ctx, KVSMC_ERR_INVALID_ARGUMENT, "cells: unknown cell type %d", cell_type);
+    if (kvsmc::dtype_size(dtype) == 0) return fail(ctx, KVSMC_ERR_UNSUPPORTED_DTYPE, "cells: data type %d", dtype);
+    if (nnodes == 0 || !values || !coords || (ncells && !connections))
+        return fail(ctx, KVSMC_ERR_INVALID_ARGUMENT, "cells: empty or null volume arrays");
+    // the mappers hold node ids in int and loop cells with a UInt32 counter
+    if (nnodes > 0x7fffffffull || ncells > 0xffffffffull)
+        return fail(ctx, KVSMC_ERR_TOO_LARGE, "cells: %llu nodes / %llu cells beyond the 32-bit ids",
+                    (unsigned long long)nnodes, (unsigned long long)ncells);
+    return KVSMC_OK;
+}
+
+// Min/max (when not given), the Math::Equal early exit, count and scan for a
+// job whose inputs are on the device.  *go is false when nothing is to be
+// emitted; sizes holds the counts.  Uses the context's scratch and d_flag.
+kvsmc_status cells_count(kvsmc_context* ctx, kvsmc::CellJob& j, int32_t has_minmax, double min_value,
+                         double max_value, kvsmc_sizes* sizes, bool* go)
+{
+    using namespace kvsmc_host;
+    *go = false;
+    if (!ctx->d_flag) KVSMC_CUDA(ctx, cudaMalloc(&ctx->d_flag, sizeof(int)));
+    j.bad_index = ctx->d_flag;
+    KVSMC_CUDA(ctx, cudaMemsetAsync(ctx->d_flag, 0, sizeof(int), ctx->stream));
+    const uint64_t tiles = kvsmc::cells_tiles(j.ncells);
+    const size_t bc = align_up(tiles * 4, 256), bo = align_up(tiles * 8, 256),
+                 bs = align_up(std::max(std::max(kvsmc::scan_scratch_bytes(tiles),
+                                                 kvsmc::cells_minmax_scratch_bytes(ctx->num_sms)),
+                                        kvsmc::minmax_scratch_bytes(ctx->num_sms)), 256);
+    kvsmc_status st = ensure_scratch(ctx, bc + bo + bs + 256);
+    if (st) return st;
+    char* base = static_cast<char*>(ctx->scratch);
+    j.tile_counts = reinterpret_cast<uint32_t*>(base);
+    j.tile_offsets = reinterpret_cast<uint64_t*>(base + bc);
+    void* d_scan = base + bc + bo;
+    uint64_t* d_tail = reinterpret_cast<uint64_t*>(base + bc + bo + bs);   // total, or min/max as doubles
+    const kvsmc::Launch L = launch_of(ctx);
+    auto read_bad = [&]() {
+        int bad = 0;
+        std::memcpy(&bad, ctx->h_small + 2, sizeof(int));
+        return bad;
+    };
+
+    // MapperBase::setRange: the volume's min/max, computed when not set
+    double vmin = min_value, vmax = max_value;
+    if (!has_minmax) {
+        if (j.ncells) {
+            KVSMC_CUDA(ctx, kvsmc::launch_cells_minmax(j, d_scan, reinterpret_cast<double*>(d_tail), L));
+        } else {
+            // no connections: the scan runs over the nodes (UnstructuredVolumeObject.cpp:88-102)
+            kvsmc::VolumeView v1;
+            std::memset(&v1, 0, sizeof v1);
+            v1.data = j.values;
+            v1.dtype = j.dtype;
+            v1.nx = (uint32_t)j.nnodes;
+            v1.ny = v1.nz = 1;
+            v1.pitch = v1.slice = j.nnodes;
+            KVSMC_CUDA(ctx, kvsmc::launch_minmax(v1, d_scan, reinterpret_cast<double*>(d_tail), L));
+        }
+        KVSMC_CUDA(ctx, cudaMemcpyAsync(ctx->h_small, d_tail, 2 * sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
+        KVSMC_CUDA(ctx, cudaMemcpyAsync(ctx->h_small + 2, ctx->d_flag, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
+        KVSMC_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+        std::memcpy(&vmin, ctx->h_small, sizeof(double));
+        std::memcpy(&vmax, ctx->h_small + 1, sizeof(double));
+        if (read_bad()) return fail(ctx, KVSMC_ERR_INVALID_ARGUMENT, "cells: a connection index is >= nnodes");
+    }
+    sizes->min_value = vmin;
+    sizes->max_value = vmax;
+    if (equal_abs(vmin, vmax)) return KVSMC_OK;   // MarchingTetrahedra.cpp:118-119
+    sizes->extracted = 1;
+    if (j.ncells == 0) return KVSMC_OK;
+    j.vmin = vmin;
+    j.vmax = vmax;
+    j.f = make_fast(j.iso, vmin, vmax, j.dtype);
+    KVSMC_CUDA(ctx, kvsmc::launch_cells_count(j, L));
+    KVSMC_CUDA(ctx, kvsmc::launch_scan(j.tile_counts, j.tile_offsets, tiles, d_scan, d_tail, L));
+    KVSMC_CUDA(ctx, cudaMemcpyAsync(ctx->h_small, d_tail, sizeof(uint64_t), cudaMemcpyDeviceToHost, ctx->stream));
+    KVSMC_CUDA(ctx, cudaMemcpyAsync(ctx->h_small + 2, ctx->d_flag, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
+    KVSMC_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    if (read_bad()) return fail(ctx, KVSMC_ERR_INVALID_ARGUMENT, "cells: a connection index is >= nnodes");
+    const uint64_t t = ctx->h_small[0];
+    sizes->ntriangles = t;
+    sizes->nvertices = 3 * t;
+    sizes->ncoords = 9 * t;
+    sizes->nnormals = 3 * t;
+    *go = t > 0;
+    return KVSMC_OK;
+}
+
+kvsmc::CellJob make_job(int cell_type, int dtype, const void* values, uint64_t nnodes, const float* coords,
+                        const uint32_t* conn, uint64_t ncells, double isolevel)
+{
+    kvsmc::CellJob j;
+    std::memset(&j, 0, sizeof j);
+    j.cell_type = cell_type;
+    j.dtype = dtype;
+    j.values = values;
+    j.nnodes = nnodes;
+    j.coords = coords;
+    j.conn = conn;
+    j.ncells = ncells;
+    j.iso = isolevel;
+    j.cls = kvsmc_host::make_classifier(isolevel);
+    j.conn_vec16 = (reinterpret_cast<uintptr_t>(conn) & 15u) == 0;
+    return j;
+}
+
 }  // namespace
 
 extern "C" {
+
+kvsmc_status kvsmc_marching_cells_device(kvsmc_context* ctx, kvsmc_cell_type cell_type, const void* values,
+                                         kvsmc_dtype dtype, uint64_t nnodes, const float* coords,
+                                         const uint32_t* connections, uint64_t ncells, double isolevel,
+                                         int32_t has_minmax, double min_value, double max_value, float* out_coords,
+                                         uint64_t coords_capacity, float* out_normals, uint64_t normals_capacity,
+                                         kvsmc_sizes* sizes)
+{
+    using namespace kvsmc_host;
+    if (!ctx || !sizes) return KVSMC_ERR_INVALID_ARGUMENT;
+    std::memset(sizes, 0, sizeof *sizes);
+    kvsmc_status st = check_args(ctx, cell_type, dtype, nnodes, values, coords, connections, ncells);
+    if (st) return st;
+    KVSMC_CUDA(ctx, cudaSetDevice(ctx->device));
+    kvsmc::CellJob j = make_job(cell_type, dtype, values, nnodes, coords, connections, ncells, isolevel);
+    bool go = false;
+    if ((st = cells_count(ctx, j, has_minmax, min_value, max_value, sizes, &go)) || !go) return st;
+    const uint64_t t = sizes->ntriangles;
+    if (!out_coords || !out_normals || coords_capacity < 9 * t || normals_capacity < 3 * t)
+        return fail(ctx, KVSMC_ERR_CAPACITY, "cells: %llu triangles do not fit the outputs", (unsigned long long)t);
+    j.out_coords = out_coords;
+    j.out_normals = out_normals;
+    j.cap_tris = t;
+    KVSMC_CUDA(ctx, kvsmc::launch_cells_emit(j, launch_of(ctx)));
+    return KVSMC_OK;
+}
 
 kvsmc_status kvsmc_marching_cells_host(kvsmc_context* ctx, kvsmc_cell_type cell_type, const void* values,
                                        kvsmc_dtype dtype, uint64_t nnodes, const float* coords,
@@ -401,134 +586,49 @@ kvsmc_status kvsmc_marching_cells_host(kvsmc_context* ctx, kvsmc_cell_type cell_
     using namespace kvsmc_host;
     if (!ctx || !alloc || !sizes) return KVSMC_ERR_INVALID_ARGUMENT;
     std::memset(sizes, 0, sizeof *sizes);
-    const int npc = nodes_per_cell(cell_type);
-    if (npc == 0) return fail(ctx, KVSMC_ERR_INVALID_ARGUMENT, "cells: unknown cell type %d", (int)cell_type);
-    if (kvsmc::dtype_size(dtype) == 0) return fail(ctx, KVSMC_ERR_UNSUPPORTED_DTYPE, "cells: data type %d", (int)dtype);
-    if (nnodes == 0 || !values || !coords || (ncells && !connections))
-        return fail(ctx, KVSMC_ERR_INVALID_ARGUMENT, "cells: empty or null volume arrays");
-    // the mappers hold node ids in int and loop cells with a UInt32 counter
-    if (nnodes > 0x7fffffffull || ncells > 0xffffffffull)
-        return fail(ctx, KVSMC_ERR_TOO_LARGE, "cells: %llu nodes / %llu cells beyond the 32-bit ids",
-                    (unsigned long long)nnodes, (unsigned long long)ncells);
+    kvsmc_status st = check_args(ctx, cell_type, dtype, nnodes, values, coords, connections, ncells);
+    if (st) return st;
     KVSMC_CUDA(ctx, cudaSetDevice(ctx->device));
+    const int npc = nodes_per_cell(cell_type);
     const size_t es = kvsmc::dtype_size(dtype);
-    void* d_values = nullptr;
-    float* d_coords = nullptr;
-    uint32_t* d_conn = nullptr;
+    // inputs and outputs in one device allocation: values | coords | connections | outputs
+    const size_t bv = align_up(nnodes * es, 256), bx = align_up(nnodes * 12, 256),
+                 bk = align_up(std::max<uint64_t>(1, ncells * npc) * 4, 256);
+    char* d_in = nullptr;
     float* d_out = nullptr;
-    int* d_bad = nullptr;
     auto done = [&](kvsmc_status s) {
         cudaStreamSynchronize(ctx->stream);
-        cudaFree(d_values);
-        cudaFree(d_coords);
-        cudaFree(d_conn);
+        cudaFree(d_in);
         cudaFree(d_out);
-        cudaFree(d_bad);
         return s;
     };
-    auto cuda_fail = [&](cudaError_t e) {
-        return done(fail(ctx, e == cudaErrorMemoryAllocation ? KVSMC_ERR_OUT_OF_MEMORY : KVSMC_ERR_CUDA, "cells: %s",
-                         cudaGetErrorString(e)));
-    };
-    cudaError_t e = cudaMalloc(&d_values, nnodes * es);
-    if (e == cudaSuccess) e = cudaMalloc(&d_coords, nnodes * 3 * sizeof(float));
-    if (e == cudaSuccess) e = cudaMalloc(&d_conn, (ncells ? ncells * npc : 1) * sizeof(uint32_t));
-    if (e == cudaSuccess) e = cudaMalloc(&d_bad, sizeof(int));
-    if (e == cudaSuccess) e = cudaMemcpyAsync(d_values, values, nnodes * es, cudaMemcpyHostToDevice, ctx->stream);
-    if (e == cudaSuccess)
-        e = cudaMemcpyAsync(d_coords, coords, nnodes * 3 * sizeof(float), cudaMemcpyHostToDevice, ctx->stream);
+    cudaError_t e = cudaMalloc(&d_in, bv + bx + bk);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(d_in, values, nnodes * es, cudaMemcpyHostToDevice, ctx->stream);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(d_in + bv, coords, nnodes * 12, cudaMemcpyHostToDevice, ctx->stream);
     if (e == cudaSuccess && ncells)
-        e = cudaMemcpyAsync(d_conn, connections, ncells * npc * sizeof(uint32_t), cudaMemcpyHostToDevice, ctx->stream);
-    if (e == cudaSuccess) e = cudaMemsetAsync(d_bad, 0, sizeof(int), ctx->stream);
-    if (e != cudaSuccess) return cuda_fail(e);
-
-    kvsmc::CellJob j;
-    std::memset(&j, 0, sizeof j);
-    j.cell_type = cell_type;
-    j.dtype = dtype;
-    j.values = d_values;
-    j.nnodes = nnodes;
-    j.coords = d_coords;
-    j.conn = d_conn;
-    j.ncells = ncells;
-    j.iso = isolevel;
-    j.bad_index = d_bad;
-    const uint64_t tiles = kvsmc::cells_tiles(ncells);
-    const size_t bc = align_up(tiles * 4, 256), bo = align_up(tiles * 8, 256),
-                 bs = align_up(std::max(kvsmc::scan_scratch_bytes(tiles), kvsmc::cells_minmax_scratch_bytes(ctx->num_sms)), 256);
-    kvsmc_status st = ensure_scratch(ctx, bc + bo + bs + 256);
-    if (st) return done(st);
-    char* base = static_cast<char*>(ctx->scratch);
-    j.tile_counts = reinterpret_cast<uint32_t*>(base);
-    j.tile_offsets = reinterpret_cast<uint64_t*>(base + bc);
-    void* d_scan = base + bc + bo;
-    uint64_t* d_tail = reinterpret_cast<uint64_t*>(base + bc + bo + bs);   // total, or min/max as doubles
-    const kvsmc::Launch L = launch_of(ctx);
-
-    // MapperBase::setRange: the volume's min/max, computed when not set
-    double vmin = min_value, vmax = max_value;
-    if (!has_minmax) {
-        if (ncells) {
-            e = kvsmc::launch_cells_minmax(j, d_scan, reinterpret_cast<double*>(d_tail), L);
-        } else {
-            // no connections: the scan runs over the nodes (UnstructuredVolumeObject.cpp:88-102)
-            kvsmc::VolumeView v1;
-            std::memset(&v1, 0, sizeof v1);
-            v1.data = d_values;
-            v1.dtype = dtype;
-            v1.nx = (uint32_t)nnodes;
-            v1.ny = v1.nz = 1;
-            v1.pitch = nnodes;
-            v1.slice = nnodes;
-            const size_t need = kvsmc::minmax_scratch_bytes(ctx->num_sms);
-            if (need > bs) return done(fail(ctx, KVSMC_ERR_CUDA, "cells: min/max scratch"));
-            e = kvsmc::launch_minmax(v1, d_scan, reinterpret_cast<double*>(d_tail), L);
-        }
-        if (e == cudaSuccess) e = cudaMemcpyAsync(ctx->h_small, d_tail, 2 * sizeof(double), cudaMemcpyDeviceToHost, ctx->stream);
-        if (e == cudaSuccess) e = cudaMemcpyAsync(ctx->h_small + 2, d_bad, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream);
-        if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
-        if (e != cudaSuccess) return cuda_fail(e);
-        std::memcpy(&vmin, ctx->h_small, sizeof(double));
-        std::memcpy(&vmax, ctx->h_small + 1, sizeof(double));
-        int bad = 0;
-        std::memcpy(&bad, ctx->h_small + 2, sizeof(int));
-        if (bad) return done(fail(ctx, KVSMC_ERR_INVALID_ARGUMENT, "cells: a connection index is >= nnodes"));
-    }
-    sizes->min_value = vmin;
-    sizes->max_value = vmax;
-    if (equal_abs(vmin, vmax)) return done(KVSMC_OK);   // MarchingTetrahedra.cpp:118-119
-    sizes->extracted = 1;
-    if (ncells == 0) return done(KVSMC_OK);
-    j.vmin = vmin;
-    j.vmax = vmax;
-
-    e = kvsmc::launch_cells_count(j, L);
-    if (e == cudaSuccess) e = kvsmc::launch_scan(j.tile_counts, j.tile_offsets, tiles, d_scan, d_tail, L);
-    if (e == cudaSuccess) e = cudaMemcpyAsync(ctx->h_small, d_tail, sizeof(uint64_t), cudaMemcpyDeviceToHost, ctx->stream);
-    if (e == cudaSuccess) e = cudaMemcpyAsync(ctx->h_small + 1, d_bad, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream);
-    if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
-    if (e != cudaSuccess) return cuda_fail(e);
-    int bad = 0;
-    std::memcpy(&bad, ctx->h_small + 1, sizeof(int));
-    if (bad) return done(fail(ctx, KVSMC_ERR_INVALID_ARGUMENT, "cells: a connection index is >= nnodes"));
-    const uint64_t t = ctx->h_small[0];
-    sizes->ntriangles = t;
-    sizes->nvertices = 3 * t;
-    sizes->ncoords = 9 * t;
-    sizes->nnormals = 3 * t;
-    if (t == 0) return done(KVSMC_OK);
-    if ((e = cudaMalloc(&d_out, t * 12 * sizeof(float))) != cudaSuccess) return cuda_fail(e);
+        e = cudaMemcpyAsync(d_in + bv + bx, connections, ncells * npc * 4, cudaMemcpyHostToDevice, ctx->stream);
+    if (e != cudaSuccess)
+        return done(fail(ctx, e == cudaErrorMemoryAllocation ? KVSMC_ERR_OUT_OF_MEMORY : KVSMC_ERR_CUDA,
+                         "cells: %s", cudaGetErrorString(e)));
+    kvsmc::CellJob j = make_job(cell_type, dtype, d_in, nnodes, reinterpret_cast<const float*>(d_in + bv),
+                                reinterpret_cast<const uint32_t*>(d_in + bv + bx), ncells, isolevel);
+    bool go = false;
+    if ((st = cells_count(ctx, j, has_minmax, min_value, max_value, sizes, &go)) || !go) return done(st);
+    const uint64_t t = sizes->ntriangles;
+    if ((e = cudaMalloc(&d_out, t * 12 * sizeof(float))) != cudaSuccess)
+        return done(fail(ctx, KVSMC_ERR_OUT_OF_MEMORY, "cells: %s", cudaGetErrorString(e)));
     j.out_coords = d_out;
     j.out_normals = d_out + 9 * t;
     j.cap_tris = t;
-    if ((e = kvsmc::launch_cells_emit(j, L)) != cudaSuccess) return cuda_fail(e);
+    if ((e = kvsmc::launch_cells_emit(j, launch_of(ctx))) != cudaSuccess)
+        return done(fail(ctx, KVSMC_ERR_CUDA, "cells: %s", cudaGetErrorString(e)));
     void* hc = alloc(user, 0, 9 * t);
     void* hn = hc ? alloc(user, 1, 3 * t) : nullptr;
     if (!hc || !hn) return done(fail(ctx, KVSMC_ERR_OUT_OF_MEMORY, "cells: host alloc"));
     e = cudaMemcpyAsync(hc, d_out, t * 9 * sizeof(float), cudaMemcpyDeviceToHost, ctx->stream);
     if (e == cudaSuccess) e = cudaMemcpyAsync(hn, d_out + 9 * t, t * 3 * sizeof(float), cudaMemcpyDeviceToHost, ctx->stream);
     if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
-    if (e != cudaSuccess) return cuda_fail(e);
+    if (e != cudaSuccess) return done(fail(ctx, KVSMC_ERR_CUDA, "cells: %s", cudaGetErrorString(e)));
     return done(KVSMC_OK);
 }
 

@@ -141,7 +141,10 @@ struct CellJob {
     const uint32_t* conn;     // nodes-per-cell x ncells
     uint64_t ncells;
     double iso, vmin, vmax;
-    uint32_t* tile_counts;    // per 256-cell tile
+    Classifier cls;           // exact thresholds of the isolevel (no FP64 for float / 32-bit values)
+    FastIso f;                // constants of the FP32 vertex certificate (emit pass)
+    int32_t conn_vec16;       // connections 16-byte aligned: vector loads for tetrahedra / hexahedra
+    uint32_t* tile_counts;    // per 32-cell group
     uint64_t* tile_offsets;
     float* out_coords;        // 9 T
     float* out_normals;       // 3 T
@@ -164,5 +167,6 @@ cudaError_t launch_stl_records(const float* coords, const float* normals, const 
 
 // ---- diagnostics (selftest.cu)
 cudaError_t launch_selftest(uint64_t n, uint64_t seed, unsigned long long* d_counters, const Launch& L);
+cudaError_t launch_selftest_cells(uint64_t n, uint64_t seed, unsigned long long* d_counters, const Launch& L);
 
 }  // namespace kvsmc

@@ -268,4 +268,96 @@ __device__ __forceinline__ float3 edge_vertex_fast(const Interp& j, const FastIs
     return interpolate_exact_slow(j, va, vb, ax, ay, az, bx, by, bz);
 }
 
+// ------------------------------------------------------------------ cells
+//
+// The unstructured mappers' vertex (interpolate_vertex, e.g.
+// MarchingTetrahedra.cpp:325-346) on arbitrary float endpoints c0, c1:
+//     r = |RN64(RN64(iso - v0) / RN64(v1 - v0))|,  d = RN32(c1 - c0)
+//     X = RN64(c0 + RN64(r * d)),  F = RN32(X)
+// With R = (iso - v0) / (v1 - v0) exactly and |R| <= 1.5:
+//     |X - (c0 + d |R|)| <= 2^-53 (|c0| + 8 |d|) <= 2^-50 (|c0| + |d|)   (E_D)
+// (three roundings in r, one in r d, one in the sum).  The FP32 path forms
+// r = q1 + q2 as fast_axis does (|r - |R|| <= EQ = 2^-40 |q1| + err_num/|den|),
+// d r1 exactly by FMA, d r2 and two additions rounded (2^-23 of each), and
+// Y = yh + yl by TwoSum: |Y - (c0 + d |R|)| <= |d| EQ + 2^-23 (|p2| + |t1| + |t|).
+// If no float rounding boundary lies within E = (E_Y + E_D) 1.001 of Y, F = yh.
+
+// The ratio part shared by the three axes of one vertex.
+struct CellRatio {
+    float r1, r2;   // |R| ~ r1 + r2
+    float eq;       // bound of |r1 + r2 - |R||
+    int ok;         // the FP32 path may be used (denominator in range, |R| <= 1.5)
+    int zero;       // iso == v0 exactly: R = 0
+};
+
+__device__ __forceinline__ CellRatio cell_ratio(float v0, float v1, const FastIso& f)
+{
+    CellRatio c;
+    float s, e;
+    two_sum(f.ih, -v0, s, e);
+    const float e2 = __fadd_rn(e, f.il);
+    float nh, nl;
+    two_sum(s, e2, nh, nl);
+    const float err_num = __fadd_rn(f.iso_err, __fmul_rn(fabsf(e2), 1.1920929e-07f));
+    float dh, dl;
+    two_sum(v1, -v0, dh, dl);
+    const float adh = fabsf(dh);
+    const bool den_ok = adh >= 8.67361738e-19f && adh <= 1.15292150e+18f;   // 2^-60 .. 2^60
+    float inv;
+    asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(inv) : "f"(dh));
+    const float q1 = __fmul_rn(nh, inv);
+    const float p = __fmul_rn(q1, dh);
+    const float pe = __fmaf_rn(q1, dh, -p);
+    const float p2 = __fmul_rn(q1, dl);
+    const float pe2 = __fmaf_rn(q1, dl, -p2);
+    const float rho = __fsub_rn(__fadd_rn(__fsub_rn(__fsub_rn(nh, p), pe), __fsub_rn(nl, p2)), pe2);
+    const float q2 = __fmul_rn(rho, inv);
+    const float aq = fabsf(q1);
+    const bool neg = q1 < 0.0f;
+    c.r1 = neg ? -q1 : q1;
+    c.r2 = neg ? -q2 : q2;
+    c.eq = __fmul_rn(__fadd_rn(__fmul_rn(aq, 9.09494702e-13f), __fmul_rn(__fmul_rn(err_num, fabsf(inv)), 1.0001f)),
+                     1.001f);
+    c.zero = nh == 0.0f && nl == 0.0f && f.iso_err == 0.0f;
+    c.ok = f.fast_ok && den_ok && aq <= 1.5f;
+    return c;
+}
+
+// F for one axis, or false when the FP32 path cannot decide.
+__device__ __forceinline__ bool cell_axis(const CellRatio& c, float c0, float c1, float& out)
+{
+    const float d = __fsub_rn(c1, c0);
+    const float ad = fabsf(d), ac = fabsf(c0);
+    const bool in_range = ad <= 1.26765060e+30f && ac <= 1.26765060e+30f;   // 2^100
+    const bool pos_zero = __float_as_uint(c0) == 0u;   // c0 = +0: +0 + (+-0) = +0
+    if (c.zero) {
+        // r = +-0: X = c0 + (+-0) = c0, except for c0 = -0
+        out = c0;
+        return c.ok && in_range && (c0 != 0.0f || pos_zero);
+    }
+    if (d == 0.0f && pos_zero) {
+        // r finite: r d = +-0 and X = +0
+        out = 0.0f;
+        return c.ok && in_range;
+    }
+    const float p1 = __fmul_rn(d, c.r1);
+    const float pe1 = __fmaf_rn(d, c.r1, -p1);
+    const float p2 = __fmul_rn(d, c.r2);
+    float s, e;
+    two_sum(c0, p1, s, e);
+    const float t1 = __fadd_rn(e, pe1);
+    const float t = __fadd_rn(t1, p2);
+    float yh, yl;
+    two_sum(s, t, yh, yl);
+    float E = __fmul_rn(ad, c.eq);
+    E = __fadd_rn(E, __fmul_rn(__fadd_rn(__fadd_rn(fabsf(p2), fabsf(t1)), fabsf(t)), 1.1920929e-07f));  // 2^-23
+    E = __fadd_rn(E, __fmul_rn(__fadd_rn(ac, ad), 8.8817842e-16f));                                       // 2^-50
+    E = __fmul_rn(E, 1.001f);
+    const float ay = fabsf(yh);
+    const bool y_ok = ay >= 7.88860905e-31f && ay <= 1.26765060e+30f;   // 2^-100 .. 2^100
+    const float dist = yh > 0.0f ? rounding_margin(yh, yl) : rounding_margin(-yh, -yl);
+    out = yh;
+    return c.ok && in_range && y_ok && dist > E;
+}
+
 }  // namespace kvsmc

@@ -9,23 +9,23 @@
  *  imply shared vertices; exec (:104-124) checks the input; mapping
  *  (:132-258) builds the per-grid mapper and shallow-copies its arrays.
  *  What changes: the structured branch's mapper is kvs::cuda::MarchingCubes,
- *  the min/max scan behind the default isolevel runs on the GPU, and a GPU
- *  failure is reported and ends exec with nullptr instead of leaving empty
- *  arrays behind.  As in the reference, this mapper never sets isSuccess()
+ *  the unstructured branch's are kvs::cuda::MarchingTetrahedra / Hexahedra /
+ *  Pyramid / Prism, the min/max scan behind the default isolevel runs on the
+ *  GPU, and a GPU failure is reported and ends exec with nullptr instead of
+ *  leaving empty arrays behind.  As in the reference, this mapper never sets isSuccess()
  *  true (MapperBase's initial false, MapperBase.cpp:23).
  */
 /*****************************************************************************/
 #include "Isosurface.h"
 
-#include <kvs/MarchingHexahedra>
-#include <kvs/MarchingPrism>
-#include <kvs/MarchingPyramid>
-#include <kvs/MarchingTetrahedra>
 #include <kvs/Message>
 #include <kvs/StructuredVolumeObject>
 #include <kvs/UnstructuredVolumeObject>
 
+#include <limits>
+
 #include "Context.h"
+#include "MarchingCells.h"
 #include "MarchingCubes.h"
 
 namespace
@@ -60,6 +60,48 @@ bool DeviceMinMax( const kvs::StructuredVolumeObject* volume, int device )
     return true;
 }
 
+// UnstructuredVolumeObject::updateMinMaxValues (UnstructuredVolumeObject.cpp:469-487)
+// by the device scan over values[0] and the cells' nodes: a marching call at
+// isolevel NaN, where no node is above, so only the scan and an empty count
+// pass run.
+bool DeviceMinMax( const kvs::UnstructuredVolumeObject* volume, int device )
+{
+    int cell = -1;
+    switch ( volume->cellType() )
+    {
+    case kvs::UnstructuredVolumeObject::Tetrahedra: cell = KVSMC_TETRAHEDRA; break;
+    case kvs::UnstructuredVolumeObject::Hexahedra: cell = KVSMC_HEXAHEDRA; break;
+    case kvs::UnstructuredVolumeObject::Pyramid: cell = KVSMC_PYRAMID; break;
+    case kvs::UnstructuredVolumeObject::Prism: cell = KVSMC_PRISM; break;
+    default: break;
+    }
+    const int dtype = kvs::cuda::DType( volume->values() );
+    if ( cell < 0 || dtype < 0 || volume->veclen() != 1 )
+    {
+        volume->updateMinMaxValues();   // what no marching mapper takes: the reference's own scan
+        return true;
+    }
+    kvsmc_status st = KVSMC_OK;
+    kvsmc_context* ctx = kvs::cuda::DeviceContext( device, &st );
+    if ( !ctx )
+    {
+        kvsMessageError("libkvsmc: %s.", kvsmc_status_string( st ) );
+        return false;
+    }
+    kvsmc_sizes sizes{};
+    st = kvsmc_marching_cells_host( ctx, kvsmc_cell_type( cell ), volume->values().data(), kvsmc_dtype( dtype ),
+                                    volume->numberOfNodes(), volume->coords().data(), volume->connections().data(),
+                                    volume->numberOfCells(), std::numeric_limits<double>::quiet_NaN(), 0, 0.0, 0.0,
+                                    []( void*, int32_t, uint64_t ) -> void* { return nullptr; }, nullptr, &sizes );
+    if ( st != KVSMC_OK )
+    {
+        kvsMessageError("libkvsmc: %s: %s", kvsmc_status_string( st ), kvsmc_last_error( ctx ) );
+        return false;
+    }
+    volume->setMinMaxValues( sizes.min_value, sizes.max_value );
+    return true;
+}
+
 } // end of namespace
 
 namespace kvs
@@ -78,8 +120,10 @@ Isosurface::Isosurface(
     if ( !volume->hasMinMaxValues() )
     {
         const auto* svolume = kvs::StructuredVolumeObject::DownCast( volume );
+        const auto* uvolume = kvs::UnstructuredVolumeObject::DownCast( volume );
         if ( svolume ) { if ( !DeviceMinMax( svolume, m_device ) ) return; }
-        else { volume->updateMinMaxValues(); }   // unstructured: the reference's own scan
+        else if ( uvolume ) { if ( !DeviceMinMax( uvolume, m_device ) ) return; }
+        else { volume->updateMinMaxValues(); }
     }
     this->setIsolevel( ( volume->maxValue() + volume->minValue() ) * 0.5 );
     if ( normal_type == kvs::PolygonObject::VertexNormal ) { m_duplication = false; }
@@ -181,30 +225,38 @@ bool Isosurface::mapping( const kvs::VolumeObjectBase* volume )
         return true;
     }
 
-    // unstructured grids: the reference's own mappers (Isosurface.cpp:193-258)
+    // unstructured grids (Isosurface.cpp:193-258)
     const auto* uvolume = kvs::UnstructuredVolumeObject::DownCast( volume );
-    kvs::PolygonObject* polygon = nullptr;
+    kvs::cuda::MarchingCellsBase* polygon = nullptr;
+    kvs::cuda::MarchingTetrahedra tet;
+    kvs::cuda::MarchingHexahedra hex;
+    kvs::cuda::MarchingPyramid pyr;
+    kvs::cuda::MarchingPrism pri;
+    kvs::PolygonObject* result = nullptr;
     switch ( uvolume->cellType() )
     {
-    case kvs::UnstructuredVolumeObject::Tetrahedra:
-        polygon = new kvs::MarchingTetrahedra( uvolume, m_isolevel, ntype, m_duplication, tfunc );
-        break;
-    case kvs::UnstructuredVolumeObject::Hexahedra:
-        polygon = new kvs::MarchingHexahedra( uvolume, m_isolevel, ntype, m_duplication, tfunc );
-        break;
-    case kvs::UnstructuredVolumeObject::Pyramid:
-        polygon = new kvs::MarchingPyramid( uvolume, m_isolevel, ntype, m_duplication, tfunc );
-        break;
-    case kvs::UnstructuredVolumeObject::Prism:
-        polygon = new kvs::MarchingPrism( uvolume, m_isolevel, ntype, m_duplication, tfunc );
-        break;
-    default: break;
+    case kvs::UnstructuredVolumeObject::Tetrahedra: polygon = &tet; break;
+    case kvs::UnstructuredVolumeObject::Hexahedra: polygon = &hex; break;
+    case kvs::UnstructuredVolumeObject::Pyramid: polygon = &pyr; break;
+    case kvs::UnstructuredVolumeObject::Prism: polygon = &pri; break;
+    default: return true;   // no mapper: empty arrays, as in the reference
     }
-    if ( polygon )
+    polygon->setDevice( m_device );
+    polygon->setNormalType( ntype );
+    polygon->setTransferFunction( tfunc );
+    polygon->setDuplication( m_duplication );
+    polygon->setIsolevel( m_isolevel );
+    if ( polygon == &tet ) result = tet.exec( uvolume );
+    else if ( polygon == &hex ) result = hex.exec( uvolume );
+    else if ( polygon == &pyr ) result = pyr.exec( uvolume );
+    else result = pri.exec( uvolume );
+    if ( !result )
     {
-        this->shallowCopy( polygon );
-        delete polygon;
+        BaseClass::setSuccess( false );
+        kvsMessageError("Cannot create isosurfaces.");
+        return false;
     }
+    this->shallowCopy( polygon );
     return true;
 }
 

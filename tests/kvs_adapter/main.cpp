@@ -8,6 +8,8 @@
 #include "kvs/cuda/MarchingCubes.h"
 #include "kvs/cuda/Isosurface.h"
 #include "kvs/cuda/SlicePlane.h"
+#include "kvs/cuda/MarchingCells.h"
+#include <kvs/UnstructuredVolumeObject>
 
 int main()
 {
@@ -44,6 +46,27 @@ int main()
     kvs::cuda::SlicePlane sq;
     sq.setPlane( kvs::Vec3( 15.0f, 15.0f, 15.0f ), kvs::Vec3( 0.3f, -0.5f, 0.8f ) );
     std::printf( "slice exec returned=%d\n", sq.exec( volume ) ? 1 : 0 );
+    // the unstructured mappers (MarchingTetrahedra.h:23-60 and alike): one tetrahedron
+    kvs::UnstructuredVolumeObject* tv = new kvs::UnstructuredVolumeObject();
+    const kvs::Real32 tc[12] = { 0, 0, 0, 1, 0, 0, 0, 1, 0, 0, 0, 1 };
+    const kvs::UInt32 tk[4] = { 0, 1, 2, 3 };
+    const kvs::Real32 tval[4] = { 0, 1, 0, 0 };
+    tv->setCellTypeToTetrahedra();
+    tv->setVeclen( 1 );
+    tv->setNumberOfNodes( 4 );
+    tv->setNumberOfCells( 1 );
+    tv->setCoords( kvs::ValueArray<kvs::Real32>( tc, 12 ) );
+    tv->setConnections( kvs::ValueArray<kvs::UInt32>( tk, 4 ) );
+    tv->setValues( kvs::ValueArray<kvs::Real32>( tval, 4 ) );
+    kvs::cuda::MarchingTetrahedra* mt = new kvs::cuda::MarchingTetrahedra( tv, 0.5, kvs::PolygonObject::PolygonNormal, true, tf );
+    std::printf( "cells vertices=%zu module=%s\n", mt->numberOfVertices(), mt->moduleName() );
+    kvs::cuda::MarchingHexahedra mh;
+    mh.setIsolevel( 0.5 );
+    std::printf( "cells wrong type returned=%d\n", mh.exec( tv ) ? 1 : 0 );
+    kvs::cuda::Isosurface ti( tv, 0.5, kvs::PolygonObject::PolygonNormal, true, tf );
+    std::printf( "cells isosurface vertices=%zu\n", ti.numberOfVertices() );
+    delete mt;
+    delete tv;
     delete sp;
     delete s;
     delete a;

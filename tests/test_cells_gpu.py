@@ -126,3 +126,66 @@ def test_bad_connection_index_is_an_error(kvsmc_ctx):
     # the context stays usable
     c, n, s = _abi.marching_cells_host(kvsmc_ctx, 1, v, xyz, conn, 1.5)
     assert same_bits(c, ocells.marching_cells(1, v, xyz, conn, 1.5)["coords"])
+
+
+def test_device_entry_point_and_capacity(kvsmc_ctx):
+    """kvsmc_marching_cells_device on torch device arrays: the same bits as the
+    host call; too small outputs are KVSMC_ERR_CAPACITY with the sizes and
+    nothing written."""
+    import ctypes as C
+    xyz, conn = cm.grid(3, 30, 28, 26, seed=11)
+    v = cm.sphere_values(xyz, (14.2, 13.1, 12.6))
+    dv, dx, dk = (torch.from_numpy(np.ascontiguousarray(a)).cuda() for a in (v, xyz, conn.view(np.int32)))
+    torch.cuda.synchronize()
+    s = _abi.Sizes()
+    lib = kvsmc_ctx.lib
+
+    def call(oc, cap_c, on, cap_n):
+        return lib.kvsmc_marching_cells_device(kvsmc_ctx.handle, 3, dv.data_ptr(), 8, v.size, dx.data_ptr(),
+                                               dk.data_ptr(), conn.shape[0], 6.5, 0, 0.0, 0.0, oc, cap_c, on, cap_n,
+                                               C.byref(s))
+
+    assert call(None, 0, None, 0) == 6          # KVSMC_ERR_CAPACITY
+    t = s.ntriangles
+    o = ocells.marching_cells(3, v, xyz, conn, 6.5)
+    assert 9 * t == o["coords"].size > 0 and (s.min_value, s.max_value) == (o["vmin"], o["vmax"])
+    oc = torch.full((9 * t,), 7.0, device="cuda")
+    on = torch.full((3 * t,), 7.0, device="cuda")
+    torch.cuda.synchronize()
+    assert call(oc.data_ptr(), 9 * t - 1, on.data_ptr(), 3 * t) == 6
+    assert bool((oc == 7.0).all())
+    assert call(oc.data_ptr(), 9 * t, on.data_ptr(), 3 * t) == 0
+    kvsmc_ctx.synchronize()
+    assert same_bits(oc.cpu().numpy(), o["coords"]) and same_bits(on.cpu().numpy(), o["normals"])
+
+
+def test_vertex_certificate_selftest(kvsmc_ctx):
+    """The FP32 certificate of the cells' vertices never disagrees with the
+    reference's FP64 sequence on adversarial random edges (close values,
+    ratios at 0, 1/2, 1, large and tiny coordinates, coordinates crossing
+    zero, equal endpoints), and decides most of them (exact midpoints, as
+    c0 + d/2, are left to FP64 by design)."""
+    for seed in (1, 2, 3):
+        tested, mism, fall = kvsmc_ctx.selftest_cells(1 << 22, seed)
+        assert tested > (1 << 21)
+        assert mism == 0, (seed, mism)
+        assert fall < 0.12 * tested, (seed, fall, tested)
+
+
+def test_fast_and_exact_vertices_agree_on_adversarial_meshes(kvsmc_ctx):
+    """Meshes built to land vertices near float rounding boundaries: integer
+    values with isolevels at k + 1/2 (ratios 1/2) on power-of-two coordinates,
+    and a preset min/max that clamps values."""
+    rng = np.random.default_rng(17)
+    for ct in range(4):
+        xyz, conn = cm.grid(ct, 24, 20, 18, jitter=0.0, seed=ct)
+        xyz = (xyz * np.float32(0.125) + np.float32(1024.0)).astype(np.float32)
+        for dt, iso in ((np.uint8, 100.5), (np.int16, -3.5), (np.float32, 0.5)):
+            v = rng.integers(0, 200, xyz.shape[0]).astype(dt) if dt is np.uint8 else (
+                rng.integers(-10, 10, xyz.shape[0]).astype(dt) if dt is np.int16
+                else (rng.integers(0, 2, xyz.shape[0]).astype(np.float32)))
+            for mm in (None, (float(v.min()) + 1, float(v.max()) - 1)):
+                c, n, s = _abi.marching_cells_host(kvsmc_ctx, ct, v, xyz, conn, iso, mm)
+                o = ocells.marching_cells(ct, v, xyz, conn, iso, mm)
+                assert same_bits(c, o["coords"]), (ct, dt, mm, first_diff(c, o["coords"]))
+                assert same_bits(n, o["normals"]), (ct, dt, mm)

@@ -43,4 +43,8 @@ def test_adapter_builds_and_fails_loudly_without_gpu(tmp_path):
     assert "Cannot create isosurfaces." in r.stdout + r.stderr
     assert "slice vertices=0 module=kvs::cuda::SlicePlane" in r.stdout
     assert "slice exec returned=0" in r.stdout
+    assert "cells vertices=0 module=kvs::cuda::MarchingTetrahedra" in r.stdout
+    assert "cells wrong type returned=0" in r.stdout
+    assert "Input volume is not hexhedra-cell data." in r.stdout + r.stderr
+    assert "cells isosurface vertices=0" in r.stdout
     assert "no CUDA device" in r.stdout + r.stderr
