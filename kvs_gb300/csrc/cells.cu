@@ -206,15 +206,20 @@ __global__ void __launch_bounds__(kCellThreads) k_cells_count(CellJob j)
     const unsigned lane = threadIdx.x & 31u;
     const uint64_t warps = (uint64_t)gridDim.x * (kCellThreads / 32);
     const uint64_t groups = (j.ncells + 31) / 32;
-    for (uint64_t g = (uint64_t)blockIdx.x * (kCellThreads / 32) + (threadIdx.x >> 5); g < groups; g += warps) {
-        const uint64_t cell = g * 32 + lane;
-        uint32_t n = 0;
-        if (cell < j.ncells) {
-            uint32_t nodes[Tr::kNodes];
-            n = Tr::ntri(cell_case<CT, T>(j, cell, nodes));
+    // two groups per step (their loads in flight together)
+    for (uint64_t g = ((uint64_t)blockIdx.x * (kCellThreads / 32) + (threadIdx.x >> 5)) * 2; g < groups;
+         g += warps * 2) {
+        const uint64_t ca = g * 32 + lane, cb = ca + 32;
+        uint32_t na = 0, nb = 0;
+        uint32_t nodes_a[Tr::kNodes], nodes_b[Tr::kNodes];
+        if (ca < j.ncells) na = Tr::ntri(cell_case<CT, T>(j, ca, nodes_a));
+        if (cb < j.ncells) nb = Tr::ntri(cell_case<CT, T>(j, cb, nodes_b));
+        const uint32_t ta = __reduce_add_sync(0xffffffffu, na);
+        const uint32_t tb = __reduce_add_sync(0xffffffffu, nb);
+        if (lane == 0) {
+            j.tile_counts[g] = ta;
+            if (g + 1 < groups) j.tile_counts[g + 1] = tb;
         }
-        const uint32_t t = __reduce_add_sync(0xffffffffu, n);
-        if (lane == 0) j.tile_counts[g] = t;
     }
 }
 
@@ -222,13 +227,22 @@ template <int CT, typename T>
 __global__ void __launch_bounds__(kCellThreads) k_cells_emit(CellJob j)
 {
     using Tr = CellTraits<CT>;
+    // launched before the host knows the total: nothing is written unless all fits
+    if (j.d_total && *j.d_total > j.cap_tris) return;
     const unsigned lane = threadIdx.x & 31u;
     const uint64_t warps = (uint64_t)gridDim.x * (kCellThreads / 32);
     const uint64_t groups = (j.ncells + 31) / 32;
-    for (uint64_t g = (uint64_t)blockIdx.x * (kCellThreads / 32) + (threadIdx.x >> 5); g < groups; g += warps) {
-        if (j.tile_counts[g] == 0) continue;   // warp-uniform: no triangle in these 32 cells
+    // a warp takes 32 groups at a time: one coalesced read of their counts,
+    // then only the groups with triangles (ballot)
+    for (uint64_t g0 = ((uint64_t)blockIdx.x * (kCellThreads / 32) + (threadIdx.x >> 5)) * 32; g0 < groups;
+         g0 += warps * 32) {
+        const uint64_t mine = g0 + lane;
+        unsigned todo = __ballot_sync(0xffffffffu, mine < groups && j.tile_counts[mine] != 0);
+        while (todo) {
+        const uint64_t g = g0 + (unsigned)(__ffs(todo) - 1);
+        todo &= todo - 1;
         const uint64_t cell = g * 32 + lane;
-        uint32_t nodes[Tr::kNodes];
+        uint32_t nodes[Tr::kNodes] = {};
         unsigned c = 0;
         uint32_t n = 0;
         if (cell < j.ncells) {
@@ -241,15 +255,35 @@ __global__ void __launch_bounds__(kCellThreads) k_cells_emit(CellJob j)
             const uint32_t y = __shfl_up_sync(0xffffffffu, inc, o);
             if (lane >= (unsigned)o) inc += y;
         }
-        uint64_t t = j.tile_offsets[g] + (inc - n);
-        uint64_t pk = Tr::tri(c);
-        for (uint32_t k = 0; k < n; ++k, ++t, pk >>= 12) {
-            if (t >= j.cap_tris) break;   // never past the outputs
+        // the group's triangles spread over the lanes: lane l builds triangles
+        // l, l + 32, ... of the group; its cell is the first lane whose
+        // inclusive count exceeds the index (a 5-step search over shuffles)
+        const uint32_t total = __shfl_sync(0xffffffffu, inc, 31);
+        const uint64_t base = j.tile_offsets[g];
+        for (uint32_t first = 0; first < total; first += 32) {   // warp-uniform: every lane shuffles
+            const uint32_t tri = first + lane;
+            unsigned lo = 0;
+#pragma unroll
+            for (unsigned step = 16; step > 0; step >>= 1) {
+                const uint32_t probe = __shfl_sync(0xffffffffu, inc, lo + step - 1);
+                if (probe <= tri) lo += step;
+            }
+            // lo: the owning lane (inc[lo] > tri, inc[lo - 1] <= tri)
+            const uint32_t own_inc = __shfl_sync(0xffffffffu, inc, lo);
+            const uint32_t own_n = __shfl_sync(0xffffffffu, n, lo);
+            const unsigned own_c = __shfl_sync(0xffffffffu, c, lo);
+            uint32_t own_nodes[Tr::kNodes];
+#pragma unroll
+            for (int k = 0; k < Tr::kNodes; ++k) own_nodes[k] = __shfl_sync(0xffffffffu, nodes[k], lo);
+            const uint64_t t = base + tri;
+            if (tri >= total || t >= j.cap_tris) continue;   // never past the group or the outputs
+            const uint32_t k = tri - (own_inc - own_n);
+            const uint64_t pk = Tr::tri(own_c) >> (12 * k);
             float3 v[3];
 #pragma unroll
             for (int s = 0; s < 3; ++s) {
                 const unsigned ed = Tr::edge((int)((pk >> (4 * s)) & 15u));
-                v[s] = cell_vertex<T>(j, nodes[ed & 15u], nodes[ed >> 4]);
+                v[s] = cell_vertex<T>(j, own_nodes[ed & 15u], own_nodes[ed >> 4]);
             }
             float* o = j.out_coords + 9 * t;
             o[0] = v[0].x; o[1] = v[0].y; o[2] = v[0].z;
@@ -258,6 +292,7 @@ __global__ void __launch_bounds__(kCellThreads) k_cells_emit(CellJob j)
             const float3 nn = tri_normal(v[0], v[1], v[2]);
             float* q = j.out_normals + 3 * t;
             q[0] = nn.x; q[1] = nn.y; q[2] = nn.z;
+        }
         }
     }
 }
@@ -453,20 +488,23 @@ kvsmc_status check_args(kvsmc_context* ctx, int cell_type, int dtype, uint64_t n
     return KVSMC_OK;
 }
 
-// Min/max (when not given), the Math::Equal early exit, count and scan for a
-// job whose inputs are on the device.  *go is false when nothing is to be
-// emitted; sizes holds the counts.  Uses the context's scratch and d_flag.
-kvsmc_status cells_count(kvsmc_context* ctx, kvsmc::CellJob& j, int32_t has_minmax, double min_value,
-                         double max_value, kvsmc_sizes* sizes, bool* go)
+// The count pass's scratch (group counts, offsets, scan scratch, a tail for
+// the total or the min/max) in the context's arena, and the bad-index flag.
+struct CellsScratch {
+    void* d_scan;
+    uint64_t* d_tail;
+    uint64_t tiles;
+};
+
+kvsmc_status cells_prepare(kvsmc_context* ctx, kvsmc::CellJob& j, CellsScratch* sc)
 {
     using namespace kvsmc_host;
-    *go = false;
     if (!ctx->d_flag) KVSMC_CUDA(ctx, cudaMalloc(&ctx->d_flag, sizeof(int)));
     j.bad_index = ctx->d_flag;
     KVSMC_CUDA(ctx, cudaMemsetAsync(ctx->d_flag, 0, sizeof(int), ctx->stream));
-    const uint64_t tiles = kvsmc::cells_tiles(j.ncells);
-    const size_t bc = align_up(tiles * 4, 256), bo = align_up(tiles * 8, 256),
-                 bs = align_up(std::max(std::max(kvsmc::scan_scratch_bytes(tiles),
+    sc->tiles = kvsmc::cells_tiles(j.ncells);
+    const size_t bc = align_up(sc->tiles * 4, 256), bo = align_up(sc->tiles * 8, 256),
+                 bs = align_up(std::max(std::max(kvsmc::scan_scratch_bytes(sc->tiles),
                                                  kvsmc::cells_minmax_scratch_bytes(ctx->num_sms)),
                                         kvsmc::minmax_scratch_bytes(ctx->num_sms)), 256);
     kvsmc_status st = ensure_scratch(ctx, bc + bo + bs + 256);
@@ -474,20 +512,31 @@ kvsmc_status cells_count(kvsmc_context* ctx, kvsmc::CellJob& j, int32_t has_minm
     char* base = static_cast<char*>(ctx->scratch);
     j.tile_counts = reinterpret_cast<uint32_t*>(base);
     j.tile_offsets = reinterpret_cast<uint64_t*>(base + bc);
-    void* d_scan = base + bc + bo;
-    uint64_t* d_tail = reinterpret_cast<uint64_t*>(base + bc + bo + bs);   // total, or min/max as doubles
-    const kvsmc::Launch L = launch_of(ctx);
-    auto read_bad = [&]() {
-        int bad = 0;
-        std::memcpy(&bad, ctx->h_small + 2, sizeof(int));
-        return bad;
-    };
+    sc->d_scan = base + bc + bo;
+    sc->d_tail = reinterpret_cast<uint64_t*>(base + bc + bo + bs);
+    return KVSMC_OK;
+}
 
+int read_bad(kvsmc_context* ctx)
+{
+    int bad = 0;
+    std::memcpy(&bad, ctx->h_small + 2, sizeof(int));
+    return bad;
+}
+
+// Min/max (when not given) and the Math::Equal early exit.  *go is false
+// when no cell is to be visited; sizes holds the range.
+kvsmc_status cells_range(kvsmc_context* ctx, kvsmc::CellJob& j, const CellsScratch& sc, int32_t has_minmax,
+                         double min_value, double max_value, kvsmc_sizes* sizes, bool* go)
+{
+    using namespace kvsmc_host;
+    *go = false;
+    const kvsmc::Launch L = launch_of(ctx);
     // MapperBase::setRange: the volume's min/max, computed when not set
     double vmin = min_value, vmax = max_value;
     if (!has_minmax) {
         if (j.ncells) {
-            KVSMC_CUDA(ctx, kvsmc::launch_cells_minmax(j, d_scan, reinterpret_cast<double*>(d_tail), L));
+            KVSMC_CUDA(ctx, kvsmc::launch_cells_minmax(j, sc.d_scan, reinterpret_cast<double*>(sc.d_tail), L));
         } else {
             // no connections: the scan runs over the nodes (UnstructuredVolumeObject.cpp:88-102)
             kvsmc::VolumeView v1;
@@ -497,14 +546,15 @@ kvsmc_status cells_count(kvsmc_context* ctx, kvsmc::CellJob& j, int32_t has_minm
             v1.nx = (uint32_t)j.nnodes;
             v1.ny = v1.nz = 1;
             v1.pitch = v1.slice = j.nnodes;
-            KVSMC_CUDA(ctx, kvsmc::launch_minmax(v1, d_scan, reinterpret_cast<double*>(d_tail), L));
+            KVSMC_CUDA(ctx, kvsmc::launch_minmax(v1, sc.d_scan, reinterpret_cast<double*>(sc.d_tail), L));
         }
-        KVSMC_CUDA(ctx, cudaMemcpyAsync(ctx->h_small, d_tail, 2 * sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
+        KVSMC_CUDA(ctx, cudaMemcpyAsync(ctx->h_small, sc.d_tail, 2 * sizeof(double), cudaMemcpyDeviceToHost,
+                                        ctx->stream));
         KVSMC_CUDA(ctx, cudaMemcpyAsync(ctx->h_small + 2, ctx->d_flag, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
         KVSMC_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
         std::memcpy(&vmin, ctx->h_small, sizeof(double));
         std::memcpy(&vmax, ctx->h_small + 1, sizeof(double));
-        if (read_bad()) return fail(ctx, KVSMC_ERR_INVALID_ARGUMENT, "cells: a connection index is >= nnodes");
+        if (read_bad(ctx)) return fail(ctx, KVSMC_ERR_INVALID_ARGUMENT, "cells: a connection index is >= nnodes");
     }
     sizes->min_value = vmin;
     sizes->max_value = vmax;
@@ -514,18 +564,33 @@ kvsmc_status cells_count(kvsmc_context* ctx, kvsmc::CellJob& j, int32_t has_minm
     j.vmin = vmin;
     j.vmax = vmax;
     j.f = make_fast(j.iso, vmin, vmax, j.dtype);
+    *go = true;
+    return KVSMC_OK;
+}
+
+// Count and scan (total in sc.d_tail), and, when `emit` is set, the emit pass
+// right behind them with the caller's capacity, guarded on the device by the
+// total; then one read-back of the total and the flag.
+kvsmc_status cells_passes(kvsmc_context* ctx, kvsmc::CellJob& j, const CellsScratch& sc, bool emit,
+                          kvsmc_sizes* sizes)
+{
+    using namespace kvsmc_host;
+    const kvsmc::Launch L = launch_of(ctx);
     KVSMC_CUDA(ctx, kvsmc::launch_cells_count(j, L));
-    KVSMC_CUDA(ctx, kvsmc::launch_scan(j.tile_counts, j.tile_offsets, tiles, d_scan, d_tail, L));
-    KVSMC_CUDA(ctx, cudaMemcpyAsync(ctx->h_small, d_tail, sizeof(uint64_t), cudaMemcpyDeviceToHost, ctx->stream));
+    KVSMC_CUDA(ctx, kvsmc::launch_scan(j.tile_counts, j.tile_offsets, sc.tiles, sc.d_scan, sc.d_tail, L));
+    if (emit) {
+        j.d_total = sc.d_tail;
+        KVSMC_CUDA(ctx, kvsmc::launch_cells_emit(j, L));
+    }
+    KVSMC_CUDA(ctx, cudaMemcpyAsync(ctx->h_small, sc.d_tail, sizeof(uint64_t), cudaMemcpyDeviceToHost, ctx->stream));
     KVSMC_CUDA(ctx, cudaMemcpyAsync(ctx->h_small + 2, ctx->d_flag, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
     KVSMC_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
-    if (read_bad()) return fail(ctx, KVSMC_ERR_INVALID_ARGUMENT, "cells: a connection index is >= nnodes");
+    if (read_bad(ctx)) return fail(ctx, KVSMC_ERR_INVALID_ARGUMENT, "cells: a connection index is >= nnodes");
     const uint64_t t = ctx->h_small[0];
     sizes->ntriangles = t;
     sizes->nvertices = 3 * t;
     sizes->ncoords = 9 * t;
     sizes->nnormals = 3 * t;
-    *go = t > 0;
     return KVSMC_OK;
 }
 
@@ -565,15 +630,21 @@ kvsmc_status kvsmc_marching_cells_device(kvsmc_context* ctx, kvsmc_cell_type cel
     if (st) return st;
     KVSMC_CUDA(ctx, cudaSetDevice(ctx->device));
     kvsmc::CellJob j = make_job(cell_type, dtype, values, nnodes, coords, connections, ncells, isolevel);
+    CellsScratch sc;
     bool go = false;
-    if ((st = cells_count(ctx, j, has_minmax, min_value, max_value, sizes, &go)) || !go) return st;
-    const uint64_t t = sizes->ntriangles;
-    if (!out_coords || !out_normals || coords_capacity < 9 * t || normals_capacity < 3 * t)
-        return fail(ctx, KVSMC_ERR_CAPACITY, "cells: %llu triangles do not fit the outputs", (unsigned long long)t);
+    if ((st = cells_prepare(ctx, j, &sc)) || (st = cells_range(ctx, j, sc, has_minmax, min_value, max_value, sizes,
+                                                                &go)) || !go)
+        return st;
+    // emit behind the count when outputs are given (the kernel writes nothing
+    // unless the total fits them): one host round trip per call
+    const bool outs = out_coords && out_normals;
     j.out_coords = out_coords;
     j.out_normals = out_normals;
-    j.cap_tris = t;
-    KVSMC_CUDA(ctx, kvsmc::launch_cells_emit(j, launch_of(ctx)));
+    j.cap_tris = outs ? std::min(coords_capacity / 9, normals_capacity / 3) : 0;
+    if ((st = cells_passes(ctx, j, sc, outs, sizes))) return st;
+    const uint64_t t = sizes->ntriangles;
+    if (t > j.cap_tris && t > 0)
+        return fail(ctx, KVSMC_ERR_CAPACITY, "cells: %llu triangles do not fit the outputs", (unsigned long long)t);
     return KVSMC_OK;
 }
 
@@ -612,8 +683,12 @@ kvsmc_status kvsmc_marching_cells_host(kvsmc_context* ctx, kvsmc_cell_type cell_
                          "cells: %s", cudaGetErrorString(e)));
     kvsmc::CellJob j = make_job(cell_type, dtype, d_in, nnodes, reinterpret_cast<const float*>(d_in + bv),
                                 reinterpret_cast<const uint32_t*>(d_in + bv + bx), ncells, isolevel);
+    CellsScratch sc;
     bool go = false;
-    if ((st = cells_count(ctx, j, has_minmax, min_value, max_value, sizes, &go)) || !go) return done(st);
+    if ((st = cells_prepare(ctx, j, &sc)) || (st = cells_range(ctx, j, sc, has_minmax, min_value, max_value, sizes,
+                                                                &go)) || !go ||
+        (st = cells_passes(ctx, j, sc, false, sizes)) || sizes->ntriangles == 0)
+        return done(st);
     const uint64_t t = sizes->ntriangles;
     if ((e = cudaMalloc(&d_out, t * 12 * sizeof(float))) != cudaSuccess)
         return done(fail(ctx, KVSMC_ERR_OUT_OF_MEMORY, "cells: %s", cudaGetErrorString(e)));

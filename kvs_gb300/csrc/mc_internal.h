@@ -149,6 +149,7 @@ struct CellJob {
     float* out_coords;        // 9 T
     float* out_normals;       // 3 T
     uint64_t cap_tris;
+    const uint64_t* d_total;  // emit: the scanned total (device); nothing is written when it exceeds cap_tris
     int* bad_index;           // set to 1 by a connection index >= nnodes
 };
 cudaError_t launch_cells_count(const CellJob& j, const Launch& L);
