@@ -426,6 +426,21 @@ kvsmc_status kvsmc_avs_read_info(const char* path, kvsmc_kvsml_info* info);
 kvsmc_status kvsmc_volume_load_avs(kvsmc_context* ctx, const char* path, kvsmc_volume** vol,
                                    kvsmc_kvsml_info* info);
 
+/* kvs::SlicePlane on an unstructured volume (SlicePlane.cpp:291-800): per
+ * cell, the case from the plane's sign at the node coordinates, the cell
+ * type's triangle table in table order, vertices (1 - r) v0 + r v1 with
+ * r = |p0 / (p1 - p0)| in float, per-vertex colours from the transfer
+ * function at the value interpolated in the value type's arithmetic, one
+ * normal -((v2 - v0) x (v1 - v0)) per triangle; coords float[9T], colours
+ * uint8[9T], normals float[3T] through `alloc` (which: 0 coords, 1 normals,
+ * 3 colours).  Arrays as kvsmc_marching_cells_host; p->min_coord and
+ * p->scale are not used (the reference slices the node coordinates as they
+ * are).  A connection index >= nnodes is KVSMC_ERR_INVALID_ARGUMENT. */
+kvsmc_status kvsmc_slice_cells_host(kvsmc_context* ctx, kvsmc_cell_type cell_type, const void* values,
+                                    kvsmc_dtype dtype, uint64_t nnodes, const float* coords,
+                                    const uint32_t* connections, uint64_t ncells, const kvsmc_slice_params* p,
+                                    kvsmc_host_alloc_fn alloc, void* user, uint64_t* ntriangles);
+
 /* ---------------------------------------------------------- polygon export */
 
 /* Binary STL records of a triangle mesh in device memory: what

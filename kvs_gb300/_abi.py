@@ -49,7 +49,7 @@ EXPORTS = [
     "kvsmc_write_stl_host", "kvsmc_volume_download", "kvsmc_kvsml_read_info", "kvsmc_volume_load_kvsml",
     "kvsmc_avs_read_info", "kvsmc_volume_load_avs",
     "kvsmc_slice_count", "kvsmc_slice_extract_device", "kvsmc_slice_plane",
-    "kvsmc_marching_cells_host", "kvsmc_marching_cells_device", "kvsmc_selftest_cells",
+    "kvsmc_marching_cells_host", "kvsmc_marching_cells_device", "kvsmc_selftest_cells", "kvsmc_slice_cells_host",
 ]
 
 PATH_AUTO = 0      # streaming kernels where eligible
@@ -200,6 +200,8 @@ def load(path=LIB_PATH):
                                                 C.c_double, C.c_double, HOST_ALLOC, vp, C.POINTER(Sizes)]),
         "kvsmc_marching_cells_device": (C.c_int, [vp, C.c_int, vp, C.c_int, u64, vp, vp, u64, C.c_double, i32,
                                                   C.c_double, C.c_double, vp, u64, vp, u64, C.POINTER(Sizes)]),
+        "kvsmc_slice_cells_host": (C.c_int, [vp, C.c_int, vp, C.c_int, u64, vp, vp, u64, C.POINTER(SliceParams),
+                                             HOST_ALLOC, vp, C.POINTER(u64)]),
         "kvsmc_kvsml_read_info": (C.c_int, [C.c_char_p, C.POINTER(KvsmlInfo)]),
         "kvsmc_volume_load_kvsml": (C.c_int, [vp, C.c_char_p, C.POINTER(vp), C.POINTER(KvsmlInfo)]),
         "kvsmc_avs_read_info": (C.c_int, [C.c_char_p, C.POINTER(KvsmlInfo)]),

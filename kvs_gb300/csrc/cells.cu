@@ -34,6 +34,7 @@
 #include "batch.h"
 #include "mc_device.cuh"
 #include "mc_interp.cuh"
+#include "slice_common.cuh"
 
 namespace kvsmc {
 
@@ -297,6 +298,146 @@ __global__ void __launch_bounds__(kCellThreads) k_cells_emit(CellJob j)
     }
 }
 
+// ---- kvs::SlicePlane on unstructured volumes (SlicePlane.cpp:291-800):
+// per cell type, a case from the plane's sign at the cell's node coordinates
+// (calculate_*_table_index, :828-942; no pyramid re-mapping), the cell type's
+// triangle table in table order [i], [i+1], [i+2] for all four types, each
+// vertex (1 - r) v0 + r v1 with r = |p0 / (p1 - p0)| in float on the node
+// coordinates (interpolate_vertex, :986-995, no coordinate transform), its
+// colour ColorMap::at of the value interpolated with the same r in the value
+// type's arithmetic (interpolate_value, :1043-1056), one normal
+// -((v2 - v0) x (v1 - v0)).
+
+template <int CT>
+__device__ __forceinline__ float3 node_xyz(const CellJob& j, uint32_t n)
+{
+    const float* c = j.coords + 3 * (uint64_t)n;
+    return make_float3(__ldg(c), __ldg(c + 1), __ldg(c + 2));
+}
+
+template <int CT>
+__device__ __forceinline__ unsigned slice_cell_case(const CellJob& j, uint64_t cell, uint32_t* nodes)
+{
+    using Tr = CellTraits<CT>;
+    cell_nodes<CT>(j, cell, nodes);
+    unsigned c = 0;
+#pragma unroll
+    for (int k = 0; k < Tr::kNodes; ++k) {
+        const float3 p = node_xyz<CT>(j, nodes[k]);
+        c |= plane_at(j, p.x, p.y, p.z) > 0.0f ? (1u << k) : 0u;
+    }
+    return c;
+}
+
+template <int CT, typename T>
+__global__ void __launch_bounds__(kCellThreads) k_cells_slice_count(CellJob j)
+{
+    using Tr = CellTraits<CT>;
+    const unsigned lane = threadIdx.x & 31u;
+    const uint64_t warps = (uint64_t)gridDim.x * (kCellThreads / 32);
+    const uint64_t groups = (j.ncells + 31) / 32;
+    for (uint64_t g = (uint64_t)blockIdx.x * (kCellThreads / 32) + (threadIdx.x >> 5); g < groups; g += warps) {
+        const uint64_t cell = g * 32 + lane;
+        uint32_t n = 0;
+        if (cell < j.ncells) {
+            uint32_t nodes[Tr::kNodes];
+            n = Tr::ntri(slice_cell_case<CT>(j, cell, nodes));
+        }
+        const uint32_t t = __reduce_add_sync(0xffffffffu, n);
+        if (lane == 0) j.tile_counts[g] = t;
+    }
+}
+
+template <typename T>
+__device__ __forceinline__ void slice_cell_vertex(const CellJob& j, uint32_t n0, uint32_t n1, float3& v, uchar3& rgb)
+{
+    const float3 a = node_xyz<0>(j, n0), b = node_xyz<0>(j, n1);
+    const float p0 = plane_at(j, a.x, a.y, a.z), p1 = plane_at(j, b.x, b.y, b.z);
+    const float r = fabsf(__fdiv_rn(p0, __fsub_rn(p1, p0)));
+    const float s = __fsub_rn(1.0f, r);
+    v.x = __fadd_rn(__fmul_rn(s, a.x), __fmul_rn(r, b.x));
+    v.y = __fadd_rn(__fmul_rn(s, a.y), __fmul_rn(r, b.y));
+    v.z = __fadd_rn(__fmul_rn(s, a.z), __fmul_rn(r, b.z));
+    const T* vals = static_cast<const T*>(j.values);
+    rgb = color_at(j, slice_value(vals[n0], vals[n1], r));
+}
+
+template <int CT, typename T>
+__global__ void __launch_bounds__(kCellThreads) k_cells_slice_emit(CellJob j)
+{
+    using Tr = CellTraits<CT>;
+    // hexahedra and pyramids are packed in the mappers' [i], [i+2], [i+1]
+    // order; the slicer takes [i], [i+1], [i+2]
+    constexpr bool kSwapped = CT == KVSMC_HEXAHEDRA || CT == KVSMC_PYRAMID;
+    if (j.d_total && *j.d_total > j.cap_tris) return;
+    const unsigned lane = threadIdx.x & 31u;
+    const uint64_t warps = (uint64_t)gridDim.x * (kCellThreads / 32);
+    const uint64_t groups = (j.ncells + 31) / 32;
+    for (uint64_t g0 = ((uint64_t)blockIdx.x * (kCellThreads / 32) + (threadIdx.x >> 5)) * 32; g0 < groups;
+         g0 += warps * 32) {
+        const uint64_t mine = g0 + lane;
+        unsigned todo = __ballot_sync(0xffffffffu, mine < groups && j.tile_counts[mine] != 0);
+        while (todo) {
+            const uint64_t g = g0 + (unsigned)(__ffs(todo) - 1);
+            todo &= todo - 1;
+            const uint64_t cell = g * 32 + lane;
+            uint32_t nodes[Tr::kNodes] = {};
+            unsigned c = 0;
+            uint32_t n = 0;
+            if (cell < j.ncells) {
+                c = slice_cell_case<CT>(j, cell, nodes);
+                n = Tr::ntri(c);
+            }
+            uint32_t inc = n;
+#pragma unroll
+            for (int o = 1; o < 32; o <<= 1) {
+                const uint32_t y = __shfl_up_sync(0xffffffffu, inc, o);
+                if (lane >= (unsigned)o) inc += y;
+            }
+            const uint32_t total = __shfl_sync(0xffffffffu, inc, 31);
+            const uint64_t base = j.tile_offsets[g];
+            for (uint32_t first = 0; first < total; first += 32) {   // warp-uniform: every lane shuffles
+                const uint32_t tri = first + lane;
+                unsigned lo = 0;
+#pragma unroll
+                for (unsigned step = 16; step > 0; step >>= 1) {
+                    const uint32_t probe = __shfl_sync(0xffffffffu, inc, lo + step - 1);
+                    if (probe <= tri) lo += step;
+                }
+                const uint32_t own_inc = __shfl_sync(0xffffffffu, inc, lo);
+                const uint32_t own_n = __shfl_sync(0xffffffffu, n, lo);
+                const unsigned own_c = __shfl_sync(0xffffffffu, c, lo);
+                uint32_t own_nodes[Tr::kNodes];
+#pragma unroll
+                for (int k = 0; k < Tr::kNodes; ++k) own_nodes[k] = __shfl_sync(0xffffffffu, nodes[k], lo);
+                const uint64_t t = base + tri;
+                if (tri >= total || t >= j.cap_tris) continue;
+                const uint32_t k = tri - (own_inc - own_n);
+                const uint64_t pk = Tr::tri(own_c) >> (12 * k);
+                float3 v[3];
+                uchar3 rgb[3];
+#pragma unroll
+                for (int sl = 0; sl < 3; ++sl) {
+                    const int src = kSwapped ? (sl == 0 ? 0 : 3 - sl) : sl;
+                    const unsigned ed = Tr::edge((int)((pk >> (4 * src)) & 15u));
+                    slice_cell_vertex<T>(j, own_nodes[ed & 15u], own_nodes[ed >> 4], v[sl], rgb[sl]);
+                }
+                float* o = j.out_coords + 9 * t;
+                o[0] = v[0].x; o[1] = v[0].y; o[2] = v[0].z;
+                o[3] = v[1].x; o[4] = v[1].y; o[5] = v[1].z;
+                o[6] = v[2].x; o[7] = v[2].y; o[8] = v[2].z;
+                uint8_t* q = j.out_colors + 9 * t;
+                q[0] = rgb[0].x; q[1] = rgb[0].y; q[2] = rgb[0].z;
+                q[3] = rgb[1].x; q[4] = rgb[1].y; q[5] = rgb[1].z;
+                q[6] = rgb[2].x; q[7] = rgb[2].y; q[8] = rgb[2].z;
+                const float3 nn = slice_normal(v[0], v[1], v[2]);
+                float* w = j.out_normals + 3 * t;
+                w[0] = nn.x; w[1] = nn.y; w[2] = nn.z;
+            }
+        }
+    }
+}
+
 // ---- min/max over the cells' nodes (GetMinMaxValues with connections,
 // UnstructuredVolumeObject.cpp:123-143): the scan starts at values[0] and
 // then visits values[conn[p]] for every connection p in order; Min/Max keep
@@ -433,6 +574,30 @@ cudaError_t launch_cells_emit(const CellJob& j, const Launch& L)
     return cudaGetLastError();
 }
 
+
+cudaError_t launch_cells_slice_count(const CellJob& j, const Launch& L)
+{
+    if (j.ncells == 0) return cudaSuccess;
+    const uint64_t tiles = cells_tiles(j.ncells);
+    prof_begin(L, "cells_slice_count");
+    KVSMC_CELL_SWITCH(j.cell_type, j.dtype,
+                      { k_cells_slice_count<CT, T><<<cell_grid(tiles, L), kCellThreads, 0, L.stream>>>(j); });
+    prof_end(L);
+    *L.counter += 1;
+    return cudaGetLastError();
+}
+
+cudaError_t launch_cells_slice_emit(const CellJob& j, const Launch& L)
+{
+    if (j.ncells == 0) return cudaSuccess;
+    const uint64_t tiles = cells_tiles(j.ncells);
+    prof_begin(L, "cells_slice_emit");
+    KVSMC_CELL_SWITCH(j.cell_type, j.dtype,
+                      { k_cells_slice_emit<CT, T><<<cell_grid(tiles, L), kCellThreads, 0, L.stream>>>(j); });
+    prof_end(L);
+    *L.counter += 1;
+    return cudaGetLastError();
+}
 
 size_t cells_minmax_scratch_bytes(int num_sms) { return (size_t)num_sms * 4 * 64; }
 
@@ -704,6 +869,85 @@ kvsmc_status kvsmc_marching_cells_host(kvsmc_context* ctx, kvsmc_cell_type cell_
     if (e == cudaSuccess) e = cudaMemcpyAsync(hn, d_out + 9 * t, t * 3 * sizeof(float), cudaMemcpyDeviceToHost, ctx->stream);
     if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
     if (e != cudaSuccess) return done(fail(ctx, KVSMC_ERR_CUDA, "cells: %s", cudaGetErrorString(e)));
+    return done(KVSMC_OK);
+}
+
+kvsmc_status kvsmc_slice_cells_host(kvsmc_context* ctx, kvsmc_cell_type cell_type, const void* values,
+                                    kvsmc_dtype dtype, uint64_t nnodes, const float* coords,
+                                    const uint32_t* connections, uint64_t ncells, const kvsmc_slice_params* p,
+                                    kvsmc_host_alloc_fn alloc, void* user, uint64_t* ntriangles)
+{
+    using namespace kvsmc_host;
+    if (!ctx || !alloc || !ntriangles) return KVSMC_ERR_INVALID_ARGUMENT;
+    *ntriangles = 0;
+    if (!p || !p->tf_table || p->tf_resolution < 1)
+        return fail(ctx, KVSMC_ERR_INVALID_ARGUMENT, "slice: bad parameters (colour table)");
+    kvsmc_status st = check_args(ctx, cell_type, dtype, nnodes, values, coords, connections, ncells);
+    if (st) return st;
+    KVSMC_CUDA(ctx, cudaSetDevice(ctx->device));
+    if (ncells == 0) return KVSMC_OK;
+    const int npc = nodes_per_cell(cell_type);
+    const size_t es = kvsmc::dtype_size(dtype);
+    // values | coords | connections | colour table in one device allocation
+    const size_t bv = align_up(nnodes * es, 256), bx = align_up(nnodes * 12, 256), bk = align_up(ncells * npc * 4, 256),
+                 bt = align_up((size_t)3 * p->tf_resolution, 256);
+    char* d_in = nullptr;
+    char* d_out = nullptr;
+    auto done = [&](kvsmc_status s) {
+        cudaStreamSynchronize(ctx->stream);
+        cudaFree(d_in);
+        cudaFree(d_out);
+        return s;
+    };
+    cudaError_t e = cudaMalloc(&d_in, bv + bx + bk + bt);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(d_in, values, nnodes * es, cudaMemcpyHostToDevice, ctx->stream);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(d_in + bv, coords, nnodes * 12, cudaMemcpyHostToDevice, ctx->stream);
+    if (e == cudaSuccess)
+        e = cudaMemcpyAsync(d_in + bv + bx, connections, ncells * npc * 4, cudaMemcpyHostToDevice, ctx->stream);
+    if (e == cudaSuccess)
+        e = cudaMemcpyAsync(d_in + bv + bx + bk, p->tf_table, (size_t)3 * p->tf_resolution, cudaMemcpyHostToDevice,
+                            ctx->stream);
+    if (e != cudaSuccess)
+        return done(fail(ctx, e == cudaErrorMemoryAllocation ? KVSMC_ERR_OUT_OF_MEMORY : KVSMC_ERR_CUDA,
+                         "slice cells: %s", cudaGetErrorString(e)));
+    kvsmc::CellJob j = make_job(cell_type, dtype, d_in, nnodes, reinterpret_cast<const float*>(d_in + bv),
+                                reinterpret_cast<const uint32_t*>(d_in + bv + bx), ncells, 0.0);
+    for (int k = 0; k < 4; ++k) j.coef[k] = p->coefficients[k];
+    j.tf_min = p->tf_min;
+    j.tf_max = p->tf_max;
+    j.tf_res = p->tf_resolution;
+    j.table = reinterpret_cast<const uint8_t*>(d_in + bv + bx + bk);
+    CellsScratch sc;
+    if ((st = cells_prepare(ctx, j, &sc))) return done(st);
+    const kvsmc::Launch L = launch_of(ctx);
+    e = kvsmc::launch_cells_slice_count(j, L);
+    if (e == cudaSuccess) e = kvsmc::launch_scan(j.tile_counts, j.tile_offsets, sc.tiles, sc.d_scan, sc.d_tail, L);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(ctx->h_small, sc.d_tail, sizeof(uint64_t), cudaMemcpyDeviceToHost, ctx->stream);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(ctx->h_small + 2, ctx->d_flag, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
+    if (e != cudaSuccess) return done(fail(ctx, KVSMC_ERR_CUDA, "slice cells: %s", cudaGetErrorString(e)));
+    if (read_bad(ctx)) return done(fail(ctx, KVSMC_ERR_INVALID_ARGUMENT, "cells: a connection index is >= nnodes"));
+    const uint64_t t = ctx->h_small[0];
+    *ntriangles = t;
+    if (t == 0) return done(KVSMC_OK);
+    const size_t oc = align_up(t * 36, 256), on = align_up(t * 12, 256);
+    if ((e = cudaMalloc(&d_out, oc + on + t * 9)) != cudaSuccess)
+        return done(fail(ctx, KVSMC_ERR_OUT_OF_MEMORY, "slice cells: %s", cudaGetErrorString(e)));
+    j.out_coords = reinterpret_cast<float*>(d_out);
+    j.out_normals = reinterpret_cast<float*>(d_out + oc);
+    j.out_colors = reinterpret_cast<uint8_t*>(d_out + oc + on);
+    j.cap_tris = t;
+    if ((e = kvsmc::launch_cells_slice_emit(j, L)) != cudaSuccess)
+        return done(fail(ctx, KVSMC_ERR_CUDA, "slice cells: %s", cudaGetErrorString(e)));
+    void* hc = alloc(user, 0, 9 * t);
+    void* hn = hc ? alloc(user, 1, 3 * t) : nullptr;
+    void* hk = hn ? alloc(user, 3, 9 * t) : nullptr;
+    if (!hc || !hn || !hk) return done(fail(ctx, KVSMC_ERR_OUT_OF_MEMORY, "slice cells: host alloc"));
+    e = cudaMemcpyAsync(hc, j.out_coords, t * 36, cudaMemcpyDeviceToHost, ctx->stream);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(hn, j.out_normals, t * 12, cudaMemcpyDeviceToHost, ctx->stream);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(hk, j.out_colors, t * 9, cudaMemcpyDeviceToHost, ctx->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
+    if (e != cudaSuccess) return done(fail(ctx, KVSMC_ERR_CUDA, "slice cells: %s", cudaGetErrorString(e)));
     return done(KVSMC_OK);
 }
 

@@ -151,10 +151,18 @@ struct CellJob {
     uint64_t cap_tris;
     const uint64_t* d_total;  // emit: the scanned total (device); nothing is written when it exceeds cap_tris
     int* bad_index;           // set to 1 by a connection index >= nnodes
+    // slice plane (kvs::SlicePlane on unstructured volumes)
+    float coef[4];            // a x + b y + c z + d
+    float tf_min, tf_max;     // colour map range
+    int32_t tf_res;
+    const uint8_t* table;     // device colour table, tf_res x RGB
+    uint8_t* out_colors;      // 9 T (RGB per vertex)
 };
 cudaError_t launch_cells_count(const CellJob& j, const Launch& L);
 cudaError_t launch_cells_emit(const CellJob& j, const Launch& L);
 uint64_t cells_tiles(uint64_t ncells);
+cudaError_t launch_cells_slice_count(const CellJob& j, const Launch& L);
+cudaError_t launch_cells_slice_emit(const CellJob& j, const Launch& L);
 // min/max over values[0] and the connected nodes' values, as doubles in d_out[0..1]
 size_t cells_minmax_scratch_bytes(int num_sms);
 cudaError_t launch_cells_minmax(const CellJob& j, void* scratch, double* d_out, const Launch& L);

@@ -23,6 +23,7 @@
 #include <cstring>
 
 #include "context.h"
+#include "slice_common.cuh"
 #include "mc_tables.h"
 
 namespace kvsmc {
@@ -34,12 +35,6 @@ __constant__ uint8_t c_slice_ntri[256] = MC_NTRI_INIT;
 __constant__ uint8_t c_slice_edge[12] = MC_EDGE_PACKED_INIT;
 
 constexpr int kSliceThreads = 128;
-
-__device__ __forceinline__ float plane_at(const SliceJob& j, float x, float y, float z)
-{
-    return __fadd_rn(__fadd_rn(__fadd_rn(__fmul_rn(j.coef[0], x), __fmul_rn(j.coef[1], y)), __fmul_rn(j.coef[2], z)),
-                     j.coef[3]);
-}
 
 __device__ __forceinline__ unsigned slice_case(const SliceJob& j, uint32_t x, uint32_t y, uint32_t z)
 {
@@ -55,79 +50,6 @@ __device__ __forceinline__ unsigned slice_case(const SliceJob& j, uint32_t x, ui
     c |= (plane_at(j, x1, y1, z1) > 0.0f) ? 64u : 0u;
     c |= (plane_at(j, fx, y1, z1) > 0.0f) ? 128u : 0u;
     return c;
-}
-
-// values[i0] + ratio * (values[i1] - values[i0]) with C++'s conversions for
-// each value type; the result as the float ColorMap::at receives.
-__device__ __forceinline__ float slice_value(int8_t a, int8_t b, float r)
-{
-    return __fadd_rn(__int2float_rn((int)a), __fmul_rn(r, __int2float_rn((int)b - (int)a)));
-}
-__device__ __forceinline__ float slice_value(uint8_t a, uint8_t b, float r)
-{
-    return __fadd_rn(__int2float_rn((int)a), __fmul_rn(r, __int2float_rn((int)b - (int)a)));
-}
-__device__ __forceinline__ float slice_value(int16_t a, int16_t b, float r)
-{
-    return __fadd_rn(__int2float_rn((int)a), __fmul_rn(r, __int2float_rn((int)b - (int)a)));
-}
-__device__ __forceinline__ float slice_value(uint16_t a, uint16_t b, float r)
-{
-    return __fadd_rn(__int2float_rn((int)a), __fmul_rn(r, __int2float_rn((int)b - (int)a)));
-}
-__device__ __forceinline__ float slice_value(int32_t a, int32_t b, float r)
-{
-    const int32_t d = (int32_t)((uint32_t)b - (uint32_t)a);   // two's-complement wrap
-    return __fadd_rn(__int2float_rn(a), __fmul_rn(r, __int2float_rn(d)));
-}
-__device__ __forceinline__ float slice_value(uint32_t a, uint32_t b, float r)
-{
-    return __fadd_rn(__uint2float_rn(a), __fmul_rn(r, __uint2float_rn(b - a)));
-}
-__device__ __forceinline__ float slice_value(long long a, long long b, float r)
-{
-    const long long d = (long long)((unsigned long long)b - (unsigned long long)a);
-    return __fadd_rn(__ll2float_rn(a), __fmul_rn(r, __ll2float_rn(d)));
-}
-__device__ __forceinline__ float slice_value(unsigned long long a, unsigned long long b, float r)
-{
-    return __fadd_rn(__ull2float_rn(a), __fmul_rn(r, __ull2float_rn(b - a)));
-}
-__device__ __forceinline__ float slice_value(float a, float b, float r)
-{
-    return __fadd_rn(a, __fmul_rn(r, __fsub_rn(b, a)));
-}
-__device__ __forceinline__ float slice_value(double a, double b, float r)
-{
-    return __double2float_rn(__dadd_rn(a, __dmul_rn((double)r, __dsub_rn(b, a))));
-}
-
-// ColorMap::at (ColorMap.cpp:1043-1054) with RGBColor::Mix and the
-// RGBColor(Vec3) rounding (RGBColor.cpp:23-31, 125-134; Math::Round).
-__device__ __forceinline__ uchar3 color_at(const SliceJob& j, float value)
-{
-    const float lo = j.tf_min, hi = j.tf_max;
-    const float v0 = value <= lo ? lo : (value <= hi ? value : hi);
-    const float r = (float)(j.tf_res - 1);
-    const float v = __fmul_rn(__fdiv_rn(__fsub_rn(v0, lo), __fsub_rn(hi, lo)), r);
-    // a NaN or out-of-range table position (undefined in the reference): entry 0
-    const uint32_t s0 = (v >= 0.0f && v <= r) ? (uint32_t)v : 0u;
-    const uint32_t s1 = (s0 + 1 < (uint32_t)j.tf_res) ? s0 + 1 : (uint32_t)j.tf_res - 1;
-    const float t = (v >= 0.0f && v <= r) ? __fsub_rn(v, __uint2float_rn(s0)) : 0.0f;
-    uint8_t out[3];
-#pragma unroll
-    for (int k = 0; k < 3; ++k) {
-        const float a = __fdiv_rn(__uint2float_rn(j.table[3 * s0 + k]), 255.0f);
-        const float b = __fdiv_rn(__uint2float_rn(j.table[3 * s1 + k]), 255.0f);
-        float m = __fadd_rn(__fmul_rn(a, __fsub_rn(1.0f, t)), __fmul_rn(b, t));
-        m = m <= 0.0f ? 0.0f : (m <= 1.0f ? m : 1.0f);
-        const float x = __fmul_rn(m, 255.0f);
-        // Math::Round: (int)(x + 0.5) in double for x in [0, 255], i.e. the
-        // integer part plus one when the (exact) fraction is at least 1/2
-        const float ip = truncf(x);
-        out[k] = (uint8_t)((int)ip + (__fsub_rn(x, ip) >= 0.5f ? 1 : 0));
-    }
-    return make_uchar3(out[0], out[1], out[2]);
 }
 
 struct SliceVertex {
@@ -159,18 +81,6 @@ __device__ __forceinline__ SliceVertex slice_vertex(const SliceJob& j, const T* 
     const T vb = vol[(uint64_t)bz * j.vol.slice + (uint64_t)by * j.vol.pitch + bx];
     o.rgb = color_at(j, slice_value(va, vb, ratio));
     return o;
-}
-
-// -((c - a) x (b - a)) (Vector3::cross, Matrix/Vector3.h; negation last)
-__device__ __forceinline__ float3 slice_normal(float3 a, float3 b, float3 c)
-{
-    const float ux = __fsub_rn(c.x, a.x), uy = __fsub_rn(c.y, a.y), uz = __fsub_rn(c.z, a.z);
-    const float vx = __fsub_rn(b.x, a.x), vy = __fsub_rn(b.y, a.y), vz = __fsub_rn(b.z, a.z);
-    float3 n;
-    n.x = -__fsub_rn(__fmul_rn(uy, vz), __fmul_rn(uz, vy));
-    n.y = -__fsub_rn(__fmul_rn(uz, vx), __fmul_rn(ux, vz));
-    n.z = -__fsub_rn(__fmul_rn(ux, vy), __fmul_rn(uy, vx));
-    return n;
 }
 
 // The cells of row (y, z) the plane can cut: an interval [x0, x1] of x (x0 >

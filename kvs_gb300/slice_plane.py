@@ -1,4 +1,5 @@
-"""kvs::SlicePlane for structured volumes, on the GPU (kvsmc_slice_plane).
+"""kvs::SlicePlane on the GPU: structured volumes (kvsmc_slice_plane) and
+unstructured ones (kvsmc_slice_cells_host).
 
 Mirrors the reference mapper (Source/Core/Visualization/Mapper/SlicePlane.h,
 SlicePlane.cpp): the two constructor forms (coefficients, or a point and a
@@ -8,12 +9,15 @@ PolygonObject: duplicated triangles in cell order, one RGB colour per vertex
 (VertexColor), one normal per triangle (PolygonNormal), opacity 255.  All
 per-cell work runs in libkvsmc's CUDA kernels.  As in the reference, the
 mapper's success flag is never set true (MapperBase starts false); a GPU
-failure is reported and exec returns None.  Unstructured volumes are not
-handled by this package.
+failure is reported and exec returns None.  An UnstructuredVolumeObject of
+tetrahedra, hexahedra, pyramids or prisms is sliced per cell by its cell
+type's marching table (SlicePlane.cpp:291-800, node coordinates as they are);
+other cell types give nothing, as in the reference.
 """
 import numpy as np
 
 from . import _abi
+from .marching_cells import MAPPERS, UnstructuredVolumeObject
 from .marching_cubes import (PolygonObject, StructuredVolumeObject, TransferFunction, _equal, default_context,
                              message_error)
 
@@ -67,7 +71,7 @@ class SlicePlane(PolygonObject):
             self._success = False
             message_error("Input object is NULL.")
             return None
-        if not isinstance(obj, StructuredVolumeObject):
+        if not isinstance(obj, (StructuredVolumeObject, UnstructuredVolumeObject)):
             self._success = False
             message_error("Input object is not volume dat.")
             return None
@@ -79,12 +83,71 @@ class SlicePlane(PolygonObject):
             return None
         return self
 
+    def _set_range(self, code, volume):
+        """MapperBase::setRange (MapperBase.cpp:54-83), the volume's min/max
+        cache filled first."""
+        if not self._tfunc.hasRange():
+            if code == 0:
+                self._tfunc.setRange(-128, 127)
+            elif code == 4:
+                self._tfunc.setRange(0, 255)
+            else:
+                lo, hi = f32(volume.minValue()), f32(volume.maxValue())
+                self._tfunc.setRange(lo, hi + f32(1.0) if _equal(float(lo), float(hi)) else hi)
+
+    def _mapping_cells(self, volume):
+        """SlicePlane::mapping, unstructured branch (SlicePlane.cpp:128-147, 291-320)."""
+        values = volume.values()
+        try:
+            code = _abi.dtype_code(values.dtype)
+        except TypeError:
+            code = None
+        mapper = MAPPERS.get(volume.cellType())
+        ctx = self._ctx or default_context()
+        n = volume.numberOfNodes()
+        conn = volume.connections()[:volume.numberOfCells() * volume.numberOfCellNodes()]
+        if mapper is not None and code is not None and not volume.hasMinMaxValues():
+            # UnstructuredVolumeObject::updateMinMaxValues by the device scan
+            _, _, sizes = _abi.marching_cells_host(ctx, mapper.ABI_CELL, values[:n], volume.coords()[:3 * n], conn,
+                                                   float("nan"))
+            volume.setMinMaxValues(sizes["min_value"], sizes["max_value"])
+        self._set_range(code, volume)
+        if not volume.hasMinMaxObjectCoords():
+            volume.updateMinMaxCoords()
+        self.setMinMaxObjectCoords(volume.minObjectCoord(), volume.maxObjectCoord())
+        self.setMinMaxExternalCoords(volume.minExternalCoord(), volume.maxExternalCoord())
+        if code is None:
+            self._success = False
+            message_error(f"Unsupported data type '{values.dtype}'.")
+            return
+        if mapper is None:
+            return                      # extract_plane: default: break
+        p = _abi.SliceParams()
+        for k in range(4):
+            p.coefficients[k] = float(self._coef[k])
+        table = np.ascontiguousarray(self._tfunc.table, np.uint8)
+        p.tf_min, p.tf_max = float(self._tfunc.min_value), float(self._tfunc.max_value)
+        p.tf_resolution = table.shape[0]
+        p.tf_table = table.ctypes.data
+        coords, normals, colors, ntri = slice_cells_host(ctx, mapper.ABI_CELL, values[:n], volume.coords()[:3 * n],
+                                                         conn, p)
+        self._coords = coords
+        self._colors = colors
+        self._normals = normals
+        self._opacities = np.array([255], np.uint8)
+        self._polygon_type = PolygonObject.Triangle
+        self._color_type = PolygonObject.VertexColor
+        self._normal_type = PolygonObject.PolygonNormal
+        self.ntriangles = ntri
+
     def _mapping(self, volume):
-        """SlicePlane::mapping (SlicePlane.cpp:88-145), structured branch."""
+        """SlicePlane::mapping (SlicePlane.cpp:88-145)."""
         if volume.veclen() != 1:
             self._success = False
             message_error("Input volume is not a sclar field data.")
             return
+        if isinstance(volume, UnstructuredVolumeObject):
+            return self._mapping_cells(volume)
         values = volume.values()
         try:
             code = _abi.dtype_code(values.dtype)
@@ -95,17 +158,10 @@ class SlicePlane(PolygonObject):
         ctx = self._ctx or default_context()
         dv = _abi.DeviceVolume.upload(ctx, volume.volume_array())
         try:
-            # MapperBase::setRange (MapperBase.cpp:54-83)
-            if not self._tfunc.hasRange():
-                if code == 0:
-                    self._tfunc.setRange(-128, 127)
-                elif code == 4:
-                    self._tfunc.setRange(0, 255)
-                else:
-                    if not volume.hasMinMaxValues():
-                        volume.setMinMaxValues(*dv.minmax())
-                    lo, hi = f32(volume.minValue()), f32(volume.maxValue())
-                    self._tfunc.setRange(lo, hi + f32(1.0) if _equal(float(lo), float(hi)) else hi)
+            # MapperBase::setRange (MapperBase.cpp:54-83): the cache first
+            if not volume.hasMinMaxValues():
+                volume.setMinMaxValues(*dv.minmax())
+            self._set_range(code, volume)
             # MapperBase::setMinMaxCoords (MapperBase.cpp:92-122)
             if not volume.hasMinMaxObjectCoords():
                 volume.updateMinMaxCoords()
@@ -152,5 +208,29 @@ def slice_plane_host(ctx, dv, params):
     n = C.c_uint64(0)
     ctx.check(ctx.lib.kvsmc_slice_plane(ctx.handle, dv.handle, C.byref(params), cb, None, C.byref(n)),
               "kvsmc_slice_plane")
+    return (bufs.get(0, np.zeros(0, f32)), bufs.get(1, np.zeros(0, f32)), bufs.get(3, np.zeros(0, np.uint8)),
+            n.value)
+
+
+def slice_cells_host(ctx, cell_type, values, coords, connections, params):
+    """kvsmc_slice_cells_host: (coords, normals, colours, triangles) of one unstructured volume."""
+    import ctypes as C
+    v = np.ascontiguousarray(values).reshape(-1)
+    c = np.ascontiguousarray(coords, np.float32).reshape(-1)
+    k = np.ascontiguousarray(connections, np.uint32).reshape(-1)
+    npc = _abi.CELL_NODES[int(cell_type)]
+    bufs = {}
+
+    def alloc(user, which, count):
+        a = np.empty(count, dtype=np.uint8 if which == 3 else np.float32)
+        bufs[which] = a
+        return a.ctypes.data
+
+    cb = _abi.HOST_ALLOC(alloc)
+    n = C.c_uint64(0)
+    ctx.check(ctx.lib.kvsmc_slice_cells_host(ctx.handle, int(cell_type), v.ctypes.data, _abi.dtype_code(v.dtype),
+                                             v.size, c.ctypes.data, k.ctypes.data if k.size else None,
+                                             k.size // npc, C.byref(params), cb, None, C.byref(n)),
+              "kvsmc_slice_cells_host")
     return (bufs.get(0, np.zeros(0, f32)), bufs.get(1, np.zeros(0, f32)), bufs.get(3, np.zeros(0, np.uint8)),
             n.value)

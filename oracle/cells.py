@@ -1,6 +1,7 @@
 """CPU restatement of the reference's unstructured marching mappers.
 
-TEST INFRASTRUCTURE ONLY: the checker for kvsmc_marching_cells_host (imported
+TEST INFRASTRUCTURE ONLY: the checker for kvsmc_marching_cells_host and
+kvsmc_slice_cells_host (imported
 by tests/ and bench.py's CPU-baseline leg, never by kvs_gb300).  numpy,
 vectorised over cells; pinned against the reference's own outputs in
 tests/golden/cells.npz.
@@ -179,3 +180,111 @@ def min_max_coords(coords, connections):
         lo[ax] = t[np.flatnonzero(t == mn)[-1]]
         hi[ax] = t[np.flatnonzero(t == mx)[-1]]
     return lo, hi
+
+
+# ---------------------------------------------------------------- SlicePlane
+
+def _slice_value(a, b, r):
+    """values[i0] + r * (values[i1] - values[i0]) with C++'s conversions per
+    value type (SlicePlane.cpp:1043-1056), as the float ColorMap::at gets."""
+    f32 = np.float32
+    k = a.dtype
+    if k in (np.int8, np.uint8, np.int16, np.uint16):
+        d = b.astype(np.int32) - a.astype(np.int32)                 # int promotion
+        return (a.astype(f32) + r * d.astype(f32)).astype(f32)
+    if k == np.int32:
+        d = (b.astype(np.int64) - a.astype(np.int64)).astype(np.uint32).view(np.int32)   # wraps
+        return (a.astype(f32) + r * d.astype(f32)).astype(f32)
+    if k == np.uint32:
+        d = (b.astype(np.uint64) - a.astype(np.uint64)).astype(np.uint32)
+        return (a.astype(f32) + r * d.astype(f32)).astype(f32)
+    if k == np.int64:
+        with np.errstate(over="ignore"):
+            d = (b.view(np.uint64) - a.view(np.uint64)).view(np.int64)
+        return (a.astype(f32) + r * d.astype(f32)).astype(f32)
+    if k == np.uint64:
+        with np.errstate(over="ignore"):
+            d = b - a
+        return (a.astype(f32) + r * d.astype(f32)).astype(f32)
+    if k == np.float32:
+        return (a + r * (b - a)).astype(f32)
+    return (a + r.astype(np.float64) * (b - a)).astype(f32)       # double
+
+
+def color_at(table, tf_min, tf_max, value):
+    """ColorMap::at (ColorMap.cpp:1043-1054), RGBColor::Mix in float and the
+    RGBColor(Vec3) rounding, vectorised; a NaN or out-of-range table position
+    (undefined in the reference) takes entry 0."""
+    f32 = np.float32
+    table = np.asarray(table, np.uint8).reshape(-1, 3)
+    res = table.shape[0]
+    lo, hi = f32(tf_min), f32(tf_max)
+    v = np.asarray(value, f32)
+    v0 = np.where(v <= lo, lo, np.where(v <= hi, v, hi)).astype(f32)
+    rr = f32(res - 1)
+    with np.errstate(all="ignore"):
+        pos = (((v0 - lo) / f32(hi - lo)).astype(f32) * rr).astype(f32)
+    ok = (pos >= 0) & (pos <= rr)
+    s0 = np.where(ok, pos, 0).astype(np.int64)
+    s1 = np.minimum(s0 + 1, res - 1)
+    t = np.where(ok, pos - s0.astype(f32), f32(0)).astype(f32)
+    a = (table[s0].astype(f32) / f32(255)).astype(f32)
+    b = (table[s1].astype(f32) / f32(255)).astype(f32)
+    m = (a * (f32(1) - t)[:, None] + b * t[:, None]).astype(f32)
+    m = np.where(m <= 0, f32(0), np.where(m <= 1, m, f32(1))).astype(f32)
+    x = (m * f32(255)).astype(f32).astype(np.float64)
+    return np.floor(x + 0.5).astype(np.uint8)
+
+
+def slice_cells(cell_type, values, coords, connections, coefficients, table, tf_min, tf_max):
+    """kvs::SlicePlane::extract_*_plane (SlicePlane.cpp:327-800) on an
+    unstructured volume: (coords f32[9T], colors u8[9T], normals f32[3T])."""
+    f32 = np.float32
+    ct = int(cell_type)
+    npc = NODES[ct]
+    v = np.asarray(values).reshape(-1)
+    xyz = np.asarray(coords, f32).reshape(-1, 3)
+    conn = np.asarray(connections, np.int64).reshape(-1, npc)
+    cf = np.asarray(coefficients, f32)
+    empty = (np.zeros(0, f32), np.zeros(0, np.uint8), np.zeros(0, f32))
+    if conn.shape[0] == 0:
+        return empty
+
+    def plane(p):   # ((a x + b y) + c z) + d in float
+        ab = ((cf[0] * p[..., 0]).astype(f32) + (cf[1] * p[..., 1]).astype(f32)).astype(f32)
+        return ((ab + (cf[2] * p[..., 2]).astype(f32)).astype(f32) + cf[3]).astype(f32)
+
+    nodes = conn[:, [4, 5, 6, 7, 0, 1, 2, 3]] if ct == HEXAHEDRA else conn
+    with np.errstate(all="ignore"):
+        pv = plane(xyz).astype(f32)
+    case = np.zeros(nodes.shape[0], np.int64)
+    for k in range(npc):
+        case |= (pv[nodes[:, k]] > 0).astype(np.int64) << k
+    ntri_t, edges_t, en = tables()[ct]
+    ntri = ntri_t[case]
+    T = int(ntri.sum())
+    if T == 0:
+        return empty
+    cell = np.repeat(np.arange(nodes.shape[0]), ntri)
+    first = np.repeat(np.cumsum(ntri) - ntri, ntri)
+    k = np.arange(T) - first
+    e = edges_t[case[cell], k]
+    if ct in (HEXAHEDRA, PYRAMID):
+        e = e[:, [0, 2, 1]]          # the tables are packed in the mappers' [i], [i+2], [i+1] order
+    n0 = nodes[cell[:, None], en[e, 0]]
+    n1 = nodes[cell[:, None], en[e, 1]]
+    p0, p1 = pv[n0], pv[n1]
+    with np.errstate(all="ignore"):
+        r = np.abs((p0 / (p1 - p0)).astype(f32)).astype(f32)
+        s = (f32(1) - r).astype(f32)
+        c0, c1 = xyz[n0], xyz[n1]
+        pos = ((s[..., None] * c0).astype(f32) + (r[..., None] * c1).astype(f32)).astype(f32)
+        val = _slice_value(v[n0], v[n1], r)
+    rgb = color_at(table, tf_min, tf_max, val.reshape(-1)).reshape(T, 3, 3)
+    with np.errstate(all="ignore"):
+        u = pos[:, 2] - pos[:, 0]
+        w = pos[:, 1] - pos[:, 0]
+        nrm = -np.stack([u[:, 1] * w[:, 2] - u[:, 2] * w[:, 1],
+                         u[:, 2] * w[:, 0] - u[:, 0] * w[:, 2],
+                         u[:, 0] * w[:, 1] - u[:, 1] * w[:, 0]], axis=1).astype(f32)
+    return pos.reshape(-1), rgb.reshape(-1), nrm.reshape(-1)

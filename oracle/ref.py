@@ -96,6 +96,11 @@ def lib():
             C.c_int, C.c_int, C.c_int, C.c_void_p, C.c_ulonglong, C.c_void_p, C.c_void_p, C.c_ulonglong,
             C.c_double, C.c_int, C.c_int, C.c_int, C.c_double, C.c_double, C.c_int, C.c_int, C.c_float,
             C.c_float, C.c_int, C.POINTER(_Result)]
+        _lib.kvsref_slice_cells.restype = C.c_int
+        _lib.kvsref_slice_cells.argtypes = [
+            C.c_int, C.c_int, C.c_int, C.c_void_p, C.c_ulonglong, C.c_void_p, C.c_void_p, C.c_ulonglong,
+            C.c_void_p, C.c_int, C.c_double, C.c_double, C.c_int, C.c_int, C.c_float, C.c_float,
+            C.POINTER(_Result)]
         _lib.kvsref_free.argtypes = [C.POINTER(_Result)]
         _lib.kvsref_hydrogen.argtypes = [C.c_uint, C.c_void_p]
         _lib.kvsref_default_colormap.argtypes = [C.c_int, C.c_void_p]
@@ -222,6 +227,32 @@ def marching_cells(cell_type, values, coords, connections, isolevel, form=0, nor
     out = _collect(r)
     out["seconds"] = seconds
     return out
+
+
+def slice_cells(cell_type, values, coords, connections, coefficients=None, point=None, normal=None, minmax=None,
+                tf_resolution=256, tf_range=None):
+    """The reference kvs::SlicePlane on an UnstructuredVolumeObject (cell types
+    as marching_cells), by plane coefficients or by a point and a normal."""
+    v = np.ascontiguousarray(values).reshape(-1)
+    c = np.ascontiguousarray(coords, np.float32).reshape(-1)
+    k = np.ascontiguousarray(connections, np.uint32).reshape(-1)
+    npc = CELL_NODES[int(cell_type)]
+    if coefficients is not None:
+        form, plane = 0, np.ascontiguousarray(coefficients, np.float32)
+    else:
+        form, plane = 1, np.ascontiguousarray(list(point) + list(normal), np.float32)
+    r = _Result()
+    st = lib().kvsref_slice_cells(
+        form, int(cell_type), dtype_code(v.dtype), v.ctypes.data, v.size, c.ctypes.data, k.ctypes.data,
+        k.size // npc, plane.ctypes.data, 1 if minmax is not None else 0,
+        float(minmax[0]) if minmax is not None else 0.0,
+        float(minmax[1]) if minmax is not None else 0.0,
+        tf_resolution, 1 if tf_range is not None else 0,
+        float(tf_range[0]) if tf_range is not None else 0.0,
+        float(tf_range[1]) if tf_range is not None else 0.0, C.byref(r))
+    if st != 0:
+        raise RuntimeError("kvsref_slice_cells failed")
+    return _collect(r)
 
 
 def slice_plane(values, coefficients=None, point=None, normal=None, minmax=None, tf_resolution=256,

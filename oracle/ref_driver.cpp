@@ -225,6 +225,43 @@ int kvsref_slice_plane(
     return 0;
 }
 
+/* kvs::SlicePlane on an UnstructuredVolumeObject (cell_type as in
+ * kvsref_marching_cells); form 0: plane = a, b, c, d; form 1: plane = point,
+ * normal. */
+int kvsref_slice_cells(
+    int form, int cell_type, int dtype, const void* values, unsigned long long nnodes, const float* coords,
+    const unsigned int* connections, unsigned long long ncells, const float* plane, int has_minmax, double vmin,
+    double vmax, int tf_resolution, int tf_has_range, float tf_min, float tf_max, kvsref_result* out )
+{
+    std::memset( out, 0, sizeof( *out ) );
+    static const kvs::UnstructuredVolumeObject::CellType types[4] = {
+        kvs::UnstructuredVolumeObject::Tetrahedra, kvs::UnstructuredVolumeObject::Hexahedra,
+        kvs::UnstructuredVolumeObject::Pyramid, kvs::UnstructuredVolumeObject::Prism };
+    static const size_t npc[4] = { 4, 8, 5, 6 };
+    if ( cell_type < 0 || cell_type > 3 ) return -1;
+    kvs::AnyValueArray vals = Values( dtype, values, nnodes );
+    if ( vals.size() != nnodes ) return -1;
+    kvs::TransferFunction tfunc( tf_resolution > 0 ? tf_resolution : 256 );
+    if ( tf_has_range ) tfunc.setRange( tf_min, tf_max );
+    auto* vol = new kvs::UnstructuredVolumeObject();
+    vol->setCellType( types[cell_type] );
+    vol->setVeclen( 1 );
+    vol->setNumberOfNodes( nnodes );
+    vol->setNumberOfCells( ncells );
+    vol->setCoords( kvs::ValueArray<kvs::Real32>( coords, 3 * nnodes ) );
+    vol->setConnections( kvs::ValueArray<kvs::UInt32>( connections, npc[cell_type] * ncells ) );
+    vol->setValues( vals );
+    if ( has_minmax ) vol->setMinMaxValues( vmin, vmax );
+    kvs::SlicePlane* s = nullptr;
+    if ( form == 0 ) s = new kvs::SlicePlane( vol, kvs::Vec4( plane[0], plane[1], plane[2], plane[3] ), tfunc );
+    else s = new kvs::SlicePlane( vol, kvs::Vec3( plane[0], plane[1], plane[2] ),
+                                  kvs::Vec3( plane[3], plane[4], plane[5] ), tfunc );
+    Fill( s, s, vol, out );
+    delete s;
+    delete vol;
+    return 0;
+}
+
 /*
  * KVSML structured volumes through the reference's own reader and writer
  * (StructuredVolumeObject::read / write, StructuredVolumeObject.cpp:171-270,

@@ -9,11 +9,14 @@ files written by the reference PolygonExporter<kvs::Stl> in tests/golden/stl.npz
 (tests/golden/stl.json), kvs::SlicePlane results in tests/golden/slice.npz
 (tests/golden/slice.json), and the unstructured marching mappers
 (MarchingTetrahedra / Hexahedra / Pyramid / Prism, directly and through
-kvs::Isosurface) in tests/golden/cells.npz (tests/golden/cells.json).  The reference
+kvs::Isosurface) in tests/golden/cells.npz (tests/golden/cells.json), and
+kvs::SlicePlane on unstructured volumes in tests/golden/slice_cells.npz
+(tests/golden/slice_cells.json).  The reference
 ships no tests or golden vectors of its own, so these fixtures pin the oracle
 restatement and the CUDA path on hosts where the reference is absent.
 
-    python tests/golden/make_golden.py [marching_cubes] [isosurface] [stl] [slice] [cells]   (default: all)
+    python tests/golden/make_golden.py [marching_cubes] [isosurface] [stl] [slice] [cells] [slice_cells]
+        (default: all)
 """
 import json
 import os
@@ -287,12 +290,71 @@ def write_cells():
     print(f"{len(manifest)} cells cases")
 
 
+def slice_cells_cases():
+    """(name, cell_type, values, coords, connections, [run: dict(coefficients | point+normal, tf_range)])"""
+    out = []
+    obl = dict(coefficients=(0.31, -0.52, 0.79, -1.37))
+    for ct, tag in ((0, "tet"), (1, "hex"), (2, "pyr"), (3, "pri")):
+        seed = 300 + ct
+        rng = np.random.default_rng(seed)
+        xyz, conn = cm.grid(ct, 7, 6, 5, seed=seed)
+        v = cm.sphere_values(xyz)
+        out.append((f"{tag}_grid_f32", ct, v, xyz, conn,
+                    [obl, dict(point=(2.9, 2.4, 1.7), normal=(0.3, -0.5, 0.8)), dict(coefficients=(1, 1, 1, -6.5)),
+                     dict(coefficients=(0, 0, 1, 100)), dict(coefficients=(0.2, 0.9, -0.4, -1.1), tf_range=(1.0, 3.0))]))
+        # nodes exactly on the plane (unjittered grid, plane z = 2 and x = 3)
+        xyz0, conn0 = cm.grid(ct, 6, 5, 5, jitter=0.0, seed=seed)
+        out.append((f"{tag}_flat_f32", ct, cm.sphere_values(xyz0), xyz0, conn0,
+                    [dict(coefficients=(0, 0, 1, -2)), dict(coefficients=(1, 0, 0, -3))]))
+        xyz, conn = cm.random_mesh(ct, 120, (300, 120, 200, 160)[ct], seed=seed)
+        n = xyz.shape[0]
+        for dt, gen in ((np.int8, lambda: rng.integers(-128, 128, n)), (np.uint8, lambda: rng.integers(0, 256, n)),
+                        (np.int16, lambda: rng.integers(-3000, 3000, n)),
+                        (np.uint16, lambda: rng.integers(0, 65536, n)),
+                        (np.int32, lambda: rng.integers(-2 ** 30, 2 ** 30, n)),
+                        (np.uint32, lambda: rng.integers(0, 2 ** 32 - 1, n, dtype=np.uint64)),
+                        (np.int64, lambda: rng.integers(-2 ** 60, 2 ** 60, n)),
+                        (np.uint64, lambda: rng.integers(0, 2 ** 63, n, dtype=np.uint64)),
+                        (np.float64, lambda: rng.standard_normal(n))):
+            out.append((f"{tag}_random_{np.dtype(dt).name}", ct, gen().astype(dt), xyz, conn, [obl]))
+        out.append((f"{tag}_nocells_f32", ct, rng.standard_normal(n).astype(np.float32), xyz,
+                    np.zeros((0, cm.NODES[ct]), np.uint32), [obl]))
+    return out
+
+
+def write_slice_cells():
+    arrays, manifest = {}, []
+    for name, ct, v, xyz, conn, runs in slice_cells_cases():
+        arrays[f"{name}__values"] = v
+        arrays[f"{name}__coords"] = xyz
+        arrays[f"{name}__connections"] = conn
+        for i, o in enumerate(runs):
+            key = f"{name}__{i}"
+            r = ref.slice_cells(ct, v, xyz, conn, coefficients=o.get("coefficients"), point=o.get("point"),
+                                normal=o.get("normal"), tf_range=o.get("tf_range"))
+            for fld in ("coords", "normals", "colors", "opacities"):
+                arrays[f"{key}__{fld}"] = r[fld]
+            arrays[f"{key}__vol_minmax"] = np.array([r["vol_min"], r["vol_max"]], np.float64)
+            manifest.append(dict(key=key, case=name, cell_type=ct, coefficients=o.get("coefficients"),
+                                 point=o.get("point"), normal=o.get("normal"), tf_range=o.get("tf_range"),
+                                 success=r["success"], polygon_type=r["polygon_type"], color_type=r["color_type"],
+                                 normal_type=r["normal_type"], min_obj=r["min_obj"].tolist(),
+                                 max_obj=r["max_obj"].tolist(), max_ext=r["max_ext"].tolist(),
+                                 ntriangles=int(r["coords"].size // 9)))
+    np.savez_compressed(os.path.join(HERE, "slice_cells.npz"), **arrays)
+    with open(os.path.join(HERE, "slice_cells.json"), "w") as f:
+        json.dump(manifest, f, indent=0)
+    print(f"{len(manifest)} slice_cells cases")
+
+
 def main():
     if not ref.available():
         ref.build()
-    parts = sys.argv[1:] or ["marching_cubes", "isosurface", "stl", "slice", "cells"]
+    parts = sys.argv[1:] or ["marching_cubes", "isosurface", "stl", "slice", "cells", "slice_cells"]
     if "cells" in parts:
         write_cells()
+    if "slice_cells" in parts:
+        write_slice_cells()
     if "slice" in parts:
         write_slice()
     if "isosurface" in parts:
