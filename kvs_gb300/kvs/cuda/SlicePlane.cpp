@@ -6,9 +6,10 @@
  *  The flow is the reference's (Source/Core/Visualization/Mapper/SlicePlane.cpp):
  *  exec (:60-80) checks the input; mapping (:88-145) checks veclen, attaches
  *  the volume, sets the colour map range (MapperBase::setRange) and the
- *  bounding box, and extracts.  What changes: for a structured volume the
- *  min/max behind the colour range comes from the device scan (filled into
- *  the volume's cache first, so setRange does no CPU scan), and every cell is
+ *  bounding box, and extracts.  What changes: the min/max behind the colour
+ *  range comes from the device scan (filled into the volume's cache first, so
+ *  setRange does no CPU scan), and every cell -- of a structured volume, or of
+ *  an unstructured one of tetrahedra, hexahedra, pyramids or prisms -- is
  *  handled by libkvsmc's kernels; the arrays arrive as kvs::ValueArrays from
  *  the C call's allocator.  As in the reference, isSuccess() is never set true
  *  by this mapper (MapperBase starts false).
@@ -17,10 +18,11 @@
 #include "SlicePlane.h"
 
 #include <kvs/Message>
-#include <kvs/SlicePlane>
 #include <kvs/StructuredVolumeObject>
 #include <kvs/UnstructuredVolumeObject>
 #include <kvs/ValueArray>
+
+#include <limits>
 
 #include "Context.h"
 
@@ -107,18 +109,7 @@ bool SlicePlane::mapping( const kvs::VolumeObjectBase* volume )
 
     if ( volume->volumeType() != kvs::VolumeObjectBase::Structured )
     {
-        // unstructured grids: the reference's own mapper
-        kvs::SlicePlane polygon( volume, m_coef, BaseClass::transferFunction() );
-        SuperClass::setCoords( polygon.coords() );
-        SuperClass::setColors( polygon.colors() );
-        SuperClass::setNormals( polygon.normals() );
-        SuperClass::setOpacities( polygon.opacities() );
-        SuperClass::setPolygonType( polygon.polygonType() );
-        SuperClass::setColorType( polygon.colorType() );
-        SuperClass::setNormalType( polygon.normalType() );
-        SuperClass::setMinMaxObjectCoords( polygon.minObjectCoord(), polygon.maxObjectCoord() );
-        SuperClass::setMinMaxExternalCoords( polygon.minExternalCoord(), polygon.maxExternalCoord() );
-        return true;
+        return this->mapping_cells( kvs::UnstructuredVolumeObject::DownCast( volume ) );
     }
 
     const auto* svolume = kvs::StructuredVolumeObject::DownCast( volume );
@@ -178,6 +169,89 @@ bool SlicePlane::mapping( const kvs::VolumeObjectBase* volume )
         return false;
     }
     // SlicePlane.cpp:196-202
+    SuperClass::setCoords( out.coords );
+    SuperClass::setColors( out.colors );
+    SuperClass::setNormals( out.normals );
+    SuperClass::setOpacity( 255 );
+    SuperClass::setPolygonType( kvs::PolygonObject::Triangle );
+    SuperClass::setColorType( kvs::PolygonObject::VertexColor );
+    SuperClass::setNormalType( kvs::PolygonObject::PolygonNormal );
+    return true;
+}
+
+// The unstructured branch (SlicePlane.cpp:128-147, 291-800): the cells of a
+// tetrahedral, hexahedral, pyramidal or prismatic volume on the GPU
+// (kvsmc_slice_cells_host), the min/max behind the colour range from the
+// device scan over the cells' nodes; other cell types give nothing.
+bool SlicePlane::mapping_cells( const kvs::UnstructuredVolumeObject* volume )
+{
+    int cell = -1;
+    switch ( volume->cellType() )
+    {
+    case kvs::UnstructuredVolumeObject::Tetrahedra: cell = KVSMC_TETRAHEDRA; break;
+    case kvs::UnstructuredVolumeObject::Hexahedra: cell = KVSMC_HEXAHEDRA; break;
+    case kvs::UnstructuredVolumeObject::Pyramid: cell = KVSMC_PYRAMID; break;
+    case kvs::UnstructuredVolumeObject::Prism: cell = KVSMC_PRISM; break;
+    default: break;
+    }
+    const int dtype = kvs::cuda::DType( volume->values() );
+    kvsmc_status st = KVSMC_OK;
+    kvsmc_context* ctx = nullptr;
+    if ( cell >= 0 && dtype >= 0 )
+    {
+        ctx = kvs::cuda::DeviceContext( m_device, &st );
+        if ( !ctx )
+        {
+            kvsMessageError("libkvsmc: %s.", kvsmc_status_string( st ) );
+            return false;
+        }
+        if ( !volume->hasMinMaxValues() )
+        {
+            // at isolevel NaN no node is above: only the min/max scan runs
+            kvsmc_sizes sizes{};
+            st = kvsmc_marching_cells_host( ctx, kvsmc_cell_type( cell ), volume->values().data(),
+                                            kvsmc_dtype( dtype ), volume->numberOfNodes(), volume->coords().data(),
+                                            volume->connections().data(), volume->numberOfCells(),
+                                            std::numeric_limits<double>::quiet_NaN(), 0, 0.0, 0.0,
+                                            []( void*, int32_t, uint64_t ) -> void* { return nullptr; }, nullptr,
+                                            &sizes );
+            if ( st != KVSMC_OK )
+            {
+                kvsMessageError("libkvsmc: %s: %s", kvsmc_status_string( st ), kvsmc_last_error( ctx ) );
+                return false;
+            }
+            volume->setMinMaxValues( sizes.min_value, sizes.max_value );
+        }
+    }
+    BaseClass::attachVolume( volume );
+    BaseClass::setRange( volume );
+    BaseClass::setMinMaxCoords( volume, this );
+    if ( dtype < 0 )
+    {
+        BaseClass::setSuccess( false );
+        kvsMessageError("Unsupported data type '%s'.", volume->values().typeInfo()->typeName() );
+        return true;
+    }
+    if ( cell < 0 ) return true;   // extract_plane: default: break
+
+    kvsmc_slice_params p;
+    for ( int k = 0; k < 4; ++k ) p.coefficients[k] = m_coef[k];
+    for ( int k = 0; k < 3; ++k ) { p.min_coord[k] = 0.0f; p.scale[k] = 1.0f; }
+    const kvs::ColorMap& cmap = BaseClass::transferFunction().colorMap();
+    p.tf_min = cmap.minValue();
+    p.tf_max = cmap.maxValue();
+    p.tf_resolution = static_cast<int32_t>( cmap.resolution() );
+    p.tf_table = cmap.table().data();
+    SliceOutputs out;
+    uint64_t ntriangles = 0;
+    st = kvsmc_slice_cells_host( ctx, kvsmc_cell_type( cell ), volume->values().data(), kvsmc_dtype( dtype ),
+                                 volume->numberOfNodes(), volume->coords().data(), volume->connections().data(),
+                                 volume->numberOfCells(), &p, &AllocateSlice, &out, &ntriangles );
+    if ( st != KVSMC_OK )
+    {
+        kvsMessageError("libkvsmc: %s: %s", kvsmc_status_string( st ), kvsmc_last_error( ctx ) );
+        return false;
+    }
     SuperClass::setCoords( out.coords );
     SuperClass::setColors( out.colors );
     SuperClass::setNormals( out.normals );

@@ -7,8 +7,8 @@
  *  Same constructors, setPlane and exec(ObjectBase*) as the reference mapper
  *  (Source/Core/Visualization/Mapper/SlicePlane.h:25-79); a structured
  *  volume is sliced by libkvsmc (kvsmc_slice_plane) with the same
- *  PolygonObject bits; unstructured volumes go to the reference's own
- *  kvs::SlicePlane, unchanged.  When the GPU call fails, exec reports
+ *  PolygonObject bits, and so is an unstructured volume of tetrahedra,
+ *  hexahedra, pyramids or prisms (kvsmc_slice_cells_host).  When the GPU call fails, exec reports
  *  kvsMessageError and returns nullptr (no CPU fallback).
  */
 /*****************************************************************************/
@@ -16,6 +16,7 @@
 #include <kvs/MapperBase>
 #include <kvs/Module>
 #include <kvs/PolygonObject>
+#include <kvs/UnstructuredVolumeObject>
 #include <kvs/VolumeObjectBase>
 #include <kvs/Vector3>
 #include <kvs/Vector4>
@@ -58,6 +59,7 @@ public:
 
 private:
     bool mapping( const kvs::VolumeObjectBase* volume );
+    bool mapping_cells( const kvs::UnstructuredVolumeObject* volume );
 };
 
 } // end of namespace cuda
