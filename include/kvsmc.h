@@ -476,6 +476,34 @@ kvsmc_status kvsmc_write_stl_host(kvsmc_context* ctx, const char* path, int32_t 
                                   uint64_t ncoords, const float* normals, uint64_t nnormals,
                                   const uint32_t* connections, uint64_t nconnections);
 
+
+/* Binary PLY (little endian) of a triangle mesh without connections: what
+ * kvs::PolygonExporter<kvs::Ply>::exec (PolygonExporter.cpp:178-361) and
+ * kvs::Ply::write with the Binary file type (Ply.cpp:389-488, header of
+ * PlyFile.cpp:399-460) write -- the header ("element vertex N", the x/y/z,
+ * red/green/blue and nx/ny/nz properties present, "element face 0") and one
+ * packed record per vertex.  color_mode: 0 no colour, 1 the one RGB colour at
+ * colors[0..2] for every vertex (a PolygonObject with a single colour), 2 one
+ * RGB per vertex (VertexColor).  normal_mode: 0 none, 1 zeros (PolygonNormal:
+ * the exporter averages polygon normals over connections, of which there are
+ * none), 2 one normal per vertex (VertexNormal).  Meshes with connections are
+ * not taken: the reference's writer stores face indices through a null
+ * pointer (Ply.cpp:470-480).  More than 2^31 - 1 vertices is
+ * KVSMC_ERR_TOO_LARGE (the header's int count). */
+uint32_t kvsmc_ply_record_bytes(int32_t color_mode, int32_t normal_mode);
+/* The header text; returns its length (written to buf when size > length). */
+int64_t kvsmc_ply_header(uint64_t nvertices, int32_t color_mode, int32_t normal_mode, char* buf, uint64_t size);
+/* The records of a device mesh into a 16-byte aligned device buffer of
+ * nvertices * kvsmc_ply_record_bytes() bytes. */
+kvsmc_status kvsmc_ply_records(kvsmc_context* ctx, const float* d_coords, uint64_t nvertices, const uint8_t* d_colors,
+                               int32_t color_mode, const float* d_normals, int32_t normal_mode, uint8_t* d_out);
+/* The file of a device mesh (records in chunks through pinned memory), or of a
+ * host mesh (uploaded first). */
+kvsmc_status kvsmc_write_ply(kvsmc_context* ctx, const char* path, const float* d_coords, uint64_t nvertices,
+                             const uint8_t* d_colors, int32_t color_mode, const float* d_normals, int32_t normal_mode);
+kvsmc_status kvsmc_write_ply_host(kvsmc_context* ctx, const char* path, const float* coords, uint64_t nvertices,
+                                  const uint8_t* colors, int32_t color_mode, const float* normals, int32_t normal_mode);
+
 /* ------------------------------------------------------------- autotuning */
 
 /* Launch shape of the streaming kernels for one (value type, volume size

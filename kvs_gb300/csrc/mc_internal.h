@@ -171,6 +171,11 @@ cudaError_t launch_cells_minmax(const CellJob& j, void* scratch, double* d_out, 
 // device word set to 1 when a connection index is >= nverts (that vertex
 // then reads as vertex 0)
 constexpr uint64_t kStlRecordBytes = 50;
+// ---- binary PLY vertex records (ply.cu): colour mode 0 none / 1 one colour /
+// 2 per vertex; normal mode 0 none / 1 zeros / 2 per vertex
+int ply_record_bytes(int color_mode, int normal_mode);
+cudaError_t launch_ply_vertices(const float* coords, const uint8_t* colors, int color_mode, const float* normals,
+                                int normal_mode, uint64_t nverts, uint8_t* out, const Launch& L);
 cudaError_t launch_stl_records(const float* coords, const float* normals, const uint32_t* conn, uint64_t nverts,
                                uint64_t ntri, int mode, uint8_t* out, int* bad_index, const Launch& L);
 

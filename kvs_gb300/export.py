@@ -1,4 +1,4 @@
-"""Binary STL export of triangle meshes, serialised on the GPU.
+"""Binary STL and PLY export of triangle meshes, serialised on the GPU.
 
 Mirrors kvs::PolygonExporter<kvs::Stl> (Source/Core/Visualization/Exporter/
 PolygonExporter.h:53-61, PolygonExporter.cpp:78-176) with kvs::Stl's Binary
@@ -9,6 +9,14 @@ output) is written without any host PolygonObject (write_stl_device).
 
 The reference's kvs::Stl defaults to ASCII; ASCII output is not provided here
 (write() reports it and returns False): set the Binary file type.
+
+PolygonExporterPly mirrors kvs::PolygonExporter<kvs::Ply> (PolygonExporter.cpp:
+178-361) with kvs::Ply's Binary type (Ply.cpp:389-488) for meshes without
+connections (the reference's writer cannot store faces); the vertex records
+are formed by kvsmc_write_ply's kernel.  The reference's writer aborts while
+freeing its element tables after the file is closed (PlyFile.cpp:1345-1366:
+the never-described face element's property array); the file it leaves is
+complete, and that file is what this writer reproduces.
 """
 import numpy as np
 
@@ -96,6 +104,116 @@ class PolygonExporterStl:
         k = np.ascontiguousarray(m.connections(), np.uint32)
         st = ctx.lib.kvsmc_write_stl_host(ctx.handle, str(filename).encode(), _mode(m), c.ctypes.data, c.size,
                                           n.ctypes.data, n.size, k.ctypes.data if k.size else None, k.size)
+        if st:
+            message_error(f"libkvsmc: {_abi.status_string(st)}: {ctx.lib.kvsmc_last_error(ctx.handle).decode()}")
+            self._success = False
+            return False
+        return True
+
+
+# ------------------------------------------------------------------ PLY
+
+def ply_modes(polygon):
+    """(colour mode, normal mode) of kvsmc_write_ply for a connection-less
+    triangle mesh, as PolygonExporter<kvs::Ply>::exec (PolygonExporter.cpp:
+    208-357) forms the vertex colours and normals; raises ValueError where the
+    reference gives no defined output."""
+    if polygon.numberOfConnections() > 0:
+        raise ValueError("meshes with connections: the reference's PLY writer stores face indices through a "
+                         "null pointer (Ply.cpp:470-480)")
+    ncol = polygon.colors().size
+    if ncol == 0:
+        cm = 0
+    elif ncol == 3:
+        cm = 1                                     # the single colour on every vertex (:208-219)
+    elif polygon.colorType() == PolygonObject.VertexColor:
+        cm = 2                                     # the vertex colours as they are (:302-305)
+    else:
+        raise ValueError("per-polygon colours: the reference sets only the red channel of the averaged vertex "
+                         "colours and leaves green and blue uninitialised (PolygonExporter.cpp:254-258)")
+    if polygon.normals().size == 0:
+        nm = 0
+    elif polygon.normalType() == PolygonObject.PolygonNormal:
+        nm = 1                                     # averaged over connections, of which there are none: zeros
+    else:
+        nm = 2                                     # the vertex normals as they are (:350-353)
+    return cm, nm
+
+
+def write_ply_device(ctx, path, d_coords, nvertices, d_colors, color_mode, d_normals, normal_mode):
+    """kvsmc_write_ply: the binary PLY file of a device mesh (device pointers as integers)."""
+    ctx.check(ctx.lib.kvsmc_write_ply(ctx.handle, str(path).encode(), d_coords, int(nvertices), d_colors or None,
+                                      int(color_mode), d_normals or None, int(normal_mode)), "write_ply")
+
+
+class PolygonExporterPly:
+    """kvs::PolygonExporter<kvs::Ply>: exec(polygon) keeps the mesh, write()
+    serialises it (binary, little endian) on the GPU."""
+
+    def __init__(self, polygon=None, context=None):
+        self._success = True
+        self._file_type = ASCII          # kvs::Ply() (Ply.cpp:96-103)
+        self._mesh = None
+        self._ctx = context
+        if polygon is not None:
+            self.exec(polygon)
+
+    def isSuccess(self):
+        return self._success
+
+    def isFailure(self):
+        return not self._success
+
+    def setFileType(self, file_type):
+        self._file_type = BINARY if file_type in (BINARY, "binary", "Binary") else ASCII
+
+    def fileType(self):
+        return self._file_type
+
+    def exec(self, obj):
+        """PolygonExporter<kvs::Ply>::exec (PolygonExporter.cpp:178-200)."""
+        self._success = True
+        if obj is None:
+            self._success = False
+            message_error("Input object is NULL.")
+            return None
+        if not isinstance(obj, PolygonObject):
+            self._success = False
+            message_error("Input object is not polygon object.")
+            return None
+        if obj.polygonType() != PolygonObject.Triangle:
+            self._success = False
+            message_error("Input object is not triangle polygon.")
+            return None
+        self._mesh = obj
+        return self
+
+    def write(self, filename):
+        """Ply::write (Ply.cpp:389-488) with the Binary file type."""
+        if self._mesh is None:
+            message_error("No polygon object to write.")
+            return False
+        if self._file_type != BINARY:
+            message_error("ASCII PLY is not provided; setFileType('binary').")
+            return False
+        m = self._mesh
+        try:
+            cm, nm = ply_modes(m)
+        except ValueError as e:
+            message_error(f"PLY: {e}")
+            self._success = False
+            return False
+        ctx = self._ctx or default_context()
+        c = np.ascontiguousarray(m.coords(), np.float32)
+        k = np.ascontiguousarray(m.colors(), np.uint8)
+        n = np.ascontiguousarray(m.normals(), np.float32)
+        nv = c.size // 3
+        if (cm == 2 and k.size < 3 * nv) or (nm == 2 and n.size < 3 * nv):
+            message_error("PLY: fewer vertex colours / normals than vertices")
+            self._success = False
+            return False
+        st = ctx.lib.kvsmc_write_ply_host(ctx.handle, str(filename).encode(), c.ctypes.data, nv,
+                                          k.ctypes.data if cm else None, cm, n.ctypes.data if nm == 2 else None, nm)
         if st:
             message_error(f"libkvsmc: {_abi.status_string(st)}: {ctx.lib.kvsmc_last_error(ctx.handle).decode()}")
             self._success = False

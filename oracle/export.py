@@ -46,3 +46,37 @@ def stl_binary(coords, normals, connections, normal_type):
     rec["n"] = n
     rec["c"] = c[:count]
     return bytes(header) + rec.tobytes()
+
+
+def ply_binary(coords, colors, normals, color_type="polygon", normal_type="polygon"):
+    """PolygonExporter<kvs::Ply>::exec (PolygonExporter.cpp:178-361) + Ply::write
+    (Ply.cpp:389-488, binary little endian; header PlyFile.cpp:399-460) of a
+    triangle mesh without connections, as bytes: vertex colours = the single
+    colour repeated (3 colour bytes) or the vertex colours (VertexColor);
+    normals = zeros for PolygonNormal (averaged over connections, none here),
+    the vertex normals for VertexNormal; 'element face 0' (faces are counted
+    only from connections)."""
+    c = np.asarray(coords, np.float32).reshape(-1, 3)
+    k = np.asarray(colors, np.uint8).reshape(-1)
+    n = np.asarray(normals, np.float32).reshape(-1)
+    nv = c.shape[0]
+    has_c, has_n = k.size > 0, n.size > 0
+    head = "ply\nformat binary_little_endian 1.0\nelement vertex %d\n" % nv
+    head += "property float x\nproperty float y\nproperty float z\n"
+    if has_c:
+        head += "property uchar red\nproperty uchar green\nproperty uchar blue\n"
+    if has_n:
+        head += "property float nx\nproperty float ny\nproperty float nz\n"
+    head += "element face 0\nend_header\n"
+    fields = [("xyz", "<f4", (3,))]
+    if has_c:
+        fields.append(("rgb", "u1", (3,)))
+    if has_n:
+        fields.append(("n", "<f4", (3,)))
+    rec = np.zeros(nv, np.dtype(fields))
+    rec["xyz"] = c
+    if has_c:
+        rec["rgb"] = np.broadcast_to(k[:3], (nv, 3)) if k.size == 3 else k.reshape(-1, 3)[:nv]
+    if has_n:
+        rec["n"] = n.reshape(-1, 3)[:nv] if normal_type == "vertex" else 0.0
+    return head.encode() + rec.tobytes()

@@ -101,6 +101,9 @@ def lib():
             C.c_int, C.c_int, C.c_int, C.c_void_p, C.c_ulonglong, C.c_void_p, C.c_void_p, C.c_ulonglong,
             C.c_void_p, C.c_int, C.c_double, C.c_double, C.c_int, C.c_int, C.c_float, C.c_float,
             C.POINTER(_Result)]
+        _lib.kvsref_write_ply.restype = C.c_int
+        _lib.kvsref_write_ply.argtypes = [C.c_void_p, C.c_ulonglong, C.c_void_p, C.c_ulonglong, C.c_void_p,
+                                          C.c_ulonglong, C.c_int, C.c_int, C.c_char_p]
         _lib.kvsref_free.argtypes = [C.POINTER(_Result)]
         _lib.kvsref_hydrogen.argtypes = [C.c_uint, C.c_void_p]
         _lib.kvsref_default_colormap.argtypes = [C.c_int, C.c_void_p]
@@ -319,3 +322,17 @@ def color_at(resolution, tf_min, tf_max, value):
     rgb = np.zeros(3, np.uint8)
     lib().kvsref_color_at(resolution, tf_min, tf_max, value, rgb.ctypes.data)
     return rgb
+
+
+def write_ply(path, coords, colors, normals, color_type="polygon", normal_type="polygon"):
+    """The reference PolygonExporter<kvs::Ply> + Ply::write (Binary) of a
+    connection-less triangle mesh; returns the file's bytes."""
+    c = np.ascontiguousarray(coords, np.float32).reshape(-1)
+    k = np.ascontiguousarray(colors, np.uint8).reshape(-1)
+    n = np.ascontiguousarray(normals, np.float32).reshape(-1)
+    st = lib().kvsref_write_ply(c.ctypes.data, c.size, k.ctypes.data if k.size else None, k.size,
+                                n.ctypes.data if n.size else None, n.size, 0 if color_type == "vertex" else 1,
+                                0 if normal_type == "vertex" else 1, str(path).encode())
+    if st != 0:
+        raise RuntimeError(f"kvsref_write_ply failed ({st})")
+    return open(path, "rb").read()

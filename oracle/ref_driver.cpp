@@ -19,6 +19,7 @@
 #include <kvs/Isosurface>
 #include <kvs/PolygonExporter>
 #include <kvs/Stl>
+#include <kvs/Ply>
 #include <kvs/AVSField>
 #include <kvs/SlicePlane>
 #include <kvs/TransferFunction>
@@ -416,6 +417,31 @@ int kvsref_marching_cubes_stl(
     delete mc;
     delete vol;
     return rc;
+}
+
+/*
+ * kvs::PolygonExporter<kvs::Ply> (PolygonExporter.cpp:178-361) + Ply::write
+ * with the Binary file type (Ply.cpp:389-488) of a PolygonObject built from
+ * raw arrays: coords (3 per vertex), colors (ncolors bytes: 3 = one colour),
+ * normals, connections (may be empty), color_type / normal_type as
+ * kvs::PolygonObject's enums (0 vertex, 1 polygon).  Returns 0 when written,
+ * -2 when the exporter failed.
+ */
+int kvsref_write_ply( const float* coords, unsigned long long ncoords, const unsigned char* colors,
+                      unsigned long long ncolors, const float* normals, unsigned long long nnormals,
+                      int color_type, int normal_type, const char* path )
+{
+    kvs::PolygonObject poly;
+    poly.setPolygonType( kvs::PolygonObject::Triangle );
+    poly.setColorType( color_type == 0 ? kvs::PolygonObject::VertexColor : kvs::PolygonObject::PolygonColor );
+    poly.setNormalType( normal_type == 0 ? kvs::PolygonObject::VertexNormal : kvs::PolygonObject::PolygonNormal );
+    poly.setCoords( kvs::ValueArray<kvs::Real32>( coords, ncoords ) );
+    if ( ncolors ) poly.setColors( kvs::ValueArray<kvs::UInt8>( colors, ncolors ) );
+    if ( nnormals ) poly.setNormals( kvs::ValueArray<kvs::Real32>( normals, nnormals ) );
+    kvs::PolygonExporter<kvs::Ply> exporter( &poly );
+    if ( !exporter.kvs::ExporterBase::isSuccess() ) return -2;
+    exporter.setFileType( kvs::Ply::Binary );
+    return exporter.write( path ) ? 0 : -3;
 }
 
 /*

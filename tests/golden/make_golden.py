@@ -11,11 +11,12 @@ files written by the reference PolygonExporter<kvs::Stl> in tests/golden/stl.npz
 (MarchingTetrahedra / Hexahedra / Pyramid / Prism, directly and through
 kvs::Isosurface) in tests/golden/cells.npz (tests/golden/cells.json), and
 kvs::SlicePlane on unstructured volumes in tests/golden/slice_cells.npz
-(tests/golden/slice_cells.json).  The reference
+(tests/golden/slice_cells.json), and binary PLY files written by the reference
+PolygonExporter<kvs::Ply> in tests/golden/ply.npz (tests/golden/ply.json).  The reference
 ships no tests or golden vectors of its own, so these fixtures pin the oracle
 restatement and the CUDA path on hosts where the reference is absent.
 
-    python tests/golden/make_golden.py [marching_cubes] [isosurface] [stl] [slice] [cells] [slice_cells]
+    python tests/golden/make_golden.py [marching_cubes] [isosurface] [stl] [slice] [cells] [slice_cells] [ply]
         (default: all)
 """
 import json
@@ -347,10 +348,67 @@ def write_slice_cells():
     print(f"{len(manifest)} slice_cells cases")
 
 
+_PLY_CHILD = """
+import sys
+sys.path.insert(0, sys.argv[1])
+import numpy as np
+from oracle import ref
+d = np.load(sys.argv[2])
+ref.write_ply(sys.argv[3], d["coords"], d["colors"], d["normals"], str(d["color_type"]), str(d["normal_type"]))
+"""
+
+
+def ply_cases():
+    """(name, coords, colors, normals, color_type, normal_type)"""
+    rng = np.random.default_rng(91)
+    blob = ref.marching_cubes(cases()[1][1], 0.45)          # a duplicated marching-cubes mesh, one colour
+    sl = ref.slice_plane(ref.hydrogen(16), coefficients=(0.3, -0.5, 0.8, -4.0))   # vertex colours
+    nv = 300
+    return [
+        ("mc_dup", blob["coords"], blob["colors"], blob["normals"], "polygon", "polygon"),
+        ("slice", sl["coords"], sl["colors"], sl["normals"], "vertex", "polygon"),
+        ("vertex_normals", rng.standard_normal(3 * nv).astype(np.float32), rng.integers(0, 256, 3 * nv).astype(np.uint8),
+         rng.standard_normal(3 * nv).astype(np.float32), "vertex", "vertex"),
+        ("bare", rng.standard_normal(3 * nv).astype(np.float32), np.zeros(0, np.uint8), np.zeros(0, np.float32),
+         "polygon", "polygon"),
+        ("one_colour_no_normals", rng.standard_normal(3 * nv).astype(np.float32), np.array([7, 8, 9], np.uint8),
+         np.zeros(0, np.float32), "polygon", "polygon"),
+        ("empty", np.zeros(0, np.float32), np.zeros(0, np.uint8), np.zeros(0, np.float32), "polygon", "polygon"),
+    ]
+
+
+def write_ply_fixtures():
+    """The reference writer aborts while freeing its tables after closing the
+    file (PlyFile.cpp:1345-1366), so each file is written by a child process
+    and read back from disk."""
+    import subprocess
+    import tempfile
+    arrays, manifest = {}, []
+    with tempfile.TemporaryDirectory() as tmp:
+        for name, c, k, n, ct, nt in ply_cases():
+            inp = os.path.join(tmp, name + ".npz")
+            out = os.path.join(tmp, name + ".ply")
+            np.savez(inp, coords=c, colors=k, normals=n, color_type=ct, normal_type=nt)
+            r = subprocess.run([sys.executable, "-c", _PLY_CHILD, ROOT, inp, out], capture_output=True)
+            data = np.frombuffer(open(out, "rb").read(), np.uint8)
+            arrays[f"{name}__coords"] = c
+            arrays[f"{name}__colors"] = k
+            arrays[f"{name}__normals"] = n
+            arrays[f"{name}__file"] = data
+            manifest.append(dict(case=name, color_type=ct, normal_type=nt, bytes=int(data.size),
+                                 child_status=r.returncode))
+    np.savez_compressed(os.path.join(HERE, "ply.npz"), **arrays)
+    with open(os.path.join(HERE, "ply.json"), "w") as f:
+        json.dump(manifest, f, indent=0)
+    print(f"{len(manifest)} ply cases")
+
+
 def main():
     if not ref.available():
         ref.build()
-    parts = sys.argv[1:] or ["marching_cubes", "isosurface", "stl", "slice", "cells", "slice_cells"]
+    parts = sys.argv[1:] or ["marching_cubes", "isosurface", "stl", "slice", "cells", "slice_cells", "ply"]
+    if "ply" in parts:
+        write_ply_fixtures()
     if "cells" in parts:
         write_cells()
     if "slice_cells" in parts:

@@ -125,3 +125,44 @@ def test_exporter_checks_like_the_reference(kvsmc_ctx, tmp_path, capsys):
     assert not ex.write(str(tmp_path / "a.stl"))          # ASCII is the default file type: not provided
     ex.setFileType("binary")
     assert ex.write(str(tmp_path / "b.stl"))
+
+
+def test_ply_exporter_matches_reference_files(kvsmc_ctx, tmp_path):
+    from kvs_gb300.export import PolygonExporterPly
+
+    from .test_ply_cpu import ply_fixtures, polygon_of
+    man, arr = ply_fixtures()
+    for e in man:
+        ex = PolygonExporterPly(polygon_of(arr, e), context=kvsmc_ctx)
+        ex.setFileType("binary")
+        p = tmp_path / f"{e['case']}.ply"
+        assert ex.write(str(p)), e["case"]
+        assert p.read_bytes() == arr[f"{e['case']}__file"].tobytes(), e["case"]
+
+
+@pytest.mark.parametrize("nv", [1, 255, 256, 257, (1 << 21) + 300])
+def test_ply_records_and_chunks_against_restatement(kvsmc_ctx, tmp_path, nv):
+    """Record tiles (256 vertices), the last partial tile, and the 2^21-vertex
+    file chunks, for every colour / normal mode."""
+    from kvs_gb300.export import write_ply_device
+    rng = np.random.default_rng(nv)
+    c = torch.from_numpy(rng.standard_normal(3 * nv).astype(np.float32)).cuda()
+    k = torch.from_numpy(rng.integers(0, 256, 3 * nv).astype(np.uint8)).cuda()
+    n = torch.from_numpy(rng.standard_normal(3 * nv).astype(np.float32)).cuda()
+    torch.cuda.synchronize()
+    hc, hk, hn = c.cpu().numpy(), k.cpu().numpy(), n.cpu().numpy()
+    for cm, nm in ((0, 0), (1, 1), (2, 1), (2, 2), (1, 0)):
+        p = tmp_path / f"m{cm}{nm}.ply"
+        write_ply_device(kvsmc_ctx, p, c.data_ptr(), nv, k.data_ptr(), cm, n.data_ptr(), nm)
+        colors = hk[:3] if cm == 1 else (hk if cm == 2 else np.zeros(0, np.uint8))
+        normals = hn if nm else np.zeros(0, np.float32)
+        want = E.ply_binary(hc, colors, normals, "vertex" if cm == 2 else "polygon", "vertex" if nm == 2 else "polygon")
+        assert p.read_bytes() == want, (nv, cm, nm)
+        # the records alone, into device memory
+        rec = kvsmc_ctx.lib.kvsmc_ply_record_bytes(cm, nm)
+        out = torch.empty(nv * rec + 16, dtype=torch.uint8, device="cuda")
+        kvsmc_ctx.check(kvsmc_ctx.lib.kvsmc_ply_records(kvsmc_ctx.handle, c.data_ptr(), nv, k.data_ptr(), cm,
+                                                        n.data_ptr(), nm, out.data_ptr()), "ply_records")
+        kvsmc_ctx.synchronize()
+        hl = int(kvsmc_ctx.lib.kvsmc_ply_header(nv, cm, nm, None, 0))
+        assert out[:nv * rec].cpu().numpy().tobytes() == want[hl:], (nv, cm, nm)
