@@ -497,6 +497,14 @@ def tet_grid(n, seed, device):
     return vals, xyz.contiguous(), conn
 
 
+def cells_traffic():
+    """DRAM bytes of one tet160 extraction step from the committed ncu summary."""
+    p = os.path.join(ROOT, "profiles", "cells_tet160.json")
+    if os.path.exists(p):
+        return json.load(open(p)).get("dram_bytes_per_step")
+    return None
+
+
 def run_cells(args, rank, world, local):
     """kvsmc_marching_cells_device on a resident tetrahedral mesh (value), and
     the mapper's host call kvsmc_marching_cells_host from pinned host arrays
@@ -574,11 +582,37 @@ def run_cells(args, rank, world, local):
                      "achieved": round(algo / (ms * 1e-3) / 1e9, 1), "peak": hbm, "peak_kind": peak_kind,
                      "unit": "GB/s", "frac": round(algo / (ms * 1e-3) / 1e9 / hbm, 4),
                      "algorithmic_bytes_per_step": int(algo), "count_ms": round(count_ms, 4),
-                     "emit_ms": round(emit_ms, 4), "traffic": None},
+                     "emit_ms": round(emit_ms, 4), "traffic": cells_traffic()},
         "kernels": {kk: {"launches": vv[0], "ms": round(vv[1], 3)} for kk, vv in prof.items()},
         "gpu_launches": int(launches // max(1, args.steps)), "clocks": clk,
     }
     if not args.no_e2e:
+        # kvs::SlicePlane on the same mesh (kvsmc_slice_cells_host, the
+        # kvs::cuda::SlicePlane call): kernel times from the library's events,
+        # and the whole call from pinned host arrays
+        from kvs_gb300.marching_cubes import TransferFunction
+        from kvs_gb300.slice_plane import slice_cells_host
+        hv0, hx0, hk0 = vals.cpu().numpy(), xyz.cpu().numpy(), conn.cpu().numpy().view(np.uint32)
+        sp = _abi.SliceParams()
+        for i, cf in enumerate((0.31, -0.52, 0.79, -0.31 * 80 + 0.52 * 80 - 0.79 * 80)):
+            sp.coefficients[i] = float(np.float32(cf))
+        table = np.ascontiguousarray(TransferFunction(256).table, np.uint8)
+        sp.tf_min, sp.tf_max, sp.tf_resolution, sp.tf_table = lo, hi, 256, table.ctypes.data
+        for _ in range(2):
+            slice_cells_host(ctx, 0, hv0, hx0, hk0, sp)
+        ctx.profile_enable(True)
+        t0 = time.perf_counter()
+        reps = 5
+        for _ in range(reps):
+            _, _, _, stri = slice_cells_host(ctx, 0, hv0, hx0, hk0, sp)
+        s_ms = (time.perf_counter() - t0) * 1e3 / reps
+        sprof = ctx.profile_read()
+        ctx.profile_enable(False)
+        line["slice"] = {"call": "kvsmc_slice_cells_host, oblique plane (0.31, -0.52, 0.79) through the centre",
+                         "triangles": int(stri), "e2e_ms": round(s_ms, 3),
+                         "count_ms": round(sprof.get("cells_slice_count", (0, 0.0))[1] / reps, 4),
+                         "emit_ms": round(sprof.get("cells_slice_emit", (0, 0.0))[1] / reps, 4)}
+        del hv0, hx0, hk0
         hv = torch.empty(vals.shape, dtype=vals.dtype, pin_memory=True)
         hx = torch.empty(xyz.shape, dtype=xyz.dtype, pin_memory=True)
         hk = torch.empty(conn.shape, dtype=conn.dtype, pin_memory=True)
