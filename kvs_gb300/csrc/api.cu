@@ -735,20 +735,35 @@ static kvsmc_status arena_outputs(kvsmc_context* ctx, std::vector<Item*>& its)
     return KVSMC_OK;
 }
 
+// Allocate each item's host arrays through the callback (once per item).
+static kvsmc_status host_alloc(kvsmc_context* ctx, std::vector<Item*>& its, const Item* first_item,
+                               kvsmc_host_alloc_fn alloc, void* user)
+{
+    for (Item* it : its) {
+        if (it->h_coords || it->h_normals || it->h_conn) continue;
+        const int32_t base = 3 * (int32_t)(it - first_item);
+        const kvsmc_sizes& s = it->sizes;
+        if (s.ncoords && !(it->h_coords = alloc(user, base + 0, s.ncoords)))
+            return fail(ctx, KVSMC_ERR_OUT_OF_MEMORY, "host alloc (coords)");
+        if (s.nnormals && !(it->h_normals = alloc(user, base + 1, s.nnormals)))
+            return fail(ctx, KVSMC_ERR_OUT_OF_MEMORY, "host alloc (normals)");
+        if (s.nconnections && !(it->h_conn = alloc(user, base + 2, s.nconnections)))
+            return fail(ctx, KVSMC_ERR_OUT_OF_MEMORY, "host alloc (connections)");
+    }
+    return KVSMC_OK;
+}
+
 // Allocate each item's host arrays through the callback and copy them back.
 static kvsmc_status copy_back(kvsmc_context* ctx, std::vector<Item*>& its, const Item* first_item,
                               kvsmc_host_alloc_fn alloc, void* user)
 {
+    kvsmc_status st = host_alloc(ctx, its, first_item, alloc, user);
+    if (st) return st;
     for (Item* it : its) {
-        const int32_t base = 3 * (int32_t)(it - first_item);
         const kvsmc_sizes& s = it->sizes;
-        void* hc = nullptr;
-        void* hn = nullptr;
-        void* hk = nullptr;
-        if (s.ncoords && !(hc = alloc(user, base + 0, s.ncoords))) return fail(ctx, KVSMC_ERR_OUT_OF_MEMORY, "host alloc (coords)");
-        if (s.nnormals && !(hn = alloc(user, base + 1, s.nnormals))) return fail(ctx, KVSMC_ERR_OUT_OF_MEMORY, "host alloc (normals)");
-        if (s.nconnections && !(hk = alloc(user, base + 2, s.nconnections)))
-            return fail(ctx, KVSMC_ERR_OUT_OF_MEMORY, "host alloc (connections)");
+        void* hc = it->h_coords;
+        void* hn = it->h_normals;
+        void* hk = it->h_conn;
         if (hc) KVSMC_CUDA(ctx, cudaMemcpyAsync(hc, it->d_coords, s.ncoords * 4, cudaMemcpyDeviceToHost, ctx->stream));
         if (hn) KVSMC_CUDA(ctx, cudaMemcpyAsync(hn, it->d_normals, s.nnormals * 4, cudaMemcpyDeviceToHost, ctx->stream));
         if (hk) KVSMC_CUDA(ctx, cudaMemcpyAsync(hk, it->d_conn, s.nconnections * 4, cudaMemcpyDeviceToHost, ctx->stream));

@@ -101,6 +101,9 @@ struct Item {
     uint32_t* d_conn = nullptr;
     uint64_t conn_cap = 0;
     bool emit = false;           // write outputs (false: count only)
+    void* h_coords = nullptr;    // host outputs from the allocator (host calls)
+    void* h_normals = nullptr;
+    void* h_conn = nullptr;
     kvsmc_sizes sizes{};
     kvsmc_status status = KVSMC_OK;
 };
