@@ -1311,6 +1311,28 @@ def run_reference(args, rank, world):
     }
 
 
+def host_cpu():
+    """CPU model, host thread count and the CPU baselines' compiler, for the
+    cpu_baseline entries."""
+    import platform
+    model = platform.machine()
+    try:
+        out = subprocess.run(["lscpu"], capture_output=True, text=True, timeout=10).stdout
+        for ln in out.splitlines():
+            if ln.startswith("Model name:"):
+                model = ln.split(":", 1)[1].strip() + " (" + platform.machine() + ")"
+                break
+    except (OSError, subprocess.SubprocessError):
+        pass
+    try:
+        gcc = subprocess.run(["gcc", "-dumpversion"], capture_output=True, text=True, timeout=10).stdout.strip()
+    except (OSError, subprocess.SubprocessError):
+        gcc = "?"
+    return {"cpu": model, "threads": os.cpu_count(),
+            "compiler": f"gcc {gcc} -O3 -ffp-contract=off (oracle/mc_oracle.c); numpy {np.__version__} "
+                        f"(oracle/*.py restatements)"}
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -1368,6 +1390,8 @@ def main():
             line["cpu_baseline"] = {"value": round(v, 1), "unit": "Mcells/s", "cores": 1, "kind": "port",
                                     "sample": sample + f"; {t:.1f} s on 1 host core; oracle/mc_oracle.c"}
     if rank == 0 and line is not None:
+        if isinstance(line.get("cpu_baseline"), dict):
+            line["cpu_baseline"]["host"] = host_cpu()
         print(json.dumps(line), flush=True)
     if world > 1:
         import torch.distributed as dist
