@@ -54,6 +54,7 @@ __constant__ uint64_t c_pri_tri[CELL_PRISM_CASES] = CELL_PRISM_TRI_INIT;
 __constant__ uint8_t c_pri_edge[CELL_PRISM_EDGES] = CELL_PRISM_EDGE_INIT;
 
 constexpr int kCellThreads = 256;
+constexpr int kCountGroups = 4;    // 32-cell groups per warp step of the count pass
 
 template <int CT> struct CellTraits;
 template <> struct CellTraits<KVSMC_TETRAHEDRA> {
@@ -207,19 +208,21 @@ __global__ void __launch_bounds__(kCellThreads) k_cells_count(CellJob j)
     const unsigned lane = threadIdx.x & 31u;
     const uint64_t warps = (uint64_t)gridDim.x * (kCellThreads / 32);
     const uint64_t groups = (j.ncells + 31) / 32;
-    // two groups per step (their loads in flight together)
-    for (uint64_t g = ((uint64_t)blockIdx.x * (kCellThreads / 32) + (threadIdx.x >> 5)) * 2; g < groups;
-         g += warps * 2) {
-        const uint64_t ca = g * 32 + lane, cb = ca + 32;
-        uint32_t na = 0, nb = 0;
-        uint32_t nodes_a[Tr::kNodes], nodes_b[Tr::kNodes];
-        if (ca < j.ncells) na = Tr::ntri(cell_case<CT, T>(j, ca, nodes_a));
-        if (cb < j.ncells) nb = Tr::ntri(cell_case<CT, T>(j, cb, nodes_b));
-        const uint32_t ta = __reduce_add_sync(0xffffffffu, na);
-        const uint32_t tb = __reduce_add_sync(0xffffffffu, nb);
-        if (lane == 0) {
-            j.tile_counts[g] = ta;
-            if (g + 1 < groups) j.tile_counts[g + 1] = tb;
+    // kCountGroups groups per step (their loads in flight together)
+    constexpr int G = kCountGroups;
+    for (uint64_t g = ((uint64_t)blockIdx.x * (kCellThreads / 32) + (threadIdx.x >> 5)) * G; g < groups;
+         g += warps * G) {
+        uint32_t n[G];
+#pragma unroll
+        for (int q = 0; q < G; ++q) {
+            const uint64_t c = (g + q) * 32 + lane;
+            uint32_t nodes[Tr::kNodes];
+            n[q] = c < j.ncells ? Tr::ntri(cell_case<CT, T>(j, c, nodes)) : 0u;
+        }
+#pragma unroll
+        for (int q = 0; q < G; ++q) {
+            const uint32_t t = __reduce_add_sync(0xffffffffu, n[q]);
+            if (lane == 0 && g + q < groups) j.tile_counts[g + q] = t;
         }
     }
 }
