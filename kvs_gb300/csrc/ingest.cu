@@ -21,6 +21,11 @@
 // (StructuredVolumeObject.cpp:214-226); object coords are the file's or
 // [0, res - 1], and then external coords default to them
 // (StructuredVolumeObject.cpp:193-209, 348-423).
+#include <fcntl.h>
+#include <unistd.h>
+
+#include <atomic>
+#include <thread>
 #include <cerrno>
 #include <cstdio>
 #include <cstdlib>
@@ -369,18 +374,47 @@ __global__ void k_byteswap(uint8_t* p, uint64_t n, int es)
 
 // External binary values (from byte `offset` of the file) streamed into the
 // device rows.
+// Read len bytes at file offset off into dst with pread, split over up to
+// `threads` host threads (page-cache copies run in parallel); false on a
+// short read or an error.
+bool pread_parallel(int fd, uint8_t* dst, size_t len, uint64_t off, unsigned threads)
+{
+    const size_t min_piece = 4u << 20;
+    unsigned t = (unsigned)std::min<size_t>(threads, std::max<size_t>(1, len / min_piece));
+    std::atomic<bool> ok{true};
+    auto part = [&](size_t a, size_t b) {
+        while (a < b) {
+            const ssize_t r = ::pread(fd, dst + a, b - a, (off_t)(off + a));
+            if (r <= 0) { ok = false; return; }
+            a += (size_t)r;
+        }
+    };
+    if (t <= 1) {
+        part(0, len);
+        return ok;
+    }
+    std::vector<std::thread> pool;
+    const size_t step = (len + t - 1) / t;
+    for (unsigned i = 0; i < t; ++i) {
+        const size_t a = std::min(len, i * step), b = std::min(len, a + step);
+        if (a < b) pool.emplace_back(part, a, b);
+    }
+    for (auto& th : pool) th.join();
+    return ok;
+}
+
+// External binary values: chunks of whole rows read into two pinned buffers
+// (each chunk by several threads) and copied into the padded device rows
+// while the next chunk is read.
 kvsmc_status load_binary(kvsmc_context* ctx, const std::string& file, kvsmc_volume* v, long offset = 0)
 {
     const size_t es = dsize(v->view.dtype);
     const size_t row = (size_t)v->view.nx * es;
     const uint64_t rows = (uint64_t)v->view.ny * v->view.nz;
     const size_t chunk_rows = std::max<size_t>(1, (64u << 20) / std::max<size_t>(row, 1));
-    FILE* f = std::fopen(file.c_str(), "rb");
-    if (!f) return fail(ctx, KVSMC_ERR_INVALID_ARGUMENT, "kvsml: Cannot open '%s'.", file.c_str());
-    if (offset && std::fseek(f, offset, SEEK_SET) != 0) {
-        std::fclose(f);
-        return fail(ctx, KVSMC_ERR_INVALID_ARGUMENT, "Cannot read '%s'.", file.c_str());
-    }
+    const int fd = ::open(file.c_str(), O_RDONLY);
+    if (fd < 0) return fail(ctx, KVSMC_ERR_INVALID_ARGUMENT, "kvsml: Cannot open '%s'.", file.c_str());
+    const unsigned threads = std::max(1u, std::min(8u, std::thread::hardware_concurrency()));
     uint8_t* h[2] = {nullptr, nullptr};
     cudaEvent_t ev[2] = {nullptr, nullptr};
     cudaError_t e = cudaSuccess;
@@ -396,14 +430,17 @@ kvsmc_status load_binary(kvsmc_context* ctx, const std::string& file, kvsmc_volu
         if (k >= 2) e = cudaEventSynchronize(ev[b]);   // its previous copy has left the buffer
         if (e != cudaSuccess) break;
         const uint64_t nr = std::min<uint64_t>(chunk_rows, rows - r0);
-        if (std::fread(h[b], 1, nr * row, f) != nr * row) { short_read = true; break; }
+        if (!pread_parallel(fd, h[b], nr * row, (uint64_t)offset + r0 * row, threads)) {
+            short_read = true;
+            break;
+        }
         e = cudaMemcpy2DAsync(static_cast<uint8_t*>(v->dev) + r0 * v->view.pitch * es, v->view.pitch * es, h[b], row,
                               row, nr, cudaMemcpyHostToDevice, ctx->stream);
         if (e == cudaSuccess) e = cudaEventRecord(ev[b], ctx->stream);
         r0 += nr;
     }
     cudaStreamSynchronize(ctx->stream);
-    std::fclose(f);
+    ::close(fd);
     for (int b = 0; b < 2; ++b) {
         if (h[b]) cudaFreeHost(h[b]);
         if (ev[b]) cudaEventDestroy(ev[b]);
