@@ -343,6 +343,13 @@ kvsmc_status kvsmc_marching_cells_host(kvsmc_context* ctx, kvsmc_cell_type cell_
                                        const uint32_t* connections, uint64_t ncells, double isolevel,
                                        int32_t has_minmax, double min_value, double max_value,
                                        kvsmc_host_alloc_fn alloc, void* user, kvsmc_sizes* sizes);
+/* The volume's bounding box as UnstructuredVolumeObject::updateMinMaxCoords
+ * (UnstructuredVolumeObject.cpp:396-466) folds it, on the GPU: per axis
+ * Math::Min / Math::Max from the first connected node over every connection
+ * (over the nodes when ncells is 0); a NaN coordinate is taken and the next
+ * replaces it, ties keep the later value.  Host arrays in, six floats out. */
+kvsmc_status kvsmc_cells_bounds(kvsmc_context* ctx, kvsmc_cell_type cell_type, const float* coords, uint64_t nnodes,
+                                const uint32_t* connections, uint64_t ncells, float* min_coord, float* max_coord);
 /* The same on DEVICE arrays (values, coords, connections) into caller-provided
  * device outputs (capacities in floats: 9 T coords, 3 T normals); on
  * KVSMC_ERR_CAPACITY nothing is written and *sizes holds the need. */

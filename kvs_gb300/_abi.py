@@ -50,7 +50,7 @@ EXPORTS = [
     "kvsmc_avs_read_info", "kvsmc_volume_load_avs",
     "kvsmc_slice_count", "kvsmc_slice_extract_device", "kvsmc_slice_plane",
     "kvsmc_marching_cells_host", "kvsmc_marching_cells_device", "kvsmc_selftest_cells", "kvsmc_slice_cells_host",
-    "kvsmc_ply_record_bytes", "kvsmc_ply_header", "kvsmc_ply_records", "kvsmc_write_ply", "kvsmc_write_ply_host",
+    "kvsmc_cells_bounds", "kvsmc_ply_record_bytes", "kvsmc_ply_header", "kvsmc_ply_records", "kvsmc_write_ply", "kvsmc_write_ply_host",
 ]
 
 PATH_AUTO = 0      # streaming kernels where eligible
@@ -203,6 +203,7 @@ def load(path=LIB_PATH):
                                                   C.c_double, C.c_double, vp, u64, vp, u64, C.POINTER(Sizes)]),
         "kvsmc_slice_cells_host": (C.c_int, [vp, C.c_int, vp, C.c_int, u64, vp, vp, u64, C.POINTER(SliceParams),
                                              HOST_ALLOC, vp, C.POINTER(u64)]),
+        "kvsmc_cells_bounds": (C.c_int, [vp, C.c_int, vp, u64, vp, u64, vp, vp]),
         "kvsmc_ply_record_bytes": (u32, [i32, i32]),
         "kvsmc_ply_header": (C.c_int64, [u64, i32, i32, C.c_char_p, u64]),
         "kvsmc_ply_records": (C.c_int, [vp, vp, u64, vp, i32, vp, i32, vp]),
@@ -482,6 +483,19 @@ def marching_cubes_host(ctx, values, params):
 
 
 CELL_NODES = (4, 8, 5, 6)   # kvsmc_cell_type: tetrahedra, hexahedra, pyramid, prism
+
+
+def cells_bounds(ctx, cell_type, coords, connections):
+    """kvsmc_cells_bounds: (min float32[3], max float32[3]) of an unstructured volume's nodes."""
+    c = np.ascontiguousarray(coords, np.float32).reshape(-1)
+    k = np.ascontiguousarray(connections, np.uint32).reshape(-1)
+    npc = CELL_NODES[int(cell_type)]
+    lo = np.zeros(3, np.float32)
+    hi = np.zeros(3, np.float32)
+    ctx.check(ctx.lib.kvsmc_cells_bounds(ctx.handle, int(cell_type), c.ctypes.data, c.size // 3,
+                                         k.ctypes.data if k.size else None, k.size // npc, lo.ctypes.data,
+                                         hi.ctypes.data), "kvsmc_cells_bounds")
+    return lo, hi
 
 
 def marching_cells_host(ctx, cell_type, values, coords, connections, isolevel, minmax=None):

@@ -519,6 +519,128 @@ __global__ void __launch_bounds__(kCellThreads) k_cells_minmax_final(CellJob j, 
     }
 }
 
+// ---- bounding box (UnstructuredVolumeObject::updateMinMaxCoords,
+// UnstructuredVolumeObject.cpp:396-466): per axis the fold
+// Min(cur, x) = cur < x ? cur : x (Max alike) over the sequence
+// [conn[0], conn[0], conn[1], ...] of node coordinates (the nodes in order
+// when there are no connections), from its first element.  A NaN x is
+// taken and the next element replaces it, ties keep the later element.  So
+// the result is NaN when the last element is NaN, else the min (max) over
+// the elements after the last NaN, the latest on ties (the sign of a zero).
+
+__device__ __forceinline__ uint64_t bounds_node(const CellJob& j, uint64_t p, bool has_conn)
+{
+    return has_conn ? (p == 0 ? j.conn[0] : j.conn[p - 1]) : p;
+}
+
+__global__ void __launch_bounds__(kCellThreads) k_bounds_last_nan(CellJob j, uint64_t npos, int has_conn,
+                                                                  unsigned long long* last_nan)
+{
+    for (uint64_t p = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; p < npos;
+         p += (uint64_t)gridDim.x * blockDim.x) {
+        const uint64_t n = bounds_node(j, p, has_conn != 0);
+        if (n >= j.nnodes) { atomicExch(j.bad_index, 1); continue; }
+        const float* c = j.coords + 3 * n;
+#pragma unroll
+        for (int ax = 0; ax < 3; ++ax)
+            if (isnan(c[ax])) atomicMax(&last_nan[ax], (unsigned long long)(p + 1));
+    }
+}
+
+struct BoundPart {
+    float mn[3], mx[3];
+    unsigned long long pmn[3], pmx[3];   // position + 1 (0: none)
+};
+
+__device__ __forceinline__ void bound_take(float& v, unsigned long long& pv, float w, unsigned long long pw, bool less)
+{
+    if (pw == 0) return;
+    if (pv == 0 || (less ? w < v : w > v) || (w == v && pw > pv)) { v = w; pv = pw; }
+}
+
+__global__ void __launch_bounds__(kCellThreads) k_bounds_partial(CellJob j, uint64_t npos, int has_conn,
+                                                                 const unsigned long long* last_nan, BoundPart* parts)
+{
+    __shared__ BoundPart sm[kCellThreads];
+    BoundPart b;
+#pragma unroll
+    for (int ax = 0; ax < 3; ++ax) { b.mn[ax] = b.mx[ax] = 0.0f; b.pmn[ax] = b.pmx[ax] = 0; }
+    const uint64_t per = (npos + gridDim.x - 1) / gridDim.x;
+    const uint64_t p0 = (uint64_t)blockIdx.x * per, p1 = p0 + per < npos ? p0 + per : npos;
+    for (uint64_t p = p0 + threadIdx.x; p < p1; p += blockDim.x) {
+        const uint64_t n = bounds_node(j, p, has_conn != 0);
+        if (n >= j.nnodes) continue;
+        const float* c = j.coords + 3 * n;
+#pragma unroll
+        for (int ax = 0; ax < 3; ++ax) {
+            if (p + 1 <= last_nan[ax]) continue;   // at or before the last NaN
+            bound_take(b.mn[ax], b.pmn[ax], c[ax], p + 1, true);
+            bound_take(b.mx[ax], b.pmx[ax], c[ax], p + 1, false);
+        }
+    }
+    sm[threadIdx.x] = b;
+    __syncthreads();
+    for (unsigned st = blockDim.x / 2; st > 0; st >>= 1) {
+        if (threadIdx.x < st) {
+            BoundPart a = sm[threadIdx.x];
+            const BoundPart& o = sm[threadIdx.x + st];
+#pragma unroll
+            for (int ax = 0; ax < 3; ++ax) {
+                bound_take(a.mn[ax], a.pmn[ax], o.mn[ax], o.pmn[ax], true);
+                bound_take(a.mx[ax], a.pmx[ax], o.mx[ax], o.pmx[ax], false);
+            }
+            sm[threadIdx.x] = a;
+        }
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) parts[blockIdx.x] = sm[0];
+}
+
+__global__ void __launch_bounds__(kCellThreads) k_bounds_final(CellJob j, uint64_t npos, int has_conn,
+                                                               const unsigned long long* last_nan,
+                                                               const BoundPart* parts, int nparts, float* out)
+{
+    __shared__ BoundPart sm[kCellThreads];
+    BoundPart b;
+#pragma unroll
+    for (int ax = 0; ax < 3; ++ax) { b.mn[ax] = b.mx[ax] = 0.0f; b.pmn[ax] = b.pmx[ax] = 0; }
+    for (int i = threadIdx.x; i < nparts; i += blockDim.x) {
+#pragma unroll
+        for (int ax = 0; ax < 3; ++ax) {
+            bound_take(b.mn[ax], b.pmn[ax], parts[i].mn[ax], parts[i].pmn[ax], true);
+            bound_take(b.mx[ax], b.pmx[ax], parts[i].mx[ax], parts[i].pmx[ax], false);
+        }
+    }
+    sm[threadIdx.x] = b;
+    __syncthreads();
+    for (unsigned st = blockDim.x / 2; st > 0; st >>= 1) {
+        if (threadIdx.x < st) {
+            BoundPart a = sm[threadIdx.x];
+            const BoundPart& o = sm[threadIdx.x + st];
+#pragma unroll
+            for (int ax = 0; ax < 3; ++ax) {
+                bound_take(a.mn[ax], a.pmn[ax], o.mn[ax], o.pmn[ax], true);
+                bound_take(a.mx[ax], a.pmx[ax], o.mx[ax], o.pmx[ax], false);
+            }
+            sm[threadIdx.x] = a;
+        }
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) {
+        const uint64_t last = bounds_node(j, npos - 1, has_conn != 0);
+#pragma unroll
+        for (int ax = 0; ax < 3; ++ax) {
+            if (last_nan[ax] == npos && last < j.nnodes) {
+                // the last element is a NaN: the fold ends on it
+                out[ax] = out[3 + ax] = j.coords[3 * last + ax];
+            } else {
+                out[ax] = sm[0].mn[ax];
+                out[3 + ax] = sm[0].mx[ax];
+            }
+        }
+    }
+}
+
 // Blocks of 8 warps, one warp per 32-cell group, at most 8 blocks per SM.
 unsigned cell_grid(uint64_t groups, const Launch& L)
 {
@@ -599,6 +721,28 @@ cudaError_t launch_cells_slice_emit(const CellJob& j, const Launch& L)
                       { k_cells_slice_emit<CT, T><<<cell_grid(tiles, L), kCellThreads, 0, L.stream>>>(j); });
     prof_end(L);
     *L.counter += 1;
+    return cudaGetLastError();
+}
+
+size_t cells_bounds_scratch_bytes(int num_sms) { return 64 + (size_t)num_sms * 4 * sizeof(BoundPart); }
+
+cudaError_t launch_cells_bounds(const CellJob& j, bool has_conn, void* scratch, float* d_out, const Launch& L)
+{
+    const uint64_t npos = has_conn ? j.ncells * (uint64_t)(j.cell_type == KVSMC_TETRAHEDRA ? 4 : j.cell_type ==
+                                                           KVSMC_HEXAHEDRA ? 8 : j.cell_type == KVSMC_PYRAMID ? 5 : 6) + 1
+                                   : j.nnodes;
+    if (npos == 0) return cudaSuccess;
+    unsigned long long* last_nan = static_cast<unsigned long long*>(scratch);
+    BoundPart* parts = reinterpret_cast<BoundPart*>(static_cast<char*>(scratch) + 64);
+    const int nb = L.num_sms * 4;
+    cudaError_t e = cudaMemsetAsync(last_nan, 0, 3 * sizeof(unsigned long long), L.stream);
+    if (e != cudaSuccess) return e;
+    prof_begin(L, "cells_bounds");
+    k_bounds_last_nan<<<nb, kCellThreads, 0, L.stream>>>(j, npos, has_conn ? 1 : 0, last_nan);
+    k_bounds_partial<<<nb, kCellThreads, 0, L.stream>>>(j, npos, has_conn ? 1 : 0, last_nan, parts);
+    k_bounds_final<<<1, kCellThreads, 0, L.stream>>>(j, npos, has_conn ? 1 : 0, last_nan, parts, nb, d_out);
+    prof_end(L);
+    *L.counter += 3;
     return cudaGetLastError();
 }
 
@@ -951,6 +1095,61 @@ kvsmc_status kvsmc_slice_cells_host(kvsmc_context* ctx, kvsmc_cell_type cell_typ
     if (e == cudaSuccess) e = cudaMemcpyAsync(hk, j.out_colors, t * 9, cudaMemcpyDeviceToHost, ctx->stream);
     if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
     if (e != cudaSuccess) return done(fail(ctx, KVSMC_ERR_CUDA, "slice cells: %s", cudaGetErrorString(e)));
+    return done(KVSMC_OK);
+}
+
+kvsmc_status kvsmc_cells_bounds(kvsmc_context* ctx, kvsmc_cell_type cell_type, const float* coords, uint64_t nnodes,
+                                const uint32_t* connections, uint64_t ncells, float* min_coord, float* max_coord)
+{
+    using namespace kvsmc_host;
+    if (!ctx || !min_coord || !max_coord) return KVSMC_ERR_INVALID_ARGUMENT;
+    const int npc = nodes_per_cell(cell_type);
+    if (npc == 0) return fail(ctx, KVSMC_ERR_INVALID_ARGUMENT, "cells: unknown cell type %d", (int)cell_type);
+    if (nnodes == 0 || !coords || (ncells && !connections))
+        return fail(ctx, KVSMC_ERR_INVALID_ARGUMENT, "cells: empty or null volume arrays");
+    KVSMC_CUDA(ctx, cudaSetDevice(ctx->device));
+    const size_t bx = align_up(nnodes * 12, 256), bk = align_up(std::max<uint64_t>(1, ncells * npc) * 4, 256);
+    char* d_in = nullptr;
+    auto done = [&](kvsmc_status st) {
+        cudaStreamSynchronize(ctx->stream);
+        cudaFree(d_in);
+        return st;
+    };
+    cudaError_t e = cudaMalloc(&d_in, bx + bk);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(d_in, coords, nnodes * 12, cudaMemcpyHostToDevice, ctx->stream);
+    if (e == cudaSuccess && ncells)
+        e = cudaMemcpyAsync(d_in + bx, connections, ncells * npc * 4, cudaMemcpyHostToDevice, ctx->stream);
+    if (e != cudaSuccess)
+        return done(fail(ctx, e == cudaErrorMemoryAllocation ? KVSMC_ERR_OUT_OF_MEMORY : KVSMC_ERR_CUDA,
+                         "cells bounds: %s", cudaGetErrorString(e)));
+    kvsmc::CellJob j = make_job(cell_type, KVSMC_F32, nullptr, nnodes, reinterpret_cast<const float*>(d_in),
+                                reinterpret_cast<const uint32_t*>(d_in + bx), ncells, 0.0);
+    const size_t bs = align_up(kvsmc::cells_bounds_scratch_bytes(ctx->num_sms), 256);
+    kvsmc_status st = ensure_scratch(ctx, bs + 256);
+    if (st) return done(st);
+    if (!ctx->d_flag) {
+        if ((e = cudaMalloc(&ctx->d_flag, sizeof(int))) != cudaSuccess)
+            return done(fail(ctx, KVSMC_ERR_OUT_OF_MEMORY, "cells bounds: %s", cudaGetErrorString(e)));
+    }
+    j.bad_index = ctx->d_flag;
+    char* base = static_cast<char*>(ctx->scratch);
+    float* d_out = reinterpret_cast<float*>(base + bs);
+    e = cudaMemsetAsync(ctx->d_flag, 0, sizeof(int), ctx->stream);
+    if (e == cudaSuccess) e = kvsmc::launch_cells_bounds(j, ncells > 0, base, d_out, launch_of(ctx));
+    if (e == cudaSuccess) e = cudaMemcpyAsync(ctx->h_small, d_out, 6 * sizeof(float), cudaMemcpyDeviceToHost, ctx->stream);
+    // the six floats fill h_small[0..2]; the flag goes behind them
+    if (e == cudaSuccess) e = cudaMemcpyAsync(ctx->h_small + 4, ctx->d_flag, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
+    if (e != cudaSuccess) return done(fail(ctx, KVSMC_ERR_CUDA, "cells bounds: %s", cudaGetErrorString(e)));
+    int bad = 0;
+    std::memcpy(&bad, ctx->h_small + 4, sizeof(int));
+    if (bad) return done(fail(ctx, KVSMC_ERR_INVALID_ARGUMENT, "cells: a connection index is >= nnodes"));
+    float out[6];
+    std::memcpy(out, ctx->h_small, sizeof out);
+    for (int k = 0; k < 3; ++k) {
+        min_coord[k] = out[k];
+        max_coord[k] = out[3 + k];
+    }
     return done(KVSMC_OK);
 }
 

@@ -163,6 +163,9 @@ cudaError_t launch_cells_emit(const CellJob& j, const Launch& L);
 uint64_t cells_tiles(uint64_t ncells);
 cudaError_t launch_cells_slice_count(const CellJob& j, const Launch& L);
 cudaError_t launch_cells_slice_emit(const CellJob& j, const Launch& L);
+// bounding box of the cells' nodes (updateMinMaxCoords' fold), d_out[0..2] min, [3..5] max
+size_t cells_bounds_scratch_bytes(int num_sms);
+cudaError_t launch_cells_bounds(const CellJob& j, bool has_conn, void* scratch, float* d_out, const Launch& L);
 // min/max over values[0] and the connected nodes' values, as doubles in d_out[0..1]
 size_t cells_minmax_scratch_bytes(int num_sms);
 cudaError_t launch_cells_minmax(const CellJob& j, void* scratch, double* d_out, const Launch& L);

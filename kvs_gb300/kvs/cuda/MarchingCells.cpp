@@ -53,6 +53,43 @@ namespace kvs
 namespace cuda
 {
 
+bool DeviceBounds( const kvs::UnstructuredVolumeObject* volume, int cell, int device )
+{
+    kvsmc_status st = KVSMC_OK;
+    kvsmc_context* ctx = DeviceContext( device, &st );
+    if ( !ctx )
+    {
+        kvsMessageError("libkvsmc: %s.", kvsmc_status_string( st ) );
+        return false;
+    }
+    float lo[3], hi[3];
+    st = kvsmc_cells_bounds( ctx, kvsmc_cell_type( cell ), volume->coords().data(), volume->numberOfNodes(),
+                             volume->connections().data(), volume->numberOfCells(), lo, hi );
+    if ( st != KVSMC_OK )
+    {
+        kvsMessageError("libkvsmc: %s: %s", kvsmc_status_string( st ), kvsmc_last_error( ctx ) );
+        return false;
+    }
+    // the cache is mutable in the reference too (MapperBase.cpp:101)
+    auto* v = const_cast<kvs::UnstructuredVolumeObject*>( volume );
+    v->setMinMaxObjectCoords( kvs::Vec3( lo[0], lo[1], lo[2] ), kvs::Vec3( hi[0], hi[1], hi[2] ) );
+    if ( !v->hasMinMaxExternalCoords() )
+    {
+        v->setMinMaxExternalCoords( kvs::Vec3( lo[0], lo[1], lo[2] ), kvs::Vec3( hi[0], hi[1], hi[2] ) );
+    }
+    return true;
+}
+
+} // end of namespace cuda
+
+} // end of namespace kvs
+
+namespace kvs
+{
+
+namespace cuda
+{
+
 MarchingCellsBase::MarchingCellsBase(
     const kvs::TransferFunction& transfer_function,
     const double isolevel,
@@ -126,6 +163,11 @@ bool MarchingCellsBase::mapping( const kvs::UnstructuredVolumeObject* volume, co
         if ( !volume->hasMinMaxValues() ) volume->setMinMaxValues( sizes.min_value, sizes.max_value );
     }
     BaseClass::setRange( volume );
+    if ( !volume->hasMinMaxObjectCoords() && volume->coords().size() > 0 )
+    {
+        // UnstructuredVolumeObject::updateMinMaxCoords' fold on the GPU
+        if ( !DeviceBounds( volume, traits.cell, m_device ) ) return false;
+    }
     BaseClass::setMinMaxCoords( volume, this );
 
     if ( m_duplication || !traits.types_need_duplication )

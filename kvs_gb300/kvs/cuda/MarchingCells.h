@@ -29,6 +29,10 @@ namespace kvs
 namespace cuda
 {
 
+/// UnstructuredVolumeObject::updateMinMaxCoords on the GPU (kvsmc_cells_bounds),
+/// written into the volume's bounding box; false (and a message) on failure.
+bool DeviceBounds( const kvs::UnstructuredVolumeObject* volume, int cell, int device );
+
 /// The body the four mappers share; not a module itself.
 class MarchingCellsBase : public kvs::MapperBase, public kvs::PolygonObject
 {

@@ -25,6 +25,7 @@
 #include <limits>
 
 #include "Context.h"
+#include "MarchingCells.h"
 
 namespace
 {
@@ -225,6 +226,10 @@ bool SlicePlane::mapping_cells( const kvs::UnstructuredVolumeObject* volume )
     }
     BaseClass::attachVolume( volume );
     BaseClass::setRange( volume );
+    if ( cell >= 0 && !volume->hasMinMaxObjectCoords() && volume->coords().size() > 0 )
+    {
+        if ( !kvs::cuda::DeviceBounds( volume, cell, m_device ) ) return false;
+    }
     BaseClass::setMinMaxCoords( volume, this );
     if ( dtype < 0 )
     {

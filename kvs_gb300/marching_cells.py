@@ -156,6 +156,16 @@ class UnstructuredVolumeObject(ObjectBase):
             self.setMinMaxExternalCoords(lo, hi)
 
 
+def set_bounds_on_device(ctx, volume, abi_cell, connections):
+    """UnstructuredVolumeObject::updateMinMaxCoords by kvsmc_cells_bounds."""
+    if volume.coords().size == 0:
+        return
+    lo, hi = _abi.cells_bounds(ctx, abi_cell, volume.coords()[:3 * volume.numberOfNodes()], connections)
+    volume.setMinMaxObjectCoords(lo, hi)
+    if not volume.hasMinMaxExternalCoords():
+        volume.setMinMaxExternalCoords(lo, hi)
+
+
 class _MarchingCells(PolygonObject):
     """Shared body of the four unstructured marching mappers."""
 
@@ -266,9 +276,10 @@ class _MarchingCells(PolygonObject):
             else:
                 lo, hi = f32(volume.minValue()), f32(volume.maxValue())
                 self._tfunc.setRange(lo, hi + f32(1.0) if _equal(float(lo), float(hi)) else hi)
-        # MapperBase::setMinMaxCoords (MapperBase.cpp:92-122)
+        # MapperBase::setMinMaxCoords (MapperBase.cpp:92-122), the volume's
+        # updateMinMaxCoords fold run on the GPU
         if not volume.hasMinMaxObjectCoords():
-            volume.updateMinMaxCoords()
+            set_bounds_on_device(ctx, volume, self.ABI_CELL, conn)
         self.setMinMaxObjectCoords(volume.minObjectCoord(), volume.maxObjectCoord())
         self.setMinMaxExternalCoords(volume.minExternalCoord(), volume.maxExternalCoord())
         if not self.TYPES_NEED_DUPLICATION or self._duplication:

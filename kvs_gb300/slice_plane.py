@@ -17,7 +17,7 @@ other cell types give nothing, as in the reference.
 import numpy as np
 
 from . import _abi
-from .marching_cells import MAPPERS, UnstructuredVolumeObject
+from .marching_cells import MAPPERS, UnstructuredVolumeObject, set_bounds_on_device
 from .marching_cubes import (PolygonObject, StructuredVolumeObject, TransferFunction, _equal, default_context,
                              message_error)
 
@@ -113,7 +113,10 @@ class SlicePlane(PolygonObject):
             volume.setMinMaxValues(sizes["min_value"], sizes["max_value"])
         self._set_range(code, volume)
         if not volume.hasMinMaxObjectCoords():
-            volume.updateMinMaxCoords()
+            if mapper is not None:
+                set_bounds_on_device(ctx, volume, mapper.ABI_CELL, conn)
+            else:
+                volume.updateMinMaxCoords()
         self.setMinMaxObjectCoords(volume.minObjectCoord(), volume.maxObjectCoord())
         self.setMinMaxExternalCoords(volume.minExternalCoord(), volume.maxExternalCoord())
         if code is None:

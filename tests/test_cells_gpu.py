@@ -189,3 +189,31 @@ def test_fast_and_exact_vertices_agree_on_adversarial_meshes(kvsmc_ctx):
                 o = ocells.marching_cells(ct, v, xyz, conn, iso, mm)
                 assert same_bits(c, o["coords"]), (ct, dt, mm, first_diff(c, o["coords"]))
                 assert same_bits(n, o["normals"]), (ct, dt, mm)
+
+
+def test_bounds_match_the_fold_on_nans_and_signed_zeros(kvsmc_ctx):
+    """kvsmc_cells_bounds against the restated fold (oracle/cells.py
+    min_max_coords, itself pinned on the reference fixtures): NaN
+    coordinates in the middle, at the very end and at the start, signed
+    zeros tied with each other, with and without connections, and a large
+    mesh."""
+    rng = np.random.default_rng(23)
+    for trial in range(24):
+        ct = trial % 4
+        xyz, conn = cm.random_mesh(ct, 400, 700, seed=trial)
+        if trial % 3 == 0:
+            xyz[rng.choice(400, 5, replace=False), rng.integers(0, 3, 5)] = np.nan
+        if trial % 4 == 1:
+            xyz[:, 1] = np.where(rng.random(400) < 0.5, np.float32(-0.0), np.float32(0.0))
+        if trial % 5 == 2:
+            xyz[conn.reshape(-1)[-1], 2] = np.nan          # the fold ends on a NaN
+        if trial % 7 == 3:
+            xyz[conn.reshape(-1)[0], 0] = np.nan           # the start is a NaN
+        k = conn if trial % 6 != 5 else np.zeros((0, cm.NODES[ct]), np.uint32)
+        lo, hi = _abi.cells_bounds(kvsmc_ctx, ct, xyz, k)
+        wlo, whi = ocells.min_max_coords(xyz, k)
+        assert same_bits(lo, wlo) and same_bits(hi, whi), (trial, lo, wlo, hi, whi)
+    xyz, conn = cm.grid(0, 96, 96, 96, seed=3)
+    lo, hi = _abi.cells_bounds(kvsmc_ctx, 0, xyz, conn)
+    wlo, whi = ocells.min_max_coords(xyz, conn)
+    assert same_bits(lo, wlo) and same_bits(hi, whi)
