@@ -1,17 +1,18 @@
 /*****************************************************************************/
 /**
  *  @file   Isosurface.h
- *  @brief  kvs::cuda::Isosurface -- kvs::Isosurface with its structured-grid
- *          branch on the GPU.
+ *  @brief  kvs::cuda::Isosurface -- kvs::Isosurface with its structured and
+ *          unstructured branches on the GPU.
  *
  *  Same constructors, setIsolevel and exec(ObjectBase*) as the reference
  *  mapper (Source/Core/Visualization/Mapper/Isosurface.h:23-57).  A
  *  structured volume goes to kvs::cuda::MarchingCubes (libkvsmc) where the
  *  reference builds a kvs::MarchingCubes (Isosurface.cpp:176-191); the
- *  arrays are the same bit for bit.  Unstructured volumes go to the
- *  reference's own MarchingTetrahedra / Hexahedra / Pyramid / Prism mappers,
- *  unchanged.  When the GPU mapper fails, exec reports kvsMessageError and
- *  returns nullptr (no CPU fallback).
+ *  arrays are the same bit for bit.  Unstructured volumes go, by cell type,
+ *  to kvs::cuda::MarchingTetrahedra / Hexahedra / Pyramid / Prism where the
+ *  reference builds its own mappers (Isosurface.cpp:193-258).  When the GPU
+ *  mapper fails, exec reports kvsMessageError and returns nullptr (no CPU
+ *  fallback).
  */
 /*****************************************************************************/
 #pragma once
