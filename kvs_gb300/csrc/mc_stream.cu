@@ -453,6 +453,14 @@ __global__ void __launch_bounds__(kStreamThreads, EMIT ? 2 : 3)
     uint32_t PA0[5], PA1[5];   // masks of plane z, this lane's rows (carried from the previous step)
     bool pa_valid = false;
     bool brick_skip = false;   // the current brick is empty
+    // emit: whether this lane's (row, isolevel) unit of step z has triangles,
+    // loaded one step ahead so the load's latency hides behind a step's work
+    const uint32_t uh = lane >> 4, uk = lane & 15u;
+    const bool u_lane = EMIT && uh < (uint32_t)R && uk < (uint32_t)niso && y + uh < cy;
+    auto unit_nonzero = [&](uint32_t zz) -> bool {
+        return u_lane && unit_counts[unit_base + (((uint64_t)zz * cy + y + uh) * wpr + seg) * niso + uk] != 0;
+    };
+    bool next_any = EMIT ? unit_nonzero(z0) : false;
 
     for (uint32_t z = z0; z < z1; ++z) {
         const uint32_t s = z - z0;
@@ -477,13 +485,11 @@ __global__ void __launch_bounds__(kStreamThreads, EMIT ? 2 : 3)
         const float fz = __uint2float_rn(z);
         if (bricks && (s == 0 || z % kBrickPlanes == 0)) brick_skip = brick_empty(z);
         bool skip = brick_skip;
-        if (EMIT && !skip) {
+        if (EMIT) {
             // the count pass found no triangle in this step's units: nothing to emit
-            const uint32_t h = lane >> 4, k = lane & 15u;
-            bool any = false;
-            if (h < (uint32_t)R && k < (uint32_t)niso && y + h < cy)
-                any = unit_counts[unit_base + (((uint64_t)z * cy + y + h) * wpr + seg) * niso + k] != 0;
-            skip = !__any_sync(FULL, any);
+            const bool any = next_any;
+            next_any = z + 1 < z1 ? unit_nonzero(z + 1) : false;
+            if (!skip) skip = !__any_sync(FULL, any);
         }
         if (skip) {
             pa_valid = false;
