@@ -586,6 +586,53 @@ def run_cells(args, rank, world, local):
         "kernels": {kk: {"launches": vv[0], "ms": round(vv[1], 3)} for kk, vv in prof.items()},
         "gpu_launches": int(launches // max(1, args.steps)), "clocks": clk,
     }
+    # a 16-isolevel sweep of the same resident mesh in one call
+    # (kvsmc_marching_cells_sweep_device) against 16 single calls
+    sweep_isos = [10.0 + 5.0 * i for i in range(16)]
+    ns = len(sweep_isos)
+    scap = []
+    for r in sweep_isos:
+        st = call(r, None, None, 0)
+        if st not in (_abi.OK, 6):
+            ctx.check(st, "marching_cells_device")
+        scap.append(max(1, s.ntriangles))
+    sbuf_c = [torch.empty(9 * c, dtype=torch.float32, device="cuda") for c in scap]
+    sbuf_n = [torch.empty(3 * c, dtype=torch.float32, device="cuda") for c in scap]
+    pc = (C.c_void_p * ns)(*[t.data_ptr() for t in sbuf_c])
+    pn = (C.c_void_p * ns)(*[t.data_ptr() for t in sbuf_n])
+    cc = (C.c_uint64 * ns)(*[9 * c for c in scap])
+    cn = (C.c_uint64 * ns)(*[3 * c for c in scap])
+    ssz = (_abi.Sizes * ns)()
+    il = (C.c_double * ns)(*sweep_isos)
+
+    def sweep():
+        ctx.check(ctx.lib.kvsmc_marching_cells_sweep_device(ctx.handle, 0, vals.data_ptr(), 8, nnodes, xyz.data_ptr(),
+                                                            conn.data_ptr(), ncells, il, ns, 1, lo, hi, pc, cc, pn,
+                                                            cn, ssz), "marching_cells_sweep_device")
+
+    def singles():
+        for i, r in enumerate(sweep_isos):
+            ctx.check(call(r, sbuf_c[i].data_ptr(), sbuf_n[i].data_ptr(), scap[i]), "marching_cells_device")
+
+    for run in (sweep, singles):
+        for _ in range(args.warmup):
+            run()
+    torch.cuda.synchronize()
+    sweep_ms = {}
+    for name, run in (("sweep", sweep), ("singles", singles)):
+        e0.record(stream)
+        for _ in range(max(3, args.steps // 5)):
+            run()
+        e1.record(stream)
+        torch.cuda.synchronize()
+        sweep_ms[name] = barrier_max(e0.elapsed_time(e1), world) / max(3, args.steps // 5)
+    line["sweep16"] = {"call": "kvsmc_marching_cells_sweep_device, 16 isolevels 10..85 in one call",
+                       "ms": round(sweep_ms["sweep"], 4),
+                       "mcells_isolevels_per_s": round(ncells * ns / (sweep_ms["sweep"] * 1e-3) / 1e6, 1),
+                       "triangles": int(sum(x.ntriangles for x in ssz)),
+                       "singles_ms": round(sweep_ms["singles"], 4),
+                       "speedup_vs_singles": round(sweep_ms["singles"] / sweep_ms["sweep"], 2)}
+    del sbuf_c, sbuf_n
     if not args.no_e2e:
         # kvs::SlicePlane on the same mesh (kvsmc_slice_cells_host, the
         # kvs::cuda::SlicePlane call): kernel times from the library's events,

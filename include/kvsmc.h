@@ -343,6 +343,21 @@ kvsmc_status kvsmc_marching_cells_host(kvsmc_context* ctx, kvsmc_cell_type cell_
                                        const uint32_t* connections, uint64_t ncells, double isolevel,
                                        int32_t has_minmax, double min_value, double max_value,
                                        kvsmc_host_alloc_fn alloc, void* user, kvsmc_sizes* sizes);
+/* An isolevel sweep of one unstructured volume on DEVICE arrays: niso (at
+ * most 64) extractions, each the same as kvsmc_marching_cells_device at its
+ * isolevel, sharing one count pass (connections and node values read once for
+ * all isolevels), one scan and one emit launch.  out_coords[k] /
+ * out_normals[k] with capacities coords_capacity[k] / normals_capacity[k]
+ * (floats) receive isolevel k's triangles; sizes[k] its counts (all get the
+ * min/max used).  If any isolevel's triangles do not fit, nothing is written
+ * and the call returns KVSMC_ERR_CAPACITY with every sizes[k] filled. */
+kvsmc_status kvsmc_marching_cells_sweep_device(kvsmc_context* ctx, kvsmc_cell_type cell_type, const void* d_values,
+                                               kvsmc_dtype dtype, uint64_t nnodes, const float* d_coords,
+                                               const uint32_t* d_connections, uint64_t ncells,
+                                               const double* isolevels, int32_t niso, int32_t has_minmax,
+                                               double min_value, double max_value, float* const* d_out_coords,
+                                               const uint64_t* coords_capacity, float* const* d_out_normals,
+                                               const uint64_t* normals_capacity, kvsmc_sizes* sizes);
 /* The volume's bounding box as UnstructuredVolumeObject::updateMinMaxCoords
  * (UnstructuredVolumeObject.cpp:396-466) folds it, on the GPU: per axis
  * Math::Min / Math::Max from the first connected node over every connection

@@ -50,7 +50,7 @@ EXPORTS = [
     "kvsmc_avs_read_info", "kvsmc_volume_load_avs",
     "kvsmc_slice_count", "kvsmc_slice_extract_device", "kvsmc_slice_plane",
     "kvsmc_marching_cells_host", "kvsmc_marching_cells_device", "kvsmc_selftest_cells", "kvsmc_slice_cells_host",
-    "kvsmc_cells_bounds", "kvsmc_ply_record_bytes", "kvsmc_ply_header", "kvsmc_ply_records", "kvsmc_write_ply", "kvsmc_write_ply_host",
+    "kvsmc_cells_bounds", "kvsmc_marching_cells_sweep_device", "kvsmc_ply_record_bytes", "kvsmc_ply_header", "kvsmc_ply_records", "kvsmc_write_ply", "kvsmc_write_ply_host",
 ]
 
 PATH_AUTO = 0      # streaming kernels where eligible
@@ -204,6 +204,10 @@ def load(path=LIB_PATH):
         "kvsmc_slice_cells_host": (C.c_int, [vp, C.c_int, vp, C.c_int, u64, vp, vp, u64, C.POINTER(SliceParams),
                                              HOST_ALLOC, vp, C.POINTER(u64)]),
         "kvsmc_cells_bounds": (C.c_int, [vp, C.c_int, vp, u64, vp, u64, vp, vp]),
+        "kvsmc_marching_cells_sweep_device": (C.c_int, [vp, C.c_int, vp, C.c_int, u64, vp, vp, u64,
+                                                        C.POINTER(C.c_double), i32, i32, C.c_double, C.c_double,
+                                                        C.POINTER(vp), C.POINTER(u64), C.POINTER(vp),
+                                                        C.POINTER(u64), C.POINTER(Sizes)]),
         "kvsmc_ply_record_bytes": (u32, [i32, i32]),
         "kvsmc_ply_header": (C.c_int64, [u64, i32, i32, C.c_char_p, u64]),
         "kvsmc_ply_records": (C.c_int, [vp, vp, u64, vp, i32, vp, i32, vp]),

@@ -28,6 +28,7 @@
 
 #include <algorithm>
 #include <cstring>
+#include <vector>
 
 #include "cell_tables.h"
 #include "context.h"
@@ -124,23 +125,21 @@ __device__ __forceinline__ void cell_nodes(const CellJob& j, uint64_t cell, uint
 // The case: bit k iff double(value of local node k) > isolevel, decided
 // without FP64 for float and up-to-32-bit integer values (Classifier).
 template <int CT, typename T>
-__device__ __forceinline__ unsigned cell_case(const CellJob& j, uint64_t cell, uint32_t* nodes)
+__device__ __forceinline__ unsigned case_of(const Classifier& cls, double iso, const T* v)
 {
     using Tr = CellTraits<CT>;
-    cell_nodes<CT>(j, cell, nodes);
-    const T* vals = static_cast<const T*>(j.values);
     unsigned c = 0;
 #pragma unroll
-    for (int k = 0; k < Tr::kNodes; ++k) c |= above(j.cls, __ldg(vals + nodes[k])) ? (1u << k) : 0u;
+    for (int k = 0; k < Tr::kNodes; ++k) c |= above(cls, v[k]) ? (1u << k) : 0u;
     if (CT == KVSMC_PYRAMID && (c == 10u || c == 11u || c == 20u || c == 21u)) {
         // x / 4 as x * 0.25: the same correctly rounded result
-        const double v1 = to_double(vals[nodes[1]]), v2 = to_double(vals[nodes[2]]);
-        const double v3 = to_double(vals[nodes[3]]), v4 = to_double(vals[nodes[4]]);
+        const double v1 = to_double(v[1]), v2 = to_double(v[2]);
+        const double v3 = to_double(v[3]), v4 = to_double(v[4]);
         const double A = __dmul_rn(__dadd_rn(__dadd_rn(__dadd_rn(v1, v2), v3), v4), 0.25);
         const double B = __dmul_rn(__dsub_rn(__dadd_rn(__dadd_rn(-v1, v2), v3), v4), 0.25);
         const double C = __dmul_rn(__dadd_rn(__dadd_rn(__dsub_rn(-v1, v2), v3), v4), 0.25);
         const double D = __dmul_rn(__dsub_rn(__dadd_rn(__dsub_rn(v1, v2), v3), v4), 0.25);
-        const double E = __dadd_rn(__dmul_rn(__dsub_rn(j.iso, A), D), __dmul_rn(B, C));
+        const double E = __dadd_rn(__dmul_rn(__dsub_rn(iso, A), D), __dmul_rn(B, C));
         if (c == 10u && E < 0) c = 32u;
         else if (c == 11u && E >= 0) c = 33u;
         else if (c == 20u && E >= 0) c = 34u;
@@ -149,16 +148,35 @@ __device__ __forceinline__ unsigned cell_case(const CellJob& j, uint64_t cell, u
     return c;
 }
 
+// The cell's nodes and their values.
+template <int CT, typename T>
+__device__ __forceinline__ void cell_load(const CellJob& j, uint64_t cell, uint32_t* nodes, T* v)
+{
+    using Tr = CellTraits<CT>;
+    cell_nodes<CT>(j, cell, nodes);
+    const T* vals = static_cast<const T*>(j.values);
+#pragma unroll
+    for (int k = 0; k < Tr::kNodes; ++k) v[k] = __ldg(vals + nodes[k]);
+}
+
+template <int CT, typename T>
+__device__ __forceinline__ unsigned cell_case(const CellJob& j, uint64_t cell, uint32_t* nodes)
+{
+    T v[CellTraits<CT>::kNodes];
+    cell_load<CT, T>(j, cell, nodes, v);
+    return case_of<CT, T>(j.cls, j.iso, v);
+}
+
 // The reference's FP64 sequence, out of line (it runs for the vertices the
 // FP32 certificate cannot decide, and for 32/64-bit integer and double values).
 template <typename T>
-static __device__ __noinline__ float3 cell_vertex_exact(const CellJob& j, uint32_t n0, uint32_t n1)
+static __device__ __noinline__ float3 cell_vertex_exact(const CellJob& j, double iso, uint32_t n0, uint32_t n1)
 {
     const double lo = j.vmin, hi = j.vmax;
     double v0 = dval<T>(j.values, n0), v1 = dval<T>(j.values, n1);
     v0 = v0 <= lo ? lo : (v0 <= hi ? v0 : hi);   // Math::Clamp
     v1 = v1 <= lo ? lo : (v1 <= hi ? v1 : hi);
-    const double q = __ddiv_rn(__dsub_rn(j.iso, v0), __dsub_rn(v1, v0));
+    const double q = __ddiv_rn(__dsub_rn(iso, v0), __dsub_rn(v1, v0));
     const double r = q < 0.0 ? -q : q;
     const float* c0 = j.coords + 3 * (uint64_t)n0;
     const float* c1 = j.coords + 3 * (uint64_t)n1;
@@ -179,13 +197,13 @@ template <> struct CellFast<uint16_t> { static constexpr bool value = true; };
 
 // interpolate_vertex: the FP32 certificate (cell_ratio / cell_axis), else FP64.
 template <typename T>
-__device__ __forceinline__ float3 cell_vertex(const CellJob& j, uint32_t n0, uint32_t n1)
+__device__ __forceinline__ float3 cell_vertex(const CellJob& j, const FastIso& f, double iso, uint32_t n0, uint32_t n1)
 {
     if constexpr (CellFast<T>::value) {
         const T* vals = static_cast<const T*>(j.values);
-        const float v0 = clampf_ref((float)__ldg(vals + n0), j.f.vmin_f, j.f.vmax_f);
-        const float v1 = clampf_ref((float)__ldg(vals + n1), j.f.vmin_f, j.f.vmax_f);
-        const CellRatio c = cell_ratio(v0, v1, j.f);
+        const float v0 = clampf_ref((float)__ldg(vals + n0), f.vmin_f, f.vmax_f);
+        const float v1 = clampf_ref((float)__ldg(vals + n1), f.vmin_f, f.vmax_f);
+        const CellRatio c = cell_ratio(v0, v1, f);
         const float* c0 = j.coords + 3 * (uint64_t)n0;
         const float* c1 = j.coords + 3 * (uint64_t)n1;
         float3 o;
@@ -194,7 +212,7 @@ __device__ __forceinline__ float3 cell_vertex(const CellJob& j, uint32_t n0, uin
         const bool oz = cell_axis(c, __ldg(c0 + 2), __ldg(c1 + 2), o.z);
         if (ox && oy && oz) return o;
     }
-    return cell_vertex_exact<T>(j, n0, n1);
+    return cell_vertex_exact<T>(j, iso, n0, n1);
 }
 
 // Both passes work on groups of 32 consecutive cells, one warp per group
@@ -287,7 +305,7 @@ __global__ void __launch_bounds__(kCellThreads) k_cells_emit(CellJob j)
 #pragma unroll
             for (int s = 0; s < 3; ++s) {
                 const unsigned ed = Tr::edge((int)((pk >> (4 * s)) & 15u));
-                v[s] = cell_vertex<T>(j, own_nodes[ed & 15u], own_nodes[ed >> 4]);
+                v[s] = cell_vertex<T>(j, j.f, j.iso, own_nodes[ed & 15u], own_nodes[ed >> 4]);
             }
             float* o = j.out_coords + 9 * t;
             o[0] = v[0].x; o[1] = v[0].y; o[2] = v[0].z;
@@ -641,6 +659,120 @@ __global__ void __launch_bounds__(kCellThreads) k_bounds_final(CellJob j, uint64
     }
 }
 
+// ---- isolevel sweep: one count pass classifies every cell for all the
+// isolevels (its connections and node values read once), one scan over the
+// isolevels' group counts, one emit pass over (isolevel, 32 groups) items.
+
+template <int CT, typename T>
+__global__ void __launch_bounds__(kCellThreads) k_cells_sweep_count(CellJob j)
+{
+    using Tr = CellTraits<CT>;
+    __shared__ CellIso s_iso[kCellSweepMax];
+    for (int i = threadIdx.x; i < j.niso; i += blockDim.x) s_iso[i] = j.isos[i];
+    __syncthreads();
+    const unsigned lane = threadIdx.x & 31u;
+    const uint64_t warps = (uint64_t)gridDim.x * (kCellThreads / 32);
+    const uint64_t groups = (j.ncells + 31) / 32;
+    for (uint64_t g = (uint64_t)blockIdx.x * (kCellThreads / 32) + (threadIdx.x >> 5); g < groups; g += warps) {
+        const uint64_t cell = g * 32 + lane;
+        const bool ok = cell < j.ncells;
+        uint32_t nodes[Tr::kNodes];
+        T v[Tr::kNodes];
+        if (ok) cell_load<CT, T>(j, cell, nodes, v);
+        for (int k = 0; k < j.niso; ++k) {
+            const uint32_t n = ok ? Tr::ntri(case_of<CT, T>(s_iso[k].cls, s_iso[k].iso, v)) : 0u;
+            const uint32_t t = __reduce_add_sync(0xffffffffu, n);
+            if (lane == 0) j.tile_counts[(uint64_t)k * groups + g] = t;
+        }
+    }
+}
+
+template <int CT, typename T>
+__global__ void __launch_bounds__(kCellThreads) k_cells_sweep_emit(CellJob j)
+{
+    using Tr = CellTraits<CT>;
+    __shared__ CellIso s_iso[kCellSweepMax];
+    for (int i = threadIdx.x; i < j.niso; i += blockDim.x) s_iso[i] = j.isos[i];
+    __syncthreads();
+    const unsigned lane = threadIdx.x & 31u;
+    const uint64_t warps = (uint64_t)gridDim.x * (kCellThreads / 32);
+    const uint64_t groups = (j.ncells + 31) / 32;
+    const uint64_t nchunks = (groups + 31) / 32;
+    const uint64_t items = nchunks * (uint64_t)j.niso;
+    for (uint64_t it = (uint64_t)blockIdx.x * (kCellThreads / 32) + (threadIdx.x >> 5); it < items; it += warps) {
+        const int k = (int)(it / nchunks);
+        const uint64_t g0 = (it - (uint64_t)k * nchunks) * 32;
+        const CellIso& I = s_iso[k];
+        const uint32_t* counts = j.tile_counts + (uint64_t)k * groups;
+        const uint64_t* offsets = j.tile_offsets + (uint64_t)k * groups;
+        const uint64_t mine = g0 + lane;
+        unsigned todo = __ballot_sync(0xffffffffu, mine < groups && counts[mine] != 0);
+        while (todo) {
+            const uint64_t g = g0 + (unsigned)(__ffs(todo) - 1);
+            todo &= todo - 1;
+            const uint64_t cell = g * 32 + lane;
+            uint32_t nodes[Tr::kNodes] = {};
+            unsigned c = 0;
+            uint32_t n = 0;
+            if (cell < j.ncells) {
+                T v[Tr::kNodes];
+                cell_load<CT, T>(j, cell, nodes, v);
+                c = case_of<CT, T>(I.cls, I.iso, v);
+                n = Tr::ntri(c);
+            }
+            uint32_t inc = n;
+#pragma unroll
+            for (int o = 1; o < 32; o <<= 1) {
+                const uint32_t y = __shfl_up_sync(0xffffffffu, inc, o);
+                if (lane >= (unsigned)o) inc += y;
+            }
+            const uint32_t total = __shfl_sync(0xffffffffu, inc, 31);
+            const uint64_t base = offsets[g] - I.base;
+            for (uint32_t first = 0; first < total; first += 32) {   // warp-uniform: every lane shuffles
+                const uint32_t tri = first + lane;
+                unsigned lo = 0;
+#pragma unroll
+                for (unsigned step = 16; step > 0; step >>= 1) {
+                    const uint32_t probe = __shfl_sync(0xffffffffu, inc, lo + step - 1);
+                    if (probe <= tri) lo += step;
+                }
+                const uint32_t own_inc = __shfl_sync(0xffffffffu, inc, lo);
+                const uint32_t own_n = __shfl_sync(0xffffffffu, n, lo);
+                const unsigned own_c = __shfl_sync(0xffffffffu, c, lo);
+                uint32_t own_nodes[Tr::kNodes];
+#pragma unroll
+                for (int q = 0; q < Tr::kNodes; ++q) own_nodes[q] = __shfl_sync(0xffffffffu, nodes[q], lo);
+                const uint64_t t = base + tri;
+                if (tri >= total || t >= I.cap_tris) continue;
+                const uint32_t kk = tri - (own_inc - own_n);
+                const uint64_t pk = Tr::tri(own_c) >> (12 * kk);
+                float3 vx[3];
+#pragma unroll
+                for (int sl = 0; sl < 3; ++sl) {
+                    const unsigned ed = Tr::edge((int)((pk >> (4 * sl)) & 15u));
+                    vx[sl] = cell_vertex<T>(j, I.f, I.iso, own_nodes[ed & 15u], own_nodes[ed >> 4]);
+                }
+                float* o = I.out_coords + 9 * t;
+                o[0] = vx[0].x; o[1] = vx[0].y; o[2] = vx[0].z;
+                o[3] = vx[1].x; o[4] = vx[1].y; o[5] = vx[1].z;
+                o[6] = vx[2].x; o[7] = vx[2].y; o[8] = vx[2].z;
+                const float3 nn = tri_normal(vx[0], vx[1], vx[2]);
+                float* q = I.out_normals + 3 * t;
+                q[0] = nn.x; q[1] = nn.y; q[2] = nn.z;
+            }
+        }
+    }
+}
+
+// base[k] = the first scanned offset of isolevel k, base[niso] = the total.
+__global__ void k_sweep_bases(const uint64_t* offsets, uint64_t groups, int niso, const uint64_t* total, uint64_t* out)
+{
+    if (threadIdx.x == 0 && blockIdx.x == 0) {
+        for (int k = 0; k < niso; ++k) out[k] = groups ? offsets[(uint64_t)k * groups] : 0;
+        out[niso] = *total;
+    }
+}
+
 // Blocks of 8 warps, one warp per 32-cell group, at most 8 blocks per SM.
 unsigned cell_grid(uint64_t groups, const Launch& L)
 {
@@ -720,6 +852,38 @@ cudaError_t launch_cells_slice_emit(const CellJob& j, const Launch& L)
     KVSMC_CELL_SWITCH(j.cell_type, j.dtype,
                       { k_cells_slice_emit<CT, T><<<cell_grid(tiles, L), kCellThreads, 0, L.stream>>>(j); });
     prof_end(L);
+    *L.counter += 1;
+    return cudaGetLastError();
+}
+
+cudaError_t launch_cells_sweep_count(const CellJob& j, const Launch& L)
+{
+    if (j.ncells == 0 || j.niso <= 0) return cudaSuccess;
+    const uint64_t tiles = cells_tiles(j.ncells);
+    prof_begin(L, "cells_sweep_count");
+    KVSMC_CELL_SWITCH(j.cell_type, j.dtype,
+                      { k_cells_sweep_count<CT, T><<<cell_grid(tiles, L), kCellThreads, 0, L.stream>>>(j); });
+    prof_end(L);
+    *L.counter += 1;
+    return cudaGetLastError();
+}
+
+cudaError_t launch_cells_sweep_emit(const CellJob& j, const Launch& L)
+{
+    if (j.ncells == 0 || j.niso <= 0) return cudaSuccess;
+    const uint64_t items = (cells_tiles(j.ncells) + 31) / 32 * (uint64_t)j.niso;
+    prof_begin(L, "cells_sweep_emit");
+    KVSMC_CELL_SWITCH(j.cell_type, j.dtype,
+                      { k_cells_sweep_emit<CT, T><<<cell_grid(items * 32, L), kCellThreads, 0, L.stream>>>(j); });
+    prof_end(L);
+    *L.counter += 1;
+    return cudaGetLastError();
+}
+
+cudaError_t launch_sweep_bases(const uint64_t* offsets, uint64_t groups, int niso, const uint64_t* total,
+                               uint64_t* out, const Launch& L)
+{
+    k_sweep_bases<<<1, 32, 0, L.stream>>>(offsets, groups, niso, total, out);
     *L.counter += 1;
     return cudaGetLastError();
 }
@@ -805,27 +969,32 @@ kvsmc_status check_args(kvsmc_context* ctx, int cell_type, int dtype, uint64_t n
 struct CellsScratch {
     void* d_scan;
     uint64_t* d_tail;
-    uint64_t tiles;
+    uint64_t tiles;      // 32-cell groups
+    uint64_t nscan;      // scanned entries: groups x isolevels
+    void* d_extra;       // sweep: isolevel records (kCellSweepMax) and bases (kCellSweepMax + 1)
 };
 
-kvsmc_status cells_prepare(kvsmc_context* ctx, kvsmc::CellJob& j, CellsScratch* sc)
+kvsmc_status cells_prepare(kvsmc_context* ctx, kvsmc::CellJob& j, CellsScratch* sc, int niso = 1)
 {
     using namespace kvsmc_host;
     if (!ctx->d_flag) KVSMC_CUDA(ctx, cudaMalloc(&ctx->d_flag, sizeof(int)));
     j.bad_index = ctx->d_flag;
     KVSMC_CUDA(ctx, cudaMemsetAsync(ctx->d_flag, 0, sizeof(int), ctx->stream));
     sc->tiles = kvsmc::cells_tiles(j.ncells);
-    const size_t bc = align_up(sc->tiles * 4, 256), bo = align_up(sc->tiles * 8, 256),
-                 bs = align_up(std::max(std::max(kvsmc::scan_scratch_bytes(sc->tiles),
+    sc->nscan = sc->tiles * (uint64_t)niso;
+    const size_t bc = align_up(sc->nscan * 4, 256), bo = align_up(sc->nscan * 8, 256),
+                 bs = align_up(std::max(std::max(kvsmc::scan_scratch_bytes(sc->nscan),
                                                  kvsmc::cells_minmax_scratch_bytes(ctx->num_sms)),
-                                        kvsmc::minmax_scratch_bytes(ctx->num_sms)), 256);
-    kvsmc_status st = ensure_scratch(ctx, bc + bo + bs + 256);
+                                        kvsmc::minmax_scratch_bytes(ctx->num_sms)), 256),
+                 be = align_up(kvsmc::kCellSweepMax * sizeof(kvsmc::CellIso) + (kvsmc::kCellSweepMax + 1) * 8, 256);
+    kvsmc_status st = ensure_scratch(ctx, bc + bo + bs + 256 + be);
     if (st) return st;
     char* base = static_cast<char*>(ctx->scratch);
     j.tile_counts = reinterpret_cast<uint32_t*>(base);
     j.tile_offsets = reinterpret_cast<uint64_t*>(base + bc);
     sc->d_scan = base + bc + bo;
     sc->d_tail = reinterpret_cast<uint64_t*>(base + bc + bo + bs);
+    sc->d_extra = base + bc + bo + bs + 256;
     return KVSMC_OK;
 }
 
@@ -889,7 +1058,7 @@ kvsmc_status cells_passes(kvsmc_context* ctx, kvsmc::CellJob& j, const CellsScra
     using namespace kvsmc_host;
     const kvsmc::Launch L = launch_of(ctx);
     KVSMC_CUDA(ctx, kvsmc::launch_cells_count(j, L));
-    KVSMC_CUDA(ctx, kvsmc::launch_scan(j.tile_counts, j.tile_offsets, sc.tiles, sc.d_scan, sc.d_tail, L));
+    KVSMC_CUDA(ctx, kvsmc::launch_scan(j.tile_counts, j.tile_offsets, sc.nscan, sc.d_scan, sc.d_tail, L));
     if (emit) {
         j.d_total = sc.d_tail;
         KVSMC_CUDA(ctx, kvsmc::launch_cells_emit(j, L));
@@ -1068,7 +1237,7 @@ kvsmc_status kvsmc_slice_cells_host(kvsmc_context* ctx, kvsmc_cell_type cell_typ
     if ((st = cells_prepare(ctx, j, &sc))) return done(st);
     const kvsmc::Launch L = launch_of(ctx);
     e = kvsmc::launch_cells_slice_count(j, L);
-    if (e == cudaSuccess) e = kvsmc::launch_scan(j.tile_counts, j.tile_offsets, sc.tiles, sc.d_scan, sc.d_tail, L);
+    if (e == cudaSuccess) e = kvsmc::launch_scan(j.tile_counts, j.tile_offsets, sc.nscan, sc.d_scan, sc.d_tail, L);
     if (e == cudaSuccess) e = cudaMemcpyAsync(ctx->h_small, sc.d_tail, sizeof(uint64_t), cudaMemcpyDeviceToHost, ctx->stream);
     if (e == cudaSuccess) e = cudaMemcpyAsync(ctx->h_small + 2, ctx->d_flag, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream);
     if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
@@ -1151,6 +1320,85 @@ kvsmc_status kvsmc_cells_bounds(kvsmc_context* ctx, kvsmc_cell_type cell_type, c
         max_coord[k] = out[3 + k];
     }
     return done(KVSMC_OK);
+}
+
+kvsmc_status kvsmc_marching_cells_sweep_device(kvsmc_context* ctx, kvsmc_cell_type cell_type, const void* values,
+                                               kvsmc_dtype dtype, uint64_t nnodes, const float* coords,
+                                               const uint32_t* connections, uint64_t ncells,
+                                               const double* isolevels, int32_t niso, int32_t has_minmax,
+                                               double min_value, double max_value, float* const* out_coords,
+                                               const uint64_t* coords_capacity, float* const* out_normals,
+                                               const uint64_t* normals_capacity, kvsmc_sizes* sizes)
+{
+    using namespace kvsmc_host;
+    if (!ctx || !isolevels || !sizes || niso < 1) return KVSMC_ERR_INVALID_ARGUMENT;
+    if (niso > kvsmc::kCellSweepMax)
+        return fail(ctx, KVSMC_ERR_INVALID_ARGUMENT, "cells sweep: %d isolevels (at most %d)", (int)niso,
+                    kvsmc::kCellSweepMax);
+    std::memset(sizes, 0, sizeof(kvsmc_sizes) * (size_t)niso);
+    kvsmc_status st = check_args(ctx, cell_type, dtype, nnodes, values, coords, connections, ncells);
+    if (st) return st;
+    KVSMC_CUDA(ctx, cudaSetDevice(ctx->device));
+    kvsmc::CellJob j = make_job(cell_type, dtype, values, nnodes, coords, connections, ncells, isolevels[0]);
+    CellsScratch sc;
+    bool go = false;
+    if ((st = cells_prepare(ctx, j, &sc, niso)) ||
+        (st = cells_range(ctx, j, sc, has_minmax, min_value, max_value, &sizes[0], &go)))
+        return st;
+    for (int k = 1; k < niso; ++k) {
+        sizes[k].min_value = sizes[0].min_value;
+        sizes[k].max_value = sizes[0].max_value;
+        sizes[k].extracted = sizes[0].extracted;
+    }
+    if (!go) return KVSMC_OK;
+    std::vector<kvsmc::CellIso> isos((size_t)niso);
+    for (int k = 0; k < niso; ++k) {
+        kvsmc::CellIso& I = isos[k];
+        std::memset(&I, 0, sizeof I);
+        I.iso = isolevels[k];
+        I.cls = make_classifier(isolevels[k]);
+        I.f = make_fast(isolevels[k], j.vmin, j.vmax, j.dtype);
+    }
+    kvsmc::CellIso* d_isos = static_cast<kvsmc::CellIso*>(sc.d_extra);
+    uint64_t* d_bases = reinterpret_cast<uint64_t*>(static_cast<char*>(sc.d_extra) +
+                                                    kvsmc::kCellSweepMax * sizeof(kvsmc::CellIso));
+    j.isos = d_isos;
+    j.niso = niso;
+    const kvsmc::Launch L = launch_of(ctx);
+    KVSMC_CUDA(ctx, cudaMemcpyAsync(d_isos, isos.data(), sizeof(kvsmc::CellIso) * niso, cudaMemcpyHostToDevice,
+                                    ctx->stream));
+    KVSMC_CUDA(ctx, kvsmc::launch_cells_sweep_count(j, L));
+    KVSMC_CUDA(ctx, kvsmc::launch_scan(j.tile_counts, j.tile_offsets, sc.nscan, sc.d_scan, sc.d_tail, L));
+    KVSMC_CUDA(ctx, kvsmc::launch_sweep_bases(j.tile_offsets, sc.tiles, niso, sc.d_tail, d_bases, L));
+    std::vector<uint64_t> bases((size_t)niso + 1);
+    int bad = 0;
+    KVSMC_CUDA(ctx, cudaMemcpyAsync(bases.data(), d_bases, 8 * ((size_t)niso + 1), cudaMemcpyDeviceToHost, ctx->stream));
+    KVSMC_CUDA(ctx, cudaMemcpyAsync(&bad, ctx->d_flag, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
+    KVSMC_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    if (bad) return fail(ctx, KVSMC_ERR_INVALID_ARGUMENT, "cells: a connection index is >= nnodes");
+    bool fits = out_coords && out_normals && coords_capacity && normals_capacity;
+    for (int k = 0; k < niso; ++k) {
+        const uint64_t t = bases[k + 1] - bases[k];
+        sizes[k].ntriangles = t;
+        sizes[k].nvertices = 3 * t;
+        sizes[k].ncoords = 9 * t;
+        sizes[k].nnormals = 3 * t;
+        if (t && (!fits || !out_coords[k] || !out_normals[k] || coords_capacity[k] < 9 * t ||
+                  normals_capacity[k] < 3 * t))
+            fits = false;
+        isos[k].base = bases[k];
+        isos[k].out_coords = fits ? out_coords[k] : nullptr;
+        isos[k].out_normals = fits ? out_normals[k] : nullptr;
+        isos[k].cap_tris = t;
+    }
+    if (!fits) return fail(ctx, KVSMC_ERR_CAPACITY, "cells sweep: the triangles do not fit the outputs");
+    if (bases[niso] == 0) return KVSMC_OK;
+    KVSMC_CUDA(ctx, cudaMemcpyAsync(d_isos, isos.data(), sizeof(kvsmc::CellIso) * niso, cudaMemcpyHostToDevice,
+                                    ctx->stream));
+    KVSMC_CUDA(ctx, kvsmc::launch_cells_sweep_emit(j, L));
+    // the records' host copy must outlive the copies above
+    KVSMC_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    return KVSMC_OK;
 }
 
 }  // extern "C"

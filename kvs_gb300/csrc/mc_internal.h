@@ -132,6 +132,18 @@ cudaError_t launch_slice_count(const SliceJob& j, const Launch& L);
 cudaError_t launch_slice_emit(const SliceJob& j, const Launch& L);
 
 // ---- marching cells on unstructured volumes (cells.cu)
+// One isolevel of a cells extraction: its exact thresholds, its vertex
+// certificate constants and its outputs.
+struct CellIso {
+    double iso;
+    Classifier cls;
+    FastIso f;
+    float* out_coords;        // 9 T
+    float* out_normals;       // 3 T
+    uint64_t cap_tris;
+    uint64_t base;            // sweep: its first slot in the scanned group offsets
+};
+constexpr int kCellSweepMax = 64;   // isolevels of one sweep
 struct CellJob {
     int32_t cell_type;        // kvsmc_cell_type
     int32_t dtype;
@@ -157,10 +169,18 @@ struct CellJob {
     int32_t tf_res;
     const uint8_t* table;     // device colour table, tf_res x RGB
     uint8_t* out_colors;      // 9 T (RGB per vertex)
+    // isolevel sweep: niso records in device memory, group counts / offsets
+    // of isolevel k at [k * groups, (k + 1) * groups)
+    const CellIso* isos;
+    int32_t niso;
 };
 cudaError_t launch_cells_count(const CellJob& j, const Launch& L);
 cudaError_t launch_cells_emit(const CellJob& j, const Launch& L);
 uint64_t cells_tiles(uint64_t ncells);
+cudaError_t launch_cells_sweep_count(const CellJob& j, const Launch& L);
+cudaError_t launch_cells_sweep_emit(const CellJob& j, const Launch& L);
+cudaError_t launch_sweep_bases(const uint64_t* offsets, uint64_t groups, int niso, const uint64_t* total,
+                               uint64_t* out, const Launch& L);
 cudaError_t launch_cells_slice_count(const CellJob& j, const Launch& L);
 cudaError_t launch_cells_slice_emit(const CellJob& j, const Launch& L);
 // bounding box of the cells' nodes (updateMinMaxCoords' fold), d_out[0..2] min, [3..5] max

@@ -217,3 +217,53 @@ def test_bounds_match_the_fold_on_nans_and_signed_zeros(kvsmc_ctx):
     lo, hi = _abi.cells_bounds(kvsmc_ctx, 0, xyz, conn)
     wlo, whi = ocells.min_max_coords(xyz, conn)
     assert same_bits(lo, wlo) and same_bits(hi, whi)
+
+
+def test_isolevel_sweep_matches_single_extractions(kvsmc_ctx):
+    """kvsmc_marching_cells_sweep_device: one count pass for all isolevels,
+    the same bits per isolevel as kvsmc_marching_cells_device (and the
+    restatement), every cell type, with and without a preset min/max; too
+    small an output refuses the whole sweep with the sizes filled."""
+    import ctypes as C
+    lib = kvsmc_ctx.lib
+    for ct in range(4):
+        xyz, conn = cm.grid(ct, 40, 36, 32, seed=70 + ct)
+        v = cm.sphere_values(xyz, (19.2, 17.4, 15.9))
+        dv, dx, dk = (torch.from_numpy(np.ascontiguousarray(a)).cuda() for a in (v, xyz, conn.view(np.int32)))
+        torch.cuda.synchronize()
+        isos = [2.5 + 1.7 * i for i in range(12)]
+        for mm in (None, (1.0, 20.0)):
+            want = [ocells.marching_cells(ct, v, xyz, conn, iso, mm) for iso in isos]
+            n = len(isos)
+            caps = [max(1, w["coords"].size // 9) for w in want]
+            oc = [torch.full((9 * c,), 7.0, device="cuda") for c in caps]
+            on = [torch.full((3 * c,), 7.0, device="cuda") for c in caps]
+            torch.cuda.synchronize()
+            pc = (C.c_void_p * n)(*[t.data_ptr() for t in oc])
+            pn = (C.c_void_p * n)(*[t.data_ptr() for t in on])
+            cc = (C.c_uint64 * n)(*[9 * c for c in caps])
+            cn = (C.c_uint64 * n)(*[3 * c for c in caps])
+            sizes = (_abi.Sizes * n)()
+            il = (C.c_double * n)(*isos)
+            st = lib.kvsmc_marching_cells_sweep_device(
+                kvsmc_ctx.handle, ct, dv.data_ptr(), 8, v.size, dx.data_ptr(), dk.data_ptr(), conn.shape[0], il, n,
+                1 if mm else 0, mm[0] if mm else 0.0, mm[1] if mm else 0.0, pc, cc, pn, cn, sizes)
+            assert st == 0, kvsmc_ctx.lib.kvsmc_last_error(kvsmc_ctx.handle)
+            kvsmc_ctx.synchronize()
+            for i, w in enumerate(want):
+                t = sizes[i].ntriangles
+                assert 9 * t == w["coords"].size, (ct, i)
+                assert same_bits(oc[i][:9 * t].cpu().numpy(), w["coords"]), (ct, mm, i)
+                assert same_bits(on[i][:3 * t].cpu().numpy(), w["normals"]), (ct, mm, i)
+            # one output one triangle short: nothing written, sizes returned
+            big = max(range(n), key=lambda i: caps[i])
+            cc[big] = 9 * caps[big] - 9
+            for t in oc:
+                t.fill_(7.0)
+            torch.cuda.synchronize()
+            st = lib.kvsmc_marching_cells_sweep_device(
+                kvsmc_ctx.handle, ct, dv.data_ptr(), 8, v.size, dx.data_ptr(), dk.data_ptr(), conn.shape[0], il, n,
+                1 if mm else 0, mm[0] if mm else 0.0, mm[1] if mm else 0.0, pc, cc, pn, cn, sizes)
+            assert st == 6 and sizes[big].ntriangles == caps[big]
+            kvsmc_ctx.synchronize()
+            assert all(bool((t == 7.0).all()) for t in oc)
