@@ -267,3 +267,35 @@ def test_isolevel_sweep_matches_single_extractions(kvsmc_ctx):
             assert st == 6 and sizes[big].ntriangles == caps[big]
             kvsmc_ctx.synchronize()
             assert all(bool((t == 7.0).all()) for t in oc)
+
+
+def test_isolevel_sweep_on_random_meshes_with_ties(kvsmc_ctx):
+    """The sweep on random connectivity (every table case, pyramid ambiguities
+    with E == 0) with small integer values and isolevels on and between them."""
+    import ctypes as C
+    lib = kvsmc_ctx.lib
+    rng = np.random.default_rng(31)
+    for ct in range(4):
+        xyz, conn = cm.random_mesh(ct, 3000, 60000, seed=200 + ct)
+        v = rng.integers(-3, 4, 3000).astype(np.int16)
+        isos = [-2.5, -1.0, 0.0, 0.5, 1.0, 2.0, 2.5]
+        n = len(isos)
+        want = [ocells.marching_cells(ct, v, xyz, conn, iso) for iso in isos]
+        dv, dx, dk = (torch.from_numpy(np.ascontiguousarray(a)).cuda() for a in (v, xyz, conn.view(np.int32)))
+        caps = [max(1, w["coords"].size // 9) for w in want]
+        oc = [torch.empty(9 * c, device="cuda") for c in caps]
+        on = [torch.empty(3 * c, device="cuda") for c in caps]
+        torch.cuda.synchronize()
+        sizes = (_abi.Sizes * n)()
+        st = lib.kvsmc_marching_cells_sweep_device(
+            kvsmc_ctx.handle, ct, dv.data_ptr(), 1, v.size, dx.data_ptr(), dk.data_ptr(), conn.shape[0],
+            (C.c_double * n)(*isos), n, 0, 0.0, 0.0, (C.c_void_p * n)(*[t.data_ptr() for t in oc]),
+            (C.c_uint64 * n)(*[9 * c for c in caps]), (C.c_void_p * n)(*[t.data_ptr() for t in on]),
+            (C.c_uint64 * n)(*[3 * c for c in caps]), sizes)
+        assert st == 0
+        kvsmc_ctx.synchronize()
+        for i, w in enumerate(want):
+            t = sizes[i].ntriangles
+            assert 9 * t == w["coords"].size, (ct, isos[i])
+            assert same_bits(oc[i][:9 * t].cpu().numpy(), w["coords"]), (ct, isos[i])
+            assert same_bits(on[i][:3 * t].cpu().numpy(), w["normals"]), (ct, isos[i])
