@@ -181,3 +181,12 @@ def test_vertex_normal_forces_shared_vertices(oracle_lib, kvsmc_ctx):
     o = oracle_lib.marching_cubes(v, 0.5, "polygon", False)
     assert o["connections"].size > 0
     assert np.array_equal(mc.connections(), o["connections"])
+
+
+@pytest.mark.parametrize("width", [4097, 4098, 4500])
+def test_widths_at_and_past_the_streaming_limit(oracle_lib, kvsmc_ctx, width):
+    """Rows of up to 4097 nodes take the streaming kernels, wider ones the
+    gather kernels: the same bits either way, all three modes."""
+    v = S.to_numpy(S.fbm((4, 5, width), seed=width))
+    for nt, dup in MODES[:3]:
+        check(oracle_lib, kvsmc_ctx, v, 0.5, nt, dup)
