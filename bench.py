@@ -87,6 +87,10 @@ WORKLOADS = {
                         "nodes jittered U[-0.2,0.2]) split into 6 tetrahedra per hexahedron (24.6 M cells, 4.17 M "
                         "nodes), float32 values = distance to (80.3, 79.6, 80.9) + 1.5 sin(x/7) sin(y/9) sin(z/11), "
                         "one isolevel per step cycling 30/50/70/90, duplication=true, PolygonNormal"),
+    "slice512": dict(shape=(512, 512, 512), kind="slice", point=(255.5, 255.5, 255.5), normal=(0.31, -0.52, 0.79),
+                     desc="kvs::SlicePlane of a 512^3 float32 fBm field by the oblique plane through its centre "
+                          "with normal (0.31, -0.52, 0.79) (the profiling case of slice1024: same kernels, "
+                          "512 MiB on the device)"),
     "blobs128": dict(shape=(128, 128, 128), kind="blobs", isos=[0.5],
                      desc="128^3 float32, 4 Gaussian blobs (sigma 8..24) + U[-0.01,0.01] noise, iso 0.5, "
                           "duplication=true, PolygonNormal"),

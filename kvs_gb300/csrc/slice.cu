@@ -13,11 +13,12 @@
 // 1043-1054, RGBColor::Mix, RGBColor(Vec3) rounding); one normal per triangle
 // -((v2 - v0) x (v1 - v0)).  Cells in z, y, x order.
 //
-// Two passes, one warp per cell row (y, z): count (cases from the plane
+// Two passes: count (one thread per cell row (y, z); cases from the plane
 // alone, only over the x-interval of cells the plane can cut, bounded
 // conservatively in double), an exclusive scan of the row counts, then emit
-// (a warp scan of each cell's triangle count; the volume read only at the
-// corners of cut edges).
+// (a warp per 32 rows: the rows' cut cells 32 at a time, one per lane, and
+// each batch's triangles one per lane; the volume read only at the corners
+// of cut edges).
 #include <cuda_runtime.h>
 
 #include <cstring>
@@ -144,42 +145,92 @@ __global__ void __launch_bounds__(kSliceThreads) k_slice_emit(SliceJob j)
     const uint32_t cx = j.vol.nx - 1, cy = j.vol.ny - 1;
     const unsigned lane = threadIdx.x & 31u;
     const uint64_t warps = (uint64_t)gridDim.x * (blockDim.x / 32);
-    // each warp takes 32 consecutive rows: every lane works out one row's
-    // interval and offset, then the warp walks the rows one after another
+    // Each warp takes 32 consecutive rows; lane i works out row i's interval
+    // and first output triangle.  The rows' cut cells, in row and x order,
+    // are then taken 32 at a time (one cell per lane, whatever row it is in),
+    // and each batch's triangles are spread over the lanes, so a row with
+    // only a few cut cells does not leave most of the warp idle.
     for (uint64_t r0 = ((uint64_t)blockIdx.x * (blockDim.x / 32) + (threadIdx.x >> 5)) * 32; r0 < j.nrows;
          r0 += warps * 32) {
         const uint64_t my = r0 + lane;
         int64_t mx0 = 0, mx1 = -1;
-        uint64_t moff = 0;
+        uint64_t rowrun = 0;   // next output triangle of this lane's row
+        uint32_t my_y = 0, my_z = 0;
         if (my < j.nrows) {
-            const uint32_t mz = (uint32_t)(my / cy), myy = (uint32_t)(my - (uint64_t)mz * cy);
-            row_interval(j, cx, myy, mz, mx0, mx1);
-            moff = j.row_offsets[my];
+            my_z = (uint32_t)(my / cy);
+            my_y = (uint32_t)(my - (uint64_t)my_z * cy);
+            row_interval(j, cx, my_y, my_z, mx0, mx1);
+            rowrun = j.row_offsets[my];
         }
-        const uint32_t nr = (uint32_t)(j.nrows - r0 < 32 ? j.nrows - r0 : 32);
-        for (uint32_t i = 0; i < nr; ++i) {
-        const uint64_t row = r0 + i;
-        const uint32_t z = (uint32_t)(row / cy), y = (uint32_t)(row - (uint64_t)z * cy);
-        const int64_t x0 = __shfl_sync(0xffffffffu, mx0, i), x1 = __shfl_sync(0xffffffffu, mx1, i);
-        uint64_t running = __shfl_sync(0xffffffffu, moff, i);
-        for (int64_t xc = x0; xc <= x1; xc += 32) {
-            const int64_t xs = xc + lane;
-            const uint32_t x = (uint32_t)xs;
-            const unsigned c = xs <= x1 ? slice_case(j, x, y, z) : 0u;
-            const uint32_t n = c_slice_ntri[c];
-            uint32_t inc = n;
-            for (int o = 1; o < 32; o <<= 1) {
-                const uint32_t t = __shfl_up_sync(0xffffffffu, inc, o);
-                if (lane >= (unsigned)o) inc += t;
+        const uint32_t len = mx1 >= mx0 ? (uint32_t)(mx1 - mx0 + 1) : 0u;
+        uint32_t linc = len;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const uint32_t t = __shfl_up_sync(0xffffffffu, linc, o);
+            if (lane >= (unsigned)o) linc += t;
+        }
+        const uint32_t lexc = linc - len;
+        const uint32_t ltot = __shfl_sync(0xffffffffu, linc, 31);
+        for (uint32_t b0 = 0; b0 < ltot; b0 += 32) {
+            // ---- one cut cell per lane: its row (the lane owning it) and x
+            const uint32_t item = b0 + lane;
+            unsigned owner = 0;
+#pragma unroll
+            for (unsigned step = 16; step > 0; step >>= 1) {
+                const uint32_t probe = __shfl_sync(0xffffffffu, linc, owner + step - 1);
+                if (probe <= item) owner += step;
             }
-            const uint32_t tot = __shfl_sync(0xffffffffu, inc, 31);
-            uint64_t t = running + inc - n;
-            uint64_t pk = c_slice_tri[c];
-            for (uint32_t k = 0; k < n; ++k, ++t, pk >>= 12) {
-                if (t >= j.cap_tris) break;   // never past the outputs
-                const SliceVertex va = slice_vertex<T>(j, vol, x, y, z, (int)(pk & 15u));
-                const SliceVertex vb = slice_vertex<T>(j, vol, x, y, z, (int)((pk >> 4) & 15u));
-                const SliceVertex vd = slice_vertex<T>(j, vol, x, y, z, (int)((pk >> 8) & 15u));
+            const int64_t ox0 = __shfl_sync(0xffffffffu, mx0, owner);
+            const uint32_t oexc = __shfl_sync(0xffffffffu, lexc, owner);
+            const uint32_t y = __shfl_sync(0xffffffffu, my_y, owner), z = __shfl_sync(0xffffffffu, my_z, owner);
+            const uint64_t orun = __shfl_sync(0xffffffffu, rowrun, owner);
+            const bool has = item < ltot;
+            const uint32_t x = has ? (uint32_t)(ox0 + (int64_t)(item - oexc)) : 0u;
+            const unsigned c = has ? slice_case(j, x, y, z) : 0u;
+            const uint32_t n = c_slice_ntri[c];
+            uint32_t ninc = n;
+#pragma unroll
+            for (int o = 1; o < 32; o <<= 1) {
+                const uint32_t t = __shfl_up_sync(0xffffffffu, ninc, o);
+                if (lane >= (unsigned)o) ninc += t;
+            }
+            const uint32_t ntot = __shfl_sync(0xffffffffu, ninc, 31);
+            // first triangle of this cell: its row's running count plus the
+            // triangles of the row's earlier cells in this batch
+            const uint32_t ofirst = oexc > b0 ? oexc - b0 : 0u;   // the row's first lane in the batch
+            const uint32_t before = __shfl_sync(0xffffffffu, ninc, ofirst ? ofirst - 1 : 0);
+            const uint64_t tbase = orun + (ninc - n) - (ofirst ? before : 0u);
+            // every row's running count moves past its cells of this batch
+            {
+                const uint32_t f = lexc > b0 ? (lexc - b0 < 32u ? lexc - b0 : 32u) : 0u;
+                const uint32_t e = linc > b0 ? (linc - b0 < 32u ? linc - b0 : 32u) : 0u;
+                const uint32_t s_end = __shfl_sync(0xffffffffu, ninc, e ? e - 1 : 0);
+                const uint32_t s_beg = __shfl_sync(0xffffffffu, ninc, f ? f - 1 : 0);
+                if (e > f) rowrun += (uint64_t)(s_end - (f ? s_beg : 0u));
+            }
+            // ---- the batch's triangles, one per lane
+            for (uint32_t first = 0; first < ntot; first += 32) {   // warp-uniform: every lane shuffles
+                const uint32_t tri = first + lane;
+                unsigned q = 0;
+#pragma unroll
+                for (unsigned step = 16; step > 0; step >>= 1) {
+                    const uint32_t probe = __shfl_sync(0xffffffffu, ninc, q + step - 1);
+                    if (probe <= tri) q += step;
+                }
+                const uint32_t q_inc = __shfl_sync(0xffffffffu, ninc, q);
+                const uint32_t q_n = __shfl_sync(0xffffffffu, n, q);
+                const unsigned q_c = __shfl_sync(0xffffffffu, c, q);
+                const uint32_t qx = __shfl_sync(0xffffffffu, x, q);
+                const uint32_t qy = __shfl_sync(0xffffffffu, y, q), qz = __shfl_sync(0xffffffffu, z, q);
+                const uint64_t q_base = __shfl_sync(0xffffffffu, tbase, q);
+                if (tri >= ntot) continue;
+                const uint32_t k = tri - (q_inc - q_n);
+                const uint64_t t = q_base + k;
+                if (t >= j.cap_tris) continue;   // never past the outputs
+                const uint64_t pk = c_slice_tri[q_c] >> (12 * k);
+                const SliceVertex va = slice_vertex<T>(j, vol, qx, qy, qz, (int)(pk & 15u));
+                const SliceVertex vb = slice_vertex<T>(j, vol, qx, qy, qz, (int)((pk >> 4) & 15u));
+                const SliceVertex vd = slice_vertex<T>(j, vol, qx, qy, qz, (int)((pk >> 8) & 15u));
                 float* o = j.coords + 9 * t;
                 o[0] = va.p.x; o[1] = va.p.y; o[2] = va.p.z;
                 o[3] = vb.p.x; o[4] = vb.p.y; o[5] = vb.p.z;
@@ -189,11 +240,9 @@ __global__ void __launch_bounds__(kSliceThreads) k_slice_emit(SliceJob j)
                 col[3] = vb.rgb.x; col[4] = vb.rgb.y; col[5] = vb.rgb.z;
                 col[6] = vd.rgb.x; col[7] = vd.rgb.y; col[8] = vd.rgb.z;
                 const float3 nn = slice_normal(va.p, vb.p, vd.p);
-                float* q = j.normals + 3 * t;
-                q[0] = nn.x; q[1] = nn.y; q[2] = nn.z;
+                float* w = j.normals + 3 * t;
+                w[0] = nn.x; w[1] = nn.y; w[2] = nn.z;
             }
-            running += tot;
-        }
         }
     }
 }
