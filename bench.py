@@ -731,7 +731,7 @@ def run_cells_cpu(w, reference, min_seconds=10.0):
         calls += 1
         if kind == "reference":
             from oracle import ref
-            # the mapper constructor alone, timed inside the driver (the
+            # the mapper constructor alone, timed inside oracle/ref_driver.cpp (the
             # volume object's setup copies are left out)
             t += ref.marching_cells(0, vals, xyz, conn, r, minmax=(lo, hi))["seconds"]
         else:

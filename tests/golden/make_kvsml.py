@@ -10,7 +10,7 @@ and what it produced -- values, type, resolution, min/max, coordinates -- is
 stored in tests/golden/kvsml/expected.npz with the case list in
 tests/golden/kvsml/cases.json.  AVS field files (.fld: header lines, "\f\f",
 raw values) are written here and read by the reference kvs::AVSField with the
-StructuredVolumeImporter rules (the driver's kvsref_read_avs).
+StructuredVolumeImporter rules (kvsref_read_avs in oracle/ref_driver.cpp).
 
     python tests/golden/make_kvsml.py
 """
