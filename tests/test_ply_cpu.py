@@ -1,7 +1,8 @@
 """Binary PLY export: the restatement (oracle/export.py ply_binary) against
 files written by the reference PolygonExporter<kvs::Ply> + Ply::write
-(tests/golden/ply.npz), byte for byte; the mirror's mode choice and refusals
-(no GPU needed)."""
+(tests/golden/ply.npz), byte for byte; the library's header writer against
+those files; the mirror's mode choice and refusals (no GPU needed)."""
+import ctypes
 import json
 import os
 
@@ -66,3 +67,26 @@ def test_refusals(capsys):
     assert not ex.write("/nonexistent/x.ply")          # ASCII (the reference default) is not provided
     assert "ASCII PLY" in capsys.readouterr().err
     assert PolygonExporterPly().exec(None) is None
+
+
+def test_library_header_matches_reference_files():
+    """kvsmc_ply_header and kvsmc_ply_record_bytes (host code in libkvsmc.so,
+    no GPU needed) give the reference file's header bytes and its size."""
+    from kvs_gb300 import _abi
+    lib = _abi.load()
+    man, arr = ply_fixtures()
+    for e in man:
+        k = e["case"]
+        f = arr[f"{k}__file"].tobytes()
+        nv = arr[f"{k}__coords"].size // 3
+        cmode, nmode = ply_modes(polygon_of(arr, e))
+        need = lib.kvsmc_ply_header(nv, cmode, nmode, None, 0)
+        assert need > 0, k
+        buf = ctypes.create_string_buffer(need + 1)
+        assert lib.kvsmc_ply_header(nv, cmode, nmode, buf, need + 1) == need, k
+        head = buf.raw[:need]
+        assert f[:need] == head and head.endswith(b"end_header\n"), k
+        assert len(f) == need + nv * lib.kvsmc_ply_record_bytes(cmode, nmode), k
+    small = ctypes.create_string_buffer(b"x" * 8)
+    assert lib.kvsmc_ply_header(3, 1, 1, small, 8) > 8
+    assert small.raw == b"x" * 8 + b"\0"                 # too small a buffer is left untouched
