@@ -148,3 +148,22 @@ def test_mirror_checks_without_gpu(capsys):
         assert mapper.exec(vol) is None and mapper.isFailure()
         assert f"Input volume is not {msg}-cell data." in capsys.readouterr().err
     assert mcells.UnstructuredVolumeObject(mcells.UnstructuredVolumeObject.Pyramid).numberOfCellNodes() == 5
+
+
+@pytest.mark.skipif(not ref.available(), reason="needs the reference build (oracle/_ref)")
+def test_oracle_matches_reference_on_random_meshes_with_ties():
+    """Random connectivity (repeated and degenerate nodes, cells in any
+    orientation) with node values on a coarse lattice so that many equal the
+    isolevel exactly; each cell type, value type and isolevel."""
+    for ct in range(4):
+        xyz, conn = cm.random_mesh(ct, 300, 900, seed=31 + ct)
+        rng = np.random.default_rng(5 + ct)
+        lattice = rng.integers(0, 9, 300)
+        for dt in (np.float32, np.int16, np.uint8):
+            v = lattice.astype(dt)
+            for iso in (3.0, 4.0, 4.5):
+                r = ref.marching_cells(ct, v, xyz, conn, iso)
+                o = ocells.marching_cells(ct, v, xyz, conn, iso)
+                assert r["coords"].size > 0, (ct, dt, iso)
+                assert same_bits(o["coords"], r["coords"]), (ct, dt, iso, first_diff(o["coords"], r["coords"]))
+                assert same_bits(o["normals"], r["normals"]), (ct, dt, iso)

@@ -84,3 +84,25 @@ def test_fixtures_are_current():
                             normal=e["normal"], tf_range=e["tf_range"])
         for f in ("coords", "normals", "colors"):
             assert same_bits(r[f], arr[f"{e['key']}__{f}"]), (e["key"], f)
+
+
+@pytest.mark.skipif(not ref.available(), reason="needs the reference build (oracle/_ref)")
+def test_oracle_matches_reference_on_random_meshes():
+    """Random connectivity (repeated nodes, any orientation) with node
+    coordinates on a half-unit lattice, cut by axis planes through lattice
+    values (many nodes exactly on the plane) and by an oblique plane."""
+    from . import cell_meshes as cm
+    table = golden()[1]["colormap256"]
+    for ct in range(4):
+        xyz, conn = cm.random_mesh(ct, 300, 900, seed=41 + ct)
+        xyz = (np.round(xyz * 2) / 2).astype(np.float32)
+        v = np.random.default_rng(ct).uniform(-1, 1, 300).astype(np.float32)
+        lo, hi = np.float32(-1.5), np.float32(2.0)
+        for coef in ((1, 0, 0, -0.5), (0, 1, 0, 1.0), (0, 0, -1, 0), (0.3, -0.7, 0.2, 0.1)):
+            r = ref.slice_cells(ct, v, xyz, conn, coefficients=coef, point=None, normal=None,
+                                tf_range=(float(lo), float(hi)))
+            c, rgb, n = ocells.slice_cells(ct, v, xyz, conn, np.asarray(coef, np.float32), table, lo, hi)
+            assert r["coords"].size > 0, (ct, coef)
+            assert same_bits(c, r["coords"]), (ct, coef, first_diff(c, r["coords"]))
+            assert np.array_equal(rgb, r["colors"]), (ct, coef)
+            assert same_bits(n, r["normals"]), (ct, coef)
