@@ -92,3 +92,21 @@ def test_slice_rejects_like_the_reference(kvsmc_ctx, capsys):
     err = capsys.readouterr().err
     assert "Input object is NULL." in err and "Input object is not volume dat." in err
     assert "Input volume is not a sclar field data." in err
+
+
+def test_large_volumes_match_oracle(kvsmc_ctx):
+    """The CUDA slicer against the restatement (oracle/slice.py) on volumes
+    with long rows and planes that cut long runs of cells per row."""
+    from oracle import slice as OS
+    from .helpers import golden
+    from .test_slice_cpu import default_tf_range, large_slice_cases
+    table = golden()[1]["colormap256"]
+    for name, v, coef in large_slice_cases():
+        s = SlicePlane(StructuredVolumeObject(v), coefficients=coef, transfer_function=TransferFunction(256),
+                       context=kvsmc_ctx)
+        lo, hi = default_tf_range(v)
+        c, rgb, n = OS.slice_plane(v, coef, table, lo, hi)
+        assert c.size > 0, name
+        assert same_bits(s.coords(), c), (name, first_diff(s.coords(), c))
+        assert np.array_equal(s.colors(), rgb), name
+        assert same_bits(s.normals(), n), name
