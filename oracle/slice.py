@@ -44,7 +44,9 @@ _tables = None
 
 
 def mc_tables():
-    """(triangle table int8[256, 16], edge endpoints int64[12, 2, 3])."""
+    """(triangle table int8[256, 16], edge endpoints int64[12, 2, 3]): the
+    reference's MarchingCubesTable::TriangleID and VertexID
+    (MarchingCubesTable.cpp:16-290), read from the generated header."""
     global _tables
     if _tables is None:
         text = open(MC_TABLES).read()
@@ -60,13 +62,15 @@ def mc_tables():
 
 
 def _plane(cf, x, y, z):
+    """substitute_plane_equation (SlicePlane.cpp:949-979) in float."""
     f32 = np.float32
     ab = ((cf[0] * x).astype(f32) + (cf[1] * y).astype(f32)).astype(f32)
     return ((ab + (cf[2] * z).astype(f32)).astype(f32) + cf[3]).astype(f32)
 
 
 def slice_plane(values, coefficients, table, tf_min, tf_max, min_coord=None, max_coord=None):
-    """values: array [nz, ny, nx] of any of the ten value types.  Returns
+    """SlicePlane::extract_plane on a structured volume (SlicePlane.cpp:157-281).
+    values: array [nz, ny, nx] of any of the ten value types.  Returns
     (coords f32[9T], colors u8[9T], normals f32[3T]) as the reference's
     SlicePlane sets them; min_coord/max_coord default to the uniform
     volume's bounding box (0 and dims - 1)."""
