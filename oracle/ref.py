@@ -87,7 +87,8 @@ def lib():
         _lib.kvsref_slice_plane.restype = C.c_int
         _lib.kvsref_slice_plane.argtypes = [
             C.c_int, C.c_int, C.c_void_p, C.c_uint, C.c_uint, C.c_uint, C.c_void_p,
-            C.c_int, C.c_double, C.c_double, C.c_int, C.c_int, C.c_float, C.c_float, C.POINTER(_Result)]
+            C.c_int, C.c_double, C.c_double, C.c_int, C.c_int, C.c_float, C.c_float,
+            C.c_int, C.c_void_p, C.c_void_p, C.POINTER(_Result)]
         _lib.kvsref_marching_cubes_stl.restype = C.c_int
         _lib.kvsref_marching_cubes_stl.argtypes = [
             C.c_int, C.c_void_p, C.c_uint, C.c_uint, C.c_uint, C.c_double, C.c_int, C.c_int, C.c_char_p]
@@ -259,15 +260,18 @@ def slice_cells(cell_type, values, coords, connections, coefficients=None, point
 
 
 def slice_plane(values, coefficients=None, point=None, normal=None, minmax=None, tf_resolution=256,
-                tf_range=None):
+                tf_range=None, obj_coords=None):
     """The reference kvs::SlicePlane on a uniform volume shaped (nz, ny, nx):
-    by plane coefficients (a, b, c, d), or by a point and a normal."""
+    by plane coefficients (a, b, c, d), or by a point and a normal;
+    obj_coords = (min xyz, max xyz) presets the volume's object coords."""
     v = np.ascontiguousarray(values)
     nz, ny, nx = v.shape
     if coefficients is not None:
         form, plane = 0, np.ascontiguousarray(coefficients, np.float32)
     else:
         form, plane = 1, np.ascontiguousarray(list(point) + list(normal), np.float32)
+    if obj_coords is not None:
+        lo, hi = (np.ascontiguousarray(c, np.float32) for c in obj_coords)
     r = _Result()
     st = lib().kvsref_slice_plane(
         form, dtype_code(v.dtype), v.ctypes.data, nx, ny, nz, plane.ctypes.data,
@@ -276,7 +280,10 @@ def slice_plane(values, coefficients=None, point=None, normal=None, minmax=None,
         float(minmax[1]) if minmax is not None else 0.0,
         tf_resolution, 1 if tf_range is not None else 0,
         float(tf_range[0]) if tf_range is not None else 0.0,
-        float(tf_range[1]) if tf_range is not None else 0.0, C.byref(r))
+        float(tf_range[1]) if tf_range is not None else 0.0,
+        1 if obj_coords is not None else 0,
+        lo.ctypes.data if obj_coords is not None else None,
+        hi.ctypes.data if obj_coords is not None else None, C.byref(r))
     if st != 0:
         raise RuntimeError("kvsref_slice_plane failed")
     return _collect(r)

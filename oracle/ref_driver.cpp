@@ -197,12 +197,13 @@ int kvsref_marching_cubes(
  * The reference kvs::SlicePlane (Source/Core/Visualization/Mapper/SlicePlane.cpp)
  * on a uniform structured volume: form 0 SlicePlane( volume, coefficients, tf ),
  * form 1 SlicePlane( volume, point, normal, tf ) (plane[0..2] point,
- * plane[3..5] normal).
+ * plane[3..5] normal); has_obj_coords presets the volume's min/max object
+ * coords.
  */
 int kvsref_slice_plane(
     int form, int dtype, const void* values, unsigned nx, unsigned ny, unsigned nz, const float* plane,
     int has_minmax, double vmin, double vmax, int tf_resolution, int tf_has_range, float tf_min, float tf_max,
-    kvsref_result* out )
+    int has_obj_coords, const float* min_obj, const float* max_obj, kvsref_result* out )
 {
     std::memset( out, 0, sizeof( *out ) );
     const size_t n = size_t( nx ) * ny * nz;
@@ -216,6 +217,11 @@ int kvsref_slice_plane(
     vol->setValues( vals );
     vol->setGridTypeToUniform();
     if ( has_minmax ) vol->setMinMaxValues( vmin, vmax );
+    if ( has_obj_coords )
+    {
+        vol->setMinMaxObjectCoords( kvs::Vec3( min_obj[0], min_obj[1], min_obj[2] ),
+                                    kvs::Vec3( max_obj[0], max_obj[1], max_obj[2] ) );
+    }
     kvs::SlicePlane* s = nullptr;
     if ( form == 0 ) s = new kvs::SlicePlane( vol, kvs::Vec4( plane[0], plane[1], plane[2], plane[3] ), tfunc );
     else s = new kvs::SlicePlane( vol, kvs::Vec3( plane[0], plane[1], plane[2] ),

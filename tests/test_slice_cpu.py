@@ -116,3 +116,23 @@ def test_restatement_matches_reference_on_gpu_test_cases():
         assert same_bits(c, r["coords"]), (name, first_diff(c, r["coords"]))
         assert np.array_equal(rgb, r["colors"]), name
         assert same_bits(n, r["normals"]), name
+
+
+@pytest.mark.skipif(not ref.available(), reason="needs the reference build (oracle/_ref)")
+def test_restatement_matches_reference_with_object_coords():
+    """A volume whose object coordinates are preset (scale_coord with a
+    non-zero origin and non-unit cell sizes)."""
+    from oracle import slice as OS
+    from .helpers import first_diff, golden
+    table = golden()[1]["colormap256"]
+    v = np.random.default_rng(19).random((13, 17, 40)).astype(np.float32)
+    lo, hi = default_tf_range(v)
+    for obj in (([1.5, -2.0, 0.25], [9.0, 3.3, 7.0]), ([-10, -10, -10], [10, 10, 10])):
+        for coef in ((0, 0, 1, -6.5), (0.4, -0.2, 0.6, -5.1)):
+            r = ref.slice_plane(v, coefficients=list(coef), point=None, normal=None,
+                                tf_range=(float(lo), float(hi)), obj_coords=obj)
+            c, rgb, n = OS.slice_plane(v, coef, table, lo, hi, min_coord=obj[0], max_coord=obj[1])
+            assert r["coords"].size > 0 and np.array_equal(r["min_obj"], np.float32(obj[0])), (obj, coef)
+            assert same_bits(c, r["coords"]), (obj, coef, first_diff(c, r["coords"]))
+            assert np.array_equal(rgb, r["colors"]), (obj, coef)
+            assert same_bits(n, r["normals"]), (obj, coef)
