@@ -1,10 +1,10 @@
 """CPU restatement of the reference's unstructured marching mappers.
 
 TEST INFRASTRUCTURE ONLY: the checker for kvsmc_marching_cells_host and
-kvsmc_slice_cells_host (imported
-by tests/ and bench.py's CPU-baseline leg, never by kvs_gb300).  numpy,
+kvsmc_slice_cells_host (imported by tests/, by __graft_entry__.smoke() as the
+checker and by bench.py's CPU-baseline leg, never by kvs_gb300).  numpy,
 vectorised over cells; pinned against the reference's own outputs in
-tests/golden/cells.npz.
+tests/golden/cells.npz and tests/golden/slice_cells.npz.
 
 Follows (Source/Core/Visualization/Mapper/):
   MarchingTetrahedra.cpp:155-236, MarchingHexahedra.cpp:143-230,

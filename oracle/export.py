@@ -1,6 +1,7 @@
-"""CPU restatement of the reference's binary STL export of a triangle mesh.
+"""CPU restatement of the reference's binary STL and PLY export of a triangle mesh.
 
-Test infrastructure only (the checker for kvsmc_stl_records / kvsmc_write_stl).
+Test infrastructure only (the checker for kvsmc_stl_records / kvsmc_write_stl
+and kvsmc_ply_records / kvsmc_write_ply; imported by tests/ only).
 Follows:
   PolygonExporter<kvs::Stl>::exec   Source/Core/Visualization/Exporter/PolygonExporter.cpp:78-176
     - no connections: the coords as they are; else coords expanded through the
