@@ -95,12 +95,13 @@ def large_slice_cases():
 
 
 def default_tf_range(v):
-    """MapperBase::setRange with a default transfer function (no NaN values)."""
+    """MapperBase::setRange with a default transfer function (no NaN values):
+    the volume's min/max as doubles, then the float range."""
     if v.dtype == np.int8:
         return np.float32(-128), np.float32(127)
     if v.dtype == np.uint8:
         return np.float32(0), np.float32(255)
-    return np.float32(v.min()), np.float32(v.max())
+    return np.float32(float(v.min())), np.float32(float(v.max()))
 
 
 @pytest.mark.skipif(not ref.available(), reason="needs the reference build (oracle/_ref)")
@@ -136,3 +137,30 @@ def test_restatement_matches_reference_with_object_coords():
             assert same_bits(c, r["coords"]), (obj, coef, first_diff(c, r["coords"]))
             assert np.array_equal(rgb, r["colors"]), (obj, coef)
             assert same_bits(n, r["normals"]), (obj, coef)
+
+
+@pytest.mark.skipif(not ref.available(), reason="needs the reference build (oracle/_ref)")
+def test_restatement_matches_reference_on_full_range_values():
+    """All ten value types with values across the type's whole range, so that
+    the difference values[i1] - values[i0] wraps in the narrow and 64-bit
+    integer types as it does in C++ (colour from the wrapped difference)."""
+    from oracle import slice as OS
+    from .helpers import first_diff, golden
+    table = golden()[1]["colormap256"]
+    rng = np.random.default_rng(23)
+    shape = (11, 14, 37)
+    for dt in (np.int8, np.uint8, np.int16, np.uint16, np.int32, np.uint32, np.int64, np.uint64,
+               np.float32, np.float64):
+        if np.issubdtype(dt, np.integer):
+            info = np.iinfo(dt)
+            v = rng.integers(info.min, info.max, shape, dtype=dt, endpoint=True)
+        else:
+            v = (rng.standard_normal(shape) * 1e6).astype(dt)
+        lo, hi = default_tf_range(v)
+        for coef in ((0.3, -0.55, 0.78, -4.2), (0, 1, 0, -6)):
+            r = ref.slice_plane(v, coefficients=list(coef), point=None, normal=None, tf_range=(float(lo), float(hi)))
+            c, rgb, n = OS.slice_plane(v, coef, table, lo, hi)
+            assert r["coords"].size > 0, (dt, coef)
+            assert same_bits(c, r["coords"]), (dt, coef, first_diff(c, r["coords"]))
+            assert np.array_equal(rgb, r["colors"]), (dt, coef, np.flatnonzero(rgb != r["colors"])[:5])
+            assert same_bits(n, r["normals"]), (dt, coef)
