@@ -167,3 +167,26 @@ def test_oracle_matches_reference_on_random_meshes_with_ties():
                 assert r["coords"].size > 0, (ct, dt, iso)
                 assert same_bits(o["coords"], r["coords"]), (ct, dt, iso, first_diff(o["coords"], r["coords"]))
                 assert same_bits(o["normals"], r["normals"]), (ct, dt, iso)
+
+
+@pytest.mark.skipif(not ref.available(), reason="needs the reference build (oracle/_ref)")
+def test_oracle_matches_reference_on_full_range_values():
+    """All ten value types with values across the type's whole range (64-bit
+    integers that doubles round, the volume's min/max clamp at the extremes),
+    isolevels inside the range."""
+    rng = np.random.default_rng(29)
+    for ct in range(4):
+        xyz, conn = cm.grid(ct, 9, 8, 7, seed=13 + ct)
+        for dt in (np.int8, np.uint8, np.int16, np.uint16, np.int32, np.uint32, np.int64, np.uint64,
+                   np.float32, np.float64):
+            if np.issubdtype(dt, np.integer):
+                info = np.iinfo(dt)
+                v = rng.integers(info.min, info.max, xyz.shape[0], dtype=dt, endpoint=True)
+            else:
+                v = (rng.standard_normal(xyz.shape[0]) * 1e30).astype(dt)
+            iso = float(v.min()) * 0.25 + float(v.max()) * 0.75
+            r = ref.marching_cells(ct, v, xyz, conn, iso)
+            o = ocells.marching_cells(ct, v, xyz, conn, iso)
+            assert r["coords"].size > 0, (ct, dt)
+            assert same_bits(o["coords"], r["coords"]), (ct, dt, first_diff(o["coords"], r["coords"]))
+            assert same_bits(o["normals"], r["normals"]), (ct, dt)
