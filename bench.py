@@ -887,7 +887,77 @@ def run_ours(args, rank, world, local):
         "gpu_launches": int(launches),
         "clocks": clk,
     }
+    # parity of this step's outputs at the bench size, after the timed region
+    if not args.no_verify and rank == 0:
+        v = verify_outputs(ctx, vol, w, reqs, outs, isos)
+        line["verified"] = v["verified"]
+        line["verify"] = v
     return line
+
+
+def verify_outputs(ctx, vol, w, reqs, outs, isos, planes=2, chunk_tris=1 << 20):
+    """Check the step's device outputs against the C oracle (oracle/mc_oracle.c)
+    without copying them back: per isovalue, position-keyed checksums of the
+    coords (9 words per triangle) and normals (3 per triangle) arrays in chunks
+    of 2^20 triangles (kvsmc_checksum_words on the device, mco_dup_checksum on
+    the host) and the triangle count.  Whole volume for the sweep and blob
+    workloads (every triangle of every output); for the 8 GiB stress volume
+    the first and last `planes` cell planes, compared with the first and last
+    triangles of each output (the last planes' node indices pass 2^32).
+    Runs after the timed region; isovalues on all host threads."""
+    from oracle import oracle
+    oracle.build()
+    t0 = time.perf_counter()
+    host = vol.download()
+    nz, ny, nx = host.shape
+    cz = nz - 1
+    full = w["kind"] != "lattice"
+    slabs = [(0, cz)] if full else [(0, planes), (cz - planes, cz)]
+    jobs = [(i, z0, z1) for i in range(len(isos)) for (z0, z1) in slabs]
+
+    def run(job):
+        i, z0, z1 = job
+        p = reqs[i].params
+        s = reqs[i].sizes
+        return oracle.dup_checksum(host, p.isolevel, s.min_value, s.max_value, z0, z1,
+                                   min_coord=tuple(p.min_coord), scale=tuple(p.scale), chunk_tris=chunk_tris)
+
+    with cf.ThreadPoolExecutor(max_workers=max(1, os.cpu_count() or 1)) as ex:
+        results = dict(zip(jobs, ex.map(run, jobs)))
+    t_oracle = time.perf_counter() - t0
+    per_iso, ok = [], True
+    for i, iso in enumerate(isos):
+        T = int(reqs[i].sizes.ntriangles)
+        entry = {"isovalue": round(float(iso), 6), "triangles": T, "slabs": []}
+        for (z0, z1) in slabs:
+            t, cs, ns = results[(i, z0, z1)]
+            first = 0 if z0 == 0 else T - t
+            sl = {"planes": [z0, z1], "triangles": int(t), "first_triangle": int(first)}
+            if full and t != T:
+                sl["count_mismatch"] = [int(t), T]
+                ok = False
+            elif t:
+                c, n = outs[i]
+                gc = ctx.checksum_words(c.data_ptr() + 4 * 9 * first, 9 * t, 9 * chunk_tris)
+                gn = ctx.checksum_words(n.data_ptr() + 4 * 3 * first, 3 * t, 3 * chunk_tris)
+                bad = [k for k in range(len(cs)) if cs[k] != gc[k] or ns[k] != gn[k]]
+                sl["coords_sum"] = f"{int(cs.sum(dtype=np.uint64)):016x}"
+                sl["normals_sum"] = f"{int(ns.sum(dtype=np.uint64)):016x}"
+                if bad:
+                    k = bad[0]
+                    sl["first_diff"] = {"chunk": k, "triangles": [first + k * chunk_tris,
+                                                                  first + min(t, (k + 1) * chunk_tris)],
+                                        "chunks_differing": len(bad)}
+                    ok = False
+            entry["slabs"].append(sl)
+        per_iso.append(entry)
+    return {"verified": ok, "oracle": "oracle/mc_oracle.c (mco_dup_checksum), one isovalue per host thread",
+            "method": "triangle counts + position-keyed checksums per 2^20 triangles of every coords and normals "
+                      "word (kvsmc_checksum_words on the device)",
+            "scope": "whole volume, every output" if full else
+                     f"first and last {planes} cell planes of every output",
+            "seconds": round(time.perf_counter() - t0, 1), "oracle_seconds": round(t_oracle, 1),
+            "isolevels": per_iso}
 
 
 def run_e2e(ctx, host_field, isos, reqs, args, stream):
@@ -1396,6 +1466,8 @@ def main():
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--tune", action="store_true", help="run the launch-shape autotuner before measuring")
+    ap.add_argument("--no-verify", action="store_true",
+                    help="skip the check of the outputs against the oracle after the timed region")
     args = ap.parse_args()
     args.warmup = max(3, args.warmup)
     rank, world, local = dist_env()

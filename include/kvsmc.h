@@ -310,7 +310,13 @@ kvsmc_status kvsmc_copy_to_host(kvsmc_context* ctx, void* host, const void* devi
  *     not fit (beyond about 512^3) is refused with KVSMC_ERR_TOO_LARGE;
  *   - the first call on each device looks up that array's device address
  *     (cudaGetSymbolAddress) with the device current: make that first call
- *     before starting any stream capture;
+ *     before starting any stream capture;  the address is kept for the life
+ *     of the process, so after a cudaDeviceReset (or anything else that
+ *     destroys and recreates the device's primary context) it is stale:
+ *     do not call this entry point again on that device;
+ *   - each call waits for its stream (cudaStreamSynchronize) to read back
+ *     the triangle count: twice, three times when the min/max is not
+ *     preset;
  *   - all calls share the array: calls that overlap on the GPU race on it
  *     and must be serialized by the caller.
  * Returns KVSMC_ERR_CAPACITY (with *sizes filled) when the outputs are too
@@ -611,6 +617,27 @@ kvsmc_status kvsmc_selftest_interpolation(kvsmc_context* ctx, uint64_t n, uint64
  * of the cells' emit pass against the FP64 sequence. */
 kvsmc_status kvsmc_selftest_cells(kvsmc_context* ctx, uint64_t n, uint64_t seed, uint64_t* tested,
                                   uint64_t* mismatches, uint64_t* fallbacks);
+
+/* Position-keyed checksums of a device array of 32-bit words, for checking
+ * outputs too large to copy back against a CPU run of the same extraction:
+ * sums[c] = sum over the words i of chunk c (words [c*chunk_words,
+ * (c+1)*chunk_words) of the array) of mix(i, w_i) mod 2^64, with
+ *   x = (i * 0x9E3779B97F4A7C15) ^ (w * 0xC2B2AE3D27D4EB4F);
+ *   x ^= x >> 31;  x *= 0xBF58476D1CE4E5B9;  x ^= x >> 29;  mix = x
+ * (64-bit unsigned arithmetic).  nchunks (at most 65535) must cover the
+ * array; sums is host memory.  No counterpart in the reference. */
+kvsmc_status kvsmc_checksum_words(kvsmc_context* ctx, const void* d_words, uint64_t nwords, uint64_t chunk_words,
+                                  uint64_t* sums, uint64_t nchunks);
+
+/* Test hook: cap the polls of the streaming count / emit kernels' bounded
+ * waits for a staged node plane (negative = the built-in limit, 2^22).  With
+ * a cap of 0 every such wait gives up at once, so an extraction returns
+ * KVSMC_ERR_TIMEOUT the way a stalled copy would make it; the kernels still
+ * drain their copies in flight under their own limit, and the context stays
+ * usable.  No counterpart in the reference (whose loop has no device waits);
+ * its error convention is a message and a null result
+ * (MarchingCubes.cpp:50-67). */
+kvsmc_status kvsmc_set_wait_limit(kvsmc_context* ctx, int64_t count_polls, int64_t emit_polls);
 
 #ifdef __cplusplus
 }

@@ -51,6 +51,7 @@ EXPORTS = [
     "kvsmc_slice_count", "kvsmc_slice_extract_device", "kvsmc_slice_plane",
     "kvsmc_marching_cells_host", "kvsmc_marching_cells_device", "kvsmc_selftest_cells", "kvsmc_slice_cells_host",
     "kvsmc_cells_bounds", "kvsmc_marching_cells_sweep_device", "kvsmc_ply_record_bytes", "kvsmc_ply_header", "kvsmc_ply_records", "kvsmc_write_ply", "kvsmc_write_ply_host",
+    "kvsmc_checksum_words", "kvsmc_set_wait_limit",
 ]
 
 PATH_AUTO = 0      # streaming kernels where eligible
@@ -228,6 +229,8 @@ def load(path=LIB_PATH):
         "kvsmc_autotune": (C.c_int, [vp, C.POINTER(AutotuneConfig), C.POINTER(TuneEntry), i32, C.POINTER(i32)]),
         "kvsmc_profile_enable": (C.c_int, [vp, i32]),
         "kvsmc_profile_read": (i32, [vp, i32, C.POINTER(C.c_char_p), C.POINTER(u64), C.POINTER(C.c_double)]),
+        "kvsmc_checksum_words": (C.c_int, [vp, vp, u64, u64, C.POINTER(u64), u64]),
+        "kvsmc_set_wait_limit": (C.c_int, [vp, C.c_int64, C.c_int64]),
     }
     for name, (res, args) in sig.items():
         f = getattr(lib, name)
@@ -285,6 +288,20 @@ class Context:
         ms = (C.c_double * max(1, n))()
         self.lib.kvsmc_profile_read(self.handle, n, names, launches, ms)
         return {names[i].decode(): (int(launches[i]), float(ms[i])) for i in range(n)}
+
+    def checksum_words(self, ptr, nwords, chunk_words):
+        """Per-chunk position-keyed sums of a device array of 32-bit words
+        (kvsmc_checksum_words); numpy uint64, one per chunk."""
+        nchunks = max(1, (int(nwords) + int(chunk_words) - 1) // int(chunk_words))
+        out = np.zeros(nchunks, dtype=np.uint64)
+        self.check(self.lib.kvsmc_checksum_words(self.handle, C.c_void_p(int(ptr)), int(nwords), int(chunk_words),
+                                                 out.ctypes.data_as(C.POINTER(C.c_uint64)), nchunks),
+                   "kvsmc_checksum_words")
+        return out
+
+    def set_wait_limit(self, count_polls=-1, emit_polls=-1):
+        self.check(self.lib.kvsmc_set_wait_limit(self.handle, int(count_polls), int(emit_polls)),
+                   "kvsmc_set_wait_limit")
 
     def selftest_interpolation(self, n, seed=1):
         t, m, f = C.c_uint64(), C.c_uint64(), C.c_uint64()

@@ -18,12 +18,6 @@ namespace {
 
 bool stream_dtype(int dt) { return dt == KVSMC_I8 || dt == KVSMC_I16 || dt == KVSMC_U8 || dt == KVSMC_U16 || dt == KVSMC_F32; }
 
-uint32_t segments_per_row(const kvsmc::VolumeView& v, int rows)
-{
-    const uint32_t seg = kvsmc::kStreamSegCells / rows;
-    return (v.nx - 1 + seg - 1) / seg;
-}
-
 }  // namespace
 
 // FP32 fast-path constants of one request (see mc_interp.cuh).
@@ -200,10 +194,9 @@ void StreamBatch::plan_tables()
             g.brick_wpr = (v.nx - 1 + kvsmc::kBrickCells - 1) / kvsmc::kBrickCells;
             g.wpr = segments_per_row(v, rows);
             g.zchunk = zchunk;
-            const uint32_t cy = v.ny - 1, cz = v.nz - 1;
-            const uint32_t zchunks = (cz + g.zchunk - 1) / g.zchunk;
+            const uint32_t cz = v.nz - 1;
             g.task_begin = L.ntasks;
-            L.ntasks += (uint64_t)((cy + rows - 1) / rows) * g.wpr * zchunks;
+            L.ntasks += stream_tasks(v, rows, g.wpr, g.zchunk);
             g.seg_elems = (uint32_t)kvsmc::stream_row_elems(dt, rows);
             g.seg_copy_bytes = g.seg_elems * (uint32_t)kvsmc::dtype_size(dt);
             g.warp_smem_bytes = (uint32_t)kvsmc::stream_warp_smem_bytes(dt, true, rows);
@@ -217,7 +210,7 @@ void StreamBatch::plan_tables()
             g.niso = (int32_t)sorted.size();
             bucket_params(sorted.front().first, sorted.back().first, g.bs, g.bo);
             g.unit_base = unit_elems;
-            unit_elems += (uint64_t)cz * cy * g.wpr * g.niso;
+            unit_elems += stream_units(v, g.wpr, g.niso);
             g.plane_begin = scan_blocks;
             scan_blocks += cz;
             for (auto& pr : sorted) {

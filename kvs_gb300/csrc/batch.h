@@ -21,6 +21,27 @@ uint32_t stream_zchunk(uint64_t warp_steps, int num_sms, int tasks_per_sm = kDef
 // that idles fewer lanes than 256-cell segments, else 1.
 int stream_rows(uint32_t cx);
 
+// Row segments per cell row of a volume tiled with `rows` cell rows per warp
+// task (256 / rows cells per segment).
+inline uint32_t segments_per_row(const kvsmc::VolumeView& v, int rows)
+{
+    const uint32_t seg = kvsmc::kStreamSegCells / rows;
+    return (v.nx - 1 + seg - 1) / seg;
+}
+
+// Warp tasks of one volume: (cell-row groups) x segments x z-chunks.
+inline uint64_t stream_tasks(const kvsmc::VolumeView& v, int rows, uint32_t wpr, uint32_t zchunk)
+{
+    const uint32_t cy = v.ny - 1, cz = v.nz - 1;
+    return (uint64_t)((cy + rows - 1) / rows) * wpr * ((cz + zchunk - 1) / zchunk);
+}
+
+// (unit, isolevel) counters of one volume: one per (z, cell row, segment, isolevel).
+inline uint64_t stream_units(const kvsmc::VolumeView& v, uint32_t wpr, int niso)
+{
+    return (uint64_t)(v.nz - 1) * (v.ny - 1) * wpr * (uint64_t)niso;
+}
+
 // A batch of streaming-eligible requests.  plan() builds the work tables,
 // count() fills every item's sizes, emit() writes the outputs of the items
 // with emit set and enough capacity (status OK), finish() waits for them.

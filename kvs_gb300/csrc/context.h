@@ -36,6 +36,8 @@ struct kvsmc_context {
     size_t h_stage_bytes = 0;
     uint64_t launches = 0;
     int path = 0;                // 0: streaming kernels where eligible, 1: gather kernels only
+    // plane-wait poll limits of the streaming count / emit kernels (kvsmc_set_wait_limit)
+    uint32_t wait_polls[2] = {kvsmc::kStreamWaitPolls, kvsmc::kStreamWaitPolls};
     kvsmc::Profiler* prof = nullptr;
     std::string last_error;
     // auxiliary streams for launches that may run side by side (created on first use)
@@ -68,7 +70,10 @@ kvsmc_status fail(kvsmc_context* ctx, kvsmc_status st, const char* fmt, ...);
 inline size_t align_up(size_t v, size_t a) { return (v + a - 1) / a * a; }
 inline kvsmc::Launch launch_of(kvsmc_context* ctx)
 {
-    return kvsmc::Launch{ctx->stream, ctx->num_sms, &ctx->launches, ctx->prof};
+    kvsmc::Launch L{ctx->stream, ctx->num_sms, &ctx->launches, ctx->prof};
+    L.wait_polls[0] = ctx->wait_polls[0];
+    L.wait_polls[1] = ctx->wait_polls[1];
+    return L;
 }
 kvsmc_status ensure_scratch(kvsmc_context* ctx, size_t bytes);
 kvsmc_status ensure_stage(kvsmc_context* ctx, size_t bytes);

@@ -12,7 +12,9 @@ order the mapper emits them (tetrahedra and prisms take TriangleID[i], [i+1],
 [i+2]; hexahedra and pyramids [i], [i+2], [i+1]), and per edge its two local
 node indices.
 
-    python kvs_gb300/csrc/gen_cell_tables.py /root/reference/Source/Core/Visualization/Mapper
+    python kvs_gb300/csrc/gen_cell_tables.py <KVS>/Source/Core/Visualization/Mapper
+
+(or with KVS_SRC=<KVS>/Source in the environment and no argument).
 """
 import os
 import re
@@ -61,7 +63,12 @@ def pack(rows, swap):
 
 
 def main():
-    src = sys.argv[1] if len(sys.argv) > 1 else "/root/reference/Source/Core/Visualization/Mapper"
+    if len(sys.argv) > 1:
+        src = sys.argv[1]
+    elif os.environ.get("KVS_SRC"):
+        src = os.path.join(os.environ["KVS_SRC"], "Core", "Visualization", "Mapper")
+    else:
+        sys.exit("usage: gen_cell_tables.py <KVS Source/Core/Visualization/Mapper directory> (or set KVS_SRC)")
     lines = ["// cell_tables.h -- generated by gen_cell_tables.py from the reference's",
              "// unstructured-grid marching tables; do not edit.", "#pragma once", "#include <cstdint>", ""]
     for name, fn, ncases, rowlen, nedges, swap in CELLS:

@@ -9,7 +9,9 @@ the CUDA kernels use, into mc_tables.h, which is committed so that builds do
 not need the reference.  tests/test_tables.py re-parses the reference (where
 it is present) and checks the committed header entry for entry.
 
-    python kvs_gb300/csrc/gen_mc_tables.py /root/reference/Source/Core/Visualization/Mapper/MarchingCubesTable.cpp
+    python kvs_gb300/csrc/gen_mc_tables.py <KVS>/Source/Core/Visualization/Mapper/MarchingCubesTable.cpp
+
+(or with KVS_SRC=<KVS>/Source in the environment and no argument).
 """
 import os
 import re
@@ -120,8 +122,12 @@ def render(tri_rows, vert_rows):
 
 
 def main():
-    src = sys.argv[1] if len(sys.argv) > 1 else \
-        "/root/reference/Source/Core/Visualization/Mapper/MarchingCubesTable.cpp"
+    if len(sys.argv) > 1:
+        src = sys.argv[1]
+    elif os.environ.get("KVS_SRC"):
+        src = os.path.join(os.environ["KVS_SRC"], "Core", "Visualization", "Mapper", "MarchingCubesTable.cpp")
+    else:
+        sys.exit("usage: gen_mc_tables.py <path of MarchingCubesTable.cpp> (or set KVS_SRC to the KVS Source tree)")
     tri, vert = parse_reference_tables(src)
     dst = os.path.join(os.path.dirname(os.path.abspath(__file__)), "mc_tables.h")
     with open(dst, "w") as f:

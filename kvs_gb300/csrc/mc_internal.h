@@ -10,12 +10,18 @@ namespace kvsmc {
 
 struct Profiler;
 
+// Polls of the streaming kernels' waits for a staged node plane before they
+// give up (KVSMC_ERR_TIMEOUT); a plane normally lands within a few polls.
+constexpr uint32_t kStreamWaitPolls = 1u << 22;
+
 // Launch bookkeeping passed to every launcher.
 struct Launch {
     cudaStream_t stream;
     int num_sms;
     uint64_t* counter;   // incremented once per kernel launch
     Profiler* prof;      // per-kernel CUDA-event timing when enabled (may be null)
+    // plane-wait poll limit of the streaming count [0] and emit [1] kernels
+    uint32_t wait_polls[2] = {kStreamWaitPolls, kStreamWaitPolls};
 };
 
 // CUDA events on the launching stream around one kernel family's launch.

@@ -284,7 +284,7 @@ __global__ void __launch_bounds__(kStreamThreads, EMIT ? 2 : 3)
     k_stream(const StreamGroup* __restrict__ groups, int ngroups, uint64_t ntasks, const StreamIso* __restrict__ isos,
              uint16_t* __restrict__ unit_counts, const uint32_t* __restrict__ unit_offsets,
              const uint64_t* __restrict__ plane_base, int* __restrict__ status,
-             unsigned long long* __restrict__ next_task)
+             unsigned long long* __restrict__ next_task, uint32_t wait_polls)
 {
     constexpr int LPR = 32 / R;                 // lanes per cell row
     constexpr int SEG = kSegCells / R;          // cells per row segment
@@ -430,7 +430,7 @@ __global__ void __launch_bounds__(kStreamThreads, EMIT ? 2 : 3)
     // wait (bounded) for plane i; on success the buffer's parity advances
     auto acquire = [&](uint32_t i) -> bool {
         const uint32_t b = i % 3u;
-        const bool ok = mbar_wait(&W.bar[b], (ph >> b) & 1u, 1u << 22);
+        const bool ok = mbar_wait(&W.bar[b], (ph >> b) & 1u, wait_polls);
         if (ok) ph ^= 1u << b;
         return ok;
     };
@@ -770,10 +770,10 @@ __global__ void __launch_bounds__(kStreamThreads, EMIT ? 2 : 3)
         }
     }
     if (dead) {
-        // After a timeout, wait (bounded) for the copies still in flight before
-        // leaving, so no bulk copy lands in shared memory this warp no longer
-        // uses; then stop taking tasks.  (A normal walk acquires every plane it
-        // issued.)
+        // After a timeout, wait (bounded, by its own limit whatever the plane
+        // waits' limit) for the copies still in flight before leaving, so no
+        // bulk copy lands in shared memory this warp no longer uses; then stop
+        // taking tasks.  (A normal walk acquires every plane it issued.)
         for (uint32_t i = acq; i < issued; ++i) {
             const uint32_t b = i % 3u;
             if (mbar_wait(&W.bar[b], (ph >> b) & 1u, 1u << 16)) ph ^= 1u << b;
@@ -980,7 +980,7 @@ cudaError_t launch_stream(bool emit, int dtype, int rows, const StreamGroup* d_g
         prof_begin(L, emit ? "stream_emit" : "stream_count");
         kern<<<(unsigned)nctas, kStreamThreads, smem, L.stream>>>(d_groups, ngroups, ntasks, d_isos, d_unit_counts,
                                                                    d_unit_offsets, d_plane_base, d_status,
-                                                                   d_next_task);
+                                                                   d_next_task, L.wait_polls[emit ? 1 : 0]);
         prof_end(L);
     });
     *L.counter += 1;

@@ -113,17 +113,16 @@ extern "C" kvsmc_status kvsmc_extract_noalloc(const void* d_values, kvsmc_dtype 
     std::memset(&g, 0, sizeof g);
     g.vol = v;
     const int rows = kvsmc_host::stream_rows(nx - 1);
-    const uint32_t seg_cells = (uint32_t)(kStreamSegCells / rows);
     g.rows = (uint32_t)rows;
-    g.wpr = (nx - 1 + seg_cells - 1) / seg_cells;
+    g.wpr = kvsmc_host::segments_per_row(v, rows);
     if (stream_shared_bytes(dtype, true, rows) > (size_t)227 * 1024 ||
         (double)(nx - 1) * (double)(ny - 1) * 5.0 >= 4294967295.0)
         return KVSMC_ERR_TOO_LARGE;
     const uint32_t cy = ny - 1, cz = nz - 1;
     const uint32_t cyr = (cy + rows - 1) / rows;
     g.zchunk = kvsmc_host::stream_zchunk((uint64_t)cz * cyr * g.wpr, num_sms);
-    const uint64_t ntasks = (uint64_t)cyr * g.wpr * ((cz + g.zchunk - 1) / g.zchunk);
-    const uint64_t units = (uint64_t)cz * cy * g.wpr;   // one isolevel: one counter per unit
+    const uint64_t ntasks = kvsmc_host::stream_tasks(v, rows, g.wpr, g.zchunk);
+    const uint64_t units = kvsmc_host::stream_units(v, g.wpr, 1);   // one isolevel: one counter per unit
     g.task_begin = 0;
     g.unit_base = 0;
     g.plane_begin = 0;

@@ -105,7 +105,61 @@ typedef struct {
     uint32_t line, slice;     /* numberOfNodesPerLine / PerSlice as UInt32 */
     double iso, vmin, vmax;
     vec3 min_coord, scale;
+    uint32_t z0, z1;          /* cell planes visited by the duplicated loop */
 } mc_state;
+
+/*
+ * Where the duplicated loop's triangles go: appended to coords/normals as the
+ * reference's push_back does, or (chunk_tris > 0) folded into position-keyed
+ * checksums per chunk of chunk_tris triangles, the same sums as
+ * kvsmc_checksum_words over the coords (9 words per triangle) and normals
+ * (3 words per triangle) arrays, so outputs too large to copy can be compared.
+ */
+typedef struct {
+    fbuf* coords;
+    fbuf* normals;
+    uint64_t chunk_tris;
+    uint64_t* coord_sums;
+    uint64_t* normal_sums;
+    uint64_t nchunks;
+    uint64_t ntri;
+    int overflow;             /* more triangles than nchunks * chunk_tris */
+} mco_sink;
+
+/* the checksum term of word w at index i (kvsmc_checksum_words) */
+static inline uint64_t mco_mix(uint64_t i, uint32_t w)
+{
+    uint64_t x = (i * 0x9E3779B97F4A7C15ull) ^ ((uint64_t)w * 0xC2B2AE3D27D4EB4Full);
+    x ^= x >> 31;
+    x *= 0xBF58476D1CE4E5B9ull;
+    x ^= x >> 29;
+    return x;
+}
+
+static inline uint32_t fbits(float f) { uint32_t u; memcpy(&u, &f, 4); return u; }
+
+static int sink_triangle(mco_sink* k, const vec3 q[3], vec3 n)
+{
+    if (!k->chunk_tris) {
+        for (int j = 0; j < 3; ++j)
+            if (fbuf_push3(k->coords, q[j].x, q[j].y, q[j].z)) return -1;
+        if (fbuf_push3(k->normals, n.x, n.y, n.z)) return -1;
+    } else {
+        const uint64_t t = k->ntri, c = t / k->chunk_tris;
+        if (c >= k->nchunks) {
+            k->overflow = 1;
+        } else {
+            const float w[9] = { q[0].x, q[0].y, q[0].z, q[1].x, q[1].y, q[1].z, q[2].x, q[2].y, q[2].z };
+            uint64_t h = 0;
+            for (int j = 0; j < 9; ++j) h += mco_mix(9 * t + (uint64_t)j, fbits(w[j]));
+            k->coord_sums[c] += h;
+            k->normal_sums[c] += mco_mix(3 * t, fbits(n.x)) + mco_mix(3 * t + 1, fbits(n.y)) +
+                                 mco_mix(3 * t + 2, fbits(n.z));
+        }
+    }
+    k->ntri++;
+    return 0;
+}
 
 /*
  * GetMinMaxValues<T>, veclen == 1 (Visualization/Object/StructuredVolumeObject.cpp:66-85):
@@ -187,11 +241,11 @@ static void cell_nodes(size_t base, uint32_t line, uint32_t slice, size_t li[8])
  * each edge interpolated in the table's direction; normal (v23-v01)x(v45-v01).
  */
 #define MCO_DUP(CODE, T) \
-    static int dup_##CODE(const mc_state* s, fbuf* coords, fbuf* normals) { \
+    static int dup_##CODE(const mc_state* s, mco_sink* sink) { \
         const T* vals = (const T*)s->values; \
-        const uint32_t cx = s->nx - 1, cy = s->ny - 1, cz = s->nz - 1; \
+        const uint32_t cx = s->nx - 1, cy = s->ny - 1; \
         size_t li[8]; \
-        for (uint32_t z = 0; z < cz; ++z) \
+        for (uint32_t z = s->z0; z < s->z1; ++z) \
         for (uint32_t y = 0; y < cy; ++y) \
         for (uint32_t x = 0; x < cx; ++x) { \
             const size_t base = (size_t)x + (size_t)y * s->line + (size_t)z * s->slice; \
@@ -208,10 +262,9 @@ static void cell_nodes(size_t base, uint32_t line, uint32_t slice, size_t li[8])
                     vec3 pa = { (float)(x + (uint32_t)a[0]), (float)(y + (uint32_t)a[1]), (float)(z + (uint32_t)a[2]) }; \
                     vec3 pb = { (float)(x + (uint32_t)b[0]), (float)(y + (uint32_t)b[1]), (float)(z + (uint32_t)b[2]) }; \
                     q[k] = interp_##CODE(s, pa, pb); \
-                    if (fbuf_push3(coords, q[k].x, q[k].y, q[k].z)) return -1; \
                 } \
                 const vec3 n = cross3(sub3(q[1], q[0]), sub3(q[2], q[0])); \
-                if (fbuf_push3(normals, n.x, n.y, n.z)) return -1; \
+                if (sink_triangle(sink, q, n)) return -1; \
             } \
         } \
         return 0; \
@@ -350,13 +403,18 @@ int mco_extract(int dtype, const void* values, uint32_t nx, uint32_t ny, uint32_
     s.iso = iso; s.vmin = vmin; s.vmax = vmax;
     s.min_coord.x = min_coord[0]; s.min_coord.y = min_coord[1]; s.min_coord.z = min_coord[2];
     s.scale.x = scale[0]; s.scale.y = scale[1]; s.scale.z = scale[2];
+    s.z0 = 0; s.z1 = nz - 1;
 
     fbuf coords = { 0 }, normals = { 0 };
     ubuf conn = { 0 };
     int rc = 0;
     if (mode == 0) {
+        mco_sink sink;
+        memset(&sink, 0, sizeof sink);
+        sink.coords = &coords;
+        sink.normals = &normals;
         switch (dtype) {
-#define MCO_DUP_CASE(CODE, T) case CODE: rc = dup_##CODE(&s, &coords, &normals); break;
+#define MCO_DUP_CASE(CODE, T) case CODE: rc = dup_##CODE(&s, &sink); break;
             MCO_TYPE_LIST(MCO_DUP_CASE)
         default: return -2;
         }
@@ -383,6 +441,47 @@ int mco_extract(int dtype, const void* values, uint32_t nx, uint32_t ny, uint32_
     out->normals = normals.p; out->nnormals = normals.n;
     out->connections = conn.p; out->nconnections = conn.n;
     return 0;
+}
+
+/*
+ * The duplicated loop of mco_extract (extract_surfaces_with_duplication<T>,
+ * MarchingCubes.cpp:156-243) over the cell planes [z0, z1) of the whole
+ * volume, with the triangles folded into per-chunk checksums instead of
+ * stored (see mco_sink); coordinates are the volume's own, so a slab's
+ * triangles are the same bits as that stretch of a whole-volume run.
+ * Returns 0, -2 for a bad dtype or range, -3 when the triangles overflow
+ * nchunks * chunk_tris (*ntri is still the count).
+ */
+int mco_dup_checksum(int dtype, const void* values, uint32_t nx, uint32_t ny, uint32_t nz, uint32_t z0,
+                     uint32_t z1, double iso, double vmin, double vmax, const float min_coord[3],
+                     const float scale[3], uint64_t chunk_tris, uint64_t* coord_sums, uint64_t* normal_sums,
+                     uint64_t nchunks, uint64_t* ntri)
+{
+    if (nx < 2 || ny < 2 || nz < 2 || z0 > z1 || z1 > nz - 1 || chunk_tris == 0) return -2;
+    mc_state s;
+    s.values = values; s.dtype = dtype; s.nx = nx; s.ny = ny; s.nz = nz;
+    s.line = nx; s.slice = nx * ny;
+    s.iso = iso; s.vmin = vmin; s.vmax = vmax;
+    s.min_coord.x = min_coord[0]; s.min_coord.y = min_coord[1]; s.min_coord.z = min_coord[2];
+    s.scale.x = scale[0]; s.scale.y = scale[1]; s.scale.z = scale[2];
+    s.z0 = z0; s.z1 = z1;
+    mco_sink sink;
+    memset(&sink, 0, sizeof sink);
+    sink.chunk_tris = chunk_tris;
+    sink.coord_sums = coord_sums;
+    sink.normal_sums = normal_sums;
+    sink.nchunks = nchunks;
+    memset(coord_sums, 0, nchunks * sizeof(uint64_t));
+    memset(normal_sums, 0, nchunks * sizeof(uint64_t));
+    int rc = 0;
+    switch (dtype) {
+#define MCO_DUP_SUM_CASE(CODE, T) case CODE: rc = dup_##CODE(&s, &sink); break;
+        MCO_TYPE_LIST(MCO_DUP_SUM_CASE)
+    default: return -2;
+    }
+    *ntri = sink.ntri;
+    if (rc) return rc;
+    return sink.overflow ? -3 : 0;
 }
 
 /*

@@ -83,6 +83,10 @@ def lib():
             C.POINTER(_Out)]
         _lib.mco_color_at.argtypes = [C.c_void_p, C.c_int, C.c_float, C.c_float, C.c_float, C.c_void_p]
         _lib.mco_free.argtypes = [C.POINTER(_Out)]
+        _lib.mco_dup_checksum.argtypes = [C.c_int, C.c_void_p, C.c_uint32, C.c_uint32, C.c_uint32,
+                                          C.c_uint32, C.c_uint32, C.c_double, C.c_double, C.c_double,
+                                          C.c_void_p, C.c_void_p, C.c_uint64, C.c_void_p, C.c_void_p,
+                                          C.c_uint64, C.POINTER(C.c_uint64)]
     return _lib
 
 
@@ -159,3 +163,45 @@ def marching_cubes(values, isolevel, normal_type="polygon", duplication=True, mi
     r = _collect(o)
     lib().mco_free(C.byref(o))
     return r
+
+
+def mix_checksum(words, chunk_words):
+    """The checksum of kvsmc_checksum_words in numpy (per chunk of a uint32
+    array, index from the array's start); a check of the C and CUDA sums."""
+    w = np.ascontiguousarray(words).view(np.uint32).astype(np.uint64)
+    i = np.arange(w.size, dtype=np.uint64)
+    with np.errstate(over="ignore"):
+        x = (i * np.uint64(0x9E3779B97F4A7C15)) ^ (w * np.uint64(0xC2B2AE3D27D4EB4F))
+        x ^= x >> np.uint64(31)
+        x *= np.uint64(0xBF58476D1CE4E5B9)
+        x ^= x >> np.uint64(29)
+    n = (w.size + chunk_words - 1) // chunk_words
+    return np.array([int(x[c * chunk_words:(c + 1) * chunk_words].sum(dtype=np.uint64)) for c in range(n)],
+                    dtype=np.uint64)
+
+
+def dup_checksum(values, isolevel, vmin, vmax, z0=0, z1=None, min_coord=(0, 0, 0), scale=(1, 1, 1),
+                 chunk_tris=1 << 20, nchunks=None):
+    """Duplicated-mode extraction over the cell planes [z0, z1) of the whole
+    volume, folded into per-chunk checksums (mco_dup_checksum).  Returns
+    (triangles, coord sums, normal sums); the sums cover chunks of chunk_tris
+    triangles, 9 words (coords) and 3 words (normals) per triangle.  The C
+    call releases the GIL, so threads can run several isolevels at once."""
+    v = np.ascontiguousarray(values)
+    nz, ny, nx = v.shape
+    z1 = nz - 1 if z1 is None else z1
+    if nchunks is None:
+        # at most 5 triangles per cell
+        nchunks = max(1, ((nx - 1) * (ny - 1) * (z1 - z0) * 5 + chunk_tris - 1) // chunk_tris)
+    cs = np.zeros(nchunks, np.uint64)
+    ns = np.zeros(nchunks, np.uint64)
+    mc = np.asarray(min_coord, np.float32)
+    sc = np.asarray(scale, np.float32)
+    t = C.c_uint64()
+    rc = lib().mco_dup_checksum(dtype_code(v.dtype), v.ctypes.data, nx, ny, nz, z0, z1, float(isolevel),
+                                float(vmin), float(vmax), mc.ctypes.data, sc.ctypes.data, chunk_tris,
+                                cs.ctypes.data, ns.ctypes.data, nchunks, C.byref(t))
+    if rc:
+        raise RuntimeError(f"oracle checksum failed ({rc})")
+    used = max(1, (t.value + chunk_tris - 1) // chunk_tris)
+    return t.value, cs[:used], ns[:used]

@@ -15,7 +15,9 @@ import numpy as np
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(HERE, "_ref", "libkvsref_mc.so")
-REFERENCE_SOURCE = "/root/reference/Source"
+# The reference tree this recipe compiles: $KVS_SRC, else the location the
+# build container mounts it at.  Every other file takes the path from here.
+REFERENCE_SOURCE = os.environ.get("KVS_SRC") or "/root/reference/Source"
 
 # dtype codes: order of the reference's type switch (MarchingCubes.cpp:115-124)
 DTYPES = [np.int8, np.int16, np.int32, np.int64, np.uint8, np.uint16,

@@ -112,3 +112,35 @@ def test_oracle_matches_reference_edge_options(oracle_lib):
             assert np.array_equal(a["connections"], b["connections"]), opts
             if a["coords"].size:
                 assert np.array_equal(a["colors"], b["color"]), opts
+
+
+def test_checksum_mode_matches_the_stored_outputs(oracle_lib):
+    """mco_dup_checksum (the oracle's loop folded into per-chunk checksums over
+    a z-range) gives the counts and sums of the stored duplicated output, and a
+    volume's slabs add up to the whole, so large outputs can be checked by sums."""
+    import numpy as np
+    from kvs_gb300 import synthetic as S
+    v = S.to_numpy(S.gaussian_blobs((40, 48, 56), seed=3))
+    lo, hi = float(v.min()), float(v.max())
+    o = oracle_lib.extract(v, 0.5, 0, lo, hi, min_coord=(1.5, -2.0, 0.25), scale=(0.5, 2.0, 1.0))
+    T = o["coords"].size // 9
+    t, cs, ns = oracle_lib.dup_checksum(v, 0.5, lo, hi, min_coord=(1.5, -2.0, 0.25), scale=(0.5, 2.0, 1.0),
+                                        chunk_tris=1000)
+    assert t == T > 3000
+    assert np.array_equal(cs, oracle_lib.mix_checksum(o["coords"], 9000))
+    assert np.array_equal(ns, oracle_lib.mix_checksum(o["normals"], 3000))
+    t0, c0, n0 = oracle_lib.dup_checksum(v, 0.5, lo, hi, 0, 17, min_coord=(1.5, -2.0, 0.25),
+                                         scale=(0.5, 2.0, 1.0), chunk_tris=1 << 30)
+    t1, c1, n1 = oracle_lib.dup_checksum(v, 0.5, lo, hi, 17, 39, min_coord=(1.5, -2.0, 0.25),
+                                         scale=(0.5, 2.0, 1.0), chunk_tris=1 << 30)
+    assert t0 + t1 == T
+    assert np.array_equal(c0, oracle_lib.mix_checksum(o["coords"][:9 * t0], 9 << 30))
+    assert np.array_equal(c1, oracle_lib.mix_checksum(o["coords"][9 * t0:], 9 << 30))
+    assert np.array_equal(n1, oracle_lib.mix_checksum(o["normals"][3 * t0:], 3 << 30))
+    # a changed bit or two swapped triangles change the sums
+    bad = o["coords"].copy()
+    bad.view(np.uint32)[5] ^= 1
+    assert not np.array_equal(cs, oracle_lib.mix_checksum(bad, 9000))
+    sw = o["coords"].reshape(-1, 9).copy()
+    sw[[10, 11]] = sw[[11, 10]]
+    assert not np.array_equal(cs, oracle_lib.mix_checksum(sw.ravel(), 9000))

@@ -7,7 +7,9 @@ import pytest
 
 ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 HEADER = os.path.join(ROOT, "kvs_gb300", "csrc", "mc_tables.h")
-REF_TABLE = "/root/reference/Source/Core/Visualization/Mapper/MarchingCubesTable.cpp"
+from oracle import ref as _ref
+
+REF_TABLE = os.path.join(_ref.REFERENCE_SOURCE, "Core", "Visualization", "Mapper", "MarchingCubesTable.cpp")
 
 
 def _header_tables():

@@ -33,13 +33,28 @@ def _existing_entry_point(ctx, vol, params):
     return c[:s.ncoords].cpu().numpy(), n[:s.nnormals].cpu().numpy(), s.ntriangles
 
 
-def test_noalloc_matches_extract_device(kvsmc_ctx):
+def _field(shape, dtype, seed):
+    """fbm in [0, 1] as float32, or spread over an integer type's range."""
+    f = S.fbm(shape, seed=seed, device="cuda")
+    dt = np.dtype(dtype)
+    if dt.kind == "f":
+        return S.to_numpy(f)
+    info = np.iinfo(dt)
+    return S.to_numpy(S._cast(f.double() * (info.max - info.min) + info.min, dt))
+
+
+def _isos(v, preset):
+    lo, hi = float(v.min()), float(v.max())
+    return [(lo + 0.45 * (hi - lo), False), (lo + 0.6 * (hi - lo), preset)]
+
+
+def _check_two_calls(kvsmc_ctx, v):
     lib = _abi.load()
-    v = S.to_numpy(S.fbm((40, 52, 64), seed=21))          # rows of 256 bytes
+    nz, ny, nx = v.shape
     d_values = torch.from_numpy(v).cuda()
     vol = _abi.DeviceVolume.upload(kvsmc_ctx, v)
     stream = torch.cuda.Stream()
-    for call, (iso, preset) in enumerate([(0.45, False), (0.6, True)]):
+    for call, (iso, preset) in enumerate(_isos(v, True)):
         params = _abi.make_params(iso, _abi.MODE_DUP_POLYGON_NORMAL,
                                   minmax=(float(v.min()), float(v.max())) if preset else None)
         ref_c, ref_n, ntri = _existing_entry_point(kvsmc_ctx, vol, params)
@@ -48,7 +63,7 @@ def test_noalloc_matches_extract_device(kvsmc_ctx):
         out_c = torch.full((cap,), -1.0, dtype=torch.float32, device="cuda")
         out_n = torch.full((cap,), -1.0, dtype=torch.float32, device="cuda")
         s = _abi.Sizes()
-        st = lib.kvsmc_extract_noalloc(C.c_void_p(d_values.data_ptr()), _abi.dtype_code(v.dtype), 64, 52, 40,
+        st = lib.kvsmc_extract_noalloc(C.c_void_p(d_values.data_ptr()), _abi.dtype_code(v.dtype), nx, ny, nz,
                                        C.byref(params), C.c_void_p(out_c.data_ptr()), cap,
                                        C.c_void_p(out_n.data_ptr()), cap, C.c_void_p(stream.cuda_stream), C.byref(s))
         assert st == _abi.OK, (call, _abi.status_string(st))
@@ -60,6 +75,23 @@ def test_noalloc_matches_extract_device(kvsmc_ctx):
         assert same_bits(got_n, ref_n), (call, first_diff(got_n, ref_n))
         # nothing written past the triangles it reported
         assert np.all(out_c[s.ncoords:].cpu().numpy() == -1.0)
+    vol.free()
+
+
+# every value type the call takes; rows of 64 values are 16-byte multiples for each
+@pytest.mark.parametrize("dtype", [np.float32, np.int8, np.uint8, np.int16, np.uint16])
+def test_noalloc_matches_extract_device(kvsmc_ctx, dtype):
+    _check_two_calls(kvsmc_ctx, _field((40, 52, 64), dtype, seed=21))
+
+
+def test_noalloc_narrow_rows(kvsmc_ctx):
+    # 99 cells per row: two 128-cell rows per warp task (the other tiling)
+    _check_two_calls(kvsmc_ctx, _field((30, 41, 100), np.float32, seed=5))
+
+
+def test_noalloc_near_the_limit(kvsmc_ctx):
+    # 512^3: intermediates of about 3.2 MB, just inside the 4 MiB array
+    _check_two_calls(kvsmc_ctx, _field((512, 512, 512), np.float32, seed=8))
 
 
 def test_noalloc_refuses_what_it_cannot_take(kvsmc_ctx):
