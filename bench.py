@@ -782,6 +782,8 @@ def run_ours(args, rank, world, local):
     vol = _abi.DeviceVolume.from_device(ctx, field.data_ptr(), dt, field.shape)
     host_field = None
     if not args.no_e2e:
+        # pinned host buffers next to the GPU's host link
+        args.numa = bind_near_gpu(local)
         host_field = torch.empty(field.shape, dtype=field.dtype, pin_memory=True)
         host_field.copy_(field)
     # the CPU baseline's sample: the first z-slab of this same field
@@ -960,6 +962,68 @@ def verify_outputs(ctx, vol, w, reqs, outs, isos, planes=2, chunk_tris=1 << 20):
             "isolevels": per_iso}
 
 
+def gpu_numa_node(local):
+    """NUMA node of the GPU's PCI function (sysfs), or None."""
+    try:
+        import torch
+        pr = torch.cuda.get_device_properties(local)
+        bdf = f"{pr.pci_domain_id:04x}:{pr.pci_bus_id:02x}:{pr.pci_device_id:02x}.0"
+        n = int(open(f"/sys/bus/pci/devices/{bdf}/numa_node").read().strip())
+        return n if n >= 0 else None
+    except Exception:
+        return None
+
+
+def node_cpus(node):
+    """CPUs of a NUMA node (sysfs cpulist), or an empty set."""
+    try:
+        text = open(f"/sys/devices/system/node/node{node}/cpulist").read().strip()
+    except OSError:
+        return set()
+    out = set()
+    for part in text.split(","):
+        if "-" in part:
+            a, b = part.split("-")
+            out.update(range(int(a), int(b) + 1))
+        elif part:
+            out.add(int(part))
+    return out
+
+
+def bind_near_gpu(local):
+    """Run this process on the host CPUs of the GPU's NUMA node (where they are
+    among the allowed ones), so pinned buffers allocated afterwards sit next to
+    the GPU's host link.  Returns what was done."""
+    node = gpu_numa_node(local)
+    info = {"gpu_numa_node": node}
+    if node is None or not hasattr(os, "sched_setaffinity"):
+        return info
+    allowed = os.sched_getaffinity(0)
+    near = node_cpus(node) & allowed
+    if near and near != allowed:
+        os.sched_setaffinity(0, near)
+        info["bound_cpus"] = len(near)
+    return info
+
+
+def page_numa_node(addr):
+    """NUMA node holding the page at a host address (move_pages query), or None."""
+    import ctypes
+    import platform
+    nr = {"x86_64": 279, "aarch64": 239}.get(platform.machine())
+    if nr is None:
+        return None
+    try:
+        libc = ctypes.CDLL(None, use_errno=True)
+        pages = (ctypes.c_void_p * 1)(addr & ~4095)
+        status = (ctypes.c_int * 1)(-1)
+        r = libc.syscall(ctypes.c_long(nr), ctypes.c_int(0), ctypes.c_ulong(1), pages, None, status,
+                         ctypes.c_int(0))
+        return int(status[0]) if r == 0 and status[0] >= 0 else None
+    except Exception:
+        return None
+
+
 def run_e2e(ctx, host_field, isos, reqs, args, stream):
     """Same sweep through kvsmc_extract_batch_host: H2D of the volume from
     pinned memory, both launches, D2H of every output into pinned buffers."""
@@ -984,16 +1048,32 @@ def run_e2e(ctx, host_field, isos, reqs, args, stream):
         _abi.extract_batch_host(ctx, host, params, buf)
     torch.cuda.synchronize()
     times = []
+    ctx.profile_enable(True)
     for _ in range(steps):
         t0 = time.perf_counter()
         out = _abi.extract_batch_host(ctx, host, params, buf)
         torch.cuda.synchronize()
         times.append(time.perf_counter() - t0)
+    prof = ctx.profile_read()
+    ctx.profile_enable(False)
     t = statistics.median(times)   # the call is host-bound (link transfers): the median damps host noise
     h2d = host.nbytes
     d2h = sum(o["coords"].nbytes + o["normals"].nbytes for o in out)
+    link = {}
+    for name, nbytes in (("copy_h2d", h2d), ("copy_d2h", d2h)):
+        n, ms = prof.get(name, (0, 0.0))
+        if n and ms > 0:
+            # device-side time of the copies (CUDA events on the copy's own stream)
+            link[name.replace("copy_", "") + "_GBs"] = round(nbytes * steps / (ms * 1e-3) / 1e9, 1)
+    link["pinned_numa_nodes"] = sorted({page_numa_node(host.ctypes.data)} |
+                                       {page_numa_node(a.ctypes.data) for a in list(pinned.values())[:4]} - {None})
+    link.update(getattr(args, "numa", {}))
     return {"step_ms": t * 1e3, "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h),
-            "api": "kvsmc_extract_batch_host", "steps": steps, "timing": "host clock, median of steps"}
+            "api": "kvsmc_extract_batch_host", "steps": steps, "timing": "host clock, median of steps",
+            "pipeline": "emit in 8 launches by plane ranges, each range's triangles copied to the host on a "
+                        "second stream while the next range is written",
+            "link": link,
+            "kernels_ms_per_step": {k: round(v[1] / steps, 3) for k, v in prof.items()}}
 
 
 # ----------------------------------------------------------------- uneven batch

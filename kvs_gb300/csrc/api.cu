@@ -488,6 +488,11 @@ void kvsmc_destroy(kvsmc_context* ctx)
         }
         cudaEventDestroy(ctx->fork_ev);
     }
+    if (ctx->copy_stream) {
+        cudaStreamSynchronize(ctx->copy_stream);
+        cudaStreamDestroy(ctx->copy_stream);
+        for (int i = 0; i < kvsmc_context::kParts; ++i) cudaEventDestroy(ctx->part_ev[i]);
+    }
     if (ctx->own_stream) cudaStreamDestroy(ctx->own_stream);
     delete ctx;
 }
@@ -772,6 +777,71 @@ static kvsmc_status copy_back(kvsmc_context* ctx, std::vector<Item*>& its, const
     return KVSMC_OK;
 }
 
+// Emit launches of a host call's streaming batch (ranges of cell planes): the
+// first part's outputs start crossing the host link after 1/8 of the emit.
+constexpr int kStreamHostParts = 8;
+
+// Streaming items of a host call: count, then the emit in parts by ranges of
+// cell planes, each part's triangles copied into the host arrays on the copy
+// stream while the next part is written.
+static kvsmc_status stream_host_pipeline(kvsmc_context* ctx, std::vector<Item*>& s_items, const Item* first_item,
+                                         kvsmc_host_alloc_fn alloc, void* user)
+{
+    StreamBatch b;
+    b.ctx = ctx;
+    b.items = s_items;
+    kvsmc_status st;
+    if ((st = b.plan()) || (st = b.count()) || (st = arena_outputs(ctx, s_items)) ||
+        (st = host_alloc(ctx, s_items, first_item, alloc, user)))
+        return st;
+    if (!ctx->copy_stream) {
+        KVSMC_CUDA(ctx, cudaStreamCreateWithFlags(&ctx->copy_stream, cudaStreamNonBlocking));
+        for (int i = 0; i < kvsmc_context::kParts; ++i)
+            KVSMC_CUDA(ctx, cudaEventCreateWithFlags(&ctx->part_ev[i], cudaEventDisableTiming));
+    }
+    // first triangle of every (isolevel, z) plane, relative to its isolevel
+    std::vector<uint64_t> pb(b.iso_planes);
+    if (b.iso_planes)
+        KVSMC_CUDA(ctx, cudaMemcpyAsync(pb.data(), b.d_plane_base, b.iso_planes * 8, cudaMemcpyDeviceToHost,
+                                        ctx->stream));
+    KVSMC_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    kvsmc::Launch Lc = launch_of(ctx);
+    Lc.stream = ctx->copy_stream;
+    int part = 0;
+    auto copy = [&](uint32_t z0, uint32_t z1, bool whole) -> kvsmc_status {
+        cudaEvent_t ev = ctx->part_ev[part++ % kvsmc_context::kParts];
+        KVSMC_CUDA(ctx, cudaEventRecord(ev, ctx->stream));
+        KVSMC_CUDA(ctx, cudaStreamWaitEvent(ctx->copy_stream, ev, 0));
+        kvsmc::prof_begin(Lc, "copy_d2h");
+        for (size_t i = 0; i < b.isos.size(); ++i) {
+            Item* it = b.iso_item[i];
+            const uint64_t total = it->sizes.ntriangles;
+            uint64_t t0 = 0, t1 = total;
+            if (!whole) {
+                const uint64_t first = pb[b.isos[i].plane_index];
+                t0 = pb[b.isos[i].plane_index + z0] - first;
+                const uint32_t cz = it->vol->view.nz - 1;
+                t1 = z1 < cz ? pb[b.isos[i].plane_index + z1] - first : total;
+            }
+            if (t1 <= t0) continue;
+            if (it->h_coords)
+                KVSMC_CUDA(ctx, cudaMemcpyAsync(static_cast<float*>(it->h_coords) + 9 * t0, it->d_coords + 9 * t0,
+                                                (t1 - t0) * 36, cudaMemcpyDeviceToHost, ctx->copy_stream));
+            if (it->h_normals)
+                KVSMC_CUDA(ctx, cudaMemcpyAsync(static_cast<float*>(it->h_normals) + 3 * t0, it->d_normals + 3 * t0,
+                                                (t1 - t0) * 12, cudaMemcpyDeviceToHost, ctx->copy_stream));
+        }
+        kvsmc::prof_end(Lc);
+        return KVSMC_OK;
+    };
+    st = b.emit_parts(kStreamHostParts, copy);
+    if (!st) st = b.finish();
+    const cudaError_t e = cudaStreamSynchronize(ctx->copy_stream);
+    if (!st && e != cudaSuccess)
+        st = fail(ctx, KVSMC_ERR_CUDA, "copy stream: %s", cudaGetErrorString(e));
+    return st;
+}
+
 kvsmc_status kvsmc_extract_batch_host(kvsmc_context* ctx, const void* host, kvsmc_dtype dtype, uint32_t nx,
                                       uint32_t ny, uint32_t nz, const kvsmc_params* params, int32_t n,
                                       kvsmc_host_alloc_fn alloc, void* user, kvsmc_sizes* sizes)
@@ -783,7 +853,13 @@ kvsmc_status kvsmc_extract_batch_host(kvsmc_context* ctx, const void* host, kvsm
     if (!ctx->host_vol) ctx->host_vol = new kvsmc_volume();
     kvsmc_volume* v = ctx->host_vol;
     if ((st = volume_alloc(ctx, dtype, nx, ny, nz, v))) return st;
-    if ((st = volume_copy_in(ctx, v, host, cudaMemcpyHostToDevice))) return st;
+    {
+        const kvsmc::Launch L = launch_of(ctx);
+        kvsmc::prof_begin(L, "copy_h2d");
+        st = volume_copy_in(ctx, v, host, cudaMemcpyHostToDevice);
+        kvsmc::prof_end(L);
+        if (st) return st;
+    }
     std::vector<Item> items((size_t)n);
     std::vector<Item*> s_items, g_items;
     kvsmc_status first = KVSMC_OK;
@@ -796,11 +872,7 @@ kvsmc_status kvsmc_extract_batch_host(kvsmc_context* ctx, const void* host, kvsm
         (stream_eligible(ctx, items[i]) ? s_items : g_items).push_back(&items[i]);
     }
     if (!s_items.empty()) {
-        StreamBatch b;
-        b.ctx = ctx;
-        b.items = s_items;
-        if ((st = b.plan()) || (st = b.count()) || (st = arena_outputs(ctx, s_items)) || (st = b.emit()) ||
-            (st = b.finish()) || (st = copy_back(ctx, s_items, items.data(), alloc, user))) {
+        if ((st = stream_host_pipeline(ctx, s_items, items.data(), alloc, user))) {
             for (Item* it : s_items) it->status = st;
             if (!first) first = st;
         }

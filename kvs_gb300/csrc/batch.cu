@@ -240,7 +240,7 @@ size_t StreamBatch::scratch_bytes() const
     return 16 * 256 + align_up(groups.size() * sizeof(StreamGroup), 256) + align_up(niso * sizeof(StreamIso), 256) +
            align_up(unit_elems * 2, 256) + align_up(unit_elems * 4, 256) + align_up(iso_planes * 4, 256) +
            align_up(iso_planes * 8, 256) + align_up(kvsmc::scan_scratch_bytes(iso_planes), 256) +
-           align_up(niso * 8, 256) + align_up(launches.size() * 16, 256) + 4 * 256;
+           align_up(niso * 8, 256) + align_up(launches.size() * 16, 256) + align_up(kMaxParts * 8, 256) + 5 * 256;
 }
 
 void StreamBatch::carve(char* base)
@@ -258,6 +258,7 @@ void StreamBatch::carve(char* base)
     d_total = cv.take<uint64_t>(256);
     d_status = cv.take<int>(256);
     d_next = cv.take<unsigned long long>(launches.size() * 16);
+    d_next_parts = cv.take<unsigned long long>(kMaxParts * 8);
 }
 
 kvsmc_status StreamBatch::plan()
@@ -354,6 +355,49 @@ kvsmc_status StreamBatch::emit()
         return kvsmc::launch_stream(true, l.dtype, l.rows, d_groups + l.g0, l.ng, l.ntasks, d_isos, d_unit_counts,
                                     d_unit_offsets, d_plane_base, d_status, d_next + 2 * i + 1, Li, l.ctas_per_sm);
     }));
+    return KVSMC_OK;
+}
+
+kvsmc_status StreamBatch::emit_parts(int parts, const std::function<kvsmc_status(uint32_t, uint32_t, bool)>& after)
+{
+    if (groups.size() != 1 || launches.size() != 1 || parts <= 1) {
+        kvsmc_status st = emit();
+        return st ? st : after(0, 0, true);
+    }
+    bool any = false;
+    for (size_t i = 0; i < isos.size(); ++i) {
+        Item* it = iso_item[i];
+        const bool ok = it->emit && it->status == KVSMC_OK && it->sizes.ntriangles > 0;
+        isos[i].coords = ok ? it->d_coords : nullptr;
+        isos[i].normals = ok ? it->d_normals : nullptr;
+        isos[i].cap_tris = ok ? cap_triangles(*it) : 0;
+        any = any || ok;
+    }
+    if (!any) return after(0, 0, true);
+    groups[0].skip_emit = 0;
+    kvsmc_status st = upload_tables();
+    if (st) return st;
+    // tasks are numbered z-chunk-major: a range of z-chunks is a range of tasks
+    const StreamGroup& g = groups[0];
+    const Launch1& l = launches[0];
+    const uint32_t cz = g.vol.nz - 1;
+    const uint64_t zchunks = (cz + g.zchunk - 1) / g.zchunk;
+    const uint64_t per_chunk = l.ntasks / zchunks;
+    if (parts > kMaxParts) parts = kMaxParts;
+    if ((uint64_t)parts > zchunks) parts = (int)zchunks;
+    KVSMC_CUDA(ctx, cudaMemsetAsync(d_next_parts, 0, kMaxParts * 8, ctx->stream));
+    const kvsmc::Launch L = launch_of(ctx);
+    uint64_t c0 = 0;
+    for (int p = 0; p < parts; ++p) {
+        const uint64_t c1 = zchunks * (uint64_t)(p + 1) / (uint64_t)parts;
+        KVSMC_CUDA(ctx, kvsmc::launch_stream(true, l.dtype, l.rows, d_groups, 1, c1 * per_chunk, d_isos, d_unit_counts,
+                                             d_unit_offsets, d_plane_base, d_status, d_next_parts + p, L,
+                                             l.ctas_per_sm, c0 * per_chunk));
+        const uint32_t z0 = (uint32_t)(c0 * g.zchunk);
+        const uint32_t z1 = (uint32_t)(c1 * g.zchunk < cz ? c1 * g.zchunk : cz);
+        if ((st = after(z0, z1, false))) return st;
+        c0 = c1;
+    }
     return KVSMC_OK;
 }
 

@@ -1,5 +1,6 @@
 // batch.h -- the streaming batch runner (batch.cu).
 #pragma once
+#include <functional>
 #include <vector>
 
 #include "context.h"
@@ -78,10 +79,22 @@ struct StreamBatch {
     int* d_status = nullptr;
     unsigned long long* d_next = nullptr;   // per launch: [2 i] count, [2 i + 1] emit task counter
 
+    unsigned long long* d_next_parts = nullptr;   // task counters of a split emit (kMaxParts)
+    static constexpr int kMaxParts = 16;
+
     kvsmc_status plan();
     kvsmc_status count();
     kvsmc_status emit();
     kvsmc_status finish();
+
+    // The emit as up to `parts` launches over consecutive ranges of cell
+    // planes, so the outputs of a finished range can leave while the next
+    // range is written.  Splits only a batch of one group (one volume, at
+    // most 16 isolevels); otherwise one launch.  After enqueueing each launch
+    // on the context's stream it calls after(z_begin, z_end, whole): the
+    // outputs of cell planes [z_begin, z_end) (every output when whole) are
+    // complete once the stream reaches that point.
+    kvsmc_status emit_parts(int parts, const std::function<kvsmc_status(uint32_t, uint32_t, bool)>& after);
 
     // The pieces of plan(): host tables, their device footprint, and the
     // device pointers carved from a region of scratch_bytes().

@@ -46,6 +46,11 @@ struct kvsmc_context {
     cudaEvent_t fork_ev = nullptr;
     cudaEvent_t join_ev[kAux] = {};
     bool aux_ready = false;
+    // copy stream of the host calls: results leave while later parts are
+    // written (created on first use), one event per emit part
+    cudaStream_t copy_stream = nullptr;
+    static constexpr int kParts = 16;
+    cudaEvent_t part_ev[kParts] = {};
     int* d_flag = nullptr;       // device word for checks of export calls (created on first use)
     int* h_flag = nullptr;       // pinned copy of it
     // export staging: two device record buffers, two pinned host buffers (grow-only)

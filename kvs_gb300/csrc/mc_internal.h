@@ -105,11 +105,13 @@ size_t stream_row_elems(int dtype, int rows);
 // d_next_task: a zeroed u64 per launch (the persistent warps' task counter).
 // d_unit_counts: written by the count launch; read by the emit launch to skip
 // steps without triangles.  ctas_per_sm: resident CTAs per SM of the
-// persistent grid (0: as many as fit; never more than fit).
+// persistent grid (0: as many as fit; never more than fit).  The launch runs
+// the warp tasks [task0, ntasks) of its groups (task0 > 0: a later part of a
+// launch split by z-chunks).
 cudaError_t launch_stream(bool emit, int dtype, int rows, const StreamGroup* d_groups, int ngroups, uint64_t ntasks,
                           const StreamIso* d_isos, uint16_t* d_unit_counts, const uint32_t* d_unit_offsets,
                           const uint64_t* d_plane_base, int* d_status, unsigned long long* d_next_task,
-                          const Launch& L, int ctas_per_sm = 0);
+                          const Launch& L, int ctas_per_sm = 0, uint64_t task0 = 0);
 // scan_threads: units per CTA pass (64, 128 or 256; 0 = 256).
 cudaError_t launch_unit_scan(const StreamGroup* d_groups, int ngroups, uint32_t nplanes, const StreamIso* d_isos,
                              const uint16_t* d_unit_counts, uint32_t* d_unit_offsets, uint32_t* d_plane_totals,

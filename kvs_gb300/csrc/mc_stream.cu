@@ -284,7 +284,7 @@ __global__ void __launch_bounds__(kStreamThreads, EMIT ? 2 : 3)
     k_stream(const StreamGroup* __restrict__ groups, int ngroups, uint64_t ntasks, const StreamIso* __restrict__ isos,
              uint16_t* __restrict__ unit_counts, const uint32_t* __restrict__ unit_offsets,
              const uint64_t* __restrict__ plane_base, int* __restrict__ status,
-             unsigned long long* __restrict__ next_task, uint32_t wait_polls)
+             unsigned long long* __restrict__ next_task, uint32_t wait_polls, uint64_t task0)
 {
     constexpr int LPR = 32 / R;                 // lanes per cell row
     constexpr int SEG = kSegCells / R;          // cells per row segment
@@ -333,7 +333,7 @@ __global__ void __launch_bounds__(kStreamThreads, EMIT ? 2 : 3)
     for (;;) {
     unsigned long long tk = 0;
     if (lane == 0) tk = atomicAdd(next_task, 1ull);
-    const uint64_t task = __shfl_sync(FULL, tk, 0);
+    const uint64_t task = task0 + __shfl_sync(FULL, tk, 0);
     if (task >= ntasks) break;
     int gi = gcur;
     if (gi < 0 || task < groups[gi].task_begin || (gi + 1 < ngroups && task >= groups[gi + 1].task_begin))
@@ -957,12 +957,12 @@ uint64_t brick_count(const VolumeView& v)
 cudaError_t launch_stream(bool emit, int dtype, int rows, const StreamGroup* d_groups, int ngroups, uint64_t ntasks,
                           const StreamIso* d_isos, uint16_t* d_unit_counts, const uint32_t* d_unit_offsets,
                           const uint64_t* d_plane_base, int* d_status, unsigned long long* d_next_task,
-                          const Launch& L, int ctas_per_sm)
+                          const Launch& L, int ctas_per_sm, uint64_t task0)
 {
-    if (ntasks == 0) return cudaSuccess;
+    if (ntasks <= task0) return cudaSuccess;
     if (rows != 1 && rows != 2) return cudaErrorInvalidValue;
     const size_t smem = stream_shared_bytes(dtype, emit, rows);
-    const uint64_t need = (ntasks + kWarps - 1) / kWarps;
+    const uint64_t need = (ntasks - task0 + kWarps - 1) / kWarps;
     KVSMC_STREAM_SWITCH(dtype, {
         auto kern = emit ? (rows == 1 ? k_stream<T, true, 1> : k_stream<T, true, 2>)
                          : (rows == 1 ? k_stream<T, false, 1> : k_stream<T, false, 2>);
@@ -980,7 +980,7 @@ cudaError_t launch_stream(bool emit, int dtype, int rows, const StreamGroup* d_g
         prof_begin(L, emit ? "stream_emit" : "stream_count");
         kern<<<(unsigned)nctas, kStreamThreads, smem, L.stream>>>(d_groups, ngroups, ntasks, d_isos, d_unit_counts,
                                                                    d_unit_offsets, d_plane_base, d_status,
-                                                                   d_next_task, L.wait_polls[emit ? 1 : 0]);
+                                                                   d_next_task, L.wait_polls[emit ? 1 : 0], task0);
         prof_end(L);
     });
     *L.counter += 1;
