@@ -91,6 +91,13 @@ WORKLOADS = {
                      desc="kvs::SlicePlane of a 512^3 float32 fBm field by the oblique plane through its centre "
                           "with normal (0.31, -0.52, 0.79) (the profiling case of slice1024: same kernels, "
                           "512 MiB on the device)"),
+    "blobs128vn": dict(shape=(128, 128, 128), kind="blobs", isos=[0.5], mode=2,
+                       desc="128^3 float32, 4 Gaussian blobs (sigma 8..24) + U[-0.01,0.01] noise, iso 0.5, "
+                            "VertexNormal (shared vertices + connections + per-vertex normals: the mode of the "
+                            "reference's own isosurface example)"),
+    "sweep1024vn": dict(shape=(1024, 1024, 1024), kind="fbm", isos=[0.2 + 0.04 * k for k in range(16)], mode=2,
+                        desc="1024^3 float32 fBm (as sweep1024), 16 isovalues 0.2..0.8 in one batched call, "
+                             "VertexNormal (shared vertices + connections + per-vertex normals)"),
     "blobs128": dict(shape=(128, 128, 128), kind="blobs", isos=[0.5],
                      desc="128^3 float32, 4 Gaussian blobs (sigma 8..24) + U[-0.01,0.01] noise, iso 0.5, "
                           "duplication=true, PolygonNormal"),
@@ -801,19 +808,24 @@ def run_ours(args, rank, world, local):
     args.isos = isos
     n = len(isos)
     reqs = (_abi.Request * n)()
+    mode = w.get("mode", _abi.MODE_DUP_POLYGON_NORMAL)
+    args.mode = mode
     for i, iso in enumerate(isos):
         reqs[i].volume = vol.handle
-        reqs[i].params = _abi.make_params(iso, _abi.MODE_DUP_POLYGON_NORMAL)
+        reqs[i].params = _abi.make_params(iso, mode)
     ctx.check(ctx.lib.kvsmc_count_batch(ctx.handle, reqs, n), "count")
     outs = []
     for i in range(n):
         s = reqs[i].sizes
         c = torch.empty(max(1, s.ncoords), dtype=torch.float32, device="cuda")
         nn = torch.empty(max(1, s.nnormals), dtype=torch.float32, device="cuda")
-        outs.append((c, nn))
+        k = torch.empty(max(1, s.nconnections), dtype=torch.int32, device="cuda")
+        outs.append((c, nn, k))
         reqs[i].d_coords, reqs[i].coords_capacity = c.data_ptr(), s.ncoords
         reqs[i].d_normals, reqs[i].normals_capacity = nn.data_ptr(), s.nnormals
+        reqs[i].d_connections, reqs[i].connections_capacity = k.data_ptr(), s.nconnections
     ntri = sum(reqs[i].sizes.ntriangles for i in range(n))
+    nvert = sum(reqs[i].sizes.nvertices for i in range(n))
     cells = (nx - 1) * (ny - 1) * (nz - 1) * n
 
     def step():
@@ -852,7 +864,16 @@ def run_ours(args, rank, world, local):
     dom = max(prof.items(), key=lambda kv: kv[1][1])
     emit_launches, emit_ms = prof.get("stream_emit", (0, 0.0))
     roofline = None
-    if emit_launches:
+    if mode != _abi.MODE_DUP_POLYGON_NORMAL:
+        # shared vertices: volume once per isovalue pass + 24 B per vertex (coords,
+        # vertex normals) + 12 B per triangle (connections), over the whole step
+        # (five kernel families, none dominant on its own)
+        algo_bytes = nx * ny * nz * dt.itemsize * n + 24 * nvert + 12 * ntri
+        achieved = algo_bytes / (step_ms * 1e-3) / 1e9
+        roofline = {"kernel": "whole step (gather kernels)", "bound": "hbm", "achieved": round(achieved, 1),
+                    "peak": hbm, "peak_kind": peak_kind, "unit": "GB/s", "frac": round(achieved / hbm, 4),
+                    "algorithmic_bytes_per_step": algo_bytes, "traffic": None}
+    elif emit_launches:
         per = emit_ms / emit_launches
         achieved = algo_bytes / (per * 1e-3) / 1e9
         tr = traffic_per_launch(args.workload)
@@ -862,7 +883,7 @@ def run_ours(args, rank, world, local):
                     "traffic": tr}
     # end to end through the C ABI with host buffers
     e2e = None
-    if host_field is not None:
+    if host_field is not None and mode == _abi.MODE_DUP_POLYGON_NORMAL:
         e2e = run_e2e(ctx, host_field, isos, reqs, args, stream)
         if e2e is not None:
             e2e["value"] = round(cells / (e2e.pop("step_ms") * 1e-3) / 1e6 * world, 1)
@@ -875,13 +896,16 @@ def run_ours(args, rank, world, local):
         "data": "synthetic (seeded field generated on the device)",
         "config": {"workload": w["desc"], "volume": [nx, ny, nz], "isovalues": n,
                    "isolevels": [round(x, 6) for x in isos],
-                   "mode": "duplication+PolygonNormal", "cache": "inputs larger than L2 (4 GiB volume, "
-                   "outputs ~48 B/triangle)" if args.workload in ("sweep1024", "heavy") else (
+                   "mode": {0: "duplication+PolygonNormal", 1: "shared vertices+PolygonNormal",
+                            2: "VertexNormal (shared vertices)"}[mode],
+                   "cache": "inputs larger than L2 (4 GiB volume, "
+                   "outputs ~48 B/triangle)" if args.workload in ("sweep1024", "sweep1024vn", "heavy") else (
                    "inputs larger than L2 (512 MiB volume)" if args.workload == "sweep512" else "input smaller than L2"),
                    "launch_shapes": "autotuned (--tune)" if tuning else "built-in rules"},
         "tuning": tuning,
         "mtris_per_s": round(ntri * world / (step_ms * 1e-3) / 1e6, 1),
         "triangles_per_step": int(ntri),
+        "vertices_per_step": int(nvert),
         "roofline": roofline,
         "kernels": {k: {"launches": v[0], "ms": round(v[1], 3)} for k, v in prof.items()},
         "dominant_kernel": dom[0],
@@ -891,7 +915,8 @@ def run_ours(args, rank, world, local):
     }
     # parity of this step's outputs at the bench size, after the timed region
     if not args.no_verify and rank == 0:
-        v = verify_outputs(ctx, vol, w, reqs, outs, isos)
+        v = (verify_outputs(ctx, vol, w, reqs, outs, isos) if mode == _abi.MODE_DUP_POLYGON_NORMAL
+             else verify_shared(vol, reqs, outs, isos))
         line["verified"] = v["verified"]
         line["verify"] = v
     return line
@@ -960,6 +985,41 @@ def verify_outputs(ctx, vol, w, reqs, outs, isos, planes=2, chunk_tris=1 << 20):
                      f"first and last {planes} cell planes of every output",
             "seconds": round(time.perf_counter() - t0, 1), "oracle_seconds": round(t_oracle, 1),
             "isolevels": per_iso}
+
+
+def verify_shared(vol, reqs, outs, isos, max_checked=2):
+    """Shared-vertex outputs against the oracle's whole arrays (coords,
+    connections, normals), bit for bit, for the middle isovalue(s): the
+    oracle's vertex map costs 12 B per node, so a 1024^3 volume takes one
+    isovalue at a time.  Runs after the timed region."""
+    from oracle import oracle
+    oracle.build()
+    t0 = time.perf_counter()
+    host = vol.download()
+    n = len(isos)
+    picks = sorted({n // 2, max(0, n // 2 - 1)})[:max_checked] if n > 1 else [0]
+    per, ok = [], True
+    for i in picks:
+        p, s = reqs[i].params, reqs[i].sizes
+        o = oracle.extract(host, p.isolevel, p.mode, s.min_value, s.max_value, tuple(p.min_coord), tuple(p.scale))
+        c, nn, k = outs[i]
+        e = {"isovalue": round(float(isos[i]), 6), "triangles": int(s.ntriangles), "vertices": int(s.nvertices)}
+        for name, got, ref in (("coords", c[:s.ncoords], o["coords"]), ("normals", nn[:s.nnormals], o["normals"]),
+                               ("connections", k[:s.nconnections], o["connections"])):
+            g = got.cpu().numpy()
+            g = g.view(np.uint32) if name == "connections" else g
+            r = ref.view(np.uint32) if name != "connections" else ref
+            same = g.size == ref.size and np.array_equal(g.view(np.uint32), r.view(np.uint32))
+            if not same:
+                ok = False
+                d = np.nonzero(g.view(np.uint32)[:min(g.size, r.size)] != r.view(np.uint32)[:min(g.size, r.size)])[0]
+                e[name + "_first_diff"] = int(d[0]) if d.size else [int(g.size), int(ref.size)]
+        per.append(e)
+        del o
+    return {"verified": ok, "oracle": "oracle/mc_oracle.c (mco_extract, whole arrays)",
+            "method": "bit-exact comparison of coords, connections and vertex normals",
+            "scope": f"isovalues {[round(float(isos[i]), 4) for i in picks]} of {n}, whole volume",
+            "seconds": round(time.perf_counter() - t0, 1), "isolevels": per}
 
 
 def gpu_numa_node(local):
@@ -1395,8 +1455,10 @@ def run_cpu(args, threads, planes, isos):
     nz, ny, nx = v.shape
     cells = (nx - 1) * (ny - 1) * (nz - 1)
 
+    mode = getattr(args, "mode", 0)
+
     def one(iso):
-        oracle.extract(v, iso, 0, vmin, vmax)
+        oracle.extract(v, iso, mode, vmin, vmax)
         return cells
 
     t0 = time.perf_counter()
