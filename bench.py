@@ -964,7 +964,7 @@ def verify_outputs(ctx, vol, w, reqs, outs, isos, planes=2, chunk_tris=1 << 20):
                 sl["count_mismatch"] = [int(t), T]
                 ok = False
             elif t:
-                c, n = outs[i]
+                c, n = outs[i][:2]
                 gc = ctx.checksum_words(c.data_ptr() + 4 * 9 * first, 9 * t, 9 * chunk_tris)
                 gn = ctx.checksum_words(n.data_ptr() + 4 * 3 * first, 3 * t, 3 * chunk_tris)
                 bad = [k for k in range(len(cs)) if cs[k] != gc[k] or ns[k] != gn[k]]

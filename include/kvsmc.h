@@ -503,6 +503,37 @@ kvsmc_status kvsmc_write_stl(kvsmc_context* ctx, const char* path, int32_t mode,
 kvsmc_status kvsmc_write_stl_host(kvsmc_context* ctx, const char* path, int32_t mode, const float* coords,
                                   uint64_t ncoords, const float* normals, uint64_t nnormals,
                                   const uint32_t* connections, uint64_t nconnections);
+/* The ASCII STL file of a device mesh, kvs::Stl's default file type
+ * (Stl.cpp:86): what Stl::write_ascii (Stl.cpp:447-480) prints for the
+ * triangles PolygonExporter<kvs::Stl> hands it -- "solid Generated by KVS",
+ * per triangle "facet normal %f %f %f", "outer loop", three "vertex %f %f %f",
+ * "endloop", "endfacet", then "endsolid", byte for byte.  The text is
+ * formatted on the GPU (exact "%f": the float's binary value rounded to six
+ * decimals, ties to even) in chunks of 2^20 triangles, each copied to pinned
+ * memory and written while the next is formatted.  Same meshes and modes as
+ * kvsmc_write_stl. */
+kvsmc_status kvsmc_write_stl_ascii(kvsmc_context* ctx, const char* path, int32_t mode, const float* d_coords,
+                                   const float* d_normals, const uint32_t* d_connections, uint64_t nvertices,
+                                   uint64_t ntriangles);
+/* The KVSML polygon file of a device mesh: what PolygonExporter<
+ * kvs::KVSMLPolygonObject> (PolygonExporter.cpp:22-68) and
+ * KVSMLPolygonObject::write (KVSMLPolygonObject.cpp:349-492) write for a
+ * marching-cubes result, byte for byte.  writing_type is the reference's
+ * WritingDataType: 0 Ascii (arrays inside the .kvsml), 1 ExternalAscii,
+ * 2 ExternalBinary (arrays in <base>_coord.dat, _normal.dat, _connect.dat
+ * beside `path`, binary arrays streamed from the device through pinned
+ * buffers).  mode sets normal_type (vertex for KVSMC_SHARED_VERTEX_NORMAL,
+ * else polygon); sizes are elements (floats, uint32); color (3 bytes) and
+ * opacity (1 byte), when not null, are the object's single colour and
+ * opacity, written as <DataValue>s. */
+kvsmc_status kvsmc_write_kvsml_polygon(kvsmc_context* ctx, const char* path, int32_t writing_type, int32_t mode,
+                                       const float* d_coords, uint64_t ncoords, const float* d_normals,
+                                       uint64_t nnormals, const uint32_t* d_connections, uint64_t nconnections,
+                                       const uint8_t* color, const uint8_t* opacity);
+/* Same for a mesh in HOST memory (uploaded first), as kvsmc_write_stl_host. */
+kvsmc_status kvsmc_write_stl_ascii_host(kvsmc_context* ctx, const char* path, int32_t mode, const float* coords,
+                                        uint64_t ncoords, const float* normals, uint64_t nnormals,
+                                        const uint32_t* connections, uint64_t nconnections);
 
 
 /* Binary PLY (little endian) of a triangle mesh without connections: what

@@ -51,7 +51,8 @@ EXPORTS = [
     "kvsmc_slice_count", "kvsmc_slice_extract_device", "kvsmc_slice_plane",
     "kvsmc_marching_cells_host", "kvsmc_marching_cells_device", "kvsmc_selftest_cells", "kvsmc_slice_cells_host",
     "kvsmc_cells_bounds", "kvsmc_marching_cells_sweep_device", "kvsmc_ply_record_bytes", "kvsmc_ply_header", "kvsmc_ply_records", "kvsmc_write_ply", "kvsmc_write_ply_host",
-    "kvsmc_checksum_words", "kvsmc_set_wait_limit",
+    "kvsmc_checksum_words", "kvsmc_set_wait_limit", "kvsmc_write_stl_ascii", "kvsmc_write_stl_ascii_host",
+    "kvsmc_write_kvsml_polygon",
 ]
 
 PATH_AUTO = 0      # streaming kernels where eligible
@@ -220,6 +221,9 @@ def load(path=LIB_PATH):
         "kvsmc_volume_load_avs": (C.c_int, [vp, C.c_char_p, C.POINTER(vp), C.POINTER(KvsmlInfo)]),
         "kvsmc_write_stl": (C.c_int, [vp, C.c_char_p, i32, vp, vp, vp, u64, u64]),
         "kvsmc_write_stl_host": (C.c_int, [vp, C.c_char_p, i32, vp, u64, vp, u64, vp, u64]),
+        "kvsmc_write_stl_ascii": (C.c_int, [vp, C.c_char_p, i32, vp, vp, vp, u64, u64]),
+        "kvsmc_write_stl_ascii_host": (C.c_int, [vp, C.c_char_p, i32, vp, u64, vp, u64, vp, u64]),
+        "kvsmc_write_kvsml_polygon": (C.c_int, [vp, C.c_char_p, i32, i32, vp, u64, vp, u64, vp, u64, vp, vp]),
         "kvsmc_size_class": (i32, [u32, u32, u32]),
         "kvsmc_tune_resolve": (C.c_int, [C.POINTER(TuneEntry), i32, C.c_int, u32, u32, u32,
                                          C.POINTER(TuneChoice)]),

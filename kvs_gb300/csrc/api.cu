@@ -475,6 +475,8 @@ void kvsmc_destroy(kvsmc_context* ctx)
         if (ctx->stl_dbuf[b]) cudaFree(ctx->stl_dbuf[b]);
         if (ctx->stl_hbuf[b]) cudaFreeHost(ctx->stl_hbuf[b]);
         if (ctx->stl_ev[b]) cudaEventDestroy(ctx->stl_ev[b]);
+        if (ctx->txt_dbuf[b]) cudaFree(ctx->txt_dbuf[b]);
+        if (ctx->txt_hbuf[b]) cudaFreeHost(ctx->txt_hbuf[b]);
     }
     if (ctx->out_arena) cudaFree(ctx->out_arena);
     if (ctx->h_small) cudaFreeHost(ctx->h_small);

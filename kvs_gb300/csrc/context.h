@@ -58,6 +58,10 @@ struct kvsmc_context {
     uint8_t* stl_hbuf[2] = {};
     size_t stl_buf_bytes = 0;
     cudaEvent_t stl_ev[2] = {};
+    // ASCII text of the STL writer: two device, two pinned buffers (grow-only)
+    char* txt_dbuf[2] = {};
+    char* txt_hbuf[2] = {};
+    size_t txt_bytes = 0;
     // streaming launch shapes: the tuning table, or one forced shape
     std::vector<kvsmc_tune_entry> tuning;
     bool tune_forced = false;

@@ -210,6 +210,14 @@ cudaError_t launch_ply_vertices(const float* coords, const uint8_t* colors, int 
 cudaError_t launch_stl_records(const float* coords, const float* normals, const uint32_t* conn, uint64_t nverts,
                                uint64_t ntri, int mode, uint8_t* out, int* bad_index, const Launch& L);
 
+// ---- ASCII STL text (stl_ascii.cu): per triangle its record length, then
+// the records at scanned offsets; triangles [t0, t0 + n) of the mesh
+cudaError_t launch_stl_ascii_len(const float* coords, const float* normals, const uint32_t* conn, uint64_t nverts,
+                                 uint64_t t0, uint64_t n, int mode, uint32_t* lens, int* bad_index, const Launch& L);
+cudaError_t launch_stl_ascii_write(const float* coords, const float* normals, const uint32_t* conn,
+                                   uint64_t nverts, uint64_t t0, uint64_t n, int mode, const uint64_t* offsets,
+                                   char* out, int* bad_index, const Launch& L);
+
 // ---- diagnostics (selftest.cu)
 cudaError_t launch_selftest(uint64_t n, uint64_t seed, unsigned long long* d_counters, const Launch& L);
 cudaError_t launch_selftest_cells(uint64_t n, uint64_t seed, unsigned long long* d_counters, const Launch& L);

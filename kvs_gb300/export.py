@@ -7,8 +7,13 @@ messages, the same bytes.  The records are formed by libkvsmc's CUDA kernel
 (kvsmc_stl_records); a mesh already on the device (kvsmc_extract_device
 output) is written without any host PolygonObject (write_stl_device).
 
-The reference's kvs::Stl defaults to ASCII; ASCII output is not provided here
-(write() reports it and returns False): set the Binary file type.
+kvs::Stl's default ASCII file type (Stl.cpp:86, write_ascii :447-480) is
+formatted on the GPU too (kvsmc_write_stl_ascii: exact "%f" text, byte for
+byte the reference's file).
+
+PolygonExporterKVSML mirrors kvs::PolygonExporter<kvs::KVSMLPolygonObject>
+(PolygonExporter.cpp:22-68) + KVSMLPolygonObject::write (KVSMLPolygonObject.cpp:
+349-492) with its three writing data types (kvsmc_write_kvsml_polygon).
 
 PolygonExporterPly mirrors kvs::PolygonExporter<kvs::Ply> (PolygonExporter.cpp:
 178-361) with kvs::Ply's Binary type (Ply.cpp:389-488) for meshes without
@@ -90,22 +95,112 @@ class PolygonExporterStl:
         return self
 
     def write(self, filename):
-        """Stl::write (Stl.cpp:170-199) with the Binary file type."""
+        """Stl::write (Stl.cpp:170-199): the ASCII (default) or Binary file type."""
         if self._mesh is None:
             message_error("No polygon object to write.")
-            return False
-        if self._file_type != BINARY:
-            message_error("ASCII STL is not provided; setFileType('binary').")
             return False
         m = self._mesh
         ctx = self._ctx or default_context()
         c = np.ascontiguousarray(m.coords(), np.float32)
         n = np.ascontiguousarray(m.normals(), np.float32)
         k = np.ascontiguousarray(m.connections(), np.uint32)
-        st = ctx.lib.kvsmc_write_stl_host(ctx.handle, str(filename).encode(), _mode(m), c.ctypes.data, c.size,
-                                          n.ctypes.data, n.size, k.ctypes.data if k.size else None, k.size)
+        fn = ctx.lib.kvsmc_write_stl_host if self._file_type == BINARY else ctx.lib.kvsmc_write_stl_ascii_host
+        st = fn(ctx.handle, str(filename).encode(), _mode(m), c.ctypes.data, c.size,
+                n.ctypes.data, n.size, k.ctypes.data if k.size else None, k.size)
         if st:
             message_error(f"libkvsmc: {_abi.status_string(st)}: {ctx.lib.kvsmc_last_error(ctx.handle).decode()}")
+            self._success = False
+            return False
+        return True
+
+
+def write_stl_ascii_device(ctx, path, mode, d_coords, d_normals, d_connections, nvertices, ntriangles):
+    """kvsmc_write_stl_ascii: the ASCII STL file of a device mesh, text formatted on the GPU."""
+    ctx.check(ctx.lib.kvsmc_write_stl_ascii(ctx.handle, str(path).encode(), int(mode), d_coords, d_normals,
+                                            d_connections or None, int(nvertices), int(ntriangles)),
+              "write_stl_ascii")
+
+
+# ------------------------------------------------------------------ KVSML
+
+KVSML_ASCII, KVSML_EXTERNAL_ASCII, KVSML_EXTERNAL_BINARY = 0, 1, 2
+
+
+def write_kvsml_device(ctx, path, writing_type, mode, d_coords, ncoords, d_normals, nnormals, d_connections,
+                       nconnections, color=None, opacity=None):
+    """kvsmc_write_kvsml_polygon on device arrays (pointers as integers, sizes in elements)."""
+    col = np.ascontiguousarray(color, np.uint8) if color is not None and len(color) == 3 else None
+    opa = np.ascontiguousarray(opacity, np.uint8).reshape(-1)[:1] if opacity is not None and len(opacity) else None
+    ctx.check(ctx.lib.kvsmc_write_kvsml_polygon(ctx.handle, str(path).encode(), int(writing_type), int(mode),
+                                                d_coords or None, int(ncoords), d_normals or None, int(nnormals),
+                                                d_connections or None, int(nconnections),
+                                                col.ctypes.data if col is not None else None,
+                                                opa.ctypes.data if opa is not None else None), "write_kvsml")
+
+
+class PolygonExporterKVSML:
+    """kvs::PolygonExporter<kvs::KVSMLPolygonObject>: exec(polygon) keeps the
+    mesh, write() writes the .kvsml file (and its external data files)."""
+
+    def __init__(self, polygon=None, context=None):
+        self._success = True
+        self._writing = KVSML_ASCII      # KVSMLPolygonObject() (KVSMLPolygonObject.cpp:33-39)
+        self._mesh = None
+        self._ctx = context
+        if polygon is not None:
+            self.exec(polygon)
+
+    def isSuccess(self):
+        return self._success
+
+    def setWritingDataTypeToAscii(self):
+        self._writing = KVSML_ASCII
+
+    def setWritingDataTypeToExternalAscii(self):
+        self._writing = KVSML_EXTERNAL_ASCII
+
+    def setWritingDataTypeToExternalBinary(self):
+        self._writing = KVSML_EXTERNAL_BINARY
+
+    def exec(self, obj):
+        """PolygonExporter<KVSMLPolygonObject>::exec (PolygonExporter.cpp:22-68)."""
+        self._success = True
+        if obj is None:
+            self._success = False
+            message_error("Input object is NULL.")
+            return None
+        if not isinstance(obj, PolygonObject):
+            self._success = False
+            message_error("Input object is not polygon object.")
+            return None
+        self._mesh = obj
+        return self
+
+    def write(self, filename):
+        """KVSMLPolygonObject::write (KVSMLPolygonObject.cpp:349-492)."""
+        if self._mesh is None:
+            message_error("No polygon object to write.")
+            return False
+        m = self._mesh
+        if m.polygonType() != PolygonObject.Triangle or m.colorType() != PolygonObject.PolygonColor:
+            message_error("KVSML: triangle meshes with one polygon colour are provided")
+            self._success = False
+            return False
+        import torch
+        ctx = self._ctx or default_context()
+        c = torch.from_numpy(np.ascontiguousarray(m.coords(), np.float32)).cuda()
+        n = torch.from_numpy(np.ascontiguousarray(m.normals(), np.float32)).cuda()
+        k = torch.from_numpy(np.ascontiguousarray(m.connections(), np.uint32).view(np.int32)).cuda()
+        mode = (_abi.MODE_SHARED_VERTEX_NORMAL if m.normalType() == PolygonObject.VertexNormal
+                else _abi.MODE_DUP_POLYGON_NORMAL)
+        col = m.colors()
+        opa = m.opacities() if hasattr(m, "opacities") else np.array([m.opacity()], np.uint8)
+        try:
+            write_kvsml_device(ctx, filename, self._writing, mode, c.data_ptr() if c.numel() else None, c.numel(),
+                               n.data_ptr() if n.numel() else None, n.numel(), k.data_ptr() if k.numel() else None,
+                               k.numel(), col if len(col) == 3 else None, opa)
+        except _abi.KvsmcError as e:
+            message_error(str(e))
             self._success = False
             return False
         return True

@@ -91,6 +91,9 @@ def lib():
             C.c_int, C.c_int, C.c_void_p, C.c_uint, C.c_uint, C.c_uint, C.c_void_p,
             C.c_int, C.c_double, C.c_double, C.c_int, C.c_int, C.c_float, C.c_float,
             C.c_int, C.c_void_p, C.c_void_p, C.POINTER(_Result)]
+        _lib.kvsref_marching_cubes_export.restype = C.c_int
+        _lib.kvsref_marching_cubes_export.argtypes = [
+            C.c_int, C.c_void_p, C.c_uint, C.c_uint, C.c_uint, C.c_double, C.c_int, C.c_int, C.c_int, C.c_char_p]
         _lib.kvsref_marching_cubes_stl.restype = C.c_int
         _lib.kvsref_marching_cubes_stl.argtypes = [
             C.c_int, C.c_void_p, C.c_uint, C.c_uint, C.c_uint, C.c_double, C.c_int, C.c_int, C.c_char_p]
@@ -312,6 +315,23 @@ def marching_cubes_stl(values, isolevel, normal_type="polygon", duplication=True
     finally:
         if own:
             os.remove(path)
+
+
+EXPORT_FORMATS = {"stl_binary": 0, "stl_ascii": 1, "kvsml_ascii": 2, "kvsml_external_ascii": 3,
+                  "kvsml_external_binary": 4}
+
+
+def marching_cubes_export(values, isolevel, normal_type, duplication, fmt, path):
+    """The reference MarchingCubes result written by the reference's STL or
+    KVSML polygon writer (EXPORT_FORMATS) to `path` (KVSML external data files
+    beside it)."""
+    v = np.ascontiguousarray(values)
+    nz, ny, nx = v.shape
+    st = lib().kvsref_marching_cubes_export(dtype_code(v.dtype), v.ctypes.data, nx, ny, nz, float(isolevel),
+                                            0 if normal_type == "polygon" else 1, 1 if duplication else 0,
+                                            EXPORT_FORMATS[fmt], path.encode())
+    if st != 0:
+        raise RuntimeError(f"kvsref_marching_cubes_export failed ({st})")
 
 
 def hydrogen(res):

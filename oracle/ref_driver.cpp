@@ -19,6 +19,7 @@
 #include <kvs/Isosurface>
 #include <kvs/PolygonExporter>
 #include <kvs/Stl>
+#include <kvs/KVSMLPolygonObject>
 #include <kvs/Ply>
 #include <kvs/AVSField>
 #include <kvs/SlicePlane>
@@ -419,6 +420,58 @@ int kvsref_marching_cubes_stl(
     {
         exporter.setFileType( kvs::Stl::Binary );
         rc = exporter.write( path ) ? 0 : -3;
+    }
+    delete mc;
+    delete vol;
+    return rc;
+}
+
+/*
+ * kvs::MarchingCubes on a uniform volume with the default TransferFunction(256),
+ * then one of the reference's polygon writers on the result:
+ *   format 0: PolygonExporter<kvs::Stl> + Stl::write, Binary (Stl.cpp:490-540)
+ *   format 1: PolygonExporter<kvs::Stl> + Stl::write, Ascii, the Stl default
+ *             (Stl.cpp:86, 447-480)
+ *   format 2/3/4: PolygonExporter<kvs::KVSMLPolygonObject> (PolygonExporter.cpp:22-68)
+ *             + KVSMLPolygonObject::write (KVSMLPolygonObject.cpp:349-492) with
+ *             the Ascii / ExternalAscii / ExternalBinary writing data type
+ * Returns 0 when the file (and its external data files) were written.
+ */
+int kvsref_marching_cubes_export(
+    int dtype, const void* values, unsigned nx, unsigned ny, unsigned nz,
+    double isolevel, int normal_type, int duplication, int format, const char* path )
+{
+    const size_t n = size_t( nx ) * ny * nz;
+    kvs::AnyValueArray vals = Values( dtype, values, n );
+    if ( vals.size() != n ) return -1;
+    kvs::TransferFunction tfunc( 256 );
+    const auto ntype = normal_type == 0 ? kvs::PolygonObject::PolygonNormal : kvs::PolygonObject::VertexNormal;
+    auto* vol = new kvs::StructuredVolumeObject();
+    vol->setVeclen( 1 );
+    vol->setResolution( kvs::Vec3ui( nx, ny, nz ) );
+    vol->setValues( vals );
+    vol->setGridTypeToUniform();
+    auto* mc = new kvs::MarchingCubes( vol, isolevel, ntype, duplication != 0, tfunc );
+    int rc = -2;
+    if ( format <= 1 )
+    {
+        kvs::PolygonExporter<kvs::Stl> exporter( mc );
+        if ( exporter.kvs::ExporterBase::isSuccess() )
+        {
+            exporter.setFileType( format == 0 ? kvs::Stl::Binary : kvs::Stl::Ascii );
+            rc = exporter.write( path ) ? 0 : -3;
+        }
+    }
+    else
+    {
+        kvs::PolygonExporter<kvs::KVSMLPolygonObject> exporter( mc );
+        if ( exporter.kvs::ExporterBase::isSuccess() )
+        {
+            if ( format == 2 ) exporter.setWritingDataTypeToAscii();
+            else if ( format == 3 ) exporter.setWritingDataTypeToExternalAscii();
+            else exporter.setWritingDataTypeToExternalBinary();
+            rc = exporter.write( path ) ? 0 : -3;
+        }
     }
     delete mc;
     delete vol;

@@ -12,11 +12,14 @@ files written by the reference PolygonExporter<kvs::Stl> in tests/golden/stl.npz
 kvs::Isosurface) in tests/golden/cells.npz (tests/golden/cells.json), and
 kvs::SlicePlane on unstructured volumes in tests/golden/slice_cells.npz
 (tests/golden/slice_cells.json), and binary PLY files written by the reference
-PolygonExporter<kvs::Ply> in tests/golden/ply.npz (tests/golden/ply.json).  The reference
+PolygonExporter<kvs::Ply> in tests/golden/ply.npz (tests/golden/ply.json), and the
+reference's ASCII STL and KVSML polygon files (each writing data type) of
+MarchingCubes results in tests/golden/exports.npz (tests/golden/exports.json).  The reference
 ships no tests or golden vectors of its own, so these fixtures pin the oracle
 restatement and the CUDA path on hosts where the reference is absent.
 
     python tests/golden/make_golden.py [marching_cubes] [isosurface] [stl] [slice] [cells] [slice_cells] [ply]
+                                       [exports]
         (default: all)
 """
 import json
@@ -153,6 +156,53 @@ def write_stl():
     with open(os.path.join(HERE, "stl.json"), "w") as f:
         json.dump(manifest, f, indent=0)
     print(f"{len(manifest)} stl cases")
+
+
+def export_cases():
+    """(name, volume, isolevel, normal_type, duplication) for the ASCII STL and
+    KVSML fixtures: the reference's MarchingCubes result written by its own
+    writers (kvsref_marching_cubes_export)."""
+    h = ref.hydrogen(24)
+    x, y, z = np.meshgrid(np.arange(12), np.arange(11), np.arange(10), indexing="xy")
+    blob = np.exp(-((x - 5.3) ** 2 + (y - 5.1) ** 2 + (z - 4.7) ** 2) / (2 * 3.0 ** 2)).transpose(2, 0, 1)
+    blob = np.ascontiguousarray(blob).astype(np.float32)
+    # coordinates far from the origin: six-decimal rounding with long integer parts, negative normals
+    big = np.ascontiguousarray(blob * np.float32(3.0) - np.float32(1.0))
+    return [
+        ("hydrogen24_dup", h, 100.5, "polygon", True),
+        ("hydrogen24_vertex", h, 100.5, "vertex", False),
+        ("hydrogen24_shared", h, 100.5, "polygon", False),
+        ("blob12_dup", blob, 0.5, "polygon", True),
+        ("blob12_vertex", blob, 0.37, "vertex", True),
+        ("blob12_scaled", big, 0.61, "polygon", True),
+        ("constant", np.full((4, 5, 6), 2.0, np.float32), 2.0, "polygon", True),
+    ]
+
+
+def write_exports():
+    """Files of the reference's ASCII STL writer and of its KVSML polygon
+    writer with each writing data type, as bytes, in tests/golden/exports.npz."""
+    import tempfile
+    arrays, manifest = {}, []
+    with tempfile.TemporaryDirectory() as tmp:
+        for name, v, iso, nt, dup in export_cases():
+            arrays[f"{name}__input"] = v
+            entry = dict(case=name, isolevel=iso, normal_type=nt, duplication=dup, files={})
+            for fmt in ("stl_ascii", "kvsml_ascii", "kvsml_external_ascii", "kvsml_external_binary"):
+                sub = os.path.join(tmp, fmt)
+                os.makedirs(sub, exist_ok=True)
+                main = os.path.join(sub, name + (".stl" if fmt.startswith("stl") else ".kvsml"))
+                ref.marching_cubes_export(v, iso, nt, dup, fmt, main)
+                files = sorted(f for f in os.listdir(sub) if f.startswith(name + ".") or f.startswith(name + "_"))
+                entry["files"][fmt] = files
+                for fn in files:
+                    with open(os.path.join(sub, fn), "rb") as f:
+                        arrays[f"{name}__{fmt}__{fn}"] = np.frombuffer(f.read(), np.uint8)
+            manifest.append(entry)
+    np.savez_compressed(os.path.join(HERE, "exports.npz"), **arrays)
+    with open(os.path.join(HERE, "exports.json"), "w") as f:
+        json.dump(manifest, f, indent=0)
+    print(f"{len(manifest)} export cases")
 
 
 def slice_cases():
@@ -406,7 +456,9 @@ def write_ply_fixtures():
 def main():
     if not ref.available():
         ref.build()
-    parts = sys.argv[1:] or ["marching_cubes", "isosurface", "stl", "slice", "cells", "slice_cells", "ply"]
+    parts = sys.argv[1:] or ["marching_cubes", "isosurface", "stl", "slice", "cells", "slice_cells", "ply", "exports"]
+    if "exports" in parts:
+        write_exports()
     if "ply" in parts:
         write_ply_fixtures()
     if "cells" in parts:
