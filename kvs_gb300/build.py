@@ -20,7 +20,7 @@ LIB_DIR = os.path.join(PKG, "lib")
 LIB_PATH = os.path.join(LIB_DIR, "libkvsmc.so")
 OBJ_DIR = os.path.join(PKG, "_build")
 
-SOURCES = ["api.cu", "autotune.cu", "batch.cu", "cells.cu", "checksum.cu", "export.cu", "ingest.cu", "kvsml_export.cu", "slice.cu", "mc_gather.cu", "mc_stream.cu", "noalloc.cu", "plan.cu", "ply.cu", "profile.cu", "selftest.cu", "server.cu", "stl_ascii.cu"]
+SOURCES = ["api.cu", "autotune.cu", "batch.cu", "cells.cu", "checksum.cu", "export.cu", "ingest.cu", "kvsml_export.cu", "slice.cu", "mc_gather.cu", "mc_snode.cu", "mc_stream.cu", "noalloc.cu", "plan.cu", "ply.cu", "profile.cu", "selftest.cu", "server.cu", "stl_ascii.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ["-O3", "-std=c++17", "-lineinfo", "--fmad=false", "-Xcompiler", "-fPIC",
               "-Xcompiler", "-ffp-contract=off", "-I" + os.path.join(ROOT, "include"), "-I" + CSRC]

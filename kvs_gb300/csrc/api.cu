@@ -220,6 +220,15 @@ struct Plan {
     Job job;
     bool shared = false;
     uint64_t ntri = 0, nvert = 0;
+    // shared-vertex node passes on the streaming kernels (8/16-bit and float32
+    // volumes): node units (plane, row, 256-node segment), their task shape,
+    // the FP32 vertex path's constants, the status word and task counters
+    bool snode = false;
+    uint32_t wprn = 0, zchunk = 0;
+    uint64_t ntasks = 0;
+    kvsmc::FastIso f{};
+    int* d_status = nullptr;
+    unsigned long long* d_next = nullptr;
 };
 
 uint32_t rows_for(uint32_t width, uint32_t limit)
@@ -260,9 +269,21 @@ kvsmc_status gather_count(kvsmc_context* ctx, Plan& pl)
 {
     pl.ntri = pl.nvert = 0;
     Job& j = pl.job;
+    const int dt = j.vol.dtype;
+    pl.snode = pl.shared && ctx->path == 0 &&
+               (dt == KVSMC_I8 || dt == KVSMC_I16 || dt == KVSMC_U8 || dt == KVSMC_U16 || dt == KVSMC_F32);
+    if (pl.snode) {
+        // node units replace the node tiles: (plane, row, 256-node segment)
+        pl.wprn = (j.vol.nx + 255) / 256;
+        const uint64_t steps = (uint64_t)j.vol.nz * j.vol.ny * pl.wprn;
+        pl.zchunk = kvsmc_host::stream_zchunk(steps, ctx->num_sms);
+        pl.ntasks = (uint64_t)((j.vol.nz + pl.zchunk - 1) / pl.zchunk) * j.vol.ny * pl.wprn;
+        pl.f = kvsmc_host::make_fast(j.ip.iso, j.ip.vmin, j.ip.vmax, dt);
+        j.node_tiles = steps;   // node units, for the counts and their scan
+    }
     const size_t ct = j.cell_tiles, nt = j.node_tiles;
     const uint64_t rank_words = pl.shared ? (uint64_t)j.vol.nz * j.vol.ny * j.words_per_row : 0;
-    const size_t need = 8 * 256 + align_up(ct * 4, 256) + align_up(ct * 8, 256) + align_up(nt * 4, 256) +
+    const size_t need = 10 * 256 + align_up(ct * 4, 256) + align_up(ct * 8, 256) + align_up(nt * 4, 256) +
                         align_up(nt * 8, 256) + align_up(rank_words * 16, 256) +
                         align_up(scan_scratch_bytes(ct), 256) + align_up(scan_scratch_bytes(nt), 256);
     kvsmc_status st = ensure_scratch(ctx, need);
@@ -276,18 +297,28 @@ kvsmc_status gather_count(kvsmc_context* ctx, Plan& pl)
     j.rank = cv.take<uint4>(rank_words * 16);
     void* scan_a = cv.take<char>(scan_scratch_bytes(ct));
     void* scan_b = cv.take<char>(scan_scratch_bytes(nt));
+    pl.d_status = cv.take<int>(256);
+    pl.d_next = cv.take<unsigned long long>(256);
     const kvsmc::Launch L = launch_of(ctx);
-    KVSMC_CUDA(ctx, cudaMemsetAsync(d_totals, 0, 2 * sizeof(uint64_t), ctx->stream));
+    KVSMC_CUDA(ctx, cudaMemsetAsync(d_totals, 0, 3 * sizeof(uint64_t), ctx->stream));
     if (ct) {
         KVSMC_CUDA(ctx, launch_cell_count(j, L));
         KVSMC_CUDA(ctx, launch_scan(j.tile_counts, j.tile_offsets, ct, scan_a, d_totals, L));
     }
-    if (nt) {
+    if (nt && pl.snode) {
+        KVSMC_CUDA(ctx, cudaMemsetAsync(pl.d_status, 0, sizeof(int), ctx->stream));
+        KVSMC_CUDA(ctx, cudaMemsetAsync(pl.d_next, 0, 2 * sizeof(unsigned long long), ctx->stream));
+        KVSMC_CUDA(ctx, kvsmc::launch_snode(false, j, pl.f, pl.wprn, pl.zchunk, pl.ntasks, j.vtile_counts, nullptr,
+                                            pl.d_status, pl.d_next, L));
+        KVSMC_CUDA(ctx, launch_scan(j.vtile_counts, j.vtile_offsets, nt, scan_b, d_totals + 1, L));
+        KVSMC_CUDA(ctx, cudaMemcpyAsync(d_totals + 2, pl.d_status, sizeof(int), cudaMemcpyDeviceToDevice, ctx->stream));
+    } else if (nt) {
         KVSMC_CUDA(ctx, launch_node_count(j, L));
         KVSMC_CUDA(ctx, launch_scan(j.vtile_counts, j.vtile_offsets, nt, scan_b, d_totals + 1, L));
     }
-    KVSMC_CUDA(ctx, cudaMemcpyAsync(ctx->h_small, d_totals, 2 * sizeof(uint64_t), cudaMemcpyDeviceToHost, ctx->stream));
+    KVSMC_CUDA(ctx, cudaMemcpyAsync(ctx->h_small, d_totals, 3 * sizeof(uint64_t), cudaMemcpyDeviceToHost, ctx->stream));
     KVSMC_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    if (ctx->h_small[2]) return fail(ctx, KVSMC_ERR_TIMEOUT, "shared-vertex count: a shared-memory load did not complete");
     pl.ntri = ctx->h_small[0];
     pl.nvert = pl.shared ? ctx->h_small[1] : 3 * pl.ntri;
     if (pl.shared && pl.nvert > 0xffffffffull)
@@ -328,9 +359,43 @@ kvsmc_status gather_emit(kvsmc_context* ctx, Plan& pl, float* coords, float* nor
         if (pl.ntri) KVSMC_CUDA(ctx, launch_emit_dup(j, L));
         return KVSMC_OK;
     }
-    if (pl.nvert) KVSMC_CUDA(ctx, launch_node_emit(j, L));
+    void* vn_scan = nullptr;
+    uint64_t* vn_total = nullptr;
+    const bool vertex_normals = pl.nvert && pl.ntri && j.mode == KVSMC_SHARED_VERTEX_NORMAL;
+    if (vertex_normals) {
+        // per-triangle normals and the vertices' triangle lists live in the
+        // context's second arena (the first holds this request's tiles and rank words)
+        if (pl.ntri > 0xffffffffull)
+            return fail(ctx, KVSMC_ERR_TOO_LARGE, "%llu triangles exceed 32-bit triangle ids of the vertex normals",
+                        (unsigned long long)pl.ntri);
+        const size_t need = kvsmc::vertex_normals_scratch_bytes(pl.ntri, pl.nvert);
+        if (need > ctx->arena2_bytes) {
+            KVSMC_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+            if (ctx->arena2) cudaFree(ctx->arena2);
+            ctx->arena2 = nullptr;
+            ctx->arena2_bytes = 0;
+            const size_t want = align_up(need + need / 4, 1 << 20);
+            KVSMC_CUDA(ctx, cudaMalloc(&ctx->arena2, want));
+            ctx->arena2_bytes = want;
+        }
+        kvsmc::vertex_normals_carve(j, pl.ntri, pl.nvert, ctx->arena2, &vn_scan, &vn_total);
+    } else {
+        j.tri_normals = nullptr;
+    }
+    if (pl.nvert && pl.snode) {
+        KVSMC_CUDA(ctx, kvsmc::launch_snode(true, j, pl.f, pl.wprn, pl.zchunk, pl.ntasks, nullptr, j.vtile_offsets,
+                                            pl.d_status, pl.d_next + 1, L));
+    } else if (pl.nvert) {
+        KVSMC_CUDA(ctx, launch_node_emit(j, L));
+    }
     if (pl.ntri) KVSMC_CUDA(ctx, launch_connect(j, L));
-    if (pl.nvert && j.mode == KVSMC_SHARED_VERTEX_NORMAL) KVSMC_CUDA(ctx, launch_vertex_normals(j, L));
+    if (vertex_normals) KVSMC_CUDA(ctx, launch_vertex_normals(j, pl.ntri, pl.nvert, vn_scan, vn_total, L));
+    if (pl.nvert && pl.snode) {
+        int* h = reinterpret_cast<int*>(ctx->h_small);
+        KVSMC_CUDA(ctx, cudaMemcpyAsync(h, pl.d_status, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
+        KVSMC_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+        if (*h) return fail(ctx, KVSMC_ERR_TIMEOUT, "shared-vertex emit: a shared-memory load did not complete");
+    }
     return KVSMC_OK;
 }
 
@@ -479,6 +544,7 @@ void kvsmc_destroy(kvsmc_context* ctx)
         if (ctx->txt_hbuf[b]) cudaFreeHost(ctx->txt_hbuf[b]);
     }
     if (ctx->out_arena) cudaFree(ctx->out_arena);
+    if (ctx->arena2) cudaFree(ctx->arena2);
     if (ctx->h_small) cudaFreeHost(ctx->h_small);
     if (ctx->h_stage) cudaFreeHost(ctx->h_stage);
     profiler_destroy(ctx->prof);

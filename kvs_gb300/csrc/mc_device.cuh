@@ -70,6 +70,14 @@ struct Job {
     float* coords;
     float* normals;
     uint32_t* connections;
+    // vertex normals (mode 2): per-triangle normals, then each vertex's
+    // triangles (counts, scanned offsets, lists) for the ordered sums
+    float* tri_normals;
+    uint32_t* vcount;
+    uint32_t* vfill;
+    uint64_t* voff;
+    uint32_t* vlist;
+    const uint64_t* vtotal;   // device: number of (vertex, triangle) incidences
 };
 
 // ------------------------------------------------------------------- values

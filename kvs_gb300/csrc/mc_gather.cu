@@ -347,7 +347,9 @@ __global__ void __launch_bounds__(kThreads) k_connect(Job j)
     load_tables(tb);
     const T* vol = static_cast<const T*>(j.vol.data);
     const uint32_t cx = j.vol.nx - 1;
-    const bool polygon_normals = j.mode == 1;
+    // polygon normals into the output (mode 1), or into the per-triangle
+    // scratch the vertex normals are summed from (mode 2)
+    float* const tri_out = j.mode == 1 ? j.normals : j.tri_normals;
     for (uint64_t tile = blockIdx.x; tile < j.cell_tiles; tile += gridDim.x) {
         uint32_t z, y0, rows;
         cell_tile(j, tile, z, y0, rows);
@@ -368,9 +370,9 @@ __global__ void __launch_bounds__(kThreads) k_connect(Job j)
                     const uint32_t i2 = cell_edge_id(j, tb.edge, x, y, z, (int)((pk >> 8) & 15u));
                     uint32_t* o = j.connections + 3 * t;
                     o[0] = i0; o[1] = i1; o[2] = i2;
-                    if (polygon_normals) {
+                    if (tri_out) {
                         const float3 nn = tri_normal(load_coord(j, i0), load_coord(j, i1), load_coord(j, i2));
-                        float* q = j.normals + 3 * t;
+                        float* q = tri_out + 3 * t;
                         q[0] = nn.x; q[1] = nn.y; q[2] = nn.z;
                     }
                 }
@@ -380,65 +382,82 @@ __global__ void __launch_bounds__(kThreads) k_connect(Job j)
     }
 }
 
-// For the edge of node (x,y,z) along each axis: the four cells sharing it,
-// in increasing linear cell order, with the edge's local number in each.
-__constant__ int8_t c_incident[3][4][4] = {
-    {{0, -1, -1, 6}, {0, 0, -1, 4}, {0, -1, 0, 2}, {0, 0, 0, 0}},     // x-edge
-    {{-1, 0, -1, 5}, {0, 0, -1, 7}, {-1, 0, 0, 1}, {0, 0, 0, 3}},     // y-edge
-    {{-1, -1, 0, 10}, {0, -1, 0, 11}, {-1, 0, 0, 9}, {0, 0, 0, 8}},   // z-edge
-};
-
-// calculate_normals_on_vertex (MarchingCubes.cpp:569-605) as a gather: each
-// vertex sums, from 0.0f and in triangle order, the normals of the triangles
-// that use it (cells in linear order, table order inside a cell).
-template <typename T>
-__global__ void __launch_bounds__(kThreads) k_vertex_normals(Job j)
+// calculate_normals_on_vertex (MarchingCubes.cpp:569-605): every vertex's
+// normal is the sum, from 0.0f and in triangle order, of the normals of the
+// triangles that use it.  Float addition is not associative, so the order is
+// kept: each triangle's normal is formed once (k_connect), every vertex gets
+// the list of its triangles (incidence counts, an exclusive scan, then the
+// triangle ids placed by atomics in any order), and one thread per vertex
+// sorts its list (a vertex lies on one cell edge: at most four cells, a few
+// triangles each) and adds the normals in increasing triangle order.
+__global__ void __launch_bounds__(256) k_vn_count(const uint32_t* __restrict__ conn, uint64_t ntri,
+                                                 uint32_t* __restrict__ vcount)
 {
-    __shared__ SmemTables tb;
-    load_tables(tb);
-    const T* vol = static_cast<const T*>(j.vol.data);
-    const uint32_t cx = j.vol.nx - 1, cy = j.vol.ny - 1, cz = j.vol.nz - 1;
-    for (uint64_t tile = blockIdx.x; tile < j.node_tiles; tile += gridDim.x) {
-        uint32_t z, y0, rows;
-        node_tile(j, tile, z, y0, rows);
-        for (uint32_t r = 0; r < rows; ++r) {
-            const uint32_t y = y0 + r;
-            const uint64_t row = (uint64_t)z * j.vol.ny + y;
-            for (uint32_t x = threadIdx.x; x < j.vol.nx; x += blockDim.x) {
-                const uint4 R = j.rank[row * j.words_per_row + (x >> 5)];
-                const uint32_t bit = x & 31u, lt = (1u << bit) - 1u;
-                const unsigned f = ((R.x >> bit) & 1u) | (((R.y >> bit) & 1u) << 1) | (((R.z >> bit) & 1u) << 2);
-                if (!f) continue;
-                uint32_t id = R.w + __popc(R.x & lt) + __popc(R.y & lt) + __popc(R.z & lt);
-                for (int axis = 0; axis < 3; ++axis) {
-                    if (!(f & (1u << axis))) continue;
-                    float ax = 0.0f, ay = 0.0f, az = 0.0f;
-                    for (int k = 0; k < 4; ++k) {
-                        const int dx = c_incident[axis][k][0], dy = c_incident[axis][k][1];
-                        const int dz = c_incident[axis][k][2], le = c_incident[axis][k][3];
-                        if ((dx < 0 && x == 0) || (dy < 0 && y == 0) || (dz < 0 && z == 0)) continue;
-                        const uint32_t qx = x + dx, qy = y + dy, qz = z + dz;
-                        if (qx >= cx || qy >= cy || qz >= cz) continue;
-                        const unsigned c = cell_case<T>(j, vol, qx, qy, qz);
-                        uint64_t pk = tb.tri[c];
-                        const uint32_t n = tb.ntri[c];
-                        for (uint32_t t = 0; t < n; ++t, pk >>= 12) {
-                            const int e0 = (int)(pk & 15u), e1 = (int)((pk >> 4) & 15u), e2 = (int)((pk >> 8) & 15u);
-                            if (e0 != le && e1 != le && e2 != le) continue;
-                            const float3 nn = tri_normal(load_coord(j, cell_edge_id(j, tb.edge, qx, qy, qz, e0)),
-                                                         load_coord(j, cell_edge_id(j, tb.edge, qx, qy, qz, e1)),
-                                                         load_coord(j, cell_edge_id(j, tb.edge, qx, qy, qz, e2)));
-                            ax = __fadd_rn(ax, nn.x);
-                            ay = __fadd_rn(ay, nn.y);
-                            az = __fadd_rn(az, nn.z);
-                        }
-                    }
-                    float* q = j.normals + 3 * (uint64_t)id;
-                    q[0] = ax; q[1] = ay; q[2] = az;
-                    ++id;
+    for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < 3 * ntri;
+         i += (uint64_t)gridDim.x * blockDim.x)
+        atomicAdd(vcount + conn[i], 1u);
+}
+
+__global__ void __launch_bounds__(256) k_vn_fill(const uint32_t* __restrict__ conn, uint64_t ntri,
+                                                const uint64_t* __restrict__ voff, uint32_t* __restrict__ vfill,
+                                                uint32_t* __restrict__ vlist)
+{
+    for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < 3 * ntri;
+         i += (uint64_t)gridDim.x * blockDim.x) {
+        const uint32_t v = conn[i];
+        const uint32_t slot = atomicAdd(vfill + v, 1u);
+        vlist[voff[v] + slot] = (uint32_t)(i / 3);
+    }
+}
+
+constexpr int kVnLocal = 32;   // incidences sorted in registers; longer lists take the selection loop
+
+__global__ void __launch_bounds__(256) k_vn_sum(const uint64_t* __restrict__ voff, const uint64_t* __restrict__ vtotal,
+                                               const uint32_t* __restrict__ vlist, uint64_t nvert,
+                                               const float* __restrict__ tri_normals, float* __restrict__ normals)
+{
+    const uint64_t total = *vtotal;
+    for (uint64_t v = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; v < nvert;
+         v += (uint64_t)gridDim.x * blockDim.x) {
+        const uint64_t a = voff[v], b = v + 1 < nvert ? voff[v + 1] : total;
+        const uint32_t n = (uint32_t)(b - a);
+        float sx = 0.0f, sy = 0.0f, sz = 0.0f;
+        auto add = [&](uint32_t t) {
+            sx = __fadd_rn(sx, tri_normals[3 * (uint64_t)t + 0]);
+            sy = __fadd_rn(sy, tri_normals[3 * (uint64_t)t + 1]);
+            sz = __fadd_rn(sz, tri_normals[3 * (uint64_t)t + 2]);
+        };
+        if (n <= (uint32_t)kVnLocal) {
+            uint32_t ids[kVnLocal];
+            for (uint32_t i = 0; i < n; ++i) {
+                // insertion sort while loading
+                const uint32_t t = vlist[a + i];
+                uint32_t k = i;
+                while (k > 0 && ids[k - 1] > t) {
+                    ids[k] = ids[k - 1];
+                    --k;
                 }
+                ids[k] = t;
+            }
+            for (uint32_t i = 0; i < n; ++i) add(ids[i]);
+        } else {
+            // selection: the next larger id each time (ids are distinct)
+            uint64_t last = 0;
+            bool first = true;
+            for (uint32_t r = 0; r < n; ++r) {
+                uint32_t best = 0xffffffffu;
+                for (uint32_t i = 0; i < n; ++i) {
+                    const uint32_t t = vlist[a + i];
+                    if ((first || t > last) && t <= best) best = t;
+                }
+                add(best);
+                last = best;
+                first = false;
             }
         }
+        normals[3 * v + 0] = sx;
+        normals[3 * v + 1] = sy;
+        normals[3 * v + 2] = sz;
     }
 }
 
@@ -643,12 +662,43 @@ cudaError_t launch_connect(const Job& j, const Launch& L)
     return cudaGetLastError();
 }
 
-cudaError_t launch_vertex_normals(const Job& j, const Launch& L)
+size_t vertex_normals_scratch_bytes(uint64_t ntri, uint64_t nvert)
 {
-    prof_begin(L, "gather_vertex_normals");
-    KVSMC_DTYPE_SWITCH(j.vol.dtype, { k_vertex_normals<T><<<grid_for(j.node_tiles, L), kThreads, 0, L.stream>>>(j); });
+    auto al = [](size_t v) { return (v + 255) / 256 * 256; };
+    return al(12 * ntri) + al(4 * nvert) * 2 + al(8 * nvert) + al(12 * ntri) + al(scan_scratch_bytes(nvert)) + 256;
+}
+
+void vertex_normals_carve(Job& j, uint64_t ntri, uint64_t nvert, void* scratch, void** scan, uint64_t** total)
+{
+    auto al = [](size_t v) { return (v + 255) / 256 * 256; };
+    char* p = static_cast<char*>(scratch);
+    j.tri_normals = reinterpret_cast<float*>(p); p += al(12 * ntri);
+    j.vcount = reinterpret_cast<uint32_t*>(p); p += al(4 * nvert);
+    j.vfill = reinterpret_cast<uint32_t*>(p); p += al(4 * nvert);
+    j.voff = reinterpret_cast<uint64_t*>(p); p += al(8 * nvert);
+    j.vlist = reinterpret_cast<uint32_t*>(p); p += al(12 * ntri);
+    *scan = p; p += al(scan_scratch_bytes(nvert));
+    *total = reinterpret_cast<uint64_t*>(p);
+    j.vtotal = *total;
+}
+
+cudaError_t launch_vertex_normals(const Job& j, uint64_t ntri, uint64_t nvert, void* scan, uint64_t* total,
+                                  const Launch& L)
+{
+    const unsigned grid = (unsigned)L.num_sms * 8;
+    cudaError_t e = cudaMemsetAsync(j.vcount, 0, 4 * nvert, L.stream);
+    if (e == cudaSuccess) e = cudaMemsetAsync(j.vfill, 0, 4 * nvert, L.stream);
+    if (e != cudaSuccess) return e;
+    prof_begin(L, "vertex_normals");
+    k_vn_count<<<grid, 256, 0, L.stream>>>(j.connections, ntri, j.vcount);
     prof_end(L);
-    *L.counter += 1;
+    e = launch_scan(j.vcount, j.voff, nvert, scan, total, L);
+    if (e != cudaSuccess) return e;
+    prof_begin(L, "vertex_normals");
+    k_vn_fill<<<grid, 256, 0, L.stream>>>(j.connections, ntri, j.voff, j.vfill, j.vlist);
+    k_vn_sum<<<grid, 256, 0, L.stream>>>(j.voff, j.vtotal, j.vlist, nvert, j.tri_normals, j.normals);
+    prof_end(L);
+    *L.counter += 3;
     return cudaGetLastError();
 }
 

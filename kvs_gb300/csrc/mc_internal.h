@@ -47,7 +47,13 @@ cudaError_t launch_emit_dup(const Job& j, const Launch& L);
 cudaError_t launch_node_count(const Job& j, const Launch& L);
 cudaError_t launch_node_emit(const Job& j, const Launch& L);
 cudaError_t launch_connect(const Job& j, const Launch& L);
-cudaError_t launch_vertex_normals(const Job& j, const Launch& L);
+// vertex normals (mode 2) from the connections and per-triangle normals
+// (k_connect writes them to j.tri_normals): scratch of
+// vertex_normals_scratch_bytes, carved into j by vertex_normals_carve
+size_t vertex_normals_scratch_bytes(uint64_t ntri, uint64_t nvert);
+void vertex_normals_carve(Job& j, uint64_t ntri, uint64_t nvert, void* scratch, void** scan, uint64_t** total);
+cudaError_t launch_vertex_normals(const Job& j, uint64_t ntri, uint64_t nvert, void* scan, uint64_t* total,
+                                  const Launch& L);
 
 // ---- streaming kernels (mc_stream.cu): duplicated mode, batched
 constexpr int kStreamThreads = 256;   // 8 independent warps per CTA
@@ -118,6 +124,16 @@ cudaError_t launch_unit_scan(const StreamGroup* d_groups, int ngroups, uint32_t 
                              const Launch& L, int scan_threads = 0);
 cudaError_t launch_iso_totals(const StreamIso* d_isos, int n, const uint64_t* d_plane_base, const uint64_t* d_total,
                               uint64_t* d_totals, const Launch& L);
+
+// ---- shared-vertex node passes on the streaming kernels (mc_snode.cu):
+// node units (plane, row, 256-node segment) numbered in node order; the count
+// pass writes one vertex count per unit, the emit pass (unit_offsets: the
+// exclusive scan of the counts) the rank words j.rank and the vertices
+// j.coords.  One isolevel; 8/16-bit and float32 volumes.
+size_t snode_shared_bytes(int dtype);
+cudaError_t launch_snode(bool emit, const Job& j, const FastIso& f, uint32_t wprn, uint32_t zchunk, uint64_t ntasks,
+                         uint32_t* unit_counts, const uint64_t* unit_offsets, int* status,
+                         unsigned long long* next_task, const Launch& L);
 
 // ---- SlicePlane on structured volumes (slice.cu): one warp per cell row
 // (y, z), rows numbered y fastest

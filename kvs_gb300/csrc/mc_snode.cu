@@ -1,0 +1,244 @@
+// mc_snode.cu -- the shared-vertex modes' node passes as streaming kernels.
+//
+// calculate_isopoints (MarchingCubes.cpp:366-446) visits every node in z, y, x
+// order and gives each of its x-, y- and z-edges (inside the grid) that the
+// isolevel crosses a vertex, numbered in that order and interpolated from the
+// node towards +axis.  Here a warp task is (a chunk of node planes, one node
+// row, a 256-node segment); the warp walks the planes of its chunk with the
+// row pair (y, y + 1) of planes z and z + 1 arriving in its shared-memory ring
+// of three buffers through bulk copies (cp.async.bulk, bounded mbarrier
+// waits), so each value is read from HBM once per pass.  A "node unit" =
+// (plane z, row y, segment): the count pass writes its number of vertices,
+// an exclusive scan over units in node order gives each unit's first vertex
+// id, and the emit pass writes, per 32-node word, the x/y/z crossing flags and
+// the word's first vertex id (the rank words the connection pass reads) and
+// the vertices themselves (the exact FP32 path of mc_interp.cuh, the FP64
+// sequence where it cannot decide).  Lane l takes the nodes l, l + 32, ...,
+// l + 224 of the segment, so each 32-node word's flags are three ballots.
+#include <cuda_runtime.h>
+
+#include "mc_internal.h"
+#include "mc_interp.cuh"
+#include "tma.cuh"
+
+namespace kvsmc {
+
+namespace {
+
+constexpr int kSnThreads = 256;
+constexpr int kSnWarps = kSnThreads / 32;
+constexpr uint32_t kSnSeg = 256;   // nodes per segment
+constexpr unsigned FULL = 0xffffffffu;
+
+__host__ __device__ __forceinline__ size_t sn_align(size_t v) { return (v + 127) / 128 * 128; }
+
+template <typename T, bool EMIT>
+__global__ void __launch_bounds__(kSnThreads)
+    k_snode(Job j, FastIso f, uint32_t wprn, uint32_t zchunk, uint64_t ntasks, uint32_t row_elems,
+            uint32_t copy_bytes, uint32_t* __restrict__ unit_counts, const uint64_t* __restrict__ unit_offsets,
+            int* __restrict__ status, unsigned long long* __restrict__ next_task, uint32_t wait_polls)
+{
+    extern __shared__ __align__(128) unsigned char smem_raw[];
+    const unsigned lane = threadIdx.x & 31u, warp = threadIdx.x >> 5;
+    const size_t plane_elems = 2 * (size_t)row_elems;
+    unsigned char* wbase = smem_raw + (size_t)warp * (128 + sn_align(3 * plane_elems * sizeof(T)));
+    uint64_t* bar = reinterpret_cast<uint64_t*>(wbase);
+    T* ring = reinterpret_cast<T*>(wbase + 128);
+    if (lane == 0) {
+        for (int b = 0; b < 3; ++b) mbar_init(&bar[b], 1);
+        fence_barrier_init();
+    }
+    __syncwarp();
+    const uint32_t nx = j.vol.nx, ny = j.vol.ny, nz = j.vol.nz;
+    const uint64_t pitch = j.vol.pitch, slice = j.vol.slice;
+    const T* vol = static_cast<const T*>(j.vol.data);
+    const unsigned lt = (1u << lane) - 1u;
+    uint32_t ph = 0;   // per ring buffer: parity of its next completion
+    for (;;) {
+        unsigned long long tk = 0;
+        if (lane == 0) tk = atomicAdd(next_task, 1ull);
+        const uint64_t task = __shfl_sync(FULL, tk, 0);
+        if (task >= ntasks) break;
+        const uint32_t s = (uint32_t)(task % wprn);
+        const uint32_t y = (uint32_t)((task / wprn) % ny);
+        const uint32_t zc = (uint32_t)(task / ((uint64_t)wprn * ny));
+        const uint32_t z0 = zc * zchunk;
+        const uint32_t z1 = z0 + zchunk < nz ? z0 + zchunk : nz;            // node planes [z0, z1)
+        const uint32_t nplanes = (z1 + 1 < nz ? z1 + 1 : nz) - z0;          // staged planes
+        const uint32_t nrows = y + 1 < ny ? 2u : 1u;
+        const uint64_t xoff = (uint64_t)s * kSnSeg;
+        const uint64_t avail = (pitch - xoff) * sizeof(T);
+        const uint32_t row_bytes = (uint32_t)(avail < copy_bytes ? avail : copy_bytes);
+        auto issue = [&](uint32_t i) {
+            const int b = (int)(i % 3u);
+            T* dst = ring + (size_t)b * plane_elems;
+            const T* src = vol + (uint64_t)(z0 + i) * slice + (uint64_t)y * pitch + xoff;
+            mbar_arrive_expect_tx(&bar[b], nrows * row_bytes);
+            for (uint32_t r = 0; r < nrows; ++r) bulk_copy_g2s(dst + r * row_elems, src + r * pitch, row_bytes, &bar[b]);
+        };
+        auto acquire = [&](uint32_t i) -> bool {
+            const uint32_t b = i % 3u;
+            const bool ok = mbar_wait(&bar[b], (ph >> b) & 1u, wait_polls);
+            if (ok) ph ^= 1u << b;
+            return ok;
+        };
+        __syncwarp();   // the previous task's reads of the ring are done
+        if (lane == 0) {
+            fence_proxy_async();
+            for (uint32_t i = 0; i < nplanes && i < 3; ++i) issue(i);
+        }
+        uint32_t acq = 0;
+        bool dead = false;
+        uint32_t issued = 0;
+        for (uint32_t z = z0; z < z1; ++z) {
+            const uint32_t st = z - z0;
+            const uint32_t need = z + 1 < nz ? st + 1 : st;   // last plane staged this step
+            bool ok = true;
+            while (ok && acq <= need) {
+                ok = acquire(acq);
+                if (ok) ++acq;
+            }
+            if (__any_sync(FULL, !ok)) {
+                if (lane == 0) atomicExch(status, 1);
+                dead = true;
+                issued = st + 3 < nplanes ? st + 3 : nplanes;
+                break;
+            }
+            const T* ra = ring + (size_t)(st % 3u) * plane_elems;            // plane z, row y
+            const T* rb = ra + row_elems;                                     // plane z, row y + 1
+            const T* rz = ring + (size_t)((st + 1) % 3u) * plane_elems;      // plane z + 1, row y
+            const bool has_y = y + 1 < ny, has_z = z + 1 < nz;
+            uint32_t fx[8], fy[8], fz[8];
+            uint32_t cnt = 0;
+#pragma unroll
+            for (int i = 0; i < 8; ++i) {
+                const uint32_t xl = lane + 32u * i;
+                const uint64_t x = xoff + xl;
+                bool bx = false, by = false, bz = false;
+                if (x < nx) {
+                    const bool a0 = above(j.cls, ra[xl]);
+                    bx = x + 1 < nx && above(j.cls, ra[xl + 1]) != a0;
+                    by = has_y && above(j.cls, rb[xl]) != a0;
+                    bz = has_z && above(j.cls, rz[xl]) != a0;
+                }
+                fx[i] = bx;
+                fy[i] = by;
+                fz[i] = bz;
+                cnt += (uint32_t)bx + (uint32_t)by + (uint32_t)bz;
+            }
+            const uint64_t unit = ((uint64_t)z * ny + y) * wprn + s;
+            if (!EMIT) {
+                const uint32_t tot = __reduce_add_sync(FULL, cnt);
+                if (lane == 0) unit_counts[unit] = tot;
+            } else {
+                uint64_t run = unit_offsets[unit];
+                const uint64_t row = (uint64_t)z * ny + y;
+                const float fxf = __uint2float_rn((uint32_t)xoff + lane);
+                const float fyf = __uint2float_rn(y), fzf = __uint2float_rn(z);
+#pragma unroll
+                for (int i = 0; i < 8; ++i) {
+                    const uint32_t wx = __ballot_sync(FULL, fx[i]);
+                    const uint32_t wy = __ballot_sync(FULL, fy[i]);
+                    const uint32_t wz = __ballot_sync(FULL, fz[i]);
+                    const uint64_t word = (uint64_t)s * (kSnSeg / 32) + i;
+                    if (lane == 0 && word < j.words_per_row)
+                        j.rank[row * j.words_per_row + word] = make_uint4(wx, wy, wz, (uint32_t)run);
+                    if (fx[i] | fy[i] | fz[i]) {
+                        uint64_t id = run + __popc(wx & lt) + __popc(wy & lt) + __popc(wz & lt);
+                        const uint32_t xl = lane + 32u * i;
+                        const float ax = __fadd_rn(fxf, (float)(32 * i));
+                        const float v0 = (float)ra[xl];
+                        if (fx[i]) {
+                            const float3 p = edge_vertex_fast(j.ip, f, v0, (float)ra[xl + 1], ax, fyf, fzf,
+                                                              __fadd_rn(ax, 1.0f), fyf, fzf, 0);
+                            float* o = j.coords + 3 * id++;
+                            o[0] = p.x; o[1] = p.y; o[2] = p.z;
+                        }
+                        if (fy[i]) {
+                            const float3 p = edge_vertex_fast(j.ip, f, v0, (float)rb[xl], ax, fyf, fzf, ax,
+                                                              __fadd_rn(fyf, 1.0f), fzf, 1);
+                            float* o = j.coords + 3 * id++;
+                            o[0] = p.x; o[1] = p.y; o[2] = p.z;
+                        }
+                        if (fz[i]) {
+                            const float3 p = edge_vertex_fast(j.ip, f, v0, (float)rz[xl], ax, fyf, fzf, ax, fyf,
+                                                              __fadd_rn(fzf, 1.0f), 2);
+                            float* o = j.coords + 3 * id;
+                            o[0] = p.x; o[1] = p.y; o[2] = p.z;
+                        }
+                    }
+                    run += __popc(wx) + __popc(wy) + __popc(wz);
+                }
+            }
+            // plane z is consumed: refill its buffer with plane z + 3
+            __syncwarp();
+            if (lane == 0 && st + 3 < nplanes) {
+                fence_proxy_async();
+                issue(st + 3);
+            }
+        }
+        if (dead) {
+            // wait (bounded, by its own limit) for the copies still in flight, then stop
+            for (uint32_t i = acq; i < issued; ++i) {
+                const uint32_t b = i % 3u;
+                if (mbar_wait(&bar[b], (ph >> b) & 1u, 1u << 16)) ph ^= 1u << b;
+            }
+            break;
+        }
+        // a normal walk acquires every staged plane: the last step's (z1 < nz) or
+        // none more (z1 == nz); keep the parity in step with what was issued
+        while (acq < nplanes) {
+            if (!acquire(acq)) break;
+            ++acq;
+        }
+    }
+}
+
+}  // namespace
+
+size_t snode_shared_bytes(int dtype)
+{
+    const size_t es = dtype_size(dtype);
+    const size_t plane = 2 * stream_row_elems(dtype, 1) * es;
+    return (size_t)kSnWarps * (128 + sn_align(3 * plane));
+}
+
+#define KVSMC_SN_SWITCH(DT, ...)                        \
+    switch (DT) {                                       \
+    case 0: { using T = int8_t; __VA_ARGS__; } break;   \
+    case 1: { using T = int16_t; __VA_ARGS__; } break;  \
+    case 4: { using T = uint8_t; __VA_ARGS__; } break;  \
+    case 5: { using T = uint16_t; __VA_ARGS__; } break; \
+    case 8: { using T = float; __VA_ARGS__; } break;    \
+    default: return cudaErrorInvalidValue;              \
+    }
+
+cudaError_t launch_snode(bool emit, const Job& j, const FastIso& f, uint32_t wprn, uint32_t zchunk, uint64_t ntasks,
+                         uint32_t* unit_counts, const uint64_t* unit_offsets, int* status,
+                         unsigned long long* next_task, const Launch& L)
+{
+    if (ntasks == 0) return cudaSuccess;
+    const int dt = j.vol.dtype;
+    const size_t smem = snode_shared_bytes(dt);
+    const uint32_t row_elems = (uint32_t)stream_row_elems(dt, 1);
+    const uint32_t copy_bytes = row_elems * (uint32_t)dtype_size(dt);
+    KVSMC_SN_SWITCH(dt, {
+        auto kern = emit ? k_snode<T, true> : k_snode<T, false>;
+        cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        int per_sm = 0;
+        if (e == cudaSuccess) e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, kSnThreads, smem);
+        if (e != cudaSuccess) return e;
+        const uint64_t resident = (uint64_t)(per_sm > 0 ? per_sm : 1) * (uint64_t)L.num_sms;
+        const uint64_t need = (ntasks + kSnWarps - 1) / kSnWarps;
+        const uint64_t nctas = need < resident ? need : resident;
+        prof_begin(L, emit ? "snode_emit" : "snode_count");
+        kern<<<(unsigned)nctas, kSnThreads, smem, L.stream>>>(j, f, wprn, zchunk, ntasks, row_elems, copy_bytes,
+                                                                unit_counts, unit_offsets, status, next_task,
+                                                                L.wait_polls[emit ? 1 : 0]);
+        prof_end(L);
+    });
+    *L.counter += 1;
+    return cudaGetLastError();
+}
+
+}  // namespace kvsmc

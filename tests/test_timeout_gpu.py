@@ -108,3 +108,25 @@ def test_wait_timeout_reported_and_context_recovers(dtype):
     fvol.free()
     ctx.close()
     fresh.close()
+
+
+def test_shared_vertex_wait_timeout_and_recovery():
+    """The shared-vertex node passes' waits (count, then emit) give up the same way."""
+    v = S.to_numpy(S.fbm((40, 48, 64), seed=3, device="cuda"))
+    params = _abi.make_params(0.5, _abi.MODE_SHARED_VERTEX_NORMAL)
+    fresh = _abi.Context(0)
+    fvol = _abi.DeviceVolume.upload(fresh, v)
+    ref = _abi.marching_cubes_host(fresh, v, params)
+    ctx = _abi.Context(0)
+    for limits in ((0, -1), (-1, 0)):
+        ctx.set_wait_limit(*limits)
+        with pytest.raises(_abi.KvsmcError) as e:
+            _abi.marching_cubes_host(ctx, v, params)
+        assert e.value.status == _abi.ERR_TIMEOUT
+    ctx.set_wait_limit(-1, -1)
+    got = _abi.marching_cubes_host(ctx, v, params)
+    for a, b in zip(got[:3], ref[:3]):
+        assert same_bits(a, b), first_diff(a, b)
+    fvol.free()
+    ctx.close()
+    fresh.close()
