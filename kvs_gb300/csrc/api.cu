@@ -6,6 +6,7 @@
 #include <cstdarg>
 #include <cstdio>
 #include <cstring>
+#include <memory>
 #include <string>
 #include <vector>
 
@@ -229,6 +230,11 @@ struct Plan {
     kvsmc::FastIso f{};
     int* d_status = nullptr;
     unsigned long long* d_next = nullptr;
+    // triangles of a shared-vertex request on the streaming count and the
+    // streaming connection pass (one group, one isolevel, one row per task)
+    Item* item = nullptr;
+    bool sconn = false;
+    std::unique_ptr<StreamBatch> batch;
 };
 
 uint32_t rows_for(uint32_t width, uint32_t limit)
@@ -242,6 +248,7 @@ uint32_t rows_for(uint32_t width, uint32_t limit)
 
 void gather_plan(const Item& it, Plan& pl)
 {
+    pl.item = const_cast<Item*>(&it);
     pl.shared = it.params.mode != KVSMC_DUP_POLYGON_NORMAL;
     Job& j = pl.job;
     std::memset(&j, 0, sizeof j);
@@ -280,12 +287,24 @@ kvsmc_status gather_count(kvsmc_context* ctx, Plan& pl)
         pl.ntasks = (uint64_t)((j.vol.nz + pl.zchunk - 1) / pl.zchunk) * j.vol.ny * pl.wprn;
         pl.f = kvsmc_host::make_fast(j.ip.iso, j.ip.vmin, j.ip.vmax, dt);
         j.node_tiles = steps;   // node units, for the counts and their scan
+        // the triangles too: the streaming count and the streaming connection
+        // pass when the volume takes the streaming layout with one row per task
+        if (stream_volume_eligible(ctx, *pl.item)) {
+            pl.batch.reset(new StreamBatch());
+            pl.batch->ctx = ctx;
+            pl.batch->items = {pl.item};
+            pl.batch->plan_tables();
+            pl.sconn = pl.batch->groups.size() == 1 && pl.batch->launches.size() == 1 && pl.batch->groups[0].rows == 1;
+            if (pl.sconn) j.cell_tiles = 0;
+            else pl.batch.reset();
+        }
     }
     const size_t ct = j.cell_tiles, nt = j.node_tiles;
     const uint64_t rank_words = pl.shared ? (uint64_t)j.vol.nz * j.vol.ny * j.words_per_row : 0;
-    const size_t need = 10 * 256 + align_up(ct * 4, 256) + align_up(ct * 8, 256) + align_up(nt * 4, 256) +
-                        align_up(nt * 8, 256) + align_up(rank_words * 16, 256) +
-                        align_up(scan_scratch_bytes(ct), 256) + align_up(scan_scratch_bytes(nt), 256);
+    const size_t own = 10 * 256 + align_up(ct * 4, 256) + align_up(ct * 8, 256) + align_up(nt * 4, 256) +
+                       align_up(nt * 8, 256) + align_up(rank_words * 16, 256) +
+                       align_up(scan_scratch_bytes(ct), 256) + align_up(scan_scratch_bytes(nt), 256);
+    const size_t need = own + (pl.sconn ? align_up(pl.batch->scratch_bytes(), 256) : 0);
     kvsmc_status st = ensure_scratch(ctx, need);
     if (st) return st;
     Carve cv{static_cast<char*>(ctx->scratch)};
@@ -301,13 +320,20 @@ kvsmc_status gather_count(kvsmc_context* ctx, Plan& pl)
     pl.d_next = cv.take<unsigned long long>(256);
     const kvsmc::Launch L = launch_of(ctx);
     KVSMC_CUDA(ctx, cudaMemsetAsync(d_totals, 0, 3 * sizeof(uint64_t), ctx->stream));
+    if (pl.sconn) {
+        // unit counts, unit scan, plane scan: the streaming count of one request
+        pl.batch->carve(static_cast<char*>(ctx->scratch) + own);
+        kvsmc_status bst = pl.batch->upload_tables();
+        if (!bst) bst = pl.batch->count();
+        if (bst) return bst;
+    }
     if (ct) {
         KVSMC_CUDA(ctx, launch_cell_count(j, L));
         KVSMC_CUDA(ctx, launch_scan(j.tile_counts, j.tile_offsets, ct, scan_a, d_totals, L));
     }
     if (nt && pl.snode) {
         KVSMC_CUDA(ctx, cudaMemsetAsync(pl.d_status, 0, sizeof(int), ctx->stream));
-        KVSMC_CUDA(ctx, cudaMemsetAsync(pl.d_next, 0, 2 * sizeof(unsigned long long), ctx->stream));
+        KVSMC_CUDA(ctx, cudaMemsetAsync(pl.d_next, 0, 3 * sizeof(unsigned long long), ctx->stream));
         KVSMC_CUDA(ctx, kvsmc::launch_snode(false, j, pl.f, pl.wprn, pl.zchunk, pl.ntasks, j.vtile_counts, nullptr,
                                             pl.d_status, pl.d_next, L));
         KVSMC_CUDA(ctx, launch_scan(j.vtile_counts, j.vtile_offsets, nt, scan_b, d_totals + 1, L));
@@ -319,7 +345,7 @@ kvsmc_status gather_count(kvsmc_context* ctx, Plan& pl)
     KVSMC_CUDA(ctx, cudaMemcpyAsync(ctx->h_small, d_totals, 3 * sizeof(uint64_t), cudaMemcpyDeviceToHost, ctx->stream));
     KVSMC_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
     if (ctx->h_small[2]) return fail(ctx, KVSMC_ERR_TIMEOUT, "shared-vertex count: a shared-memory load did not complete");
-    pl.ntri = ctx->h_small[0];
+    pl.ntri = pl.sconn ? pl.item->sizes.ntriangles : ctx->h_small[0];
     pl.nvert = pl.shared ? ctx->h_small[1] : 3 * pl.ntri;
     if (pl.shared && pl.nvert > 0xffffffffull)
         return fail(ctx, KVSMC_ERR_TOO_LARGE, "%llu shared vertices exceed 32-bit connection ids",
@@ -388,9 +414,15 @@ kvsmc_status gather_emit(kvsmc_context* ctx, Plan& pl, float* coords, float* nor
     } else if (pl.nvert) {
         KVSMC_CUDA(ctx, launch_node_emit(j, L));
     }
-    if (pl.ntri) KVSMC_CUDA(ctx, launch_connect(j, L));
+    if (pl.ntri && pl.sconn) {
+        StreamBatch& b = *pl.batch;
+        KVSMC_CUDA(ctx, kvsmc::launch_sconnect(j, b.d_groups, b.d_isos, b.d_unit_counts, b.d_unit_offsets,
+                                               b.d_plane_base, b.launches[0].ntasks, pl.d_status, pl.d_next + 2, L));
+    } else if (pl.ntri) {
+        KVSMC_CUDA(ctx, launch_connect(j, L));
+    }
     if (vertex_normals) KVSMC_CUDA(ctx, launch_vertex_normals(j, pl.ntri, pl.nvert, vn_scan, vn_total, L));
-    if (pl.nvert && pl.snode) {
+    if ((pl.nvert && pl.snode) || pl.sconn) {
         int* h = reinterpret_cast<int*>(ctx->h_small);
         KVSMC_CUDA(ctx, cudaMemcpyAsync(h, pl.d_status, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
         KVSMC_CUDA(ctx, cudaStreamSynchronize(ctx->stream));

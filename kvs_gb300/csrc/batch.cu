@@ -111,8 +111,12 @@ uint32_t stream_zchunk(uint64_t warp_steps, int num_sms, int tasks_per_sm)
 
 bool stream_eligible(const kvsmc_context* ctx, const Item& it)
 {
+    return it.params.mode == KVSMC_DUP_POLYGON_NORMAL && stream_volume_eligible(ctx, it);
+}
+
+bool stream_volume_eligible(const kvsmc_context* ctx, const Item& it)
+{
     if (ctx->path != 0 || !it.vol) return false;
-    if (it.params.mode != KVSMC_DUP_POLYGON_NORMAL) return false;
     const kvsmc::VolumeView& v = it.vol->view;
     if (!stream_dtype(v.dtype)) return false;
     if (v.nx < 2 || v.ny < 2 || v.nz < 2) return false;

@@ -149,6 +149,9 @@ kvsmc_tune_choice stream_shape(const kvsmc_context* ctx, const kvsmc::VolumeView
 // Requests the streaming kernels can take (duplicated mode, 8/16-bit and
 // float32 data, finite isolevel, width <= 4096 cells).
 bool stream_eligible(const kvsmc_context* ctx, const Item& it);
+// The same volume and isolevel conditions, whatever the mode (the streaming
+// count of a shared-vertex request).
+bool stream_volume_eligible(const kvsmc_context* ctx, const Item& it);
 // Count (and, for items with emit set, emit) all eligible items together.
 kvsmc_status stream_run(kvsmc_context* ctx, std::vector<Item*>& items);
 

@@ -135,6 +135,16 @@ cudaError_t launch_snode(bool emit, const Job& j, const FastIso& f, uint32_t wpr
                          uint32_t* unit_counts, const uint64_t* unit_offsets, int* status,
                          unsigned long long* next_task, const Launch& L);
 
+// connect_isopoints on the streaming cell tasks of a one-group, one-isolevel,
+// one-row-per-task streaming count (its unit counts and offsets, plane
+// bases): connections, and polygon normals (mode 1) or per-triangle normals
+// for the vertex normals (mode 2); the node emit pass must have written
+// j.rank and j.coords.
+size_t sconnect_shared_bytes(int dtype);
+cudaError_t launch_sconnect(const Job& j, const StreamGroup* d_groups, const StreamIso* d_isos,
+                            const uint16_t* unit_counts, const uint32_t* unit_offsets, const uint64_t* plane_base,
+                            uint64_t ntasks, int* status, unsigned long long* next_task, const Launch& L);
+
 // ---- SlicePlane on structured volumes (slice.cu): one warp per cell row
 // (y, z), rows numbered y fastest
 struct SliceJob {

@@ -23,6 +23,16 @@
 
 namespace kvsmc {
 
+#define KVSMC_SN_SWITCH(DT, ...)                        \
+    switch (DT) {                                       \
+    case 0: { using T = int8_t; __VA_ARGS__; } break;   \
+    case 1: { using T = int16_t; __VA_ARGS__; } break;  \
+    case 4: { using T = uint8_t; __VA_ARGS__; } break;  \
+    case 5: { using T = uint16_t; __VA_ARGS__; } break; \
+    case 8: { using T = float; __VA_ARGS__; } break;    \
+    default: return cudaErrorInvalidValue;              \
+    }
+
 namespace {
 
 constexpr int kSnThreads = 256;
@@ -194,7 +204,234 @@ __global__ void __launch_bounds__(kSnThreads)
     }
 }
 
+__constant__ uint64_t c_sc_tri[256] = MC_TRI_PACKED_INIT;
+__constant__ uint8_t c_sc_ntri[256] = MC_NTRI_INIT;
+__constant__ uint8_t c_sc_edge[12] = MC_EDGE_PACKED_INIT;
+
+// Vertex id of node (x, y, z)'s edge along `axis` from the rank words.
+__device__ __forceinline__ uint32_t sc_rank_id(const Job& j, uint32_t x, uint32_t y, uint32_t z, int axis)
+{
+    const uint4 R = j.rank[((uint64_t)z * j.vol.ny + y) * j.words_per_row + (x >> 5)];
+    const uint32_t bit = x & 31u, lt = (1u << bit) - 1u;
+    uint32_t id = R.w + __popc(R.x & lt) + __popc(R.y & lt) + __popc(R.z & lt);
+    if (axis >= 1) id += (R.x >> bit) & 1u;
+    if (axis >= 2) id += (R.y >> bit) & 1u;
+    return id;
+}
+
+// connect_isopoints (MarchingCubes.cpp:456-521) on the streaming layout: a
+// warp task is a cell task of the streaming count (one 256-cell row segment,
+// a chunk of planes, row pair (y, y + 1) of planes z, z + 1 in its ring); the
+// count pass's unit counts and scanned unit and plane offsets give every
+// unit's first triangle, a warp scan each lane's.  Lane l takes cells 8 l ..
+// 8 l + 7; per triangle (table order, vertices e[i], e[i+2], e[i+1]) the three
+// vertex ids come from the rank words of the edges' lower nodes, and the
+// polygon normal from the three vertices' coordinates (written by the node
+// emit pass): into the normals (polygon normals) or the per-triangle scratch
+// the vertex normals are summed from.  One isolevel per launch.
+template <typename T>
+__global__ void __launch_bounds__(kSnThreads)
+    k_sconnect(Job j, const StreamGroup* __restrict__ groups, const StreamIso* __restrict__ isos,
+               const uint16_t* __restrict__ unit_counts, const uint32_t* __restrict__ unit_offsets,
+               const uint64_t* __restrict__ plane_base, uint64_t ntasks, int* __restrict__ status,
+               unsigned long long* __restrict__ next_task, uint32_t wait_polls)
+{
+    extern __shared__ __align__(128) unsigned char smem_raw[];
+    __shared__ uint64_t s_tri[256];
+    __shared__ uint8_t s_ntri[256];
+    __shared__ uint8_t s_edge[16];
+    const unsigned tid = threadIdx.x, lane = tid & 31u, warp = tid >> 5;
+    for (unsigned c = tid; c < 256; c += blockDim.x) {
+        s_tri[c] = c_sc_tri[c];
+        s_ntri[c] = c_sc_ntri[c];
+        if (c < 12) s_edge[c] = c_sc_edge[c];
+    }
+    __syncthreads();
+    const StreamGroup& G = groups[0];
+    const uint32_t row_elems = G.seg_elems;
+    const size_t plane_elems = 2 * (size_t)row_elems;
+    unsigned char* wbase = smem_raw + (size_t)warp * (128 + sn_align(3 * plane_elems * sizeof(T)));
+    uint64_t* bar = reinterpret_cast<uint64_t*>(wbase);
+    T* ring = reinterpret_cast<T*>(wbase + 128);
+    if (lane == 0) {
+        for (int b = 0; b < 3; ++b) mbar_init(&bar[b], 1);
+        fence_barrier_init();
+    }
+    __syncwarp();
+    const uint32_t cx = G.vol.nx - 1, cy = G.vol.ny - 1, cz = G.vol.nz - 1;
+    const uint32_t wpr = G.wpr;
+    const uint64_t pitch = G.vol.pitch, slice = G.vol.slice;
+    const T* vol = static_cast<const T*>(G.vol.data);
+    const StreamIso& I = isos[G.iso_begin];
+    const uint64_t first_plane = plane_base[I.plane_index];
+    float* const tri_out = j.mode == 1 ? j.normals : j.tri_normals;
+    uint32_t ph = 0;
+    for (;;) {
+        unsigned long long tk = 0;
+        if (lane == 0) tk = atomicAdd(next_task, 1ull);
+        const uint64_t task = __shfl_sync(FULL, tk, 0);
+        if (task >= ntasks) break;
+        const uint32_t seg = (uint32_t)(task % wpr);
+        const uint32_t y = (uint32_t)((task / wpr) % cy);
+        const uint32_t zc = (uint32_t)(task / ((uint64_t)wpr * cy));
+        const uint32_t z0 = zc * G.zchunk;
+        const uint32_t z1 = z0 + G.zchunk < cz ? z0 + G.zchunk : cz;   // cell planes [z0, z1)
+        const uint32_t nplanes = z1 - z0 + 1;
+        const uint64_t xoff = (uint64_t)seg * 256;
+        const uint64_t avail = (pitch - xoff) * sizeof(T);
+        const uint32_t row_bytes = (uint32_t)(avail < G.seg_copy_bytes ? avail : G.seg_copy_bytes);
+        auto issue = [&](uint32_t i) {
+            const int b = (int)(i % 3u);
+            T* dst = ring + (size_t)b * plane_elems;
+            const T* src = vol + (uint64_t)(z0 + i) * slice + (uint64_t)y * pitch + xoff;
+            mbar_arrive_expect_tx(&bar[b], 2 * row_bytes);
+            for (uint32_t r = 0; r < 2; ++r) bulk_copy_g2s(dst + r * row_elems, src + r * pitch, row_bytes, &bar[b]);
+        };
+        auto acquire = [&](uint32_t i) -> bool {
+            const uint32_t b = i % 3u;
+            const bool ok = mbar_wait(&bar[b], (ph >> b) & 1u, wait_polls);
+            if (ok) ph ^= 1u << b;
+            return ok;
+        };
+        __syncwarp();
+        if (lane == 0) {
+            fence_proxy_async();
+            for (uint32_t i = 0; i < nplanes && i < 3; ++i) issue(i);
+        }
+        uint32_t acq = 0, issued = 0;
+        bool dead = false;
+        const uint32_t x0 = (uint32_t)xoff + 8 * lane;
+        const int lim = (int)cx - (int)x0;   // cells of this lane inside the row (if < 8)
+        for (uint32_t z = z0; z < z1; ++z) {
+            const uint32_t st = z - z0;
+            bool ok = true;
+            while (ok && acq <= st + 1) {
+                ok = acquire(acq);
+                if (ok) ++acq;
+            }
+            if (__any_sync(FULL, !ok)) {
+                if (lane == 0) atomicExch(status, 1);
+                dead = true;
+                issued = st + 3 < nplanes ? st + 3 : nplanes;
+                break;
+            }
+            const uint64_t unit = ((uint64_t)z * cy + y) * wpr + seg;
+            if (unit_counts[G.unit_base + unit] != 0) {
+                const T* a0 = ring + (size_t)(st % 3u) * plane_elems + 8 * lane;
+                const T* a1 = a0 + row_elems;
+                const T* b0 = ring + (size_t)((st + 1) % 3u) * plane_elems + 8 * lane;
+                const T* b1 = b0 + row_elems;
+                uint32_t m[4] = {0, 0, 0, 0};   // per staged row: node above bits of this lane's 9 nodes
+#pragma unroll
+                for (int k = 0; k < 9; ++k) {
+                    m[0] |= (above(j.cls, a0[k]) ? 1u : 0u) << k;
+                    m[1] |= (above(j.cls, a1[k]) ? 1u : 0u) << k;
+                    m[2] |= (above(j.cls, b0[k]) ? 1u : 0u) << k;
+                    m[3] |= (above(j.cls, b1[k]) ? 1u : 0u) << k;
+                }
+                uint32_t cases[8];
+                uint32_t n = 0;
+#pragma unroll
+                for (int i = 0; i < 8; ++i) {
+                    // corners 0:(x,y,z) 1:(x+1,y,z) 2:(x+1,y+1,z) 3:(x,y+1,z), 4..7 the same at z+1
+                    uint32_t c = ((m[0] >> i) & 1u) | (((m[0] >> (i + 1)) & 1u) << 1) |
+                                 (((m[1] >> (i + 1)) & 1u) << 2) | (((m[1] >> i) & 1u) << 3) |
+                                 (((m[2] >> i) & 1u) << 4) | (((m[2] >> (i + 1)) & 1u) << 5) |
+                                 (((m[3] >> (i + 1)) & 1u) << 6) | (((m[3] >> i) & 1u) << 7);
+                    if (i >= lim) c = 0;
+                    cases[i] = c;
+                    n += s_ntri[c];
+                }
+                uint32_t inc = n;
+#pragma unroll
+                for (int o = 1; o < 32; o <<= 1) {
+                    const uint32_t t = __shfl_up_sync(FULL, inc, o);
+                    if (lane >= (unsigned)o) inc += t;
+                }
+                if (n) {
+                    uint64_t t = plane_base[I.plane_index + z] - first_plane + unit_offsets[G.unit_base + unit] +
+                                 (inc - n);
+                    for (int i = 0; i < 8; ++i) {
+                        const uint32_t c = cases[i];
+                        const uint32_t nt = s_ntri[c];
+                        uint64_t pk = s_tri[c];
+                        const uint32_t x = x0 + i;
+                        for (uint32_t k = 0; k < nt; ++k, ++t, pk >>= 12) {
+                            uint32_t id[3];
+#pragma unroll
+                            for (int q = 0; q < 3; ++q) {
+                                const unsigned ep = s_edge[(pk >> (4 * q)) & 15u];
+                                const unsigned ca = ep & 7u, cb = ep >> 3;
+                                const unsigned nd = ca & cb, d = ca ^ cb;   // lower node, axis bit
+                                const int axis = d == 1u ? 0 : (d == 2u ? 1 : 2);
+                                id[q] = sc_rank_id(j, x + (nd & 1u), y + ((nd >> 1) & 1u), z + (nd >> 2), axis);
+                            }
+                            uint32_t* o = j.connections + 3 * t;
+                            o[0] = id[0]; o[1] = id[1]; o[2] = id[2];
+                            if (tri_out) {
+                                const float* p0 = j.coords + 3 * (uint64_t)id[0];
+                                const float* p1 = j.coords + 3 * (uint64_t)id[1];
+                                const float* p2 = j.coords + 3 * (uint64_t)id[2];
+                                const float3 nn = tri_normal(make_float3(p0[0], p0[1], p0[2]),
+                                                             make_float3(p1[0], p1[1], p1[2]),
+                                                             make_float3(p2[0], p2[1], p2[2]));
+                                float* q = tri_out + 3 * t;
+                                q[0] = nn.x; q[1] = nn.y; q[2] = nn.z;
+                            }
+                        }
+                    }
+                }
+            }
+            __syncwarp();
+            if (lane == 0 && st + 3 < nplanes) {
+                fence_proxy_async();
+                issue(st + 3);
+            }
+        }
+        if (dead) {
+            for (uint32_t i = acq; i < issued; ++i) {
+                const uint32_t b = i % 3u;
+                if (mbar_wait(&bar[b], (ph >> b) & 1u, 1u << 16)) ph ^= 1u << b;
+            }
+            break;
+        }
+    }
+}
+
 }  // namespace
+
+size_t sconnect_shared_bytes(int dtype)
+{
+    const size_t es = dtype_size(dtype);
+    const size_t plane = 2 * stream_row_elems(dtype, 1) * es;
+    return (size_t)kSnWarps * (128 + sn_align(3 * plane));
+}
+
+cudaError_t launch_sconnect(const Job& j, const StreamGroup* d_groups, const StreamIso* d_isos,
+                            const uint16_t* unit_counts, const uint32_t* unit_offsets, const uint64_t* plane_base,
+                            uint64_t ntasks, int* status, unsigned long long* next_task, const Launch& L)
+{
+    if (ntasks == 0) return cudaSuccess;
+    const int dt = j.vol.dtype;
+    const size_t smem = sconnect_shared_bytes(dt);
+    KVSMC_SN_SWITCH(dt, {
+        auto kern = k_sconnect<T>;
+        cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        int per_sm = 0;
+        if (e == cudaSuccess) e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, kSnThreads, smem);
+        if (e != cudaSuccess) return e;
+        const uint64_t resident = (uint64_t)(per_sm > 0 ? per_sm : 1) * (uint64_t)L.num_sms;
+        const uint64_t need = (ntasks + kSnWarps - 1) / kSnWarps;
+        const uint64_t nctas = need < resident ? need : resident;
+        prof_begin(L, "sconnect");
+        kern<<<(unsigned)nctas, kSnThreads, smem, L.stream>>>(j, d_groups, d_isos, unit_counts, unit_offsets,
+                                                                plane_base, ntasks, status, next_task,
+                                                                L.wait_polls[1]);
+        prof_end(L);
+    });
+    *L.counter += 1;
+    return cudaGetLastError();
+}
 
 size_t snode_shared_bytes(int dtype)
 {
@@ -202,16 +439,6 @@ size_t snode_shared_bytes(int dtype)
     const size_t plane = 2 * stream_row_elems(dtype, 1) * es;
     return (size_t)kSnWarps * (128 + sn_align(3 * plane));
 }
-
-#define KVSMC_SN_SWITCH(DT, ...)                        \
-    switch (DT) {                                       \
-    case 0: { using T = int8_t; __VA_ARGS__; } break;   \
-    case 1: { using T = int16_t; __VA_ARGS__; } break;  \
-    case 4: { using T = uint8_t; __VA_ARGS__; } break;  \
-    case 5: { using T = uint16_t; __VA_ARGS__; } break; \
-    case 8: { using T = float; __VA_ARGS__; } break;    \
-    default: return cudaErrorInvalidValue;              \
-    }
 
 cudaError_t launch_snode(bool emit, const Job& j, const FastIso& f, uint32_t wprn, uint32_t zchunk, uint64_t ntasks,
                          uint32_t* unit_counts, const uint64_t* unit_offsets, int* status,

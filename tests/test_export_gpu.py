@@ -122,7 +122,8 @@ def test_exporter_checks_like_the_reference(kvsmc_ctx, tmp_path, capsys):
     v[1, 1, 1] = 1
     mc = MarchingCubes(StructuredVolumeObject(v), 0.5, context=kvsmc_ctx)
     ex = PolygonExporterStl(mc, context=kvsmc_ctx)
-    assert not ex.write(str(tmp_path / "a.stl"))          # ASCII is the default file type: not provided
+    assert ex.write(str(tmp_path / "a.stl"))              # ASCII, the default file type (Stl.cpp:86)
+    assert (tmp_path / "a.stl").read_bytes().startswith(b"solid Generated by KVS\nfacet normal ")
     ex.setFileType("binary")
     assert ex.write(str(tmp_path / "b.stl"))
 
