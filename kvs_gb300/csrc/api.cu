@@ -408,25 +408,39 @@ kvsmc_status gather_emit(kvsmc_context* ctx, Plan& pl, float* coords, float* nor
     } else {
         j.tri_normals = nullptr;
     }
+    // A pass whose bounded waits gave up leaves its outputs unwritten: the next
+    // pass would read those as vertex ids, so the status is checked before it.
+    auto check_status = [&](const char* what) -> kvsmc_status {
+        int* h = reinterpret_cast<int*>(ctx->h_small);
+        KVSMC_CUDA(ctx, cudaMemcpyAsync(h, pl.d_status, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
+        KVSMC_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+        if (*h == 1) return fail(ctx, KVSMC_ERR_TIMEOUT, "%s: a shared-memory load did not complete", what);
+        if (*h) return fail(ctx, KVSMC_ERR_CUDA, "%s: a vertex id out of range", what);
+        return KVSMC_OK;
+    };
+    kvsmc_status st = KVSMC_OK;
     if (pl.nvert && pl.snode) {
         KVSMC_CUDA(ctx, kvsmc::launch_snode(true, j, pl.f, pl.wprn, pl.zchunk, pl.ntasks, nullptr, j.vtile_offsets,
                                             pl.d_status, pl.d_next + 1, L));
+        if ((st = check_status("shared-vertex node emit"))) return st;
     } else if (pl.nvert) {
         KVSMC_CUDA(ctx, launch_node_emit(j, L));
     }
     if (pl.ntri && pl.sconn) {
         StreamBatch& b = *pl.batch;
         KVSMC_CUDA(ctx, kvsmc::launch_sconnect(j, b.d_groups, b.d_isos, b.d_unit_counts, b.d_unit_offsets,
-                                               b.d_plane_base, b.launches[0].ntasks, pl.d_status, pl.d_next + 2, L));
+                                               b.d_plane_base, b.launches[0].ntasks, pl.nvert, pl.d_status,
+                                               pl.d_next + 2, L));
+        if ((st = check_status("shared-vertex connections"))) return st;
     } else if (pl.ntri) {
         KVSMC_CUDA(ctx, launch_connect(j, L));
     }
-    if (vertex_normals) KVSMC_CUDA(ctx, launch_vertex_normals(j, pl.ntri, pl.nvert, vn_scan, vn_total, L));
-    if ((pl.nvert && pl.snode) || pl.sconn) {
-        int* h = reinterpret_cast<int*>(ctx->h_small);
-        KVSMC_CUDA(ctx, cudaMemcpyAsync(h, pl.d_status, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
-        KVSMC_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
-        if (*h) return fail(ctx, KVSMC_ERR_TIMEOUT, "shared-vertex emit: a shared-memory load did not complete");
+    if (vertex_normals) {
+        KVSMC_CUDA(ctx, launch_vertex_normals(j, pl.ntri, pl.nvert, vn_scan, vn_total, L));
+    } else if (pl.nvert && j.mode == KVSMC_SHARED_VERTEX_NORMAL) {
+        // vertices without any triangle (a volume one node thick): zero normals
+        // (calculate_normals_on_vertex adds nothing to its zeroed array)
+        KVSMC_CUDA(ctx, cudaMemsetAsync(j.normals, 0, 12 * pl.nvert, ctx->stream));
     }
     return KVSMC_OK;
 }

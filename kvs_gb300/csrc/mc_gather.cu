@@ -390,21 +390,26 @@ __global__ void __launch_bounds__(kThreads) k_connect(Job j)
 // triangle ids placed by atomics in any order), and one thread per vertex
 // sorts its list (a vertex lies on one cell edge: at most four cells, a few
 // triangles each) and adds the normals in increasing triangle order.
-__global__ void __launch_bounds__(256) k_vn_count(const uint32_t* __restrict__ conn, uint64_t ntri,
+// (connections hold vertex ids below nvert; an id at or above it, which
+// consistent inputs never give, is skipped so nothing is touched out of range)
+__global__ void __launch_bounds__(256) k_vn_count(const uint32_t* __restrict__ conn, uint64_t ntri, uint64_t nvert,
                                                  uint32_t* __restrict__ vcount)
 {
     for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < 3 * ntri;
-         i += (uint64_t)gridDim.x * blockDim.x)
-        atomicAdd(vcount + conn[i], 1u);
+         i += (uint64_t)gridDim.x * blockDim.x) {
+        const uint32_t v = conn[i];
+        if (v < nvert) atomicAdd(vcount + v, 1u);
+    }
 }
 
-__global__ void __launch_bounds__(256) k_vn_fill(const uint32_t* __restrict__ conn, uint64_t ntri,
+__global__ void __launch_bounds__(256) k_vn_fill(const uint32_t* __restrict__ conn, uint64_t ntri, uint64_t nvert,
                                                 const uint64_t* __restrict__ voff, uint32_t* __restrict__ vfill,
                                                 uint32_t* __restrict__ vlist)
 {
     for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < 3 * ntri;
          i += (uint64_t)gridDim.x * blockDim.x) {
         const uint32_t v = conn[i];
+        if (v >= nvert) continue;
         const uint32_t slot = atomicAdd(vfill + v, 1u);
         vlist[voff[v] + slot] = (uint32_t)(i / 3);
     }
@@ -690,12 +695,12 @@ cudaError_t launch_vertex_normals(const Job& j, uint64_t ntri, uint64_t nvert, v
     if (e == cudaSuccess) e = cudaMemsetAsync(j.vfill, 0, 4 * nvert, L.stream);
     if (e != cudaSuccess) return e;
     prof_begin(L, "vertex_normals");
-    k_vn_count<<<grid, 256, 0, L.stream>>>(j.connections, ntri, j.vcount);
+    k_vn_count<<<grid, 256, 0, L.stream>>>(j.connections, ntri, nvert, j.vcount);
     prof_end(L);
     e = launch_scan(j.vcount, j.voff, nvert, scan, total, L);
     if (e != cudaSuccess) return e;
     prof_begin(L, "vertex_normals");
-    k_vn_fill<<<grid, 256, 0, L.stream>>>(j.connections, ntri, j.voff, j.vfill, j.vlist);
+    k_vn_fill<<<grid, 256, 0, L.stream>>>(j.connections, ntri, nvert, j.voff, j.vfill, j.vlist);
     k_vn_sum<<<grid, 256, 0, L.stream>>>(j.voff, j.vtotal, j.vlist, nvert, j.tri_normals, j.normals);
     prof_end(L);
     *L.counter += 3;

@@ -118,7 +118,7 @@ __global__ void __launch_bounds__(kSnThreads)
             const T* rb = ra + row_elems;                                     // plane z, row y + 1
             const T* rz = ring + (size_t)((st + 1) % 3u) * plane_elems;      // plane z + 1, row y
             const bool has_y = y + 1 < ny, has_z = z + 1 < nz;
-            uint32_t fx[8], fy[8], fz[8];
+            uint32_t fx = 0, fy = 0, fz = 0;   // crossing flags of this lane's 8 nodes, bit i = node lane + 32 i
             uint32_t cnt = 0;
 #pragma unroll
             for (int i = 0; i < 8; ++i) {
@@ -131,9 +131,9 @@ __global__ void __launch_bounds__(kSnThreads)
                     by = has_y && above(j.cls, rb[xl]) != a0;
                     bz = has_z && above(j.cls, rz[xl]) != a0;
                 }
-                fx[i] = bx;
-                fy[i] = by;
-                fz[i] = bz;
+                fx |= (uint32_t)bx << i;
+                fy |= (uint32_t)by << i;
+                fz |= (uint32_t)bz << i;
                 cnt += (uint32_t)bx + (uint32_t)by + (uint32_t)bz;
             }
             const uint64_t unit = ((uint64_t)z * ny + y) * wprn + s;
@@ -143,37 +143,32 @@ __global__ void __launch_bounds__(kSnThreads)
             } else {
                 uint64_t run = unit_offsets[unit];
                 const uint64_t row = (uint64_t)z * ny + y;
-                const float fxf = __uint2float_rn((uint32_t)xoff + lane);
                 const float fyf = __uint2float_rn(y), fzf = __uint2float_rn(z);
-#pragma unroll
+#pragma unroll 1
                 for (int i = 0; i < 8; ++i) {
-                    const uint32_t wx = __ballot_sync(FULL, fx[i]);
-                    const uint32_t wy = __ballot_sync(FULL, fy[i]);
-                    const uint32_t wz = __ballot_sync(FULL, fz[i]);
+                    const uint32_t bx = (fx >> i) & 1u, by = (fy >> i) & 1u, bz = (fz >> i) & 1u;
+                    const uint32_t wx = __ballot_sync(FULL, bx);
+                    const uint32_t wy = __ballot_sync(FULL, by);
+                    const uint32_t wz = __ballot_sync(FULL, bz);
                     const uint64_t word = (uint64_t)s * (kSnSeg / 32) + i;
                     if (lane == 0 && word < j.words_per_row)
                         j.rank[row * j.words_per_row + word] = make_uint4(wx, wy, wz, (uint32_t)run);
-                    if (fx[i] | fy[i] | fz[i]) {
+                    const uint32_t flags = bx | (by << 1) | (bz << 2);
+                    if (flags) {
                         uint64_t id = run + __popc(wx & lt) + __popc(wy & lt) + __popc(wz & lt);
                         const uint32_t xl = lane + 32u * i;
-                        const float ax = __fadd_rn(fxf, (float)(32 * i));
+                        const float ax = __uint2float_rn((uint32_t)xoff + xl);
                         const float v0 = (float)ra[xl];
-                        if (fx[i]) {
-                            const float3 p = edge_vertex_fast(j.ip, f, v0, (float)ra[xl + 1], ax, fyf, fzf,
-                                                              __fadd_rn(ax, 1.0f), fyf, fzf, 0);
+                        // one copy of the vertex code for the three axes (a loop, not unrolled)
+#pragma unroll 1
+                        for (int axis = 0; axis < 3; ++axis) {
+                            if (!((flags >> axis) & 1u)) continue;
+                            const float v1 = (float)(axis == 0 ? ra[xl + 1] : (axis == 1 ? rb[xl] : rz[xl]));
+                            const float bx = axis == 0 ? __fadd_rn(ax, 1.0f) : ax;
+                            const float by = axis == 1 ? __fadd_rn(fyf, 1.0f) : fyf;
+                            const float bz = axis == 2 ? __fadd_rn(fzf, 1.0f) : fzf;
+                            const float3 p = edge_vertex_fast(j.ip, f, v0, v1, ax, fyf, fzf, bx, by, bz, axis);
                             float* o = j.coords + 3 * id++;
-                            o[0] = p.x; o[1] = p.y; o[2] = p.z;
-                        }
-                        if (fy[i]) {
-                            const float3 p = edge_vertex_fast(j.ip, f, v0, (float)rb[xl], ax, fyf, fzf, ax,
-                                                              __fadd_rn(fyf, 1.0f), fzf, 1);
-                            float* o = j.coords + 3 * id++;
-                            o[0] = p.x; o[1] = p.y; o[2] = p.z;
-                        }
-                        if (fz[i]) {
-                            const float3 p = edge_vertex_fast(j.ip, f, v0, (float)rz[xl], ax, fyf, fzf, ax, fyf,
-                                                              __fadd_rn(fzf, 1.0f), 2);
-                            float* o = j.coords + 3 * id;
                             o[0] = p.x; o[1] = p.y; o[2] = p.z;
                         }
                     }
@@ -233,7 +228,7 @@ template <typename T>
 __global__ void __launch_bounds__(kSnThreads)
     k_sconnect(Job j, const StreamGroup* __restrict__ groups, const StreamIso* __restrict__ isos,
                const uint16_t* __restrict__ unit_counts, const uint32_t* __restrict__ unit_offsets,
-               const uint64_t* __restrict__ plane_base, uint64_t ntasks, int* __restrict__ status,
+               const uint64_t* __restrict__ plane_base, uint64_t ntasks, uint64_t nvert, int* __restrict__ status,
                unsigned long long* __restrict__ next_task, uint32_t wait_polls)
 {
     extern __shared__ __align__(128) unsigned char smem_raw[];
@@ -348,36 +343,61 @@ __global__ void __launch_bounds__(kSnThreads)
                     const uint32_t t = __shfl_up_sync(FULL, inc, o);
                     if (lane >= (unsigned)o) inc += t;
                 }
-                if (n) {
-                    uint64_t t = plane_base[I.plane_index + z] - first_plane + unit_offsets[G.unit_base + unit] +
-                                 (inc - n);
-                    for (int i = 0; i < 8; ++i) {
-                        const uint32_t c = cases[i];
-                        const uint32_t nt = s_ntri[c];
-                        uint64_t pk = s_tri[c];
-                        const uint32_t x = x0 + i;
-                        for (uint32_t k = 0; k < nt; ++k, ++t, pk >>= 12) {
-                            uint32_t id[3];
+                const uint32_t total = __shfl_sync(FULL, inc, 31);
+                const uint64_t tbase = plane_base[I.plane_index + z] - first_plane + unit_offsets[G.unit_base + unit];
+                // the step's triangles spread over the lanes: triangle q belongs to the
+                // first lane whose inclusive count exceeds q (binary search over lanes)
+                for (uint32_t q0 = 0; q0 < total; q0 += 32) {
+                    const uint32_t q = q0 + lane;
+                    uint32_t lo = 0;
 #pragma unroll
-                            for (int q = 0; q < 3; ++q) {
-                                const unsigned ep = s_edge[(pk >> (4 * q)) & 15u];
-                                const unsigned ca = ep & 7u, cb = ep >> 3;
-                                const unsigned nd = ca & cb, d = ca ^ cb;   // lower node, axis bit
-                                const int axis = d == 1u ? 0 : (d == 2u ? 1 : 2);
-                                id[q] = sc_rank_id(j, x + (nd & 1u), y + ((nd >> 1) & 1u), z + (nd >> 2), axis);
-                            }
-                            uint32_t* o = j.connections + 3 * t;
-                            o[0] = id[0]; o[1] = id[1]; o[2] = id[2];
-                            if (tri_out) {
-                                const float* p0 = j.coords + 3 * (uint64_t)id[0];
-                                const float* p1 = j.coords + 3 * (uint64_t)id[1];
-                                const float* p2 = j.coords + 3 * (uint64_t)id[2];
-                                const float3 nn = tri_normal(make_float3(p0[0], p0[1], p0[2]),
-                                                             make_float3(p1[0], p1[1], p1[2]),
-                                                             make_float3(p2[0], p2[1], p2[2]));
-                                float* q = tri_out + 3 * t;
-                                q[0] = nn.x; q[1] = nn.y; q[2] = nn.z;
-                            }
+                    for (int b = 4; b >= 0; --b) {
+                        const uint32_t mid = lo + (1u << b) - 1u;
+                        const uint32_t im = __shfl_sync(FULL, inc, mid);
+                        if (im <= q) lo = mid + 1;
+                    }
+                    const uint32_t owner = lo < 32 ? lo : 31;
+                    const uint32_t first = __shfl_sync(FULL, inc - n, owner);
+                    uint32_t oc[8];
+#pragma unroll
+                    for (int i = 0; i < 8; ++i) oc[i] = __shfl_sync(FULL, cases[i], owner);
+                    if (q < total) {
+                        // the owner's cell and triangle of local triangle r
+                        uint32_t r = q - first, ci = 0, c = oc[0];
+#pragma unroll
+                        for (int i = 0; i < 8; ++i) {
+                            const uint32_t nt = s_ntri[oc[i]];
+                            if (ci == (uint32_t)i && r >= nt) { r -= nt; ci = i + 1; }
+                        }
+#pragma unroll
+                        for (int i = 0; i < 8; ++i) if ((uint32_t)i == ci) c = oc[i];
+                        const uint64_t pk = s_tri[c] >> (12 * r);
+                        const uint32_t x = (uint32_t)xoff + 8 * owner + ci;
+                        const uint64_t t = tbase + q;
+                        uint32_t id[3];
+                        bool good = true;
+#pragma unroll
+                        for (int e = 0; e < 3; ++e) {
+                            const unsigned ep = s_edge[(pk >> (4 * e)) & 15u];
+                            const unsigned ca = ep & 7u, cb = ep >> 3;
+                            const unsigned nd = ca & cb, d = ca ^ cb;   // lower node, axis bit
+                            const int axis = d == 1u ? 0 : (d == 2u ? 1 : 2);
+                            id[e] = sc_rank_id(j, x + (nd & 1u), y + ((nd >> 1) & 1u), z + (nd >> 2), axis);
+                            good = good && id[e] < nvert;
+                        }
+                        uint32_t* o = j.connections + 3 * t;
+                        o[0] = id[0]; o[1] = id[1]; o[2] = id[2];
+                        if (!good) {
+                            atomicExch(status, 2);   // never with consistent rank words; nothing read out of range
+                        } else if (tri_out) {
+                            const float* p0 = j.coords + 3 * (uint64_t)id[0];
+                            const float* p1 = j.coords + 3 * (uint64_t)id[1];
+                            const float* p2 = j.coords + 3 * (uint64_t)id[2];
+                            const float3 nn = tri_normal(make_float3(p0[0], p0[1], p0[2]),
+                                                         make_float3(p1[0], p1[1], p1[2]),
+                                                         make_float3(p2[0], p2[1], p2[2]));
+                            float* qn = tri_out + 3 * t;
+                            qn[0] = nn.x; qn[1] = nn.y; qn[2] = nn.z;
                         }
                     }
                 }
@@ -409,7 +429,8 @@ size_t sconnect_shared_bytes(int dtype)
 
 cudaError_t launch_sconnect(const Job& j, const StreamGroup* d_groups, const StreamIso* d_isos,
                             const uint16_t* unit_counts, const uint32_t* unit_offsets, const uint64_t* plane_base,
-                            uint64_t ntasks, int* status, unsigned long long* next_task, const Launch& L)
+                            uint64_t ntasks, uint64_t nvert, int* status, unsigned long long* next_task,
+                            const Launch& L)
 {
     if (ntasks == 0) return cudaSuccess;
     const int dt = j.vol.dtype;
@@ -425,7 +446,7 @@ cudaError_t launch_sconnect(const Job& j, const StreamGroup* d_groups, const Str
         const uint64_t nctas = need < resident ? need : resident;
         prof_begin(L, "sconnect");
         kern<<<(unsigned)nctas, kSnThreads, smem, L.stream>>>(j, d_groups, d_isos, unit_counts, unit_offsets,
-                                                                plane_base, ntasks, status, next_task,
+                                                                plane_base, ntasks, nvert, status, next_task,
                                                                 L.wait_polls[1]);
         prof_end(L);
     });

@@ -92,6 +92,10 @@ def test_fixed6_formatting_against_c_conversion(kvsmc_ctx, tmp_path, mode):
     assert st == _abi.OK, _abi.status_string(st)
     want = E.stl_ascii(coords, normals, conn, E.POLYGON_NORMAL if mode == 0 else E.VERTEX_NORMAL)
     got = p.read_bytes()
+    if mode != _abi.MODE_DUP_POLYGON_NORMAL:
+        # normals averaged from NaN inputs: the sign of a NaN that arithmetic
+        # produces is not specified (x86, Arm and the GPU differ)
+        got, want = got.replace(b"-nan", b"nan"), want.replace(b"-nan", b"nan")
     if got != want:
         a, b = got.split(b"\n"), want.split(b"\n")
         i = next(i for i in range(min(len(a), len(b))) if a[i] != b[i])
