@@ -429,8 +429,8 @@ kvsmc_status gather_emit(kvsmc_context* ctx, Plan& pl, float* coords, float* nor
     if (pl.ntri && pl.sconn) {
         StreamBatch& b = *pl.batch;
         KVSMC_CUDA(ctx, kvsmc::launch_sconnect(j, b.d_groups, b.d_isos, b.d_unit_counts, b.d_unit_offsets,
-                                               b.d_plane_base, b.launches[0].ntasks, pl.nvert, pl.d_status,
-                                               pl.d_next + 2, L));
+                                               b.d_plane_base, b.launches[0].ntasks, pl.nvert, pl.ntri,
+                                               pl.d_status, pl.d_next + 2, L));
         if ((st = check_status("shared-vertex connections"))) return st;
     } else if (pl.ntri) {
         KVSMC_CUDA(ctx, launch_connect(j, L));

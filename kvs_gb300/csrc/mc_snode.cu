@@ -228,7 +228,8 @@ template <typename T>
 __global__ void __launch_bounds__(kSnThreads)
     k_sconnect(Job j, const StreamGroup* __restrict__ groups, const StreamIso* __restrict__ isos,
                const uint16_t* __restrict__ unit_counts, const uint32_t* __restrict__ unit_offsets,
-               const uint64_t* __restrict__ plane_base, uint64_t ntasks, uint64_t nvert, int* __restrict__ status,
+               const uint64_t* __restrict__ plane_base, uint64_t ntasks, uint64_t nvert, uint64_t ntri,
+               int* __restrict__ status,
                unsigned long long* __restrict__ next_task, uint32_t wait_polls)
 {
     extern __shared__ __align__(128) unsigned char smem_raw[];
@@ -385,6 +386,10 @@ __global__ void __launch_bounds__(kSnThreads)
                             id[e] = sc_rank_id(j, x + (nd & 1u), y + ((nd >> 1) & 1u), z + (nd >> 2), axis);
                             good = good && id[e] < nvert;
                         }
+                        if (t >= ntri) {
+                            atomicExch(status, 2);   // never with the count's offsets; nothing written out of range
+                            continue;
+                        }
                         uint32_t* o = j.connections + 3 * t;
                         o[0] = id[0]; o[1] = id[1]; o[2] = id[2];
                         if (!good) {
@@ -429,8 +434,8 @@ size_t sconnect_shared_bytes(int dtype)
 
 cudaError_t launch_sconnect(const Job& j, const StreamGroup* d_groups, const StreamIso* d_isos,
                             const uint16_t* unit_counts, const uint32_t* unit_offsets, const uint64_t* plane_base,
-                            uint64_t ntasks, uint64_t nvert, int* status, unsigned long long* next_task,
-                            const Launch& L)
+                            uint64_t ntasks, uint64_t nvert, uint64_t ntri, int* status,
+                            unsigned long long* next_task, const Launch& L)
 {
     if (ntasks == 0) return cudaSuccess;
     const int dt = j.vol.dtype;
@@ -446,7 +451,7 @@ cudaError_t launch_sconnect(const Job& j, const StreamGroup* d_groups, const Str
         const uint64_t nctas = need < resident ? need : resident;
         prof_begin(L, "sconnect");
         kern<<<(unsigned)nctas, kSnThreads, smem, L.stream>>>(j, d_groups, d_isos, unit_counts, unit_offsets,
-                                                                plane_base, ntasks, nvert, status, next_task,
+                                                                plane_base, ntasks, nvert, ntri, status, next_task,
                                                                 L.wait_polls[1]);
         prof_end(L);
     });
