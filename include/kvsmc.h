@@ -114,10 +114,11 @@ kvsmc_status kvsmc_set_stream(kvsmc_context* ctx, void* cuda_stream);
 kvsmc_status kvsmc_synchronize(kvsmc_context* ctx);
 /* Number of kernels this context has launched since creation. */
 uint64_t kvsmc_kernel_launches(const kvsmc_context* ctx);
-/* Kernel family: 0 (default) = streaming kernels for duplicated-mode requests
- * on 8/16-bit and float32 volumes, gather kernels for the rest; 1 = gather
- * kernels for everything.  Both give identical results.  No counterpart in
- * the reference (which has one CPU loop). */
+/* Kernel family: 0 (default) = streaming kernels for requests on 8/16-bit and
+ * float32 volumes (duplicated mode; in the shared-vertex modes the node and
+ * connection passes), gather kernels for the rest; 1 = gather kernels for
+ * everything.  Both give identical results.  No counterpart in the reference
+ * (which has one CPU loop). */
 kvsmc_status kvsmc_set_kernel_path(kvsmc_context* ctx, int32_t path);
 
 /* ------------------------------------------------------------------ volumes */
