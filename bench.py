@@ -98,6 +98,9 @@ WORKLOADS = {
     "sweep1024vn": dict(shape=(1024, 1024, 1024), kind="fbm", isos=[0.2 + 0.04 * k for k in range(16)], mode=2,
                         desc="1024^3 float32 fBm (as sweep1024), 16 isovalues 0.2..0.8 in one batched call, "
                              "VertexNormal (shared vertices + connections + per-vertex normals)"),
+    "sweep512vn": dict(shape=(512, 512, 512), kind="fbm", isos=[0.2 + 0.04 * k for k in range(16)], mode=2,
+                       desc="512^3 float32 fBm (as sweep1024), 16 isovalues, VertexNormal (the profiling case of "
+                            "sweep1024vn: same kernels, 512 MiB on the device)"),
     "blobs128": dict(shape=(128, 128, 128), kind="blobs", isos=[0.5],
                      desc="128^3 float32, 4 Gaussian blobs (sigma 8..24) + U[-0.01,0.01] noise, iso 0.5, "
                           "duplication=true, PolygonNormal"),

@@ -62,7 +62,6 @@ __global__ void __launch_bounds__(kSnThreads)
     const uint32_t nx = j.vol.nx, ny = j.vol.ny, nz = j.vol.nz;
     const uint64_t pitch = j.vol.pitch, slice = j.vol.slice;
     const T* vol = static_cast<const T*>(j.vol.data);
-    const unsigned lt = (1u << lane) - 1u;
     uint32_t ph = 0;   // per ring buffer: parity of its next completion
     for (;;) {
         unsigned long long tk = 0;
@@ -141,38 +140,69 @@ __global__ void __launch_bounds__(kSnThreads)
                 const uint32_t tot = __reduce_add_sync(FULL, cnt);
                 if (lane == 0) unit_counts[unit] = tot;
             } else {
-                uint64_t run = unit_offsets[unit];
+                const uint64_t base = unit_offsets[unit];
                 const uint64_t row = (uint64_t)z * ny + y;
-                const float fyf = __uint2float_rn(y), fzf = __uint2float_rn(z);
-#pragma unroll 1
+                // per 32-node word i: its crossing flags (three ballots) and its first
+                // vertex within the unit; items (node, axis) are numbered like the ids
+                uint32_t wx[8], wy[8], wz[8], wrun[8];
+                uint32_t total = 0;
+#pragma unroll
                 for (int i = 0; i < 8; ++i) {
-                    const uint32_t bx = (fx >> i) & 1u, by = (fy >> i) & 1u, bz = (fz >> i) & 1u;
-                    const uint32_t wx = __ballot_sync(FULL, bx);
-                    const uint32_t wy = __ballot_sync(FULL, by);
-                    const uint32_t wz = __ballot_sync(FULL, bz);
-                    const uint64_t word = (uint64_t)s * (kSnSeg / 32) + i;
-                    if (lane == 0 && word < j.words_per_row)
-                        j.rank[row * j.words_per_row + word] = make_uint4(wx, wy, wz, (uint32_t)run);
-                    const uint32_t flags = bx | (by << 1) | (bz << 2);
-                    if (flags) {
-                        uint64_t id = run + __popc(wx & lt) + __popc(wy & lt) + __popc(wz & lt);
-                        const uint32_t xl = lane + 32u * i;
-                        const float ax = __uint2float_rn((uint32_t)xoff + xl);
-                        const float v0 = (float)ra[xl];
-                        // one copy of the vertex code for the three axes (a loop, not unrolled)
-#pragma unroll 1
-                        for (int axis = 0; axis < 3; ++axis) {
-                            if (!((flags >> axis) & 1u)) continue;
-                            const float v1 = (float)(axis == 0 ? ra[xl + 1] : (axis == 1 ? rb[xl] : rz[xl]));
-                            const float bx = axis == 0 ? __fadd_rn(ax, 1.0f) : ax;
-                            const float by = axis == 1 ? __fadd_rn(fyf, 1.0f) : fyf;
-                            const float bz = axis == 2 ? __fadd_rn(fzf, 1.0f) : fzf;
-                            const float3 p = edge_vertex_fast(j.ip, f, v0, v1, ax, fyf, fzf, bx, by, bz, axis);
-                            float* o = j.coords + 3 * id++;
-                            o[0] = p.x; o[1] = p.y; o[2] = p.z;
-                        }
+                    wx[i] = __ballot_sync(FULL, (fx >> i) & 1u);
+                    wy[i] = __ballot_sync(FULL, (fy >> i) & 1u);
+                    wz[i] = __ballot_sync(FULL, (fz >> i) & 1u);
+                    wrun[i] = total;
+                    total += __popc(wx[i]) + __popc(wy[i]) + __popc(wz[i]);
+                }
+                // lane i < 8 writes word i's rank word
+                {
+                    uint32_t mx = 0, my = 0, mz = 0, mr = 0;
+#pragma unroll
+                    for (int i = 0; i < 8; ++i)
+                        if ((int)lane == i) { mx = wx[i]; my = wy[i]; mz = wz[i]; mr = wrun[i]; }
+                    const uint64_t word = (uint64_t)s * (kSnSeg / 32) + lane;
+                    if (lane < 8 && word < j.words_per_row)
+                        j.rank[row * j.words_per_row + word] = make_uint4(mx, my, mz, (uint32_t)(base + mr));
+                }
+                // the step's vertices spread over the lanes: item q has id base + q
+                const float fyf = __uint2float_rn(y), fzf = __uint2float_rn(z);
+                for (uint32_t q = lane; q < total; q += 32) {
+                    // its word: the last i with wrun[i] <= q (words without items share
+                    // the next word's start, so the last such i holds items)
+                    int wi = 0;
+                    uint32_t bx = wx[0], by = wy[0], bz = wz[0], r0 = wrun[0];
+#pragma unroll
+                    for (int i = 1; i < 8; ++i)
+                        if (wrun[i] <= q) { wi = i; bx = wx[i]; by = wy[i]; bz = wz[i]; r0 = wrun[i]; }
+                    const uint32_t r = q - r0;
+                    // its node: the last lane L whose flags before it (all axes) are at most r
+                    uint32_t lo = 0;
+#pragma unroll
+                    for (int k = 4; k >= 0; --k) {
+                        const uint32_t mid = lo + (1u << k);
+                        const uint32_t ltm = (1u << mid) - 1u;   // mid <= 31
+                        if ((uint32_t)(__popc(bx & ltm) + __popc(by & ltm) + __popc(bz & ltm)) <= r) lo = mid;
                     }
-                    run += __popc(wx) + __popc(wy) + __popc(wz);
+                    const uint32_t L = lo;
+                    const uint32_t ltl = (1u << L) - 1u;
+                    uint32_t k = r - (__popc(bx & ltl) + __popc(by & ltl) + __popc(bz & ltl));   // k-th flag of node L
+                    const uint32_t nf = ((bx >> L) & 1u) | (((by >> L) & 1u) << 1) | (((bz >> L) & 1u) << 2);
+                    int axis = 0;
+                    for (; axis < 3; ++axis)
+                        if ((nf >> axis) & 1u) {
+                            if (k == 0) break;
+                            --k;
+                        }
+                    const uint32_t xl = L + 32u * wi;
+                    const float ax = __uint2float_rn((uint32_t)xoff + xl);
+                    const float v0 = (float)ra[xl];
+                    const float v1 = (float)(axis == 0 ? ra[xl + 1] : (axis == 1 ? rb[xl] : rz[xl]));
+                    const float bxf = axis == 0 ? __fadd_rn(ax, 1.0f) : ax;
+                    const float byf = axis == 1 ? __fadd_rn(fyf, 1.0f) : fyf;
+                    const float bzf = axis == 2 ? __fadd_rn(fzf, 1.0f) : fzf;
+                    const float3 p = edge_vertex_fast(j.ip, f, v0, v1, ax, fyf, fzf, bxf, byf, bzf, axis);
+                    float* o = j.coords + 3 * (base + q);
+                    o[0] = p.x; o[1] = p.y; o[2] = p.z;
                 }
             }
             // plane z is consumed: refill its buffer with plane z + 3
