@@ -71,6 +71,10 @@ WORKLOADS = {
                    desc="binary STL serialisation on the GPU of the 16 duplicated-vertex meshes of the 512^3 "
                         "float32 fBm sweep (80 M triangles, 3.9 GB in, 4.0 GB of 50-byte records out per step); "
                         "e2e = kvsmc_write_stl of all 16 to /dev/null (GPU records, copy to pinned memory, fwrite)"),
+    "stlascii512": dict(shape=(512, 512, 512), kind="stlascii", isos=[0.2 + 0.04 * k for k in range(16)],
+                        desc="ASCII STL (the kvs::Stl default file type) of the 16 duplicated-vertex meshes of the "
+                             "512^3 float32 fBm sweep, text formatted on the GPU (exact %f), copied to pinned memory "
+                             "and written to /dev/null, kvsmc_write_stl_ascii per mesh"),
     "stl384": dict(shape=(384, 384, 384), kind="stl", isos=[0.2 + 0.04 * k for k in range(16)],
                    desc="binary STL serialisation of the 16 meshes of a 384^3 float32 fBm sweep (the profiling "
                         "case of stl512: same kernel, ~3.5 GB on the device, each launch larger than L2)"),
@@ -754,6 +758,109 @@ def run_cells_cpu(w, reference, min_seconds=10.0):
             else "oracle/cells.py (numpy restatement of kvs::MarchingTetrahedra)")
     return (done / t / 1e6, t, f"{calls} calls (isolevels 30/50/70/90 in turn) on the central 17-plane slab "
             f"({ncells / 1e6:.2f} M tetrahedra), {what}", kind)
+
+
+def run_stl_ascii(args, rank, world, local):
+    """kvsmc_write_stl_ascii of every mesh of a multi-isovalue sweep (text
+    formatted on the GPU, copied to pinned memory, written to /dev/null)."""
+    import torch
+
+    from kvs_gb300 import _abi
+    from kvs_gb300.export import write_stl_ascii_device
+
+    torch.cuda.set_device(local)
+    w = WORKLOADS[args.workload]
+    ctx = _abi.Context(local)
+    stream = torch.cuda.Stream()
+    ctx.set_stream(stream.cuda_stream)
+    field = make_field(dict(w, kind="fbm"), "cuda")
+    torch.cuda.synchronize()
+    vol = _abi.DeviceVolume.from_device(ctx, field.data_ptr(), np.float32, field.shape)
+    del field
+    torch.cuda.empty_cache()
+    n = len(w["isos"])
+    reqs = (_abi.Request * n)()
+    for i, iso in enumerate(w["isos"]):
+        reqs[i].volume = vol.handle
+        reqs[i].params = _abi.make_params(iso, _abi.MODE_DUP_POLYGON_NORMAL)
+    ctx.check(ctx.lib.kvsmc_count_batch(ctx.handle, reqs, n), "count")
+    meshes = []
+    for i in range(n):
+        s = reqs[i].sizes
+        c = torch.empty(max(1, s.ncoords), dtype=torch.float32, device="cuda")
+        nn = torch.empty(max(1, s.nnormals), dtype=torch.float32, device="cuda")
+        meshes.append((c, nn, s.ntriangles))
+        reqs[i].d_coords, reqs[i].coords_capacity = c.data_ptr(), s.ncoords
+        reqs[i].d_normals, reqs[i].normals_capacity = nn.data_ptr(), s.nnormals
+    ctx.check(ctx.lib.kvsmc_extract_batch(ctx.handle, reqs, n), "extract")
+    ntri = sum(m[2] for m in meshes)
+
+    def step():
+        for c, nn, t in meshes:
+            write_stl_ascii_device(ctx, "/dev/null", _abi.MODE_DUP_POLYGON_NORMAL, c.data_ptr(), nn.data_ptr(),
+                                   None, 3 * t, t)
+
+    for _ in range(args.warmup):
+        step()
+    torch.cuda.synchronize()
+    clocks = Clocks(local)
+    clocks.start()
+    ctx.profile_enable(True)
+    launches0 = ctx.kernel_launches
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        step()
+    torch.cuda.synchronize()
+    t = (time.perf_counter() - t0) / args.steps
+    t = barrier_max(t * 1e3, world) / 1e3
+    prof = ctx.profile_read()
+    ctx.profile_enable(False)
+    launches = ctx.kernel_launches - launches0
+    clk = clocks.stop()
+    # text bytes of one step: the file sizes the writer produced
+    import tempfile
+    text = 0
+    with tempfile.NamedTemporaryFile(suffix=".stl") as f:
+        write_stl_ascii_device(ctx, f.name, 0, meshes[0][0].data_ptr(), meshes[0][1].data_ptr(), None,
+                               3 * meshes[0][2], meshes[0][2])
+        per_tri = os.path.getsize(f.name) / max(1, meshes[0][2])
+    text = per_tri * ntri
+    hbm, peak_kind = peaks()
+    w_launches, w_ms = prof.get("stl_ascii_write", (0, 0.0))
+    l_launches, l_ms = prof.get("stl_ascii_len", (0, 0.0))
+    k_ms = (w_ms + l_ms) / args.steps
+    algo = 48 * ntri + text               # coords + normals read once, the text written once
+    achieved = algo / (k_ms * 1e-3) / 1e9 if k_ms else 0.0
+    return {
+        "metric": "Mtris/s", "value": round(ntri * world / t / 1e6, 1), "unit": "Mtris/s",
+        "n_gpus": world, "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(t * 1e3, 2),
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32 -> text",
+        "data": "synthetic (seeded fBm meshes extracted on the device)",
+        "config": {"workload": w["desc"], "meshes": n, "triangles": int(ntri),
+                   "text_bytes_per_step": int(text), "timing": "host clock around the whole calls"},
+        "gpu_format": {"ms_per_step": round(k_ms, 3), "mtris_per_s": round(ntri / (k_ms * 1e-3) / 1e6, 1)
+                       if k_ms else None, "note": "length + write kernels only (CUDA events)"},
+        "roofline": {"kernel": "stl_ascii_len + stl_ascii_write", "bound": "hbm", "achieved": round(achieved, 1),
+                     "peak": hbm, "peak_kind": peak_kind, "unit": "GB/s", "frac": round(achieved / hbm, 4),
+                     "algorithmic_bytes_per_step": int(algo), "traffic": None},
+        "kernels": {k: {"launches": v[0], "ms": round(v[1], 3)} for k, v in prof.items()},
+        "e2e": {"value": round(ntri * world / t / 1e6, 1), "unit": "Mtris/s", "h2d_bytes_per_step": 0,
+                "d2h_bytes_per_step": int(text), "api": "kvsmc_write_stl_ascii x%d (to /dev/null)" % n},
+        "gpu_launches": int(launches), "clocks": clk,
+        "_sample_mesh": (meshes[0][0][:9 * min(meshes[0][2], 20000)].cpu().numpy(),
+                         meshes[0][1][:3 * min(meshes[0][2], 20000)].cpu().numpy()),
+    }
+
+
+def run_stl_ascii_cpu(mesh):
+    """The ASCII STL restatement (oracle/export.py, the C library's %f through
+    Python's formatting) on one host core, on a 20 k-triangle sample."""
+    from oracle import export as E
+    coords, normals = mesh
+    t0 = time.perf_counter()
+    E.stl_ascii(coords, normals, np.zeros(0, np.uint32), E.POLYGON_NORMAL)
+    t = time.perf_counter() - t0
+    return normals.size // 3 / t / 1e6, t, normals.size // 3
 
 
 def run_stl_cpu(mesh):
@@ -1642,6 +1749,14 @@ def main():
                                     "sample": f"{nt} triangles of the first mesh, oracle/export.py (numpy "
                                               f"restatement of PolygonExporter<Stl> + Stl::write_binary), "
                                               f"{t:.1f} s on 1 host core"}
+    elif WORKLOADS[args.workload]["kind"] == "stlascii":
+        line = run_stl_ascii(args, rank, world, local)
+        mesh = line.pop("_sample_mesh")
+        if rank == 0 and world == 1 and not args.no_cpu:
+            v, t, nt = run_stl_ascii_cpu(mesh)
+            line["cpu_baseline"] = {"value": round(v, 3), "unit": "Mtris/s", "cores": 1, "kind": "port",
+                                    "sample": f"{nt} triangles of the first mesh, oracle/export.py stl_ascii "
+                                              f"(restatement of Stl::write_ascii), {t:.1f} s on 1 host core"}
     elif WORKLOADS[args.workload]["kind"] == "serve":
         line = run_serve(args, rank, world, local)
     elif WORKLOADS[args.workload]["kind"] == "batch":

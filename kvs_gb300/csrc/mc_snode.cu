@@ -40,10 +40,15 @@ constexpr int kSnWarps = kSnThreads / 32;
 constexpr uint32_t kSnSeg = 256;   // nodes per segment
 constexpr unsigned FULL = 0xffffffffu;
 
+// resident CTAs per SM the node emit pass is compiled for (registers per thread)
+#ifndef KVSMC_SNODE_EMIT_CTAS
+#define KVSMC_SNODE_EMIT_CTAS 1
+#endif
+
 __host__ __device__ __forceinline__ size_t sn_align(size_t v) { return (v + 127) / 128 * 128; }
 
 template <typename T, bool EMIT>
-__global__ void __launch_bounds__(kSnThreads)
+__global__ void __launch_bounds__(kSnThreads, EMIT ? KVSMC_SNODE_EMIT_CTAS : 1)
     k_snode(Job j, FastIso f, uint32_t wprn, uint32_t zchunk, uint64_t ntasks, uint32_t row_elems,
             uint32_t copy_bytes, uint32_t* __restrict__ unit_counts, const uint64_t* __restrict__ unit_offsets,
             int* __restrict__ status, unsigned long long* __restrict__ next_task, uint32_t wait_polls)
