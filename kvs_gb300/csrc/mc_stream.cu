@@ -31,6 +31,8 @@
 //     of a shared-memory vertex table and writes the pair's triangles, cells
 //     in linear order, table order inside a cell, each isolevel into its own
 //     arrays.
+#include <cstddef>
+
 #include <cuda_runtime.h>
 
 #include "mc_internal.h"
@@ -40,12 +42,25 @@
 #ifndef KVSMC_VERTS_PER_LANE
 #define KVSMC_VERTS_PER_LANE 1
 #endif
+// launch shape of the emit kernel: warps per CTA, resident CTAs per SM it is
+// compiled for (registers per thread), vertex items per round (shared memory)
+#ifndef KVSMC_EMIT_WARPS
+#define KVSMC_EMIT_WARPS 8
+#endif
+#ifndef KVSMC_EMIT_CTAS
+#define KVSMC_EMIT_CTAS 2
+#endif
+#ifndef KVSMC_EMIT_MAX_VERTS
+#define KVSMC_EMIT_MAX_VERTS 192
+#endif
 
 namespace kvsmc {
 
 namespace {
 
 constexpr int kWarps = kStreamThreads / 32;
+constexpr int kEmitThreads = 32 * KVSMC_EMIT_WARPS;
+constexpr int kEmitWarps = KVSMC_EMIT_WARPS;
 constexpr int kLaneCells = 8;
 constexpr int kSegCells = 32 * kLaneCells;
 constexpr int kPairCap = 128;   // pair buffer entries per warp
@@ -103,7 +118,8 @@ template <> __device__ __forceinline__ void load8<int8_t>(const int8_t* row, uin
 
 constexpr int kLut = kStreamBuckets + 1;   // bucket indices 0 .. kStreamBuckets
 constexpr uint32_t kMultiThr = 1u << 31;   // LUT flag: two or more thresholds lie in this bucket
-constexpr int kMaxVerts = 256;             // vertex items of one round (rounds end before it is exceeded)
+constexpr int kMaxVerts = KVSMC_EMIT_MAX_VERTS;   // vertex items of one round (rounds end before it is exceeded)
+static_assert(kMaxVerts >= 12 && kMaxVerts <= 256, "a round holds one pair's 12 edges; item maps are 8-bit");
 constexpr int kMaxTris = 32 * 5;           // triangle items of one round (5 per pair at most)
 constexpr int kVertsPerLane = KVSMC_VERTS_PER_LANE;   // vertex items per lane per pass
 
@@ -111,12 +127,23 @@ constexpr int kVertsPerLane = KVSMC_VERTS_PER_LANE;   // vertex items per lane p
 // reference's case number: the code -> case permutation is applied when the
 // tables are filled).
 struct Tables {
-    uint64_t tri_packed[256];   // edges per triangle, emission order, 4 bits each
+    // per triangle in emission order, its three corners' positions in the
+    // pair's vertex list (the rank of each corner's edge among the used
+    // edges), 4 bits each, 12 bits per triangle
+    uint64_t tri_slots[256];
     uint64_t edge_list[256];    // the used edges in increasing order, 4 bits each
+    // per edge: corner A's offsets (dx, dy, dz) and corner B's offset along
+    // the edge's axis, as floats (0 or 1)
+    float4 edge_geo[12];
+    // per ring phase p (plane z in ring buffer p) and edge: element offsets
+    // from the warp's ring of corner A (bits 0-13) and corner B (bits 14-27)
+    // for the cell at row 0, x 0 of the segment; the edge's axis in bits 28-29
+    uint32_t edge_off[3][12];
     uint16_t edge_mask[256];
     uint8_t ntri[256];
-    uint8_t edge_packed[16];
 };
+// ring offsets: 3 planes x at most 3 node rows x at most kSegCells + 16 elements
+static_assert(3 * 3 * (kSegCells + 16) < (1 << 14), "edge_off packs ring offsets into 14 bits");
 
 // Per-warp state.
 struct WarpState {
@@ -134,7 +161,7 @@ struct WarpState {
 // (one entry per (pair, used edge)) and the item -> pair maps.
 // An isolevel's constants as the emit loops read them (copied from the
 // group's StreamIso entries when a warp starts on a group).
-struct IsoConst {
+struct __align__(16) IsoConst {
     FastIso f;
     float mc[3], sc[3];   // min_coord, scale
     float* coords;
@@ -147,10 +174,87 @@ struct WarpEmit {
     uint32_t pairs_round[32];   // this round's pair entry and vertex base per lane
     uint32_t vpre_round[32];
     uint32_t pairs[kPairCap];
-    float px[kMaxVerts], py[kMaxVerts], pz[kMaxVerts];
+    float4 pv[kMaxVerts];   // vertex pool: x, y, z, unused (one 16-byte access per vertex)
     uint8_t item_v[kMaxVerts];
     uint8_t item_t[kMaxTris];
 };
+
+__device__ __forceinline__ void store_vertex(WarpEmit* WE, uint32_t j, float3 v)
+{
+    WE->pv[j] = make_float4(v.x, v.y, v.z, 0.0f);
+}
+
+__device__ __forceinline__ float3 load_vertex(const WarpEmit* WE, uint32_t j)
+{
+    const float4 v = WE->pv[j];
+    return make_float3(v.x, v.y, v.z);
+}
+
+// An isolevel's interpolation constants in registers, read from its IsoConst
+// with four 16-byte loads.
+struct IsoRegs {
+    FastIso f;
+    float mc[3], sc[3];
+};
+
+static_assert(offsetof(IsoConst, f) == 0 && sizeof(FastIso) == 32 && offsetof(IsoConst, mc) == 32 &&
+                  offsetof(IsoConst, sc) == 44 && sizeof(IsoConst) % 16 == 0,
+              "load_iso reads IsoConst as four float4");
+
+__device__ __forceinline__ IsoRegs load_iso(const IsoConst& c)
+{
+    const float4* p = reinterpret_cast<const float4*>(&c);
+    const float4 a = p[0], b = p[1], m = p[2], n = p[3];
+    IsoRegs r;
+    r.f.ih = a.x;
+    r.f.il = a.y;
+    r.f.iso_err = a.z;
+    r.f.f_thr = a.w;
+    r.f.vmin_f = b.x;
+    r.f.vmax_f = b.y;
+    r.f.fast_ok = __float_as_int(b.z);
+    r.f.pad = 0;
+    r.mc[0] = m.x;
+    r.mc[1] = m.y;
+    r.mc[2] = m.z;
+    r.sc[0] = m.w;
+    r.sc[1] = n.x;
+    r.sc[2] = n.y;
+    return r;
+}
+
+// One vertex item: where its edge's two corner values sit in the warp's ring,
+// the edge's axis, corner A's coordinates and corner B's coordinate along the
+// axis.  qe = the pair entry (warp cell | isolevel << 8 | code << 16), r = the
+// edge's rank among the code's used edges, phase = ring buffer of plane z.
+struct EdgeItem {
+    uint32_t oa, ob;
+    int axis;
+    float ax, ay, az, b;
+};
+
+template <int SEG_SHIFT>
+__device__ __forceinline__ EdgeItem edge_item(const Tables& TB, uint32_t qe, uint32_t r, uint32_t phase,
+                                              uint32_t row_elems, uint64_t xoff, float fy, float fz)
+{
+    const uint32_t qh = (qe & 0xffu) >> SEG_SHIFT, cell = qe & ((1u << SEG_SHIFT) - 1u);
+    const uint32_t e = (uint32_t)(TB.edge_list[qe >> 16] >> (4 * (r & 15u))) & 15u;
+    const uint32_t ow = TB.edge_off[phase][e];
+    const float4 g = TB.edge_geo[e];
+    const uint32_t base = qh * row_elems + cell;
+    EdgeItem it;
+    it.oa = (ow & 0x3fffu) + base;
+    it.ob = ((ow >> 14) & 0x3fffu) + base;
+    it.axis = (int)(ow >> 28);
+    // corner coordinates: integers below 2^24, exact as floats
+    const float fx = __uint2float_rn((uint32_t)xoff + cell);
+    const float fyh = __fadd_rn(fy, qh ? 1.0f : 0.0f);
+    it.ax = __fadd_rn(fx, g.x);
+    it.ay = __fadd_rn(fyh, g.y);
+    it.az = __fadd_rn(fz, g.z);
+    it.b = __fadd_rn(it.axis == 0 ? fx : (it.axis == 1 ? fyh : fz), g.w);
+    return it;
+}
 
 __host__ __device__ __forceinline__ size_t align128(size_t v) { return (v + 127) / 128 * 128; }
 
@@ -280,7 +384,7 @@ __device__ __forceinline__ int find_group(const StreamGroup* groups, int ngroups
 // whose other warps still run.  Tasks come out in increasing order; the
 // group's isolevel tables are rebuilt when a warp crosses a group boundary.
 template <typename T, bool EMIT, int R>
-__global__ void __launch_bounds__(kStreamThreads, EMIT ? 2 : 3)
+__global__ void __launch_bounds__(EMIT ? kEmitThreads : kStreamThreads, EMIT ? KVSMC_EMIT_CTAS : 3)
     k_stream(const StreamGroup* __restrict__ groups, int ngroups, uint64_t ntasks, const StreamIso* __restrict__ isos,
              uint16_t* __restrict__ unit_counts, const uint32_t* __restrict__ unit_offsets,
              const uint64_t* __restrict__ plane_base, int* __restrict__ status,
@@ -292,28 +396,46 @@ __global__ void __launch_bounds__(kStreamThreads, EMIT ? 2 : 3)
     extern __shared__ __align__(128) unsigned char smem_raw[];
     const unsigned tid = threadIdx.x, lane = tid & 31u, warp = tid >> 5;
     Tables& TB = *reinterpret_cast<Tables*>(smem_raw);
+    // per-warp shared memory: state, then (emit) buffers, then the row ring
+    // (the same layout as stream_warp_smem_bytes on the host; one value type
+    // and one rows-per-task per launch, so one layout for all groups)
+    const uint32_t row_elems = groups[0].seg_elems;      // staged elements per row
+    const uint32_t plane_elems = (R + 1) * row_elems;
     for (unsigned code = tid; code < 256; code += blockDim.x) {
         const uint32_t cs = code_to_case(code);
         TB.ntri[code] = c_ntri[cs];
         const uint32_t em = c_edge_mask[cs];
         TB.edge_mask[code] = (uint16_t)em;
         if (EMIT) {
-            TB.tri_packed[code] = c_tri_packed[cs];
             uint64_t list = 0;
             int n = 0;
             for (int e = 0; e < 12; ++e)
                 if ((em >> e) & 1u) list |= (uint64_t)e << (4 * n++);
             TB.edge_list[code] = list;
+            const uint64_t tp = c_tri_packed[cs];
+            uint64_t slots = 0;
+            for (int c = 0; c < 3 * (int)c_ntri[cs]; ++c) {
+                const uint32_t e = (uint32_t)(tp >> (4 * c)) & 15u;
+                slots |= (uint64_t)__popc(em & ((1u << e) - 1u)) << (4 * c);
+            }
+            TB.tri_slots[code] = slots;
         }
-        if (code < 12) TB.edge_packed[code] = c_edge_packed[code];
+        if (EMIT && code < 36) {
+            const uint32_t e = code % 12u, ph = code / 12u;
+            const uint32_t ep = c_edge_packed[e], c0 = ep & 7u, c1 = ep >> 3, d = c0 ^ c1;
+            const uint32_t axis = d == 1u ? 0u : (d == 2u ? 1u : 2u);
+            auto corner = [&](uint32_t c) -> uint32_t {
+                const uint32_t buf = (c >> 2) ? (ph + 1u) % 3u : ph;   // plane z + 1 or z
+                return buf * plane_elems + ((c >> 1) & 1u) * row_elems + (c & 1u);
+            };
+            TB.edge_off[ph][e] = corner(c0) | (corner(c1) << 14) | (axis << 28);
+            if (ph == 0)
+                TB.edge_geo[e] = make_float4((c0 & 1u) ? 1.0f : 0.0f, (c0 & 2u) ? 1.0f : 0.0f,
+                                             (c0 & 4u) ? 1.0f : 0.0f, (c1 & d) ? 1.0f : 0.0f);
+        }
     }
     __syncthreads();   // the only CTA-wide barrier: tables are read-only from here on
 
-    // per-warp shared memory: state, then (emit) buffers, then the row ring
-    // (the same layout as stream_warp_smem_bytes on the host; one value type
-    // and one rows-per-task per launch, so one layout for all groups)
-    const uint32_t row_elems = groups[0].seg_elems;      // staged elements per row
-    const uint32_t plane_elems = (R + 1) * row_elems;
     const size_t wstride = align128(sizeof(WarpState)) + (EMIT ? align128(sizeof(WarpEmit)) : 0) +
                            align128((size_t)3 * plane_elems * sizeof(T));
     unsigned char* wbase = smem_raw + align128(sizeof(Tables)) + (size_t)warp * wstride;
@@ -478,6 +600,7 @@ __global__ void __launch_bounds__(kStreamThreads, EMIT ? 2 : 3)
         }
         const T* pa = ring + (size_t)(s % 3u) * plane_elems;         // plane z
         const T* pb = ring + (size_t)((s + 1) % 3u) * plane_elems;   // plane z + 1
+        const uint32_t phase = s % 3u;
         const T* ra0 = pa + half * row_elems;
         const T* ra1 = ra0 + row_elems;
         const T* rb0 = pb + half * row_elems;
@@ -659,31 +782,14 @@ __global__ void __launch_bounds__(kStreamThreads, EMIT ? 2 : 3)
                                 const uint32_t q = hv ? WE->item_v[j] : 0u;
                                 const uint32_t qe = __shfl_sync(FULL, pe, q);
                                 const uint32_t qv = __shfl_sync(FULL, vpre, q);
-                                const uint32_t qh = (qe & 0xffu) >> SEG_SHIFT, cell = qe & (SEG - 1);
-                                const uint32_t qk = (qe >> 8) & 0xffu, qc = qe >> 16;
-                                const uint32_t e = (uint32_t)(TB.edge_list[qc] >> (4 * ((j - qv) & 15u))) & 15u;
-                                const unsigned ep = TB.edge_packed[e];
-                                const unsigned c0 = ep & 7u, c1 = ep >> 3;
-                                const T* sa = ((c0 >> 2) ? pb : pa) + (qh + ((c0 >> 1) & 1u)) * row_elems + cell + (c0 & 1u);
-                                const T* sb = ((c1 >> 2) ? pb : pa) + (qh + ((c1 >> 1) & 1u)) * row_elems + cell + (c1 & 1u);
-                                const unsigned d = c0 ^ c1;
-                                const int axis = d == 1u ? 0 : (d == 2u ? 1 : 2);
-                                // corner coordinates: integers below 2^24, exact as floats
-                                const float fx = __uint2float_rn((uint32_t)xoff + cell);
-                                const float fyh = __fadd_rn(fy, qh ? 1.0f : 0.0f);
-                                const float ax = __fadd_rn(fx, (c0 & 1u) ? 1.0f : 0.0f);
-                                const float ay = __fadd_rn(fyh, (c0 & 2u) ? 1.0f : 0.0f);
-                                const float az = __fadd_rn(fz, (c0 & 4u) ? 1.0f : 0.0f);
-                                const float bcoord = __fadd_rn(axis == 0 ? fx : (axis == 1 ? fyh : fz),
-                                                               (c1 & d) ? 1.0f : 0.0f);
-                                const IsoConst& IC = WE->ic[qk];
+                                const EdgeItem it = edge_item<SEG_SHIFT>(TB, qe, j - qv, phase, row_elems, xoff, fy, fz);
+                                const IsoRegs I = load_iso(WE->ic[(qe >> 8) & 0xffu]);
                                 float3 v;
-                                const bool ok = edge_vertex_axis_try(IC.f, IC.mc, IC.sc, (float)*sa, (float)*sb, ax,
-                                                                     ay, az, axis, bcoord, v);
+                                const bool ok = edge_vertex_axis_try(I.f, I.mc, I.sc, (float)ring[it.oa],
+                                                                     (float)ring[it.ob], it.ax, it.ay, it.az, it.axis,
+                                                                     it.b, v);
                                 if (hv) {
-                                    WE->px[j] = v.x;
-                                    WE->py[j] = v.y;
-                                    WE->pz[j] = v.z;
+                                    store_vertex(WE, j, v);
                                     if (!ok) fail |= 1u << u;
                                 }
                             }
@@ -693,28 +799,13 @@ __global__ void __launch_bounds__(kStreamThreads, EMIT ? 2 : 3)
                                     const uint32_t j = j0 + 32 * u + lane;
                                     const uint32_t q = WE->item_v[j];
                                     const uint32_t qe = WE->pairs_round[q], qv = WE->vpre_round[q];
-                                    const uint32_t qh = (qe & 0xffu) >> SEG_SHIFT, cell = qe & (SEG - 1);
-                                    const uint32_t qk = (qe >> 8) & 0xffu, qc = qe >> 16;
-                                    const uint32_t e = (uint32_t)(TB.edge_list[qc] >> (4 * (j - qv))) & 15u;
-                                    const unsigned ep = TB.edge_packed[e];
-                                    const unsigned c0 = ep & 7u, c1 = ep >> 3;
-                                    const T* sa = ((c0 >> 2) ? pb : pa) + (qh + ((c0 >> 1) & 1u)) * row_elems + cell + (c0 & 1u);
-                                    const T* sb = ((c1 >> 2) ? pb : pa) + (qh + ((c1 >> 1) & 1u)) * row_elems + cell + (c1 & 1u);
-                                    const unsigned d = c0 ^ c1;
-                                    const int axis = d == 1u ? 0 : (d == 2u ? 1 : 2);
-                                    const float fx = __uint2float_rn((uint32_t)xoff + cell);
-                                    const float fyh = __fadd_rn(fy, qh ? 1.0f : 0.0f);
-                                    const float ax = __fadd_rn(fx, (c0 & 1u) ? 1.0f : 0.0f);
-                                    const float ay = __fadd_rn(fyh, (c0 & 2u) ? 1.0f : 0.0f);
-                                    const float az = __fadd_rn(fz, (c0 & 4u) ? 1.0f : 0.0f);
-                                    const float bcoord = __fadd_rn(axis == 0 ? fx : (axis == 1 ? fyh : fz),
-                                                                   (c1 & d) ? 1.0f : 0.0f);
-                                    const IsoConst& IC = WE->ic[qk];
-                                    const float3 v = edge_vertex_axis(IC.f, IC.mc, IC.sc, isos[iso_begin + qk].ip,
-                                                                      (float)*sa, (float)*sb, ax, ay, az, axis, bcoord);
-                                    WE->px[j] = v.x;
-                                    WE->py[j] = v.y;
-                                    WE->pz[j] = v.z;
+                                    const uint32_t qk = (qe >> 8) & 0xffu;
+                                    const EdgeItem it = edge_item<SEG_SHIFT>(TB, qe, j - qv, phase, row_elems, xoff, fy, fz);
+                                    const IsoRegs I = load_iso(WE->ic[qk]);
+                                    const float3 v = edge_vertex_axis(I.f, I.mc, I.sc, isos[iso_begin + qk].ip,
+                                                                      (float)ring[it.oa], (float)ring[it.ob], it.ax,
+                                                                      it.ay, it.az, it.axis, it.b);
+                                    store_vertex(WE, j, v);
                                 }
                             }
                         }
@@ -731,14 +822,11 @@ __global__ void __launch_bounds__(kStreamThreads, EMIT ? 2 : 3)
                             if (ht) {
                                 const uint32_t qk = (qe >> 8) & 0xffu, qc = qe >> 16;
                                 const uint32_t t = j - qt;
-                                const uint32_t emq = TB.edge_mask[qc];
-                                const uint32_t pk = (uint32_t)(TB.tri_packed[qc] >> (12 * t));
-                                const uint32_t s0 = qv + __popc(emq & ((1u << (pk & 15u)) - 1u));
-                                const uint32_t s1 = qv + __popc(emq & ((1u << ((pk >> 4) & 15u)) - 1u));
-                                const uint32_t s2 = qv + __popc(emq & ((1u << ((pk >> 8) & 15u)) - 1u));
-                                const float3 A = make_float3(WE->px[s0], WE->py[s0], WE->pz[s0]);
-                                const float3 B = make_float3(WE->px[s1], WE->py[s1], WE->pz[s1]);
-                                const float3 C = make_float3(WE->px[s2], WE->py[s2], WE->pz[s2]);
+                                const uint32_t sl = (uint32_t)(TB.tri_slots[qc] >> (12 * t));
+                                const uint32_t s0 = qv + (sl & 15u), s1 = qv + ((sl >> 4) & 15u), s2 = qv + ((sl >> 8) & 15u);
+                                const float3 A = load_vertex(WE, s0);
+                                const float3 B = load_vertex(WE, s1);
+                                const float3 C = load_vertex(WE, s2);
                                 const float3 n = tri_normal(A, B, C);
                                 const IsoConst& IC = WE->ic[qk];
                                 float* const pc = IC.coords;
@@ -933,7 +1021,7 @@ size_t stream_warp_smem_offset() { return align128(sizeof(Tables)); }
 
 size_t stream_shared_bytes(int dtype, bool emit, int rows)
 {
-    return stream_warp_smem_offset() + (size_t)kWarps * stream_warp_smem_bytes(dtype, emit, rows);
+    return stream_warp_smem_offset() + (size_t)(emit ? kEmitWarps : kWarps) * stream_warp_smem_bytes(dtype, emit, rows);
 }
 
 uint64_t brick_count(const VolumeView& v)
@@ -962,7 +1050,8 @@ cudaError_t launch_stream(bool emit, int dtype, int rows, const StreamGroup* d_g
     if (ntasks <= task0) return cudaSuccess;
     if (rows != 1 && rows != 2) return cudaErrorInvalidValue;
     const size_t smem = stream_shared_bytes(dtype, emit, rows);
-    const uint64_t need = (ntasks - task0 + kWarps - 1) / kWarps;
+    const int threads = emit ? kEmitThreads : kStreamThreads;
+    const uint64_t need = (ntasks - task0 + threads / 32 - 1) / (threads / 32);
     KVSMC_STREAM_SWITCH(dtype, {
         auto kern = emit ? (rows == 1 ? k_stream<T, true, 1> : k_stream<T, true, 2>)
                          : (rows == 1 ? k_stream<T, false, 1> : k_stream<T, false, 2>);
@@ -971,16 +1060,16 @@ cudaError_t launch_stream(bool emit, int dtype, int rows, const StreamGroup* d_g
             e = cudaFuncSetAttribute(kern, cudaFuncAttributePreferredSharedMemoryCarveout,
                                      (int)cudaSharedmemCarveoutMaxShared);
         int per_sm = 0;
-        if (e == cudaSuccess) e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, kStreamThreads, smem);
+        if (e == cudaSuccess) e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, threads, smem);
         if (e != cudaSuccess) return e;
         if (ctas_per_sm > 0 && ctas_per_sm < per_sm) per_sm = ctas_per_sm;
         // persistent: as many CTAs as are resident at once (never more than the tasks need)
         const uint64_t resident = (uint64_t)(per_sm > 0 ? per_sm : 1) * (uint64_t)L.num_sms;
         const uint64_t nctas = need < resident ? need : resident;
         prof_begin(L, emit ? "stream_emit" : "stream_count");
-        kern<<<(unsigned)nctas, kStreamThreads, smem, L.stream>>>(d_groups, ngroups, ntasks, d_isos, d_unit_counts,
-                                                                   d_unit_offsets, d_plane_base, d_status,
-                                                                   d_next_task, L.wait_polls[emit ? 1 : 0], task0);
+        kern<<<(unsigned)nctas, threads, smem, L.stream>>>(d_groups, ngroups, ntasks, d_isos, d_unit_counts,
+                                                           d_unit_offsets, d_plane_base, d_status, d_next_task,
+                                                           L.wait_polls[emit ? 1 : 0], task0);
         prof_end(L);
     });
     *L.counter += 1;
