@@ -8,6 +8,7 @@
 #include <cstring>
 #include <memory>
 #include <string>
+#include <unordered_map>
 #include <vector>
 
 #include "batch.h"
@@ -231,10 +232,17 @@ struct Plan {
     int* d_status = nullptr;
     unsigned long long* d_next = nullptr;
     // triangles of a shared-vertex request on the streaming count and the
-    // streaming connection pass (one group, one isolevel, one row per task)
+    // streaming connection pass (one row per task): the request is isolevel
+    // sb_iso of group sb_group of the count `sb`, either its own (`batch`) or
+    // one shared by the batch's requests on the same volume, counted before
+    // (set by the caller before gather_count; sb_tasks = the group's tasks)
     Item* item = nullptr;
     bool sconn = false;
     std::unique_ptr<StreamBatch> batch;
+    StreamBatch* sb = nullptr;
+    int sb_group = 0;
+    uint32_t sb_iso = 0;
+    uint64_t sb_tasks = 0;
 };
 
 uint32_t rows_for(uint32_t width, uint32_t limit)
@@ -289,14 +297,24 @@ kvsmc_status gather_count(kvsmc_context* ctx, Plan& pl)
         j.node_tiles = steps;   // node units, for the counts and their scan
         // the triangles too: the streaming count and the streaming connection
         // pass when the volume takes the streaming layout with one row per task
-        if (stream_volume_eligible(ctx, *pl.item)) {
+        if (pl.sb) {
+            pl.sconn = true;
+            j.cell_tiles = 0;
+        } else if (stream_volume_eligible(ctx, *pl.item)) {
             pl.batch.reset(new StreamBatch());
             pl.batch->ctx = ctx;
             pl.batch->items = {pl.item};
             pl.batch->plan_tables();
             pl.sconn = pl.batch->groups.size() == 1 && pl.batch->launches.size() == 1 && pl.batch->groups[0].rows == 1;
-            if (pl.sconn) j.cell_tiles = 0;
-            else pl.batch.reset();
+            if (pl.sconn) {
+                j.cell_tiles = 0;
+                pl.sb = pl.batch.get();
+                pl.sb_group = 0;
+                pl.sb_iso = 0;
+                pl.sb_tasks = pl.batch->launches[0].ntasks;
+            } else {
+                pl.batch.reset();
+            }
         }
     }
     const size_t ct = j.cell_tiles, nt = j.node_tiles;
@@ -304,7 +322,7 @@ kvsmc_status gather_count(kvsmc_context* ctx, Plan& pl)
     const size_t own = 10 * 256 + align_up(ct * 4, 256) + align_up(ct * 8, 256) + align_up(nt * 4, 256) +
                        align_up(nt * 8, 256) + align_up(rank_words * 16, 256) +
                        align_up(scan_scratch_bytes(ct), 256) + align_up(scan_scratch_bytes(nt), 256);
-    const size_t need = own + (pl.sconn ? align_up(pl.batch->scratch_bytes(), 256) : 0);
+    const size_t need = own + (pl.sconn && pl.batch ? align_up(pl.batch->scratch_bytes(), 256) : 0);
     kvsmc_status st = ensure_scratch(ctx, need);
     if (st) return st;
     Carve cv{static_cast<char*>(ctx->scratch)};
@@ -320,7 +338,7 @@ kvsmc_status gather_count(kvsmc_context* ctx, Plan& pl)
     pl.d_next = cv.take<unsigned long long>(256);
     const kvsmc::Launch L = launch_of(ctx);
     KVSMC_CUDA(ctx, cudaMemsetAsync(d_totals, 0, 3 * sizeof(uint64_t), ctx->stream));
-    if (pl.sconn) {
+    if (pl.sconn && pl.batch) {
         // unit counts, unit scan, plane scan: the streaming count of one request
         pl.batch->carve(static_cast<char*>(ctx->scratch) + own);
         kvsmc_status bst = pl.batch->upload_tables();
@@ -427,10 +445,10 @@ kvsmc_status gather_emit(kvsmc_context* ctx, Plan& pl, float* coords, float* nor
         KVSMC_CUDA(ctx, launch_node_emit(j, L));
     }
     if (pl.ntri && pl.sconn) {
-        StreamBatch& b = *pl.batch;
-        KVSMC_CUDA(ctx, kvsmc::launch_sconnect(j, b.d_groups, b.d_isos, b.d_unit_counts, b.d_unit_offsets,
-                                               b.d_plane_base, b.launches[0].ntasks, pl.nvert, pl.ntri,
-                                               pl.d_status, pl.d_next + 2, L));
+        StreamBatch& b = *pl.sb;
+        KVSMC_CUDA(ctx, kvsmc::launch_sconnect(j, b.d_groups + pl.sb_group, b.d_isos, b.d_unit_counts,
+                                               b.d_unit_offsets, b.d_plane_base, pl.sb_iso, pl.sb_tasks, pl.nvert,
+                                               pl.ntri, pl.d_status, pl.d_next + 2, L));
         if ((st = check_status("shared-vertex connections"))) return st;
     } else if (pl.ntri) {
         KVSMC_CUDA(ctx, launch_connect(j, L));
@@ -441,6 +459,76 @@ kvsmc_status gather_emit(kvsmc_context* ctx, Plan& pl, float* coords, float* nor
         // vertices without any triangle (a volume one node thick): zero normals
         // (calculate_normals_on_vertex adds nothing to its zeroed array)
         KVSMC_CUDA(ctx, cudaMemsetAsync(j.normals, 0, 12 * pl.nvert, ctx->stream));
+    }
+    return KVSMC_OK;
+}
+
+// The streaming triangle count of a batch's shared-vertex requests in one
+// pass: requests on the same volume share one read of it (up to 16
+// isolevels per group), and each request's connection pass takes its
+// isolevel's unit offsets from it.  Requests whose group does not take one
+// row per task, and a batch with a single such request, keep their own count.
+struct SharedCount {
+    std::unique_ptr<StreamBatch> sb;
+    std::vector<Item*> cand;   // the requests counted here
+    struct Ref {
+        int group;
+        uint32_t iso;
+        uint64_t tasks;
+    };
+    std::unordered_map<const Item*, Ref> ref;
+
+    void attach(const Item* it, Plan& pl) const
+    {
+        const auto r = ref.find(it);
+        if (r == ref.end()) return;
+        pl.sb = sb.get();
+        pl.sb_group = r->second.group;
+        pl.sb_iso = r->second.iso;
+        pl.sb_tasks = r->second.tasks;
+    }
+};
+
+kvsmc_status shared_count(kvsmc_context* ctx, const std::vector<Item*>& items, SharedCount& sc)
+{
+    for (Item* it : items) {
+        const int m = it->params.mode, dt = it->vol->view.dtype;
+        if ((m == KVSMC_SHARED_POLYGON_NORMAL || m == KVSMC_SHARED_VERTEX_NORMAL) && ctx->path == 0 &&
+            (dt == KVSMC_I8 || dt == KVSMC_I16 || dt == KVSMC_U8 || dt == KVSMC_U16 || dt == KVSMC_F32) &&
+            stream_volume_eligible(ctx, *it))
+            sc.cand.push_back(it);
+    }
+    if (sc.cand.size() < 2) {
+        sc.cand.clear();
+        return KVSMC_OK;
+    }
+    sc.sb.reset(new StreamBatch());
+    StreamBatch& b = *sc.sb;
+    b.ctx = ctx;
+    b.items = sc.cand;
+    b.plan_tables();
+    const size_t need = b.scratch_bytes();
+    if (need > ctx->arena3_bytes) {
+        KVSMC_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+        if (ctx->arena3) cudaFree(ctx->arena3);
+        ctx->arena3 = nullptr;
+        ctx->arena3_bytes = 0;
+        const size_t want = align_up(need, 1 << 20);
+        KVSMC_CUDA(ctx, cudaMalloc(&ctx->arena3, want));
+        ctx->arena3_bytes = want;
+    }
+    b.carve(static_cast<char*>(ctx->arena3));
+    kvsmc_status st = b.upload_tables();
+    if (!st) st = b.count();
+    if (st) return st;
+    for (const StreamBatch::Launch1& l : b.launches) {
+        for (int g = l.g0; g < l.g0 + l.ng; ++g) {
+            const kvsmc::StreamGroup& G = b.groups[g];
+            if (G.rows != 1) continue;
+            const uint64_t end = g + 1 < l.g0 + l.ng ? b.groups[g + 1].task_begin : l.ntasks;
+            for (int k = 0; k < G.niso; ++k)
+                sc.ref[b.iso_item[G.iso_begin + k]] = SharedCount::Ref{g, (uint32_t)k, end - G.task_begin};
+        }
     }
     return KVSMC_OK;
 }
@@ -488,9 +576,16 @@ kvsmc_status run_items(kvsmc_context* ctx, std::vector<Item*>& items, bool emit)
             first = st;
         }
     }
+    SharedCount sc;
+    if (kvsmc_status st = shared_count(ctx, gather_items, sc)) {
+        for (Item* it : sc.cand) it->status = st;
+        if (!first) first = st;
+    }
     for (Item* it : gather_items) {
+        if (it->status) continue;
         Plan pl;
         gather_plan(*it, pl);
+        sc.attach(it, pl);
         kvsmc_status st = gather_count(ctx, pl);
         if (!st) {
             gather_sizes(pl, *it, &it->sizes);
@@ -591,6 +686,7 @@ void kvsmc_destroy(kvsmc_context* ctx)
     }
     if (ctx->out_arena) cudaFree(ctx->out_arena);
     if (ctx->arena2) cudaFree(ctx->arena2);
+    if (ctx->arena3) cudaFree(ctx->arena3);
     if (ctx->h_small) cudaFreeHost(ctx->h_small);
     if (ctx->h_stage) cudaFreeHost(ctx->h_stage);
     profiler_destroy(ctx->prof);
@@ -991,9 +1087,16 @@ kvsmc_status kvsmc_extract_batch_host(kvsmc_context* ctx, const void* host, kvsm
             if (!first) first = st;
         }
     }
+    SharedCount sc;
+    if ((st = shared_count(ctx, g_items, sc))) {
+        for (Item* it : sc.cand) it->status = st;
+        if (!first) first = st;
+    }
     for (Item* it : g_items) {
+        if (it->status) continue;
         Plan pl;
         gather_plan(*it, pl);
+        sc.attach(it, pl);
         st = gather_count(ctx, pl);
         if (!st) {
             gather_sizes(pl, *it, &it->sizes);

@@ -143,7 +143,7 @@ cudaError_t launch_snode(bool emit, const Job& j, const FastIso& f, uint32_t wpr
 size_t sconnect_shared_bytes(int dtype);
 cudaError_t launch_sconnect(const Job& j, const StreamGroup* d_groups, const StreamIso* d_isos,
                             const uint16_t* unit_counts, const uint32_t* unit_offsets, const uint64_t* plane_base,
-                            uint64_t ntasks, uint64_t nvert, uint64_t ntri, int* status,
+                            uint32_t iso_k, uint64_t ntasks, uint64_t nvert, uint64_t ntri, int* status,
                             unsigned long long* next_task, const Launch& L);
 
 // ---- SlicePlane on structured volumes (slice.cu): one warp per cell row

@@ -258,14 +258,16 @@ __device__ __forceinline__ uint32_t sc_rank_id(const Job& j, uint32_t x, uint32_
 // vertex ids come from the rank words of the edges' lower nodes, and the
 // polygon normal from the three vertices' coordinates (written by the node
 // emit pass): into the normals (polygon normals) or the per-triangle scratch
-// the vertex normals are summed from.  One isolevel per launch.
+// the vertex normals are summed from.  One isolevel per launch: isolevel
+// iso_k of the streaming count's group `groups[0]` (whose counters hold all
+// the group's isolevels, niso per unit).
 template <typename T>
 __global__ void __launch_bounds__(kSnThreads)
     k_sconnect(Job j, const StreamGroup* __restrict__ groups, const StreamIso* __restrict__ isos,
                const uint16_t* __restrict__ unit_counts, const uint32_t* __restrict__ unit_offsets,
-               const uint64_t* __restrict__ plane_base, uint64_t ntasks, uint64_t nvert, uint64_t ntri,
-               int* __restrict__ status,
-               unsigned long long* __restrict__ next_task, uint32_t wait_polls)
+               const uint64_t* __restrict__ plane_base, uint32_t iso_k, uint64_t ntasks, uint64_t nvert,
+               uint64_t ntri, int* __restrict__ status, unsigned long long* __restrict__ next_task,
+               uint32_t wait_polls)
 {
     extern __shared__ __align__(128) unsigned char smem_raw[];
     __shared__ uint64_t s_tri[256];
@@ -293,7 +295,8 @@ __global__ void __launch_bounds__(kSnThreads)
     const uint32_t wpr = G.wpr;
     const uint64_t pitch = G.vol.pitch, slice = G.vol.slice;
     const T* vol = static_cast<const T*>(G.vol.data);
-    const StreamIso& I = isos[G.iso_begin];
+    const StreamIso& I = isos[G.iso_begin + iso_k];
+    const uint32_t niso = (uint32_t)G.niso;
     const uint64_t first_plane = plane_base[I.plane_index];
     float* const tri_out = j.mode == 1 ? j.normals : j.tri_normals;
     uint32_t ph = 0;
@@ -347,7 +350,7 @@ __global__ void __launch_bounds__(kSnThreads)
                 break;
             }
             const uint64_t unit = ((uint64_t)z * cy + y) * wpr + seg;
-            if (unit_counts[G.unit_base + unit] != 0) {
+            if (unit_counts[G.unit_base + unit * niso + iso_k] != 0) {
                 const T* a0 = ring + (size_t)(st % 3u) * plane_elems + 8 * lane;
                 const T* a1 = a0 + row_elems;
                 const T* b0 = ring + (size_t)((st + 1) % 3u) * plane_elems + 8 * lane;
@@ -380,7 +383,8 @@ __global__ void __launch_bounds__(kSnThreads)
                     if (lane >= (unsigned)o) inc += t;
                 }
                 const uint32_t total = __shfl_sync(FULL, inc, 31);
-                const uint64_t tbase = plane_base[I.plane_index + z] - first_plane + unit_offsets[G.unit_base + unit];
+                const uint64_t tbase =
+                    plane_base[I.plane_index + z] - first_plane + unit_offsets[G.unit_base + unit * niso + iso_k];
                 // the step's triangles spread over the lanes: triangle q belongs to the
                 // first lane whose inclusive count exceeds q (binary search over lanes)
                 for (uint32_t q0 = 0; q0 < total; q0 += 32) {
@@ -469,7 +473,7 @@ size_t sconnect_shared_bytes(int dtype)
 
 cudaError_t launch_sconnect(const Job& j, const StreamGroup* d_groups, const StreamIso* d_isos,
                             const uint16_t* unit_counts, const uint32_t* unit_offsets, const uint64_t* plane_base,
-                            uint64_t ntasks, uint64_t nvert, uint64_t ntri, int* status,
+                            uint32_t iso_k, uint64_t ntasks, uint64_t nvert, uint64_t ntri, int* status,
                             unsigned long long* next_task, const Launch& L)
 {
     if (ntasks == 0) return cudaSuccess;
@@ -486,8 +490,8 @@ cudaError_t launch_sconnect(const Job& j, const StreamGroup* d_groups, const Str
         const uint64_t nctas = need < resident ? need : resident;
         prof_begin(L, "sconnect");
         kern<<<(unsigned)nctas, kSnThreads, smem, L.stream>>>(j, d_groups, d_isos, unit_counts, unit_offsets,
-                                                                plane_base, ntasks, nvert, ntri, status, next_task,
-                                                                L.wait_polls[1]);
+                                                                plane_base, iso_k, ntasks, nvert, ntri, status,
+                                                                next_task, L.wait_polls[1]);
         prof_end(L);
     });
     *L.counter += 1;

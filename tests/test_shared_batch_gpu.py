@@ -1,0 +1,104 @@
+"""Batches of shared-vertex requests: one streaming triangle count for all of them.
+
+kvsmc_extract_batch / kvsmc_count_batch / kvsmc_extract_batch_host count the
+triangles of every shared-vertex request of a batch (PolygonNormal without
+duplication, VertexNormal) in one streaming pass per volume group (up to 16
+isolevels share one read of the volume), and each request's connection pass
+takes its isolevel's offsets from that count.  The results must be the
+oracle's (oracle/mc_oracle.c) bit for bit, and equal each request run alone
+(which counts on its own), including volumes that do not take the shared
+count (two rows per task), more than 16 isolevels on one volume, mixed modes
+and value types, and a count whose bounded waits give up.
+"""
+import numpy as np
+import pytest
+
+from kvs_gb300 import _abi
+from kvs_gb300 import synthetic as S
+
+from .helpers import first_diff, same_bits
+from .test_stream_gpu import extract_batch
+
+pytestmark = pytest.mark.gpu
+
+torch = pytest.importorskip("torch")
+
+
+def _same(a, b, tag):
+    assert a["ntri"] == b["ntri"], (tag, a["ntri"], b["ntri"])
+    for k in ("coords", "normals"):
+        assert same_bits(a[k], b[k]), (tag, k, first_diff(a[k], b[k]))
+    assert np.array_equal(a["connections"], b["connections"]), tag
+
+
+def test_shared_batch_matches_the_oracle(kvsmc_ctx, oracle_lib):
+    v = S.to_numpy(S.fbm((40, 48, 200), seed=21, device="cuda"))   # 199 cells per row: one row per task
+    lo, hi = float(v.min()), float(v.max())
+    reqs = [(0.35, 1), (0.4, 2), (0.45, 0), (0.5, 2), (0.55, 1), (0.62, 2)]
+    vol = _abi.DeviceVolume.upload(kvsmc_ctx, v)
+    out = extract_batch(kvsmc_ctx, [vol] * len(reqs), [_abi.make_params(x, m) for x, m in reqs], _abi.PATH_AUTO)
+    for (x, m), o in zip(reqs, out):
+        assert o["status"] == _abi.OK
+        ref = oracle_lib.extract(v, x, m, lo, hi)
+        assert same_bits(o["coords"], ref["coords"]), (x, m, first_diff(o["coords"], ref["coords"]))
+        assert same_bits(o["normals"], ref["normals"]), (x, m, first_diff(o["normals"], ref["normals"]))
+        assert np.array_equal(o["connections"], ref["connections"].view(np.uint32)), (x, m)
+    vol.free()
+
+
+def test_shared_batch_equals_alone(kvsmc_ctx):
+    """Groups of more than 16 isolevels, four value types, a two-rows-per-task volume."""
+    rng = np.random.default_rng(5)
+    vols, params = [], []
+    f = S.fbm((40, 44, 256), seed=8, device="cuda")
+    cases = [
+        (S.to_numpy(f), 20),                                                          # f32, 2 groups
+        (S.to_numpy(S._cast(f.double() * 255.0, np.uint8)), 3),                       # u8
+        (S.to_numpy(S._cast(f.double() * 65535.0, np.uint16)), 3),                    # u16
+        (S.to_numpy(S._cast(f.double() * 60000.0 - 30000.0, np.int16)), 2),           # i16
+        (S.to_numpy(S.fbm((36, 40, 100), seed=9, device="cuda")), 3),                 # 99 cells: 2 rows per task
+    ]
+    for v, n in cases:
+        dv = _abi.DeviceVolume.upload(kvsmc_ctx, v)
+        lo, hi = dv.minmax()
+        for _ in range(n):
+            vols.append(dv)
+            params.append(_abi.make_params(lo + rng.uniform(0.25, 0.75) * (hi - lo), int(rng.integers(1, 3))))
+    batch = extract_batch(kvsmc_ctx, vols, params, _abi.PATH_AUTO)
+    for i in range(len(params)):
+        assert batch[i]["status"] == _abi.OK
+        alone = extract_batch(kvsmc_ctx, [vols[i]], [params[i]], _abi.PATH_AUTO)[0]
+        _same(batch[i], alone, f"request {i}")
+    for dv in {id(d): d for d in vols}.values():
+        dv.free()
+
+
+def test_shared_batch_count_timeout_and_recovery():
+    """The shared count's plane waits give up with KVSMC_ERR_TIMEOUT for every
+    request it covers; the next batch on the same context is exact again."""
+    v = S.to_numpy(S.fbm((30, 40, 150), seed=3, device="cuda"))
+    ctx = _abi.Context(0)
+    vol = _abi.DeviceVolume.upload(ctx, v)
+    params = [_abi.make_params(x, _abi.MODE_SHARED_VERTEX_NORMAL) for x in (0.4, 0.5, 0.6)]
+    ref = [extract_batch(ctx, [vol], [p], _abi.PATH_AUTO)[0] for p in params]
+    ctx.set_wait_limit(0, -1)
+    with pytest.raises(_abi.KvsmcError) as e:
+        extract_batch(ctx, [vol] * 3, params, _abi.PATH_AUTO)
+    assert e.value.status == _abi.ERR_TIMEOUT
+    ctx.set_wait_limit(-1, -1)
+    got = extract_batch(ctx, [vol] * 3, params, _abi.PATH_AUTO)
+    for a, b in zip(got, ref):
+        _same(a, b, "after timeout")
+    vol.free()
+    ctx.close()
+
+
+def test_host_batch_shared_requests_match_alone(kvsmc_ctx):
+    v = S.to_numpy(S.gaussian_blobs((40, 50, 160), seed=12, device="cuda"))
+    params = [_abi.make_params(x, m) for x, m in ((0.3, 2), (0.45, 1), (0.5, 0), (0.6, 2))]
+    out = _abi.extract_batch_host(kvsmc_ctx, v, params)
+    for k, p in enumerate(params):
+        alone = _abi.extract_batch_host(kvsmc_ctx, v, [p])[0]
+        for key in ("coords", "normals"):
+            assert same_bits(out[k][key], alone[key]), (k, key, first_diff(out[k][key], alone[key]))
+        assert np.array_equal(out[k]["connections"], alone["connections"]), k
