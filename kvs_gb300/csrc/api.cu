@@ -243,6 +243,9 @@ struct Plan {
     int sb_group = 0;
     uint32_t sb_iso = 0;
     uint64_t sb_tasks = 0;
+    // the request's vertex counts per node unit from that shared count (null:
+    // the node count pass counts them)
+    const uint32_t* sb_nodes = nullptr;
 };
 
 uint32_t rows_for(uint32_t width, uint32_t limit)
@@ -352,9 +355,11 @@ kvsmc_status gather_count(kvsmc_context* ctx, Plan& pl)
     if (nt && pl.snode) {
         KVSMC_CUDA(ctx, cudaMemsetAsync(pl.d_status, 0, sizeof(int), ctx->stream));
         KVSMC_CUDA(ctx, cudaMemsetAsync(pl.d_next, 0, 3 * sizeof(unsigned long long), ctx->stream));
-        KVSMC_CUDA(ctx, kvsmc::launch_snode(false, j, pl.f, pl.wprn, pl.zchunk, pl.ntasks, j.vtile_counts, nullptr,
-                                            pl.d_status, pl.d_next, L));
-        KVSMC_CUDA(ctx, launch_scan(j.vtile_counts, j.vtile_offsets, nt, scan_b, d_totals + 1, L));
+        if (!pl.sb_nodes)
+            KVSMC_CUDA(ctx, kvsmc::launch_snode(false, j, pl.f, pl.wprn, pl.zchunk, pl.ntasks, j.vtile_counts,
+                                                nullptr, pl.d_status, pl.d_next, L));
+        KVSMC_CUDA(ctx, launch_scan(pl.sb_nodes ? pl.sb_nodes : j.vtile_counts, j.vtile_offsets, nt, scan_b,
+                                    d_totals + 1, L));
         KVSMC_CUDA(ctx, cudaMemcpyAsync(d_totals + 2, pl.d_status, sizeof(int), cudaMemcpyDeviceToDevice, ctx->stream));
     } else if (nt) {
         KVSMC_CUDA(ctx, launch_node_count(j, L));
@@ -466,8 +471,11 @@ kvsmc_status gather_emit(kvsmc_context* ctx, Plan& pl, float* coords, float* nor
 // The streaming triangle count of a batch's shared-vertex requests in one
 // pass: requests on the same volume share one read of it (up to 16
 // isolevels per group), and each request's connection pass takes its
-// isolevel's unit offsets from it.  Requests whose group does not take one
-// row per task, and a batch with a single such request, keep their own count.
+// isolevel's unit offsets from it.  The same pass counts each request's
+// vertices per node unit (groups whose node segments are their cell
+// segments), so the requests skip their node count passes.  Requests whose
+// group does not take one row per task, and a batch with a single such
+// request, keep their own counts.
 struct SharedCount {
     std::unique_ptr<StreamBatch> sb;
     std::vector<Item*> cand;   // the requests counted here
@@ -475,6 +483,7 @@ struct SharedCount {
         int group;
         uint32_t iso;
         uint64_t tasks;
+        const uint32_t* nodes;
     };
     std::unordered_map<const Item*, Ref> ref;
 
@@ -486,6 +495,7 @@ struct SharedCount {
         pl.sb_group = r->second.group;
         pl.sb_iso = r->second.iso;
         pl.sb_tasks = r->second.tasks;
+        pl.sb_nodes = r->second.nodes;
     }
 };
 
@@ -506,6 +516,7 @@ kvsmc_status shared_count(kvsmc_context* ctx, const std::vector<Item*>& items, S
     StreamBatch& b = *sc.sb;
     b.ctx = ctx;
     b.items = sc.cand;
+    b.want_nodes = true;
     b.plan_tables();
     const size_t need = b.scratch_bytes();
     if (need > ctx->arena3_bytes) {
@@ -526,8 +537,11 @@ kvsmc_status shared_count(kvsmc_context* ctx, const std::vector<Item*>& items, S
             const kvsmc::StreamGroup& G = b.groups[g];
             if (G.rows != 1) continue;
             const uint64_t end = g + 1 < l.g0 + l.ng ? b.groups[g + 1].task_begin : l.ntasks;
-            for (int k = 0; k < G.niso; ++k)
-                sc.ref[b.iso_item[G.iso_begin + k]] = SharedCount::Ref{g, (uint32_t)k, end - G.task_begin};
+            for (int k = 0; k < G.niso; ++k) {
+                const uint32_t* nodes = G.node_units ? b.d_node_counts + G.node_base + (uint64_t)k * G.node_units
+                                                     : nullptr;
+                sc.ref[b.iso_item[G.iso_begin + k]] = SharedCount::Ref{g, (uint32_t)k, end - G.task_begin, nodes};
+            }
         }
     }
     return KVSMC_OK;

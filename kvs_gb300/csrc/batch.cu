@@ -166,6 +166,7 @@ void StreamBatch::plan_tables()
     unit_elems = 0;
     scan_blocks = 0;
     iso_planes = 0;
+    node_elems = 0;
     for (const auto& kd : kinds) {
         const int dt = kd.first, rows = kd.second;
         Launch1 L;
@@ -215,6 +216,11 @@ void StreamBatch::plan_tables()
             bucket_params(sorted.front().first, sorted.back().first, g.bs, g.bo);
             g.unit_base = unit_elems;
             unit_elems += stream_units(v, g.wpr, g.niso);
+            if (want_nodes && rows == 1 && g.wpr == (v.nx + 255) / 256) {
+                g.node_units = (uint64_t)v.nz * v.ny * g.wpr;
+                g.node_base = node_elems;
+                node_elems += (uint64_t)g.niso * g.node_units;
+            }
             g.plane_begin = scan_blocks;
             scan_blocks += cz;
             for (auto& pr : sorted) {
@@ -244,7 +250,8 @@ size_t StreamBatch::scratch_bytes() const
     return 16 * 256 + align_up(groups.size() * sizeof(StreamGroup), 256) + align_up(niso * sizeof(StreamIso), 256) +
            align_up(unit_elems * 2, 256) + align_up(unit_elems * 4, 256) + align_up(iso_planes * 4, 256) +
            align_up(iso_planes * 8, 256) + align_up(kvsmc::scan_scratch_bytes(iso_planes), 256) +
-           align_up(niso * 8, 256) + align_up(launches.size() * 16, 256) + align_up(kMaxParts * 8, 256) + 5 * 256;
+           align_up(niso * 8, 256) + align_up(launches.size() * 16, 256) + align_up(kMaxParts * 8, 256) +
+           align_up(node_elems * 4, 256) + 6 * 256;
 }
 
 void StreamBatch::carve(char* base)
@@ -263,6 +270,7 @@ void StreamBatch::carve(char* base)
     d_status = cv.take<int>(256);
     d_next = cv.take<unsigned long long>(launches.size() * 16);
     d_next_parts = cv.take<unsigned long long>(kMaxParts * 8);
+    d_node_counts = node_elems ? cv.take<uint32_t>(node_elems * 4) : nullptr;
 }
 
 kvsmc_status StreamBatch::plan()
@@ -294,13 +302,15 @@ kvsmc_status StreamBatch::count()
     // units the kernels skip as empty space keep these zeros
     KVSMC_CUDA(ctx, cudaMemsetAsync(d_unit_counts, 0, unit_elems * sizeof(uint16_t), ctx->stream));
     KVSMC_CUDA(ctx, cudaMemsetAsync(d_next, 0, launches.size() * 16, ctx->stream));
+    if (node_elems) KVSMC_CUDA(ctx, cudaMemsetAsync(d_node_counts, 0, node_elems * 4, ctx->stream));
     // one count launch per (value type, rows) kind, side by side
     KVSMC_CUDA(ctx, fan_out(ctx, ctx->stream, launches.size(), [&](size_t i, cudaStream_t st) {
         const Launch1& l = launches[i];
         kvsmc::Launch Li = L;
         Li.stream = st;
         return kvsmc::launch_stream(false, l.dtype, l.rows, d_groups + l.g0, l.ng, l.ntasks, d_isos, d_unit_counts,
-                                    nullptr, nullptr, d_status, d_next + 2 * i, Li, l.ctas_per_sm);
+                                    nullptr, nullptr, d_status, d_next + 2 * i, Li, l.ctas_per_sm, 0,
+                                    node_elems && l.rows == 1 ? d_node_counts : nullptr);
     }));
     KVSMC_CUDA(ctx, kvsmc::launch_unit_scan(d_groups, (int)groups.size(), scan_blocks, d_isos, d_unit_counts,
                                             d_unit_offsets, d_plane_totals, L, scan_threads));

@@ -66,6 +66,12 @@ struct StreamBatch {
     uint32_t scan_blocks = 0;    // unit-scan blocks: one per (group, z)
     int scan_threads = 256;      // unit-scan tile
     uint64_t iso_planes = 0;     // (isolevel, z) planes
+    // the count pass also counts the shared-vertex modes' vertices per
+    // (isolevel, node unit) for the groups that take one row per task and
+    // whose node segments are its cell segments (set before plan_tables)
+    bool want_nodes = false;
+    uint64_t node_elems = 0;
+    uint32_t* d_node_counts = nullptr;
 
     kvsmc::StreamGroup* d_groups = nullptr;
     kvsmc::StreamIso* d_isos = nullptr;

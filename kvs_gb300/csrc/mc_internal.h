@@ -92,6 +92,11 @@ struct StreamGroup {
     const float2* bricks;    // the volume's brick min/max table, or null
     int32_t skip_emit;       // 1: no isolevel of the group is written by this emit launch
     uint32_t brick_wpr;      // bricks per row pair (128-cell brick segments per row)
+    // shared-vertex vertex counts from the count pass (one-row tasks only):
+    // per isolevel k, node unit u = (plane, node row, 256-node segment) at
+    // node_base + k * node_units + u; node_units == 0: not counted
+    uint64_t node_base;
+    uint64_t node_units;
 };
 
 // Brick min/max table of a volume: one float2 per (8 cell planes, 2 cell
@@ -117,7 +122,8 @@ size_t stream_row_elems(int dtype, int rows);
 cudaError_t launch_stream(bool emit, int dtype, int rows, const StreamGroup* d_groups, int ngroups, uint64_t ntasks,
                           const StreamIso* d_isos, uint16_t* d_unit_counts, const uint32_t* d_unit_offsets,
                           const uint64_t* d_plane_base, int* d_status, unsigned long long* d_next_task,
-                          const Launch& L, int ctas_per_sm = 0, uint64_t task0 = 0);
+                          const Launch& L, int ctas_per_sm = 0, uint64_t task0 = 0,
+                          uint32_t* d_node_counts = nullptr);
 // scan_threads: units per CTA pass (64, 128 or 256; 0 = 256).
 cudaError_t launch_unit_scan(const StreamGroup* d_groups, int ngroups, uint32_t nplanes, const StreamIso* d_isos,
                              const uint16_t* d_unit_counts, uint32_t* d_unit_offsets, uint32_t* d_plane_totals,

@@ -383,13 +383,23 @@ __device__ __forceinline__ int find_group(const StreamGroup* groups, int ngroups
 // so warps that skip empty tasks go on at once instead of idling in a CTA
 // whose other warps still run.  Tasks come out in increasing order; the
 // group's isolevel tables are rebuilt when a warp crosses a group boundary.
-template <typename T, bool EMIT, int R>
+//
+// NODES (count pass, one row per task): the pass also counts, per isolevel,
+// the vertices of the shared-vertex modes' node units (plane, node row,
+// 256-node segment): the cut x, y and z edges from each node to its upper
+// neighbours, the edges whose two ends' threshold masks differ.  A task of
+// cell row y counts node row y at its planes; on the last cell row also node
+// row y + 1, on the last cell plane also the last node plane.  Groups with
+// node_units == 0 are not counted.
+template <typename T, bool EMIT, int R, bool NODES = false>
 __global__ void __launch_bounds__(EMIT ? kEmitThreads : kStreamThreads, EMIT ? KVSMC_EMIT_CTAS : 3)
     k_stream(const StreamGroup* __restrict__ groups, int ngroups, uint64_t ntasks, const StreamIso* __restrict__ isos,
              uint16_t* __restrict__ unit_counts, const uint32_t* __restrict__ unit_offsets,
              const uint64_t* __restrict__ plane_base, int* __restrict__ status,
-             unsigned long long* __restrict__ next_task, uint32_t wait_polls, uint64_t task0)
+             unsigned long long* __restrict__ next_task, uint32_t wait_polls, uint64_t task0,
+             uint32_t* __restrict__ node_counts)
 {
+    static_assert(!NODES || (!EMIT && R == 1), "node counts come from one-row count tasks");
     constexpr int LPR = 32 / R;                 // lanes per cell row
     constexpr int SEG = kSegCells / R;          // cells per row segment
     constexpr int SEG_SHIFT = R == 1 ? 8 : 7;   // log2(SEG)
@@ -677,6 +687,51 @@ __global__ void __launch_bounds__(EMIT ? kEmitThreads : kStreamThreads, EMIT ? K
                     }
                 }
                 __syncwarp();
+                if (NODES && G.node_units) {
+                    // (a node edge that is cut for isolevel k belongs to a cell active
+                    // for k, so a step without active cells has no vertices either)
+                    const int nlim = (int)G.vol.nx - (int)((uint32_t)xoff + xl);   // this lane's nodes in the row
+                    // vertices of node row (plane zn, row yn): masks Pn, and the rows
+                    // across its y edges (Py) and z edges (Pz) when it has them
+                    auto node_unit = [&](const uint32_t* Pn, const uint32_t* Py, const uint32_t* Pz, bool has_y,
+                                         bool has_z, uint32_t zn, uint32_t yn) {
+                        uint32_t X[4], Y[4], Z[4], U = 0;
+#pragma unroll
+                        for (int w = 0; w < 4; ++w) {
+                            // halves: nodes 2w (low) and 2w + 1 (high)
+                            const uint32_t vn = (2 * w < nlim ? 0xffffu : 0u) | (2 * w + 1 < nlim ? 0xffff0000u : 0u);
+                            const uint32_t vx =
+                                (2 * w + 1 < nlim ? 0xffffu : 0u) | (2 * w + 2 < nlim ? 0xffff0000u : 0u);
+                            X[w] = (Pn[w] ^ __funnelshift_r(Pn[w], Pn[w + 1], 16)) & vx;
+                            Y[w] = has_y ? (Pn[w] ^ Py[w]) & vn : 0u;
+                            Z[w] = has_z ? (Pn[w] ^ Pz[w]) & vn : 0u;
+                            U |= X[w] | Y[w] | Z[w];
+                        }
+                        uint32_t am = (U | (U >> 16)) & 0xffffu;
+                        if (!__any_sync(FULL, am != 0)) return;
+                        while (am) {
+                            const uint32_t k = __ffs(am) - 1;
+                            am &= am - 1;
+                            const uint32_t mk = 0x10001u << k;
+                            uint32_t c = 0;
+#pragma unroll
+                            for (int w = 0; w < 4; ++w) c += __popc(X[w] & mk) + __popc(Y[w] & mk) + __popc(Z[w] & mk);
+                            atomicAdd(&W.add[k], c);
+                        }
+                        __syncwarp();
+                        if (lane < (unsigned)niso) {
+                            const uint64_t un = ((uint64_t)zn * G.vol.ny + yn) * wpr + seg;
+                            node_counts[G.node_base + (uint64_t)lane * G.node_units + un] = W.add[lane];
+                            W.add[lane] = 0;
+                        }
+                        __syncwarp();
+                    };
+                    const bool last_row = y + 1 == cy, last_plane = z + 1 == cz;
+                    node_unit(PA0, PA1, PB0, true, true, z, y);
+                    if (last_row) node_unit(PA1, PA1, PB1, false, true, z, y + 1);
+                    if (last_plane) node_unit(PB0, PB1, PB0, true, false, z + 1, y);
+                    if (last_row && last_plane) node_unit(PB1, PB1, PB1, false, false, z + 1, y + 1);
+                }
             }
             const uint32_t h = lane >> 4, k = lane & 15u;
             if (h < (uint32_t)R && k < (uint32_t)niso && y + h < cy) {
@@ -1045,7 +1100,7 @@ uint64_t brick_count(const VolumeView& v)
 cudaError_t launch_stream(bool emit, int dtype, int rows, const StreamGroup* d_groups, int ngroups, uint64_t ntasks,
                           const StreamIso* d_isos, uint16_t* d_unit_counts, const uint32_t* d_unit_offsets,
                           const uint64_t* d_plane_base, int* d_status, unsigned long long* d_next_task,
-                          const Launch& L, int ctas_per_sm, uint64_t task0)
+                          const Launch& L, int ctas_per_sm, uint64_t task0, uint32_t* d_node_counts)
 {
     if (ntasks <= task0) return cudaSuccess;
     if (rows != 1 && rows != 2) return cudaErrorInvalidValue;
@@ -1054,7 +1109,8 @@ cudaError_t launch_stream(bool emit, int dtype, int rows, const StreamGroup* d_g
     const uint64_t need = (ntasks - task0 + threads / 32 - 1) / (threads / 32);
     KVSMC_STREAM_SWITCH(dtype, {
         auto kern = emit ? (rows == 1 ? k_stream<T, true, 1> : k_stream<T, true, 2>)
-                         : (rows == 1 ? k_stream<T, false, 1> : k_stream<T, false, 2>);
+                         : (rows == 1 ? (d_node_counts ? k_stream<T, false, 1, true> : k_stream<T, false, 1>)
+                                      : k_stream<T, false, 2>);
         cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
         if (e == cudaSuccess)
             e = cudaFuncSetAttribute(kern, cudaFuncAttributePreferredSharedMemoryCarveout,
@@ -1069,7 +1125,8 @@ cudaError_t launch_stream(bool emit, int dtype, int rows, const StreamGroup* d_g
         prof_begin(L, emit ? "stream_emit" : "stream_count");
         kern<<<(unsigned)nctas, threads, smem, L.stream>>>(d_groups, ngroups, ntasks, d_isos, d_unit_counts,
                                                            d_unit_offsets, d_plane_base, d_status, d_next_task,
-                                                           L.wait_polls[emit ? 1 : 0], task0);
+                                                           L.wait_polls[emit ? 1 : 0], task0,
+                                                           emit ? nullptr : d_node_counts);
         prof_end(L);
     });
     *L.counter += 1;

@@ -47,7 +47,9 @@ def test_shared_batch_matches_the_oracle(kvsmc_ctx, oracle_lib):
 
 
 def test_shared_batch_equals_alone(kvsmc_ctx):
-    """Groups of more than 16 isolevels, four value types, a two-rows-per-task volume."""
+    """Groups of more than 16 isolevels, four value types, a two-rows-per-task
+    volume, rows of several segments, and a row whose last node starts a
+    segment of its own (its requests count their vertices on their own)."""
     rng = np.random.default_rng(5)
     vols, params = [], []
     f = S.fbm((40, 44, 256), seed=8, device="cuda")
@@ -57,6 +59,8 @@ def test_shared_batch_equals_alone(kvsmc_ctx):
         (S.to_numpy(S._cast(f.double() * 65535.0, np.uint16)), 3),                    # u16
         (S.to_numpy(S._cast(f.double() * 60000.0 - 30000.0, np.int16)), 2),           # i16
         (S.to_numpy(S.fbm((36, 40, 100), seed=9, device="cuda")), 3),                 # 99 cells: 2 rows per task
+        (S.to_numpy(S.fbm((20, 24, 700), seed=10, device="cuda")), 3),                # 3 segments, the last partial
+        (S.to_numpy(S.fbm((18, 22, 257), seed=11, device="cuda")), 2),                # node 256 alone in a segment
     ]
     for v, n in cases:
         dv = _abi.DeviceVolume.upload(kvsmc_ctx, v)
