@@ -975,12 +975,13 @@ def run_ours(args, rank, world, local):
     emit_launches, emit_ms = prof.get("stream_emit", (0, 0.0))
     roofline = None
     if mode != _abi.MODE_DUP_POLYGON_NORMAL:
-        # shared vertices: volume once per isovalue pass + 24 B per vertex (coords,
-        # vertex normals) + 12 B per triangle (connections), over the whole step
-        # (five kernel families, none dominant on its own)
+        # shared vertices: volume once per isovalue (the minimum for one request
+        # at a time) + 24 B per vertex (coords, vertex normals) + 12 B per
+        # triangle (connections), over the whole step (several kernel families,
+        # none dominant on its own)
         algo_bytes = nx * ny * nz * dt.itemsize * n + 24 * nvert + 12 * ntri
         achieved = algo_bytes / (step_ms * 1e-3) / 1e9
-        roofline = {"kernel": "whole step (gather kernels)", "bound": "hbm", "achieved": round(achieved, 1),
+        roofline = {"kernel": "whole step (shared-vertex passes)", "bound": "hbm", "achieved": round(achieved, 1),
                     "peak": hbm, "peak_kind": peak_kind, "unit": "GB/s", "frac": round(achieved / hbm, 4),
                     "algorithmic_bytes_per_step": algo_bytes, "traffic": None}
     elif emit_launches:
