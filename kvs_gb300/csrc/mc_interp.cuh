@@ -161,8 +161,11 @@ __device__ __forceinline__ bool fast_axis_bf(float v0, float v1, float a, float 
     const float aq = fabsf(q1);
     const bool up = b > a;
     const float dq1 = up ? q1 : -q1, dq2 = up ? q2 : -q2;
-    float ya, yb;
-    two_sum(a, dq1, ya, yb);
+    // a + dq1 exactly as (ya, yb) by Dekker's Fast2Sum: a is an integer
+    // coordinate (0, or at least 1 in magnitude) and |dq1| <= 1.5 on every
+    // accepted result, so a == 0 or exponent(a) >= exponent(dq1)
+    const float ya = __fadd_rn(a, dq1);
+    const float yb = __fsub_rn(dq1, __fsub_rn(ya, a));
     const float yb2 = __fadd_rn(yb, dq2);
     float yh, yl;
     two_sum(ya, yb2, yh, yl);

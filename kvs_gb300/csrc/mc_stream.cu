@@ -190,6 +190,26 @@ __device__ __forceinline__ float3 load_vertex(const WarpEmit* WE, uint32_t j)
     return make_float3(v.x, v.y, v.z);
 }
 
+// One triangle's 9 coordinates and 3 normal components, as the 8-byte
+// stores the addresses allow: a word whose address is 8-byte aligned pairs
+// with the next one, the odd word out is stored alone (the first word when
+// the array starts off an 8-byte boundary, else the last).  Seven stores
+// instead of twelve; the values are chosen by selects, so lanes with either
+// alignment run the same instructions.
+__device__ __forceinline__ void store_triangle(float* oc, float* on, float3 A, float3 B, float3 C, float3 n)
+{
+    const bool ho = (reinterpret_cast<uintptr_t>(oc) & 4u) != 0;
+    *(ho ? oc : oc + 8) = ho ? A.x : C.z;
+    float2* p2 = reinterpret_cast<float2*>(ho ? oc + 1 : oc);
+    p2[0] = make_float2(ho ? A.y : A.x, ho ? A.z : A.y);
+    p2[1] = make_float2(ho ? B.x : A.z, ho ? B.y : B.x);
+    p2[2] = make_float2(ho ? B.z : B.y, ho ? C.x : B.z);
+    p2[3] = make_float2(ho ? C.y : C.x, ho ? C.z : C.y);
+    const bool hn = (reinterpret_cast<uintptr_t>(on) & 4u) != 0;
+    *(hn ? on : on + 2) = hn ? n.x : n.z;
+    *reinterpret_cast<float2*>(hn ? on + 1 : on) = make_float2(hn ? n.y : n.x, hn ? n.z : n.y);
+}
+
 // An isolevel's interpolation constants in registers, read from its IsoConst
 // with four 16-byte loads.
 struct IsoRegs {
@@ -885,14 +905,8 @@ __global__ void __launch_bounds__(EMIT ? kEmitThreads : kStreamThreads, EMIT ? K
                                 const float3 n = tri_normal(A, B, C);
                                 const IsoConst& IC = WE->ic[qk];
                                 float* const pc = IC.coords;
-                                if (pc && qo + t < IC.cap_tris) {
-                                    float* oc = pc + 9 * (qo + t);
-                                    float* on = IC.normals + 3 * (qo + t);
-                                    oc[0] = A.x; oc[1] = A.y; oc[2] = A.z;
-                                    oc[3] = B.x; oc[4] = B.y; oc[5] = B.z;
-                                    oc[6] = C.x; oc[7] = C.y; oc[8] = C.z;
-                                    on[0] = n.x; on[1] = n.y; on[2] = n.z;
-                                }
+                                if (pc && qo + t < IC.cap_tris)
+                                    store_triangle(pc + 9 * (qo + t), IC.normals + 3 * (qo + t), A, B, C, n);
                             }
                         }
                         __syncwarp();
