@@ -432,7 +432,27 @@ __global__ void __launch_bounds__(256) k_vn_sum(const uint64_t* __restrict__ vof
             sy = __fadd_rn(sy, tri_normals[3 * (uint64_t)t + 1]);
             sz = __fadd_rn(sz, tri_normals[3 * (uint64_t)t + 2]);
         };
-        if (n <= (uint32_t)kVnLocal) {
+        if (n <= 8u) {
+            // the common case (a vertex lies on one cell edge: four cells, a
+            // triangle or two each): a 19-comparator sorting network in registers,
+            // missing entries padded with the largest id
+            uint32_t d[8];
+#pragma unroll
+            for (int i = 0; i < 8; ++i) d[i] = (uint32_t)i < n ? vlist[a + i] : 0xffffffffu;
+            auto cx = [&](int i, int k) {
+                const uint32_t lo = min(d[i], d[k]), hi = max(d[i], d[k]);
+                d[i] = lo;
+                d[k] = hi;
+            };
+            cx(0, 1); cx(2, 3); cx(4, 5); cx(6, 7);
+            cx(0, 2); cx(1, 3); cx(4, 6); cx(5, 7);
+            cx(1, 2); cx(5, 6); cx(0, 4); cx(3, 7);
+            cx(1, 5); cx(2, 6); cx(1, 4); cx(3, 6);
+            cx(2, 4); cx(3, 5); cx(3, 4);
+#pragma unroll
+            for (int i = 0; i < 8; ++i)
+                if ((uint32_t)i < n) add(d[i]);
+        } else if (n <= (uint32_t)kVnLocal) {
             uint32_t ids[kVnLocal];
             for (uint32_t i = 0; i < n; ++i) {
                 // insertion sort while loading
