@@ -336,8 +336,16 @@ __global__ void __launch_bounds__(kSnThreads)
         bool dead = false;
         const uint32_t x0 = (uint32_t)xoff + 8 * lane;
         const int lim = (int)cx - (int)x0;   // cells of this lane inside the row (if < 8)
+        // the unit's triangle count, loaded one step ahead so its latency hides
+        // behind a step's work
+        auto unit_count = [&](uint32_t zz) -> uint32_t {
+            return unit_counts[G.unit_base + (((uint64_t)zz * cy + y) * wpr + seg) * niso + iso_k];
+        };
+        uint32_t next_count = unit_count(z0);
         for (uint32_t z = z0; z < z1; ++z) {
             const uint32_t st = z - z0;
+            const uint32_t count_now = next_count;
+            if (z + 1 < z1) next_count = unit_count(z + 1);
             bool ok = true;
             while (ok && acq <= st + 1) {
                 ok = acquire(acq);
@@ -350,7 +358,7 @@ __global__ void __launch_bounds__(kSnThreads)
                 break;
             }
             const uint64_t unit = ((uint64_t)z * cy + y) * wpr + seg;
-            if (unit_counts[G.unit_base + unit * niso + iso_k] != 0) {
+            if (count_now != 0) {
                 const T* a0 = ring + (size_t)(st % 3u) * plane_elems + 8 * lane;
                 const T* a1 = a0 + row_elems;
                 const T* b0 = ring + (size_t)((st + 1) % 3u) * plane_elems + 8 * lane;
