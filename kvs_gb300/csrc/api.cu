@@ -443,7 +443,8 @@ kvsmc_status gather_emit(kvsmc_context* ctx, Plan& pl, float* coords, float* nor
     };
     kvsmc_status st = KVSMC_OK;
     if (pl.nvert && pl.snode) {
-        KVSMC_CUDA(ctx, kvsmc::launch_snode(true, j, pl.f, pl.wprn, pl.zchunk, pl.ntasks, nullptr, j.vtile_offsets,
+        uint32_t* counts = const_cast<uint32_t*>(pl.sb_nodes ? pl.sb_nodes : j.vtile_counts);
+        KVSMC_CUDA(ctx, kvsmc::launch_snode(true, j, pl.f, pl.wprn, pl.zchunk, pl.ntasks, counts, j.vtile_offsets,
                                             pl.d_status, pl.d_next + 1, L));
         if ((st = check_status("shared-vertex node emit"))) return st;
     } else if (pl.nvert) {

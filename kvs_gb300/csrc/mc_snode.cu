@@ -53,6 +53,7 @@ __global__ void __launch_bounds__(kSnThreads, EMIT ? KVSMC_SNODE_EMIT_CTAS : 1)
             uint32_t copy_bytes, uint32_t* __restrict__ unit_counts, const uint64_t* __restrict__ unit_offsets,
             int* __restrict__ status, unsigned long long* __restrict__ next_task, uint32_t wait_polls)
 {
+    // count pass: writes unit_counts; emit pass: reads them with their scan
     extern __shared__ __align__(128) unsigned char smem_raw[];
     const unsigned lane = threadIdx.x & 31u, warp = threadIdx.x >> 5;
     const size_t plane_elems = 2 * (size_t)row_elems;
@@ -104,9 +105,25 @@ __global__ void __launch_bounds__(kSnThreads, EMIT ? KVSMC_SNODE_EMIT_CTAS : 1)
         uint32_t acq = 0;
         bool dead = false;
         uint32_t issued = 0;
+        // emit: the unit's vertex count and first id, loaded one step ahead so
+        // their latency hides behind a step's work; a unit without vertices
+        // is skipped (no rank word of it is ever read)
+        uint32_t next_n = 0;
+        uint64_t next_base = 0;
+        auto unit_of = [&](uint32_t zz) -> uint64_t { return ((uint64_t)zz * ny + y) * wprn + s; };
+        if (EMIT) {
+            next_n = unit_counts[unit_of(z0)];
+            next_base = unit_offsets[unit_of(z0)];
+        }
         for (uint32_t z = z0; z < z1; ++z) {
             const uint32_t st = z - z0;
             const uint32_t need = z + 1 < nz ? st + 1 : st;   // last plane staged this step
+            const uint32_t n_now = next_n;
+            const uint64_t base_now = next_base;
+            if (EMIT && z + 1 < z1) {
+                next_n = unit_counts[unit_of(z + 1)];
+                next_base = unit_offsets[unit_of(z + 1)];
+            }
             bool ok = true;
             while (ok && acq <= need) {
                 ok = acquire(acq);
@@ -117,6 +134,14 @@ __global__ void __launch_bounds__(kSnThreads, EMIT ? KVSMC_SNODE_EMIT_CTAS : 1)
                 dead = true;
                 issued = st + 3 < nplanes ? st + 3 : nplanes;
                 break;
+            }
+            if (EMIT && n_now == 0) {
+                __syncwarp();
+                if (lane == 0 && st + 3 < nplanes) {
+                    fence_proxy_async();
+                    issue(st + 3);
+                }
+                continue;
             }
             const T* ra = ring + (size_t)(st % 3u) * plane_elems;            // plane z, row y
             const T* rb = ra + row_elems;                                     // plane z, row y + 1
@@ -145,7 +170,7 @@ __global__ void __launch_bounds__(kSnThreads, EMIT ? KVSMC_SNODE_EMIT_CTAS : 1)
                 const uint32_t tot = __reduce_add_sync(FULL, cnt);
                 if (lane == 0) unit_counts[unit] = tot;
             } else {
-                const uint64_t base = unit_offsets[unit];
+                const uint64_t base = base_now;
                 const uint64_t row = (uint64_t)z * ny + y;
                 // per 32-node word i: its crossing flags (three ballots) and its first
                 // vertex within the unit; items (node, axis) are numbered like the ids
