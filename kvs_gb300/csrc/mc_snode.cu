@@ -361,16 +361,24 @@ __global__ void __launch_bounds__(kSnThreads)
         bool dead = false;
         const uint32_t x0 = (uint32_t)xoff + 8 * lane;
         const int lim = (int)cx - (int)x0;   // cells of this lane inside the row (if < 8)
-        // the unit's triangle count, loaded one step ahead so its latency hides
-        // behind a step's work
-        auto unit_count = [&](uint32_t zz) -> uint32_t {
-            return unit_counts[G.unit_base + (((uint64_t)zz * cy + y) * wpr + seg) * niso + iso_k];
+        // the unit's triangle count and first triangle, loaded one step ahead
+        // so their latency hides behind a step's work
+        auto unit_elem = [&](uint32_t zz) -> uint64_t {
+            return G.unit_base + (((uint64_t)zz * cy + y) * wpr + seg) * niso + iso_k;
         };
-        uint32_t next_count = unit_count(z0);
+        auto unit_first = [&](uint32_t zz) -> uint64_t {
+            return plane_base[I.plane_index + zz] - first_plane + unit_offsets[unit_elem(zz)];
+        };
+        uint32_t next_count = unit_counts[unit_elem(z0)];
+        uint64_t next_first = unit_first(z0);
         for (uint32_t z = z0; z < z1; ++z) {
             const uint32_t st = z - z0;
             const uint32_t count_now = next_count;
-            if (z + 1 < z1) next_count = unit_count(z + 1);
+            const uint64_t tbase = next_first;
+            if (z + 1 < z1) {
+                next_count = unit_counts[unit_elem(z + 1)];
+                next_first = unit_first(z + 1);
+            }
             bool ok = true;
             while (ok && acq <= st + 1) {
                 ok = acquire(acq);
@@ -382,7 +390,6 @@ __global__ void __launch_bounds__(kSnThreads)
                 issued = st + 3 < nplanes ? st + 3 : nplanes;
                 break;
             }
-            const uint64_t unit = ((uint64_t)z * cy + y) * wpr + seg;
             if (count_now != 0) {
                 const T* a0 = ring + (size_t)(st % 3u) * plane_elems + 8 * lane;
                 const T* a1 = a0 + row_elems;
@@ -396,19 +403,27 @@ __global__ void __launch_bounds__(kSnThreads)
                     m[2] |= (above(j.cls, b0[k]) ? 1u : 0u) << k;
                     m[3] |= (above(j.cls, b1[k]) ? 1u : 0u) << k;
                 }
-                uint32_t cases[8];
+                // the 8 cells' cases (corners 0:(x,y,z) 1:(x+1,y,z) 2:(x+1,y+1,z)
+                // 3:(x,y+1,z), 4..7 the same at z+1), byte i = cell i: byte b of
+                // the word below holds case bit b of the 8 cells, and an 8x8 bit
+                // transpose turns it into one case per byte
+                uint64_t cw =
+                    (uint64_t)((m[0] & 0xffu) | (((m[0] >> 1) & 0xffu) << 8) | (((m[1] >> 1) & 0xffu) << 16) |
+                               ((m[1] & 0xffu) << 24)) |
+                    ((uint64_t)((m[2] & 0xffu) | (((m[2] >> 1) & 0xffu) << 8) | (((m[3] >> 1) & 0xffu) << 16) |
+                                ((m[3] & 0xffu) << 24))
+                     << 32);
+                uint64_t tt = (cw ^ (cw >> 7)) & 0x00AA00AA00AA00AAull;
+                cw ^= tt ^ (tt << 7);
+                tt = (cw ^ (cw >> 14)) & 0x0000CCCC0000CCCCull;
+                cw ^= tt ^ (tt << 14);
+                tt = (cw ^ (cw >> 28)) & 0x00000000F0F0F0F0ull;
+                cw ^= tt ^ (tt << 28);
+                if (lim < 8) cw &= lim <= 0 ? 0ull : (~0ull >> (64 - 8 * lim));   // cells past the row: none
+                const uint32_t clo = (uint32_t)cw, chi = (uint32_t)(cw >> 32);     // cells 0-3, 4-7
                 uint32_t n = 0;
 #pragma unroll
-                for (int i = 0; i < 8; ++i) {
-                    // corners 0:(x,y,z) 1:(x+1,y,z) 2:(x+1,y+1,z) 3:(x,y+1,z), 4..7 the same at z+1
-                    uint32_t c = ((m[0] >> i) & 1u) | (((m[0] >> (i + 1)) & 1u) << 1) |
-                                 (((m[1] >> (i + 1)) & 1u) << 2) | (((m[1] >> i) & 1u) << 3) |
-                                 (((m[2] >> i) & 1u) << 4) | (((m[2] >> (i + 1)) & 1u) << 5) |
-                                 (((m[3] >> (i + 1)) & 1u) << 6) | (((m[3] >> i) & 1u) << 7);
-                    if (i >= lim) c = 0;
-                    cases[i] = c;
-                    n += s_ntri[c];
-                }
+                for (int i = 0; i < 8; ++i) n += s_ntri[((i < 4 ? clo : chi) >> (8 * (i & 3))) & 0xffu];
                 uint32_t inc = n;
 #pragma unroll
                 for (int o = 1; o < 32; o <<= 1) {
@@ -416,8 +431,6 @@ __global__ void __launch_bounds__(kSnThreads)
                     if (lane >= (unsigned)o) inc += t;
                 }
                 const uint32_t total = __shfl_sync(FULL, inc, 31);
-                const uint64_t tbase =
-                    plane_base[I.plane_index + z] - first_plane + unit_offsets[G.unit_base + unit * niso + iso_k];
                 // the step's triangles spread over the lanes: triangle q belongs to the
                 // first lane whose inclusive count exceeds q (binary search over lanes)
                 for (uint32_t q0 = 0; q0 < total; q0 += 32) {
@@ -431,9 +444,10 @@ __global__ void __launch_bounds__(kSnThreads)
                     }
                     const uint32_t owner = lo < 32 ? lo : 31;
                     const uint32_t first = __shfl_sync(FULL, inc - n, owner);
+                    const uint32_t olo = __shfl_sync(FULL, clo, owner), ohi = __shfl_sync(FULL, chi, owner);
                     uint32_t oc[8];
 #pragma unroll
-                    for (int i = 0; i < 8; ++i) oc[i] = __shfl_sync(FULL, cases[i], owner);
+                    for (int i = 0; i < 8; ++i) oc[i] = ((i < 4 ? olo : ohi) >> (8 * (i & 3))) & 0xffu;
                     if (q < total) {
                         // the owner's cell and triangle of local triangle r
                         uint32_t r = q - first, ci = 0, c = oc[0];
