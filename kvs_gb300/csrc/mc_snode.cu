@@ -42,7 +42,7 @@ constexpr unsigned FULL = 0xffffffffu;
 
 // resident CTAs per SM the node emit pass is compiled for (registers per thread)
 #ifndef KVSMC_SNODE_EMIT_CTAS
-#define KVSMC_SNODE_EMIT_CTAS 4
+#define KVSMC_SNODE_EMIT_CTAS 3
 #endif
 
 __host__ __device__ __forceinline__ size_t sn_align(size_t v) { return (v + 127) / 128 * 128; }
