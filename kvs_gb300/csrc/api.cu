@@ -526,7 +526,14 @@ kvsmc_status shared_count(kvsmc_context* ctx, const std::vector<Item*>& items, S
         ctx->arena3 = nullptr;
         ctx->arena3_bytes = 0;
         const size_t want = align_up(need, 1 << 20);
-        KVSMC_CUDA(ctx, cudaMalloc(&ctx->arena3, want));
+        if (cudaMalloc(&ctx->arena3, want) != cudaSuccess) {
+            // no room for the shared count: each request counts on its own
+            cudaGetLastError();
+            ctx->arena3 = nullptr;
+            sc.cand.clear();
+            sc.sb.reset();
+            return KVSMC_OK;
+        }
         ctx->arena3_bytes = want;
     }
     b.carve(static_cast<char*>(ctx->arena3));
