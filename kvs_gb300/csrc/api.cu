@@ -6,6 +6,7 @@
 #include <cstdarg>
 #include <cstdio>
 #include <cstring>
+#include <map>
 #include <memory>
 #include <string>
 #include <unordered_map>
@@ -246,6 +247,8 @@ struct Plan {
     // the request's vertex counts per node unit from that shared count (null:
     // the node count pass counts them)
     const uint32_t* sb_nodes = nullptr;
+    // its vertices and rank words were written by the multi-isolevel node emit
+    bool nodes_done = false;
 };
 
 uint32_t rows_for(uint32_t width, uint32_t limit)
@@ -281,9 +284,9 @@ void gather_plan(const Item& it, Plan& pl)
     j.words_per_row = (nx + 31) / 32;
 }
 
-// Count pass of one gather request: fills pl.ntri / pl.nvert and leaves the
-// per-tile offsets in the scratch arena for gather_emit.
-kvsmc_status gather_count(kvsmc_context* ctx, Plan& pl)
+// The pass shapes of one gather request (node units of the streaming node
+// passes, the streaming connection pass or the cell tiles).
+void gather_setup(kvsmc_context* ctx, Plan& pl)
 {
     pl.ntri = pl.nvert = 0;
     Job& j = pl.job;
@@ -320,15 +323,29 @@ kvsmc_status gather_count(kvsmc_context* ctx, Plan& pl)
             }
         }
     }
+}
+
+// Bytes of a set-up request's own count arrays (tiles, rank words, scans,
+// status words), its own streaming count excluded.
+size_t gather_own_bytes(const Plan& pl)
+{
+    const Job& j = pl.job;
     const size_t ct = j.cell_tiles, nt = j.node_tiles;
     const uint64_t rank_words = pl.shared ? (uint64_t)j.vol.nz * j.vol.ny * j.words_per_row : 0;
-    const size_t own = 10 * 256 + align_up(ct * 4, 256) + align_up(ct * 8, 256) + align_up(nt * 4, 256) +
-                       align_up(nt * 8, 256) + align_up(rank_words * 16, 256) +
-                       align_up(scan_scratch_bytes(ct), 256) + align_up(scan_scratch_bytes(nt), 256);
-    const size_t need = own + (pl.sconn && pl.batch ? align_up(pl.batch->scratch_bytes(), 256) : 0);
-    kvsmc_status st = ensure_scratch(ctx, need);
-    if (st) return st;
-    Carve cv{static_cast<char*>(ctx->scratch)};
+    return 10 * 256 + align_up(ct * 4, 256) + align_up(ct * 8, 256) + align_up(nt * 4, 256) + align_up(nt * 8, 256) +
+           align_up(rank_words * 16, 256) + align_up(scan_scratch_bytes(ct), 256) + align_up(scan_scratch_bytes(nt), 256);
+}
+
+// Count pass of one set-up request with its arrays carved from `base`
+// (gather_own_bytes, then its own streaming count): fills pl.ntri / pl.nvert
+// and leaves the per-tile offsets there for gather_emit.
+kvsmc_status gather_count_at(kvsmc_context* ctx, Plan& pl, char* base)
+{
+    Job& j = pl.job;
+    const size_t ct = j.cell_tiles, nt = j.node_tiles;
+    const uint64_t rank_words = pl.shared ? (uint64_t)j.vol.nz * j.vol.ny * j.words_per_row : 0;
+    const size_t own = gather_own_bytes(pl);
+    Carve cv{base};
     uint64_t* d_totals = cv.take<uint64_t>(256);
     j.tile_counts = cv.take<uint32_t>(ct * 4);
     j.tile_offsets = cv.take<uint64_t>(ct * 8);
@@ -343,7 +360,7 @@ kvsmc_status gather_count(kvsmc_context* ctx, Plan& pl)
     KVSMC_CUDA(ctx, cudaMemsetAsync(d_totals, 0, 3 * sizeof(uint64_t), ctx->stream));
     if (pl.sconn && pl.batch) {
         // unit counts, unit scan, plane scan: the streaming count of one request
-        pl.batch->carve(static_cast<char*>(ctx->scratch) + own);
+        pl.batch->carve(base + own);
         kvsmc_status bst = pl.batch->upload_tables();
         if (!bst) bst = pl.batch->count();
         if (bst) return bst;
@@ -374,6 +391,17 @@ kvsmc_status gather_count(kvsmc_context* ctx, Plan& pl)
         return fail(ctx, KVSMC_ERR_TOO_LARGE, "%llu shared vertices exceed 32-bit connection ids",
                     (unsigned long long)pl.nvert);
     return KVSMC_OK;
+}
+
+// Count pass of one gather request in the context's scratch arena.
+kvsmc_status gather_count(kvsmc_context* ctx, Plan& pl)
+{
+    gather_setup(ctx, pl);
+    const size_t need =
+        gather_own_bytes(pl) + (pl.sconn && pl.batch ? align_up(pl.batch->scratch_bytes(), 256) : 0);
+    kvsmc_status st = ensure_scratch(ctx, need);
+    if (st) return st;
+    return gather_count_at(ctx, pl, static_cast<char*>(ctx->scratch));
 }
 
 void gather_sizes(const Plan& pl, const Item& it, kvsmc_sizes* s)
@@ -442,7 +470,9 @@ kvsmc_status gather_emit(kvsmc_context* ctx, Plan& pl, float* coords, float* nor
         return KVSMC_OK;
     };
     kvsmc_status st = KVSMC_OK;
-    if (pl.nvert && pl.snode) {
+    if (pl.nodes_done) {
+        // written already
+    } else if (pl.nvert && pl.snode) {
         uint32_t* counts = const_cast<uint32_t*>(pl.sb_nodes ? pl.sb_nodes : j.vtile_counts);
         KVSMC_CUDA(ctx, kvsmc::launch_snode(true, j, pl.f, pl.wprn, pl.zchunk, pl.ntasks, counts, j.vtile_offsets,
                                             pl.d_status, pl.d_next + 1, L));
@@ -487,6 +517,13 @@ struct SharedCount {
         const uint32_t* nodes;
     };
     std::unordered_map<const Item*, Ref> ref;
+
+    // whether the request's group carries its vertex counts
+    bool has_nodes(const Item* it) const
+    {
+        const auto r = ref.find(it);
+        return r != ref.end() && r->second.nodes != nullptr;
+    }
 
     void attach(const Item* it, Plan& pl) const
     {
@@ -555,6 +592,104 @@ kvsmc_status shared_count(kvsmc_context* ctx, const std::vector<Item*>& items, S
     return KVSMC_OK;
 }
 
+// The requests of a shared count whose groups carry their vertex counts, run
+// together: each request's count arrays in its own part of the context's
+// fourth arena (they live until its connection pass), then (emit) the
+// device outputs from `outputs`, one node emit per group for all its
+// requests (k_snode_multi: the volume read once, every node classified once),
+// and each request's connections and vertex normals.  Per-request failures
+// go to it->status.
+kvsmc_status grouped_shared(kvsmc_context* ctx, const SharedCount& sc, std::vector<Item*>& items, bool emit,
+                            const std::function<kvsmc_status(std::vector<Item*>&)>& outputs)
+{
+    std::vector<Plan> plans(items.size());
+    size_t total = 0;
+    std::vector<size_t> off(items.size());
+    for (size_t i = 0; i < items.size(); ++i) {
+        gather_plan(*items[i], plans[i]);
+        sc.attach(items[i], plans[i]);
+        gather_setup(ctx, plans[i]);
+        off[i] = total;
+        total += align_up(gather_own_bytes(plans[i]), 256);
+    }
+    const size_t need = total + align_up((size_t)kvsmc::kStreamMaxIso * sizeof(kvsmc::NodeIso), 256);
+    if (need > ctx->arena4_bytes) {
+        KVSMC_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+        if (ctx->arena4) cudaFree(ctx->arena4);
+        ctx->arena4 = nullptr;
+        ctx->arena4_bytes = 0;
+        const size_t want = align_up(need, 1 << 20);
+        KVSMC_CUDA(ctx, cudaMalloc(&ctx->arena4, want));
+        ctx->arena4_bytes = want;
+    }
+    char* base = static_cast<char*>(ctx->arena4);
+    std::vector<Item*> ok;
+    for (size_t i = 0; i < items.size(); ++i) {
+        Item* it = items[i];
+        kvsmc_status st = gather_count_at(ctx, plans[i], base + off[i]);
+        if (!st) gather_sizes(plans[i], *it, &it->sizes);
+        if (st) it->status = st;
+        else ok.push_back(it);
+    }
+    if (!emit || ok.empty()) return KVSMC_OK;
+    if (kvsmc_status st = outputs(ok)) return st;
+    std::map<const Item*, Plan*> plan_of;
+    for (size_t i = 0; i < items.size(); ++i) plan_of[items[i]] = &plans[i];
+    // one node emit per group: its requests in threshold order
+    const StreamBatch& b = *sc.sb;
+    kvsmc::NodeIso* d_node = reinterpret_cast<kvsmc::NodeIso*>(base + total);
+    const kvsmc::Launch L = launch_of(ctx);
+    for (size_t g = 0; g < b.groups.size(); ++g) {
+        const kvsmc::StreamGroup& G = b.groups[g];
+        std::vector<Plan*> gp;
+        for (int k = 0; k < G.niso; ++k) {
+            Item* it = b.iso_item[G.iso_begin + k];
+            const auto f = plan_of.find(it);
+            if (f == plan_of.end() || it->status || !it->emit || !f->second->sb_nodes || !f->second->nvert) continue;
+            gp.push_back(f->second);
+        }
+        if (gp.empty()) continue;
+        kvsmc_status st = ensure_stage(ctx, gp.size() * sizeof(kvsmc::NodeIso));
+        if (!st) {
+            kvsmc::NodeIso* h = static_cast<kvsmc::NodeIso*>(ctx->h_stage);
+            for (size_t k = 0; k < gp.size(); ++k) {
+                const Plan& pl = *gp[k];
+                h[k].f = pl.f;
+                h[k].ip = pl.job.ip;
+                h[k].coords = pl.item->d_coords;
+                h[k].rank = pl.job.rank;
+                h[k].offsets = pl.job.vtile_offsets;
+                h[k].counts = pl.sb_nodes;
+            }
+            const Plan& p0 = *gp[0];
+            int* d_status = p0.d_status;
+            unsigned long long* d_next = p0.d_next + 1;
+            KVSMC_CUDA(ctx, cudaMemcpyAsync(d_node, h, gp.size() * sizeof(kvsmc::NodeIso), cudaMemcpyHostToDevice,
+                                            ctx->stream));
+            KVSMC_CUDA(ctx, cudaMemsetAsync(d_status, 0, sizeof(int), ctx->stream));
+            KVSMC_CUDA(ctx, cudaMemsetAsync(d_next, 0, sizeof(unsigned long long), ctx->stream));
+            KVSMC_CUDA(ctx, kvsmc::launch_snode_multi(p0.job.vol, d_node, (int)gp.size(), G.bs, G.bo, p0.wprn,
+                                                      p0.zchunk, p0.ntasks, p0.job.words_per_row, d_status, d_next, L));
+            int* hs = reinterpret_cast<int*>(ctx->h_small);
+            KVSMC_CUDA(ctx, cudaMemcpyAsync(hs, d_status, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
+            KVSMC_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+            if (*hs) st = fail(ctx, KVSMC_ERR_TIMEOUT, "shared-vertex node emit: a shared-memory load did not complete");
+        }
+        for (Plan* pl : gp) {
+            if (st) pl->item->status = st;
+            else pl->nodes_done = true;
+        }
+    }
+    for (size_t i = 0; i < items.size(); ++i) {
+        Item* it = items[i];
+        if (it->status || !it->emit) continue;
+        kvsmc_status st = gather_emit(ctx, plans[i], it->d_coords, it->d_normals, it->d_conn);
+        if (!st) KVSMC_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+        if (st) it->status = st;
+    }
+    return KVSMC_OK;
+}
+
 // ------------------------------------------------------------ request setup
 
 bool capacity_ok(const Item& it)
@@ -603,8 +738,29 @@ kvsmc_status run_items(kvsmc_context* ctx, std::vector<Item*>& items, bool emit)
         for (Item* it : sc.cand) it->status = st;
         if (!first) first = st;
     }
+    // requests whose group carries their vertex counts: one node emit per group
+    std::vector<Item*> grouped;
+    for (Item* it : gather_items)
+        if (!it->status && sc.has_nodes(it)) grouped.push_back(it);
+    if (!grouped.empty()) {
+        auto outputs = [&](std::vector<Item*>& its) -> kvsmc_status {
+            for (Item* it : its) {
+                if (!capacity_ok(*it))
+                    it->status = fail(ctx, KVSMC_ERR_CAPACITY, "output needs %llu coords, %llu normals, %llu connections",
+                                      (unsigned long long)it->sizes.ncoords, (unsigned long long)it->sizes.nnormals,
+                                      (unsigned long long)it->sizes.nconnections);
+                else
+                    it->emit = true;
+            }
+            return KVSMC_OK;
+        };
+        if (kvsmc_status st = grouped_shared(ctx, sc, grouped, emit, outputs))
+            for (Item* it : grouped)
+                if (!it->status) it->status = st;
+    }
     for (Item* it : gather_items) {
         if (it->status) continue;
+        if (sc.has_nodes(it)) continue;   // done above
         Plan pl;
         gather_plan(*it, pl);
         sc.attach(it, pl);
@@ -709,6 +865,7 @@ void kvsmc_destroy(kvsmc_context* ctx)
     if (ctx->out_arena) cudaFree(ctx->out_arena);
     if (ctx->arena2) cudaFree(ctx->arena2);
     if (ctx->arena3) cudaFree(ctx->arena3);
+    if (ctx->arena4) cudaFree(ctx->arena4);
     if (ctx->h_small) cudaFreeHost(ctx->h_small);
     if (ctx->h_stage) cudaFreeHost(ctx->h_stage);
     profiler_destroy(ctx->prof);
@@ -1114,8 +1271,25 @@ kvsmc_status kvsmc_extract_batch_host(kvsmc_context* ctx, const void* host, kvsm
         for (Item* it : sc.cand) it->status = st;
         if (!first) first = st;
     }
+    std::vector<Item*> grouped;
+    for (Item* it : g_items)
+        if (!it->status && sc.has_nodes(it)) grouped.push_back(it);
+    if (!grouped.empty()) {
+        auto outputs = [&](std::vector<Item*>& its) { return arena_outputs(ctx, its); };
+        if ((st = grouped_shared(ctx, sc, grouped, true, outputs)))
+            for (Item* it : grouped)
+                if (!it->status) it->status = st;
+        std::vector<Item*> done;
+        for (Item* it : grouped)
+            if (!it->status) done.push_back(it);
+        if (!done.empty() && (st = copy_back(ctx, done, items.data(), alloc, user)))
+            for (Item* it : done) it->status = st;
+        for (Item* it : grouped)
+            if (it->status && !first) first = it->status;
+    }
     for (Item* it : g_items) {
         if (it->status) continue;
+        if (sc.has_nodes(it)) continue;   // done above
         Plan pl;
         gather_plan(*it, pl);
         sc.attach(it, pl);

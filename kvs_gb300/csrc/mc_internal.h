@@ -137,6 +137,25 @@ cudaError_t launch_iso_totals(const StreamIso* d_isos, int n, const uint64_t* d_
 // exclusive scan of the counts) the rank words j.rank and the vertices
 // j.coords.  One isolevel; 8/16-bit and float32 volumes.
 size_t snode_shared_bytes(int dtype);
+
+// One request of the multi-isolevel node emit: a batch's shared-vertex
+// requests on one volume (at most kStreamMaxIso, sorted by threshold) written
+// by one pass over the volume.
+struct NodeIso {
+    FastIso f;
+    Interp ip;
+    float* coords;              // the request's vertices
+    uint4* rank;                // its rank words (nz * ny * words_per_row)
+    const uint64_t* offsets;    // per node unit: its first vertex id
+    const uint32_t* counts;     // per node unit: its vertices
+};
+size_t snode_multi_shared_bytes(int dtype);
+// vol: the volume; d_isos: niso requests; bs, bo: the bucket map of their
+// thresholds; wprn, zchunk, ntasks: the node-unit task shape of the single
+// request passes; words_per_row: rank words per node row.
+cudaError_t launch_snode_multi(const VolumeView& vol, const NodeIso* d_isos, int niso, float bs, float bo,
+                               uint32_t wprn, uint32_t zchunk, uint64_t ntasks, uint32_t words_per_row, int* status,
+                               unsigned long long* next_task, const Launch& L);
 cudaError_t launch_snode(bool emit, const Job& j, const FastIso& f, uint32_t wprn, uint32_t zchunk, uint64_t ntasks,
                          uint32_t* unit_counts, const uint64_t* unit_offsets, int* status,
                          unsigned long long* next_task, const Launch& L);

@@ -19,6 +19,7 @@
 
 #include "mc_internal.h"
 #include "mc_interp.cuh"
+#include "mc_thermo.cuh"
 #include "tma.cuh"
 
 namespace kvsmc {
@@ -252,6 +253,271 @@ __global__ void __launch_bounds__(kSnThreads, EMIT ? KVSMC_SNODE_EMIT_CTAS : 1)
         }
         // a normal walk acquires every staged plane: the last step's (z1 < nz) or
         // none more (z1 == nz); keep the parity in step with what was issued
+        while (acq < nplanes) {
+            if (!acquire(acq)) break;
+            ++acq;
+        }
+    }
+}
+
+
+// resident CTAs per SM the multi-isolevel node emit is compiled for
+#ifndef KVSMC_SNODE_MULTI_CTAS
+#define KVSMC_SNODE_MULTI_CTAS 3
+#endif
+
+// Per-warp tables of the multi-isolevel node emit: for each isolevel with
+// vertices in the current node unit (active index m, in threshold order), its
+// 32-node words' x/y/z crossing flags and first vertex within the unit, its
+// first item of the step, the isolevel and the unit's first vertex id.
+struct SnMulti {
+    uint32_t fx[kStreamMaxIso * 8], fy[kStreamMaxIso * 8], fz[kStreamMaxIso * 8];
+    uint32_t run[kStreamMaxIso * 8];
+    uint32_t first[kStreamMaxIso];
+    uint32_t iso[kStreamMaxIso];
+    uint64_t base[kStreamMaxIso];
+};
+
+// Per-CTA tables: the thresholds' bucket map and the requests' constants.
+struct SnMultiCta {
+    ThermoTables th;
+    NodeIso iso[kStreamMaxIso];
+};
+
+// calculate_isopoints for up to kStreamMaxIso requests on one volume in one
+// pass: the same tasks, ring and numbering as k_snode<T, true>, but each node
+// value is classified once for all the requests (threshold masks), the cut
+// edges of request k are bit k of the masks' XORs, and the step's vertices of
+// all the requests share the lanes.  Every request's ids and rank words are
+// the ones its own node emit writes.
+template <typename T>
+__global__ void __launch_bounds__(kSnThreads, KVSMC_SNODE_MULTI_CTAS)
+    k_snode_multi(VolumeView vol, const NodeIso* __restrict__ isos, int niso, float bs, float bo, uint32_t wprn,
+                  uint32_t zchunk, uint64_t ntasks, uint32_t row_elems, uint32_t copy_bytes, uint32_t words_per_row,
+                  int* __restrict__ status, unsigned long long* __restrict__ next_task, uint32_t wait_polls)
+{
+    extern __shared__ __align__(128) unsigned char smem_raw[];
+    const unsigned lane = threadIdx.x & 31u, warp = threadIdx.x >> 5;
+    SnMultiCta& C = *reinterpret_cast<SnMultiCta*>(smem_raw);
+    const size_t plane_elems = 2 * (size_t)row_elems;
+    const size_t ring_bytes = sn_align(3 * plane_elems * sizeof(T));
+    unsigned char* wbase =
+        smem_raw + sn_align(sizeof(SnMultiCta)) + (size_t)warp * (128 + ring_bytes + sn_align(sizeof(SnMulti)));
+    uint64_t* bar = reinterpret_cast<uint64_t*>(wbase);
+    T* ring = reinterpret_cast<T*>(wbase + 128);
+    SnMulti& M = *reinterpret_cast<SnMulti*>(wbase + 128 + ring_bytes);
+    if (warp == 0) {
+        float t = 0.0f;
+        if (lane < (unsigned)niso) t = isos[lane].f.f_thr;
+        __shared__ float s_thr[kStreamMaxIso];
+        if (lane < (unsigned)niso) s_thr[lane] = t;
+        __syncwarp();
+        thermo_build(C.th, s_thr, niso, bs, bo, lane);
+    }
+    for (unsigned i = threadIdx.x; i < (unsigned)niso; i += blockDim.x) C.iso[i] = isos[i];
+    __syncthreads();   // the only CTA-wide barrier: the tables are read-only from here on
+    if (lane == 0) {
+        for (int b = 0; b < 3; ++b) mbar_init(&bar[b], 1);
+        fence_barrier_init();
+    }
+    __syncwarp();
+    const uint32_t nx = vol.nx, ny = vol.ny, nz = vol.nz;
+    const uint64_t pitch = vol.pitch, slice = vol.slice;
+    const T* vp = static_cast<const T*>(vol.data);
+    uint32_t ph = 0;
+    for (;;) {
+        unsigned long long tk = 0;
+        if (lane == 0) tk = atomicAdd(next_task, 1ull);
+        const uint64_t task = __shfl_sync(FULL, tk, 0);
+        if (task >= ntasks) break;
+        const uint32_t s = (uint32_t)(task % wprn);
+        const uint32_t y = (uint32_t)((task / wprn) % ny);
+        const uint32_t zc = (uint32_t)(task / ((uint64_t)wprn * ny));
+        const uint32_t z0 = zc * zchunk;
+        const uint32_t z1 = z0 + zchunk < nz ? z0 + zchunk : nz;            // node planes [z0, z1)
+        const uint32_t nplanes = (z1 + 1 < nz ? z1 + 1 : nz) - z0;          // staged planes
+        const uint32_t nrows = y + 1 < ny ? 2u : 1u;
+        const uint64_t xoff = (uint64_t)s * kSnSeg;
+        const uint64_t avail = (pitch - xoff) * sizeof(T);
+        const uint32_t row_bytes = (uint32_t)(avail < copy_bytes ? avail : copy_bytes);
+        auto issue = [&](uint32_t i) {
+            const int b = (int)(i % 3u);
+            T* dst = ring + (size_t)b * plane_elems;
+            const T* src = vp + (uint64_t)(z0 + i) * slice + (uint64_t)y * pitch + xoff;
+            mbar_arrive_expect_tx(&bar[b], nrows * row_bytes);
+            for (uint32_t r = 0; r < nrows; ++r) bulk_copy_g2s(dst + r * row_elems, src + r * pitch, row_bytes, &bar[b]);
+        };
+        auto acquire = [&](uint32_t i) -> bool {
+            const uint32_t b = i % 3u;
+            const bool ok = mbar_wait(&bar[b], (ph >> b) & 1u, wait_polls);
+            if (ok) ph ^= 1u << b;
+            return ok;
+        };
+        __syncwarp();   // the previous task's reads of the ring are done
+        if (lane == 0) {
+            fence_proxy_async();
+            for (uint32_t i = 0; i < nplanes && i < 3; ++i) issue(i);
+        }
+        uint32_t acq = 0, issued = 0;
+        bool dead = false;
+        // lane k < niso: request k's vertex count and first id of the unit,
+        // loaded one step ahead
+        auto unit_of = [&](uint32_t zz) -> uint64_t { return ((uint64_t)zz * ny + y) * wprn + s; };
+        uint32_t next_n = 0;
+        uint64_t next_base = 0;
+        if (lane < (unsigned)niso) {
+            next_n = C.iso[lane].counts[unit_of(z0)];
+            next_base = C.iso[lane].offsets[unit_of(z0)];
+        }
+        const float fyf = __uint2float_rn(y);
+        for (uint32_t z = z0; z < z1; ++z) {
+            const uint32_t st = z - z0;
+            const uint32_t need = z + 1 < nz ? st + 1 : st;   // last plane staged this step
+            const uint32_t n_now = next_n;
+            const uint64_t base_now = next_base;
+            if (z + 1 < z1 && lane < (unsigned)niso) {
+                next_n = C.iso[lane].counts[unit_of(z + 1)];
+                next_base = C.iso[lane].offsets[unit_of(z + 1)];
+            }
+            bool ok = true;
+            while (ok && acq <= need) {
+                ok = acquire(acq);
+                if (ok) ++acq;
+            }
+            if (__any_sync(FULL, !ok)) {
+                if (lane == 0) atomicExch(status, 1);
+                dead = true;
+                issued = st + 3 < nplanes ? st + 3 : nplanes;
+                break;
+            }
+            const uint32_t act = __ballot_sync(FULL, lane < (unsigned)niso && n_now != 0);
+            if (act) {
+                const T* ra = ring + (size_t)(st % 3u) * plane_elems;            // plane z, row y
+                const T* rb = ra + row_elems;                                     // plane z, row y + 1
+                const T* rz = ring + (size_t)((st + 1) % 3u) * plane_elems;      // plane z + 1, row y
+                const bool has_y = y + 1 < ny, has_z = z + 1 < nz;
+                // per node lane + 32 i: the requests whose isolevel its x, y, z edges
+                // cross (XOR of the two ends' masks), two nodes per word
+                uint32_t CX[4] = {0, 0, 0, 0}, CY[4] = {0, 0, 0, 0}, CZ[4] = {0, 0, 0, 0};
+#pragma unroll
+                for (int i = 0; i < 8; ++i) {
+                    const uint32_t xl = lane + 32u * i;
+                    const uint64_t x = xoff + xl;
+                    uint32_t cx = 0, cy = 0, cz = 0;
+                    if (x < nx) {
+                        const uint32_t a = thermo_mask(C.th, niso, bs, bo, (float)ra[xl]);
+                        if (x + 1 < nx) cx = a ^ thermo_mask(C.th, niso, bs, bo, (float)ra[xl + 1]);
+                        if (has_y) cy = a ^ thermo_mask(C.th, niso, bs, bo, (float)rb[xl]);
+                        if (has_z) cz = a ^ thermo_mask(C.th, niso, bs, bo, (float)rz[xl]);
+                    }
+                    CX[i >> 1] |= cx << (16 * (i & 1));
+                    CY[i >> 1] |= cy << (16 * (i & 1));
+                    CZ[i >> 1] |= cz << (16 * (i & 1));
+                }
+                const uint64_t row = (uint64_t)z * ny + y;
+                uint32_t total = 0, nact = 0;
+                for (uint32_t rem = act; rem; rem &= rem - 1) {
+                    const uint32_t k = __ffs(rem) - 1;
+                    const uint64_t base = __shfl_sync(FULL, base_now, k);
+                    uint32_t wx[8], wy[8], wz[8], wrun[8];
+                    uint32_t tot = 0;
+#pragma unroll
+                    for (int i = 0; i < 8; ++i) {
+                        const uint32_t sh = k + 16u * (uint32_t)(i & 1);
+                        wx[i] = __ballot_sync(FULL, (CX[i >> 1] >> sh) & 1u);
+                        wy[i] = __ballot_sync(FULL, (CY[i >> 1] >> sh) & 1u);
+                        wz[i] = __ballot_sync(FULL, (CZ[i >> 1] >> sh) & 1u);
+                        wrun[i] = tot;
+                        tot += __popc(wx[i]) + __popc(wy[i]) + __popc(wz[i]);
+                    }
+                    // lane i < 8: word i's rank word, and the same words for the items below
+                    uint32_t mx = 0, my = 0, mz = 0, mr = 0;
+#pragma unroll
+                    for (int i = 0; i < 8; ++i)
+                        if ((int)lane == i) { mx = wx[i]; my = wy[i]; mz = wz[i]; mr = wrun[i]; }
+                    if (lane < 8) {
+                        const uint64_t word = (uint64_t)s * (kSnSeg / 32) + lane;
+                        if (word < words_per_row)
+                            C.iso[k].rank[row * words_per_row + word] = make_uint4(mx, my, mz, (uint32_t)(base + mr));
+                        M.fx[nact * 8 + lane] = mx;
+                        M.fy[nact * 8 + lane] = my;
+                        M.fz[nact * 8 + lane] = mz;
+                        M.run[nact * 8 + lane] = mr;
+                    }
+                    if (lane == 0) {
+                        M.first[nact] = total;
+                        M.iso[nact] = k;
+                        M.base[nact] = base;
+                    }
+                    total += tot;
+                    ++nact;
+                }
+                __syncwarp();
+                // the step's vertices of all the requests spread over the lanes: item
+                // q belongs to active request m (the last whose first item <= q)
+                const float fzf = __uint2float_rn(z);
+                for (uint32_t q = lane; q < total; q += 32) {
+                    uint32_t m = 0;
+#pragma unroll
+                    for (uint32_t step = 8; step >= 1; step >>= 1)
+                        if (m + step < nact && M.first[m + step] <= q) m += step;
+                    const uint32_t r0q = q - M.first[m];
+                    // its word: the last i with run[i] <= r0q (words without items share
+                    // the next word's start, so the last such i holds items)
+                    const uint4 ra4 = *reinterpret_cast<const uint4*>(&M.run[m * 8]);
+                    const uint4 rb4 = *reinterpret_cast<const uint4*>(&M.run[m * 8 + 4]);
+                    const uint32_t runs[8] = {ra4.x, ra4.y, ra4.z, ra4.w, rb4.x, rb4.y, rb4.z, rb4.w};
+                    uint32_t wi = 0;
+#pragma unroll
+                    for (uint32_t i = 1; i < 8; ++i)
+                        if (runs[i] <= r0q) wi = i;
+                    const uint32_t bx = M.fx[m * 8 + wi], by = M.fy[m * 8 + wi], bz = M.fz[m * 8 + wi];
+                    const uint32_t r = r0q - M.run[m * 8 + wi];
+                    // its node: the last lane L whose flags before it (all axes) are at most r
+                    uint32_t lo = 0;
+#pragma unroll
+                    for (int b = 4; b >= 0; --b) {
+                        const uint32_t mid = lo + (1u << b);
+                        const uint32_t ltm = (1u << mid) - 1u;   // mid <= 31
+                        if ((uint32_t)(__popc(bx & ltm) + __popc(by & ltm) + __popc(bz & ltm)) <= r) lo = mid;
+                    }
+                    const uint32_t L = lo;
+                    const uint32_t ltl = (1u << L) - 1u;
+                    uint32_t kk = r - (__popc(bx & ltl) + __popc(by & ltl) + __popc(bz & ltl));   // kk-th flag of L
+                    const uint32_t nf = ((bx >> L) & 1u) | (((by >> L) & 1u) << 1) | (((bz >> L) & 1u) << 2);
+                    int axis = 0;
+                    for (; axis < 3; ++axis)
+                        if ((nf >> axis) & 1u) {
+                            if (kk == 0) break;
+                            --kk;
+                        }
+                    const uint32_t xl = L + 32u * wi;
+                    const float ax = __uint2float_rn((uint32_t)xoff + xl);
+                    const float v0 = (float)ra[xl];
+                    const float v1 = (float)(axis == 0 ? ra[xl + 1] : (axis == 1 ? rb[xl] : rz[xl]));
+                    const float bxf = axis == 0 ? __fadd_rn(ax, 1.0f) : ax;
+                    const float byf = axis == 1 ? __fadd_rn(fyf, 1.0f) : fyf;
+                    const float bzf = axis == 2 ? __fadd_rn(fzf, 1.0f) : fzf;
+                    const NodeIso& I = C.iso[M.iso[m]];
+                    const float3 p = edge_vertex_fast(I.ip, I.f, v0, v1, ax, fyf, fzf, bxf, byf, bzf, axis);
+                    float* o = I.coords + 3 * (M.base[m] + r0q);
+                    o[0] = p.x; o[1] = p.y; o[2] = p.z;
+                }
+            }
+            // plane z is consumed: refill its buffer with plane z + 3
+            __syncwarp();
+            if (lane == 0 && st + 3 < nplanes) {
+                fence_proxy_async();
+                issue(st + 3);
+            }
+        }
+        if (dead) {
+            for (uint32_t i = acq; i < issued; ++i) {
+                const uint32_t b = i % 3u;
+                if (mbar_wait(&bar[b], (ph >> b) & 1u, 1u << 16)) ph ^= 1u << b;
+            }
+            break;
+        }
         while (acq < nplanes) {
             if (!acquire(acq)) break;
             ++acq;
@@ -550,6 +816,42 @@ size_t snode_shared_bytes(int dtype)
     const size_t es = dtype_size(dtype);
     const size_t plane = 2 * stream_row_elems(dtype, 1) * es;
     return (size_t)kSnWarps * (128 + sn_align(3 * plane));
+}
+
+size_t snode_multi_shared_bytes(int dtype)
+{
+    const size_t es = dtype_size(dtype);
+    const size_t plane = 2 * stream_row_elems(dtype, 1) * es;
+    return sn_align(sizeof(SnMultiCta)) + (size_t)kSnWarps * (128 + sn_align(3 * plane) + sn_align(sizeof(SnMulti)));
+}
+
+cudaError_t launch_snode_multi(const VolumeView& vol, const NodeIso* d_isos, int niso, float bs, float bo,
+                               uint32_t wprn, uint32_t zchunk, uint64_t ntasks, uint32_t words_per_row, int* status,
+                               unsigned long long* next_task, const Launch& L)
+{
+    if (ntasks == 0) return cudaSuccess;
+    if (niso < 1 || niso > kStreamMaxIso) return cudaErrorInvalidValue;
+    const int dt = vol.dtype;
+    const size_t smem = snode_multi_shared_bytes(dt);
+    const uint32_t row_elems = (uint32_t)stream_row_elems(dt, 1);
+    const uint32_t copy_bytes = row_elems * (uint32_t)dtype_size(dt);
+    KVSMC_SN_SWITCH(dt, {
+        auto kern = k_snode_multi<T>;
+        cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        int per_sm = 0;
+        if (e == cudaSuccess) e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, kSnThreads, smem);
+        if (e != cudaSuccess) return e;
+        const uint64_t resident = (uint64_t)(per_sm > 0 ? per_sm : 1) * (uint64_t)L.num_sms;
+        const uint64_t need = (ntasks + kSnWarps - 1) / kSnWarps;
+        const uint64_t nctas = need < resident ? need : resident;
+        prof_begin(L, "snode_emit_multi");
+        kern<<<(unsigned)nctas, kSnThreads, smem, L.stream>>>(vol, d_isos, niso, bs, bo, wprn, zchunk, ntasks,
+                                                                row_elems, copy_bytes, words_per_row, status,
+                                                                next_task, L.wait_polls[1]);
+        prof_end(L);
+    });
+    *L.counter += 1;
+    return cudaGetLastError();
 }
 
 cudaError_t launch_snode(bool emit, const Job& j, const FastIso& f, uint32_t wprn, uint32_t zchunk, uint64_t ntasks,

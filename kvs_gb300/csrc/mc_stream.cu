@@ -37,6 +37,7 @@
 
 #include "mc_internal.h"
 #include "mc_interp.cuh"
+#include "mc_thermo.cuh"
 #include "tma.cuh"
 
 #ifndef KVSMC_VERTS_PER_LANE
@@ -116,8 +117,6 @@ template <> __device__ __forceinline__ void load8<int8_t>(const int8_t* row, uin
 
 // ------------------------------------------------------------ shared layout
 
-constexpr int kLut = kStreamBuckets + 1;   // bucket indices 0 .. kStreamBuckets
-constexpr uint32_t kMultiThr = 1u << 31;   // LUT flag: two or more thresholds lie in this bucket
 constexpr int kMaxVerts = KVSMC_EMIT_MAX_VERTS;   // vertex items of one round (rounds end before it is exceeded)
 static_assert(kMaxVerts >= 12 && kMaxVerts <= 256, "a round holds one pair's 12 edges; item maps are 8-bit");
 constexpr int kMaxTris = 32 * 5;           // triangle items of one round (5 per pair at most)
@@ -277,21 +276,6 @@ __device__ __forceinline__ EdgeItem edge_item(const Tables& TB, uint32_t qe, uin
 }
 
 __host__ __device__ __forceinline__ size_t align128(size_t v) { return (v + 127) / 128 * 128; }
-
-// Monotone (non-decreasing) bucket of a value in [0, kStreamBuckets]:
-// floor(kStreamBuckets * sat(v * bs + bo)).  Thresholds and node values go
-// through exactly this function, so a threshold in a lower bucket than v is
-// below v, one in a higher bucket is not, and only a shared bucket needs an
-// exact compare.  NaN saturates to 0 (the fma's .sat flushes NaN to +0): it
-// is above no threshold, as in the reference's double compare.
-__device__ __forceinline__ uint32_t bucket_index(float v, float bs, float bo)
-{
-    float u;
-    asm("fma.rn.sat.f32 %0, %1, %2, %3;" : "=f"(u) : "f"(v), "f"(bs), "f"(bo));
-    // u * NB + 2^23 rounded down: 2^23 + floor(u * NB) exactly
-    const float t = __fmaf_rd(u, (float)kStreamBuckets, 8388608.0f);
-    return (uint32_t)__float_as_int(t) - 0x4B000000u;
-}
 
 // Thermometer masks of the 9 nodes x0 .. x0+8 of a staged row: bit k set when
 // the value is above isolevel k's threshold (v > t_k; thresholds sorted, so

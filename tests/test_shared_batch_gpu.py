@@ -1,10 +1,11 @@
 """Batches of shared-vertex requests: one streaming triangle count for all of them.
 
 kvsmc_extract_batch / kvsmc_count_batch / kvsmc_extract_batch_host count the
-triangles of every shared-vertex request of a batch (PolygonNormal without
-duplication, VertexNormal) in one streaming pass per volume group (up to 16
-isolevels share one read of the volume), and each request's connection pass
-takes its isolevel's offsets from that count.  The results must be the
+triangles and vertices of every shared-vertex request of a batch (PolygonNormal
+without duplication, VertexNormal) in one streaming pass per volume group (up
+to 16 isolevels share one read of the volume), write the group's vertices and
+rank words in one node emit pass, and each request's connection pass takes its
+isolevel's offsets from that count.  The results must be the
 oracle's (oracle/mc_oracle.c) bit for bit, and equal each request run alone
 (which counts on its own), including volumes that do not take the shared
 count (two rows per task), more than 16 isolevels on one volume, mixed modes
@@ -78,17 +79,19 @@ def test_shared_batch_equals_alone(kvsmc_ctx):
 
 
 def test_shared_batch_count_timeout_and_recovery():
-    """The shared count's plane waits give up with KVSMC_ERR_TIMEOUT for every
-    request it covers; the next batch on the same context is exact again."""
+    """The shared count's plane waits, then the grouped node emit's, give up
+    with KVSMC_ERR_TIMEOUT for every request they cover; the next batch on the
+    same context is exact again."""
     v = S.to_numpy(S.fbm((30, 40, 150), seed=3, device="cuda"))
     ctx = _abi.Context(0)
     vol = _abi.DeviceVolume.upload(ctx, v)
     params = [_abi.make_params(x, _abi.MODE_SHARED_VERTEX_NORMAL) for x in (0.4, 0.5, 0.6)]
     ref = [extract_batch(ctx, [vol], [p], _abi.PATH_AUTO)[0] for p in params]
-    ctx.set_wait_limit(0, -1)
-    with pytest.raises(_abi.KvsmcError) as e:
-        extract_batch(ctx, [vol] * 3, params, _abi.PATH_AUTO)
-    assert e.value.status == _abi.ERR_TIMEOUT
+    for limits in ((0, -1), (-1, 0)):
+        ctx.set_wait_limit(*limits)
+        with pytest.raises(_abi.KvsmcError) as e:
+            extract_batch(ctx, [vol] * 3, params, _abi.PATH_AUTO)
+        assert e.value.status == _abi.ERR_TIMEOUT
     ctx.set_wait_limit(-1, -1)
     got = extract_batch(ctx, [vol] * 3, params, _abi.PATH_AUTO)
     for a, b in zip(got, ref):
