@@ -2,6 +2,7 @@
 // volumes, and request pipelines.  Duplicated-mode requests on 8/16-bit and
 // float32 volumes run through the streaming kernels (batch.cu); the others
 // through the gather kernels (mc_gather.cu), one request at a time.
+#include <algorithm>
 #include <cmath>
 #include <cstdarg>
 #include <cstdio>
@@ -249,6 +250,11 @@ struct Plan {
     const uint32_t* sb_nodes = nullptr;
     // its vertices and rank words were written by the multi-isolevel node emit
     bool nodes_done = false;
+    // its connections and (per-triangle) normals were written by the
+    // multi-isolevel connection pass; tri_normals: where its per-triangle
+    // normals are (VertexNormal), kept until its vertex normals
+    bool conn_done = false;
+    float* tri_normals = nullptr;
 };
 
 uint32_t rows_for(uint32_t width, uint32_t limit)
@@ -456,6 +462,7 @@ kvsmc_status gather_emit(kvsmc_context* ctx, Plan& pl, float* coords, float* nor
             ctx->arena2_bytes = want;
         }
         kvsmc::vertex_normals_carve(j, pl.ntri, pl.nvert, ctx->arena2, &vn_scan, &vn_total);
+        if (pl.conn_done) j.tri_normals = pl.tri_normals;   // written by the connection pass already
     } else {
         j.tri_normals = nullptr;
     }
@@ -480,7 +487,9 @@ kvsmc_status gather_emit(kvsmc_context* ctx, Plan& pl, float* coords, float* nor
     } else if (pl.nvert) {
         KVSMC_CUDA(ctx, launch_node_emit(j, L));
     }
-    if (pl.ntri && pl.sconn) {
+    if (pl.conn_done) {
+        // written already
+    } else if (pl.ntri && pl.sconn) {
         StreamBatch& b = *pl.sb;
         KVSMC_CUDA(ctx, kvsmc::launch_sconnect(j, b.d_groups + pl.sb_group, b.d_isos, b.d_unit_counts,
                                                b.d_unit_offsets, b.d_plane_base, pl.sb_iso, pl.sb_tasks, pl.nvert,
@@ -612,7 +621,9 @@ kvsmc_status grouped_shared(kvsmc_context* ctx, const SharedCount& sc, std::vect
         off[i] = total;
         total += align_up(gather_own_bytes(plans[i]), 256);
     }
-    const size_t need = total + align_up((size_t)kvsmc::kStreamMaxIso * sizeof(kvsmc::NodeIso), 256);
+    const size_t tables = align_up((size_t)kvsmc::kStreamMaxIso * sizeof(kvsmc::NodeIso), 256) +
+                          align_up((size_t)kvsmc::kStreamMaxIso * sizeof(kvsmc::ConnIso), 256);
+    const size_t need = total + tables;
     if (need > ctx->arena4_bytes) {
         KVSMC_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
         if (ctx->arena4) cudaFree(ctx->arena4);
@@ -633,11 +644,36 @@ kvsmc_status grouped_shared(kvsmc_context* ctx, const SharedCount& sc, std::vect
     }
     if (!emit || ok.empty()) return KVSMC_OK;
     if (kvsmc_status st = outputs(ok)) return st;
+    // the VertexNormal requests' per-triangle normals, written by the
+    // connection pass, summed by their vertex normals afterwards
+    size_t tn_total = 0;
+    for (size_t i = 0; i < items.size(); ++i)
+        if (!items[i]->status && items[i]->emit && plans[i].job.mode == KVSMC_SHARED_VERTEX_NORMAL)
+            tn_total += align_up(12 * plans[i].ntri, 256);
+    if (tn_total > ctx->arena5_bytes) {
+        KVSMC_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+        if (ctx->arena5) cudaFree(ctx->arena5);
+        ctx->arena5 = nullptr;
+        ctx->arena5_bytes = 0;
+        const size_t want = align_up(tn_total, 1 << 20);
+        KVSMC_CUDA(ctx, cudaMalloc(&ctx->arena5, want));
+        ctx->arena5_bytes = want;
+    }
+    {
+        size_t o = 0;
+        for (size_t i = 0; i < items.size(); ++i)
+            if (!items[i]->status && items[i]->emit && plans[i].job.mode == KVSMC_SHARED_VERTEX_NORMAL) {
+                plans[i].tri_normals = reinterpret_cast<float*>(static_cast<char*>(ctx->arena5) + o);
+                o += align_up(12 * plans[i].ntri, 256);
+            }
+    }
     std::map<const Item*, Plan*> plan_of;
     for (size_t i = 0; i < items.size(); ++i) plan_of[items[i]] = &plans[i];
     // one node emit per group: its requests in threshold order
     const StreamBatch& b = *sc.sb;
     kvsmc::NodeIso* d_node = reinterpret_cast<kvsmc::NodeIso*>(base + total);
+    kvsmc::ConnIso* d_conn = reinterpret_cast<kvsmc::ConnIso*>(
+        base + total + align_up((size_t)kvsmc::kStreamMaxIso * sizeof(kvsmc::NodeIso), 256));
     const kvsmc::Launch L = launch_of(ctx);
     for (size_t g = 0; g < b.groups.size(); ++g) {
         const kvsmc::StreamGroup& G = b.groups[g];
@@ -674,10 +710,52 @@ kvsmc_status grouped_shared(kvsmc_context* ctx, const SharedCount& sc, std::vect
             KVSMC_CUDA(ctx, cudaMemcpyAsync(hs, d_status, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
             KVSMC_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
             if (*hs) st = fail(ctx, KVSMC_ERR_TIMEOUT, "shared-vertex node emit: a shared-memory load did not complete");
+            // then the group's connection pass, every request of the group in its
+            // isolevel order (the ones not written here disabled)
+            if (!st) st = ensure_stage(ctx, (size_t)G.niso * sizeof(kvsmc::ConnIso));
+            if (!st) {
+                kvsmc::ConnIso* hc = static_cast<kvsmc::ConnIso*>(ctx->h_stage);
+                std::memset(hc, 0, (size_t)G.niso * sizeof(kvsmc::ConnIso));
+                uint64_t tasks = 0;
+                for (int k = 0; k < G.niso; ++k) {
+                    Item* it = b.iso_item[G.iso_begin + k];
+                    const auto f = plan_of.find(it);
+                    if (f == plan_of.end()) continue;
+                    const Plan& pl = *f->second;
+                    if (std::find(gp.begin(), gp.end(), f->second) == gp.end() || !pl.ntri) continue;
+                    hc[k].rank = pl.job.rank;
+                    hc[k].coords = it->d_coords;
+                    hc[k].connections = it->d_conn;
+                    hc[k].tri_out = pl.job.mode == KVSMC_SHARED_VERTEX_NORMAL ? pl.tri_normals : it->d_normals;
+                    hc[k].nvert = pl.nvert;
+                    hc[k].ntri = pl.ntri;
+                    hc[k].enabled = 1;
+                    tasks = pl.sb_tasks;
+                }
+                if (tasks) {
+                    KVSMC_CUDA(ctx, cudaMemcpyAsync(d_conn, hc, (size_t)G.niso * sizeof(kvsmc::ConnIso),
+                                                    cudaMemcpyHostToDevice, ctx->stream));
+                    KVSMC_CUDA(ctx, cudaMemsetAsync(d_status, 0, sizeof(int), ctx->stream));
+                    KVSMC_CUDA(ctx, cudaMemsetAsync(d_next, 0, sizeof(unsigned long long), ctx->stream));
+                    KVSMC_CUDA(ctx, kvsmc::launch_sconnect_multi(b.d_groups + g, b.d_isos, d_conn, p0.job.vol.dtype,
+                                                                 b.d_unit_counts, b.d_unit_offsets, b.d_plane_base,
+                                                                 tasks, d_status, d_next, L));
+                    KVSMC_CUDA(ctx, cudaMemcpyAsync(hs, d_status, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
+                    KVSMC_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+                    if (*hs == 1)
+                        st = fail(ctx, KVSMC_ERR_TIMEOUT, "shared-vertex connections: a shared-memory load did not complete");
+                    else if (*hs)
+                        st = fail(ctx, KVSMC_ERR_CUDA, "shared-vertex connections: a vertex id out of range");
+                }
+            }
         }
         for (Plan* pl : gp) {
-            if (st) pl->item->status = st;
-            else pl->nodes_done = true;
+            if (st) {
+                pl->item->status = st;
+            } else {
+                pl->nodes_done = true;
+                pl->conn_done = pl->ntri != 0;
+            }
         }
     }
     for (size_t i = 0; i < items.size(); ++i) {
@@ -866,6 +944,7 @@ void kvsmc_destroy(kvsmc_context* ctx)
     if (ctx->arena2) cudaFree(ctx->arena2);
     if (ctx->arena3) cudaFree(ctx->arena3);
     if (ctx->arena4) cudaFree(ctx->arena4);
+    if (ctx->arena5) cudaFree(ctx->arena5);
     if (ctx->h_small) cudaFreeHost(ctx->h_small);
     if (ctx->h_stage) cudaFreeHost(ctx->h_stage);
     profiler_destroy(ctx->prof);

@@ -35,6 +35,8 @@ struct kvsmc_context {
     size_t arena3_bytes = 0;
     void* arena4 = nullptr;      // grow-only fourth arena (grouped shared-vertex requests' count arrays)
     size_t arena4_bytes = 0;
+    void* arena5 = nullptr;      // grow-only fifth arena (their per-triangle normals)
+    size_t arena5_bytes = 0;
     size_t out_bytes = 0;
     kvsmc_volume* host_vol = nullptr;  // staging volume of the host call
     uint64_t* h_small = nullptr; // pinned: small read-backs (totals, min/max, status)

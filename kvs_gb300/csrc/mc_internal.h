@@ -150,6 +150,24 @@ struct NodeIso {
     const uint32_t* counts;     // per node unit: its vertices
 };
 size_t snode_multi_shared_bytes(int dtype);
+
+// One request of the multi-isolevel connection pass (the requests of one
+// streaming count group, in its isolevel order).
+struct ConnIso {
+    const uint4* rank;       // its rank words
+    const float* coords;     // its vertices
+    uint32_t* connections;   // its triangles' vertex ids
+    float* tri_out;          // polygon normals, or the per-triangle normals its vertex normals sum
+    uint64_t nvert, ntri;
+    uint32_t enabled;        // 0: nothing of it is written
+    uint32_t pad;
+};
+size_t sconnect_multi_shared_bytes(int dtype);
+// The connection pass of every enabled request of streaming count group
+// d_group (one-row tasks) at once: the group's tasks, its counters and scans.
+cudaError_t launch_sconnect_multi(const StreamGroup* d_group, const StreamIso* d_isos, const ConnIso* d_conn, int dtype,
+                                  const uint16_t* unit_counts, const uint32_t* unit_offsets, const uint64_t* plane_base,
+                                  uint64_t ntasks, int* status, unsigned long long* next_task, const Launch& L);
 // vol: the volume; d_isos: niso requests; bs, bo: the bucket map of their
 // thresholds; wprn, zchunk, ntasks: the node-unit task shape of the single
 // request passes; words_per_row: rank words per node row.

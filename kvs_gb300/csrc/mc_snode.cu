@@ -775,6 +775,328 @@ __global__ void __launch_bounds__(kSnThreads)
     }
 }
 
+
+// ------------------------------------------------------------------
+// connect_isopoints for up to kStreamMaxIso requests on one volume in one pass
+// (the requests of one streaming count group): the cell tasks of k_sconnect,
+// each cell classified once for all the requests by threshold masks, the
+// step's active (cell, request) pairs taken 32 at a time, one lane per
+// triangle.  Every request's connections and normals are the ones its own
+// connection pass writes.
+
+constexpr int kScPairCap = 128;   // listed (cell, request) pairs per warp at a time
+
+struct ScMultiCta {
+    ThermoTables th;
+    ConnIso iso[kStreamMaxIso];
+    uint64_t tri[256];   // per reference case: edges per triangle, 4 bits each
+    uint8_t ntri[256];
+    uint8_t edge[16];
+};
+
+struct ScMultiWarp {
+    uint32_t pairs[kScPairCap];   // cell | request << 8 | corner code << 16
+    uint32_t run[kStreamMaxIso];  // per request: triangles of the unit written so far this step
+    uint32_t add[kStreamMaxIso];
+    uint8_t item[32 * 5];         // triangle -> its pair's lane, one round
+};
+
+// Vertex id of node (x, y, z)'s edge along `axis` from a request's rank words.
+__device__ __forceinline__ uint32_t sc_rank_id_of(const uint4* rank, uint32_t ny, uint32_t words_per_row, uint32_t x,
+                                                  uint32_t y, uint32_t z, int axis)
+{
+    const uint4 R = rank[((uint64_t)z * ny + y) * words_per_row + (x >> 5)];
+    const uint32_t bit = x & 31u, lt = (1u << bit) - 1u;
+    uint32_t id = R.w + __popc(R.x & lt) + __popc(R.y & lt) + __popc(R.z & lt);
+    if (axis >= 1) id += (R.x >> bit) & 1u;
+    if (axis >= 2) id += (R.y >> bit) & 1u;
+    return id;
+}
+
+template <typename T>
+__global__ void __launch_bounds__(kSnThreads, 3)
+    k_sconnect_multi(const StreamGroup* __restrict__ groups, const StreamIso* __restrict__ isos,
+                     const ConnIso* __restrict__ conn, const uint16_t* __restrict__ unit_counts,
+                     const uint32_t* __restrict__ unit_offsets, const uint64_t* __restrict__ plane_base,
+                     uint64_t ntasks, int* __restrict__ status, unsigned long long* __restrict__ next_task,
+                     uint32_t wait_polls)
+{
+    extern __shared__ __align__(128) unsigned char smem_raw[];
+    const unsigned tid = threadIdx.x, lane = tid & 31u, warp = tid >> 5;
+    const StreamGroup& G = groups[0];
+    const int niso = G.niso;
+    const float bs = G.bs, bo = G.bo;
+    ScMultiCta& C = *reinterpret_cast<ScMultiCta*>(smem_raw);
+    const uint32_t row_elems = G.seg_elems;
+    const size_t plane_elems = 2 * (size_t)row_elems;
+    const size_t ring_bytes = sn_align(3 * plane_elems * sizeof(T));
+    unsigned char* wbase =
+        smem_raw + sn_align(sizeof(ScMultiCta)) + (size_t)warp * (128 + ring_bytes + sn_align(sizeof(ScMultiWarp)));
+    uint64_t* bar = reinterpret_cast<uint64_t*>(wbase);
+    T* ring = reinterpret_cast<T*>(wbase + 128);
+    ScMultiWarp& W = *reinterpret_cast<ScMultiWarp*>(wbase + 128 + ring_bytes);
+    for (unsigned c = tid; c < 256; c += blockDim.x) {
+        C.tri[c] = c_sc_tri[c];
+        C.ntri[c] = c_sc_ntri[c];
+        if (c < 12) C.edge[c] = c_sc_edge[c];
+        if (c < (unsigned)niso) C.iso[c] = conn[c];
+    }
+    if (warp == 0) {
+        __shared__ float s_thr[kStreamMaxIso];
+        if (lane < (unsigned)niso) s_thr[lane] = isos[G.iso_begin + lane].f.f_thr;
+        __syncwarp();
+        thermo_build(C.th, s_thr, niso, bs, bo, lane);
+    }
+    __syncthreads();   // the only CTA-wide barrier: the tables are read-only from here on
+    if (lane == 0) {
+        for (int b = 0; b < 3; ++b) mbar_init(&bar[b], 1);
+        fence_barrier_init();
+    }
+    if (lane < (unsigned)kStreamMaxIso) {
+        W.run[lane] = 0;
+        W.add[lane] = 0;
+    }
+    __syncwarp();
+    const uint32_t nx = G.vol.nx, cx = G.vol.nx - 1, cy = G.vol.ny - 1, cz = G.vol.nz - 1;
+    const uint32_t ny = G.vol.ny;
+    const uint32_t wpr = G.wpr, words_per_row = (nx + 31) / 32;
+    const uint64_t pitch = G.vol.pitch, slice = G.vol.slice;
+    const T* vol = static_cast<const T*>(G.vol.data);
+    const unsigned lt = (1u << lane) - 1u;
+    // lane k < niso: request k's first (isolevel, z) plane of the scans
+    const uint64_t my_plane = lane < (unsigned)niso ? isos[G.iso_begin + lane].plane_index : 0;
+    const uint64_t my_plane0 = lane < (unsigned)niso ? plane_base[my_plane] : 0;
+    const bool my_on = lane < (unsigned)niso && C.iso[lane].enabled;
+    uint32_t ph = 0;
+    for (;;) {
+        unsigned long long tk = 0;
+        if (lane == 0) tk = atomicAdd(next_task, 1ull);
+        const uint64_t task = __shfl_sync(FULL, tk, 0);
+        if (task >= ntasks) break;
+        const uint32_t seg = (uint32_t)(task % wpr);
+        const uint32_t y = (uint32_t)((task / wpr) % cy);
+        const uint32_t zc = (uint32_t)(task / ((uint64_t)wpr * cy));
+        const uint32_t z0 = zc * G.zchunk;
+        const uint32_t z1 = z0 + G.zchunk < cz ? z0 + G.zchunk : cz;   // cell planes [z0, z1)
+        const uint32_t nplanes = z1 - z0 + 1;
+        const uint64_t xoff = (uint64_t)seg * 256;
+        const uint64_t avail = (pitch - xoff) * sizeof(T);
+        const uint32_t row_bytes = (uint32_t)(avail < G.seg_copy_bytes ? avail : G.seg_copy_bytes);
+        auto issue = [&](uint32_t i) {
+            const int b = (int)(i % 3u);
+            T* dst = ring + (size_t)b * plane_elems;
+            const T* src = vol + (uint64_t)(z0 + i) * slice + (uint64_t)y * pitch + xoff;
+            mbar_arrive_expect_tx(&bar[b], 2 * row_bytes);
+            for (uint32_t r = 0; r < 2; ++r) bulk_copy_g2s(dst + r * row_elems, src + r * pitch, row_bytes, &bar[b]);
+        };
+        auto acquire = [&](uint32_t i) -> bool {
+            const uint32_t b = i % 3u;
+            const bool ok = mbar_wait(&bar[b], (ph >> b) & 1u, wait_polls);
+            if (ok) ph ^= 1u << b;
+            return ok;
+        };
+        __syncwarp();
+        if (lane == 0) {
+            fence_proxy_async();
+            for (uint32_t i = 0; i < nplanes && i < 3; ++i) issue(i);
+        }
+        uint32_t acq = 0, issued = 0;
+        bool dead = false;
+        const uint32_t xl = 8 * lane;                         // this lane's first cell in the segment
+        const int lim = (int)cx - (int)((uint32_t)xoff + xl);  // its cells inside the row (if < 8)
+        // lane k: request k's triangle count and first triangle of the unit, one step ahead
+        auto unit_elem = [&](uint32_t zz) -> uint64_t {
+            return G.unit_base + (((uint64_t)zz * cy + y) * wpr + seg) * niso + lane;
+        };
+        uint32_t next_n = my_on ? unit_counts[unit_elem(z0)] : 0u;
+        uint64_t next_first = my_on ? plane_base[my_plane + z0] - my_plane0 + unit_offsets[unit_elem(z0)] : 0;
+        for (uint32_t z = z0; z < z1; ++z) {
+            const uint32_t st = z - z0;
+            const uint32_t n_now = next_n;
+            const uint64_t first_now = next_first;
+            if (z + 1 < z1 && my_on) {
+                next_n = unit_counts[unit_elem(z + 1)];
+                next_first = plane_base[my_plane + z + 1] - my_plane0 + unit_offsets[unit_elem(z + 1)];
+            }
+            bool ok = true;
+            while (ok && acq <= st + 1) {
+                ok = acquire(acq);
+                if (ok) ++acq;
+            }
+            if (__any_sync(FULL, !ok)) {
+                if (lane == 0) atomicExch(status, 1);
+                dead = true;
+                issued = st + 3 < nplanes ? st + 3 : nplanes;
+                break;
+            }
+            const uint32_t act_iso = __ballot_sync(FULL, n_now != 0) & ((1u << niso) - 1u);
+            if (act_iso) {
+                const T* pa = ring + (size_t)(st % 3u) * plane_elems;
+                const T* pb = ring + (size_t)((st + 1) % 3u) * plane_elems;
+                // threshold masks of this lane's 9 nodes in the 4 staged rows,
+                // two nodes per word (node 2m low, 2m + 1 high; word 4 = node 8)
+                uint32_t P[4][5];
+#pragma unroll
+                for (int r = 0; r < 4; ++r) {
+                    const T* row = (r < 2 ? pa : pb) + (r & 1) * row_elems + xl;
+                    uint32_t e[9];
+#pragma unroll
+                    for (int i = 0; i < 9; ++i) e[i] = thermo_mask(C.th, niso, bs, bo, (float)row[i]);
+                    P[r][0] = e[0] | (e[1] << 16);
+                    P[r][1] = e[2] | (e[3] << 16);
+                    P[r][2] = e[4] | (e[5] << 16);
+                    P[r][3] = e[6] | (e[7] << 16);
+                    P[r][4] = e[8];
+                }
+                // per cell: the requests (with triangles in this unit) whose
+                // isolevel lies between its lowest and highest corner
+                const uint32_t want = act_iso | (act_iso << 16);
+                uint32_t act[4];
+                uint32_t m = 0;
+#pragma unroll
+                for (int w = 0; w < 4; ++w) {
+                    const uint32_t co0 = P[0][w] | P[1][w] | P[2][w] | P[3][w];
+                    const uint32_t co1 = P[0][w + 1] | P[1][w + 1] | P[2][w + 1] | P[3][w + 1];
+                    const uint32_t ca0 = P[0][w] & P[1][w] & P[2][w] & P[3][w];
+                    const uint32_t ca1 = P[0][w + 1] & P[1][w + 1] & P[2][w + 1] & P[3][w + 1];
+                    const uint32_t o = co0 | __funnelshift_r(co0, co1, 16);
+                    const uint32_t a = ca0 & __funnelshift_r(ca0, ca1, 16);
+                    uint32_t keep = want;
+                    if (2 * w >= lim) keep &= 0xffff0000u;
+                    if (2 * w + 1 >= lim) keep &= 0x0000ffffu;
+                    act[w] = o & ~a & keep;
+                    m += __popc(act[w]);
+                }
+                uint32_t inc = m;
+#pragma unroll
+                for (int o = 1; o < 32; o <<= 1) {
+                    const uint32_t t = __shfl_up_sync(FULL, inc, o);
+                    if (lane >= (unsigned)o) inc += t;
+                }
+                const uint32_t npairs = __shfl_sync(FULL, inc, 31);
+                const uint32_t my_first = inc - m;
+                for (uint32_t fill0 = 0; fill0 < npairs; fill0 += kScPairCap) {
+                    // this lane's pairs (cell order, then request) that fall into
+                    // [fill0, fill0 + kScPairCap)
+                    if (m && my_first < fill0 + kScPairCap && my_first + m > fill0) {
+                        uint32_t slot = my_first;
+#pragma unroll
+                        for (int i = 0; i < 8; ++i) {
+                            uint32_t am = (act[i >> 1] >> (16 * (i & 1))) & 0xffffu;
+                            if (am) {
+                                const uint32_t w0 = cell_word(P[0], i), w1 = cell_word(P[1], i);
+                                const uint32_t w2 = cell_word(P[2], i), w3 = cell_word(P[3], i);
+                                do {
+                                    const uint32_t k = __ffs(am) - 1;
+                                    am &= am - 1;
+                                    if (slot >= fill0 && slot < fill0 + kScPairCap)
+                                        W.pairs[slot - fill0] =
+                                            (xl + i) | (k << 8) | (code_to_case(case_code(w0, w1, w2, w3, k)) << 16);
+                                    ++slot;
+                                } while (am);
+                            }
+                        }
+                    }
+                    __syncwarp();
+                    const uint32_t nfill = npairs - fill0 < (uint32_t)kScPairCap ? npairs - fill0 : (uint32_t)kScPairCap;
+                    for (uint32_t r0 = 0; r0 < nfill; r0 += 32) {
+                        // one pair per lane; its first triangle: the request's running
+                        // count in the unit plus the triangles of the earlier lanes with
+                        // the same request
+                        const uint32_t p = r0 + lane;
+                        const bool has = p < nfill;
+                        const uint32_t pe = has ? W.pairs[p] : 0u;
+                        const uint32_t k = (pe >> 8) & 0xffu, cs = pe >> 16;
+                        const uint32_t nt = has ? C.ntri[cs] : 0u;
+                        const uint32_t grp = __match_any_sync(FULL, has ? (int)k : 32 + (int)lane);
+                        uint32_t pre = 0, gtot = 0, tpre = 0, ntr = 0;
+#pragma unroll
+                        for (int bit = 0; bit < 3; ++bit) {
+                            const uint32_t bm = __ballot_sync(FULL, (nt >> bit) & 1u);
+                            pre += (uint32_t)__popc(bm & grp & lt) << bit;
+                            gtot += (uint32_t)__popc(bm & grp) << bit;
+                            tpre += (uint32_t)__popc(bm & lt) << bit;
+                            ntr += (uint32_t)__popc(bm) << bit;
+                        }
+                        const uint64_t kfirst = __shfl_sync(FULL, first_now, k);
+                        const uint64_t obase = kfirst + (has ? W.run[k] : 0u) + pre;
+                        __syncwarp();
+                        if (has && (31 - __clz(grp)) == (int)lane) W.add[k] = gtot;
+                        for (uint32_t t = 0; t < nt; ++t) W.item[tpre + t] = (uint8_t)lane;
+                        __syncwarp();
+                        if (lane < (unsigned)kStreamMaxIso) {
+                            W.run[lane] += W.add[lane];
+                            W.add[lane] = 0;
+                        }
+                        __syncwarp();
+                        for (uint32_t j0 = 0; j0 < ntr; j0 += 32) {
+                            const uint32_t jj = j0 + lane;
+                            const bool ht = jj < ntr;
+                            const uint32_t q = ht ? W.item[jj] : 0u;
+                            const uint32_t qe = __shfl_sync(FULL, pe, q);
+                            const uint32_t qt = __shfl_sync(FULL, tpre, q);
+                            const uint64_t qo = __shfl_sync(FULL, obase, q);
+                            if (!ht) continue;
+                            const uint32_t qk = (qe >> 8) & 0xffu, qc = qe >> 16;
+                            const uint32_t t = jj - qt;
+                            const uint64_t tt = qo + t;
+                            const ConnIso& R = C.iso[qk];
+                            const uint64_t pk = C.tri[qc] >> (12 * t);
+                            const uint32_t x = (uint32_t)xoff + (qe & 0xffu);
+                            uint32_t id[3];
+                            bool good = true;
+#pragma unroll
+                            for (int e = 0; e < 3; ++e) {
+                                const unsigned ep = C.edge[(pk >> (4 * e)) & 15u];
+                                const unsigned ca = ep & 7u, cb = ep >> 3;
+                                const unsigned nd = ca & cb, d = ca ^ cb;   // lower node, axis bit
+                                const int axis = d == 1u ? 0 : (d == 2u ? 1 : 2);
+                                id[e] = sc_rank_id_of(R.rank, ny, words_per_row, x + (nd & 1u), y + ((nd >> 1) & 1u),
+                                                      z + (nd >> 2), axis);
+                                good = good && id[e] < R.nvert;
+                            }
+                            if (tt >= R.ntri) {
+                                atomicExch(status, 2);   // never with the count's offsets; nothing written out of range
+                                continue;
+                            }
+                            uint32_t* o = R.connections + 3 * tt;
+                            o[0] = id[0]; o[1] = id[1]; o[2] = id[2];
+                            if (!good) {
+                                atomicExch(status, 2);   // never with consistent rank words; nothing read out of range
+                            } else if (R.tri_out) {
+                                const float* p0 = R.coords + 3 * (uint64_t)id[0];
+                                const float* p1 = R.coords + 3 * (uint64_t)id[1];
+                                const float* p2 = R.coords + 3 * (uint64_t)id[2];
+                                const float3 nn = tri_normal(make_float3(p0[0], p0[1], p0[2]),
+                                                             make_float3(p1[0], p1[1], p1[2]),
+                                                             make_float3(p2[0], p2[1], p2[2]));
+                                float* qn = R.tri_out + 3 * tt;
+                                qn[0] = nn.x; qn[1] = nn.y; qn[2] = nn.z;
+                            }
+                        }
+                        __syncwarp();
+                    }
+                    __syncwarp();
+                }
+                if (lane < (unsigned)kStreamMaxIso) W.run[lane] = 0;
+                __syncwarp();
+            }
+            __syncwarp();
+            if (lane == 0 && st + 3 < nplanes) {
+                fence_proxy_async();
+                issue(st + 3);
+            }
+        }
+        if (dead) {
+            for (uint32_t i = acq; i < issued; ++i) {
+                const uint32_t b = i % 3u;
+                if (mbar_wait(&bar[b], (ph >> b) & 1u, 1u << 16)) ph ^= 1u << b;
+            }
+            break;
+        }
+    }
+}
+
 }  // namespace
 
 size_t sconnect_shared_bytes(int dtype)
@@ -805,6 +1127,37 @@ cudaError_t launch_sconnect(const Job& j, const StreamGroup* d_groups, const Str
         kern<<<(unsigned)nctas, kSnThreads, smem, L.stream>>>(j, d_groups, d_isos, unit_counts, unit_offsets,
                                                                 plane_base, iso_k, ntasks, nvert, ntri, status,
                                                                 next_task, L.wait_polls[1]);
+        prof_end(L);
+    });
+    *L.counter += 1;
+    return cudaGetLastError();
+}
+
+size_t sconnect_multi_shared_bytes(int dtype)
+{
+    const size_t es = dtype_size(dtype);
+    const size_t plane = 2 * stream_row_elems(dtype, 1) * es;
+    return sn_align(sizeof(ScMultiCta)) + (size_t)kSnWarps * (128 + sn_align(3 * plane) + sn_align(sizeof(ScMultiWarp)));
+}
+
+cudaError_t launch_sconnect_multi(const StreamGroup* d_group, const StreamIso* d_isos, const ConnIso* d_conn, int dtype,
+                                  const uint16_t* unit_counts, const uint32_t* unit_offsets, const uint64_t* plane_base,
+                                  uint64_t ntasks, int* status, unsigned long long* next_task, const Launch& L)
+{
+    if (ntasks == 0) return cudaSuccess;
+    const size_t smem = sconnect_multi_shared_bytes(dtype);
+    KVSMC_SN_SWITCH(dtype, {
+        auto kern = k_sconnect_multi<T>;
+        cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        int per_sm = 0;
+        if (e == cudaSuccess) e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, kSnThreads, smem);
+        if (e != cudaSuccess) return e;
+        const uint64_t resident = (uint64_t)(per_sm > 0 ? per_sm : 1) * (uint64_t)L.num_sms;
+        const uint64_t need = (ntasks + kSnWarps - 1) / kSnWarps;
+        const uint64_t nctas = need < resident ? need : resident;
+        prof_begin(L, "sconnect_multi");
+        kern<<<(unsigned)nctas, kSnThreads, smem, L.stream>>>(d_group, d_isos, d_conn, unit_counts, unit_offsets,
+                                                                plane_base, ntasks, status, next_task, L.wait_polls[1]);
         prof_end(L);
     });
     *L.counter += 1;

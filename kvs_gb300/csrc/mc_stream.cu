@@ -331,32 +331,6 @@ __device__ __forceinline__ uint32_t value_mask(const WarpState& W, int niso, flo
     return e & 0xffffu;
 }
 
-// The row word of cell i (0..7): node i in the low half, node i+1 in the high half.
-__device__ __forceinline__ uint32_t cell_word(const uint32_t* P, int i)
-{
-    return (i & 1) ? __funnelshift_r(P[i >> 1], P[(i >> 1) + 1], 16) : P[i >> 1];
-}
-
-// Corner code of a cell for isolevel k from its four row words (plane z rows
-// y, y+1 = a0, a1; plane z+1 = b0, b1): bit r = row r's node i above, bit
-// 4 + r = row r's node i+1 above.
-__device__ __forceinline__ uint32_t case_code(uint32_t a0, uint32_t a1, uint32_t b0, uint32_t b1, uint32_t k)
-{
-    const uint32_t m0 = (a0 >> k) & 0x10001u, m1 = (a1 >> k) & 0x10001u;
-    const uint32_t m2 = (b0 >> k) & 0x10001u, m3 = (b1 >> k) & 0x10001u;
-    const uint32_t x = m0 | (m1 << 1) | (m2 << 2) | (m3 << 3);
-    return (x & 0xfu) | ((x >> 12) & 0xf0u);
-}
-
-// The reference's case number of a corner code: bit c = corner c above, with
-// corners (x,y,z) 0:(0,0,0) 1:(1,0,0) 2:(1,1,0) 3:(0,1,0) 4:(0,0,1) 5:(1,0,1)
-// 6:(1,1,1) 7:(0,1,1) (MarchingCubes.cpp:187-194).
-__device__ __forceinline__ uint32_t code_to_case(uint32_t c)
-{
-    return (c & 1u) | (((c >> 4) & 1u) << 1) | (((c >> 5) & 1u) << 2) | (((c >> 1) & 1u) << 3) |
-           (((c >> 2) & 1u) << 4) | (((c >> 6) & 1u) << 5) | (((c >> 7) & 1u) << 6) | (((c >> 3) & 1u) << 7);
-}
-
 __device__ __forceinline__ uint32_t warp_inclusive_scan(uint32_t v, unsigned lane)
 {
 #pragma unroll
