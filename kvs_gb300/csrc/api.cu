@@ -552,8 +552,8 @@ kvsmc_status shared_count(kvsmc_context* ctx, const std::vector<Item*>& items, S
         const int m = it->params.mode, dt = it->vol->view.dtype;
         if ((m == KVSMC_SHARED_POLYGON_NORMAL || m == KVSMC_SHARED_VERTEX_NORMAL) && ctx->path == 0 &&
             (dt == KVSMC_I8 || dt == KVSMC_I16 || dt == KVSMC_U8 || dt == KVSMC_U16 || dt == KVSMC_F32) &&
-            stream_volume_eligible(ctx, *it))
-            sc.cand.push_back(it);
+            stream_volume_eligible(ctx, *it) && stream_shape(ctx, it->vol->view).rows == 1)
+            sc.cand.push_back(it);   // (the connection pass takes one-row tasks only)
     }
     if (sc.cand.size() < 2) {
         sc.cand.clear();
