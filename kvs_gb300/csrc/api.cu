@@ -607,7 +607,8 @@ kvsmc_status shared_count(kvsmc_context* ctx, const std::vector<Item*>& items, S
 // device outputs from `outputs`, one node emit per group for all its
 // requests (k_snode_multi: the volume read once, every node classified once),
 // and each request's connections and vertex normals.  Per-request failures
-// go to it->status.
+// go to it->status; KVSMC_ERR_OUT_OF_MEMORY (an arena could not grow, before
+// any output was written) asks the caller to run the requests one by one.
 kvsmc_status grouped_shared(kvsmc_context* ctx, const SharedCount& sc, std::vector<Item*>& items, bool emit,
                             const std::function<kvsmc_status(std::vector<Item*>&)>& outputs)
 {
@@ -630,7 +631,11 @@ kvsmc_status grouped_shared(kvsmc_context* ctx, const SharedCount& sc, std::vect
         ctx->arena4 = nullptr;
         ctx->arena4_bytes = 0;
         const size_t want = align_up(need, 1 << 20);
-        KVSMC_CUDA(ctx, cudaMalloc(&ctx->arena4, want));
+        if (cudaMalloc(&ctx->arena4, want) != cudaSuccess) {
+            cudaGetLastError();
+            ctx->arena4 = nullptr;
+            return KVSMC_ERR_OUT_OF_MEMORY;   // the caller runs the requests one by one
+        }
         ctx->arena4_bytes = want;
     }
     char* base = static_cast<char*>(ctx->arena4);
@@ -656,7 +661,11 @@ kvsmc_status grouped_shared(kvsmc_context* ctx, const SharedCount& sc, std::vect
         ctx->arena5 = nullptr;
         ctx->arena5_bytes = 0;
         const size_t want = align_up(tn_total, 1 << 20);
-        KVSMC_CUDA(ctx, cudaMalloc(&ctx->arena5, want));
+        if (cudaMalloc(&ctx->arena5, want) != cudaSuccess) {
+            cudaGetLastError();
+            ctx->arena5 = nullptr;
+            return KVSMC_ERR_OUT_OF_MEMORY;   // the caller runs the requests one by one
+        }
         ctx->arena5_bytes = want;
     }
     {
@@ -832,13 +841,15 @@ kvsmc_status run_items(kvsmc_context* ctx, std::vector<Item*>& items, bool emit)
             }
             return KVSMC_OK;
         };
-        if (kvsmc_status st = grouped_shared(ctx, sc, grouped, emit, outputs))
+        const kvsmc_status st = grouped_shared(ctx, sc, grouped, emit, outputs);
+        if (st == KVSMC_ERR_OUT_OF_MEMORY) grouped.clear();   // each request on its own below
+        else if (st)
             for (Item* it : grouped)
                 if (!it->status) it->status = st;
     }
     for (Item* it : gather_items) {
         if (it->status) continue;
-        if (sc.has_nodes(it)) continue;   // done above
+        if (!grouped.empty() && sc.has_nodes(it)) continue;   // done above
         Plan pl;
         gather_plan(*it, pl);
         sc.attach(it, pl);
@@ -1355,7 +1366,9 @@ kvsmc_status kvsmc_extract_batch_host(kvsmc_context* ctx, const void* host, kvsm
         if (!it->status && sc.has_nodes(it)) grouped.push_back(it);
     if (!grouped.empty()) {
         auto outputs = [&](std::vector<Item*>& its) { return arena_outputs(ctx, its); };
-        if ((st = grouped_shared(ctx, sc, grouped, true, outputs)))
+        st = grouped_shared(ctx, sc, grouped, true, outputs);
+        if (st == KVSMC_ERR_OUT_OF_MEMORY) grouped.clear();   // each request on its own below
+        else if (st)
             for (Item* it : grouped)
                 if (!it->status) it->status = st;
         std::vector<Item*> done;
@@ -1368,7 +1381,7 @@ kvsmc_status kvsmc_extract_batch_host(kvsmc_context* ctx, const void* host, kvsm
     }
     for (Item* it : g_items) {
         if (it->status) continue;
-        if (sc.has_nodes(it)) continue;   // done above
+        if (!grouped.empty() && sc.has_nodes(it)) continue;   // done above
         Plan pl;
         gather_plan(*it, pl);
         sc.attach(it, pl);
