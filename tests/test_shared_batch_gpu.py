@@ -109,3 +109,39 @@ def test_host_batch_shared_requests_match_alone(kvsmc_ctx):
         for key in ("coords", "normals"):
             assert same_bits(out[k][key], alone[key]), (k, key, first_diff(out[k][key], alone[key]))
         assert np.array_equal(out[k]["connections"], alone["connections"]), k
+
+
+def test_shared_batch_capacity_error_leaves_the_others_exact(kvsmc_ctx):
+    """A request whose buffers are too small fails alone with KVSMC_ERR_CAPACITY;
+    the grouped passes still write the other requests exactly."""
+    v = S.to_numpy(S.fbm((30, 36, 180), seed=14, device="cuda"))
+    vol = _abi.DeviceVolume.upload(kvsmc_ctx, v)
+    params = [_abi.make_params(x, _abi.MODE_SHARED_VERTEX_NORMAL) for x in (0.35, 0.5, 0.65)]
+    alone = [extract_batch(kvsmc_ctx, [vol], [p], _abi.PATH_AUTO)[0] for p in params]
+    n = len(params)
+    reqs = (_abi.Request * n)()
+    for i, p in enumerate(params):
+        reqs[i].volume = vol.handle
+        reqs[i].params = p
+    kvsmc_ctx.check(kvsmc_ctx.lib.kvsmc_count_batch(kvsmc_ctx.handle, reqs, n), "count_batch")
+    bufs = []
+    for i in range(n):
+        s = reqs[i].sizes
+        short = 3 if i == 1 else 0   # request 1: three coordinates too few
+        c = torch.empty(max(1, s.ncoords), dtype=torch.float32, device="cuda")
+        nn = torch.empty(max(1, s.nnormals), dtype=torch.float32, device="cuda")
+        k = torch.empty(max(1, s.nconnections), dtype=torch.int32, device="cuda")
+        bufs.append((c, nn, k, s.ncoords, s.nnormals, s.nconnections))
+        reqs[i].d_coords, reqs[i].coords_capacity = c.data_ptr(), s.ncoords - short
+        reqs[i].d_normals, reqs[i].normals_capacity = nn.data_ptr(), s.nnormals
+        reqs[i].d_connections, reqs[i].connections_capacity = k.data_ptr(), s.nconnections
+    st = kvsmc_ctx.lib.kvsmc_extract_batch(kvsmc_ctx.handle, reqs, n)
+    assert st == _abi.ERR_CAPACITY
+    assert reqs[1].status == _abi.ERR_CAPACITY
+    for i in (0, 2):
+        assert reqs[i].status == _abi.OK
+        c, nn, k, a, b, d = bufs[i]
+        got = dict(coords=c[:a].cpu().numpy(), normals=nn[:b].cpu().numpy(),
+                   connections=k[:d].cpu().numpy().view(np.uint32), ntri=reqs[i].sizes.ntriangles)
+        _same(got, alone[i], f"request {i}")
+    vol.free()
