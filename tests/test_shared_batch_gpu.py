@@ -145,3 +145,36 @@ def test_shared_batch_capacity_error_leaves_the_others_exact(kvsmc_ctx):
                    connections=k[:d].cpu().numpy().view(np.uint32), ntri=reqs[i].sizes.ntriangles)
         _same(got, alone[i], f"request {i}")
     vol.free()
+
+
+@pytest.mark.parametrize("seed", [101, 202, 303])
+def test_shared_batch_random_shapes_equal_alone(kvsmc_ctx, seed):
+    """Random shapes (rows of one to three segments, the last one partial, or a
+    last node alone in a segment; two-row volumes; as few as two planes or rows),
+    value types and isolevel sets: every grouped request equals the same request
+    run alone."""
+    rng = np.random.default_rng(seed)
+    vols, params = [], []
+    for _ in range(4):
+        nx = int(rng.choice([129, 200, 255, 256, 300, 511, 512, 513, 700]))
+        ny = int(rng.integers(2, 24))
+        nz = int(rng.integers(2, 20))
+        dt = [np.uint8, np.uint16, np.int16, np.float32][int(rng.integers(0, 4))]
+        f = S.fbm((nz, ny, nx), seed=int(rng.integers(0, 1 << 16)), device="cuda")
+        if np.dtype(dt).kind == "f":
+            v = S.to_numpy(f)
+        else:
+            lo, hi = (-30000.0, 30000.0) if np.dtype(dt) == np.int16 else (0.0, 250.0 if dt == np.uint8 else 60000.0)
+            v = S.to_numpy(S._cast(f.double() * (hi - lo) + lo, dt))
+        dv = _abi.DeviceVolume.upload(kvsmc_ctx, v)
+        mn, mx = dv.minmax()
+        for _ in range(int(rng.integers(2, 6))):
+            vols.append(dv)
+            params.append(_abi.make_params(mn + rng.uniform(0.1, 0.9) * (mx - mn), int(rng.integers(1, 3))))
+    batch = extract_batch(kvsmc_ctx, vols, params, _abi.PATH_AUTO)
+    for i in range(len(params)):
+        assert batch[i]["status"] == _abi.OK
+        alone = extract_batch(kvsmc_ctx, [vols[i]], [params[i]], _abi.PATH_AUTO)[0]
+        _same(batch[i], alone, f"seed {seed} request {i}")
+    for dv in {id(d): d for d in vols}.values():
+        dv.free()
