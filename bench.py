@@ -994,8 +994,8 @@ def run_ours(args, rank, world, local):
                     "traffic": tr}
     # end to end through the C ABI with host buffers
     e2e = None
-    if host_field is not None and mode == _abi.MODE_DUP_POLYGON_NORMAL:
-        e2e = run_e2e(ctx, host_field, isos, reqs, args, stream)
+    if host_field is not None:
+        e2e = run_e2e(ctx, host_field, isos, reqs, args, stream, mode)
         if e2e is not None:
             e2e["value"] = round(cells / (e2e.pop("step_ms") * 1e-3) / 1e6 * world, 1)
             e2e["unit"] = "Mcells/s"
@@ -1195,9 +1195,9 @@ def page_numa_node(addr):
         return None
 
 
-def run_e2e(ctx, host_field, isos, reqs, args, stream):
+def run_e2e(ctx, host_field, isos, reqs, args, stream, mode=0):
     """Same sweep through kvsmc_extract_batch_host: H2D of the volume from
-    pinned memory, both launches, D2H of every output into pinned buffers."""
+    pinned memory, the passes, D2H of every output into pinned buffers."""
     import torch
 
     from kvs_gb300 import _abi
@@ -1207,7 +1207,10 @@ def run_e2e(ctx, host_field, isos, reqs, args, stream):
         s = reqs[i].sizes
         pinned[(i, 0)] = torch.empty(max(1, s.ncoords), dtype=torch.float32, pin_memory=True).numpy()
         pinned[(i, 1)] = torch.empty(max(1, s.nnormals), dtype=torch.float32, pin_memory=True).numpy()
-    params = [_abi.make_params(iso, _abi.MODE_DUP_POLYGON_NORMAL) for iso in isos]
+        if mode != _abi.MODE_DUP_POLYGON_NORMAL:
+            pinned[(i, 2)] = torch.empty(max(1, s.nconnections), dtype=torch.int32,
+                                         pin_memory=True).numpy().view(np.uint32)
+    params = [_abi.make_params(iso, mode) for iso in isos]
     host = host_field.numpy()
 
     def buf(req, kind, count):
@@ -1229,7 +1232,7 @@ def run_e2e(ctx, host_field, isos, reqs, args, stream):
     ctx.profile_enable(False)
     t = statistics.median(times)   # the call is host-bound (link transfers): the median damps host noise
     h2d = host.nbytes
-    d2h = sum(o["coords"].nbytes + o["normals"].nbytes for o in out)
+    d2h = sum(o["coords"].nbytes + o["normals"].nbytes + o["connections"].nbytes for o in out)
     link = {}
     for name, nbytes in (("copy_h2d", h2d), ("copy_d2h", d2h)):
         n, ms = prof.get(name, (0, 0.0))
@@ -1241,8 +1244,11 @@ def run_e2e(ctx, host_field, isos, reqs, args, stream):
     link.update(getattr(args, "numa", {}))
     return {"step_ms": t * 1e3, "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h),
             "api": "kvsmc_extract_batch_host", "steps": steps, "timing": "host clock, median of steps",
-            "pipeline": "emit in 8 launches by plane ranges, each range's triangles copied to the host on a "
-                        "second stream while the next range is written",
+            "pipeline": ("emit in 8 launches by plane ranges, each range's triangles copied to the host on a "
+                         "second stream while the next range is written") if mode == _abi.MODE_DUP_POLYGON_NORMAL else
+                        ("one count, one node emit and one connection pass for all the requests, then each "
+                         "request's vertex normals; each request's vertices, connections and normals copied "
+                         "to the host on a second stream as soon as the pass that writes them ends"),
             "link": link,
             "kernels_ms_per_step": {k: round(v[1] / steps, 3) for k, v in prof.items()}}
 

@@ -609,8 +609,14 @@ kvsmc_status shared_count(kvsmc_context* ctx, const std::vector<Item*>& items, S
 // and each request's connections and vertex normals.  Per-request failures
 // go to it->status; KVSMC_ERR_OUT_OF_MEMORY (an arena could not grow, before
 // any output was written) asks the caller to run the requests one by one.
+//
+// ready(it, what), when given, is called as soon as outputs of a request are
+// final on the context's stream (what: 0 its vertices, 1 its connections and
+// any polygon normals, 2 all of its outputs), so a caller can start copying
+// them while the later passes run.
 kvsmc_status grouped_shared(kvsmc_context* ctx, const SharedCount& sc, std::vector<Item*>& items, bool emit,
-                            const std::function<kvsmc_status(std::vector<Item*>&)>& outputs)
+                            const std::function<kvsmc_status(std::vector<Item*>&)>& outputs,
+                            const std::function<kvsmc_status(Item*, int)>& ready = {})
 {
     std::vector<Plan> plans(items.size());
     size_t total = 0;
@@ -719,6 +725,9 @@ kvsmc_status grouped_shared(kvsmc_context* ctx, const SharedCount& sc, std::vect
             KVSMC_CUDA(ctx, cudaMemcpyAsync(hs, d_status, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
             KVSMC_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
             if (*hs) st = fail(ctx, KVSMC_ERR_TIMEOUT, "shared-vertex node emit: a shared-memory load did not complete");
+            if (!st && ready)   // the vertices leave while the connections are written
+                for (Plan* p : gp)
+                    if ((st = ready(p->item, 0))) break;
             // then the group's connection pass, every request of the group in its
             // isolevel order (the ones not written here disabled)
             if (!st) st = ensure_stage(ctx, (size_t)G.niso * sizeof(kvsmc::ConnIso));
@@ -764,6 +773,8 @@ kvsmc_status grouped_shared(kvsmc_context* ctx, const SharedCount& sc, std::vect
             } else {
                 pl->nodes_done = true;
                 pl->conn_done = pl->ntri != 0;
+                if (ready)
+                    if (kvsmc_status rs = ready(pl->item, 1)) pl->item->status = rs;
             }
         }
     }
@@ -771,9 +782,11 @@ kvsmc_status grouped_shared(kvsmc_context* ctx, const SharedCount& sc, std::vect
         Item* it = items[i];
         if (it->status || !it->emit) continue;
         kvsmc_status st = gather_emit(ctx, plans[i], it->d_coords, it->d_normals, it->d_conn);
-        if (!st) KVSMC_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+        if (!st && ready) st = ready(it, 2);
+        if (!st && !ready) KVSMC_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
         if (st) it->status = st;
     }
+    if (ready) KVSMC_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
     return KVSMC_OK;
 }
 
@@ -1365,17 +1378,51 @@ kvsmc_status kvsmc_extract_batch_host(kvsmc_context* ctx, const void* host, kvsm
     for (Item* it : g_items)
         if (!it->status && sc.has_nodes(it)) grouped.push_back(it);
     if (!grouped.empty()) {
-        auto outputs = [&](std::vector<Item*>& its) { return arena_outputs(ctx, its); };
-        st = grouped_shared(ctx, sc, grouped, true, outputs);
+        // device outputs and the caller's host arrays once the sizes are known;
+        // each array leaves on the copy stream as soon as it is final, while
+        // the later passes run
+        auto outputs = [&](std::vector<Item*>& its) -> kvsmc_status {
+            kvsmc_status s2 = arena_outputs(ctx, its);
+            if (!s2) s2 = host_alloc(ctx, its, items.data(), alloc, user);
+            return s2;
+        };
+        if (!ctx->copy_stream) {
+            KVSMC_CUDA(ctx, cudaStreamCreateWithFlags(&ctx->copy_stream, cudaStreamNonBlocking));
+            for (int i = 0; i < kvsmc_context::kParts; ++i)
+                KVSMC_CUDA(ctx, cudaEventCreateWithFlags(&ctx->part_ev[i], cudaEventDisableTiming));
+        }
+        int ev = 0;
+        const kvsmc::Launch Lc = [&] { kvsmc::Launch l = launch_of(ctx); l.stream = ctx->copy_stream; return l; }();
+        auto ready = [&](Item* it, int what) -> kvsmc_status {
+            cudaEvent_t e = ctx->part_ev[ev++ % kvsmc_context::kParts];
+            KVSMC_CUDA(ctx, cudaEventRecord(e, ctx->stream));
+            KVSMC_CUDA(ctx, cudaStreamWaitEvent(ctx->copy_stream, e, 0));
+            const kvsmc_sizes& z = it->sizes;
+            const bool pn = it->params.mode == KVSMC_SHARED_POLYGON_NORMAL;
+            kvsmc::prof_begin(Lc, "copy_d2h");
+            if (what == 0 && it->h_coords)
+                KVSMC_CUDA(ctx, cudaMemcpyAsync(it->h_coords, it->d_coords, z.ncoords * 4, cudaMemcpyDeviceToHost,
+                                                ctx->copy_stream));
+            if (what == 1 && it->h_conn)
+                KVSMC_CUDA(ctx, cudaMemcpyAsync(it->h_conn, it->d_conn, z.nconnections * 4, cudaMemcpyDeviceToHost,
+                                                ctx->copy_stream));
+            if (((what == 1 && pn) || (what == 2 && !pn)) && it->h_normals)
+                KVSMC_CUDA(ctx, cudaMemcpyAsync(it->h_normals, it->d_normals, z.nnormals * 4, cudaMemcpyDeviceToHost,
+                                                ctx->copy_stream));
+            kvsmc::prof_end(Lc);
+            return KVSMC_OK;
+        };
+        st = grouped_shared(ctx, sc, grouped, true, outputs, ready);
+        const cudaError_t ce = cudaStreamSynchronize(ctx->copy_stream);
         if (st == KVSMC_ERR_OUT_OF_MEMORY) grouped.clear();   // each request on its own below
         else if (st)
             for (Item* it : grouped)
                 if (!it->status) it->status = st;
-        std::vector<Item*> done;
-        for (Item* it : grouped)
-            if (!it->status) done.push_back(it);
-        if (!done.empty() && (st = copy_back(ctx, done, items.data(), alloc, user)))
-            for (Item* it : done) it->status = st;
+        if (ce != cudaSuccess && !grouped.empty()) {
+            st = fail(ctx, KVSMC_ERR_CUDA, "copy stream: %s", cudaGetErrorString(ce));
+            for (Item* it : grouped)
+                if (!it->status) it->status = st;
+        }
         for (Item* it : grouped)
             if (it->status && !first) first = it->status;
     }
