@@ -442,8 +442,6 @@ kvsmc_status gather_emit(kvsmc_context* ctx, Plan& pl, float* coords, float* nor
         if (pl.ntri) KVSMC_CUDA(ctx, launch_emit_dup(j, L));
         return KVSMC_OK;
     }
-    void* vn_scan = nullptr;
-    uint64_t* vn_total = nullptr;
     const bool vertex_normals = pl.nvert && pl.ntri && j.mode == KVSMC_SHARED_VERTEX_NORMAL;
     if (vertex_normals) {
         // per-triangle normals and the vertices' triangle lists live in the
@@ -461,7 +459,7 @@ kvsmc_status gather_emit(kvsmc_context* ctx, Plan& pl, float* coords, float* nor
             KVSMC_CUDA(ctx, cudaMalloc(&ctx->arena2, want));
             ctx->arena2_bytes = want;
         }
-        kvsmc::vertex_normals_carve(j, pl.ntri, pl.nvert, ctx->arena2, &vn_scan, &vn_total);
+        kvsmc::vertex_normals_carve(j, pl.ntri, pl.nvert, ctx->arena2);
         if (pl.conn_done) j.tri_normals = pl.tri_normals;   // written by the connection pass already
     } else {
         j.tri_normals = nullptr;
@@ -499,7 +497,7 @@ kvsmc_status gather_emit(kvsmc_context* ctx, Plan& pl, float* coords, float* nor
         KVSMC_CUDA(ctx, launch_connect(j, L));
     }
     if (vertex_normals) {
-        KVSMC_CUDA(ctx, launch_vertex_normals(j, pl.ntri, pl.nvert, vn_scan, vn_total, L));
+        KVSMC_CUDA(ctx, launch_vertex_normals(j, pl.ntri, pl.nvert, L));
     } else if (pl.nvert && j.mode == KVSMC_SHARED_VERTEX_NORMAL) {
         // vertices without any triangle (a volume one node thick): zero normals
         // (calculate_normals_on_vertex adds nothing to its zeroed array)

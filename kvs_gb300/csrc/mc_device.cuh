@@ -73,11 +73,8 @@ struct Job {
     // vertex normals (mode 2): per-triangle normals, then each vertex's
     // triangles (counts, scanned offsets, lists) for the ordered sums
     float* tri_normals;
-    uint32_t* vcount;
-    uint32_t* vfill;
-    uint64_t* voff;
-    uint32_t* vlist;
-    const uint64_t* vtotal;   // device: number of (vertex, triangle) incidences
+    uint32_t* vcount;         // triangles per vertex
+    uint32_t* vlist;          // their ids, slot-major (slot s of vertex v at s * nvert + v)
 };
 
 // ------------------------------------------------------------------- values

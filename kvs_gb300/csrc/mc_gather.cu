@@ -385,47 +385,51 @@ __global__ void __launch_bounds__(kThreads) k_connect(Job j)
 // calculate_normals_on_vertex (MarchingCubes.cpp:569-605): every vertex's
 // normal is the sum, from 0.0f and in triangle order, of the normals of the
 // triangles that use it.  Float addition is not associative, so the order is
-// kept: each triangle's normal is formed once (k_connect), every vertex gets
-// the list of its triangles (incidence counts, an exclusive scan, then the
-// triangle ids placed by atomics in any order), and one thread per vertex
-// sorts its list (a vertex lies on one cell edge: at most four cells, a few
-// triangles each) and adds the normals in increasing triangle order.
+// kept: each triangle's normal is formed once (by the connection pass), the
+// triangle ids of every vertex are placed into its own slots by atomics (in
+// any order), and one thread per vertex sorts them and adds the normals in
+// increasing triangle order.  A vertex lies on one cell edge, shared by at
+// most four cells, and no case of the table puts one edge into more than five
+// of its triangles, so a vertex has at most kVnMaxInc triangles: fixed slots,
+// no count pass and no scan.  The slots are stored slot-major (slot s of
+// vertex v at s * nvert + v) so the summing threads read them coalesced.
 // (connections hold vertex ids below nvert; an id at or above it, which
-// consistent inputs never give, is skipped so nothing is touched out of range)
-__global__ void __launch_bounds__(256) k_vn_count(const uint32_t* __restrict__ conn, uint64_t ntri, uint64_t nvert,
-                                                 uint32_t* __restrict__ vcount)
-{
-    for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < 3 * ntri;
-         i += (uint64_t)gridDim.x * blockDim.x) {
-        const uint32_t v = conn[i];
-        if (v < nvert) atomicAdd(vcount + v, 1u);
-    }
-}
+// consistent inputs never give, is skipped so nothing is touched out of
+// range, and so is a slot past kVnMaxInc)
+constexpr uint32_t kVnMaxInc = 20;   // 4 cells x 5 triangles of one cell on one edge
 
+// One incidence per lane, 32 consecutive ones per warp: lanes holding the
+// same vertex (a cell's triangles share corners) take their slots with one
+// atomic for the group.  (Four incidences per lane in flight measured slower:
+// the pass is not bound by the atomics' latency.)
 __global__ void __launch_bounds__(256) k_vn_fill(const uint32_t* __restrict__ conn, uint64_t ntri, uint64_t nvert,
-                                                const uint64_t* __restrict__ voff, uint32_t* __restrict__ vfill,
-                                                uint32_t* __restrict__ vlist)
+                                                uint32_t* __restrict__ vcount, uint32_t* __restrict__ vlist)
 {
-    for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < 3 * ntri;
-         i += (uint64_t)gridDim.x * blockDim.x) {
-        const uint32_t v = conn[i];
-        if (v >= nvert) continue;
-        const uint32_t slot = atomicAdd(vfill + v, 1u);
-        vlist[voff[v] + slot] = (uint32_t)(i / 3);
+    const unsigned lane = threadIdx.x & 31u;
+    const uint32_t lt = (1u << lane) - 1u;
+    const uint64_t n = 3 * ntri;
+    for (uint64_t i0 = (uint64_t)blockIdx.x * blockDim.x + (threadIdx.x & ~31u); i0 < n;
+         i0 += (uint64_t)gridDim.x * blockDim.x) {
+        const uint64_t i = i0 + lane;
+        const uint32_t v = i < n ? conn[i] : 0xffffffffu;
+        const bool ok = v < nvert;
+        const uint32_t grp = __match_any_sync(0xffffffffu, ok ? v : 0xffffffffu);
+        const int leader = __ffs(grp) - 1;
+        uint32_t base = 0;
+        if (ok && (int)lane == leader) base = atomicAdd(vcount + v, (uint32_t)__popc(grp));
+        base = __shfl_sync(0xffffffffu, base, leader);
+        const uint32_t s = base + (uint32_t)__popc(grp & lt);
+        if (ok && s < kVnMaxInc) vlist[s * nvert + v] = (uint32_t)(i / 3);
     }
 }
 
-constexpr int kVnLocal = 32;   // incidences sorted in registers; longer lists take the selection loop
-
-__global__ void __launch_bounds__(256) k_vn_sum(const uint64_t* __restrict__ voff, const uint64_t* __restrict__ vtotal,
+__global__ void __launch_bounds__(256) k_vn_sum(const uint32_t* __restrict__ vcount,
                                                const uint32_t* __restrict__ vlist, uint64_t nvert,
                                                const float* __restrict__ tri_normals, float* __restrict__ normals)
 {
-    const uint64_t total = *vtotal;
     for (uint64_t v = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; v < nvert;
          v += (uint64_t)gridDim.x * blockDim.x) {
-        const uint64_t a = voff[v], b = v + 1 < nvert ? voff[v + 1] : total;
-        const uint32_t n = (uint32_t)(b - a);
+        const uint32_t n = min(vcount[v], kVnMaxInc);
         float sx = 0.0f, sy = 0.0f, sz = 0.0f;
         auto add = [&](uint32_t t) {
             sx = __fadd_rn(sx, tri_normals[3 * (uint64_t)t + 0]);
@@ -433,12 +437,12 @@ __global__ void __launch_bounds__(256) k_vn_sum(const uint64_t* __restrict__ vof
             sz = __fadd_rn(sz, tri_normals[3 * (uint64_t)t + 2]);
         };
         if (n <= 8u) {
-            // the common case (a vertex lies on one cell edge: four cells, a
-            // triangle or two each): a 19-comparator sorting network in registers,
-            // missing entries padded with the largest id
+            // the common case (four cells, a triangle or two each): a
+            // 19-comparator sorting network in registers, missing entries
+            // padded with the largest id
             uint32_t d[8];
 #pragma unroll
-            for (int i = 0; i < 8; ++i) d[i] = (uint32_t)i < n ? vlist[a + i] : 0xffffffffu;
+            for (int i = 0; i < 8; ++i) d[i] = (uint32_t)i < n ? vlist[i * nvert + v] : 0xffffffffu;
             auto cx = [&](int i, int k) {
                 const uint32_t lo = min(d[i], d[k]), hi = max(d[i], d[k]);
                 d[i] = lo;
@@ -452,11 +456,11 @@ __global__ void __launch_bounds__(256) k_vn_sum(const uint64_t* __restrict__ vof
 #pragma unroll
             for (int i = 0; i < 8; ++i)
                 if ((uint32_t)i < n) add(d[i]);
-        } else if (n <= (uint32_t)kVnLocal) {
-            uint32_t ids[kVnLocal];
+        } else {
+            uint32_t ids[kVnMaxInc];
             for (uint32_t i = 0; i < n; ++i) {
                 // insertion sort while loading
-                const uint32_t t = vlist[a + i];
+                const uint32_t t = vlist[i * nvert + v];
                 uint32_t k = i;
                 while (k > 0 && ids[k - 1] > t) {
                     ids[k] = ids[k - 1];
@@ -465,20 +469,6 @@ __global__ void __launch_bounds__(256) k_vn_sum(const uint64_t* __restrict__ vof
                 ids[k] = t;
             }
             for (uint32_t i = 0; i < n; ++i) add(ids[i]);
-        } else {
-            // selection: the next larger id each time (ids are distinct)
-            uint64_t last = 0;
-            bool first = true;
-            for (uint32_t r = 0; r < n; ++r) {
-                uint32_t best = 0xffffffffu;
-                for (uint32_t i = 0; i < n; ++i) {
-                    const uint32_t t = vlist[a + i];
-                    if ((first || t > last) && t <= best) best = t;
-                }
-                add(best);
-                last = best;
-                first = false;
-            }
         }
         normals[3 * v + 0] = sx;
         normals[3 * v + 1] = sy;
@@ -690,40 +680,30 @@ cudaError_t launch_connect(const Job& j, const Launch& L)
 size_t vertex_normals_scratch_bytes(uint64_t ntri, uint64_t nvert)
 {
     auto al = [](size_t v) { return (v + 255) / 256 * 256; };
-    return al(12 * ntri) + al(4 * nvert) * 2 + al(8 * nvert) + al(12 * ntri) + al(scan_scratch_bytes(nvert)) + 256;
+    return al(12 * ntri) + al(4 * nvert) + al(4 * (size_t)kVnMaxInc * nvert);
 }
 
-void vertex_normals_carve(Job& j, uint64_t ntri, uint64_t nvert, void* scratch, void** scan, uint64_t** total)
+void vertex_normals_carve(Job& j, uint64_t ntri, uint64_t nvert, void* scratch)
 {
     auto al = [](size_t v) { return (v + 255) / 256 * 256; };
     char* p = static_cast<char*>(scratch);
     j.tri_normals = reinterpret_cast<float*>(p); p += al(12 * ntri);
     j.vcount = reinterpret_cast<uint32_t*>(p); p += al(4 * nvert);
-    j.vfill = reinterpret_cast<uint32_t*>(p); p += al(4 * nvert);
-    j.voff = reinterpret_cast<uint64_t*>(p); p += al(8 * nvert);
-    j.vlist = reinterpret_cast<uint32_t*>(p); p += al(12 * ntri);
-    *scan = p; p += al(scan_scratch_bytes(nvert));
-    *total = reinterpret_cast<uint64_t*>(p);
-    j.vtotal = *total;
+    j.vlist = reinterpret_cast<uint32_t*>(p);
 }
 
-cudaError_t launch_vertex_normals(const Job& j, uint64_t ntri, uint64_t nvert, void* scan, uint64_t* total,
-                                  const Launch& L)
+cudaError_t launch_vertex_normals(const Job& j, uint64_t ntri, uint64_t nvert, const Launch& L)
 {
     const unsigned grid = (unsigned)L.num_sms * 8;
     cudaError_t e = cudaMemsetAsync(j.vcount, 0, 4 * nvert, L.stream);
-    if (e == cudaSuccess) e = cudaMemsetAsync(j.vfill, 0, 4 * nvert, L.stream);
     if (e != cudaSuccess) return e;
-    prof_begin(L, "vertex_normals");
-    k_vn_count<<<grid, 256, 0, L.stream>>>(j.connections, ntri, nvert, j.vcount);
+    prof_begin(L, "vn_fill");
+    k_vn_fill<<<grid, 256, 0, L.stream>>>(j.connections, ntri, nvert, j.vcount, j.vlist);
     prof_end(L);
-    e = launch_scan(j.vcount, j.voff, nvert, scan, total, L);
-    if (e != cudaSuccess) return e;
-    prof_begin(L, "vertex_normals");
-    k_vn_fill<<<grid, 256, 0, L.stream>>>(j.connections, ntri, nvert, j.voff, j.vfill, j.vlist);
-    k_vn_sum<<<grid, 256, 0, L.stream>>>(j.voff, j.vtotal, j.vlist, nvert, j.tri_normals, j.normals);
+    prof_begin(L, "vn_sum");
+    k_vn_sum<<<grid, 256, 0, L.stream>>>(j.vcount, j.vlist, nvert, j.tri_normals, j.normals);
     prof_end(L);
-    *L.counter += 3;
+    *L.counter += 2;
     return cudaGetLastError();
 }
 

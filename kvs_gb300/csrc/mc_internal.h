@@ -51,9 +51,8 @@ cudaError_t launch_connect(const Job& j, const Launch& L);
 // (k_connect writes them to j.tri_normals): scratch of
 // vertex_normals_scratch_bytes, carved into j by vertex_normals_carve
 size_t vertex_normals_scratch_bytes(uint64_t ntri, uint64_t nvert);
-void vertex_normals_carve(Job& j, uint64_t ntri, uint64_t nvert, void* scratch, void** scan, uint64_t** total);
-cudaError_t launch_vertex_normals(const Job& j, uint64_t ntri, uint64_t nvert, void* scan, uint64_t* total,
-                                  const Launch& L);
+void vertex_normals_carve(Job& j, uint64_t ntri, uint64_t nvert, void* scratch);
+cudaError_t launch_vertex_normals(const Job& j, uint64_t ntri, uint64_t nvert, const Launch& L);
 
 // ---- streaming kernels (mc_stream.cu): duplicated mode, batched
 constexpr int kStreamThreads = 256;   // 8 independent warps per CTA

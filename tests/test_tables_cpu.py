@@ -59,3 +59,19 @@ def test_tables_equal_reference():
     from gen_mc_tables import parse_reference_tables, render
     tri, vert = parse_reference_tables(REF_TABLE)
     assert open(HEADER).read() == render(tri, vert)
+
+
+def test_vertex_triangle_bound():
+    """The vertex normals keep fixed slots per vertex: a vertex lies on one
+    cell edge, shared by at most 4 cells, and no case puts one edge into more
+    than 5 of its triangles, so 4 x 5 slots hold every vertex's triangles."""
+    tri = _header_tables()[0]
+    most = 0
+    for c in range(256):
+        tris = [tri[c][3 * t:3 * t + 3] for t in range(5) if tri[c][3 * t] != -1]
+        for e in range(12):
+            most = max(most, sum(e in t for t in tris))
+    assert most == 5
+    src = open(os.path.join(ROOT, "kvs_gb300", "csrc", "mc_gather.cu")).read()
+    m = re.search(r"constexpr uint32_t kVnMaxInc = (\d+);", src)
+    assert m and int(m.group(1)) == 4 * most
