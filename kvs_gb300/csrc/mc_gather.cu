@@ -391,12 +391,19 @@ __global__ void __launch_bounds__(kThreads) k_connect(Job j)
 // increasing triangle order.  A vertex lies on one cell edge, shared by at
 // most four cells, and no case of the table puts one edge into more than five
 // of its triangles, so a vertex has at most kVnMaxInc triangles: fixed slots,
-// no count pass and no scan.  The slots are stored slot-major (slot s of
-// vertex v at s * nvert + v) so the summing threads read them coalesced.
+// no count pass and no scan.  Slots 0-7 of a vertex fill one 32-byte sector
+// of their own (v * 8 + s: a vertex's triangles, written close together in
+// time, land in one sector, and the sum reads them with two 16-byte loads);
+// slots 8-19, rarely used, follow slot-major (8 nvert + (s - 8) nvert + v).
 // (connections hold vertex ids below nvert; an id at or above it, which
 // consistent inputs never give, is skipped so nothing is touched out of
 // range, and so is a slot past kVnMaxInc)
 constexpr uint32_t kVnMaxInc = 20;   // 4 cells x 5 triangles of one cell on one edge
+
+__device__ __forceinline__ uint64_t vn_slot(uint32_t s, uint64_t v, uint64_t nvert)
+{
+    return s < 8u ? 8 * v + s : (uint64_t)s * nvert + v;
+}
 
 // One incidence per lane, 32 consecutive ones per warp: lanes holding the
 // same vertex (a cell's triangles share corners) take their slots with one
@@ -419,7 +426,7 @@ __global__ void __launch_bounds__(256) k_vn_fill(const uint32_t* __restrict__ co
         if (ok && (int)lane == leader) base = atomicAdd(vcount + v, (uint32_t)__popc(grp));
         base = __shfl_sync(0xffffffffu, base, leader);
         const uint32_t s = base + (uint32_t)__popc(grp & lt);
-        if (ok && s < kVnMaxInc) vlist[s * nvert + v] = (uint32_t)(i / 3);
+        if (ok && s < kVnMaxInc) vlist[vn_slot(s, v, nvert)] = (uint32_t)(i / 3);
     }
 }
 
@@ -440,9 +447,12 @@ __global__ void __launch_bounds__(256) k_vn_sum(const uint32_t* __restrict__ vco
             // the common case (four cells, a triangle or two each): a
             // 19-comparator sorting network in registers, missing entries
             // padded with the largest id
-            uint32_t d[8];
+            const uint4* q = reinterpret_cast<const uint4*>(vlist + 8 * v);
+            const uint4 lo = q[0], hi = n > 4u ? q[1] : make_uint4(0, 0, 0, 0);
+            uint32_t d[8] = {lo.x, lo.y, lo.z, lo.w, hi.x, hi.y, hi.z, hi.w};
 #pragma unroll
-            for (int i = 0; i < 8; ++i) d[i] = (uint32_t)i < n ? vlist[i * nvert + v] : 0xffffffffu;
+            for (int i = 0; i < 8; ++i)
+                if ((uint32_t)i >= n) d[i] = 0xffffffffu;
             auto cx = [&](int i, int k) {
                 const uint32_t lo = min(d[i], d[k]), hi = max(d[i], d[k]);
                 d[i] = lo;
@@ -460,7 +470,7 @@ __global__ void __launch_bounds__(256) k_vn_sum(const uint32_t* __restrict__ vco
             uint32_t ids[kVnMaxInc];
             for (uint32_t i = 0; i < n; ++i) {
                 // insertion sort while loading
-                const uint32_t t = vlist[i * nvert + v];
+                const uint32_t t = vlist[vn_slot(i, v, nvert)];
                 uint32_t k = i;
                 while (k > 0 && ids[k - 1] > t) {
                     ids[k] = ids[k - 1];
