@@ -975,15 +975,21 @@ def run_ours(args, rank, world, local):
     emit_launches, emit_ms = prof.get("stream_emit", (0, 0.0))
     roofline = None
     if mode != _abi.MODE_DUP_POLYGON_NORMAL:
-        # shared vertices: volume once per isovalue (the minimum for one request
-        # at a time) + 24 B per vertex (coords, vertex normals) + 12 B per
-        # triangle (connections), over the whole step (several kernel families,
-        # none dominant on its own)
-        algo_bytes = nx * ny * nz * dt.itemsize * n + 24 * nvert + 12 * ntri
+        # shared vertices, over the whole step (several kernel families, none
+        # dominant on its own): the volume once per launch that reads it,
+        # however many isovalues share the launch, + the outputs: VertexNormal
+        # 24 B per vertex (coords, normals) + 12 B per triangle (connections),
+        # PolygonNormal 12 B per vertex + 24 B per triangle
+        readers = ("stream_count", "snode_count", "snode_emit", "snode_emit_multi", "sconnect", "sconnect_multi",
+                   "gather_cell_count", "gather_node_count", "gather_node_emit", "gather_connect")
+        passes = sum(prof[k][0] for k in readers if k in prof) / args.steps
+        outputs = 24 * nvert + 12 * ntri if mode == _abi.MODE_SHARED_VERTEX_NORMAL else 12 * nvert + 24 * ntri
+        algo_bytes = int(nx * ny * nz * dt.itemsize * passes + outputs)
         achieved = algo_bytes / (step_ms * 1e-3) / 1e9
         roofline = {"kernel": "whole step (shared-vertex passes)", "bound": "hbm", "achieved": round(achieved, 1),
                     "peak": hbm, "peak_kind": peak_kind, "unit": "GB/s", "frac": round(achieved / hbm, 4),
-                    "algorithmic_bytes_per_step": algo_bytes, "traffic": None}
+                    "algorithmic_bytes_per_step": algo_bytes, "volume_passes_per_step": round(passes, 2),
+                    "traffic": None}
     elif emit_launches:
         per = emit_ms / emit_launches
         achieved = algo_bytes / (per * 1e-3) / 1e9
