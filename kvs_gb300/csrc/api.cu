@@ -1379,9 +1379,12 @@ kvsmc_status kvsmc_extract_batch_host(kvsmc_context* ctx, const void* host, kvsm
         // device outputs and the caller's host arrays once the sizes are known;
         // each array leaves on the copy stream as soon as it is final, while
         // the later passes run
+        // (a failure of the caller's allocator fails these requests; it is not
+        // the arena shortage on which they would run again one by one)
+        bool host_failed = false;
         auto outputs = [&](std::vector<Item*>& its) -> kvsmc_status {
             kvsmc_status s2 = arena_outputs(ctx, its);
-            if (!s2) s2 = host_alloc(ctx, its, items.data(), alloc, user);
+            if (!s2 && (s2 = host_alloc(ctx, its, items.data(), alloc, user))) host_failed = true;
             return s2;
         };
         if (!ctx->copy_stream) {
@@ -1412,7 +1415,7 @@ kvsmc_status kvsmc_extract_batch_host(kvsmc_context* ctx, const void* host, kvsm
         };
         st = grouped_shared(ctx, sc, grouped, true, outputs, ready);
         const cudaError_t ce = cudaStreamSynchronize(ctx->copy_stream);
-        if (st == KVSMC_ERR_OUT_OF_MEMORY) grouped.clear();   // each request on its own below
+        if (st == KVSMC_ERR_OUT_OF_MEMORY && !host_failed) grouped.clear();   // each request on its own below
         else if (st)
             for (Item* it : grouped)
                 if (!it->status) it->status = st;
