@@ -1638,7 +1638,8 @@ def run_reference_batch(args, world, threads):
         "n_gpus": world, "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(t * 1e3, 1),
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "u8/u16/f32", "data": "synthetic",
         "config": {"workload": w["desc"], "sample": sample},
-        "cpu_baseline": {"value": round(value, 1), "unit": "Mcells/s", "cores": threads, "kind": "port",
+        "cpu_baseline": {"value": round(value, 1), "unit": "Mcells/s", "cores": min(threads, len(reqs)),
+                         "kind": "port",
                          "sample": sample + "; oracle/mc_oracle.c (C restatement of kvs::MarchingCubes, "
                          "-O3 -ffp-contract=off)"},
         "e2e": {"value": round(value, 1), "unit": "Mcells/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
@@ -1692,7 +1693,8 @@ def run_reference(args, rank, world):
         "n_gpus": world, "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(ms, 1),
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
         "config": {"workload": w["desc"], "sample": sample},
-        "cpu_baseline": {"value": round(value, 1), "unit": "Mcells/s", "cores": threads, "kind": "port",
+        "cpu_baseline": {"value": round(value, 1), "unit": "Mcells/s", "cores": min(threads, len(isos)),
+                         "kind": "port",
                          "sample": sample + "; oracle/mc_oracle.c (C restatement of kvs::MarchingCubes, "
                          "-O3 -ffp-contract=off), one isovalue per thread"},
         "e2e": {"value": round(value, 1), "unit": "Mcells/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
