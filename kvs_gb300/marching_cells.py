@@ -32,7 +32,8 @@ Reference behaviour kept:
 import numpy as np
 
 from . import _abi
-from .marching_cubes import ObjectBase, PolygonObject, TransferFunction, _equal, default_context, message_error
+from .marching_cubes import (ObjectBase, PolygonObject, TransferFunction, _equal, default_context, message_error,
+                             set_mapper_range)
 
 
 class UnstructuredVolumeObject(ObjectBase):
@@ -267,15 +268,7 @@ class _MarchingCells(PolygonObject):
             if not volume.hasMinMaxValues():
                 volume.setMinMaxValues(sizes["min_value"], sizes["max_value"])
         self.sizes = sizes
-        if not self._tfunc.hasRange():
-            f32 = np.float32
-            if code == 0:
-                self._tfunc.setRange(-128, 127)
-            elif code == 4:
-                self._tfunc.setRange(0, 255)
-            else:
-                lo, hi = f32(volume.minValue()), f32(volume.maxValue())
-                self._tfunc.setRange(lo, hi + f32(1.0) if _equal(float(lo), float(hi)) else hi)
+        set_mapper_range(self._tfunc, code, volume.minValue(), volume.maxValue())
         # MapperBase::setMinMaxCoords (MapperBase.cpp:92-122), the volume's
         # updateMinMaxCoords fold run on the GPU
         if not volume.hasMinMaxObjectCoords():

@@ -279,6 +279,23 @@ class TransferFunction:
         return out
 
 
+def set_mapper_range(tfunc, code, vmin, vmax):
+    """MapperBase::setRange (MapperBase.cpp:54-83) for a transfer function
+    without a range: int8 and uint8 volumes take their type's range (dtype
+    codes 0 and 4), the others the volume's min/max as floats, widened by 1
+    when kvs::Math::Equal calls them equal."""
+    if tfunc.hasRange():
+        return
+    if code == 0:
+        tfunc.setRange(-128, 127)
+    elif code == 4:
+        tfunc.setRange(0, 255)
+    else:
+        f32 = np.float32
+        lo, hi = f32(vmin), f32(vmax)
+        tfunc.setRange(lo, hi + f32(1.0) if _equal(float(lo), float(hi)) else hi)
+
+
 _context = None
 
 
@@ -386,14 +403,7 @@ class MarchingCubes(PolygonObject):
         # cache is filled (here by the device scan), then the TF range.
         if not volume.hasMinMaxValues():
             volume.setMinMaxValues(sizes["min_value"], sizes["max_value"])
-        if not self._tfunc.hasRange():
-            if code == 0:
-                self._tfunc.setRange(-128, 127)
-            elif code == 4:
-                self._tfunc.setRange(0, 255)
-            else:
-                lo, hi = f32(volume.minValue()), f32(volume.maxValue())
-                self._tfunc.setRange(lo, hi + f32(1.0) if _equal(float(lo), float(hi)) else hi)
+        set_mapper_range(self._tfunc, code, volume.minValue(), volume.maxValue())
         if not sizes["extracted"] or coords.size == 0:
             return
         self._coords = coords

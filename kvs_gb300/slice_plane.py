@@ -19,7 +19,7 @@ import numpy as np
 from . import _abi
 from .marching_cells import MAPPERS, UnstructuredVolumeObject, set_bounds_on_device
 from .marching_cubes import (PolygonObject, StructuredVolumeObject, TransferFunction, _equal, default_context,
-                             message_error)
+                             message_error, set_mapper_range)
 
 f32 = np.float32
 
@@ -86,14 +86,7 @@ class SlicePlane(PolygonObject):
     def _set_range(self, code, volume):
         """MapperBase::setRange (MapperBase.cpp:54-83), the volume's min/max
         cache filled first."""
-        if not self._tfunc.hasRange():
-            if code == 0:
-                self._tfunc.setRange(-128, 127)
-            elif code == 4:
-                self._tfunc.setRange(0, 255)
-            else:
-                lo, hi = f32(volume.minValue()), f32(volume.maxValue())
-                self._tfunc.setRange(lo, hi + f32(1.0) if _equal(float(lo), float(hi)) else hi)
+        set_mapper_range(self._tfunc, code, volume.minValue(), volume.maxValue())
 
     def _mapping_cells(self, volume):
         """SlicePlane::mapping, unstructured branch (SlicePlane.cpp:128-147, 291-320)."""
