@@ -138,3 +138,53 @@ def test_mapper_host_decisions_match_reference(monkeypatch):
             assert m.coords() is g["coords"], tag
         else:
             assert m.coords().size == 0, tag
+
+
+def test_cells_mapper_host_decisions_match_reference(monkeypatch):
+    """The unstructured mappers' host side (e.g. MarchingTetrahedra.cpp:94-136)
+    on every cells fixture, with the device calls replaced: the extraction by
+    the fixture's outputs and min/max, the bounding-box fold by its numpy
+    restatement.  Success flag, types, the volume's min/max cache, colour,
+    opacity and bounding box as the reference reported them."""
+    from kvs_gb300 import _abi
+    from kvs_gb300 import marching_cells as mcells
+    from kvs_gb300.marching_cubes import PolygonObject
+    from oracle import cells as ocells
+
+    from .test_cells_cpu import case_inputs, cells_fixtures
+    man, arr = cells_fixtures()
+    for e in man:
+        k = e["key"]
+        v, xyz, conn = case_inputs(arr, e)
+        want_mm = arr[f"{k}__vol_minmax"]
+
+        def fake_extract(ctx, ct, values, coords, connections, iso, minmax=None, k=k, want_mm=want_mm):
+            sizes = dict(ntriangles=arr[f"{k}__coords"].size // 9, min_value=float(want_mm[0]),
+                         max_value=float(want_mm[1]))
+            return arr[f"{k}__coords"], arr[f"{k}__normals"], sizes
+
+        def fake_bounds(ctx, ct, coords, connections):
+            return ocells.min_max_coords(coords, connections)
+
+        monkeypatch.setattr(_abi, "marching_cells_host", fake_extract)
+        monkeypatch.setattr(_abi, "cells_bounds", fake_bounds)
+        vol = mcells.UnstructuredVolumeObject(mcells.MAPPERS_BY_ABI[e["cell_type"]].CELL, v.size, conn.shape[0], 1,
+                                              xyz, conn, v)
+        if e["minmax"] is not None:
+            vol.setMinMaxValues(*e["minmax"])
+        tf = TransferFunction(256)
+        if e["tf_range"]:
+            tf.setRange(*e["tf_range"])
+        nt = PolygonObject.PolygonNormal if e["normal_type"] == "polygon" else PolygonObject.VertexNormal
+        if e["form"] == 1:
+            continue   # the Isosurface form routes through the same mapper; its GPU test covers it
+        m = mcells.MAPPERS_BY_ABI[e["cell_type"]](vol, e["iso"], nt, e["duplication"], tf, context=object())
+        assert m.isSuccess() == e["success"], k
+        assert np.array_equal(m.colors(), arr[f"{k}__colors"]), k
+        assert np.array_equal(m.opacities(), arr[f"{k}__opacities"]), k
+        assert (m.polygonType(), m.colorType(), m.normalType()) == (
+            e["polygon_type"], e["color_type"], e["normal_type_out"]), k
+        assert vol.hasMinMaxValues() == e["vol_has_minmax"], k
+        assert np.array_equal(m.minObjectCoord(), np.float32(e["min_obj"])), k
+        assert np.array_equal(m.maxObjectCoord(), np.float32(e["max_obj"])), k
+        assert np.array_equal(m.maxExternalCoord(), np.float32(e["max_ext"])), k
