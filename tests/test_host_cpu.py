@@ -6,7 +6,7 @@ import numpy as np
 
 from kvs_gb300.marching_cubes import TransferFunction
 
-from .helpers import golden
+from .helpers import golden, same_bits
 
 
 def test_default_table_is_the_references():
@@ -188,3 +188,69 @@ def test_cells_mapper_host_decisions_match_reference(monkeypatch):
         assert np.array_equal(m.minObjectCoord(), np.float32(e["min_obj"])), k
         assert np.array_equal(m.maxObjectCoord(), np.float32(e["max_obj"])), k
         assert np.array_equal(m.maxExternalCoord(), np.float32(e["max_ext"])), k
+
+
+def test_isosurface_host_decisions_match_reference(monkeypatch, oracle_lib):
+    """kvs::Isosurface's structured branch (Isosurface.cpp:23-191) through the
+    mirror on every isosurface fixture, with the device calls replaced: the
+    min/max scan by the oracle's GetMinMaxValues restatement, the extraction
+    by the fixture's outputs.  The isolevel and mode it hands to the device,
+    then success flag, types, colour, bounding box and the volume's min/max
+    cache as the reference reported them."""
+    from kvs_gb300 import _abi
+    from kvs_gb300 import marching_cubes as M
+    from kvs_gb300.isosurface import Isosurface
+
+    from .test_isosurface_cpu import effective, fixtures
+    man, arr = fixtures()
+    for e in man:
+        k = e["key"]
+        v = arr[f"{e['case']}__input"]
+        iso_want, dup_want = effective(e, v, oracle_lib.minmax)
+        mode_want = (_abi.MODE_SHARED_VERTEX_NORMAL if e["normal_type"] == "vertex"
+                     else _abi.MODE_DUP_POLYGON_NORMAL if dup_want else _abi.MODE_SHARED_POLYGON_NORMAL)
+
+        class FakeVolume:
+            def __init__(self, values):
+                self.values = values
+
+            @classmethod
+            def upload(cls, ctx, values):
+                return cls(values)
+
+            def minmax(self):
+                return oracle_lib.minmax(self.values)
+
+            def free(self):
+                pass
+
+        def fake(ctx, values, params, e=e, k=k, iso_want=iso_want, mode_want=mode_want):
+            assert params.isolevel == iso_want and params.mode == mode_want, k
+            return (arr[f"{k}__coords"], arr[f"{k}__normals"], arr[f"{k}__connections"],
+                    dict(min_value=e["vol_min"], max_value=e["vol_max"],
+                         extracted=not M._equal(e["vol_min"], e["vol_max"])))
+
+        monkeypatch.setattr(_abi, "DeviceVolume", FakeVolume)
+        monkeypatch.setattr(_abi, "marching_cubes_host", fake)
+        vol = M.StructuredVolumeObject(v)
+        if e["minmax"]:
+            vol.setMinMaxValues(*e["minmax"])
+        nt = M.PolygonObject.PolygonNormal if e["normal_type"] == "polygon" else M.PolygonObject.VertexNormal
+        ctx = object()
+        if e["form"] == 0:
+            iso = Isosurface(vol, normal_type=nt, context=ctx)
+        elif e["form"] == 1:
+            iso = Isosurface(vol, e["isolevel"], nt, context=ctx)
+        else:
+            tf = TransferFunction(256)
+            if e["tf_range"]:
+                tf.setRange(*e["tf_range"])
+            iso = Isosurface(vol, e["isolevel"], nt, e["duplication"], tf, context=ctx)
+        assert iso.isSuccess() == e["success"], k
+        assert np.array_equal(iso.colors(), arr[f"{k}__colors"]), k
+        assert np.array_equal(iso.opacities(), arr[f"{k}__opacities"]), k
+        assert (iso.polygonType(), iso.normalType(), iso.colorType()) == (
+            e["polygon_type"], e["normal_type_out"], e["color_type"]), k
+        assert np.array_equal(iso.minObjectCoord(), np.float32(e["min_obj"])), k
+        assert np.array_equal(iso.maxExternalCoord(), np.float32(e["max_ext"])), k
+        assert same_bits(np.float64([vol.minValue(), vol.maxValue()]), np.float64([e["vol_min"], e["vol_max"]])), k
