@@ -254,3 +254,65 @@ def test_isosurface_host_decisions_match_reference(monkeypatch, oracle_lib):
         assert np.array_equal(iso.minObjectCoord(), np.float32(e["min_obj"])), k
         assert np.array_equal(iso.maxExternalCoord(), np.float32(e["max_ext"])), k
         assert same_bits(np.float64([vol.minValue(), vol.maxValue()]), np.float64([e["vol_min"], e["vol_max"]])), k
+
+
+def test_slice_plane_host_decisions_match_reference(monkeypatch, oracle_lib):
+    """SlicePlane on structured volumes through the mirror (SlicePlane.cpp:
+    setPlane, mapping) on every slice fixture, with the device calls replaced
+    by the oracle (GetMinMaxValues restatement, oracle/slice.py for the
+    extraction) fed with exactly the parameters the mirror hands to the
+    device: the plane's coefficients, bounding box, scale and the transfer
+    function's range.  Coordinates, colours and normals equal the
+    reference's bit for bit, and so do the types and bounding box."""
+    from kvs_gb300 import _abi
+    from kvs_gb300 import slice_plane as SP
+    from kvs_gb300.marching_cubes import StructuredVolumeObject
+    from oracle import slice as OS
+
+    from .test_slice_cpu import slice_fixtures
+    table = golden()[1]["colormap256"]
+    man, arr = slice_fixtures()
+
+    class FakeVolume:
+        def __init__(self, values):
+            self.values = values
+
+        @classmethod
+        def upload(cls, ctx, values):
+            return cls(values)
+
+        def minmax(self):
+            return oracle_lib.minmax(self.values)
+
+        def free(self):
+            pass
+
+    def fake_slice(ctx, dv, p):
+        nz, ny, nx = dv.values.shape
+        assert list(p.min_coord) == [0.0, 0.0, 0.0] and list(p.scale) == [1.0, 1.0, 1.0]
+        c, rgb, n = OS.slice_plane(dv.values, np.float32(list(p.coefficients)), table, np.float32(p.tf_min),
+                                   np.float32(p.tf_max))
+        return c, n, rgb, c.size // 9
+
+    monkeypatch.setattr(_abi, "DeviceVolume", FakeVolume)
+    monkeypatch.setattr(SP, "slice_plane_host", fake_slice)
+    for e in man:
+        k = e["key"]
+        v = arr[f"{e['case']}__input"]
+        tf = TransferFunction(256)
+        if e["tf_range"]:
+            tf.setRange(*e["tf_range"])
+        vol = StructuredVolumeObject(v)
+        if e["coefficients"] is not None:
+            s = SP.SlicePlane(vol, coefficients=e["coefficients"], transfer_function=tf, context=object())
+        else:
+            s = SP.SlicePlane(vol, point=e["point"], normal=e["normal"], transfer_function=tf, context=object())
+        assert s.isSuccess() == e["success"], k
+        assert same_bits(s.coords(), arr[f"{k}__coords"]), k
+        assert same_bits(s.normals(), arr[f"{k}__normals"]), k
+        assert np.array_equal(s.colors(), arr[f"{k}__colors"]), k
+        assert np.array_equal(s.opacities(), arr[f"{k}__opacities"]), k
+        assert (s.polygonType(), s.colorType(), s.normalType()) == (
+            e["polygon_type"], e["color_type"], e["normal_type"]), k
+        assert np.array_equal(s.minObjectCoord(), np.float32(e["min_obj"])), k
+        assert np.array_equal(s.maxExternalCoord(), np.float32(e["max_ext"])), k
