@@ -316,3 +316,52 @@ def test_slice_plane_host_decisions_match_reference(monkeypatch, oracle_lib):
             e["polygon_type"], e["color_type"], e["normal_type"]), k
         assert np.array_equal(s.minObjectCoord(), np.float32(e["min_obj"])), k
         assert np.array_equal(s.maxExternalCoord(), np.float32(e["max_ext"])), k
+
+
+def test_mapper_parameters_reproduce_reference(monkeypatch, oracle_lib):
+    """The parameters the MarchingCubes mirror hands to the device (mode,
+    isolevel, preset range, min_coord and scale as MarchingCubes.cpp:166-168
+    decides them from the bounding box) fed to the oracle's extraction in
+    place of the device reproduce the reference's arrays bit for bit on every
+    golden case (uniform, rectilinear and preset object coordinates)."""
+    from kvs_gb300 import _abi
+    from kvs_gb300 import marching_cubes as M
+
+    from .helpers import golden_inputs, golden_outputs
+    man, arr = golden()
+    cmap = arr["colormap256"]
+
+    def fake(ctx, values, params):
+        vmin, vmax = ((params.min_value, params.max_value) if params.has_minmax else oracle_lib.minmax(values))
+        sizes = dict(min_value=vmin, max_value=vmax, extracted=not M._equal(vmin, vmax))
+        if not sizes["extracted"]:
+            z = np.zeros(0, np.float32)
+            return z, z, np.zeros(0, np.uint32), sizes
+        o = oracle_lib.extract(values, params.isolevel, params.mode, vmin, vmax, list(params.min_coord),
+                               list(params.scale))
+        return o["coords"], o["normals"], o["connections"], sizes
+
+    monkeypatch.setattr(_abi, "marching_cubes_host", fake)
+    for e in man:
+        v, rect = golden_inputs(e, arr)
+        g = golden_outputs(e, arr)
+        nz, ny, nx = v.shape
+        vol = M.StructuredVolumeObject(values=v.ravel(), resolution=(nx, ny, nz))
+        if rect is not None:
+            vol.setGridTypeToRectilinear()
+            vol.setCoords(np.asarray(rect, np.float32))
+        if e["obj"]:
+            vol.setMinMaxObjectCoords(e["obj"][0], e["obj"][1])
+        if e["minmax"]:
+            vol.setMinMaxValues(*e["minmax"])
+        tf = M.TransferFunction(256, cmap)
+        if e["tf_range"]:
+            tf.setRange(*e["tf_range"])
+        nt = M.PolygonObject.VertexNormal if e["normal_type"] == "vertex" else M.PolygonObject.PolygonNormal
+        m = M.MarchingCubes(vol, e["iso"], nt, e["duplication"], tf, context=object())
+        k = e["key"]
+        assert same_bits(m.coords(), g["coords"]), k
+        assert same_bits(m.normals(), g["normals"]), k
+        assert np.array_equal(m.connections(), g["connections"]), k
+        if g["coords"].size:
+            assert np.array_equal(m.colors(), g["colors"]), k
