@@ -1591,7 +1591,9 @@ def run_cpu(args, threads, planes, isos):
         with cf.ThreadPoolExecutor(max_workers=threads) as ex:
             done = sum(ex.map(one, isos))
     t = time.perf_counter() - t0
-    return done / t / 1e6, t, f"{len(isos)} isovalues x {nx}x{ny}x{nz} slab ({done / 1e6:.0f} M cell-isovalues)"
+    mode_name = {0: "duplication+PolygonNormal", 1: "shared vertices+PolygonNormal", 2: "VertexNormal"}[mode]
+    return (done / t / 1e6, t,
+            f"{len(isos)} isovalues x {nx}x{ny}x{nz} slab ({done / 1e6:.0f} M cell-isovalues, {mode_name})")
 
 
 def batch_reference_sample(w, count):
@@ -1675,6 +1677,7 @@ def run_reference(args, rank, world):
                 "at a time on the caller's thread); its per-request CPU cost is the uneven200 / sweep1024 reference "
                 "arms"}
     planes = min(65, w["shape"][0]) if w["kind"] in ("fbm", "lattice") else w["shape"][0]
+    args.mode = w.get("mode", 0)   # the workload's mode (duplicated, shared vertices, VertexNormal)
     if "pcts" in w:
         args.cpu_slab = cpu_slab_sample(args, planes)
         isos = workload_isos(w, args.cpu_slab.astype(np.float64).ravel())

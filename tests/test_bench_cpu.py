@@ -29,3 +29,8 @@ def test_reference_arm_line():
     assert cb["cores"] == 1   # one isovalue: one thread works
     assert d["e2e"] == {"value": d["value"], "unit": d["unit"], "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}
     assert "workload" in d["config"] and "sample" in d["config"]
+
+
+def test_reference_arm_times_the_workloads_mode():
+    d = _reference_line("blobs128vn")
+    assert "VertexNormal" in d["config"]["sample"] and d["value"] > 0
