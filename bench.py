@@ -1648,6 +1648,98 @@ def run_reference_batch(args, world, threads):
     }
 
 
+def reference_line(args, world, w, metric, value, ms, sample, dtype="f32"):
+    """The reference arm's JSON line for a workload timed on one host core."""
+    return {
+        "impl": "reference", "metric": metric, "value": round(value, 3), "unit": metric, "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(ms, 1), "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": dtype, "data": "synthetic",
+        "config": {"workload": w["desc"], "sample": sample},
+        "cpu_baseline": {"value": round(value, 3), "unit": metric, "cores": 1, "kind": "port", "sample": sample},
+        "e2e": {"value": round(value, 3), "unit": metric, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+
+
+def run_reference_stl(args, world, w):
+    """kvs::Stl's writer (binary, or the ASCII default) restated in
+    oracle/export.py, on one host core, over meshes of the workload's field:
+    the workload's isovalues on a 65-plane slab, extracted by the oracle."""
+    from oracle import oracle
+    oracle.build()
+    v = cpu_slab_sample(args, 65)
+    outs = [oracle.extract(v, iso, 0, float(v.min()), float(v.max())) for iso in w["isos"]]
+    ascii_ = w["kind"] == "stlascii"
+    coords = np.concatenate([o["coords"] for o in outs])
+    normals = np.concatenate([o["normals"] for o in outs])
+    nt = min(normals.size // 3, 20000 if ascii_ else 1 << 20)
+    mesh = (coords[:9 * nt], normals[:3 * nt])
+    vals = []
+    for i in range(args.warmup + args.steps):
+        mt, t, _ = (run_stl_ascii_cpu if ascii_ else run_stl_cpu)(mesh)
+        if i >= args.warmup:
+            vals.append((mt, nt / mt / 1e3))
+    value = statistics.median(x for x, _ in vals)
+    ms = statistics.median(x for _, x in vals)
+    sample = (f"{nt} triangles of the {len(w['isos'])} isovalues' meshes of a 65-plane slab of the field, "
+              f"{'ASCII' if ascii_ else 'binary'} STL records; oracle/export.py (restatement of kvs::Stl's writer)")
+    return reference_line(args, world, w, "Mtris/s", value, ms, sample, "f32 -> bytes")
+
+
+def run_reference_slice(args, world, w):
+    """kvs::SlicePlane's extract_plane restated in oracle/slice.py (every cell
+    visited, as the reference does) on one host core, over a z-slab of the
+    workload's field cut by the workload's plane normal through the slab's
+    centre."""
+    from kvs_gb300.marching_cubes import TransferFunction
+    from oracle import slice as OS
+    nz, ny, nx = w["shape"]
+    planes = max(2, min(nz, (1 << 24) // (nx * ny) + 1))
+    v = cpu_slab_sample(args, planes)
+    f32 = np.float32
+    pt = np.array([w["point"][0], w["point"][1], (planes - 1) / 2], f32)
+    nrm = np.array(w["normal"], f32)
+    dot = f32(f32(f32(pt[0] * nrm[0]) + f32(pt[1] * nrm[1])) + f32(pt[2] * nrm[2]))
+    coef = np.array([nrm[0], nrm[1], nrm[2], -dot], f32)
+    table = TransferFunction(256).table
+    lo, hi = f32(v.min()), f32(v.max())
+    cells = (nx - 1) * (ny - 1) * (planes - 1)
+    times = []
+    for i in range(args.warmup + args.steps):
+        t0 = time.perf_counter()
+        OS.slice_plane(v, coef, table, lo, hi)
+        if i >= args.warmup:
+            times.append(time.perf_counter() - t0)
+    t = statistics.median(times)
+    sample = (f"{nx}x{ny}x{planes} slab of the field ({cells / 1e6:.0f} M cells), the workload's plane normal through "
+              f"the slab's centre; oracle/slice.py (restatement of SlicePlane::extract_plane)")
+    return reference_line(args, world, w, "Mcells/s", cells / t / 1e6, t * 1e3, sample)
+
+
+def run_reference_ingest(args, world, w):
+    """The reference's external-binary KVSML read (the fread of
+    DataArray::ReadExternalData, DataArray.h:175-190) as numpy.fromfile on one
+    host core, over a 128 MiB float32 value file in the page cache."""
+    import shutil
+    import tempfile
+    base = "/dev/shm" if os.path.isdir("/dev/shm") else None
+    d = tempfile.mkdtemp(dir=base)
+    try:
+        path = os.path.join(d, "vol_value.dat")
+        nbytes = 128 << 20
+        np.random.default_rng(1).random(nbytes // 4, dtype=np.float32).astype("<f4").tofile(path)
+        times = []
+        for i in range(args.warmup + args.steps):
+            t0 = time.perf_counter()
+            np.fromfile(path, "<f4")
+            if i >= args.warmup:
+                times.append(time.perf_counter() - t0)
+    finally:
+        shutil.rmtree(d, ignore_errors=True)
+    t = statistics.median(times)
+    sample = "a 128 MiB float32 value file in the page cache read into host memory (numpy.fromfile)"
+    return reference_line(args, world, w, "GB/s", nbytes / t / 1e9, t * 1e3, sample)
+
+
 def run_reference(args, rank, world):
     if rank != 0:
         return None
@@ -1655,6 +1747,12 @@ def run_reference(args, rank, world):
     threads = os.cpu_count() or 1
     if w["kind"] == "batch":
         return run_reference_batch(args, world, threads)
+    if w["kind"] in ("stl", "stlascii"):
+        return run_reference_stl(args, world, w)
+    if w["kind"] == "slice":
+        return run_reference_slice(args, world, w)
+    if w["kind"] == "ingest":
+        return run_reference_ingest(args, world, w)
     if w["kind"] == "cells":
         vals = []
         for i in range(args.warmup + args.steps):

@@ -6,6 +6,8 @@ import os
 import subprocess
 import sys
 
+import pytest
+
 ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 
 
@@ -34,3 +36,10 @@ def test_reference_arm_line():
 def test_reference_arm_times_the_workloads_mode():
     d = _reference_line("blobs128vn")
     assert "VertexNormal" in d["config"]["sample"] and d["value"] > 0
+
+
+@pytest.mark.parametrize("workload,metric", [("kvsml512", "GB/s"), ("stlascii512", "Mtris/s")])
+def test_reference_arm_uses_the_workloads_metric(workload, metric):
+    d = _reference_line(workload)
+    assert d["metric"] == metric and d["unit"] == metric and d["value"] > 0
+    assert d["cpu_baseline"]["unit"] == metric and d["e2e"]["unit"] == metric
