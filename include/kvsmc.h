@@ -185,7 +185,10 @@ typedef struct kvsmc_request {
 /* Several isolevels (or modes) of one HOST volume in one call: the volume is
  * uploaded once, all requests run batched, and each request's arrays are
  * allocated through `alloc` (user pointer `alloc_user`, `which` as above plus
- * 3 * request index) and copied back.  sizes: n entries.  The reference
+ * 3 * request index) and copied back: duplicated-mode triangles in plane
+ * ranges while later ranges are written, a shared-vertex request's vertices,
+ * connections and normals as soon as the pass that writes each is done, so
+ * the copies overlap the remaining passes.  sizes: n entries.  The reference
  * equivalent is n kvs::MarchingCubes constructions on the same volume
  * (Tool/kvsview/Isosurface.cpp:238-249 re-extracts per isolevel). */
 kvsmc_status kvsmc_extract_batch_host(kvsmc_context* ctx, const void* host_values, kvsmc_dtype dtype,
